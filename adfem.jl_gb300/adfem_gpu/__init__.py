@@ -1,0 +1,353 @@
+"""adfem_gpu -- GB300 implementation of AdFem.jl's P1-triangle forward/adjoint path.
+
+This module mirrors the Julia operator API of AdFem on top of the C ABI of
+libadfem_gpu.so (include/adfem_gpu.h): the same function names, argument
+meaning, 1-based node numbering and sparse outputs (scipy CSC standing in for
+Julia's SparseMatrixCSC).  All arithmetic runs in the CUDA library; this layer
+only converts arguments.
+
+    Mesh(coords, elems)                          src/MFEM/MFEM.jl:60-119
+    Mesh.rectangle(m, n, h)                      src/MFEM/MFEM.jl:134-170
+    get_ngauss / get_area / gauss_nodes          src/MFEM/MFEM.jl:207-232
+    compute_fem_laplace_matrix1(kappa, mesh)     src/MFEM/MCore.jl:112-120
+    compute_fem_source_term1(f, mesh)            src/MFEM/MCore.jl:77-82
+    compute_fem_source_term(f1, f2, mesh)        src/MFEM/MCore.jl:87-94
+    compute_fem_stiffness_matrix(D, mesh)        src/MFEM/MCore.jl:287-315
+    compute_plane_strain_matrix(E, nu)           src/Core.jl:777-785
+    bcnode(mesh)                                 src/MFEM/MCore.jl:439-450
+    impose_Dirichlet_boundary_conditions(...)    src/MFEM/MUtils.jl:184-199
+    solve(K, F)  (K\\F)                          README.md:54
+"""
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+import scipy.sparse as sp
+
+from . import _lib
+from ._lib import AdFemError, SolverOpts, SolverStats, check, ptr
+
+__all__ = [
+    "AdFemError", "Mesh", "get_ngauss", "get_area", "gauss_nodes", "fem_nodes", "bcnode",
+    "compute_fem_laplace_matrix1", "compute_fem_source_term1", "compute_fem_source_term",
+    "compute_fem_stiffness_matrix", "compute_plane_strain_matrix", "compute_plane_stress_matrix",
+    "impose_Dirichlet_boundary_conditions", "impose_Dirichlet_coo", "impose_Dirichlet_coo_backward",
+    "solve", "solver_opts",
+]
+
+
+def _lib_():
+    return _lib.load()
+
+
+def _c(a, dt):
+    return np.ascontiguousarray(a, dtype=dt)
+
+
+class Mesh:
+    """P1 triangle mesh resident on the GPU (mirror of AdFem's ``Mesh``).
+
+    ``coords``: (nnode, 2) float; ``elems``: (nelem, 3) 1-based vertex ids.  Only
+    degree 1 (P1) with the order-2 rule is supported; anything else raises
+    ``AdFemError`` with status ``ERR_UNSUPPORTED``.
+    """
+
+    def __init__(self, coords, elems, order: int = -1, degree: int = 1, lorder: int = -1):
+        if degree != 1:
+            raise AdFemError(_lib.ERR_UNSUPPORTED, "only degree 1 (P1) elements are implemented")
+        if order not in (-1, 2):
+            raise AdFemError(_lib.ERR_UNSUPPORTED, "only the order-2 triangle rule is implemented")
+        L = _lib_()
+        coords = _c(coords, np.float64)
+        elems = np.asarray(elems)
+        if coords.ndim != 2 or coords.shape[1] != 2 or elems.ndim != 2 or elems.shape[1] != 3:
+            raise AdFemError(_lib.ERR_INVALID, "coords must be (n,2) and elems (m,3)")
+        nv, ne = coords.shape[0], elems.shape[0]
+        xyz = np.zeros((nv, 3))
+        xyz[:, :2] = coords
+        e0 = _c(elems - 1, np.int32)
+        h = ctypes.c_void_p()
+        check(L.adfem_mesh_create(ptr(xyz), nv, ptr(e0), ne, 1, ctypes.byref(h)), "Mesh")
+        self._h = h
+        self.nodes = coords
+        self.nnode = nv
+        self.nelem = ne
+        self.ndof = nv
+        self.elem_ndof = 3
+        self.lorder = 6 if lorder == -1 else lorder
+        el = np.empty(3 * ne, np.int64)
+        check(L.adfem_mesh_elements(h, ptr(el)))
+        self.elems = el.reshape(ne, 3)
+        self.conn = self.elems
+        nedge = ctypes.c_longlong()
+        check(L.adfem_mesh_edges(h, None, ctypes.byref(nedge)))
+        ed = np.empty(2 * nedge.value, np.int64)
+        check(L.adfem_mesh_edges(h, ptr(ed), ctypes.byref(nedge)))
+        self.nedge = nedge.value
+        self.edges = ed.reshape(2, self.nedge).T.copy()
+        self._pattern = None
+        self._pattern_el = None
+
+    @classmethod
+    def rectangle(cls, m: int, n: int, h: float, version: int = 1):
+        """``Mesh(m, n, h)``: m x n cells of size h, nodes x-fastest (MFEM.jl:134-170)."""
+        if version not in (1, 2):
+            raise AdFemError(_lib.ERR_UNSUPPORTED, "versions 1 and 2 are implemented")
+        jj, ii = np.meshgrid(np.arange(m + 1), np.arange(n + 1))
+        coords = np.stack([(jj * h).ravel(), (ii * h).ravel()], axis=1).astype(np.float64)
+        i = np.arange(n)[:, None]
+        j = np.arange(m)[None, :]
+        a = (i * (m + 1) + j).ravel()
+        b, c = a + 1, ((i + 1) * (m + 1) + j).ravel()
+        d = c + 1
+        el = np.empty((2 * m * n, 3), np.int64)
+        if version == 1:
+            el[0::2] = np.stack([a, b, c], 1)
+            el[1::2] = np.stack([b, c, d], 1)
+        else:
+            el[0::2] = np.stack([a, d, c], 1)
+            el[1::2] = np.stack([a, b, d], 1)
+        return cls(coords, el + 1)
+
+    @property
+    def handle(self):
+        return self._h
+
+    def close(self):
+        if getattr(self, "_h", None) is not None and _lib._LIB is not None:
+            _lib._LIB.adfem_mesh_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def pattern(self):
+        """1-based CSC (colptr, rowval) of the scalar operator."""
+        if self._pattern is None:
+            L = _lib_()
+            nnz = ctypes.c_longlong()
+            check(L.adfem_mesh_sizes(self._h, None, None, None, ctypes.byref(nnz)))
+            cp = np.empty(self.nnode + 1, np.int64)
+            rv = np.empty(nnz.value, np.int64)
+            check(L.adfem_mesh_pattern(self._h, ptr(cp), ptr(rv)))
+            self._pattern = (cp, rv)
+        return self._pattern
+
+    def pattern_elasticity(self):
+        if self._pattern_el is None:
+            L = _lib_()
+            cp0, rv0 = self.pattern()
+            cp = np.empty(2 * self.nnode + 1, np.int64)
+            rv = np.empty(4 * rv0.size, np.int64)
+            check(L.adfem_mesh_pattern_elasticity(self._h, ptr(cp), ptr(rv)))
+            self._pattern_el = (cp, rv)
+        return self._pattern_el
+
+    def __len__(self):
+        return self.ndof
+
+
+def get_ngauss(mesh: Mesh) -> int:
+    return 3 * mesh.nelem
+
+
+def get_area(mesh: Mesh):
+    a = np.empty(mesh.nelem)
+    check(_lib_().adfem_mesh_area(mesh.handle, ptr(a)))
+    return a
+
+
+def gauss_nodes(mesh: Mesh):
+    x = np.empty(get_ngauss(mesh))
+    y = np.empty(get_ngauss(mesh))
+    check(_lib_().adfem_mesh_gauss_nodes(mesh.handle, ptr(x), ptr(y)))
+    return np.stack([x, y], axis=1)
+
+
+def fem_nodes(mesh: Mesh):
+    return mesh.nodes
+
+
+def bcnode(mesh: Mesh):
+    """Boundary node ids, 1-based, ascending (the reference returns Julia Set order)."""
+    L = _lib_()
+    n = ctypes.c_longlong()
+    check(L.adfem_mesh_bcnode(mesh.handle, None, ctypes.byref(n)))
+    out = np.empty(n.value, np.int64)
+    check(L.adfem_mesh_bcnode(mesh.handle, ptr(out), ctypes.byref(n)))
+    return out
+
+
+def _csc(nzval, cp1, rv1, n):
+    return sp.csc_matrix((nzval, rv1 - 1, cp1 - 1), shape=(n, n))
+
+
+def compute_fem_laplace_matrix1(kappa, mesh: Mesh):
+    """Stiffness matrix of -div(kappa grad u) (SparseMatrixCSC arm), kappa at the Gauss points."""
+    kappa = _c(kappa, np.float64).ravel()
+    if kappa.size != get_ngauss(mesh):
+        raise AdFemError(_lib.ERR_INVALID, "length(kappa) must equal get_ngauss(mesh)")
+    cp, rv = mesh.pattern()
+    nz = np.empty(rv.size)
+    check(_lib_().adfem_laplace_csc(mesh.handle, ptr(kappa), kappa.size, ptr(nz)), "compute_fem_laplace_matrix1")
+    return _csc(nz, cp, rv, mesh.ndof)
+
+
+def compute_fem_source_term1(f, mesh: Mesh):
+    f = _c(f, np.float64).ravel()
+    if f.size != get_ngauss(mesh):
+        raise AdFemError(_lib.ERR_INVALID, "length(f) must equal get_ngauss(mesh)")
+    out = np.zeros(mesh.ndof)
+    check(_lib_().adfem_source(mesh.handle, ptr(f), f.size, ptr(out), 0), "compute_fem_source_term1")
+    return out
+
+
+def compute_fem_source_term(f1, f2=None, mesh: Mesh | None = None):
+    """[src(f1); src(f2)], or a single stacked vector of length 2 ngauss (MCore.jl:87-94)."""
+    if mesh is None and isinstance(f2, Mesh):
+        mesh, f = f2, _c(f1, np.float64).ravel()
+        ng = get_ngauss(mesh)
+        if f.size != 2 * ng:
+            raise AdFemError(_lib.ERR_INVALID, "length(f) must be 2 ngauss")
+        f1, f2 = f[:ng], f[ng:]
+    return np.concatenate([compute_fem_source_term1(f1, mesh), compute_fem_source_term1(f2, mesh)])
+
+
+def compute_fem_stiffness_matrix(D, mesh: Mesh):
+    """Elasticity stiffness (2 ndof x 2 ndof, [x; y] DOF blocks); D is (3,3) or (ngauss,3,3)."""
+    D = np.asarray(D, dtype=np.float64)
+    ng = get_ngauss(mesh)
+    if D.shape == (3, 3):
+        D = np.broadcast_to(D, (ng, 3, 3))
+    if D.shape != (ng, 3, 3):
+        raise AdFemError(_lib.ERR_INVALID, "D must be (3,3) or (ngauss,3,3)")
+    D = _c(D, np.float64).ravel()
+    cp, rv = mesh.pattern_elasticity()
+    nz = np.empty(rv.size)
+    check(_lib_().adfem_stiffness_csc(mesh.handle, ptr(D), D.size, ptr(nz)), "compute_fem_stiffness_matrix")
+    return _csc(nz, cp, rv, 2 * mesh.ndof)
+
+
+def _plane(E, nu, fn):
+    E = _c(E, np.float64).ravel()
+    nu = _c(nu, np.float64).ravel()
+    if E.size != nu.size:
+        raise AdFemError(_lib.ERR_INVALID, "E and nu must have the same length")
+    out = np.empty((E.size, 3, 3))
+    getattr(_lib_(), fn)(ptr(out), ptr(E), ptr(nu), E.size)
+    return out
+
+
+def compute_plane_strain_matrix(E, nu):
+    """Pointwise plane-strain matrices (N,3,3), the reference's nine-entry formula."""
+    if np.isscalar(E) and np.isscalar(nu):
+        return _plane([E], [nu], "PlaneStrainMatrix_forward")[0]
+    return _plane(E, nu, "PlaneStrainMatrix_forward")
+
+
+def compute_plane_stress_matrix(E, nu):
+    if np.isscalar(E) and np.isscalar(nu):
+        return _plane([E], [nu], "PlaneStressMatrix_forward")[0]
+    return _plane(E, nu, "PlaneStressMatrix_forward")
+
+
+def impose_Dirichlet_boundary_conditions(A, rhs, bdnode, bdval, keep_zeros: bool = False):
+    """SparseMatrixCSC arm: returns (B, r) with B = [A_II 0; 0 I], r_I = rhs_I - A_IB bdval, r_B = bdval."""
+    A = sp.csc_matrix(A)
+    A.sort_indices()
+    n = A.shape[0]
+    if A.shape[1] != n or len(rhs) != n:
+        raise AdFemError(_lib.ERR_INVALID, "A must be square and match rhs")
+    cp = _c(A.indptr, np.int64) + 1
+    rv = _c(A.indices, np.int64) + 1
+    nz = _c(A.data, np.float64)
+    rhs = _c(rhs, np.float64)
+    bd = _c(bdnode, np.int64).ravel()
+    bv = _c(bdval, np.float64).ravel()
+    if bd.size != bv.size:
+        raise AdFemError(_lib.ERR_INVALID, "length(bdnode) must equal length(bdval)")
+    L = _lib_()
+    onnz = ctypes.c_longlong()
+    check(L.adfem_dirichlet_csc(n, ptr(cp), ptr(rv), ptr(nz), ptr(rhs), ptr(bd), bd.size, ptr(bv), int(keep_zeros),
+                                None, None, None, ctypes.byref(onnz), None), "impose_Dirichlet_boundary_conditions")
+    ocp = np.empty(n + 1, np.int64)
+    orv = np.empty(onnz.value, np.int64)
+    onz = np.empty(onnz.value)
+    orhs = np.empty(n)
+    check(L.adfem_dirichlet_csc(n, ptr(cp), ptr(rv), ptr(nz), ptr(rhs), ptr(bd), bd.size, ptr(bv), int(keep_zeros),
+                                ptr(ocp), ptr(orv), ptr(onz), ctypes.byref(onnz), ptr(orhs)),
+          "impose_Dirichlet_boundary_conditions")
+    return _csc(onz, ocp, orv, n), orhs
+
+
+def impose_Dirichlet_coo(indices, vv, n, rhs, bdnode, bdval):
+    """SparseTensor arm (ImposeDirichlet op): indices (N,2) 0-based; returns (oindices, ov, orhs)."""
+    idx = _c(indices, np.int64).reshape(-1)
+    vv = _c(vv, np.float64)
+    rhs = _c(rhs, np.float64)
+    bd = _c(bdnode, np.int64).ravel()
+    bv = _c(bdval, np.float64).ravel()
+    L = _lib_()
+    cnt = ctypes.c_longlong()
+    check(L.adfem_dirichlet_coo(ptr(idx), ptr(vv), vv.size, ptr(bd), bd.size, ptr(rhs), ptr(bv), n, None, None, None,
+                                ctypes.byref(cnt)), "impose_Dirichlet (COO)")
+    oi = np.empty(2 * cnt.value, np.int64)
+    ov = np.empty(cnt.value)
+    orhs = np.empty(n)
+    check(L.adfem_dirichlet_coo(ptr(idx), ptr(vv), vv.size, ptr(bd), bd.size, ptr(rhs), ptr(bv), n, ptr(oi), ptr(ov),
+                                ptr(orhs), ctypes.byref(cnt)), "impose_Dirichlet (COO)")
+    return oi.reshape(-1, 2), ov, orhs
+
+
+def impose_Dirichlet_coo_backward(grad_vv, grad_rhs, indices, vv, n, bdnode, bdval):
+    idx = _c(indices, np.int64).reshape(-1)
+    vv = _c(vv, np.float64)
+    g = _c(grad_vv, np.float64)
+    gr = _c(grad_rhs, np.float64)
+    bd = _c(bdnode, np.int64).ravel()
+    bv = _c(bdval, np.float64).ravel()
+    gvi = np.empty(vv.size)
+    gri = np.empty(n)
+    gb = np.empty(bd.size)
+    check(_lib_().adfem_dirichlet_coo_backward(ptr(g), ptr(gr), ptr(idx), ptr(vv), vv.size, ptr(bd), bd.size, ptr(bv),
+                                               n, ptr(gvi), ptr(gri), ptr(gb)), "impose_Dirichlet backward (COO)")
+    return gvi, gri, gb
+
+
+def solver_opts(precision: str = "fp64", rtol: float = 1e-12, max_iter: int = 200000, ru_delta: float = 0.1,
+                chunk: int = 32, warm_start: bool = False) -> SolverOpts:
+    o = SolverOpts()
+    _lib_().adfem_solver_opts_default(ctypes.byref(o))
+    o.rtol = rtol
+    o.max_iter = max_iter
+    o.precision = {"fp64": _lib.PREC_FP64, "mixed": _lib.PREC_MIXED}[precision]
+    o.ru_delta = ru_delta
+    o.chunk = chunk
+    o.warm_start = int(warm_start)
+    return o
+
+
+def solve(K, F, precision: str = "fp64", rtol: float = 1e-12, max_iter: int = 200000, return_stats: bool = False):
+    """``K\\F`` for a symmetric positive definite sparse K (GPU Jacobi-CG)."""
+    K = sp.csc_matrix(K)
+    K.sort_indices()
+    n = K.shape[0]
+    cp = _c(K.indptr, np.int64) + 1
+    rv = _c(K.indices, np.int64) + 1
+    nz = _c(K.data, np.float64)
+    F = _c(F, np.float64)
+    u = np.zeros(n)
+    o = solver_opts(precision, rtol, max_iter)
+    st = SolverStats()
+    check(_lib_().adfem_csc_solve(n, ptr(cp), ptr(rv), ptr(nz), ptr(F), ptr(u), ctypes.byref(o), ctypes.byref(st)),
+          "solve")
+    return (u, st) if return_stats else u
+
+
+from .system import ElasticitySystem, PoissonSystem  # noqa: E402
+
+__all__ += ["PoissonSystem", "ElasticitySystem"]

@@ -1,0 +1,168 @@
+// Internal declarations shared by the host runtime and the CUDA kernels of
+// libadfem_gpu.  Nothing here is part of the C ABI (see include/adfem_gpu.h).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <memory>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "../../include/adfem_gpu.h"
+
+namespace adfem {
+
+// ---------------------------------------------------------------------------
+// errors: every entry point returns an adfem status; the message of the last
+// failure on the calling thread is kept for adfem_last_error().
+void set_error(const std::string& msg);
+int fail(int status, const std::string& msg);
+int cuda_fail(cudaError_t e, const char* what);
+
+#define ADFEM_CUDA(call)                                   \
+  do {                                                     \
+    cudaError_t _e = (call);                               \
+    if (_e != cudaSuccess) return ::adfem::cuda_fail(_e, #call); \
+  } while (0)
+
+#define ADFEM_TRY(call)                  \
+  do {                                   \
+    int _s = (call);                     \
+    if (_s != ADFEM_OK) return _s;       \
+  } while (0)
+
+// ---------------------------------------------------------------------------
+// device buffer with RAII ownership (cudaMalloc / cudaFree)
+struct DevBuf {
+  void* p = nullptr;
+  size_t bytes = 0;
+  DevBuf() = default;
+  DevBuf(const DevBuf&) = delete;
+  DevBuf& operator=(const DevBuf&) = delete;
+  ~DevBuf() { release(); }
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    bytes = 0;
+  }
+  int alloc(size_t nbytes);  // (re)allocates only when larger storage is needed
+  template <class T>
+  T* as() const { return reinterpret_cast<T*>(p); }
+};
+
+// ---------------------------------------------------------------------------
+// Packed node->element incidence record.  For node i, each incident element e in
+// ascending element order contributes one record:
+//   x = e
+//   y = a | off0 << 2 | off1 << 12 | off2 << 22
+// where a is i's local vertex index in e and off_b is the position (within row i
+// of the scalar CSR pattern) of the column of e's local vertex b.  Rows are
+// limited to 1024 entries by the 10-bit fields.
+__host__ __device__ inline unsigned inc_a(unsigned y) { return y & 3u; }
+__host__ __device__ inline unsigned inc_off(unsigned y, unsigned b) { return (y >> (2 + 10 * b)) & 1023u; }
+
+// Sliced-ELL layout (slices of 32 consecutive rows, entries stored column-major
+// within a slice so that one warp reads 32 consecutive values per step).
+// Entry k of row r sits at sptr[r>>5] + 32*k + (r&31); a slice is as wide as its
+// longest row, padding entries have value 0 and delta 0 (column = row).
+struct Sell {
+  int64_t n = 0;        // rows
+  int64_t nslices = 0;  // ceil(n / 32)
+  int64_t nent = 0;     // stored entries incl. padding
+  int maxw = 0;         // widest slice
+  bool delta16 = false; // column stored as int16 delta to the row, else int32 column
+  DevBuf sptr;          // int32 [nslices + 1]  (units of entries)
+  DevBuf col;           // int16 [nent] (delta) or int32 [nent]
+  DevBuf val64;         // double [nent]
+  DevBuf val32;         // float  [nent]
+};
+
+// Device-resident P1 mesh: geometry, incidence, scalar CSR pattern and the
+// sliced-ELL copy of that pattern.
+struct Mesh {
+  int64_t nv = 0, ne = 0;
+  int64_t nnz = 0;      // scalar CSR pattern entries
+  int maxrow = 0;       // longest scalar row
+  int maxinc = 0;       // largest node valence (incident elements)
+  int flipped = 0;      // elements reoriented
+
+  // host copies (needed by the getters and by the legacy API)
+  std::vector<double> xy;        // 2*nv
+  std::vector<int32_t> elem;     // 3*ne vertex ids after the orientation fix
+  std::vector<double> area;      // ne (Heron)
+  std::vector<double> grad;      // 6*ne: hx0 hy0 hx1 hy1 hx2 hy2
+  std::vector<int32_t> rowptr;   // nv+1
+  std::vector<int32_t> colind;   // nnz
+  std::vector<int32_t> inc_ptr;  // nv+1
+  std::vector<uint32_t> inc;     // 2 * 3ne (x,y pairs)
+  std::vector<int64_t> edges;    // 2*nedges, 1-based (min block then max block); filled lazily
+  int64_t nedges = -1;
+
+  // device copies
+  DevBuf d_xy;       // double2 [nv]
+  DevBuf d_conn;     // int4 [ne] {v0,v1,v2,0}
+  DevBuf d_geo;      // double4 [ne] {g01, g02, g12, w}; g_ab = w * grad_a . grad_b
+  DevBuf d_grad;     // double2 [3*ne] {hx_a, hy_a}
+  DevBuf d_inc_ptr;  // int32 [nv+1]
+  DevBuf d_inc;      // uint2 [3*ne]
+  DevBuf d_rowptr;   // int32 [nv+1]
+  DevBuf d_colind;   // int32 [nnz]
+  DevBuf d_diagpos;  // int32 [nv] position of the diagonal within its row
+
+  Sell sell;         // scalar pattern in sliced-ELL (values unused here)
+  DevBuf d_sell2;    // (built lazily) interleaved 2-dof pattern: see Elasticity
+
+  // per-mesh scratch reused by the host-pointer entry points
+  std::mutex mu;
+  DevBuf s_in0, s_in1, s_out0, s_out1, s_el0, s_el1;
+};
+
+// Build a mesh from xyz triples (z ignored) and 0-based triangles.  Host work
+// (orientation fix, geometry, incidence, pattern) then upload.
+int mesh_build(const double* xyz, int64_t nv, const int32_t* elems0, int64_t ne, Mesh** out);
+int mesh_edges(Mesh* m);  // fills m->edges / nedges (first-appearance numbering)
+int64_t mesh_bcnode(const Mesh* m, int64_t* out1);  // ascending 1-based boundary nodes
+void mesh_gauss(const Mesh* m, double* x, double* y);  // 3 points per element
+
+// ---------------------------------------------------------------------------
+// kernels (launchers; every launcher returns cudaError_t from cudaGetLastError)
+enum class Layout { CSR = 0, CSRT = 1, SELL = 2 };
+
+// per-element prepass: sigma_e = kappa_e0 + kappa_e1 + kappa_e2 (may be null),
+// src_e[r] = w * sum_k f_k phi_r(x_k) (may be null)
+cudaError_t launch_element_prepass(const Mesh& m, const double* kappa, const double* f, double* sigma,
+                                   double* src3, cudaStream_t st);
+// Laplace values into the scalar pattern (CSR or sliced-ELL), no Dirichlet
+cudaError_t launch_laplace_rows(const Mesh& m, const double* sigma, double* vals, Layout lay, cudaStream_t st);
+// load vector: rhs[i] (+)= sum over incident elements of src_e[a]
+cudaError_t launch_source_rows(const Mesh& m, const double* src3, double* rhs, bool accumulate, cudaStream_t st);
+// unsummed COO of the reference op (FemLaplaceScalar_forward): 9 entries per Gauss point
+cudaError_t launch_laplace_coo(const Mesh& m, const double* kappa, long long* indices, double* vv, cudaStream_t st);
+cudaError_t launch_laplace_coo_backward(const Mesh& m, const double* grad_vv, double* grad_kappa, cudaStream_t st);
+cudaError_t launch_source_backward(const Mesh& m, const double* grad_rhs, double* grad_f, cudaStream_t st);
+// fused Poisson system: Laplace + load + Dirichlet (bd rows -> identity, bd columns
+// dropped into the rhs lift), values into sliced-ELL (full pattern, dropped entries 0)
+cudaError_t launch_poisson_system(const Mesh& m, const double* sigma, const double* src3, const uint8_t* isbd,
+                                  const double* bdval_dense, double* sell_vals, double* rhs, cudaStream_t st);
+// adjoint element kernel: grad_kappa[3e+k] = -w_e (grad lam_e).(grad u_e), lam zero on bd
+cudaError_t launch_poisson_kappa_grad(const Mesh& m, const double* u, const double* lam, const uint8_t* isbd,
+                                      double* grad_kappa, cudaStream_t st);
+
+// elasticity
+cudaError_t launch_plane_strain(int mode, int64_t n, const double* E, const double* nu, double* D, cudaStream_t st);
+cudaError_t launch_plane_strain_backward(int mode, int64_t n, const double* g, const double* E, const double* nu,
+                                         double* gE, double* gnu, cudaStream_t st);
+// Dbar_e = w_e * sum_k D_k (9 per element)
+cudaError_t launch_stiffness_prepass(const Mesh& m, const double* D, double* Dbar, cudaStream_t st);
+// Dbar_e from E (plane strain, reference formula) -- fused material path
+cudaError_t launch_stiffness_prepass_E(const Mesh& m, const double* E, const double* nu, double* Dbar,
+                                       cudaStream_t st);
+// block-ordered [x; y] CSR rows (reference ordering); transpose => CSC values
+cudaError_t launch_stiffness_rows(const Mesh& m, const double* Dbar, double* vals, bool transpose,
+                                  cudaStream_t st);
+cudaError_t launch_stiffness_coo(const Mesh& m, const double* D, long long* indices, double* vv, cudaStream_t st);
+cudaError_t launch_stiffness_coo_backward(const Mesh& m, const double* grad_vv, double* grad_D, cudaStream_t st);
+
+}  // namespace adfem

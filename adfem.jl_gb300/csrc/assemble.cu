@@ -1,0 +1,363 @@
+// Assembly kernels for the P1 path (sm_103a).
+//
+// Design: GB300 executes FP64 at ~1.2 TFLOP/s (1/58 of FP32), so the kernels are
+// built to spend as few FP64 instructions as possible per byte moved:
+//  * per-mesh geometry is precomputed once: g_ab = w * grad phi_a . grad phi_b for
+//    the three vertex pairs of each element, and w = ip.weight * area / 0.5;
+//  * an element prepass reduces the per-Gauss-point inputs to per-element values
+//    (sigma_e = sum_k kappa_k, src_e[r] = w sum_k f_k phi_r(x_k));
+//  * the matrix is then assembled ROW BY ROW: the thread owning node i walks the
+//    elements around i in ascending element order and accumulates its row in
+//    shared memory.  Each CSR value is summed by exactly one thread in a fixed
+//    order, so assembly is bit-reproducible, needs no atomics and writes each
+//    output value once.  The diagonal is the negated sum of the off-diagonals
+//    (P1 element matrices have zero row sums).
+#include "adfem_internal.h"
+
+namespace adfem {
+
+static constexpr int kBlock = 256;
+
+__device__ __forceinline__ int64_t gtid() { return (int64_t)blockIdx.x * blockDim.x + threadIdx.x; }
+static inline unsigned nblocks(int64_t n, int b = kBlock) { return (unsigned)((n + b - 1) / b); }
+
+// barycentric coordinate of vertex r at quadrature point k: points 0,1,2 are
+// (xi,eta) = (1/6,1/6), (1/6,2/3), (2/3,1/6) so phi = (1-xi-eta, xi, eta)
+__device__ __forceinline__ double lam(int k, int r) {
+  const double qx = (k == 2) ? 2.0 / 3.0 : 1.0 / 6.0;
+  const double qy = (k == 1) ? 2.0 / 3.0 : 1.0 / 6.0;
+  return r == 0 ? 1.0 - qx - qy : (r == 1 ? qx : qy);
+}
+
+// g of the vertex pair (a, b), a != b, from {g01, g02, g12}
+__device__ __forceinline__ double gpair(const double4& g, int a, int b) {
+  int s = a + b;  // 1 -> (0,1), 2 -> (0,2), 3 -> (1,2)
+  return s == 1 ? g.x : (s == 2 ? g.y : g.z);
+}
+
+// ---------------------------------------------------------------------------
+__global__ void k_element_prepass(int64_t ne, const double* __restrict__ kappa, const double* __restrict__ f,
+                                  const double4* __restrict__ geo, double* __restrict__ sigma,
+                                  double* __restrict__ src3) {
+  int64_t e = gtid();
+  if (e >= ne) return;
+  if (kappa) sigma[e] = kappa[3 * e] + kappa[3 * e + 1] + kappa[3 * e + 2];
+  if (f) {
+    double w = geo[e].w;
+    double f0 = f[3 * e], f1 = f[3 * e + 1], f2 = f[3 * e + 2];
+#pragma unroll
+    for (int r = 0; r < 3; r++) src3[3 * e + r] = w * (f0 * lam(0, r) + f1 * lam(1, r) + f2 * lam(2, r));
+  }
+}
+
+cudaError_t launch_element_prepass(const Mesh& m, const double* kappa, const double* f, double* sigma, double* src3,
+                                   cudaStream_t st) {
+  k_element_prepass<<<nblocks(m.ne), kBlock, 0, st>>>(m.ne, kappa, f, m.d_geo.as<double4>(), sigma, src3);
+  return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
+// output addressing of entry k of row i
+struct OutCSR {
+  const int32_t* rowptr;
+  __device__ __forceinline__ int64_t at(int64_t i, int k) const { return (int64_t)rowptr[i] + k; }
+};
+struct OutSELL {
+  const int32_t* sptr;
+  __device__ __forceinline__ int64_t at(int64_t i, int k) const { return (int64_t)sptr[i >> 5] + 32 * k + (i & 31); }
+};
+
+// accumulate the Laplace row of node i into acc[.][t]; returns the row length
+template <int MAXW>
+__device__ __forceinline__ void laplace_row_acc(int64_t i, const int32_t* __restrict__ inc_ptr,
+                                                const uint2* __restrict__ inc, const double4* __restrict__ geo,
+                                                const double* __restrict__ sigma, int w, int dp,
+                                                double (*acc)[kBlock], int t) {
+  for (int k = 0; k < w; k++) acc[k][t] = 0.0;
+  const int32_t s1 = inc_ptr[i + 1];
+  for (int32_t s = inc_ptr[i]; s < s1; s++) {
+    const uint2 rec = inc[s];
+    const unsigned e = rec.x, y = rec.y, a = inc_a(y);
+    const double4 g = geo[e];
+    const double sg = sigma[e];
+    const unsigned b = (a == 0) ? 1 : 0, c = (a == 2) ? 1 : 2;
+    const unsigned ob = inc_off(y, b), oc = inc_off(y, c);
+    acc[ob][t] = fma(gpair(g, a, b), sg, acc[ob][t]);
+    acc[oc][t] = fma(gpair(g, a, c), sg, acc[oc][t]);
+  }
+  double d = 0.0;
+  for (int k = 0; k < w; k++)
+    if (k != dp) d -= acc[k][t];
+  acc[dp][t] = d;
+}
+
+template <int MAXW, class Out>
+__global__ void __launch_bounds__(kBlock) k_laplace_rows(int64_t n, const int32_t* __restrict__ inc_ptr,
+                                                         const uint2* __restrict__ inc,
+                                                         const double4* __restrict__ geo,
+                                                         const double* __restrict__ sigma,
+                                                         const int32_t* __restrict__ rowptr,
+                                                         const int32_t* __restrict__ diagpos, Out out,
+                                                         double* __restrict__ vals) {
+  __shared__ double acc[MAXW][kBlock];
+  const int t = threadIdx.x;
+  const int64_t i = gtid();
+  if (i >= n) return;
+  const int w = rowptr[i + 1] - rowptr[i];
+  const int dp = diagpos[i];
+  laplace_row_acc<MAXW>(i, inc_ptr, inc, geo, sigma, w, dp, acc, t);
+  for (int k = 0; k < w; k++) vals[out.at(i, k)] = acc[k][t];
+}
+
+template <class Out>
+static cudaError_t laplace_rows_dispatch(const Mesh& m, const double* sigma, double* vals, Out out, cudaStream_t st) {
+  const auto* ip = m.d_inc_ptr.as<int32_t>();
+  const auto* inc = m.d_inc.as<uint2>();
+  const auto* geo = m.d_geo.as<double4>();
+  const auto* rp = m.d_rowptr.as<int32_t>();
+  const auto* dp = m.d_diagpos.as<int32_t>();
+  if (m.maxrow <= 8)
+    k_laplace_rows<8, Out><<<nblocks(m.nv), kBlock, 0, st>>>(m.nv, ip, inc, geo, sigma, rp, dp, out, vals);
+  else if (m.maxrow <= 16)
+    k_laplace_rows<16, Out><<<nblocks(m.nv), kBlock, 0, st>>>(m.nv, ip, inc, geo, sigma, rp, dp, out, vals);
+  else if (m.maxrow <= 24)
+    k_laplace_rows<24, Out><<<nblocks(m.nv), kBlock, 0, st>>>(m.nv, ip, inc, geo, sigma, rp, dp, out, vals);
+  else
+    return cudaErrorInvalidValue;  // mesh_build rejects rows > 64; wider rows take the generic path below
+  return cudaGetLastError();
+}
+
+// generic (wide rows, up to 64): dynamic shared memory, smaller blocks
+template <class Out>
+__global__ void __launch_bounds__(64) k_laplace_rows_wide(int64_t n, const int32_t* __restrict__ inc_ptr,
+                                                          const uint2* __restrict__ inc,
+                                                          const double4* __restrict__ geo,
+                                                          const double* __restrict__ sigma,
+                                                          const int32_t* __restrict__ rowptr,
+                                                          const int32_t* __restrict__ diagpos, Out out,
+                                                          double* __restrict__ vals) {
+  __shared__ double acc[64][64];
+  const int t = threadIdx.x;
+  const int64_t i = (int64_t)blockIdx.x * 64 + t;
+  if (i >= n) return;
+  const int w = rowptr[i + 1] - rowptr[i];
+  const int dp = diagpos[i];
+  for (int k = 0; k < w; k++) acc[k][t] = 0.0;
+  for (int32_t s = inc_ptr[i]; s < inc_ptr[i + 1]; s++) {
+    const uint2 rec = inc[s];
+    const unsigned e = rec.x, y = rec.y, a = inc_a(y);
+    const double4 g = geo[e];
+    const double sg = sigma[e];
+    const unsigned b = (a == 0) ? 1 : 0, c = (a == 2) ? 1 : 2;
+    acc[inc_off(y, b)][t] = fma(gpair(g, a, b), sg, acc[inc_off(y, b)][t]);
+    acc[inc_off(y, c)][t] = fma(gpair(g, a, c), sg, acc[inc_off(y, c)][t]);
+  }
+  double d = 0.0;
+  for (int k = 0; k < w; k++)
+    if (k != dp) d -= acc[k][t];
+  acc[dp][t] = d;
+  for (int k = 0; k < w; k++) vals[out.at(i, k)] = acc[k][t];
+}
+
+cudaError_t launch_laplace_rows(const Mesh& m, const double* sigma, double* vals, Layout lay, cudaStream_t st) {
+  if (m.maxrow > 24) {
+    if (lay == Layout::SELL)
+      k_laplace_rows_wide<OutSELL><<<nblocks(m.nv, 64), 64, 0, st>>>(
+          m.nv, m.d_inc_ptr.as<int32_t>(), m.d_inc.as<uint2>(), m.d_geo.as<double4>(), sigma,
+          m.d_rowptr.as<int32_t>(), m.d_diagpos.as<int32_t>(), OutSELL{m.sell.sptr.as<int32_t>()}, vals);
+    else
+      k_laplace_rows_wide<OutCSR><<<nblocks(m.nv, 64), 64, 0, st>>>(
+          m.nv, m.d_inc_ptr.as<int32_t>(), m.d_inc.as<uint2>(), m.d_geo.as<double4>(), sigma,
+          m.d_rowptr.as<int32_t>(), m.d_diagpos.as<int32_t>(), OutCSR{m.d_rowptr.as<int32_t>()}, vals);
+    return cudaGetLastError();
+  }
+  if (lay == Layout::SELL) return laplace_rows_dispatch(m, sigma, vals, OutSELL{m.sell.sptr.as<int32_t>()}, st);
+  return laplace_rows_dispatch(m, sigma, vals, OutCSR{m.d_rowptr.as<int32_t>()}, st);
+}
+
+// ---------------------------------------------------------------------------
+__global__ void k_source_rows(int64_t n, const int32_t* __restrict__ inc_ptr, const uint2* __restrict__ inc,
+                              const double* __restrict__ src3, double* __restrict__ rhs, int accumulate) {
+  const int64_t i = gtid();
+  if (i >= n) return;
+  double s = accumulate ? rhs[i] : 0.0;
+  for (int32_t j = inc_ptr[i]; j < inc_ptr[i + 1]; j++) {
+    const uint2 rec = inc[j];
+    s += src3[3 * (int64_t)rec.x + inc_a(rec.y)];
+  }
+  rhs[i] = s;
+}
+
+cudaError_t launch_source_rows(const Mesh& m, const double* src3, double* rhs, bool accumulate, cudaStream_t st) {
+  k_source_rows<<<nblocks(m.nv), kBlock, 0, st>>>(m.nv, m.d_inc_ptr.as<int32_t>(), m.d_inc.as<uint2>(), src3, rhs,
+                                                  accumulate ? 1 : 0);
+  return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
+// Fused Poisson system: Laplace row + load + Dirichlet in one pass, into sliced-ELL.
+// isbd[i]: 0 interior, 1 Dirichlet node, 2 interior with a Dirichlet neighbour.
+template <int MAXW>
+__global__ void __launch_bounds__(kBlock) k_poisson_system(
+    int64_t n, const int32_t* __restrict__ inc_ptr, const uint2* __restrict__ inc, const double4* __restrict__ geo,
+    const double* __restrict__ sigma, const double* __restrict__ src3, const int32_t* __restrict__ rowptr,
+    const int32_t* __restrict__ colind, const int32_t* __restrict__ diagpos, const int32_t* __restrict__ sptr,
+    const uint8_t* __restrict__ isbd, const double* __restrict__ bdval, double* __restrict__ vals,
+    double* __restrict__ rhs) {
+  __shared__ double acc[MAXW][kBlock];
+  const int t = threadIdx.x;
+  const int64_t i = gtid();
+  if (i >= n) return;
+  const int w = rowptr[i + 1] - rowptr[i];
+  const int dp = diagpos[i];
+  const int64_t base = (int64_t)sptr[i >> 5] + (i & 31);
+  const uint8_t tag = isbd[i];
+  if (tag == 1) {
+    for (int k = 0; k < w; k++) vals[base + 32 * k] = (k == dp) ? 1.0 : 0.0;
+    rhs[i] = bdval[i];
+    return;
+  }
+  laplace_row_acc<MAXW>(i, inc_ptr, inc, geo, sigma, w, dp, acc, t);
+  double r = 0.0;
+  for (int32_t s = inc_ptr[i]; s < inc_ptr[i + 1]; s++) {
+    const uint2 rec = inc[s];
+    r += src3[3 * (int64_t)rec.x + inc_a(rec.y)];
+  }
+  if (tag == 2) {
+    const int32_t r0 = rowptr[i];
+    for (int k = 0; k < w; k++) {
+      const int32_t j = colind[r0 + k];
+      if (isbd[j] == 1) {
+        r = fma(-acc[k][t], bdval[j], r);
+        acc[k][t] = 0.0;
+      }
+    }
+  }
+  rhs[i] = r;
+  for (int k = 0; k < w; k++) vals[base + 32 * k] = acc[k][t];
+}
+
+cudaError_t launch_poisson_system(const Mesh& m, const double* sigma, const double* src3, const uint8_t* isbd,
+                                  const double* bdval_dense, double* sell_vals, double* rhs, cudaStream_t st) {
+  const auto* ip = m.d_inc_ptr.as<int32_t>();
+  const auto* inc = m.d_inc.as<uint2>();
+  const auto* geo = m.d_geo.as<double4>();
+  const auto* rp = m.d_rowptr.as<int32_t>();
+  const auto* ci = m.d_colind.as<int32_t>();
+  const auto* dp = m.d_diagpos.as<int32_t>();
+  const auto* sp = m.sell.sptr.as<int32_t>();
+  if (m.maxrow <= 8)
+    k_poisson_system<8><<<nblocks(m.nv), kBlock, 0, st>>>(m.nv, ip, inc, geo, sigma, src3, rp, ci, dp, sp, isbd,
+                                                          bdval_dense, sell_vals, rhs);
+  else if (m.maxrow <= 16)
+    k_poisson_system<16><<<nblocks(m.nv), kBlock, 0, st>>>(m.nv, ip, inc, geo, sigma, src3, rp, ci, dp, sp, isbd,
+                                                           bdval_dense, sell_vals, rhs);
+  else if (m.maxrow <= 24)
+    k_poisson_system<24><<<nblocks(m.nv), kBlock, 0, st>>>(m.nv, ip, inc, geo, sigma, src3, rp, ci, dp, sp, isbd,
+                                                           bdval_dense, sell_vals, rhs);
+  else
+    return cudaErrorNotSupported;
+  return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
+// Unsummed COO of FemLaplaceScalar_forward (FemLaplaceScalar.h:3-26): entry
+// z = 27 e + 9 k + 3 p + q is (dof_p, dof_q, (w grad_p.grad_q) kappa_{3e+k}).
+// One thread per entry keeps the 16-byte index and 8-byte value stores coalesced.
+__global__ void k_laplace_coo(int64_t ne, const int4* __restrict__ conn, const double4* __restrict__ geo,
+                              const double* __restrict__ kappa, longlong2* __restrict__ idx,
+                              double* __restrict__ vv) {
+  const int64_t z = gtid();
+  if (z >= 27 * ne) return;
+  const int64_t e = z / 27;
+  const int rem = (int)(z - 27 * e);
+  const int k = rem / 9, p = (rem / 3) % 3, q = rem % 3;
+  const int4 c = conn[e];
+  const double4 g = geo[e];
+  double gpq;
+  if (p != q) {
+    gpq = gpair(g, p, q);
+  } else {
+    const int b = (p == 0) ? 1 : 0, cc = (p == 2) ? 1 : 2;
+    gpq = -(gpair(g, p, b) + gpair(g, p, cc));
+  }
+  const int vp = p == 0 ? c.x : (p == 1 ? c.y : c.z);
+  const int vq = q == 0 ? c.x : (q == 1 ? c.y : c.z);
+  idx[z] = make_longlong2(vp, vq);
+  vv[z] = gpq * kappa[3 * e + k];
+}
+
+cudaError_t launch_laplace_coo(const Mesh& m, const double* kappa, long long* indices, double* vv, cudaStream_t st) {
+  k_laplace_coo<<<nblocks(27 * m.ne), kBlock, 0, st>>>(m.ne, m.d_conn.as<int4>(), m.d_geo.as<double4>(), kappa,
+                                                       reinterpret_cast<longlong2*>(indices), vv);
+  return cudaGetLastError();
+}
+
+// FemLaplaceScalar_backward (FemLaplaceScalar.h:28-54): grad_kappa[3e+k] = sum_pq grad_vv * (w grad_p.grad_q)
+__global__ void k_laplace_coo_backward(int64_t ne, const double4* __restrict__ geo, const double* __restrict__ gvv,
+                                       double* __restrict__ gk) {
+  const int64_t s = gtid();
+  if (s >= 3 * ne) return;
+  const int64_t e = s / 3;
+  const double4 g = geo[e];
+  const double g00 = -(g.x + g.y), g11 = -(g.x + g.z), g22 = -(g.y + g.z);
+  const double G[9] = {g00, g.x, g.y, g.x, g11, g.z, g.y, g.z, g22};
+  const double* src = gvv + 9 * s;
+  double v = 0.0;
+#pragma unroll
+  for (int j = 0; j < 9; j++) v = fma(src[j], G[j], v);
+  gk[s] = v;
+}
+
+cudaError_t launch_laplace_coo_backward(const Mesh& m, const double* grad_vv, double* grad_kappa, cudaStream_t st) {
+  k_laplace_coo_backward<<<nblocks(3 * m.ne), kBlock, 0, st>>>(m.ne, m.d_geo.as<double4>(), grad_vv, grad_kappa);
+  return cudaGetLastError();
+}
+
+// FemSourceScalar_backward (FemSourceScalar.h:17-32)
+__global__ void k_source_backward(int64_t ne, const int4* __restrict__ conn, const double4* __restrict__ geo,
+                                  const double* __restrict__ grhs, double* __restrict__ gf) {
+  const int64_t s = gtid();
+  if (s >= 3 * ne) return;
+  const int64_t e = s / 3;
+  const int k = (int)(s - 3 * e);
+  const int4 c = conn[e];
+  const double w = geo[e].w;
+  gf[s] = w * (lam(k, 0) * grhs[c.x] + lam(k, 1) * grhs[c.y] + lam(k, 2) * grhs[c.z]);
+}
+
+cudaError_t launch_source_backward(const Mesh& m, const double* grad_rhs, double* grad_f, cudaStream_t st) {
+  k_source_backward<<<nblocks(3 * m.ne), kBlock, 0, st>>>(m.ne, m.d_conn.as<int4>(), m.d_geo.as<double4>(),
+                                                          grad_rhs, grad_f);
+  return cudaGetLastError();
+}
+
+// Adjoint element kernel: dL/dkappa_{3e+k} = -w (grad lam).(grad u)
+//   = sum_{a<b} g_ab (lam_a - lam_b)(u_a - u_b)      (row sums of g vanish)
+__global__ void k_poisson_kappa_grad(int64_t ne, const int4* __restrict__ conn, const double4* __restrict__ geo,
+                                     const double* __restrict__ u, const double* __restrict__ lam,
+                                     const uint8_t* __restrict__ isbd, double* __restrict__ gk) {
+  const int64_t e = gtid();
+  if (e >= ne) return;
+  const int4 c = conn[e];
+  const double4 g = geo[e];
+  const double u0 = u[c.x], u1 = u[c.y], u2 = u[c.z];
+  const double l0 = isbd[c.x] == 1 ? 0.0 : lam[c.x];
+  const double l1 = isbd[c.y] == 1 ? 0.0 : lam[c.y];
+  const double l2 = isbd[c.z] == 1 ? 0.0 : lam[c.z];
+  double v = g.x * (l0 - l1) * (u0 - u1);
+  v = fma(g.y * (l0 - l2), (u0 - u2), v);
+  v = fma(g.z * (l1 - l2), (u1 - u2), v);
+  gk[3 * e] = v;
+  gk[3 * e + 1] = v;
+  gk[3 * e + 2] = v;
+}
+
+cudaError_t launch_poisson_kappa_grad(const Mesh& m, const double* u, const double* lam, const uint8_t* isbd,
+                                      double* grad_kappa, cudaStream_t st) {
+  k_poisson_kappa_grad<<<nblocks(m.ne), kBlock, 0, st>>>(m.ne, m.d_conn.as<int4>(), m.d_geo.as<double4>(), u, lam,
+                                                         isbd, grad_kappa);
+  return cudaGetLastError();
+}
+
+}  // namespace adfem

@@ -1,0 +1,1028 @@
+// extern "C" entry points of libadfem_gpu.so (declared in include/adfem_gpu.h).
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "adfem_internal.h"
+#include "dirichlet.cuh"
+#include "elastic.cuh"
+#include "solver.cuh"
+
+using namespace adfem;
+
+namespace adfem {
+const char* last_error_cstr();
+}
+
+struct adfem_mesh {
+  Mesh* m;
+};
+
+struct adfem_system {
+  adfem_mesh* mesh = nullptr;
+  int kind = ADFEM_SYS_POISSON;
+  int64_t ndof = 0;  // nv (Poisson) or 2 nv (elasticity)
+  Sell A;            // operator in solver DOF order (interleaved for elasticity)
+  DevBuf diagpos;    // int32 [ndof]
+  DevBuf isbd;       // uint8 [ndof] 0 free, 1 Dirichlet, 2 free next to a Dirichlet DOF
+  DevBuf bdval;      // double [ndof] dense Dirichlet values
+  DevBuf rhs;        // double [ndof]
+  DevBuf sigma, src3, srcy3, Dbar;  // per-element scratch
+  DevBuf t0, t1, t2;                // ndof scratch (interleaving, host staging)
+  DevBuf in0, in1;                  // host-staging of per-Gauss-point inputs
+  Solver solver;
+  bool assembled = false;
+  std::mutex mu;
+};
+
+namespace {
+
+std::mutex g_cur_mu;
+adfem_mesh* g_current = nullptr;
+bool g_current_owned = false;
+
+cudaStream_t S(void* p) { return reinterpret_cast<cudaStream_t>(p); }
+
+Mesh* current_mesh() {
+  std::lock_guard<std::mutex> lk(g_cur_mu);
+  return g_current ? g_current->m : nullptr;
+}
+
+template <class T>
+int to_dev(DevBuf& b, const T* h, size_t n) {
+  ADFEM_TRY(b.alloc(sizeof(T) * std::max<size_t>(n, 1)));
+  if (n) ADFEM_CUDA(cudaMemcpy(b.p, h, sizeof(T) * n, cudaMemcpyHostToDevice));
+  return ADFEM_OK;
+}
+template <class T>
+int to_host(T* h, const DevBuf& b, size_t n) {
+  if (n) ADFEM_CUDA(cudaMemcpy(h, b.p, sizeof(T) * n, cudaMemcpyDeviceToHost));
+  return ADFEM_OK;
+}
+int kerr(cudaError_t e, const char* what) {
+  if (e != cudaSuccess) return cuda_fail(e, what);
+  return ADFEM_OK;
+}
+
+void legacy_report(int st, const char* fn) {
+  if (st != ADFEM_OK) std::fprintf(stderr, "libadfem_gpu: %s failed: %s\n", fn, last_error_cstr());
+}
+
+// Dirichlet data for a system: tags over the solver DOF order
+int system_set_bd(adfem_system* s, const long long* bd, long long nbd, const double* bdval) {
+  Mesh& m = *s->mesh->m;
+  const int64_t nd = s->ndof;
+  std::vector<uint8_t> tag(nd, 0);
+  std::vector<double> val(nd, 0.0);
+  auto map = [&](int64_t d0) -> int64_t {  // reference DOF -> solver DOF
+    if (s->kind == ADFEM_SYS_POISSON) return d0;
+    return d0 < m.nv ? 2 * d0 : 2 * (d0 - m.nv) + 1;
+  };
+  for (long long k = 0; k < nbd; k++) {
+    const long long d = bd[k] - 1;
+    if (d < 0 || d >= nd) return fail(ADFEM_ERR_INVALID, "Dirichlet DOF " + std::to_string(bd[k]) + " out of range");
+    const int64_t q = map(d);
+    if (tag[q]) return fail(ADFEM_ERR_INVALID, "duplicate Dirichlet DOF " + std::to_string(bd[k]));
+    tag[q] = 1;
+    val[q] = bdval ? bdval[k] : 0.0;
+  }
+  for (int64_t i = 0; i < m.nv; i++) {
+    bool near = false;
+    for (int32_t k = m.rowptr[i]; k < m.rowptr[i + 1]; k++) {
+      const int64_t j = m.colind[k];
+      if (s->kind == ADFEM_SYS_POISSON) near |= tag[j] == 1;
+      else near |= (tag[2 * j] == 1) || (tag[2 * j + 1] == 1);
+    }
+    if (!near) continue;
+    if (s->kind == ADFEM_SYS_POISSON) {
+      if (tag[i] == 0) tag[i] = 2;
+    } else {
+      if (tag[2 * i] == 0) tag[2 * i] = 2;
+      if (tag[2 * i + 1] == 0) tag[2 * i + 1] = 2;
+    }
+  }
+  ADFEM_TRY(to_dev(s->isbd, tag.data(), tag.size()));
+  ADFEM_TRY(to_dev(s->bdval, val.data(), val.size()));
+  s->assembled = false;
+  return ADFEM_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* adfem_status_string(int st) {
+  switch (st) {
+    case ADFEM_OK: return "ok";
+    case ADFEM_ERR_INVALID: return "invalid argument";
+    case ADFEM_ERR_CUDA: return "CUDA error";
+    case ADFEM_ERR_NOMEM: return "out of memory";
+    case ADFEM_ERR_NOT_CONVERGED: return "not converged";
+    case ADFEM_ERR_BREAKDOWN: return "CG breakdown";
+    case ADFEM_ERR_NO_MESH: return "no current mesh";
+    case ADFEM_ERR_NONFINITE: return "non-finite input";
+    case ADFEM_ERR_UNSUPPORTED: return "unsupported";
+    case ADFEM_ERR_BUSY: return "busy";
+    case ADFEM_ERR_TIMEOUT: return "timeout";
+    default: return "unknown status";
+  }
+}
+const char* adfem_last_error(void) { return last_error_cstr(); }
+const char* adfem_version(void) { return "adfem_gpu 0.1 (sm_103a)"; }
+
+// ------------------------------------------------------------------ meshes
+int adfem_mesh_create(const double* xyz, long long nv, const int* elems0, long long ne, int degree,
+                      adfem_mesh** out) {
+  if (!out) return fail(ADFEM_ERR_INVALID, "null output handle");
+  *out = nullptr;
+  if (degree != 1) return fail(ADFEM_ERR_UNSUPPORTED, "only P1 (degree 1) elements are implemented");
+  Mesh* m = nullptr;
+  ADFEM_TRY(mesh_build(xyz, nv, reinterpret_cast<const int32_t*>(elems0), ne, &m));
+  *out = new adfem_mesh{m};
+  return ADFEM_OK;
+}
+
+int adfem_mesh_destroy(adfem_mesh* mesh) {
+  if (!mesh) return ADFEM_OK;
+  {
+    std::lock_guard<std::mutex> lk(g_cur_mu);
+    if (g_current == mesh) {
+      g_current = nullptr;
+      g_current_owned = false;
+    }
+  }
+  delete mesh->m;
+  delete mesh;
+  return ADFEM_OK;
+}
+
+int adfem_mesh_sizes(const adfem_mesh* mesh, long long* nv, long long* ne, long long* ngauss, long long* nnz) {
+  if (!mesh) return fail(ADFEM_ERR_INVALID, "null mesh");
+  if (nv) *nv = mesh->m->nv;
+  if (ne) *ne = mesh->m->ne;
+  if (ngauss) *ngauss = 3 * mesh->m->ne;
+  if (nnz) *nnz = mesh->m->nnz;
+  return ADFEM_OK;
+}
+
+int adfem_set_current_mesh(adfem_mesh* mesh) {
+  std::lock_guard<std::mutex> lk(g_cur_mu);
+  if (g_current && g_current_owned && g_current != mesh) {
+    delete g_current->m;
+    delete g_current;
+  }
+  g_current = mesh;
+  g_current_owned = false;
+  return ADFEM_OK;
+}
+adfem_mesh* adfem_current_mesh(void) {
+  std::lock_guard<std::mutex> lk(g_cur_mu);
+  return g_current;
+}
+
+int adfem_mesh_pattern(const adfem_mesh* mesh, long long* colptr1, long long* rowval1) {
+  if (!mesh || !colptr1 || !rowval1) return fail(ADFEM_ERR_INVALID, "null argument");
+  const Mesh& m = *mesh->m;
+  for (int64_t i = 0; i <= m.nv; i++) colptr1[i] = (long long)m.rowptr[i] + 1;
+  for (int64_t k = 0; k < m.nnz; k++) rowval1[k] = (long long)m.colind[k] + 1;
+  return ADFEM_OK;
+}
+
+int adfem_mesh_pattern_elasticity(const adfem_mesh* mesh, long long* colptr1, long long* rowval1) {
+  if (!mesh || !colptr1 || !rowval1) return fail(ADFEM_ERR_INVALID, "null argument");
+  const Mesh& m = *mesh->m;
+  long long z = 0;
+  for (int c = 0; c < 2; c++)
+    for (int64_t i = 0; i < m.nv; i++) {
+      colptr1[c * m.nv + i] = z + 1;
+      for (int cc = 0; cc < 2; cc++)
+        for (int32_t k = m.rowptr[i]; k < m.rowptr[i + 1]; k++) rowval1[z++] = (long long)m.colind[k] + cc * m.nv + 1;
+    }
+  colptr1[2 * m.nv] = z + 1;
+  return ADFEM_OK;
+}
+
+int adfem_mesh_bcnode(const adfem_mesh* mesh, long long* out, long long* count) {
+  if (!mesh || !count) return fail(ADFEM_ERR_INVALID, "null argument");
+  *count = mesh_bcnode(mesh->m, reinterpret_cast<int64_t*>(out));
+  return ADFEM_OK;
+}
+
+int adfem_mesh_gauss_nodes(const adfem_mesh* mesh, double* x, double* y) {
+  if (!mesh || !x || !y) return fail(ADFEM_ERR_INVALID, "null argument");
+  mesh_gauss(mesh->m, x, y);
+  return ADFEM_OK;
+}
+
+int adfem_mesh_elements(const adfem_mesh* mesh, long long* elems1) {
+  if (!mesh || !elems1) return fail(ADFEM_ERR_INVALID, "null argument");
+  for (int64_t k = 0; k < 3 * mesh->m->ne; k++) elems1[k] = (long long)mesh->m->elem[k] + 1;
+  return ADFEM_OK;
+}
+
+int adfem_mesh_area(const adfem_mesh* mesh, double* area) {
+  if (!mesh || !area) return fail(ADFEM_ERR_INVALID, "null argument");
+  std::memcpy(area, mesh->m->area.data(), sizeof(double) * mesh->m->ne);
+  return ADFEM_OK;
+}
+
+int adfem_mesh_edges(const adfem_mesh* mesh, long long* out, long long* nedges) {
+  if (!mesh || !nedges) return fail(ADFEM_ERR_INVALID, "null argument");
+  ADFEM_TRY(mesh_edges(mesh->m));
+  *nedges = mesh->m->nedges;
+  if (out) std::memcpy(out, mesh->m->edges.data(), sizeof(long long) * 2 * mesh->m->nedges);
+  return ADFEM_OK;
+}
+
+// ------------------------------------------------------------------ Laplace
+int adfem_laplace_csr_d(adfem_mesh* mesh, const double* kappa_d, double* vals_d, void* stream) {
+  if (!mesh || !kappa_d || !vals_d) return fail(ADFEM_ERR_INVALID, "null argument");
+  Mesh& m = *mesh->m;
+  std::lock_guard<std::mutex> lk(m.mu);
+  ADFEM_TRY(m.s_el0.alloc(sizeof(double) * m.ne));
+  ADFEM_TRY(kerr(launch_element_prepass(m, kappa_d, nullptr, m.s_el0.as<double>(), nullptr, S(stream)), "prepass"));
+  ADFEM_TRY(kerr(launch_laplace_rows(m, m.s_el0.as<double>(), vals_d, Layout::CSR, S(stream)), "laplace rows"));
+  ADFEM_CUDA(cudaStreamSynchronize(S(stream)));
+  return ADFEM_OK;
+}
+
+int adfem_laplace_csc(adfem_mesh* mesh, const double* kappa, long long nkappa, double* nzval) {
+  if (!mesh || !kappa || !nzval) return fail(ADFEM_ERR_INVALID, "null argument");
+  Mesh& m = *mesh->m;
+  if (nkappa != 3 * m.ne) return fail(ADFEM_ERR_INVALID, "kappa must have one value per Gauss point (3 per element)");
+  DevBuf k, v;
+  ADFEM_TRY(to_dev(k, kappa, (size_t)nkappa));
+  ADFEM_TRY(v.alloc(sizeof(double) * (size_t)m.nnz));
+  ADFEM_TRY(adfem_laplace_csr_d(mesh, k.as<double>(), v.as<double>(), nullptr));
+  return to_host(nzval, v, (size_t)m.nnz);
+}
+
+int adfem_laplace_coo_d(adfem_mesh* mesh, const double* kappa_d, long long* indices_d, double* vv_d, void* stream) {
+  if (!mesh || !kappa_d || !indices_d || !vv_d) return fail(ADFEM_ERR_INVALID, "null argument");
+  ADFEM_TRY(kerr(launch_laplace_coo(*mesh->m, kappa_d, indices_d, vv_d, S(stream)), "laplace coo"));
+  return ADFEM_OK;
+}
+
+int adfem_laplace_coo_backward_d(adfem_mesh* mesh, const double* grad_vv_d, double* grad_kappa_d, void* stream) {
+  if (!mesh || !grad_vv_d || !grad_kappa_d) return fail(ADFEM_ERR_INVALID, "null argument");
+  ADFEM_TRY(kerr(launch_laplace_coo_backward(*mesh->m, grad_vv_d, grad_kappa_d, S(stream)), "laplace coo backward"));
+  return ADFEM_OK;
+}
+
+// ------------------------------------------------------------------ source
+int adfem_source_d(adfem_mesh* mesh, const double* f_d, double* rhs_d, int accumulate, void* stream) {
+  if (!mesh || !f_d || !rhs_d) return fail(ADFEM_ERR_INVALID, "null argument");
+  Mesh& m = *mesh->m;
+  std::lock_guard<std::mutex> lk(m.mu);
+  ADFEM_TRY(m.s_el1.alloc(sizeof(double) * 3 * m.ne));
+  ADFEM_TRY(kerr(launch_element_prepass(m, nullptr, f_d, nullptr, m.s_el1.as<double>(), S(stream)), "prepass"));
+  ADFEM_TRY(kerr(launch_source_rows(m, m.s_el1.as<double>(), rhs_d, accumulate != 0, S(stream)), "source rows"));
+  ADFEM_CUDA(cudaStreamSynchronize(S(stream)));
+  return ADFEM_OK;
+}
+
+int adfem_source(adfem_mesh* mesh, const double* f, long long nf, double* rhs, int accumulate) {
+  if (!mesh || !f || !rhs) return fail(ADFEM_ERR_INVALID, "null argument");
+  Mesh& m = *mesh->m;
+  if (nf != 3 * m.ne) return fail(ADFEM_ERR_INVALID, "f must have one value per Gauss point (3 per element)");
+  DevBuf fd, r;
+  ADFEM_TRY(to_dev(fd, f, (size_t)nf));
+  if (accumulate) ADFEM_TRY(to_dev(r, rhs, (size_t)m.nv));
+  else ADFEM_TRY(r.alloc(sizeof(double) * m.nv));
+  ADFEM_TRY(adfem_source_d(mesh, fd.as<double>(), r.as<double>(), accumulate, nullptr));
+  return to_host(rhs, r, (size_t)m.nv);
+}
+
+int adfem_source_backward_d(adfem_mesh* mesh, const double* grad_rhs_d, double* grad_f_d, void* stream) {
+  if (!mesh || !grad_rhs_d || !grad_f_d) return fail(ADFEM_ERR_INVALID, "null argument");
+  ADFEM_TRY(kerr(launch_source_backward(*mesh->m, grad_rhs_d, grad_f_d, S(stream)), "source backward"));
+  return ADFEM_OK;
+}
+
+// ------------------------------------------------------------------ stiffness
+int adfem_stiffness_csr_d(adfem_mesh* mesh, const double* D_d, double* vals_d, void* stream) {
+  if (!mesh || !D_d || !vals_d) return fail(ADFEM_ERR_INVALID, "null argument");
+  Mesh& m = *mesh->m;
+  std::lock_guard<std::mutex> lk(m.mu);
+  ADFEM_TRY(m.s_el0.alloc(sizeof(double) * 9 * m.ne));
+  ADFEM_TRY(kerr(launch_stiffness_prepass(m, D_d, m.s_el0.as<double>(), S(stream)), "stiffness prepass"));
+  ADFEM_TRY(kerr(launch_stiffness_rows(m, m.s_el0.as<double>(), vals_d, false, S(stream)), "stiffness rows"));
+  ADFEM_CUDA(cudaStreamSynchronize(S(stream)));
+  return ADFEM_OK;
+}
+
+int adfem_stiffness_csc(adfem_mesh* mesh, const double* D, long long nD, double* nzval) {
+  if (!mesh || !D || !nzval) return fail(ADFEM_ERR_INVALID, "null argument");
+  Mesh& m = *mesh->m;
+  if (nD != 27 * m.ne) return fail(ADFEM_ERR_INVALID, "D must hold a 3x3 matrix per Gauss point (27 per element)");
+  DevBuf dd, v;
+  ADFEM_TRY(to_dev(dd, D, (size_t)nD));
+  ADFEM_TRY(v.alloc(sizeof(double) * 4 * (size_t)m.nnz));
+  {
+    std::lock_guard<std::mutex> lk(m.mu);
+    ADFEM_TRY(m.s_el0.alloc(sizeof(double) * 9 * m.ne));
+    ADFEM_TRY(kerr(launch_stiffness_prepass(m, dd.as<double>(), m.s_el0.as<double>(), nullptr), "stiffness prepass"));
+    ADFEM_TRY(kerr(launch_stiffness_rows(m, m.s_el0.as<double>(), v.as<double>(), true, nullptr), "stiffness rows"));
+  }
+  return to_host(nzval, v, 4 * (size_t)m.nnz);
+}
+
+int adfem_stiffness_coo_d(adfem_mesh* mesh, const double* D_d, long long* indices_d, double* vv_d, void* stream) {
+  if (!mesh || !D_d || !indices_d || !vv_d) return fail(ADFEM_ERR_INVALID, "null argument");
+  ADFEM_TRY(kerr(launch_stiffness_coo(*mesh->m, D_d, indices_d, vv_d, S(stream)), "stiffness coo"));
+  return ADFEM_OK;
+}
+
+int adfem_stiffness_coo_backward_d(adfem_mesh* mesh, const double* grad_vv_d, double* grad_D_d, void* stream) {
+  if (!mesh || !grad_vv_d || !grad_D_d) return fail(ADFEM_ERR_INVALID, "null argument");
+  ADFEM_TRY(kerr(launch_stiffness_coo_backward(*mesh->m, grad_vv_d, grad_D_d, S(stream)), "stiffness coo backward"));
+  return ADFEM_OK;
+}
+
+int adfem_plane_strain_d(int mode, long long n, const double* E_d, const double* nu_d, double* D_d, void* stream) {
+  if (mode != 0 && mode != 1) return fail(ADFEM_ERR_INVALID, "mode must be 0 (plane strain) or 1 (plane stress)");
+  if (n < 0 || (n > 0 && (!E_d || !nu_d || !D_d))) return fail(ADFEM_ERR_INVALID, "bad arguments");
+  if (n == 0) return ADFEM_OK;
+  ADFEM_TRY(kerr(launch_plane_strain(mode, n, E_d, nu_d, D_d, S(stream)), "plane strain"));
+  return ADFEM_OK;
+}
+
+int adfem_plane_strain_backward_d(int mode, long long n, const double* g_d, const double* E_d, const double* nu_d,
+                                  double* gE_d, double* gnu_d, void* stream) {
+  if (mode != 0 && mode != 1) return fail(ADFEM_ERR_INVALID, "mode must be 0 (plane strain) or 1 (plane stress)");
+  if (n < 0 || (n > 0 && (!g_d || !E_d || !nu_d || !gE_d || !gnu_d))) return fail(ADFEM_ERR_INVALID, "bad arguments");
+  if (n == 0) return ADFEM_OK;
+  ADFEM_TRY(kerr(launch_plane_strain_backward(mode, n, g_d, E_d, nu_d, gE_d, gnu_d, S(stream)), "plane strain bwd"));
+  return ADFEM_OK;
+}
+
+// ------------------------------------------------------------------ Dirichlet
+// Validate a 1-based CSC matrix from the caller (monotone colptr, row ids in range) so
+// that no kernel ever sees an index outside its arrays.
+static int check_csc1(long long n, const long long* colptr1, const long long* rowval1) {
+  if (colptr1[0] != 1) return fail(ADFEM_ERR_INVALID, "colptr[1] must be 1");
+  for (long long j = 0; j < n; j++)
+    if (colptr1[j + 1] < colptr1[j]) return fail(ADFEM_ERR_INVALID, "colptr is not monotone");
+  const long long nnz = colptr1[n] - 1;
+  for (long long k = 0; k < nnz; k++)
+    if (rowval1[k] < 1 || rowval1[k] > n) return fail(ADFEM_ERR_INVALID, "row index out of range");
+  return ADFEM_OK;
+}
+
+int adfem_dirichlet_csc(long long n, const long long* colptr1, const long long* rowval1, const double* nzval,
+                        const double* rhs, const long long* bd, long long nbd, const double* bdval, int keep_zeros,
+                        long long* out_colptr1, long long* out_rowval1, double* out_nzval, long long* out_nnz,
+                        double* out_rhs) {
+  if (n < 0 || !colptr1 || !out_nnz || (nbd > 0 && (!bd || !bdval))) return fail(ADFEM_ERR_INVALID, "bad arguments");
+  const int64_t nnz = colptr1[n] - 1;
+  if (nnz < 0 || (nnz > 0 && (!rowval1 || !nzval))) return fail(ADFEM_ERR_INVALID, "bad CSC arrays");
+  ADFEM_TRY(check_csc1(n, colptr1, rowval1));
+  std::vector<uint8_t> tag(std::max<long long>(n, 1), 0);
+  for (long long k = 0; k < nbd; k++) {
+    if (bd[k] < 1 || bd[k] > n) return fail(ADFEM_ERR_INVALID, "bd index " + std::to_string(bd[k]) + " out of range");
+    if (tag[bd[k] - 1]) return fail(ADFEM_ERR_INVALID, "duplicate bd index " + std::to_string(bd[k]));
+    tag[bd[k] - 1] = 1;
+  }
+  DevBuf cp1, cp0, rv1, rv0, nz, isbd, ocp, orv, onz;
+  ADFEM_TRY(to_dev(cp1, colptr1, (size_t)n + 1));
+  ADFEM_TRY(to_dev(rv1, rowval1, (size_t)nnz));
+  ADFEM_TRY(to_dev(nz, nzval, (size_t)nnz));
+  ADFEM_TRY(to_dev(isbd, tag.data(), (size_t)n));
+  ADFEM_TRY(cp0.alloc(sizeof(int64_t) * (n + 1)));
+  ADFEM_TRY(rv0.alloc(sizeof(int64_t) * std::max<int64_t>(nnz, 1)));
+  ADFEM_TRY(kerr(launch_to0(n + 1, cp1.as<int64_t>(), cp0.as<int64_t>(), nullptr), "to0"));
+  ADFEM_TRY(kerr(launch_to0(nnz, rv1.as<int64_t>(), rv0.as<int64_t>(), nullptr), "to0"));
+  int64_t onn = 0;
+  const bool count_only = (out_colptr1 == nullptr);
+  ADFEM_TRY(dirichlet_csc_device(n, nnz, cp0.as<int64_t>(), rv0.as<int64_t>(), nz.as<double>(), isbd.as<uint8_t>(),
+                                 keep_zeros, ocp, &onn, orv, onz, count_only, nullptr));
+  *out_nnz = onn;
+  if (count_only) return ADFEM_OK;
+  if (!out_rowval1 || !out_nzval) return fail(ADFEM_ERR_INVALID, "null output arrays");
+  ADFEM_TRY(kerr(launch_to1(n + 1, ocp.as<int64_t>(), ocp.as<int64_t>(), 1, nullptr), "to1"));
+  ADFEM_TRY(to_host(out_colptr1, ocp, (size_t)n + 1));
+  ADFEM_TRY(to_host(out_rowval1, orv, (size_t)onn));
+  ADFEM_TRY(to_host(out_nzval, onz, (size_t)onn));
+  if (out_rhs) {
+    // r_I = rhs_I - A_IB bdval, the product accumulated column by column in bd order
+    // (SparseMatrixCSC * Vector), r_B = bdval
+    std::vector<double> acc(n, 0.0);
+    for (long long k = 0; k < nbd; k++) {
+      const int64_t j = bd[k] - 1;
+      for (long long p = colptr1[j] - 1; p < colptr1[j + 1] - 1; p++) {
+        const int64_t i = rowval1[p] - 1;
+        if (!tag[i]) acc[i] += nzval[p] * bdval[k];
+      }
+    }
+    for (long long i = 0; i < n; i++) out_rhs[i] = tag[i] ? 0.0 : rhs[i] - acc[i];
+    for (long long k = 0; k < nbd; k++) out_rhs[bd[k] - 1] = bdval[k];
+  }
+  return ADFEM_OK;
+}
+
+// bd map with std::map semantics (sorted unique, last assignment wins)
+static void bd_unique(const long long* bd, long long nbd, std::vector<std::pair<int64_t, int64_t>>& u) {
+  u.clear();
+  for (long long k = 0; k < nbd; k++) u.push_back({bd[k] - 1, k});
+  std::stable_sort(u.begin(), u.end(), [](auto& a, auto& b) { return a.first < b.first; });
+  std::vector<std::pair<int64_t, int64_t>> out;
+  for (auto& p : u) {
+    if (!out.empty() && out.back().first == p.first) out.back() = p;
+    else out.push_back(p);
+  }
+  u.swap(out);
+}
+
+int adfem_dirichlet_coo(const long long* indices, const double* vv, long long sN, const long long* bd, long long nbd,
+                        const double* rhs, const double* bdval, long long N, long long* oindices, double* ov,
+                        double* orhs, long long* out_n) {
+  if (sN < 0 || N < 0 || !out_n || (sN > 0 && (!indices || !vv)) || (nbd > 0 && (!bd || !bdval)))
+    return fail(ADFEM_ERR_INVALID, "bad arguments");
+  std::vector<std::pair<int64_t, int64_t>> u;
+  bd_unique(bd, nbd, u);
+  std::vector<uint8_t> tag(std::max<long long>(N, 1), 0);
+  for (auto& p : u) {
+    if (p.first < 0 || p.first >= N) return fail(ADFEM_ERR_INVALID, "bd index out of range");
+    tag[p.first] = 1;
+  }
+  DevBuf di, dv, isbd, oidx, oval, liftk;
+  ADFEM_TRY(to_dev(di, indices, 2 * (size_t)sN));
+  ADFEM_TRY(to_dev(dv, vv, (size_t)sN));
+  ADFEM_TRY(to_dev(isbd, tag.data(), (size_t)N));
+  int64_t nkeep = 0, nlift = 0;
+  const bool count_only = (oindices == nullptr);
+  ADFEM_TRY(dirichlet_coo_device(sN, di.as<long long>(), dv.as<double>(), isbd.as<uint8_t>(), N, &nkeep, oidx, oval,
+                                 &nlift, liftk, count_only, nullptr));
+  *out_n = nkeep + (long long)u.size();
+  if (count_only) return ADFEM_OK;
+  if (!ov) return fail(ADFEM_ERR_INVALID, "null output values");
+  ADFEM_TRY(to_host(oindices, oidx, 2 * (size_t)nkeep));
+  ADFEM_TRY(to_host(ov, oval, (size_t)nkeep));
+  for (size_t q = 0; q < u.size(); q++) {
+    oindices[2 * (nkeep + q)] = u[q].first;
+    oindices[2 * (nkeep + q) + 1] = u[q].first;
+    ov[nkeep + q] = 1.0;
+  }
+  if (orhs) {
+    std::vector<int64_t> lk(nlift);
+    ADFEM_TRY(to_host(lk.data(), liftk, (size_t)nlift));
+    std::vector<int64_t> pos(N, -1);
+    for (auto& p : u) pos[p.first] = p.second;
+    for (long long i = 0; i < N; i++) orhs[i] = rhs[i];
+    for (int64_t k : lk) {  // ascending entry order, as ImposeDirichlet.h:41-43
+      const int64_t i = indices[2 * k], j = indices[2 * k + 1];
+      orhs[i] = orhs[i] - vv[k] * bdval[pos[j]];
+    }
+    for (auto& p : u) orhs[p.first] = bdval[p.second];
+  }
+  return ADFEM_OK;
+}
+
+int adfem_dirichlet_coo_backward(const double* grad_vv, const double* grad_rhs, const long long* indices,
+                                 const double* vv, long long sN, const long long* bd, long long nbd,
+                                 const double* bdval, long long N, double* grad_vv_in, double* grad_rhs_in,
+                                 double* grad_bdval) {
+  if (sN < 0 || N < 0 || (sN > 0 && (!indices || !vv || !grad_vv_in)) || !grad_rhs || !grad_rhs_in ||
+      (nbd > 0 && (!bd || !bdval || !grad_bdval)))
+    return fail(ADFEM_ERR_INVALID, "bad arguments");
+  std::vector<std::pair<int64_t, int64_t>> u;
+  bd_unique(bd, nbd, u);
+  std::vector<uint8_t> tag(std::max<long long>(N, 1), 0);
+  std::vector<double> bdd(std::max<long long>(N, 1), 0.0);
+  std::vector<int64_t> pos(std::max<long long>(N, 1), -1);
+  for (auto& p : u) {
+    if (p.first < 0 || p.first >= N) return fail(ADFEM_ERR_INVALID, "bd index out of range");
+    tag[p.first] = 1;
+    bdd[p.first] = bdval[p.second];
+    pos[p.first] = p.second;
+  }
+  // number of kept entries = length of grad_vv
+  DevBuf di, dv, isbd, gv, gr, bdv, gin, oidx, oval, liftk;
+  ADFEM_TRY(to_dev(di, indices, 2 * (size_t)sN));
+  ADFEM_TRY(to_dev(dv, vv, (size_t)sN));
+  ADFEM_TRY(to_dev(isbd, tag.data(), (size_t)N));
+  int64_t nkeep = 0, nlift = 0;
+  ADFEM_TRY(dirichlet_coo_device(sN, di.as<long long>(), dv.as<double>(), isbd.as<uint8_t>(), N, &nkeep, oidx, oval,
+                                 &nlift, liftk, false, nullptr));
+  ADFEM_TRY(to_dev(gv, grad_vv, (size_t)nkeep));
+  ADFEM_TRY(to_dev(gr, grad_rhs, (size_t)N));
+  ADFEM_TRY(to_dev(bdv, bdd.data(), (size_t)N));
+  ADFEM_TRY(gin.alloc(sizeof(double) * std::max<int64_t>(sN, 1)));
+  ADFEM_TRY(dirichlet_coo_backward_device(sN, di.as<long long>(), isbd.as<uint8_t>(), N, gv.as<double>(),
+                                          bdv.as<double>(), gr.as<double>(), gin.as<double>(), nullptr));
+  ADFEM_TRY(to_host(grad_vv_in, gin, (size_t)sN));
+  std::vector<int64_t> lk(nlift);
+  ADFEM_TRY(to_host(lk.data(), liftk, (size_t)nlift));
+  for (long long b = 0; b < nbd; b++) grad_bdval[b] = 0.0;
+  for (int64_t k : lk) {  // ImposeDirichlet.h:79-83, entry order
+    const int64_t i = indices[2 * k], j = indices[2 * k + 1];
+    grad_bdval[pos[j]] -= vv[k] * grad_rhs[i];
+  }
+  for (long long i = 0; i < N; i++) grad_rhs_in[i] = tag[i] ? 0.0 : grad_rhs[i];
+  for (auto& p : u) grad_bdval[p.second] += grad_rhs[p.first];
+  return ADFEM_OK;
+}
+
+// ------------------------------------------------------------------ solves
+void adfem_solver_opts_default(adfem_solver_opts* o) {
+  if (!o) return;
+  o->rtol = 1e-12;
+  o->max_iter = 200000;
+  o->precision = ADFEM_PREC_FP64;
+  o->ru_delta = 0.1;
+  o->chunk = 32;
+  o->warm_start = 0;
+}
+
+int adfem_csc_solve(long long n, const long long* colptr1, const long long* rowval1, const double* nzval,
+                    const double* rhs, double* u, const adfem_solver_opts* opts, adfem_solver_stats* stats) {
+  if (n <= 0 || !colptr1 || !rowval1 || !nzval || !rhs || !u) return fail(ADFEM_ERR_INVALID, "bad arguments");
+  if (n > INT32_MAX) return fail(ADFEM_ERR_UNSUPPORTED, "n > 2^31");
+  adfem_solver_opts o;
+  adfem_solver_opts_default(&o);
+  if (opts) o = *opts;
+  ADFEM_TRY(check_csc1(n, colptr1, rowval1));
+  const int64_t nnz = colptr1[n] - 1;
+  if (nnz > INT32_MAX) return fail(ADFEM_ERR_UNSUPPORTED, "nnz > 2^31");
+  // a symmetric matrix's CSC arrays are its CSR arrays
+  std::vector<int32_t> rp(n + 1), ci(std::max<int64_t>(nnz, 1)), dp(n, 0);
+  for (long long i = 0; i <= n; i++) rp[i] = (int32_t)(colptr1[i] - 1);
+  for (int64_t k = 0; k < nnz; k++) {
+    const long long c = rowval1[k] - 1;
+    if (c < 0 || c >= n) return fail(ADFEM_ERR_INVALID, "row index out of range");
+    ci[k] = (int32_t)c;
+  }
+  for (long long i = 0; i < n; i++) {
+    int found = -1;
+    for (int32_t k = rp[i]; k < rp[i + 1]; k++)
+      if (ci[k] == i) found = k - rp[i];
+    if (found < 0) return fail(ADFEM_ERR_INVALID, "column " + std::to_string(i + 1) + " has no stored diagonal");
+    dp[i] = found;
+  }
+  Sell A;
+  ADFEM_TRY(sell_build_pattern(n, rp.data(), ci.data(), A));
+  ADFEM_TRY(A.val64.alloc(sizeof(double) * std::max<int64_t>(A.nent, 1)));
+  ADFEM_TRY(A.val32.alloc(sizeof(float) * std::max<int64_t>(A.nent, 1)));
+  ADFEM_CUDA(cudaMemset(A.val64.p, 0, sizeof(double) * std::max<int64_t>(A.nent, 1)));
+  DevBuf drp, dvals, ddp, db, du;
+  ADFEM_TRY(to_dev(drp, rp.data(), rp.size()));
+  ADFEM_TRY(to_dev(dvals, nzval, (size_t)nnz));
+  ADFEM_TRY(to_dev(ddp, dp.data(), dp.size()));
+  ADFEM_TRY(to_dev(db, rhs, (size_t)n));
+  if (o.warm_start) ADFEM_TRY(to_dev(du, u, (size_t)n));
+  else ADFEM_TRY(du.alloc(sizeof(double) * n));
+  ADFEM_TRY(kerr(launch_csr_to_sell(A, n, drp.as<int32_t>(), dvals.as<double>(), A.val64.as<double>(), nullptr),
+                 "csr to sell"));
+  Solver sv;
+  ADFEM_TRY(sv.init(&A, n));
+  ADFEM_TRY(solver_prepare(sv, ddp.as<int32_t>(), nullptr));
+  const int st = solver_solve(sv, db.as<double>(), du.as<double>(), nullptr, o, stats, nullptr);
+  if (st != ADFEM_OK && st != ADFEM_ERR_NOT_CONVERGED) return st;
+  ADFEM_TRY(to_host(u, du, (size_t)n));
+  return st;
+}
+
+// ------------------------------------------------------------------ systems
+int adfem_system_create(adfem_mesh* mesh, int kind, adfem_system** out) {
+  if (!mesh || !out) return fail(ADFEM_ERR_INVALID, "null argument");
+  if (kind != ADFEM_SYS_POISSON && kind != ADFEM_SYS_ELASTICITY) return fail(ADFEM_ERR_INVALID, "unknown kind");
+  *out = nullptr;
+  std::unique_ptr<adfem_system> s(new adfem_system());
+  s->mesh = mesh;
+  s->kind = kind;
+  Mesh& m = *mesh->m;
+  if (kind == ADFEM_SYS_POISSON) {
+    s->ndof = m.nv;
+    ADFEM_TRY(sell_build_pattern(m.nv, m.rowptr.data(), m.colind.data(), s->A));
+    std::vector<int32_t> dp(m.nv);
+    for (int64_t i = 0; i < m.nv; i++)
+      for (int32_t k = m.rowptr[i]; k < m.rowptr[i + 1]; k++)
+        if (m.colind[k] == i) dp[i] = k - m.rowptr[i];
+    ADFEM_TRY(to_dev(s->diagpos, dp.data(), dp.size()));
+  } else {
+    if (m.maxrow > 16) return fail(ADFEM_ERR_UNSUPPORTED, "elasticity systems support at most 15 neighbours per node");
+    s->ndof = 2 * m.nv;
+    std::vector<int32_t> rp2(2 * m.nv + 1, 0), dp2(2 * m.nv);
+    for (int64_t r = 0; r < 2 * m.nv; r++) {
+      const int64_t i = r >> 1;
+      rp2[r + 1] = rp2[r] + 2 * (m.rowptr[i + 1] - m.rowptr[i]);
+    }
+    std::vector<int32_t> ci2(rp2[2 * m.nv]);
+    for (int64_t r = 0; r < 2 * m.nv; r++) {
+      const int64_t i = r >> 1;
+      int32_t z = rp2[r];
+      for (int32_t k = m.rowptr[i]; k < m.rowptr[i + 1]; k++) {
+        if (m.colind[k] == i) dp2[r] = 2 * (k - m.rowptr[i]) + (int32_t)(r & 1);
+        ci2[z++] = 2 * m.colind[k];
+        ci2[z++] = 2 * m.colind[k] + 1;
+      }
+    }
+    ADFEM_TRY(sell_build_pattern(2 * m.nv, rp2.data(), ci2.data(), s->A));
+    ADFEM_TRY(to_dev(s->diagpos, dp2.data(), dp2.size()));
+  }
+  const size_t ne = std::max<int64_t>(s->A.nent, 1);
+  ADFEM_TRY(s->A.val64.alloc(sizeof(double) * ne));
+  ADFEM_TRY(s->A.val32.alloc(sizeof(float) * ne));
+  ADFEM_CUDA(cudaMemset(s->A.val64.p, 0, sizeof(double) * ne));
+  ADFEM_CUDA(cudaMemset(s->A.val32.p, 0, sizeof(float) * ne));
+  ADFEM_TRY(s->rhs.alloc(sizeof(double) * s->ndof));
+  ADFEM_TRY(s->t0.alloc(sizeof(double) * s->ndof));
+  ADFEM_TRY(s->t1.alloc(sizeof(double) * s->ndof));
+  ADFEM_TRY(s->t2.alloc(sizeof(double) * s->ndof));
+  ADFEM_TRY(s->solver.init(&s->A, s->ndof));
+  ADFEM_TRY(system_set_bd(s.get(), nullptr, 0, nullptr));
+  *out = s.release();
+  return ADFEM_OK;
+}
+
+int adfem_system_destroy(adfem_system* sys) {
+  delete sys;
+  return ADFEM_OK;
+}
+
+int adfem_system_set_dirichlet(adfem_system* sys, const long long* bd, long long nbd, const double* bdval) {
+  if (!sys || nbd < 0 || (nbd > 0 && !bd)) return fail(ADFEM_ERR_INVALID, "bad arguments");
+  std::lock_guard<std::mutex> lk(sys->mu);
+  return system_set_bd(sys, bd, nbd, bdval);
+}
+
+int adfem_system_assemble_poisson_d(adfem_system* sys, const double* kappa_d, const double* f_d, void* stream) {
+  if (!sys || !kappa_d || !f_d) return fail(ADFEM_ERR_INVALID, "null argument");
+  if (sys->kind != ADFEM_SYS_POISSON) return fail(ADFEM_ERR_INVALID, "not a Poisson system");
+  std::lock_guard<std::mutex> lk(sys->mu);
+  Mesh& m = *sys->mesh->m;
+  cudaStream_t st = S(stream);
+  sys->assembled = false;
+  ADFEM_TRY(sys->sigma.alloc(sizeof(double) * m.ne));
+  ADFEM_TRY(sys->src3.alloc(sizeof(double) * 3 * m.ne));
+  ADFEM_TRY(kerr(launch_element_prepass(m, kappa_d, f_d, sys->sigma.as<double>(), sys->src3.as<double>(), st),
+                 "element prepass"));
+  ADFEM_TRY(kerr(launch_poisson_system(m, sys->sigma.as<double>(), sys->src3.as<double>(), sys->isbd.as<uint8_t>(),
+                                       sys->bdval.as<double>(), sys->A.val64.as<double>(), sys->rhs.as<double>(), st),
+                 "poisson system"));
+  ADFEM_TRY(solver_prepare(sys->solver, sys->diagpos.as<int32_t>(), st));
+  sys->assembled = true;
+  return ADFEM_OK;
+}
+
+int adfem_system_assemble_elasticity_d(adfem_system* sys, const double* E_d, const double* nu_d, const double* fx_d,
+                                       const double* fy_d, void* stream) {
+  if (!sys || !E_d || !nu_d || !fx_d || !fy_d) return fail(ADFEM_ERR_INVALID, "null argument");
+  if (sys->kind != ADFEM_SYS_ELASTICITY) return fail(ADFEM_ERR_INVALID, "not an elasticity system");
+  std::lock_guard<std::mutex> lk(sys->mu);
+  Mesh& m = *sys->mesh->m;
+  cudaStream_t st = S(stream);
+  sys->assembled = false;
+  ADFEM_TRY(sys->Dbar.alloc(sizeof(double) * 9 * m.ne));
+  ADFEM_TRY(sys->src3.alloc(sizeof(double) * 3 * m.ne));
+  ADFEM_TRY(sys->srcy3.alloc(sizeof(double) * 3 * m.ne));
+  ADFEM_TRY(kerr(launch_stiffness_prepass_E(m, E_d, nu_d, sys->Dbar.as<double>(), st), "stiffness prepass"));
+  ADFEM_TRY(kerr(launch_element_prepass(m, nullptr, fx_d, nullptr, sys->src3.as<double>(), st), "prepass fx"));
+  ADFEM_TRY(kerr(launch_element_prepass(m, nullptr, fy_d, nullptr, sys->srcy3.as<double>(), st), "prepass fy"));
+  ADFEM_TRY(kerr(launch_elastic_system(m, sys->Dbar.as<double>(), sys->src3.as<double>(), sys->srcy3.as<double>(),
+                                       sys->A.sptr.as<int32_t>(), sys->isbd.as<uint8_t>(), sys->bdval.as<double>(),
+                                       sys->A.val64.as<double>(), sys->rhs.as<double>(), st),
+                 "elastic system"));
+  ADFEM_TRY(solver_prepare(sys->solver, sys->diagpos.as<int32_t>(), st));
+  sys->assembled = true;
+  return ADFEM_OK;
+}
+
+int adfem_system_solve_d(adfem_system* sys, double* u_d, const adfem_solver_opts* opts, adfem_solver_stats* stats,
+                         void* stream) {
+  if (!sys || !u_d) return fail(ADFEM_ERR_INVALID, "null argument");
+  std::lock_guard<std::mutex> lk(sys->mu);
+  if (!sys->assembled) return fail(ADFEM_ERR_INVALID, "system not assembled");
+  adfem_solver_opts o;
+  adfem_solver_opts_default(&o);
+  if (opts) o = *opts;
+  cudaStream_t st = S(stream);
+  if (sys->kind == ADFEM_SYS_POISSON)
+    return solver_solve(sys->solver, sys->rhs.as<double>(), u_d, nullptr, o, stats, st);
+  const int64_t nv = sys->mesh->m->nv;
+  if (o.warm_start) ADFEM_TRY(kerr(launch_to_interleaved(nv, u_d, sys->t0.as<double>(), st), "interleave"));
+  const int r = solver_solve(sys->solver, sys->rhs.as<double>(), sys->t0.as<double>(), nullptr, o, stats, st);
+  if (r != ADFEM_OK && r != ADFEM_ERR_NOT_CONVERGED) return r;
+  ADFEM_TRY(kerr(launch_from_interleaved(nv, sys->t0.as<double>(), u_d, st), "deinterleave"));
+  return r;
+}
+
+int adfem_system_solve_profiled_d(adfem_system* sys, double* u_d, const adfem_solver_opts* opts,
+                                  adfem_solver_stats* stats, double* kernel_ms, long long* launches, void* stream) {
+  if (!sys || !u_d || !kernel_ms || !launches) return fail(ADFEM_ERR_INVALID, "null argument");
+  if (sys->kind != ADFEM_SYS_POISSON) return fail(ADFEM_ERR_UNSUPPORTED, "profiled solves are for Poisson systems");
+  std::lock_guard<std::mutex> lk(sys->mu);
+  if (!sys->assembled) return fail(ADFEM_ERR_INVALID, "system not assembled");
+  adfem_solver_opts o;
+  adfem_solver_opts_default(&o);
+  if (opts) o = *opts;
+  SolveProfile prof;
+  const int r = solver_solve(sys->solver, sys->rhs.as<double>(), u_d, nullptr, o, stats, S(stream), &prof);
+  for (int j = 0; j < 4; j++) {
+    kernel_ms[j] = prof.ms[j];
+    launches[j] = prof.n[j];
+  }
+  return r;
+}
+
+int adfem_system_adjoint_d(adfem_system* sys, const double* g_d, double* lam_d, const adfem_solver_opts* opts,
+                           adfem_solver_stats* stats, void* stream) {
+  if (!sys || !g_d || !lam_d) return fail(ADFEM_ERR_INVALID, "null argument");
+  std::lock_guard<std::mutex> lk(sys->mu);
+  if (!sys->assembled) return fail(ADFEM_ERR_INVALID, "system not assembled");
+  adfem_solver_opts o;
+  adfem_solver_opts_default(&o);
+  if (opts) o = *opts;
+  cudaStream_t st = S(stream);
+  if (sys->kind == ADFEM_SYS_POISSON)
+    return solver_solve(sys->solver, g_d, lam_d, sys->isbd.as<uint8_t>(), o, stats, st);
+  const int64_t nv = sys->mesh->m->nv;
+  ADFEM_TRY(kerr(launch_to_interleaved(nv, g_d, sys->t1.as<double>(), st), "interleave"));
+  if (o.warm_start) ADFEM_TRY(kerr(launch_to_interleaved(nv, lam_d, sys->t0.as<double>(), st), "interleave"));
+  const int r = solver_solve(sys->solver, sys->t1.as<double>(), sys->t0.as<double>(), sys->isbd.as<uint8_t>(), o,
+                             stats, st);
+  if (r != ADFEM_OK && r != ADFEM_ERR_NOT_CONVERGED) return r;
+  ADFEM_TRY(kerr(launch_from_interleaved(nv, sys->t0.as<double>(), lam_d, st), "deinterleave"));
+  return r;
+}
+
+int adfem_system_grad_kappa_d(adfem_system* sys, const double* u_d, const double* lam_d, double* grad_kappa_d,
+                              void* stream) {
+  if (!sys || !u_d || !lam_d || !grad_kappa_d) return fail(ADFEM_ERR_INVALID, "null argument");
+  if (sys->kind != ADFEM_SYS_POISSON) return fail(ADFEM_ERR_INVALID, "not a Poisson system");
+  ADFEM_TRY(kerr(launch_poisson_kappa_grad(*sys->mesh->m, u_d, lam_d, sys->isbd.as<uint8_t>(), grad_kappa_d,
+                                           S(stream)),
+                 "kappa grad"));
+  return ADFEM_OK;
+}
+
+int adfem_system_grad_E_d(adfem_system* sys, const double* u_d, const double* lam_d, const double* E_d,
+                          const double* nu_d, double* grad_E_d, void* stream) {
+  (void)E_d;
+  if (!sys || !u_d || !lam_d || !nu_d || !grad_E_d) return fail(ADFEM_ERR_INVALID, "null argument");
+  if (sys->kind != ADFEM_SYS_ELASTICITY) return fail(ADFEM_ERR_INVALID, "not an elasticity system");
+  std::lock_guard<std::mutex> lk(sys->mu);
+  const int64_t nv = sys->mesh->m->nv;
+  cudaStream_t st = S(stream);
+  ADFEM_TRY(kerr(launch_to_interleaved(nv, u_d, sys->t1.as<double>(), st), "interleave"));
+  ADFEM_TRY(kerr(launch_to_interleaved(nv, lam_d, sys->t2.as<double>(), st), "interleave"));
+  ADFEM_TRY(kerr(launch_elastic_grad_E(*sys->mesh->m, sys->t1.as<double>(), sys->t2.as<double>(),
+                                       sys->isbd.as<uint8_t>(), nu_d, grad_E_d, st),
+                 "grad E"));
+  return ADFEM_OK;
+}
+
+int adfem_system_apply_d(adfem_system* sys, const double* x_d, double* y_d, void* stream) {
+  if (!sys || !x_d || !y_d) return fail(ADFEM_ERR_INVALID, "null argument");
+  std::lock_guard<std::mutex> lk(sys->mu);
+  if (!sys->assembled) return fail(ADFEM_ERR_INVALID, "system not assembled");
+  cudaStream_t st = S(stream);
+  if (sys->kind == ADFEM_SYS_POISSON) return solver_apply(sys->solver, x_d, y_d, st);
+  const int64_t nv = sys->mesh->m->nv;
+  ADFEM_TRY(kerr(launch_to_interleaved(nv, x_d, sys->t1.as<double>(), st), "interleave"));
+  ADFEM_TRY(solver_apply(sys->solver, sys->t1.as<double>(), sys->t2.as<double>(), st));
+  ADFEM_TRY(kerr(launch_from_interleaved(nv, sys->t2.as<double>(), y_d, st), "deinterleave"));
+  return ADFEM_OK;
+}
+
+int adfem_system_rhs_d(adfem_system* sys, double* rhs_d, void* stream) {
+  if (!sys || !rhs_d) return fail(ADFEM_ERR_INVALID, "null argument");
+  std::lock_guard<std::mutex> lk(sys->mu);
+  if (!sys->assembled) return fail(ADFEM_ERR_INVALID, "system not assembled");
+  cudaStream_t st = S(stream);
+  if (sys->kind == ADFEM_SYS_POISSON) {
+    ADFEM_CUDA(cudaMemcpyAsync(rhs_d, sys->rhs.p, sizeof(double) * sys->ndof, cudaMemcpyDeviceToDevice, st));
+    return ADFEM_OK;
+  }
+  ADFEM_TRY(kerr(launch_from_interleaved(sys->mesh->m->nv, sys->rhs.as<double>(), rhs_d, st), "deinterleave"));
+  return ADFEM_OK;
+}
+
+int adfem_poisson_solve(adfem_system* sys, const double* kappa, const double* f, double* u,
+                        const adfem_solver_opts* opts, adfem_solver_stats* stats) {
+  if (!sys || !kappa || !f || !u) return fail(ADFEM_ERR_INVALID, "null argument");
+  if (sys->kind != ADFEM_SYS_POISSON) return fail(ADFEM_ERR_INVALID, "not a Poisson system");
+  Mesh& m = *sys->mesh->m;
+  const size_t ng = 3 * (size_t)m.ne;
+  ADFEM_TRY(sys->in0.alloc(sizeof(double) * ng));
+  ADFEM_TRY(sys->in1.alloc(sizeof(double) * ng));
+  ADFEM_CUDA(cudaMemcpy(sys->in0.p, kappa, sizeof(double) * ng, cudaMemcpyHostToDevice));
+  ADFEM_CUDA(cudaMemcpy(sys->in1.p, f, sizeof(double) * ng, cudaMemcpyHostToDevice));
+  ADFEM_TRY(adfem_system_assemble_poisson_d(sys, sys->in0.as<double>(), sys->in1.as<double>(), nullptr));
+  if (opts && opts->warm_start) ADFEM_CUDA(cudaMemcpy(sys->t2.p, u, sizeof(double) * m.nv, cudaMemcpyHostToDevice));
+  const int r = adfem_system_solve_d(sys, sys->t2.as<double>(), opts, stats, nullptr);
+  if (r != ADFEM_OK && r != ADFEM_ERR_NOT_CONVERGED) return r;
+  ADFEM_CUDA(cudaMemcpy(u, sys->t2.p, sizeof(double) * m.nv, cudaMemcpyDeviceToHost));
+  return r;
+}
+
+// ================================================================== legacy layer
+long long* init_nnfem_mesh(double* vertices, int num_vertices, int* element_indices, int num_elements, int order,
+                           int lorder, int degree, long long* nedges) {
+  (void)lorder;
+  if (degree != 1 || (order != 2 && order != -1)) {
+    fail(ADFEM_ERR_UNSUPPORTED, "only P1 elements with the order-2 triangle rule are implemented");
+    legacy_report(ADFEM_ERR_UNSUPPORTED, "init_nnfem_mesh");
+    return nullptr;
+  }
+  adfem_mesh* h = nullptr;
+  int st = adfem_mesh_create(vertices, num_vertices, element_indices, num_elements, 1, &h);
+  if (st != ADFEM_OK) {
+    legacy_report(st, "init_nnfem_mesh");
+    return nullptr;
+  }
+  {
+    std::lock_guard<std::mutex> lk(g_cur_mu);
+    if (g_current) {
+      std::printf("WARNING: Internal mesh is being overwritten!\n");
+      if (g_current_owned) {
+        delete g_current->m;
+        delete g_current;
+      }
+    }
+    g_current = h;
+    g_current_owned = true;
+  }
+  mesh_edges(h->m);
+  if (nedges) *nedges = h->m->nedges;
+  long long* out = static_cast<long long*>(std::malloc(sizeof(long long) * std::max<int64_t>(2 * h->m->nedges, 1)));
+  if (out) std::memcpy(out, h->m->edges.data(), sizeof(long long) * 2 * h->m->nedges);
+  return out;
+}
+
+#define LEGACY_MESH(fn, ret)                                 \
+  Mesh* m = current_mesh();                                  \
+  if (!m) {                                                  \
+    fail(ADFEM_ERR_NO_MESH, "no current mesh");              \
+    legacy_report(ADFEM_ERR_NO_MESH, fn);                    \
+    return ret;                                              \
+  }
+
+int mfem_get_ngauss(void) {
+  LEGACY_MESH("mfem_get_ngauss", 0);
+  return (int)(3 * m->ne);
+}
+void mfem_get_gauss(double* x, double* y) {
+  LEGACY_MESH("mfem_get_gauss", );
+  mesh_gauss(m, x, y);
+}
+void mfem_get_gauss_weights(double* w) {
+  LEGACY_MESH("mfem_get_gauss_weights", );
+  for (int64_t e = 0; e < m->ne; e++)
+    for (int k = 0; k < 3; k++) w[3 * e + k] = (1.0 / 6.0) * m->area[e] / 0.5;
+}
+void mfem_get_area(double* a) {
+  LEGACY_MESH("mfem_get_area", );
+  for (int64_t e = 0; e < m->ne; e++) a[e] = m->area[e];
+}
+int mfem_get_elem_ndof(void) {
+  LEGACY_MESH("mfem_get_elem_ndof", 0);
+  return 3;
+}
+int mfem_get_ndof(void) {
+  LEGACY_MESH("mfem_get_ndof", 0);
+  return (int)m->nv;
+}
+void mfem_get_connectivity(long long* conn) {
+  LEGACY_MESH("mfem_get_connectivity", );
+  for (int64_t e = 0; e < 3 * m->ne; e++) conn[e] = (long long)m->elem[e] + 1;
+}
+void mfem_get_element_to_vertices(long long* elems) {
+  LEGACY_MESH("mfem_get_element_to_vertices", );
+  for (int64_t e = 0; e < m->ne; e++)
+    for (int k = 0; k < 3; k++) elems[k * m->ne + e] = (long long)m->elem[3 * e + k] + 1;
+}
+
+static int legacy_laplace_coo(Mesh* m, long long* indices, double* vv, const double* kappa) {
+  const size_t ng = 3 * (size_t)m->ne, N = 9 * ng;
+  DevBuf k, idx, v;
+  ADFEM_TRY(to_dev(k, kappa, ng));
+  ADFEM_TRY(idx.alloc(sizeof(long long) * 2 * N));
+  ADFEM_TRY(v.alloc(sizeof(double) * N));
+  ADFEM_TRY(kerr(launch_laplace_coo(*m, k.as<double>(), idx.as<long long>(), v.as<double>(), nullptr), "laplace coo"));
+  ADFEM_TRY(to_host(indices, idx, 2 * N));
+  return to_host(vv, v, N);
+}
+
+void FemLaplaceScalar_forward_Julia(long long* indices, double* vv, const double* kappa) {
+  LEGACY_MESH("FemLaplaceScalar_forward_Julia", );
+  legacy_report(legacy_laplace_coo(m, indices, vv, kappa), "FemLaplaceScalar_forward_Julia");
+}
+
+void FemSourceScalar_forward_Julia(double* rhs, const double* f) {
+  LEGACY_MESH("FemSourceScalar_forward_Julia", );
+  adfem_mesh h{m};
+  legacy_report(adfem_source(&h, f, 3 * m->ne, rhs, 1), "FemSourceScalar_forward_Julia");
+}
+
+static int legacy_stiffness_coo(Mesh* m, long long* indices, double* vv, const double* hmat) {
+  const size_t ng = 3 * (size_t)m->ne, N = 36 * ng;
+  DevBuf d, idx, v;
+  ADFEM_TRY(to_dev(d, hmat, 9 * ng));
+  ADFEM_TRY(idx.alloc(sizeof(long long) * 2 * N));
+  ADFEM_TRY(v.alloc(sizeof(double) * N));
+  ADFEM_TRY(kerr(launch_stiffness_coo(*m, d.as<double>(), idx.as<long long>(), v.as<double>(), nullptr),
+                 "stiffness coo"));
+  ADFEM_TRY(to_host(indices, idx, 2 * N));
+  return to_host(vv, v, N);
+}
+
+void ComputeFemStiffnessMatrixMfem_forward_Julia(long long* indices, double* vv, const double* hmat) {
+  LEGACY_MESH("ComputeFemStiffnessMatrixMfem_forward_Julia", );
+  legacy_report(legacy_stiffness_coo(m, indices, vv, hmat), "ComputeFemStiffnessMatrixMfem_forward_Julia");
+}
+
+static int legacy_laplace_backward(Mesh* m, double* grad_kappa, const double* grad_vv) {
+  const size_t ng = 3 * (size_t)m->ne;
+  DevBuf g, o;
+  ADFEM_TRY(to_dev(g, grad_vv, 9 * ng));
+  ADFEM_TRY(o.alloc(sizeof(double) * ng));
+  ADFEM_TRY(kerr(launch_laplace_coo_backward(*m, g.as<double>(), o.as<double>(), nullptr), "laplace backward"));
+  return to_host(grad_kappa, o, ng);
+}
+
+void FemLaplaceScalar_backward(double* grad_kappa, const double* grad_vv, const long long* indices, const double* vv,
+                               const double* kappa) {
+  (void)indices;
+  (void)vv;
+  (void)kappa;
+  LEGACY_MESH("FemLaplaceScalar_backward", );
+  legacy_report(legacy_laplace_backward(m, grad_kappa, grad_vv), "FemLaplaceScalar_backward");
+}
+
+static int legacy_source_backward(Mesh* m, double* grad_f, const double* grad_rhs) {
+  const size_t ng = 3 * (size_t)m->ne;
+  DevBuf g, o;
+  ADFEM_TRY(to_dev(g, grad_rhs, (size_t)m->nv));
+  ADFEM_TRY(o.alloc(sizeof(double) * ng));
+  ADFEM_TRY(kerr(launch_source_backward(*m, g.as<double>(), o.as<double>(), nullptr), "source backward"));
+  return to_host(grad_f, o, ng);
+}
+
+void FemSourceScalar_backward(double* grad_f, const double* grad_rhs, const double* rhs, const double* f) {
+  (void)rhs;
+  (void)f;
+  LEGACY_MESH("FemSourceScalar_backward", );
+  legacy_report(legacy_source_backward(m, grad_f, grad_rhs), "FemSourceScalar_backward");
+}
+
+static int legacy_stiffness_backward(Mesh* m, double* grad_hmat, const double* grad_vv) {
+  const size_t ng = 3 * (size_t)m->ne;
+  DevBuf g, o;
+  ADFEM_TRY(to_dev(g, grad_vv, 36 * ng));
+  ADFEM_TRY(o.alloc(sizeof(double) * 9 * ng));
+  ADFEM_TRY(kerr(launch_stiffness_coo_backward(*m, g.as<double>(), o.as<double>(), nullptr), "stiffness backward"));
+  return to_host(grad_hmat, o, 9 * ng);
+}
+
+void ComputeFemStiffnessMatrixMfem_backward(double* grad_hmat, const double* grad_vv) {
+  LEGACY_MESH("ComputeFemStiffnessMatrixMfem_backward", );
+  legacy_report(legacy_stiffness_backward(m, grad_hmat, grad_vv), "ComputeFemStiffnessMatrixMfem_backward");
+}
+
+static int host_plane(int mode, const double* E, const double* nu, int N, double* out) {
+  if (N <= 0) return ADFEM_OK;
+  DevBuf e, v, o;
+  ADFEM_TRY(to_dev(e, E, (size_t)N));
+  ADFEM_TRY(to_dev(v, nu, (size_t)N));
+  ADFEM_TRY(o.alloc(sizeof(double) * 9 * (size_t)N));
+  ADFEM_TRY(kerr(launch_plane_strain(mode, N, e.as<double>(), v.as<double>(), o.as<double>(), nullptr), "plane"));
+  return to_host(out, o, 9 * (size_t)N);
+}
+static int host_plane_bwd(int mode, const double* g, const double* E, const double* nu, int N, double* gE,
+                          double* gnu) {
+  if (N <= 0) return ADFEM_OK;
+  DevBuf dg, e, v, oe, on;
+  ADFEM_TRY(to_dev(dg, g, 9 * (size_t)N));
+  ADFEM_TRY(to_dev(e, E, (size_t)N));
+  ADFEM_TRY(to_dev(v, nu, (size_t)N));
+  ADFEM_TRY(oe.alloc(sizeof(double) * (size_t)N));
+  ADFEM_TRY(on.alloc(sizeof(double) * (size_t)N));
+  ADFEM_TRY(kerr(launch_plane_strain_backward(mode, N, dg.as<double>(), e.as<double>(), v.as<double>(),
+                                              oe.as<double>(), on.as<double>(), nullptr),
+                 "plane backward"));
+  ADFEM_TRY(to_host(gE, oe, (size_t)N));
+  return to_host(gnu, on, (size_t)N);
+}
+
+void PlaneStrainMatrix_forward(double* out, const double* E, const double* nu, int N) {
+  legacy_report(host_plane(0, E, nu, N, out), "PlaneStrainMatrix_forward");
+}
+void PlaneStrainMatrix_backward(double* grad_nu, double* grad_E, const double* grad_out, const double* E,
+                                const double* nu, int N) {
+  legacy_report(host_plane_bwd(0, grad_out, E, nu, N, grad_E, grad_nu), "PlaneStrainMatrix_backward");
+}
+void PlaneStressMatrix_forward(double* out, const double* E, const double* nu, int N) {
+  legacy_report(host_plane(1, E, nu, N, out), "PlaneStressMatrix_forward");
+}
+void PlaneStressMatrix_backward(double* grad_nu, double* grad_E, const double* grad_out, const double* E,
+                                const double* nu, int N) {
+  legacy_report(host_plane_bwd(1, grad_out, E, nu, N, grad_E, grad_nu), "PlaneStressMatrix_backward");
+}
+
+}  // extern "C"

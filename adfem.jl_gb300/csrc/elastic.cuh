@@ -1,0 +1,13 @@
+// Elasticity launchers used by the C API (see elastic.cu).
+#pragma once
+#include "adfem_internal.h"
+
+namespace adfem {
+cudaError_t launch_elastic_system(const Mesh& m, const double* Dbar, const double* srcx, const double* srcy,
+                                  const int32_t* sptr2, const uint8_t* isbd2, const double* bdval2, double* vals,
+                                  double* rhs, cudaStream_t st);
+cudaError_t launch_elastic_grad_E(const Mesh& m, const double* u2, const double* lam2, const uint8_t* isbd2,
+                                  const double* nu, double* gE, cudaStream_t st);
+cudaError_t launch_to_interleaved(int64_t nv, const double* ref, double* il, cudaStream_t st);
+cudaError_t launch_from_interleaved(int64_t nv, const double* il, double* ref, cudaStream_t st);
+}  // namespace adfem

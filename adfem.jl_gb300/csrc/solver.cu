@@ -1,0 +1,751 @@
+// Jacobi-scaled conjugate gradients on a sliced-ELL operator (sm_103a).
+//
+//  * The operator is scaled once, K~ = S K S with S = diag(1/sqrt(K_ii)), so CG on
+//    K~ is Jacobi-preconditioned CG on K with no preconditioner vector in the loop.
+//  * FP64 path: three kernels per iteration (SpMV + p.q, update + r.r, p update).
+//  * Mixed path: FP32 copy of K~, FP32 vectors and FP32 accumulation in the inner
+//    iteration (two kernels: SpMV with the p update folded into the gather, and the
+//    x/r update); when the FP32 residual has dropped by ru_delta the FP32 iterate is
+//    folded into the FP64 solution and the residual is recomputed in FP64 on the
+//    device (reliable update, with the search direction re-orthogonalised against
+//    the new residual).  The stopping test is on that FP64 residual.
+//  * Reductions are deterministic: a fixed grid, per-block partials, and the last
+//    block to arrive sums the partials in block order.  No kernel ever waits on
+//    another: every kernel reads a device flag at entry and returns early once the
+//    solve has finished, so a chunk of iterations captured in a CUDA graph can be
+//    replayed without a host round trip per iteration.
+#include <cmath>
+#include <cstring>
+
+#include "solver.cuh"
+
+namespace adfem {
+
+static constexpr int kT = 256;
+static constexpr int kBlocksPerSM = 8;
+
+__device__ __forceinline__ int64_t gtid() { return (int64_t)blockIdx.x * blockDim.x + threadIdx.x; }
+__device__ __forceinline__ int64_t gstride() { return (int64_t)gridDim.x * blockDim.x; }
+
+template <bool D16>
+__device__ __forceinline__ int64_t colof(const void* c, int64_t idx, int64_t r) {
+  if constexpr (D16) return r + (int64_t)__ldg(reinterpret_cast<const int16_t*>(c) + idx);
+  else return (int64_t)__ldg(reinterpret_cast<const int32_t*>(c) + idx);
+}
+
+template <class T>
+__device__ __forceinline__ T warp_sum(T v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+// Deterministic block sum of NV values; the totals end up in thread 0.
+template <class T, int NV>
+__device__ __forceinline__ void block_sum(T (&v)[NV]) {
+  __shared__ T sh[NV][kT / 32];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+  for (int j = 0; j < NV; j++) v[j] = warp_sum(v[j]);
+  if (lane == 0)
+#pragma unroll
+    for (int j = 0; j < NV; j++) sh[j][wid] = v[j];
+  __syncthreads();
+  if (wid == 0) {
+#pragma unroll
+    for (int j = 0; j < NV; j++) {
+      T x = lane < (kT / 32) ? sh[j][lane] : T(0);
+      v[j] = warp_sum(x);
+    }
+  }
+  __syncthreads();
+}
+
+// Publish this block's partial sums; the last block to arrive sums all partials in
+// block order into tot (valid in thread 0) and returns true (block-uniform).
+template <class T, int NV>
+__device__ __forceinline__ bool reduce_grid(T (&v)[NV], T* partials, unsigned* counter, T (&tot)[NV]) {
+  __shared__ bool last;
+  block_sum<T, NV>(v);
+  if (threadIdx.x == 0) {
+#pragma unroll
+    for (int j = 0; j < NV; j++) partials[j * gridDim.x + blockIdx.x] = v[j];
+    __threadfence();
+    const unsigned prev = atomicAdd(counter, 1u);
+    last = (prev == gridDim.x - 1);
+  }
+  __syncthreads();
+  if (!last) return false;
+  __threadfence();
+  T s[NV];
+#pragma unroll
+  for (int j = 0; j < NV; j++) s[j] = T(0);
+  for (int b = threadIdx.x; b < (int)gridDim.x; b += blockDim.x)
+#pragma unroll
+    for (int j = 0; j < NV; j++) s[j] += __ldcg(partials + j * gridDim.x + b);
+  block_sum<T, NV>(s);
+  if (threadIdx.x == 0) {
+#pragma unroll
+    for (int j = 0; j < NV; j++) tot[j] = s[j];
+    *counter = 0u;
+  }
+  return true;
+}
+
+// ---------------------------------------------------------------------------
+// setup kernels
+__global__ void k_csr_to_sell(int64_t n, const int32_t* __restrict__ sptr, const int32_t* __restrict__ rowptr,
+                              const double* __restrict__ csr, double* __restrict__ sell) {
+  const int64_t r = gtid();
+  if (r >= n) return;
+  const int64_t base = (int64_t)sptr[r >> 5] + (r & 31);
+  for (int32_t k = rowptr[r]; k < rowptr[r + 1]; k++) sell[base + 32 * (int64_t)(k - rowptr[r])] = csr[k];
+}
+
+cudaError_t launch_csr_to_sell(const Sell& A, int64_t n, const int32_t* rowptr, const double* csr, double* sell,
+                               cudaStream_t st) {
+  k_csr_to_sell<<<(unsigned)((n + kT - 1) / kT), kT, 0, st>>>(n, A.sptr.as<int32_t>(), rowptr, csr, sell);
+  return cudaGetLastError();
+}
+
+// s_i = rsqrt(K_ii) in FP32; flags a non-positive or non-finite diagonal
+template <bool D16>
+__global__ void k_scale_diag(int64_t n, const int32_t* __restrict__ sptr, const void* __restrict__ col,
+                             const double* __restrict__ val, const int32_t* __restrict__ diagpos,
+                             float* __restrict__ s, int* __restrict__ bad) {
+  const int64_t r = gtid();
+  if (r >= n) return;
+  const int64_t base = (int64_t)sptr[r >> 5] + (r & 31);
+  const int w = (sptr[(r >> 5) + 1] - sptr[r >> 5]) >> 5;
+  double d = 0.0;
+  if (diagpos) {
+    d = val[base + 32 * (int64_t)diagpos[r]];
+  } else {
+    for (int k = 0; k < w; k++)
+      if (colof<D16>(col, base + 32 * (int64_t)k, r) == r) d += val[base + 32 * (int64_t)k];
+  }
+  const float df = (float)d;
+  if (!(df > 0.0f) || !isfinite(df)) {
+    atomicExch(bad, 1);
+    s[r] = 1.0f;
+    return;
+  }
+  s[r] = rsqrtf(df);
+}
+
+template <bool D16>
+__global__ void k_scale_values(int64_t n, const int32_t* __restrict__ sptr, const void* __restrict__ col,
+                               double* __restrict__ val, float* __restrict__ val32, const float* __restrict__ s) {
+  const int64_t r = gtid();
+  if (r >= n) return;
+  const int64_t base = (int64_t)sptr[r >> 5] + (r & 31);
+  const int w = (sptr[(r >> 5) + 1] - sptr[r >> 5]) >> 5;
+  const double si = (double)s[r];
+  for (int k = 0; k < w; k++) {
+    const int64_t idx = base + 32 * (int64_t)k;
+    const double v = si * val[idx] * (double)s[colof<D16>(col, idx, r)];
+    val[idx] = v;
+    val32[idx] = (float)v;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// solve set-up: b~ = s * rhs (rows tagged 1 in zero_rows get 0), y0 = u / s or 0,
+// ||b~||^2 and the stopping threshold.
+__global__ void __launch_bounds__(kT) k_init(int64_t n, const double* __restrict__ rhs, const uint8_t* zero_rows,
+                                             const float* __restrict__ s, const double* __restrict__ u0,
+                                             double* __restrict__ b, double* __restrict__ y, CgState* st,
+                                             double* partials, double rtol2) {
+  double acc = 0.0;
+  for (int64_t i = gtid(); i < n; i += gstride()) {
+    const double si = (double)s[i];
+    const double bi = (zero_rows && zero_rows[i] == 1) ? 0.0 : si * rhs[i];
+    b[i] = bi;
+    y[i] = u0 ? u0[i] * (double)(1.0f / s[i]) : 0.0;
+    acc = fma(bi, bi, acc);
+  }
+  double v[1] = {acc}, tot[1];
+  if (reduce_grid<double, 1>(v, partials, &st->counter[0], tot) && threadIdx.x == 0) {
+    st->bnorm2 = tot[0];
+    st->stop2 = rtol2 * tot[0];
+  }
+}
+
+// FP64 residual r = b~ - K~ y.  mode 0: FP64 CG start (p = r, rho = r.r);
+// mode 1: mixed reliable update (r32 = (float) r, re-orthogonalise p, new coefficients);
+// mode 2: final check only (rr64).
+template <bool D16>
+__global__ void __launch_bounds__(kT) k_residual64(int64_t n, const int32_t* __restrict__ sptr,
+                                                   const void* __restrict__ col, const double* __restrict__ val,
+                                                   const double* __restrict__ b, const double* __restrict__ y,
+                                                   double* __restrict__ r64, double* __restrict__ p64,
+                                                   float* __restrict__ r32, const float* __restrict__ pa,
+                                                   const float* __restrict__ pb, CgState* st, double* partials,
+                                                   int mode, int force) {
+  if (!force && st->done != 3) return;
+  const int it = st->iters;
+  const float* plat = (it & 1) ? pb : pa;
+  double a0 = 0.0, a1 = 0.0, a2 = 0.0;
+  for (int64_t r = gtid(); r < n; r += gstride()) {
+    const int64_t base = (int64_t)sptr[r >> 5] + (r & 31);
+    const int w = (sptr[(r >> 5) + 1] - sptr[r >> 5]) >> 5;
+    double s = 0.0;
+    for (int k = 0; k < w; k++) {
+      const int64_t idx = base + 32 * (int64_t)k;
+      s = fma(val[idx], y[colof<D16>(col, idx, r)], s);
+    }
+    const double ri = b[r] - s;
+    a0 = fma(ri, ri, a0);
+    if (mode == 0) {
+      r64[r] = ri;
+      p64[r] = ri;
+    } else if (mode == 1) {
+      const float rf = (float)ri;
+      r32[r] = rf;
+      a1 = fma((double)rf, (double)rf, a1);
+      a2 = fma((double)rf, (double)plat[r], a2);
+    }
+  }
+  double v[3] = {a0, a1, a2}, tot[3];
+  if (reduce_grid<double, 3>(v, partials, &st->counter[1], tot) && threadIdx.x == 0) {
+    const double rr = tot[0];
+    st->rr64 = rr;
+    if (mode == 2) return;
+    if (!isfinite(rr)) {
+      st->done = 2;
+      return;
+    }
+    if (rr <= st->stop2) {
+      st->done = 1;
+      return;
+    }
+    if (st->iters >= st->max_iter) {
+      st->done = 4;
+      return;
+    }
+    if (mode == 0) {
+      st->rho = rr;
+      st->done = 0;
+      return;
+    }
+    const double rn = tot[1];
+    if (st->updates == 0) {
+      st->ar = 1.0;
+      st->ap = 0.0;
+    } else {
+      const double c = tot[2] / rn;
+      const double beta = rn / st->rho;
+      st->ar = 1.0 - beta * c;
+      st->ap = beta;
+    }
+    st->updates += 1;
+    st->rho = rn;
+    st->ru2 = st->delta2 * rn;
+    st->done = 0;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// FP64 CG iteration
+template <bool D16>
+__global__ void __launch_bounds__(kT) k_cg64_spmv(int64_t n, const int32_t* __restrict__ sptr,
+                                                  const void* __restrict__ col, const double* __restrict__ val,
+                                                  const double* __restrict__ p, double* __restrict__ q, CgState* st,
+                                                  double* partials) {
+  if (st->done) return;
+  double acc = 0.0;
+  for (int64_t r = gtid(); r < n; r += gstride()) {
+    const int64_t base = (int64_t)sptr[r >> 5] + (r & 31);
+    const int w = (sptr[(r >> 5) + 1] - sptr[r >> 5]) >> 5;
+    double s = 0.0;
+    for (int k = 0; k < w; k++) {
+      const int64_t idx = base + 32 * (int64_t)k;
+      s = fma(val[idx], p[colof<D16>(col, idx, r)], s);
+    }
+    q[r] = s;
+    acc = fma(p[r], s, acc);
+  }
+  double v[1] = {acc}, tot[1];
+  if (reduce_grid<double, 1>(v, partials, &st->counter[0], tot) && threadIdx.x == 0) {
+    const double pq = tot[0];
+    if (!(pq > 0.0) || !isfinite(pq)) st->done = 2;
+    else st->alpha = st->rho / pq;
+  }
+}
+
+__global__ void __launch_bounds__(kT) k_cg64_update(int64_t n, double* __restrict__ y, double* __restrict__ r,
+                                                    const double* __restrict__ p, const double* __restrict__ q,
+                                                    CgState* st, double* partials) {
+  if (st->done) return;
+  const double a = st->alpha;
+  double acc = 0.0;
+  for (int64_t i = gtid(); i < n; i += gstride()) {
+    y[i] = fma(a, p[i], y[i]);
+    const double ri = fma(-a, q[i], r[i]);
+    r[i] = ri;
+    acc = fma(ri, ri, acc);
+  }
+  double v[1] = {acc}, tot[1];
+  if (reduce_grid<double, 1>(v, partials + gridDim.x, &st->counter[2], tot) && threadIdx.x == 0) {
+    const double rn = tot[0];
+    st->iters += 1;
+    st->rho_new = rn;
+    if (!isfinite(rn)) st->done = 2;
+    else if (rn <= st->stop2) st->done = 1;
+    else if (st->iters >= st->max_iter) st->done = 4;
+    else {
+      st->beta = rn / st->rho;
+      st->rho = rn;
+    }
+  }
+}
+
+__global__ void __launch_bounds__(kT) k_cg64_p(int64_t n, const double* __restrict__ r, double* __restrict__ p,
+                                               const CgState* st) {
+  if (st->done) return;
+  const double bt = st->beta;
+  for (int64_t i = gtid(); i < n; i += gstride()) p[i] = fma(bt, p[i], r[i]);
+}
+
+// ---------------------------------------------------------------------------
+// FP32 inner iteration of the mixed solve.  The two p buffers alternate: the
+// iteration with counter it reads p_old = P[it&1] and writes p_new = P[(it+1)&1],
+// P = {pa, pb}.
+template <bool D16>
+__global__ void __launch_bounds__(kT) k_cg32_spmv(int64_t n, const int32_t* __restrict__ sptr,
+                                                  const void* __restrict__ col, const float* __restrict__ val,
+                                                  const float* __restrict__ r, float* pa, float* pb,
+                                                  float* __restrict__ q, CgState* st, float* partials) {
+  if (st->done) return;
+  const int it = st->iters;
+  const float* __restrict__ pold = (it & 1) ? pb : pa;
+  float* __restrict__ pnew = (it & 1) ? pa : pb;
+  const float ar = (float)st->ar, ap = (float)st->ap;
+  float acc = 0.0f;
+  for (int64_t row = gtid(); row < n; row += gstride()) {
+    const int64_t base = (int64_t)sptr[row >> 5] + (row & 31);
+    const int w = (sptr[(row >> 5) + 1] - sptr[row >> 5]) >> 5;
+    float s = 0.0f;
+    for (int k = 0; k < w; k++) {
+      const int64_t idx = base + 32 * (int64_t)k;
+      const int64_t j = colof<D16>(col, idx, row);
+      const float pj = fmaf(ap, pold[j], ar * r[j]);
+      s = fmaf(val[idx], pj, s);
+    }
+    const float pr = fmaf(ap, pold[row], ar * r[row]);
+    pnew[row] = pr;
+    q[row] = s;
+    acc = fmaf(pr, s, acc);
+  }
+  float v[1] = {acc}, tot[1];
+  if (reduce_grid<float, 1>(v, partials, &st->counter[0], tot) && threadIdx.x == 0) {
+    const double pq = (double)tot[0];
+    if (!(pq > 0.0) || !isfinite(pq)) st->done = 2;
+    else st->alpha = st->rho / pq;
+  }
+}
+
+__global__ void __launch_bounds__(kT) k_cg32_update(int64_t n, float* __restrict__ y, float* __restrict__ r,
+                                                    const float* pa, const float* pb, const float* __restrict__ q,
+                                                    CgState* st, float* partials) {
+  if (st->done) return;
+  const int it = st->iters;
+  const float* __restrict__ pnew = (it & 1) ? pa : pb;
+  const float a = (float)st->alpha;
+  float acc = 0.0f;
+  for (int64_t i = gtid(); i < n; i += gstride()) {
+    y[i] = fmaf(a, pnew[i], y[i]);
+    const float ri = fmaf(-a, q[i], r[i]);
+    r[i] = ri;
+    acc = fmaf(ri, ri, acc);
+  }
+  float v[1] = {acc}, tot[1];
+  if (reduce_grid<float, 1>(v, partials + gridDim.x, &st->counter[2], tot) && threadIdx.x == 0) {
+    const double rn = (double)tot[0];
+    st->iters = it + 1;
+    st->rho_new = rn;
+    if (!isfinite(rn)) st->done = 2;
+    else if (rn <= st->ru2 || rn <= st->stop2) st->done = 3;
+    else if (st->iters >= st->max_iter) st->done = 3;  // final FP64 check decides
+    else {
+      const double beta = rn / st->rho;
+      st->ar = 1.0;
+      st->ap = beta;
+      st->rho = rn;
+    }
+  }
+}
+
+// fold the FP32 iterate into the FP64 solution: y64 += y32, y32 = 0
+__global__ void __launch_bounds__(kT) k_fold(int64_t n, double* __restrict__ y64, float* __restrict__ y32,
+                                             const CgState* st, int force) {
+  if (!force && st->done != 3) return;
+  for (int64_t i = gtid(); i < n; i += gstride()) {
+    y64[i] += (double)y32[i];
+    y32[i] = 0.0f;
+  }
+}
+
+__global__ void k_unscale(int64_t n, const double* __restrict__ y, const float* __restrict__ s,
+                          double* __restrict__ u) {
+  const int64_t i = gtid();
+  if (i < n) u[i] = (double)s[i] * y[i];
+}
+
+// y = K x = S^-1 K~ S^-1 x
+template <bool D16>
+__global__ void k_apply(int64_t n, const int32_t* __restrict__ sptr, const void* __restrict__ col,
+                        const double* __restrict__ val, const float* __restrict__ s, const double* __restrict__ x,
+                        double* __restrict__ y) {
+  const int64_t r = gtid();
+  if (r >= n) return;
+  const int64_t base = (int64_t)sptr[r >> 5] + (r & 31);
+  const int w = (sptr[(r >> 5) + 1] - sptr[r >> 5]) >> 5;
+  double acc = 0.0;
+  for (int k = 0; k < w; k++) {
+    const int64_t idx = base + 32 * (int64_t)k;
+    const int64_t j = colof<D16>(col, idx, r);
+    acc = fma(val[idx], x[j] / (double)s[j], acc);
+  }
+  y[r] = acc / (double)s[r];
+}
+
+// ---------------------------------------------------------------------------
+Solver::~Solver() {
+  if (g64) cudaGraphExecDestroy(g64);
+  if (g32) cudaGraphExecDestroy(g32);
+  for (auto& e : ev)
+    if (e) cudaEventDestroy(e);
+  for (auto& e : pev) cudaEventDestroy(e);
+  if (stream) cudaStreamDestroy(stream);
+  if (h_state) cudaFreeHost(h_state);
+}
+
+int Solver::init(const Sell* A_, int64_t n_) {
+  A = A_;
+  n = n_;
+  int dev = 0, sms = 0;
+  ADFEM_CUDA(cudaGetDevice(&dev));
+  ADFEM_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+  const int64_t need = (n + kT - 1) / kT;
+  grid = (int)std::max<int64_t>(1, std::min<int64_t>(need, (int64_t)sms * kBlocksPerSM));
+  ADFEM_TRY(state.alloc(sizeof(CgState)));
+  ADFEM_CUDA(cudaMemset(state.p, 0, sizeof(CgState)));
+  ADFEM_TRY(partials.alloc(sizeof(double) * 4 * (size_t)grid));
+  const size_t n8 = sizeof(double) * (size_t)n, n4 = sizeof(float) * (size_t)n;
+  ADFEM_TRY(s32.alloc(n4));
+  ADFEM_TRY(b.alloc(n8));
+  ADFEM_TRY(y64.alloc(n8));
+  ADFEM_TRY(r64.alloc(n8));
+  ADFEM_TRY(p64.alloc(n8));
+  ADFEM_TRY(q64.alloc(n8));
+  ADFEM_TRY(y32.alloc(n4));
+  ADFEM_TRY(r32.alloc(n4));
+  ADFEM_TRY(pa32.alloc(n4));
+  ADFEM_TRY(pb32.alloc(n4));
+  ADFEM_TRY(q32.alloc(n4));
+  if (!h_state) ADFEM_CUDA(cudaMallocHost(&h_state, 2 * sizeof(CgState)));
+  if (!stream) ADFEM_CUDA(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
+  for (auto& e : ev)
+    if (!e) ADFEM_CUDA(cudaEventCreate(&e));
+  return ADFEM_OK;
+}
+
+int solver_prepare(Solver& S, const int32_t* diagpos_dev, cudaStream_t user) {
+  const Sell& A = *S.A;
+  S.prepared = false;
+  DevBuf bad;
+  ADFEM_TRY(bad.alloc(sizeof(int)));
+  ADFEM_CUDA(cudaMemsetAsync(bad.p, 0, sizeof(int), user));
+  const unsigned nb = (unsigned)((S.n + kT - 1) / kT);
+  if (A.delta16) {
+    k_scale_diag<true><<<nb, kT, 0, user>>>(S.n, A.sptr.as<int32_t>(), A.col.p, A.val64.as<double>(), diagpos_dev,
+                                            S.s32.as<float>(), bad.as<int>());
+    k_scale_values<true><<<nb, kT, 0, user>>>(S.n, A.sptr.as<int32_t>(), A.col.p, A.val64.as<double>(),
+                                              A.val32.as<float>(), S.s32.as<float>());
+  } else {
+    k_scale_diag<false><<<nb, kT, 0, user>>>(S.n, A.sptr.as<int32_t>(), A.col.p, A.val64.as<double>(), diagpos_dev,
+                                             S.s32.as<float>(), bad.as<int>());
+    k_scale_values<false><<<nb, kT, 0, user>>>(S.n, A.sptr.as<int32_t>(), A.col.p, A.val64.as<double>(),
+                                               A.val32.as<float>(), S.s32.as<float>());
+  }
+  ADFEM_CUDA(cudaGetLastError());
+  int hbad = 0;
+  ADFEM_CUDA(cudaMemcpyAsync(&hbad, bad.p, sizeof(int), cudaMemcpyDeviceToHost, user));
+  ADFEM_CUDA(cudaStreamSynchronize(user));
+  if (hbad) return fail(ADFEM_ERR_BREAKDOWN, "operator has a non-positive or non-finite diagonal entry");
+  S.prepared = true;
+  return ADFEM_OK;
+}
+
+// Optional per-launch timing: a pair of events around each launch (profiled solves only).
+struct Timer {
+  Solver* S = nullptr;
+  SolveProfile* prof = nullptr;
+  std::vector<std::pair<int, int>> pending;  // (kind, first event index)
+  int next = 0;
+  template <class F>
+  void run(int kind, cudaStream_t st, F&& launch) {
+    if (!prof) {
+      launch();
+      return;
+    }
+    if (next + 2 > (int)S->pev.size()) {
+      for (int i = 0; i < 64; i++) {
+        cudaEvent_t e;
+        cudaEventCreate(&e);
+        S->pev.push_back(e);
+      }
+    }
+    cudaEventRecord(S->pev[next], st);
+    launch();
+    cudaEventRecord(S->pev[next + 1], st);
+    pending.push_back({kind, next});
+    next += 2;
+  }
+  // after a stream sync: add the measured durations, recycle the events
+  void collect() {
+    for (auto& pk : pending) {
+      float ms = 0.0f;
+      cudaEventElapsedTime(&ms, S->pev[pk.second], S->pev[pk.second + 1]);
+      prof->ms[pk.first] += ms;
+      prof->n[pk.first] += 1;
+    }
+    pending.clear();
+    next = 0;
+  }
+};
+
+// enqueue one FP64 CG iteration
+static void enqueue_cg64(Solver& S, cudaStream_t st, Timer* tm = nullptr) {
+  Timer none;
+  if (!tm) tm = &none;
+  const Sell& A = *S.A;
+  auto* sp = A.sptr.as<int32_t>();
+  auto* cs = S.state.as<CgState>();
+  auto* part = S.partials.as<double>();
+  tm->run(0, st, [&] {
+    if (A.delta16)
+      k_cg64_spmv<true><<<S.grid, kT, 0, st>>>(S.n, sp, A.col.p, A.val64.as<double>(), S.p64.as<double>(),
+                                               S.q64.as<double>(), cs, part);
+    else
+      k_cg64_spmv<false><<<S.grid, kT, 0, st>>>(S.n, sp, A.col.p, A.val64.as<double>(), S.p64.as<double>(),
+                                                S.q64.as<double>(), cs, part);
+  });
+  tm->run(1, st, [&] {
+    k_cg64_update<<<S.grid, kT, 0, st>>>(S.n, S.y64.as<double>(), S.r64.as<double>(), S.p64.as<double>(),
+                                         S.q64.as<double>(), cs, part);
+  });
+  tm->run(2, st, [&] { k_cg64_p<<<S.grid, kT, 0, st>>>(S.n, S.r64.as<double>(), S.p64.as<double>(), cs); });
+}
+
+static void enqueue_residual(Solver& S, cudaStream_t st, int mode, int force, Timer* tm = nullptr) {
+  Timer none;
+  if (!tm) tm = &none;
+  const Sell& A = *S.A;
+  auto* sp = A.sptr.as<int32_t>();
+  tm->run(3, st, [&] {
+  if (A.delta16)
+    k_residual64<true><<<S.grid, kT, 0, st>>>(S.n, sp, A.col.p, A.val64.as<double>(), S.b.as<double>(),
+                                              S.y64.as<double>(), S.r64.as<double>(), S.p64.as<double>(),
+                                              S.r32.as<float>(), S.pa32.as<float>(), S.pb32.as<float>(),
+                                              S.state.as<CgState>(), S.partials.as<double>(), mode, force);
+  else
+    k_residual64<false><<<S.grid, kT, 0, st>>>(S.n, sp, A.col.p, A.val64.as<double>(), S.b.as<double>(),
+                                               S.y64.as<double>(), S.r64.as<double>(), S.p64.as<double>(),
+                                               S.r32.as<float>(), S.pa32.as<float>(), S.pb32.as<float>(),
+                                               S.state.as<CgState>(), S.partials.as<double>(), mode, force);
+  });
+}
+
+static void enqueue_cg32(Solver& S, cudaStream_t st, Timer* tm = nullptr) {
+  Timer none;
+  if (!tm) tm = &none;
+  const Sell& A = *S.A;
+  auto* sp = A.sptr.as<int32_t>();
+  auto* cs = S.state.as<CgState>();
+  auto* part = reinterpret_cast<float*>(S.partials.p);
+  tm->run(0, st, [&] {
+    if (A.delta16)
+      k_cg32_spmv<true><<<S.grid, kT, 0, st>>>(S.n, sp, A.col.p, A.val32.as<float>(), S.r32.as<float>(),
+                                               S.pa32.as<float>(), S.pb32.as<float>(), S.q32.as<float>(), cs, part);
+    else
+      k_cg32_spmv<false><<<S.grid, kT, 0, st>>>(S.n, sp, A.col.p, A.val32.as<float>(), S.r32.as<float>(),
+                                                S.pa32.as<float>(), S.pb32.as<float>(), S.q32.as<float>(), cs, part);
+  });
+  tm->run(1, st, [&] {
+    k_cg32_update<<<S.grid, kT, 0, st>>>(S.n, S.y32.as<float>(), S.r32.as<float>(), S.pa32.as<float>(),
+                                         S.pb32.as<float>(), S.q32.as<float>(), cs, part);
+  });
+}
+
+static void enqueue_reliable_update(Solver& S, cudaStream_t st, int force, Timer* tm = nullptr) {
+  Timer none;
+  if (!tm) tm = &none;
+  tm->run(2, st, [&] {
+    k_fold<<<S.grid, kT, 0, st>>>(S.n, S.y64.as<double>(), S.y32.as<float>(), S.state.as<CgState>(), force);
+  });
+  enqueue_residual(S, st, 1, force, tm);
+}
+
+static int chunk_launches(bool mixed, int chunk) {
+  if (!mixed) return 3 * chunk;
+  int ru = 0;
+  for (int i = 0; i < chunk; i++)
+    if ((i + 1) % 8 == 0 || i + 1 == chunk) ru++;
+  return 2 * chunk + 2 * ru;
+}
+
+// capture `chunk` iterations into a graph (kernels read all scalars from device state)
+static int capture_chunk(Solver& S, bool mixed, int chunk, cudaGraphExec_t* out) {
+  cudaGraph_t g = nullptr;
+  ADFEM_CUDA(cudaStreamBeginCapture(S.stream, cudaStreamCaptureModeThreadLocal));
+  for (int i = 0; i < chunk; i++) {
+    if (mixed) {
+      enqueue_cg32(S, S.stream);
+      if ((i + 1) % 8 == 0 || i + 1 == chunk) enqueue_reliable_update(S, S.stream, 0);
+    } else {
+      enqueue_cg64(S, S.stream);
+    }
+  }
+  cudaError_t e = cudaStreamEndCapture(S.stream, &g);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaStreamEndCapture");
+  e = cudaGraphInstantiate(out, g, 0);
+  cudaGraphDestroy(g);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaGraphInstantiate");
+  return ADFEM_OK;
+}
+
+int solver_solve(Solver& S, const double* rhs, double* u, const uint8_t* zero_rows, const adfem_solver_opts& o,
+                 adfem_solver_stats* stats, cudaStream_t user, SolveProfile* prof) {
+  if (!S.prepared) return fail(ADFEM_ERR_INVALID, "solver: operator not prepared");
+  const bool mixed = o.precision == ADFEM_PREC_MIXED;
+  if (o.precision != ADFEM_PREC_FP64 && !mixed) return fail(ADFEM_ERR_INVALID, "solver: unknown precision");
+  if (!(o.rtol > 0.0) || o.max_iter < 1) return fail(ADFEM_ERR_INVALID, "solver: rtol must be > 0, max_iter >= 1");
+  const int chunk = std::max(1, std::min(o.chunk > 0 ? o.chunk : 32, 512));
+  cudaStream_t st = S.stream;
+  cudaGraphExec_t* gx = mixed ? &S.g32 : &S.g64;
+  int* gc = mixed ? &S.g32_chunk : &S.g64_chunk;
+  if (!prof) {
+    if (*gx && *gc != chunk) {
+      cudaGraphExecDestroy(*gx);
+      *gx = nullptr;
+    }
+    if (!*gx) {
+      ADFEM_TRY(capture_chunk(S, mixed, chunk, gx));
+      *gc = chunk;
+    }
+  }
+  long long launches = 0;
+  ADFEM_CUDA(cudaEventRecord(S.ev[0], user));
+  ADFEM_CUDA(cudaStreamWaitEvent(st, S.ev[0], 0));
+  ADFEM_CUDA(cudaEventRecord(S.ev[1], st));
+
+  CgState init;
+  std::memset(&init, 0, sizeof(init));
+  init.max_iter = o.max_iter;
+  const double dl = (o.ru_delta > 0.0 && o.ru_delta < 1.0) ? o.ru_delta : 0.1;
+  init.delta2 = dl * dl;
+  init.done = 3;  // lets the forced residual kernel run in mixed mode
+  ADFEM_CUDA(cudaMemcpyAsync(S.state.p, &init, sizeof(CgState), cudaMemcpyHostToDevice, st));
+  k_init<<<S.grid, kT, 0, st>>>(S.n, rhs, zero_rows, S.s32.as<float>(), o.warm_start ? u : nullptr,
+                                S.b.as<double>(), S.y64.as<double>(), S.state.as<CgState>(), S.partials.as<double>(),
+                                o.rtol * o.rtol);
+  ADFEM_CUDA(cudaGetLastError());
+  if (mixed) {
+    ADFEM_CUDA(cudaMemsetAsync(S.y32.p, 0, sizeof(float) * S.n, st));
+    ADFEM_CUDA(cudaMemsetAsync(S.pa32.p, 0, sizeof(float) * S.n, st));
+    ADFEM_CUDA(cudaMemsetAsync(S.pb32.p, 0, sizeof(float) * S.n, st));
+    enqueue_residual(S, st, 1, 1);
+  } else {
+    enqueue_residual(S, st, 0, 1);
+  }
+  ADFEM_CUDA(cudaGetLastError());
+  launches += 2;
+
+  CgState cur;
+  if (prof) {
+    // kernel-by-kernel loop with an event pair around every launch
+    Timer tm;
+    tm.S = &S;
+    tm.prof = prof;
+    for (;;) {
+      for (int i = 0; i < chunk; i++) {
+        if (mixed) {
+          enqueue_cg32(S, st, &tm);
+          if ((i + 1) % 8 == 0 || i + 1 == chunk) enqueue_reliable_update(S, st, 0, &tm);
+        } else {
+          enqueue_cg64(S, st, &tm);
+        }
+      }
+      launches += chunk_launches(mixed, chunk);
+      ADFEM_CUDA(cudaGetLastError());
+      ADFEM_CUDA(cudaMemcpyAsync(&S.h_state[0], S.state.p, sizeof(CgState), cudaMemcpyDeviceToHost, st));
+      ADFEM_CUDA(cudaStreamSynchronize(st));
+      tm.collect();
+      cur = S.h_state[0];
+      if (cur.done == 1 || cur.done == 2 || cur.done == 4) break;
+    }
+  } else {
+    // pipelined host loop: keep one chunk in flight beyond the one being checked
+    int slot = 0;
+    ADFEM_CUDA(cudaGraphLaunch(*gx, st));
+    ADFEM_CUDA(cudaMemcpyAsync(&S.h_state[0], S.state.p, sizeof(CgState), cudaMemcpyDeviceToHost, st));
+    ADFEM_CUDA(cudaEventRecord(S.ev[2], st));
+    launches += chunk_launches(mixed, chunk);
+    for (;;) {
+      ADFEM_CUDA(cudaGraphLaunch(*gx, st));
+      launches += chunk_launches(mixed, chunk);
+      ADFEM_CUDA(cudaMemcpyAsync(&S.h_state[1 - slot], S.state.p, sizeof(CgState), cudaMemcpyDeviceToHost, st));
+      ADFEM_CUDA(cudaEventRecord(S.ev[2 + (1 - slot)], st));
+      ADFEM_CUDA(cudaEventSynchronize(S.ev[2 + slot]));
+      cur = S.h_state[slot];
+      if (cur.done == 1 || cur.done == 2 || cur.done == 4) break;
+      slot = 1 - slot;
+    }
+  }
+  // final FP64 residual (the mixed path's stop test already is one; recompute for both)
+  if (mixed) k_fold<<<S.grid, kT, 0, st>>>(S.n, S.y64.as<double>(), S.y32.as<float>(), S.state.as<CgState>(), 1);
+  enqueue_residual(S, st, 2, 1);
+  k_unscale<<<(unsigned)((S.n + kT - 1) / kT), kT, 0, st>>>(S.n, S.y64.as<double>(), S.s32.as<float>(), u);
+  ADFEM_CUDA(cudaGetLastError());
+  launches += mixed ? 3 : 2;
+  ADFEM_CUDA(cudaMemcpyAsync(&S.h_state[0], S.state.p, sizeof(CgState), cudaMemcpyDeviceToHost, st));
+  ADFEM_CUDA(cudaEventRecord(S.ev[3], st));
+  ADFEM_CUDA(cudaEventSynchronize(S.ev[3]));
+  CgState fin = S.h_state[0];
+  ADFEM_CUDA(cudaStreamWaitEvent(user, S.ev[3], 0));
+  float ms = 0.0f;
+  cudaEventElapsedTime(&ms, S.ev[1], S.ev[3]);
+  int status = ADFEM_OK;
+  if (cur.done == 2) status = ADFEM_ERR_BREAKDOWN;
+  else if (cur.done == 4) status = ADFEM_ERR_NOT_CONVERGED;
+  const double relres = fin.bnorm2 > 0.0 ? std::sqrt(fin.rr64 / fin.bnorm2) : 0.0;
+  if (stats) {
+    stats->iterations = fin.iters;
+    stats->updates = fin.updates;
+    stats->relres = relres;
+    stats->ms = ms;
+    stats->status = status;
+    stats->launches = launches;
+  }
+  if (status == ADFEM_ERR_BREAKDOWN) return fail(status, "CG breakdown: p.Ap <= 0 or non-finite (operator not SPD?)");
+  if (status == ADFEM_ERR_NOT_CONVERGED)
+    return fail(status, "CG did not reach rtol within max_iter (relres " + std::to_string(relres) + ")");
+  return ADFEM_OK;
+}
+
+int solver_apply(Solver& S, const double* x, double* y, cudaStream_t user) {
+  const Sell& A = *S.A;
+  const unsigned nb = (unsigned)((S.n + kT - 1) / kT);
+  if (A.delta16)
+    k_apply<true><<<nb, kT, 0, user>>>(S.n, A.sptr.as<int32_t>(), A.col.p, A.val64.as<double>(), S.s32.as<float>(), x,
+                                       y);
+  else
+    k_apply<false><<<nb, kT, 0, user>>>(S.n, A.sptr.as<int32_t>(), A.col.p, A.val64.as<double>(), S.s32.as<float>(),
+                                        x, y);
+  ADFEM_CUDA(cudaGetLastError());
+  return ADFEM_OK;
+}
+
+}  // namespace adfem

@@ -1,0 +1,69 @@
+// Solver internals shared by solver.cu and capi.cpp.
+#pragma once
+#include "adfem_internal.h"
+
+namespace adfem {
+
+// Device-resident CG scalars.  Written only by the last block of a reduction
+// kernel (or by single-thread kernels), read by every kernel of the next step.
+struct CgState {
+  double rho;          // current (recursive) r.r
+  double rho_new;      // r.r computed by the last update step
+  double alpha, beta;  // CG coefficients
+  double ar, ap;       // mixed: p_new = ar*r + ap*p_old
+  double bnorm2;       // ||b~||^2
+  double stop2;        // stop when ||r||^2 <= stop2 (= rtol^2 ||b~||^2)
+  double ru2;          // mixed: replace the residual when rho_new <= ru2
+  double delta2;       // mixed: reliable-update factor squared
+  double rr64;         // last FP64 true-residual norm^2 (mixed) / final check
+  int iters;           // inner iterations done
+  int max_iter;
+  int done;            // 0 running, 1 converged, 2 breakdown, 3 residual replacement due, 4 max_iter
+  int updates;         // residual replacements done (mixed)
+  unsigned counter[4]; // last-block arrival counters (returned to 0 by the last block)
+};
+
+struct Solver {
+  int64_t n = 0;
+  int grid = 0;            // blocks of the reduction kernels (grid-stride)
+  const Sell* A = nullptr; // sliced-ELL operator (val64 scaled in place, val32 scaled copy)
+  DevBuf s32;              // Jacobi scaling s_i = 1/sqrt(K_ii) (float, exact in double)
+  DevBuf state;            // CgState
+  DevBuf partials;         // 4 * grid doubles
+  DevBuf b;                // scaled rhs (FP64)
+  DevBuf y64, r64, p64, q64;
+  DevBuf y32, r32, pa32, pb32, q32;
+  CgState* h_state = nullptr;  // pinned, 2 slots
+  cudaStream_t stream = nullptr;
+  cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+  cudaGraphExec_t g64 = nullptr, g32 = nullptr;
+  std::vector<cudaEvent_t> pev;  // event pool of profiled solves
+  int g64_chunk = 0, g32_chunk = 0;
+  bool prepared = false;
+  ~Solver();
+  int init(const Sell* A, int64_t n);
+};
+
+// scale the operator: s_i = rsqrt(K_ii) (FP32), val64 <- s_i K_ij s_j, val32 <- (float) val64.
+// diagpos: entry index k of the diagonal within row i (null: search by column).
+int solver_prepare(Solver& S, const int32_t* diagpos_dev, cudaStream_t user);
+// Per-kernel timing of a profiled solve: 0 SpMV+dot, 1 update+dot, 2 p update / fold,
+// 3 FP64 residual.
+struct SolveProfile {
+  double ms[4] = {0, 0, 0, 0};
+  long long n[4] = {0, 0, 0, 0};
+};
+// Solve K u = rhs (rhs, u unscaled, device).  zero_rows (optional, uint8 tags == 1): rows
+// whose rhs is replaced by 0 (adjoint solves).  With prof != null every kernel is launched
+// on its own between two CUDA events (no graph) and timed.
+int solver_solve(Solver& S, const double* rhs, double* u, const uint8_t* zero_rows, const adfem_solver_opts& o,
+                 adfem_solver_stats* stats, cudaStream_t user, SolveProfile* prof = nullptr);
+// y = K x with the unscaled operator (via the scaled copy)
+int solver_apply(Solver& S, const double* x, double* y, cudaStream_t user);
+
+// Fill sliced-ELL values from CSR values (same pattern).
+cudaError_t launch_csr_to_sell(const Sell& A, int64_t n, const int32_t* rowptr, const double* csr, double* sell,
+                               cudaStream_t st);
+int sell_build_pattern(int64_t n, const int32_t* rowptr, const int32_t* colind, Sell& s);
+
+}  // namespace adfem

@@ -1,0 +1,467 @@
+#!/usr/bin/env python
+"""Benchmark: Poisson forward (+adjoint) of AdFem's P1 path at 4M DOF on GB300.
+
+Workload (one "step"): the 2000x2000-cell jittered unit square (8M triangles,
+4,004,001 DOF), kappa = 1 + exp(sigma G) with G a 64-mode random Fourier field
+(seed 1) and sigma set so max/min kappa = 1e3, f = 1e5 (x + y), u = 0 on the
+boundary.  A step assembles the Laplace matrix and load vector, imposes the
+Dirichlet condition (one fused pass) and solves with the mixed-precision
+Jacobi-CG (FP32 inner iteration, FP64 residual replacement and stop test) to
+the residual tolerance that gives <= 1e-10 relative error against the FP64
+reference solution.  Inputs are resident in HBM; the working set (about 700 MB
+of matrix and vectors) is larger than L2 (129 MB), so no flush is needed.
+
+Printed: one JSON line (rank 0) with value = solves/s over all ranks, the
+FP64-CG comparison, grads/s, roofline of the dominant kernel, the end-to-end
+rate through the host-buffer C ABI call, the CPU baseline and SM clocks.
+``--impl reference`` times the CPU restatement of the reference path instead.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(ROOT, "adfem.jl_gb300"))
+sys.path.insert(0, os.path.join(ROOT, "oracle"))
+
+METRIC = "solves/s & grads/s at 4M DOF, mixed vs FP64 @1e-10; serve p50/p99 ms"
+UNIT = "solves/s"
+# FP64 Jacobi-CG iterations this workload needs at the default rtol on GB300; the
+# reference arm scales its per-iteration CPU time by this count.
+FP64_ITERS_DEFAULT = 9000
+
+
+def peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return float(d.get("hbm_gbs", 6800.0)), "measured"
+    return 6800.0, "fallback"
+
+
+# ----------------------------------------------------------------------------- clocks
+class ClockSampler:
+    """nvidia-smi sampling of SM clock and throttle reasons during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index=0):
+        self.index = index
+        self.rows = []
+        self.proc = None
+        self.th = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.Q,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except Exception:
+            self.proc = None
+            return
+        self.th = threading.Thread(target=self._read, daemon=True)
+        self.th.start()
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.rows.append([x.strip() for x in line.split(",")])
+
+    def stop(self):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+        if self.th is not None:
+            self.th.join(timeout=2)
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in self.rows:
+            try:
+                sm.append(float(r[1]))
+                mx = float(r[2])
+                for nm, v in zip(names, r[5:9]):
+                    if v.lower().startswith("active"):
+                        reasons.add(nm)
+            except (ValueError, IndexError):
+                pass
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+# ----------------------------------------------------------------------------- workload
+def make_workload(m, seed_mesh=0, seed_field=1, contrast=1e3):
+    """Mesh, Gauss points and the C3 fields (kappa on the device)."""
+    import torch
+
+    import adfem_gpu as A
+    from adfem_gpu import synth
+
+    coords, elems = synth.jittered_square(m, seed=seed_mesh)
+    mesh = A.Mesh(coords, elems)
+    g = A.gauss_nodes(mesh)
+    gx = torch.tensor(g[:, 0], device="cuda")
+    gy = torch.tensor(g[:, 1], device="cuda")
+    G = synth.fourier_field(gx, gy, seed=seed_field)
+    sigma = synth.contrast_sigma(G.cpu().numpy(), contrast)
+    kappa = synth.lognormal_kappa(G, sigma).contiguous()
+    f = (1e5 * (gx + gy)).contiguous()
+    bd = A.bcnode(mesh)
+    return mesh, coords, elems, kappa, f, bd, sigma
+
+
+def spmv32_bytes(mesh_nent, n, nslices):
+    # values (4 B) + int16 column deltas (2 B) per stored entry, slice pointers,
+    # r and p_old gathered once, p_new and q written
+    return 6 * mesh_nent + 4 * (nslices + 1) + 16 * n
+
+
+def spmv64_bytes(mesh_nent, n, nslices):
+    return 10 * mesh_nent + 4 * (nslices + 1) + 16 * n
+
+
+def sell_entries(mesh):
+    """Stored entries (incl. padding) of the sliced-ELL operator of the mesh's scalar pattern."""
+    cp, rv = mesh.pattern()
+    lens = np.diff(cp)
+    n = lens.size
+    ns = (n + 31) // 32
+    pad = np.zeros(ns * 32, np.int64)
+    pad[:n] = lens
+    w = pad.reshape(ns, 32).max(axis=1)
+    return int(32 * w.sum()), n, ns
+
+
+# ----------------------------------------------------------------------------- CPU leg
+def cpu_sample(mesh_m, threads, pcg_iters, Bcsr=None, fp64_iters=FP64_ITERS_DEFAULT, asm_m=500):
+    """Bounded CPU sample of the oracle restatement of the reference path.
+
+    (a) serial oracle assembly (unsummed COO -> Julia-sparse CSC -> load -> Dirichlet) on an
+        asm_m x asm_m sub-mesh, scaled to the full mesh by element count;
+    (b) pcg_iters Jacobi-PCG iterations (oracle, `threads` pthreads) on the full-size
+        Dirichlet-imposed operator Bcsr, scaled to fp64_iters iterations.
+    Returns (solves/s, details)."""
+    import oracle as O
+
+    from adfem_gpu import synth
+
+    O.build()
+    coords, elems = synth.jittered_square(asm_m, seed=0)
+    t0 = time.perf_counter()
+    M = O.OracleMesh(coords, elems)
+    g = M.gauss_nodes()
+    kap = 1 + np.exp(0.5 * synth.fourier_field(g[:, 0], g[:, 1], seed=1))
+    K = M.laplace_csc(kap)
+    F = M.source(1e5 * (g[:, 0] + g[:, 1]))
+    bd = M.bcnode()
+    O.dirichlet_csc(K, F, bd, np.zeros(bd.size))
+    t_asm = (time.perf_counter() - t0) * (mesh_m / asm_m) ** 2
+    n = Bcsr.shape[0]
+    b = np.ones(n)
+    t0 = time.perf_counter()
+    O.pcg(Bcsr, b, rtol=0.0, max_iter=pcg_iters, threads=threads)
+    t_it = (time.perf_counter() - t0) / pcg_iters
+    t_solve = t_asm + fp64_iters * t_it
+    return 1.0 / t_solve, {"t_assembly_s": t_asm, "t_iter_s": t_it, "iters": fp64_iters}
+
+
+def cpu_operator_from_oracle(m, chunks=8):
+    """Full-size Dirichlet-imposed operator built by the oracle (chunked COO -> CSR)."""
+    import scipy.sparse as sp
+
+    import oracle as O
+
+    from adfem_gpu import synth
+
+    coords, elems = synth.jittered_square(m, seed=0)
+    n = coords.shape[0]
+    K = None
+    ne = elems.shape[0]
+    for c in range(chunks):
+        sub = elems[ne * c // chunks: ne * (c + 1) // chunks]
+        M = O.OracleMesh(coords, sub)
+        idx, vv = M.laplace_coo(np.ones(M.ngauss))
+        Kc = sp.coo_matrix((vv, (idx[:, 0], idx[:, 1])), shape=(n, n)).tocsr()
+        K = Kc if K is None else K + Kc
+    bmask = np.zeros(n, bool)
+    x, y = coords[:, 0], coords[:, 1]
+    bmask[(x == 0) | (x == 1) | (y == 0) | (y == 1)] = True
+    keep = ~bmask
+    D = sp.diags(keep.astype(float))
+    B = (D @ K @ D + sp.diags(bmask.astype(float))).tocsr()
+    B.sort_indices()
+    return B
+
+
+# ----------------------------------------------------------------------------- reference arm
+def run_reference(args, rank, world):
+    if rank != 0:
+        return 0
+    threads = os.cpu_count() or 1
+    B = cpu_operator_from_oracle(args.m)
+    vals = []
+    for i in range(args.warmup + args.steps):
+        v, det = cpu_sample(args.m, threads, args.ref_iters, B, args.fp64_iters)
+        if i >= args.warmup:
+            vals.append(v)
+    v = statistics.median(vals)
+    sample = ("serial oracle assembly (COO -> Julia-sparse CSC -> load -> Dirichlet) timed on the 500x500 "
+              "sub-mesh and scaled x%d by element count, plus %d Jacobi-PCG iterations on the full %d-DOF "
+              "operator with %d threads scaled to %d iterations" %
+              ((args.m // 500) ** 2, args.ref_iters, B.shape[0], threads, args.fp64_iters))
+    line = {"metric": METRIC, "value": v, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1000.0 / v, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": "poisson-2000x2000-jittered-4M-dof-contrast1e3", "m": args.m,
+                       "parallelism": "replicas"},
+            "impl": "reference",
+            "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},
+            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+# ----------------------------------------------------------------------------- our arm
+def run_ours(args, rank, world, dist):
+    import torch
+
+    import adfem_gpu as A
+
+    torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+    mesh, coords, elems, kappa, f, bd, sigma = make_workload(args.m)
+    n = mesh.ndof
+    S = A.PoissonSystem(mesh)
+    S.set_dirichlet(bd)
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    # FP64 reference solution (untimed): the error bar of both solves is measured against it
+    S.assemble(kappa, f)
+    u_ref = S.solve(precision="fp64", rtol=args.ref_rtol)
+    ref_stats = S.last_stats
+
+    def step(prec, u):
+        S.assemble(kappa, f)
+        S.solve(u, precision=prec, rtol=args.rtol)
+        return S.last_stats
+
+    u = torch.zeros(n, dtype=torch.float64, device="cuda")
+    # ------------------------------------------------------------------ mixed (headline)
+    for _ in range(args.warmup):
+        step("mixed", u)
+    barrier()
+    clk = ClockSampler(int(os.environ.get("LOCAL_RANK", "0")))
+    clk.start()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    launches = 0
+    mixed_stats = []
+    for _ in range(args.steps):
+        st = step("mixed", u)
+        mixed_stats.append((st.iterations, st.updates, st.relres))
+        launches += st.launches + 4  # + prepass, system, scale_diag, scale_values
+    e1.record()
+    barrier()
+    clocks = clk.stop()
+    ms = e0.elapsed_time(e1)
+    if dist is not None:
+        t = torch.tensor([ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    err_mixed = float((u - u_ref).abs().max() / u_ref.abs().max())
+    value = world * args.steps / (ms / 1000.0)
+
+    # ------------------------------------------------------------------ FP64 CG comparison
+    u64 = torch.zeros_like(u)
+    for _ in range(max(1, args.warmup // 2)):
+        step("fp64", u64)
+    barrier()
+    f0, f1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    f0.record()
+    fp64_stats = []
+    for _ in range(args.fp64_steps):
+        st = step("fp64", u64)
+        fp64_stats.append((st.iterations, st.relres))
+    f1.record()
+    barrier()
+    ms64 = f0.elapsed_time(f1)
+    err_fp64 = float((u64 - u_ref).abs().max() / u_ref.abs().max())
+    fp64_value = world * args.fp64_steps / (ms64 / 1000.0)
+
+    # ------------------------------------------------------------------ grads/s (mixed)
+    from adfem_gpu import synth
+
+    obs = torch.tensor(synth.observation_nodes(n, seed=3), device="cuda")
+    uobs = u_ref[obs] + 1e-3 * torch.randn(obs.numel(), dtype=torch.float64, device="cuda",
+                                           generator=torch.Generator(device="cuda").manual_seed(4))
+    g0, g1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    barrier()
+    g0.record()
+    for _ in range(args.grad_steps):
+        S.assemble(kappa, f)
+        S.solve(u, precision="mixed", rtol=args.rtol)
+        gu = torch.zeros_like(u)
+        gu[obs] = 2 * (u[obs] - uobs)
+        lam = S.adjoint(gu, precision="mixed", rtol=args.rtol)
+        gk = S.grad_kappa(u, lam)
+    g1.record()
+    barrier()
+    grads_value = world * args.grad_steps / (g0.elapsed_time(g1) / 1000.0)
+
+    # ------------------------------------------------------------------ roofline (profiled solve)
+    import ctypes
+
+    from adfem_gpu import _lib
+
+    S.assemble(kappa, f)
+    kms = (ctypes.c_double * 4)()
+    kn = (ctypes.c_longlong * 4)()
+    o = A.solver_opts("mixed", args.rtol)
+    pst = _lib.SolverStats()
+    up = torch.zeros_like(u)
+    _lib.check(_lib.load().adfem_system_solve_profiled_d(S.handle, _lib.ptr(up), ctypes.byref(o), ctypes.byref(pst),
+                                                         kms, kn, _lib.stream_ptr(torch.cuda.current_stream())))
+    nent, nrow, nsl = sell_entries(mesh)
+    spmv_ms = kms[0] / max(kn[0], 1)
+    upd_ms = kms[1] / max(kn[1], 1)
+    hbm, peak_kind = peaks()
+    b32 = spmv32_bytes(nent, nrow, nsl)
+    achieved = b32 / (spmv_ms * 1e-3) / 1e9
+    # assembly pass timing (prepass + fused system kernel + scaling), for the record
+    a0, a1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    a0.record()
+    for _ in range(3):
+        S.assemble(kappa, f)
+    a1.record()
+    torch.cuda.synchronize()
+    asm_ms = a0.elapsed_time(a1) / 3
+
+    # ------------------------------------------------------------------ e2e through host buffers
+    kh = kappa.cpu().pin_memory()
+    fh = f.cpu().pin_memory()
+    uh = torch.zeros(n, dtype=torch.float64).pin_memory()
+    import numpy as _np
+
+    kn_ = kh.numpy()
+    fn_ = fh.numpy()
+    S.solve_host(kn_, fn_, precision="mixed", rtol=args.rtol)
+    barrier()
+    t0 = time.perf_counter()
+    o = A.solver_opts("mixed", args.rtol)
+    est = _lib.SolverStats()
+    for _ in range(args.steps):
+        _lib.check(_lib.load().adfem_poisson_solve(S.handle, _lib.ptr(kh), _lib.ptr(fh), _lib.ptr(uh),
+                                                   ctypes.byref(o), ctypes.byref(est)))
+    barrier()
+    e2e_s = time.perf_counter() - t0
+    if dist is not None:
+        t = torch.tensor([e2e_s], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_s = float(t.item())
+    e2e_value = world * args.steps / e2e_s
+    err_e2e = float(_np.max(_np.abs(uh.numpy() - u_ref.cpu().numpy())) / float(u_ref.abs().max()))
+
+    # ------------------------------------------------------------------ CPU baseline (rank 0, N=1)
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu:
+        import scipy.sparse as sp
+
+        K = A.compute_fem_laplace_matrix1(kappa.cpu().numpy(), mesh)
+        B, _ = A.impose_Dirichlet_boundary_conditions(K, _np.zeros(n), bd, _np.zeros(bd.size))
+        Bcsr = sp.csr_matrix(B)
+        fp64_iters = int(round(statistics.median([s[0] for s in fp64_stats])))
+        cv, det = cpu_sample(args.m, 1, args.cpu_iters, Bcsr, fp64_iters)
+        cpu = {"value": cv, "unit": UNIT, "cores": 1, "kind": "port",
+               "sample": "serial oracle assembly on the 500x500 sub-mesh scaled x%d by element count + %d "
+                         "single-thread oracle Jacobi-PCG iterations on the full %d-DOF operator scaled to the "
+                         "%d FP64 iterations of this run" % ((args.m // 500) ** 2, args.cpu_iters, n, fp64_iters),
+               "detail": det}
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic",
+            "config": {"workload": "poisson-2000x2000-jittered-4M-dof-contrast1e3", "m": args.m, "dof": n,
+                       "nnz": int(mesh.pattern()[1].size), "rtol": args.rtol, "precision": "mixed",
+                       "parallelism": "replicas" if world > 1 else "single",
+                       "l2": "working set > L2 (no flush needed)", "kappa_sigma": sigma},
+            "mixed": {"solves_per_s": value, "iters": [s[0] for s in mixed_stats],
+                      "fp64_residual_evals": [s[1] for s in mixed_stats], "relres": mixed_stats[-1][2],
+                      "rel_err_vs_fp64_ref": err_mixed},
+            "fp64": {"solves_per_s": fp64_value, "iters": [s[0] for s in fp64_stats], "rel_err_vs_fp64_ref": err_fp64,
+                     "speedup_mixed_over_fp64": value / fp64_value},
+            "grads_per_s": grads_value,
+            "fp64_reference": {"rtol": args.ref_rtol, "iters": ref_stats.iterations, "relres": ref_stats.relres},
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
+                         "traffic": None, "kernel": "k_cg32_spmv", "bytes_per_launch": b32,
+                         "avg_launch_ms": spmv_ms, "launches": int(kn[0]), "peak_kind": peak_kind,
+                         "other_kernels_avg_ms": {"k_cg32_update": upd_ms,
+                                                  "k_fold": kms[2] / max(kn[2], 1),
+                                                  "k_residual64": kms[3] / max(kn[3], 1)},
+                         "assembly_ms": asm_ms},
+            "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 2 * 8 * int(kappa.numel()),
+                    "d2h_bytes_per_step": 8 * n, "rel_err_vs_fp64_ref": err_e2e},
+            "gpu_launches": launches,
+            "clocks": clocks,
+            "cpu_baseline": cpu,
+        }
+        print(json.dumps(line), flush=True)
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--m", type=int, default=2000)
+    ap.add_argument("--rtol", type=float, default=1e-11)
+    ap.add_argument("--ref-rtol", type=float, default=1e-14)
+    ap.add_argument("--fp64-steps", type=int, default=2)
+    ap.add_argument("--grad-steps", type=int, default=2)
+    ap.add_argument("--cpu-iters", type=int, default=5)
+    ap.add_argument("--ref-iters", type=int, default=10)
+    ap.add_argument("--fp64-iters", type=int, default=FP64_ITERS_DEFAULT)
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    dist = None
+    if args.impl == "reference":
+        return run_reference(args, rank, world)
+    if world > 1:
+        import torch
+        import torch.distributed as td
+
+        torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+        td.init_process_group("nccl")
+        dist = td
+    r = run_ours(args, rank, world, dist)
+    if dist is not None:
+        dist.destroy_process_group()
+    return r
+
+
+if __name__ == "__main__":
+    sys.exit(main())

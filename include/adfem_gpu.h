@@ -1,0 +1,291 @@
+/*
+ * adfem_gpu.h -- C ABI of libadfem_gpu.so, a GB300 (sm_103a) implementation of
+ * AdFem.jl's P1-triangle forward and adjoint path:
+ *   compute_fem_laplace_matrix1, compute_fem_source_term1,
+ *   compute_fem_stiffness_matrix, impose_Dirichlet_boundary_conditions, K\F.
+ *
+ * Two layers:
+ *   1. The symbols AdFem's Julia code already ccalls from libadmfem
+ *      (src/MFEM/MFEM.jl, src/MFEM/MCore.jl), with the same names, argument
+ *      order, 0/1-based conventions and "current mesh" global state, so that
+ *      AdFem's LIBMFEM constant can point at this library unchanged.  They
+ *      return void like the originals; a failure is recorded and can be read
+ *      with adfem_last_error().
+ *   2. New entry points (prefix adfem_) returning an int status, with explicit
+ *      mesh handles, explicit lengths, caller-owned buffers and, for the
+ *      "_d" variants, device pointers plus a CUDA stream (passed as void*).
+ *
+ * All pointers are plain host or device pointers; no framework types appear.
+ * Indices: long long = int64 (Julia Int64), int = int32.
+ */
+#ifndef ADFEM_GPU_H
+#define ADFEM_GPU_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#if defined(__GNUC__)
+#define ADFEM_API __attribute__((visibility("default")))
+#else
+#define ADFEM_API
+#endif
+
+/* ---------------------------------------------------------------- status */
+enum {
+  ADFEM_OK = 0,
+  ADFEM_ERR_INVALID = 1,       /* bad argument: size, index out of range, duplicate ... */
+  ADFEM_ERR_CUDA = 2,          /* a CUDA call failed (message has the CUDA error string) */
+  ADFEM_ERR_NOMEM = 3,         /* device or host allocation failed */
+  ADFEM_ERR_NOT_CONVERGED = 4, /* iterative solve hit max_iter before rtol */
+  ADFEM_ERR_BREAKDOWN = 5,     /* CG breakdown: p.Ap <= 0 or non-finite (matrix not SPD) */
+  ADFEM_ERR_NO_MESH = 6,       /* legacy call without a current mesh */
+  ADFEM_ERR_NONFINITE = 7,     /* NaN/Inf found in an input field */
+  ADFEM_ERR_UNSUPPORTED = 8,   /* valid request outside what this build implements */
+  ADFEM_ERR_BUSY = 9,          /* server: request does not fit the HBM budget now */
+  ADFEM_ERR_TIMEOUT = 10       /* server: request exceeded its deadline */
+};
+
+ADFEM_API const char *adfem_status_string(int status);
+/* Message of the last failure on the calling thread ("" if none). */
+ADFEM_API const char *adfem_last_error(void);
+ADFEM_API const char *adfem_version(void);
+
+/* ====================================================================
+ * Layer 1: libadmfem-compatible symbols (current-mesh global state)
+ * ==================================================================== */
+
+/* deps/MFEM/API.cpp:4-14 (init_nnfem_mesh); caller src/MFEM/MFEM.jl:95-97.
+ * vertices: 3*num_vertices xyz triples (z ignored); element_indices: 3*num_elements
+ * 0-based vertex ids.  Only degree 1 (P1) with order 2 (or -1) is implemented;
+ * other degrees record ADFEM_ERR_UNSUPPORTED and return NULL.  Builds a new mesh,
+ * makes it current (replacing the previous current mesh, with the same warning the
+ * reference prints), writes the edge count and returns a malloc'ed array of
+ * 2*nedges 1-based vertex ids (all minimum endpoints, then all maximum endpoints)
+ * that the caller releases with free() (Julia: unsafe_wrap(..., own=true)). */
+ADFEM_API long long *init_nnfem_mesh(double *vertices, int num_vertices, int *element_indices, int num_elements,
+                                     int order, int lorder, int degree, long long *nedges);
+/* deps/MFEM/API.cpp:17-65 -- getters on the current mesh */
+ADFEM_API int mfem_get_ngauss(void);
+ADFEM_API void mfem_get_gauss(double *x, double *y);
+ADFEM_API void mfem_get_gauss_weights(double *w);
+ADFEM_API void mfem_get_area(double *a);
+ADFEM_API int mfem_get_elem_ndof(void);
+ADFEM_API int mfem_get_ndof(void);
+ADFEM_API void mfem_get_connectivity(long long *conn);
+ADFEM_API void mfem_get_element_to_vertices(long long *elems);
+
+/* deps/MFEM/FemLaplace1/FemLaplaceScalar.h:59-61 (caller src/MFEM/MCore.jl:117).
+ * Unsummed COO: 9 entries per Gauss point, indices 0-based (row,col) pairs. */
+ADFEM_API void FemLaplaceScalar_forward_Julia(long long *indices, double *vv, const double *kappa);
+/* deps/MFEM/FemSource1/FemSourceScalar.h:35-37 (caller MCore.jl:80).  Accumulates
+ * into rhs, which the caller pre-zeroes (MCore.jl:79). */
+ADFEM_API void FemSourceScalar_forward_Julia(double *rhs, const double *f);
+/* deps/MFEM/ComputeFemStiffnessMatrixMfem/ComputeFemStiffnessMatrixMfem.h:84-87
+ * (caller MCore.jl:311-312).  hmat: 9 row-major entries per Gauss point. */
+ADFEM_API void ComputeFemStiffnessMatrixMfem_forward_Julia(long long *indices, double *vv, const double *hmat);
+
+/* Compute functions behind AdFem's TensorFlow custom ops, same argument order as
+ * the reference MFEM:: functions, on the current mesh, host pointers. */
+/* FemLaplaceScalar.h:28-54 (grad op FemLaplaceScalarGrad, FemLaplaceScalar.cpp:88-144) */
+ADFEM_API void FemLaplaceScalar_backward(double *grad_kappa, const double *grad_vv, const long long *indices,
+                                         const double *vv, const double *kappa);
+/* FemSourceScalar.h:17-32 */
+ADFEM_API void FemSourceScalar_backward(double *grad_f, const double *grad_rhs, const double *rhs, const double *f);
+/* ComputeFemStiffnessMatrixMfem.h:50-81 */
+ADFEM_API void ComputeFemStiffnessMatrixMfem_backward(double *grad_hmat, const double *grad_vv);
+/* deps/MFEM/PlaneStrainAndStress/PlaneStrainAndStress.h:5-78 (op plane_strain_and_stress,
+ * mode 0 = strain with the reference's all-nine-entries formula, mode 1 = stress) */
+ADFEM_API void PlaneStrainMatrix_forward(double *out, const double *E, const double *nu, int N);
+ADFEM_API void PlaneStrainMatrix_backward(double *grad_nu, double *grad_E, const double *grad_out, const double *E,
+                                          const double *nu, int N);
+ADFEM_API void PlaneStressMatrix_forward(double *out, const double *E, const double *nu, int N);
+ADFEM_API void PlaneStressMatrix_backward(double *grad_nu, double *grad_E, const double *grad_out, const double *E,
+                                          const double *nu, int N);
+
+/* ====================================================================
+ * Layer 2: handle-based API (int status)
+ * ==================================================================== */
+typedef struct adfem_mesh adfem_mesh;
+typedef struct adfem_system adfem_system;
+
+/* Same inputs as init_nnfem_mesh (src/MFEM/MFEM.jl:60-119).  degree must be 1. */
+ADFEM_API int adfem_mesh_create(const double *xyz, long long num_vertices, const int *elems0, long long num_elements,
+                                int degree, adfem_mesh **out);
+ADFEM_API int adfem_mesh_destroy(adfem_mesh *mesh);
+/* nv, ne, ngauss (=3 ne), scalar pattern nnz */
+ADFEM_API int adfem_mesh_sizes(const adfem_mesh *mesh, long long *nv, long long *ne, long long *ngauss,
+                               long long *nnz);
+/* Make a handle the "current mesh" of layer 1 (NULL clears it).  The library keeps
+ * one current mesh like the reference's global mmesh (deps/MFEM/Common.cpp:7). */
+ADFEM_API int adfem_set_current_mesh(adfem_mesh *mesh);
+ADFEM_API adfem_mesh *adfem_current_mesh(void);
+/* 1-based CSC pattern of the scalar operator (Julia SparseMatrixCSC colptr/rowval).
+ * Equal to the pattern of sparse(I,J,V) on the unsummed COO (src/MFEM/MCore.jl:119):
+ * the full node graph, stored zeros included.  colptr: nv+1, rowval: nnz. */
+ADFEM_API int adfem_mesh_pattern(const adfem_mesh *mesh, long long *colptr1, long long *rowval1);
+/* Same for the 2 nv x 2 nv elasticity operator in the reference's [x block; y block]
+ * ordering (MCore.jl:314): colptr 2nv+1, rowval 4 nnz. */
+ADFEM_API int adfem_mesh_pattern_elasticity(const adfem_mesh *mesh, long long *colptr1, long long *rowval1);
+/* bcnode (src/MFEM/MCore.jl:439-450): nodes on edges used by exactly one element, 1-based,
+ * ascending (the reference returns Julia Set order).  With out == NULL only *count is set. */
+ADFEM_API int adfem_mesh_bcnode(const adfem_mesh *mesh, long long *out, long long *count);
+/* gauss_nodes (src/MFEM/MFEM.jl:226-232): 3 points per element, element-major */
+ADFEM_API int adfem_mesh_gauss_nodes(const adfem_mesh *mesh, double *x, double *y);
+/* Element vertices after the orientation fix, 1-based, row-major ne x 3 (the content
+ * mfem_get_element_to_vertices writes back into Julia's mesh.elems, API.cpp:57-64). */
+ADFEM_API int adfem_mesh_elements(const adfem_mesh *mesh, long long *elems1);
+/* get_area (src/MFEM/MFEM.jl:216-220 / API.cpp:36-39): Heron area per element */
+ADFEM_API int adfem_mesh_area(const adfem_mesh *mesh, double *area);
+/* Edge list as returned by init_nnfem_mesh (Common.cpp:133-139): 2*nedges 1-based ids,
+ * minimum endpoints then maximum endpoints.  With out == NULL only *nedges is set. */
+ADFEM_API int adfem_mesh_edges(const adfem_mesh *mesh, long long *out, long long *nedges);
+
+/* ---- compute_fem_laplace_matrix1 (src/MFEM/MCore.jl:112-120), Array arm ----
+ * kappa: ngauss values (host).  nzval: nnz values in the adfem_mesh_pattern order,
+ * i.e. the nzval of the SparseMatrixCSC the reference returns. */
+ADFEM_API int adfem_laplace_csc(adfem_mesh *mesh, const double *kappa, long long nkappa, double *nzval);
+/* device variant: values in 0-based CSR order of the same pattern (symmetric, so equal) */
+ADFEM_API int adfem_laplace_csr_d(adfem_mesh *mesh, const double *kappa_d, double *vals_d, void *stream);
+/* graph-op arm (FemLaplaceScalar.h:3-26): unsummed COO on the device */
+ADFEM_API int adfem_laplace_coo_d(adfem_mesh *mesh, const double *kappa_d, long long *indices_d, double *vv_d,
+                                  void *stream);
+/* FemLaplaceScalar.h:28-54 on the device */
+ADFEM_API int adfem_laplace_coo_backward_d(adfem_mesh *mesh, const double *grad_vv_d, double *grad_kappa_d,
+                                           void *stream);
+
+/* ---- compute_fem_source_term1 (MCore.jl:77-82) ----
+ * f: ngauss values.  accumulate = 1 adds into rhs (FemSourceScalar_forward_Julia
+ * semantics), 0 overwrites it. */
+ADFEM_API int adfem_source(adfem_mesh *mesh, const double *f, long long nf, double *rhs, int accumulate);
+ADFEM_API int adfem_source_d(adfem_mesh *mesh, const double *f_d, double *rhs_d, int accumulate, void *stream);
+/* FemSourceScalar.h:17-32 on the device */
+ADFEM_API int adfem_source_backward_d(adfem_mesh *mesh, const double *grad_rhs_d, double *grad_f_d, void *stream);
+
+/* ---- compute_fem_stiffness_matrix (MCore.jl:296-315), Array arm ----
+ * D: ngauss row-major 3x3 blocks (the flattening of MCore.jl:298-307).
+ * nzval: 4 nnz values in adfem_mesh_pattern_elasticity order. */
+ADFEM_API int adfem_stiffness_csc(adfem_mesh *mesh, const double *D, long long nD, double *nzval);
+/* device variant: 0-based CSR values of the same pattern (transpose of the CSC values) */
+ADFEM_API int adfem_stiffness_csr_d(adfem_mesh *mesh, const double *D_d, double *vals_d, void *stream);
+/* graph-op arm (ComputeFemStiffnessMatrixMfem.h:4-48): unsummed COO, 36 per Gauss point */
+ADFEM_API int adfem_stiffness_coo_d(adfem_mesh *mesh, const double *D_d, long long *indices_d, double *vv_d,
+                                    void *stream);
+ADFEM_API int adfem_stiffness_coo_backward_d(adfem_mesh *mesh, const double *grad_vv_d, double *grad_D_d,
+                                             void *stream);
+/* compute_plane_strain_matrix(E, nu) (src/Core.jl:777-785) / plane stress, on the device */
+ADFEM_API int adfem_plane_strain_d(int mode, long long n, const double *E_d, const double *nu_d, double *D_d,
+                                   void *stream);
+ADFEM_API int adfem_plane_strain_backward_d(int mode, long long n, const double *grad_D_d, const double *E_d,
+                                            const double *nu_d, double *grad_E_d, double *grad_nu_d, void *stream);
+
+/* ---- impose_Dirichlet_boundary_conditions ----
+ * SparseMatrixCSC arm (src/MFEM/MUtils.jl:184-199), host pointers, 1-based CSC in and out.
+ * B = [A_II 0; 0 I], r_I = rhs_I - A_IB * bdval, r_B = bdval.  Entries of A_II equal to
+ * 0.0 are not stored unless keep_zeros != 0 (Julia's sparse setindex! into spzeros does
+ * not insert zeros).  bd: 1-based, no duplicates.  Two calls: with out_colptr1 == NULL
+ * only *out_nnz is set. */
+ADFEM_API int adfem_dirichlet_csc(long long n, const long long *colptr1, const long long *rowval1,
+                                  const double *nzval, const double *rhs, const long long *bd, long long nbd,
+                                  const double *bdval, int keep_zeros, long long *out_colptr1,
+                                  long long *out_rowval1, double *out_nzval, long long *out_nnz, double *out_rhs);
+/* SparseTensor arm (deps/MFEM/ImposeDirichlet/ImposeDirichlet.h:27-60), host pointers:
+ * keeps COO entries with row and column outside bd in input order, lifts the rhs,
+ * appends (b,b,1.0) for each distinct bd node in ascending order.  indices 0-based
+ * (row,col) pairs; bd 1-based (duplicates allowed, last bdval wins).  Returns the
+ * output entry count in *out_n; with oindices == NULL only counts. */
+ADFEM_API int adfem_dirichlet_coo(const long long *indices, const double *vv, long long sN, const long long *bd,
+                                  long long nbd, const double *rhs, const double *bdval, long long N,
+                                  long long *oindices, double *ov, double *orhs, long long *out_n);
+/* ImposeDirichlet.h:63-93 */
+ADFEM_API int adfem_dirichlet_coo_backward(const double *grad_vv, const double *grad_rhs, const long long *indices,
+                                           const double *vv, long long sN, const long long *bd, long long nbd,
+                                           const double *bdval, long long N, double *grad_vv_in,
+                                           double *grad_rhs_in, double *grad_bdval);
+
+/* ---- K \ F ---- */
+enum { ADFEM_PREC_FP64 = 0, ADFEM_PREC_MIXED = 1 };
+typedef struct {
+  double rtol;     /* stop when ||b~ - K~ y|| <= rtol ||b~|| in the Jacobi-scaled system (default 1e-12) */
+  int max_iter;    /* cap on CG iterations (default 200000) */
+  int precision;   /* ADFEM_PREC_FP64: FP64 Jacobi-CG; ADFEM_PREC_MIXED: FP32 inner CG with FP64
+                      reliable updates (FP64 residual r = F - K u, FP64 solution, FP64 stop test) */
+  double ru_delta; /* mixed: replace the FP32 residual by the FP64 one when it dropped by this factor
+                      since the last replacement (default 0.1) */
+  int chunk;       /* iterations per device-resident chunk between host checks (default 32) */
+  int warm_start;  /* 1: start from the u passed in; 0: from zero */
+} adfem_solver_opts;
+
+typedef struct {
+  int iterations;      /* inner CG iterations */
+  int updates;         /* FP64 residual replacements (mixed) */
+  double relres;       /* final scaled residual ||b~ - K~ y|| / ||b~||, FP64 */
+  double ms;           /* wall time of the solve on the stream (CUDA events) */
+  int status;
+  long long launches;  /* kernels launched by the solve (graph-resident ones included) */
+} adfem_solver_stats;
+
+ADFEM_API void adfem_solver_opts_default(adfem_solver_opts *opts);
+
+/* K\F for a symmetric positive definite 1-based CSC matrix (e.g. the output of the
+ * Dirichlet entry), host pointers.  Replaces Julia SparseArrays' `\` on this path
+ * (README.md:54) with a GPU Jacobi-CG; u receives the solution. */
+ADFEM_API int adfem_csc_solve(long long n, const long long *colptr1, const long long *rowval1, const double *nzval,
+                              const double *rhs, double *u, const adfem_solver_opts *opts,
+                              adfem_solver_stats *stats);
+
+/* ---- resident solver systems (device pointers) ----
+ * A system keeps the assembled, Dirichlet-imposed operator of one mesh resident in
+ * sliced-ELL form (FP64 and FP32 Jacobi-scaled copies) with its right-hand side and
+ * CG work vectors, so repeated solves and adjoint solves reuse them. */
+enum { ADFEM_SYS_POISSON = 0, ADFEM_SYS_ELASTICITY = 1 };
+ADFEM_API int adfem_system_create(adfem_mesh *mesh, int kind, adfem_system **out);
+ADFEM_API int adfem_system_destroy(adfem_system *sys);
+/* Dirichlet data: bd 1-based DOF ids (for elasticity DOF ids in the [x; y] ordering,
+ * 1..2nv), host arrays, no duplicates; bdval may be NULL (all zero). */
+ADFEM_API int adfem_system_set_dirichlet(adfem_system *sys, const long long *bd, long long nbd, const double *bdval);
+/* Poisson: K(kappa), F(f), Dirichlet imposed -- one fused pass.  kappa_d, f_d: ngauss. */
+ADFEM_API int adfem_system_assemble_poisson_d(adfem_system *sys, const double *kappa_d, const double *f_d,
+                                              void *stream);
+/* Elasticity with plane-strain D(E, nu) (reference formula) at each Gauss point and
+ * body force (fx, fy) at the Gauss points. */
+ADFEM_API int adfem_system_assemble_elasticity_d(adfem_system *sys, const double *E_d, const double *nu_d,
+                                                 const double *fx_d, const double *fy_d, void *stream);
+/* Solve the assembled system; u_d: ndof (nv or 2nv, reference DOF ordering). */
+ADFEM_API int adfem_system_solve_d(adfem_system *sys, double *u_d, const adfem_solver_opts *opts,
+                                   adfem_solver_stats *stats, void *stream);
+/* Adjoint solve K lambda = g (K symmetric); lambda is zero on Dirichlet DOFs. */
+ADFEM_API int adfem_system_adjoint_d(adfem_system *sys, const double *g_d, double *lam_d,
+                                     const adfem_solver_opts *opts, adfem_solver_stats *stats, void *stream);
+/* dL/dkappa at every Gauss point: -w_e (grad lam_e).(grad u_e) (equal for the 3 points of
+ * an element); the composition of the reference's FemLaplaceScalar, ImposeDirichlet and
+ * sparse-solve gradients. */
+ADFEM_API int adfem_system_grad_kappa_d(adfem_system *sys, const double *u_d, const double *lam_d,
+                                        double *grad_kappa_d, void *stream);
+/* dL/dE at every Gauss point for the plane-strain material used by the last
+ * assemble_elasticity call: sum_pq (-w (B lam_e)(B u_e)^T)_pq dD_pq/dE. */
+ADFEM_API int adfem_system_grad_E_d(adfem_system *sys, const double *u_d, const double *lam_d, const double *E_d,
+                                    const double *nu_d, double *grad_E_d, void *stream);
+/* y = K x with the system's FP64 operator (unscaled), for checks. */
+ADFEM_API int adfem_system_apply_d(adfem_system *sys, const double *x_d, double *y_d, void *stream);
+/* copy out the assembled right-hand side (reference DOF ordering) */
+ADFEM_API int adfem_system_rhs_d(adfem_system *sys, double *rhs_d, void *stream);
+/* Same solve as adfem_system_solve_d, launched kernel by kernel (no graph) with a CUDA
+ * event pair around every launch on the solver's stream, for measurement.  kernel_ms[j]
+ * and launches[j] receive the summed duration and launch count of: 0 SpMV+dot,
+ * 1 vector update+dot, 2 p update (FP64) / fold (mixed), 3 FP64 residual. */
+ADFEM_API int adfem_system_solve_profiled_d(adfem_system *sys, double *u_d, const adfem_solver_opts *opts,
+                                            adfem_solver_stats *stats, double *kernel_ms, long long *launches,
+                                            void *stream);
+
+/* One host-buffer call for the whole Poisson forward path: upload kappa and f,
+ * assemble, impose u = bdval on bd, solve, download u.  The end-to-end entry a Julia
+ * caller uses for `K\F` after compute_fem_laplace_matrix1 / compute_fem_source_term1 /
+ * impose_Dirichlet_boundary_conditions. */
+ADFEM_API int adfem_poisson_solve(adfem_system *sys, const double *kappa, const double *f, double *u,
+                                  const adfem_solver_opts *opts, adfem_solver_stats *stats);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* ADFEM_GPU_H */

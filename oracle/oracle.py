@@ -1,0 +1,286 @@
+"""Parity oracle for the P1-triangle path -- TEST INFRASTRUCTURE ONLY.
+
+ctypes wrapper around ``fem_oracle.c`` (a serial C restatement of AdFem's
+deps/MFEM kernels, each function citing the reference file:line it follows),
+plus scipy's SuperLU direct solve standing in for Julia's ``K\\F``.  Only
+``tests/``, ``__graft_entry__.smoke()`` and the CPU-baseline legs of
+``bench.py`` import this module; the product library never does.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+import scipy.sparse as sp
+import scipy.sparse.linalg as spla
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+BUILD = os.path.join(HERE, "_build")
+LIB = os.path.join(BUILD, "libfem_oracle.so")
+SRC = os.path.join(HERE, "fem_oracle.c")
+
+_P = ctypes.c_void_p
+_I = ctypes.c_int
+_L = ctypes.c_longlong
+_D = ctypes.c_double
+
+
+def build(force: bool = False) -> str:
+    """Compile fem_oracle.c into oracle/_build/libfem_oracle.so (gcc, no FMA contraction)."""
+    os.makedirs(BUILD, exist_ok=True)
+    if force or not os.path.exists(LIB) or os.path.getmtime(LIB) < os.path.getmtime(SRC):
+        tmp = LIB + ".tmp%d" % os.getpid()
+        subprocess.check_call(["gcc", "-O2", "-fPIC", "-shared", "-ffp-contract=off", "-o", tmp, SRC,
+                               "-lm", "-lpthread"])
+        os.replace(tmp, LIB)
+    return LIB
+
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        build()
+        L = ctypes.CDLL(LIB)
+        sig = {
+            "orc_mesh_geometry": (_I, [_I, _P, _I, _P, _P, _P, _P, _P, _P, _P, _P, _P]),
+            "orc_mesh_edges": (_L, [_I, _I, _P, _P]),
+            "orc_laplace_coo": (None, [_I, _P, _P, _P, _P, _P, _P, _P]),
+            "orc_laplace_coo_backward": (None, [_I, _P, _P, _P, _P, _P]),
+            "orc_source": (None, [_I, _P, _P, _P, _P, _P]),
+            "orc_source_backward": (None, [_I, _P, _P, _P, _P, _P]),
+            "orc_stiffness_coo": (None, [_I, _I, _P, _P, _P, _P, _P, _P, _P]),
+            "orc_stiffness_coo_backward": (None, [_I, _P, _P, _P, _P, _P]),
+            "orc_plane_strain_stress": (None, [_I, _L, _P, _P, _P]),
+            "orc_plane_strain_stress_backward": (None, [_I, _L, _P, _P, _P, _P, _P]),
+            "orc_dirichlet_coo": (_L, [_P, _P, _L, _P, _I, _P, _P, _L, _P, _P, _P]),
+            "orc_dirichlet_coo_backward": (None, [_P, _P, _P, _P, _L, _P, _I, _P, _L, _P, _P, _P]),
+            "orc_coo_to_csc": (_L, [_P, _P, _L, _L, _P, _P, _P]),
+            "orc_dirichlet_csc": (_L, [_L, _P, _P, _P, _P, _P, _I, _P, _I, _P, _P, _P, _P]),
+            "orc_bcnode": (_L, [_I, _I, _P, _P]),
+            "orc_pcg": (_I, [_L, _P, _P, _P, _P, _P, _D, _I, _I, _P]),
+        }
+        for name, (res, args) in sig.items():
+            f = getattr(L, name)
+            f.restype = res
+            f.argtypes = args
+        _lib = L
+    return _lib
+
+
+def _p(a):
+    return a.ctypes.data_as(ctypes.c_void_p) if a is not None else None
+
+
+def _c(a, dt):
+    return np.ascontiguousarray(a, dtype=dt)
+
+
+class OracleMesh:
+    """Restated NNFEM_Mesh (deps/MFEM/Common.cpp:20-142) for a P1 mesh.
+
+    ``elems`` is 1-based (ne, 3) like the Julia constructor ``Mesh(coords, elems)``.
+    """
+
+    def __init__(self, coords, elems):
+        coords = _c(coords, np.float64)
+        elems = np.asarray(elems)
+        self.nnode = coords.shape[0]
+        self.nelem = elems.shape[0]
+        self.ndof = self.nnode
+        self.coords = coords
+        xyz = np.zeros((self.nnode, 3))
+        xyz[:, :2] = coords
+        e0 = _c(elems - 1, np.int32)
+        ne = self.nelem
+        self.elem = np.empty((ne, 3), np.int32)
+        self.area = np.empty(ne)
+        self.w = np.empty((ne, 3))
+        self.hx = np.empty((ne, 3))
+        self.hy = np.empty((ne, 3))
+        self.h = np.empty((ne, 3, 3))
+        self.gx = np.empty((ne, 3))
+        self.gy = np.empty((ne, 3))
+        self.flipped = lib().orc_mesh_geometry(self.nnode, _p(xyz), ne, _p(e0), _p(self.elem), _p(self.area),
+                                               _p(self.w), _p(self.hx), _p(self.hy), _p(self.h), _p(self.gx),
+                                               _p(self.gy))
+        self.ngauss = 3 * ne
+
+    # --- getters (deps/MFEM/API.cpp:17-65) ---
+    def gauss_nodes(self):
+        return np.stack([self.gx.ravel(), self.gy.ravel()], axis=1)
+
+    def edges(self):
+        n = lib().orc_mesh_edges(self.nnode, self.nelem, _p(self.elem), None)
+        out = np.empty(2 * n, np.int64)
+        lib().orc_mesh_edges(self.nnode, self.nelem, _p(self.elem), _p(out))
+        return out.reshape(2, n).T.copy()
+
+    def elems1(self):
+        return self.elem.astype(np.int64) + 1
+
+    # --- operators ---
+    def laplace_coo(self, kappa):
+        kappa = _c(kappa, np.float64)
+        N = 9 * self.ngauss
+        idx = np.empty(2 * N, np.int64)
+        vv = np.empty(N)
+        lib().orc_laplace_coo(self.nelem, _p(self.elem), _p(self.w), _p(self.hx), _p(self.hy), _p(kappa), _p(idx),
+                              _p(vv))
+        return idx.reshape(N, 2), vv
+
+    def laplace_coo_backward(self, grad_vv):
+        g = _c(grad_vv, np.float64)
+        out = np.empty(self.ngauss)
+        lib().orc_laplace_coo_backward(self.nelem, _p(self.w), _p(self.hx), _p(self.hy), _p(g), _p(out))
+        return out
+
+    def laplace_csc(self, kappa):
+        idx, vv = self.laplace_coo(kappa)
+        return coo_to_csc(idx, vv, self.ndof)
+
+    def source(self, f, rhs=None):
+        f = _c(f, np.float64)
+        out = np.zeros(self.ndof) if rhs is None else _c(rhs, np.float64).copy()
+        lib().orc_source(self.nelem, _p(self.elem), _p(self.w), _p(self.h), _p(f), _p(out))
+        return out
+
+    def source_backward(self, grad_rhs):
+        g = _c(grad_rhs, np.float64)
+        out = np.empty(self.ngauss)
+        lib().orc_source_backward(self.nelem, _p(self.elem), _p(self.w), _p(self.h), _p(g), _p(out))
+        return out
+
+    def stiffness_coo(self, D):
+        D = _c(D, np.float64).reshape(-1)
+        assert D.size == 9 * self.ngauss
+        N = 36 * self.ngauss
+        idx = np.empty(2 * N, np.int64)
+        vv = np.empty(N)
+        lib().orc_stiffness_coo(self.nelem, self.ndof, _p(self.elem), _p(self.w), _p(self.hx), _p(self.hy), _p(D),
+                                _p(idx), _p(vv))
+        return idx.reshape(N, 2), vv
+
+    def stiffness_csc(self, D):
+        idx, vv = self.stiffness_coo(D)
+        return coo_to_csc(idx, vv, 2 * self.ndof)
+
+    def stiffness_coo_backward(self, grad_vv):
+        g = _c(grad_vv, np.float64)
+        out = np.empty(9 * self.ngauss)
+        lib().orc_stiffness_coo_backward(self.nelem, _p(self.w), _p(self.hx), _p(self.hy), _p(g), _p(out))
+        return out.reshape(self.ngauss, 3, 3)
+
+    def bcnode(self):
+        n = lib().orc_bcnode(self.nnode, self.nelem, _p(self.elem), None)
+        out = np.empty(n, np.int64)
+        lib().orc_bcnode(self.nnode, self.nelem, _p(self.elem), _p(out))
+        return out
+
+
+def plane_strain(E, nu, mode: int = 0):
+    E = _c(E, np.float64)
+    nu = _c(nu, np.float64)
+    out = np.empty((E.size, 3, 3))
+    lib().orc_plane_strain_stress(mode, E.size, _p(E), _p(nu), _p(out))
+    return out
+
+
+def plane_strain_backward(grad_out, E, nu, mode: int = 0):
+    g = _c(grad_out, np.float64)
+    E = _c(E, np.float64)
+    nu = _c(nu, np.float64)
+    gE = np.empty(E.size)
+    gn = np.empty(E.size)
+    lib().orc_plane_strain_stress_backward(mode, E.size, _p(g), _p(E), _p(nu), _p(gE), _p(gn))
+    return gE, gn
+
+
+def coo_to_csc(indices, vv, n):
+    """Julia ``sparse(I+1, J+1, V, n, n)`` (src/MFEM/MCore.jl:118-119) as a scipy CSC matrix."""
+    idx = _c(indices, np.int64).reshape(-1)
+    vv = _c(vv, np.float64)
+    N = vv.size
+    nnz = lib().orc_coo_to_csc(_p(idx), _p(vv), N, n, None, None, None)
+    colptr = np.empty(n + 1, np.int64)
+    rowval = np.empty(nnz, np.int64)
+    nzval = np.empty(nnz)
+    lib().orc_coo_to_csc(_p(idx), _p(vv), N, n, _p(colptr), _p(rowval), _p(nzval))
+    return sp.csc_matrix((nzval, rowval, colptr), shape=(n, n))
+
+
+def dirichlet_coo(indices, vv, bd, rhs, bdval, n):
+    """ImposeDirichlet forward (deps/MFEM/ImposeDirichlet/ImposeDirichlet.h:27-60); bd 1-based."""
+    idx = _c(indices, np.int64).reshape(-1)
+    vv = _c(vv, np.float64)
+    bd = _c(bd, np.int64)
+    rhs = _c(rhs, np.float64)
+    bdval = _c(bdval, np.float64)
+    z = lib().orc_dirichlet_coo(_p(idx), _p(vv), vv.size, _p(bd), bd.size, _p(rhs), _p(bdval), n, None, None, None)
+    oi = np.empty(2 * z, np.int64)
+    ov = np.empty(z)
+    orhs = np.empty(n)
+    lib().orc_dirichlet_coo(_p(idx), _p(vv), vv.size, _p(bd), bd.size, _p(rhs), _p(bdval), n, _p(oi), _p(ov),
+                            _p(orhs))
+    return oi.reshape(z, 2), ov, orhs
+
+
+def dirichlet_coo_backward(grad_vv, grad_rhs, indices, vv, bd, bdval, n):
+    """ImposeDirichlet backward (ImposeDirichlet.h:63-93)."""
+    idx = _c(indices, np.int64).reshape(-1)
+    vv = _c(vv, np.float64)
+    bd = _c(bd, np.int64)
+    bdval = _c(bdval, np.float64)
+    g = _c(grad_vv, np.float64)
+    gr = _c(grad_rhs, np.float64)
+    gvi = np.empty(vv.size)
+    gri = np.empty(n)
+    gb = np.empty(bd.size)
+    lib().orc_dirichlet_coo_backward(_p(g), _p(gr), _p(idx), _p(vv), vv.size, _p(bd), bd.size, _p(bdval), n,
+                                     _p(gvi), _p(gri), _p(gb))
+    return gvi, gri, gb
+
+
+def dirichlet_csc(A, rhs, bd, bdval, keep_zeros: bool = False):
+    """impose_Dirichlet_boundary_conditions, SparseMatrixCSC arm (src/MFEM/MUtils.jl:184-199)."""
+    A = sp.csc_matrix(A)
+    A.sort_indices()
+    n = A.shape[0]
+    colptr = _c(A.indptr, np.int64)
+    rowval = _c(A.indices, np.int64)
+    nzval = _c(A.data, np.float64)
+    rhs = _c(rhs, np.float64)
+    bd = _c(bd, np.int64)
+    bdval = _c(bdval, np.float64)
+    z = lib().orc_dirichlet_csc(n, _p(colptr), _p(rowval), _p(nzval), _p(rhs), _p(bd), bd.size, _p(bdval),
+                                int(keep_zeros), None, None, None, None)
+    oc = np.empty(n + 1, np.int64)
+    orr = np.empty(z, np.int64)
+    ov = np.empty(z)
+    orhs = np.empty(n)
+    lib().orc_dirichlet_csc(n, _p(colptr), _p(rowval), _p(nzval), _p(rhs), _p(bd), bd.size, _p(bdval),
+                            int(keep_zeros), _p(oc), _p(orr), _p(ov), _p(orhs))
+    return sp.csc_matrix((ov, orr, oc), shape=(n, n)), orhs
+
+
+def spsolve(A, b):
+    """FP64 sparse direct solve (SuperLU) standing in for Julia's ``K\\F``."""
+    return spla.spsolve(sp.csc_matrix(A), np.asarray(b, dtype=np.float64))
+
+
+def pcg(A, b, rtol=1e-13, max_iter=100000, threads=1):
+    """CPU Jacobi-PCG (FP64) from zero; returns (x, iterations, final relative residual)."""
+    A = sp.csr_matrix(A)
+    n = A.shape[0]
+    rp = _c(A.indptr, np.int64)
+    ci = _c(A.indices, np.int32)
+    va = _c(A.data, np.float64)
+    b = _c(b, np.float64)
+    x = np.empty(n)
+    rr = ctypes.c_double(0.0)
+    it = lib().orc_pcg(n, _p(rp), _p(ci), _p(va), _p(b), _p(x), rtol, max_iter, threads, ctypes.byref(rr))
+    return x, it, rr.value

@@ -1,0 +1,248 @@
+"""GPU parity of K\\F, the fused resident systems and the adjoint.
+
+Bars: solutions within 1e-9 relative (max norm) of the oracle's direct sparse
+solve (scipy SuperLU on the oracle's matrices); gradients within 1e-7 relative
+of the reference's backward chain (FemLaplaceScalar / ImposeDirichlet / sparse
+solve gradients, restated in the oracle) and of central finite differences.
+"""
+import numpy as np
+import pytest
+import scipy.sparse as sp
+
+from adfem_gpu import synth
+
+pytestmark = pytest.mark.gpu
+
+
+def rel(a, b):
+    return float(np.max(np.abs(np.asarray(a) - np.asarray(b))) / max(np.max(np.abs(b)), 1e-300))
+
+
+def poisson_case(oracle, m=64, seed=0):
+    coords, elems = synth.jittered_square(m, seed=seed)
+    O = oracle.OracleMesh(coords, elems)
+    g = O.gauss_nodes()
+    kappa, f = synth.poisson_c1_fields(g[:, 0], g[:, 1])
+    bd = O.bcnode()
+    K = O.laplace_csc(kappa)
+    F = O.source(f)
+    B, r = oracle.dirichlet_csc(K, F, bd, np.zeros(bd.size))
+    return coords, elems, O, kappa, f, bd, B, r
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_csc_solve_matches_direct(oracle, gpulib, precision):
+    coords, elems, O, kappa, f, bd, B, r = poisson_case(oracle, 64)
+    u0 = oracle.spsolve(B, r)
+    u, st = gpulib.solve(B, r, precision=precision, rtol=1e-13, return_stats=True)
+    assert st.status == 0 and st.relres <= 1e-13
+    assert rel(u, u0) < 1e-9
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_poisson_system_matches_oracle_pipeline(oracle, gpulib, precision):
+    import torch
+
+    coords, elems, O, kappa, f, bd, B, r = poisson_case(oracle, 64)
+    G = gpulib.Mesh(coords, elems)
+    S = gpulib.PoissonSystem(G)
+    S.set_dirichlet(bd)
+    S.assemble(torch.tensor(kappa, device="cuda"), torch.tensor(f, device="cuda"))
+    assert rel(S.rhs().cpu().numpy(), r) < 1e-12
+    u = S.solve(precision=precision, rtol=1e-13)
+    st = S.last_stats
+    assert st.status == 0
+    u0 = oracle.spsolve(B, r)
+    assert rel(u.cpu().numpy(), u0) < 1e-9
+    # the resident operator is the Dirichlet-imposed matrix
+    x = np.random.default_rng(0).standard_normal(O.ndof)
+    y = S.apply(torch.tensor(x, device="cuda")).cpu().numpy()
+    assert rel(y, B @ x) < 1e-12
+    # end-to-end host-buffer entry
+    uh = S.solve_host(kappa, f, precision=precision, rtol=1e-13)
+    assert rel(uh, u0) < 1e-9
+
+
+def test_nonzero_dirichlet_values(oracle, gpulib):
+    import torch
+
+    coords, elems = synth.jittered_square(24, seed=2)
+    O = oracle.OracleMesh(coords, elems)
+    rng = np.random.default_rng(8)
+    kappa = 1 + rng.random(O.ngauss)
+    f = rng.standard_normal(O.ngauss)
+    bd = O.bcnode()
+    bv = np.sin(3 * coords[bd - 1, 0]) + coords[bd - 1, 1]
+    B, r = oracle.dirichlet_csc(O.laplace_csc(kappa), O.source(f), bd, bv)
+    G = gpulib.Mesh(coords, elems)
+    S = gpulib.PoissonSystem(G)
+    S.set_dirichlet(bd[::-1], bv[::-1])
+    S.assemble(torch.tensor(kappa, device="cuda"), torch.tensor(f, device="cuda"))
+    assert rel(S.rhs().cpu().numpy(), r) < 1e-12
+    u = S.solve(rtol=1e-14).cpu().numpy()
+    assert rel(u, oracle.spsolve(B, r)) < 1e-9
+    np.testing.assert_array_equal(u[bd - 1], bv)
+
+
+def oracle_kappa_gradient(oracle, O, kappa, f, bd, obs, uobs):
+    """dL/dkappa through the reference's backward ops: sparse-solve gradient, then
+    ImposeDirichlet backward (ImposeDirichlet.h:63-93), then FemLaplaceScalar backward
+    (FemLaplaceScalar.h:28-54)."""
+    n = O.ndof
+    idx, vv = O.laplace_coo(kappa)
+    F = O.source(f)
+    bv = np.zeros(bd.size)
+    oi, ov, orhs = oracle.dirichlet_coo(idx, vv, bd, F, bv, n)
+    A = sp.coo_matrix((ov, (oi[:, 0], oi[:, 1])), shape=(n, n)).tocsc()
+    u = oracle.spsolve(A, orhs)
+    g = np.zeros(n)
+    g[obs] = 2 * (u[obs] - uobs)
+    lam = oracle.spsolve(A.T.tocsc(), g)
+    grad_ov = -lam[oi[:, 0]] * u[oi[:, 1]]  # x = A\b: dL/dA_ij = -lam_i x_j for each stored entry
+    gvv, _, _ = oracle.dirichlet_coo_backward(grad_ov, lam, idx, vv, bd, bv, n)
+    return O.laplace_coo_backward(gvv), u
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_adjoint_gradient_matches_reference_chain(oracle, gpulib, precision):
+    import torch
+
+    coords, elems = synth.jittered_square(32, seed=0)
+    O = oracle.OracleMesh(coords, elems)
+    g = O.gauss_nodes()
+    G0 = synth.fourier_field(g[:, 0], g[:, 1], seed=1)
+    kappa = 1 + np.exp(0.5 * G0)
+    f = 1e5 * (g[:, 0] + g[:, 1])
+    bd = O.bcnode()
+    obs = synth.observation_nodes(O.ndof, seed=3, frac=0.05)
+    uobs = np.random.default_rng(5).standard_normal(obs.size) * 1e-3
+    gref, uref = oracle_kappa_gradient(oracle, O, kappa, f, bd, obs, uobs)
+    G = gpulib.Mesh(coords, elems)
+    S = gpulib.PoissonSystem(G)
+    S.set_dirichlet(bd)
+    S.assemble(torch.tensor(kappa, device="cuda"), torch.tensor(f, device="cuda"))
+    u = S.solve(precision=precision, rtol=1e-14)
+    assert rel(u.cpu().numpy(), uref) < 1e-9
+    gu = torch.zeros_like(u)
+    gu[torch.tensor(obs, device="cuda")] = 2 * (u[torch.tensor(obs, device="cuda")] -
+                                                torch.tensor(uobs, device="cuda"))
+    lam = S.adjoint(gu, precision=precision, rtol=1e-14)
+    gk = S.grad_kappa(u, lam).cpu().numpy()
+    assert rel(gk, gref) < 1e-7
+
+
+def test_gradient_central_differences(oracle, gpulib):
+    import torch
+
+    coords, elems = synth.jittered_square(16, seed=0)
+    G = gpulib.Mesh(coords, elems)
+    O = oracle.OracleMesh(coords, elems)
+    g = O.gauss_nodes()
+    kappa = 1 + np.exp(0.5 * synth.fourier_field(g[:, 0], g[:, 1], seed=1))
+    f = 1e5 * (g[:, 0] + g[:, 1])
+    bd = O.bcnode()
+    obs = synth.observation_nodes(O.ndof, seed=3, frac=0.1)
+    uobs = np.zeros(obs.size)
+    S = gpulib.PoissonSystem(G)
+    S.set_dirichlet(bd)
+    ft = torch.tensor(f, device="cuda")
+
+    def loss(k):
+        S.assemble(torch.tensor(k, device="cuda"), ft)
+        u = S.solve(rtol=1e-15, max_iter=100000).cpu().numpy()
+        return float(np.sum((u[obs] - uobs) ** 2)), u
+
+    L0, u = loss(kappa)
+    ut = torch.tensor(u, device="cuda")
+    gu = torch.zeros_like(ut)
+    gu[torch.tensor(obs, device="cuda")] = 2 * torch.tensor(u[obs] - uobs, device="cuda")
+    lam = S.adjoint(gu, rtol=1e-15)
+    gk = S.grad_kappa(ut, lam).cpu().numpy()
+    rng = np.random.default_rng(233)
+    for _ in range(4):
+        v = rng.standard_normal(kappa.size)
+        v /= np.linalg.norm(v)
+        eps = 1e-4 * np.linalg.norm(kappa) / np.sqrt(kappa.size)
+        fd = (loss(kappa + eps * v)[0] - loss(kappa - eps * v)[0]) / (2 * eps)
+        assert abs(fd - gk @ v) <= 1e-6 * max(abs(fd), 1e-30) + 1e-12 * L0
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_elasticity_system(oracle, gpulib, precision):
+    import torch
+
+    coords, elems = synth.jittered_square(24, seed=2)
+    O = oracle.OracleMesh(coords, elems)
+    g = O.gauss_nodes()
+    E = 1e9 * np.exp(0.3 * synth.fourier_field(g[:, 0], g[:, 1], seed=2))
+    nu = np.full(O.ngauss, 0.3)
+    D = oracle.plane_strain(E, nu, 0)
+    K = O.stiffness_csc(D)
+    fx = np.zeros(O.ngauss)
+    fy = np.full(O.ngauss, -1e6)
+    F = np.concatenate([O.source(fx), O.source(fy)])
+    left = synth.left_edge_nodes(coords)
+    bd = np.concatenate([left + 1, left + 1 + O.ndof])
+    B, r = oracle.dirichlet_csc(K, F, bd, np.zeros(bd.size))
+    u0 = oracle.spsolve(B, r)
+    G = gpulib.Mesh(coords, elems)
+    S = gpulib.ElasticitySystem(G)
+    S.set_dirichlet(bd)
+    t = lambda a: torch.tensor(a, device="cuda")  # noqa: E731
+    S.assemble(t(E), t(nu), t(fx), t(fy))
+    assert rel(S.rhs().cpu().numpy(), r) < 1e-12
+    x = np.random.default_rng(0).standard_normal(2 * O.ndof)
+    assert rel(S.apply(t(x)).cpu().numpy(), B @ x) < 1e-12
+    u = S.solve(precision=precision, rtol=1e-14)
+    assert S.last_stats.status == 0
+    assert rel(u.cpu().numpy(), u0) < 1e-9
+    # adjoint gradient wrt E against central differences
+    obs = synth.observation_nodes(O.ndof, seed=4, frac=0.05)
+    oidx = np.concatenate([obs, obs + O.ndof])
+
+    def loss(Ev):
+        S.assemble(t(Ev), t(nu), t(fx), t(fy))
+        uu = S.solve(rtol=1e-15).cpu().numpy()
+        return float(np.sum(uu[oidx] ** 2)), uu
+
+    L0, uu = loss(E)
+    gu = np.zeros(2 * O.ndof)
+    gu[oidx] = 2 * uu[oidx]
+    lam = S.adjoint(t(gu), rtol=1e-15)
+    gE = S.grad_E(t(uu), lam, t(E), t(nu)).cpu().numpy()
+    rng = np.random.default_rng(233)
+    for _ in range(3):
+        v = rng.standard_normal(E.size)
+        v /= np.linalg.norm(v)
+        eps = 1e-5 * np.linalg.norm(E) / np.sqrt(E.size)
+        fd = (loss(E + eps * v)[0] - loss(E - eps * v)[0]) / (2 * eps)
+        assert abs(fd - gE @ v) <= 1e-6 * abs(fd) + 1e-12 * L0
+
+
+def test_not_converged_and_breakdown_are_statuses(oracle, gpulib):
+    import torch
+
+    from adfem_gpu import AdFemError
+
+    coords, elems = synth.jittered_square(32, seed=0)
+    G = gpulib.Mesh(coords, elems)
+    O = oracle.OracleMesh(coords, elems)
+    S = gpulib.PoissonSystem(G)
+    S.set_dirichlet(O.bcnode())
+    k = torch.ones(O.ngauss, dtype=torch.float64, device="cuda")
+    f = torch.ones(O.ngauss, dtype=torch.float64, device="cuda")
+    S.assemble(k, f)
+    with pytest.raises(AdFemError) as ei:
+        S.solve(max_iter=3)
+    assert ei.value.status == 4
+    # the context stays usable
+    u = S.solve(rtol=1e-12)
+    assert S.last_stats.status == 0 and torch.isfinite(u).all()
+    # a non-positive diagonal (negative conductivity) is rejected
+    with pytest.raises(AdFemError) as ei:
+        S.assemble(-k, f)
+    assert ei.value.status in (5, 7)
+    kn = k.clone()
+    kn[5] = float("nan")
+    with pytest.raises(AdFemError):
+        S.assemble(kn, f)
