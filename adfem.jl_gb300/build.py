@@ -24,7 +24,7 @@ INCLUDE = os.path.join(ROOT, "include")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "--expt-relaxed-constexpr",
-                     "-Xcompiler", "-fPIC,-fvisibility=hidden,-O3", "-I", INCLUDE, "-I", CSRC]
+                     "-Xcompiler", "-fPIC,-fvisibility=hidden,-O3,-ffp-contract=off", "-I", INCLUDE, "-I", CSRC]
 
 
 def nvcc() -> str:

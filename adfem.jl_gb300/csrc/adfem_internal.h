@@ -75,7 +75,18 @@ struct Sell {
   bool delta16 = false; // column stored as int16 delta to the row, else int32 column
   DevBuf sptr;          // int32 [nslices + 1]  (units of entries)
   DevBuf col;           // int16 [nent] (delta) or int32 [nent]
-  DevBuf val64;         // double [nent]
+  // Slice-uniform column patterns: when every row r of a slice has the same column
+  // offsets col - r (for period 2: the same per row parity, as for interleaved x/y
+  // DOFs), they are stored once in `pat` and spat[slice] points at them (int16
+  // units; pattern for parity q at pat[spat + q*w]); spat = -1 keeps the per-row
+  // columns of `col`.  Kernels then issue the gathers of a row without waiting for
+  // its column loads, and the column bytes of uniform slices are never read.
+  DevBuf spat;          // int32 [nslices]
+  DevBuf pat;           // int16 pool
+  int pat_period = 1;
+  int64_t uniform_slices = 0;
+  DevBuf val64;         // double [nent]  (Jacobi-scaled, standard form)
+  DevBuf valD64;        // double [nent]  (Jacobi-scaled, difference form, for FP64 residuals)
   DevBuf val32;         // float  [nent]
 };
 

@@ -565,9 +565,10 @@ int adfem_csc_solve(long long n, const long long* colptr1, const long long* rowv
     dp[i] = found;
   }
   Sell A;
-  ADFEM_TRY(sell_build_pattern(n, rp.data(), ci.data(), A));
+  ADFEM_TRY(sell_build_pattern(n, rp.data(), ci.data(), A, 1));
   ADFEM_TRY(A.val64.alloc(sizeof(double) * std::max<int64_t>(A.nent, 1)));
   ADFEM_TRY(A.val32.alloc(sizeof(float) * std::max<int64_t>(A.nent, 1)));
+  ADFEM_TRY(A.valD64.alloc(sizeof(double) * std::max<int64_t>(A.nent, 1)));
   ADFEM_CUDA(cudaMemset(A.val64.p, 0, sizeof(double) * std::max<int64_t>(A.nent, 1)));
   DevBuf drp, dvals, ddp, db, du;
   ADFEM_TRY(to_dev(drp, rp.data(), rp.size()));
@@ -581,7 +582,7 @@ int adfem_csc_solve(long long n, const long long* colptr1, const long long* rowv
   Solver sv;
   ADFEM_TRY(sv.init(&A, n));
   ADFEM_TRY(solver_prepare(sv, ddp.as<int32_t>(), nullptr));
-  const int st = solver_solve(sv, db.as<double>(), du.as<double>(), nullptr, o, stats, nullptr);
+  const int st = solver_solve(sv, db.as<double>(), du.as<double>(), nullptr, nullptr, nullptr, o, stats, nullptr);
   if (st != ADFEM_OK && st != ADFEM_ERR_NOT_CONVERGED) return st;
   ADFEM_TRY(to_host(u, du, (size_t)n));
   return st;
@@ -598,7 +599,7 @@ int adfem_system_create(adfem_mesh* mesh, int kind, adfem_system** out) {
   Mesh& m = *mesh->m;
   if (kind == ADFEM_SYS_POISSON) {
     s->ndof = m.nv;
-    ADFEM_TRY(sell_build_pattern(m.nv, m.rowptr.data(), m.colind.data(), s->A));
+    ADFEM_TRY(sell_build_pattern(m.nv, m.rowptr.data(), m.colind.data(), s->A, 1));
     std::vector<int32_t> dp(m.nv);
     for (int64_t i = 0; i < m.nv; i++)
       for (int32_t k = m.rowptr[i]; k < m.rowptr[i + 1]; k++)
@@ -622,12 +623,13 @@ int adfem_system_create(adfem_mesh* mesh, int kind, adfem_system** out) {
         ci2[z++] = 2 * m.colind[k] + 1;
       }
     }
-    ADFEM_TRY(sell_build_pattern(2 * m.nv, rp2.data(), ci2.data(), s->A));
+    ADFEM_TRY(sell_build_pattern(2 * m.nv, rp2.data(), ci2.data(), s->A, 2));
     ADFEM_TRY(to_dev(s->diagpos, dp2.data(), dp2.size()));
   }
   const size_t ne = std::max<int64_t>(s->A.nent, 1);
   ADFEM_TRY(s->A.val64.alloc(sizeof(double) * ne));
   ADFEM_TRY(s->A.val32.alloc(sizeof(float) * ne));
+  ADFEM_TRY(s->A.valD64.alloc(sizeof(double) * ne));
   ADFEM_CUDA(cudaMemset(s->A.val64.p, 0, sizeof(double) * ne));
   ADFEM_CUDA(cudaMemset(s->A.val32.p, 0, sizeof(float) * ne));
   ADFEM_TRY(s->rhs.alloc(sizeof(double) * s->ndof));
@@ -703,10 +705,12 @@ int adfem_system_solve_d(adfem_system* sys, double* u_d, const adfem_solver_opts
   if (opts) o = *opts;
   cudaStream_t st = S(stream);
   if (sys->kind == ADFEM_SYS_POISSON)
-    return solver_solve(sys->solver, sys->rhs.as<double>(), u_d, nullptr, o, stats, st);
+    return solver_solve(sys->solver, sys->rhs.as<double>(), u_d, nullptr, sys->isbd.as<uint8_t>(),
+                        sys->bdval.as<double>(), o, stats, st);
   const int64_t nv = sys->mesh->m->nv;
   if (o.warm_start) ADFEM_TRY(kerr(launch_to_interleaved(nv, u_d, sys->t0.as<double>(), st), "interleave"));
-  const int r = solver_solve(sys->solver, sys->rhs.as<double>(), sys->t0.as<double>(), nullptr, o, stats, st);
+  const int r = solver_solve(sys->solver, sys->rhs.as<double>(), sys->t0.as<double>(), nullptr,
+                             sys->isbd.as<uint8_t>(), sys->bdval.as<double>(), o, stats, st);
   if (r != ADFEM_OK && r != ADFEM_ERR_NOT_CONVERGED) return r;
   ADFEM_TRY(kerr(launch_from_interleaved(nv, sys->t0.as<double>(), u_d, st), "deinterleave"));
   return r;
@@ -722,7 +726,8 @@ int adfem_system_solve_profiled_d(adfem_system* sys, double* u_d, const adfem_so
   adfem_solver_opts_default(&o);
   if (opts) o = *opts;
   SolveProfile prof;
-  const int r = solver_solve(sys->solver, sys->rhs.as<double>(), u_d, nullptr, o, stats, S(stream), &prof);
+  const int r = solver_solve(sys->solver, sys->rhs.as<double>(), u_d, nullptr, sys->isbd.as<uint8_t>(),
+                             sys->bdval.as<double>(), o, stats, S(stream), &prof);
   for (int j = 0; j < 4; j++) {
     kernel_ms[j] = prof.ms[j];
     launches[j] = prof.n[j];
@@ -740,12 +745,13 @@ int adfem_system_adjoint_d(adfem_system* sys, const double* g_d, double* lam_d, 
   if (opts) o = *opts;
   cudaStream_t st = S(stream);
   if (sys->kind == ADFEM_SYS_POISSON)
-    return solver_solve(sys->solver, g_d, lam_d, sys->isbd.as<uint8_t>(), o, stats, st);
+    return solver_solve(sys->solver, g_d, lam_d, sys->isbd.as<uint8_t>(), sys->isbd.as<uint8_t>(), nullptr, o, stats,
+                        st);
   const int64_t nv = sys->mesh->m->nv;
   ADFEM_TRY(kerr(launch_to_interleaved(nv, g_d, sys->t1.as<double>(), st), "interleave"));
   if (o.warm_start) ADFEM_TRY(kerr(launch_to_interleaved(nv, lam_d, sys->t0.as<double>(), st), "interleave"));
-  const int r = solver_solve(sys->solver, sys->t1.as<double>(), sys->t0.as<double>(), sys->isbd.as<uint8_t>(), o,
-                             stats, st);
+  const int r = solver_solve(sys->solver, sys->t1.as<double>(), sys->t0.as<double>(), sys->isbd.as<uint8_t>(),
+                             sys->isbd.as<uint8_t>(), nullptr, o, stats, st);
   if (r != ADFEM_OK && r != ADFEM_ERR_NOT_CONVERGED) return r;
   ADFEM_TRY(kerr(launch_from_interleaved(nv, sys->t0.as<double>(), lam_d, st), "deinterleave"));
   return r;

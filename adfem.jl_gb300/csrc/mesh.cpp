@@ -6,6 +6,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <map>
 #include <thread>
 
 #include "adfem_internal.h"
@@ -78,8 +79,10 @@ static int upload(DevBuf& b, const T* src, size_t n) {
 }
 
 // Sliced-ELL pattern of a CSR matrix (rows n, 0-based rowptr/colind).  Columns are
-// stored as int16 deltas when every |col-row| fits, else as int32.
-int sell_build_pattern(int64_t n, const int32_t* rowptr, const int32_t* colind, Sell& s) {
+// stored as int16 deltas when every |col-row| fits, else as int32.  Slices whose rows
+// share their column offsets (with the given period in the row index) also get a
+// slice-level pattern (see Sell::spat).
+int sell_build_pattern(int64_t n, const int32_t* rowptr, const int32_t* colind, Sell& s, int period) {
   s.n = n;
   s.nslices = (n + 31) / 32;
   std::vector<int32_t> sptr(s.nslices + 1, 0);
@@ -129,6 +132,51 @@ int sell_build_pattern(int64_t n, const int32_t* rowptr, const int32_t* colind, 
     });
     ADFEM_TRY(upload(s.col, col.data(), (size_t)s.nent));
   }
+  // slice-uniform patterns
+  s.pat_period = period;
+  s.uniform_slices = 0;
+  std::vector<int32_t> spat(std::max<int64_t>(s.nslices, 1), -1);
+  std::vector<int16_t> pool;
+  if (s.delta16 && (period == 1 || period == 2)) {
+    std::map<std::vector<int16_t>, int32_t> dedupe;
+    std::vector<int16_t> pt;
+    for (int64_t sl = 0; sl < s.nslices; sl++) {
+      const int w = (sptr[sl + 1] - sptr[sl]) / 32;
+      if (sl * 32 + 32 > n || w == 0) continue;
+      pt.assign((size_t)period * w, 0);
+      bool ok = true;
+      for (int64_t r = sl * 32; r < sl * 32 + 32 && ok; r++) {
+        if (rowptr[r + 1] - rowptr[r] != w) {
+          ok = false;
+          break;
+        }
+        const int q = (int)(r % period);
+        for (int k = 0; k < w; k++) {
+          const int16_t d = (int16_t)(colind[rowptr[r] + k] - r);
+          if (r - sl * 32 < period) pt[(size_t)q * w + k] = d;
+          else if (pt[(size_t)q * w + k] != d) {
+            ok = false;
+            break;
+          }
+        }
+      }
+      if (!ok) continue;
+      auto it = dedupe.find(pt);
+      int32_t off;
+      if (it == dedupe.end()) {
+        off = (int32_t)pool.size();
+        pool.insert(pool.end(), pt.begin(), pt.end());
+        dedupe.emplace(pt, off);
+      } else {
+        off = it->second;
+      }
+      spat[sl] = off;
+      s.uniform_slices++;
+    }
+  }
+  if (pool.empty()) pool.push_back(0);
+  ADFEM_TRY(upload(s.spat, spat.data(), spat.size()));
+  ADFEM_TRY(upload(s.pat, pool.data(), pool.size()));
   return ADFEM_OK;
 }
 
@@ -298,7 +346,7 @@ int mesh_build(const double* xyz, int64_t nv, const int32_t* elems0, int64_t ne,
   ADFEM_TRY(upload(m->d_rowptr, m->rowptr.data(), m->rowptr.size()));
   ADFEM_TRY(upload(m->d_colind, m->colind.data(), m->colind.size()));
   ADFEM_TRY(upload(m->d_diagpos, diagpos.data(), diagpos.size()));
-  ADFEM_TRY(sell_build_pattern(nv, m->rowptr.data(), m->colind.data(), m->sell));
+  ADFEM_TRY(sell_build_pattern(nv, m->rowptr.data(), m->colind.data(), m->sell, 1));
   *out = m.release();
   return ADFEM_OK;
 }

@@ -3,18 +3,24 @@
 //  * The operator is scaled once, K~ = S K S with S = diag(1/sqrt(K_ii)), so CG on
 //    K~ is Jacobi-preconditioned CG on K with no preconditioner vector in the loop.
 //  * FP64 path: three kernels per iteration (SpMV + p.q, update + r.r, p update).
-//  * Mixed path: FP32 copy of K~, FP32 vectors and FP32 accumulation in the inner
-//    iteration (two kernels: SpMV with the p update folded into the gather, and the
-//    x/r update); when the FP32 residual has dropped by ru_delta the FP32 iterate is
-//    folded into the FP64 solution and the residual is recomputed in FP64 on the
-//    device (reliable update, with the search direction re-orthogonalised against
-//    the new residual).  The stopping test is on that FP64 residual.
+//  * Mixed path: FP32 difference-form copy of K~, FP32 residual/direction vectors
+//    and FP32 accumulation of the dot products in the inner iteration (two kernels:
+//    SpMV with the p update folded into the gather, and the x/r update).  The
+//    solution correction is accumulated as an FP32 hi+lo pair (about 48 bits, no
+//    FP64 instructions in the loop) and folded into the FP64 solution whenever the
+//    FP32 residual has dropped by ru_delta; the residual is then recomputed in FP64
+//    on the device (reliable update, with the search direction re-orthogonalised
+//    against the new residual).  The stopping test is on that FP64 residual.
+//  * SpMV kernels unroll the entries of a row (sliced-ELL widths are at most 8 for
+//    the scalar operator and 16 for elasticity) so that every load of a row is in
+//    flight at once; a plain loop serves wider operators.
 //  * Reductions are deterministic: a fixed grid, per-block partials, and the last
 //    block to arrive sums the partials in block order.  No kernel ever waits on
 //    another: every kernel reads a device flag at entry and returns early once the
 //    solve has finished, so a chunk of iterations captured in a CUDA graph can be
 //    replayed without a host round trip per iteration.
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 
 #include "solver.cuh"
@@ -22,15 +28,15 @@
 namespace adfem {
 
 static constexpr int kT = 256;
-static constexpr int kBlocksPerSM = 8;
+static constexpr int kMaxBlocksPerSM = 8;
 
 __device__ __forceinline__ int64_t gtid() { return (int64_t)blockIdx.x * blockDim.x + threadIdx.x; }
 __device__ __forceinline__ int64_t gstride() { return (int64_t)gridDim.x * blockDim.x; }
 
 template <bool D16>
-__device__ __forceinline__ int64_t colof(const void* c, int64_t idx, int64_t r) {
-  if constexpr (D16) return r + (int64_t)__ldg(reinterpret_cast<const int16_t*>(c) + idx);
-  else return (int64_t)__ldg(reinterpret_cast<const int32_t*>(c) + idx);
+__device__ __forceinline__ int colof(const void* c, int64_t idx, int64_t r) {
+  if constexpr (D16) return (int)(r + (int64_t)__ldg(reinterpret_cast<const int16_t*>(c) + idx));
+  else return __ldg(reinterpret_cast<const int32_t*>(c) + idx);
 }
 
 template <class T>
@@ -92,6 +98,13 @@ __device__ __forceinline__ bool reduce_grid(T (&v)[NV], T* partials, unsigned* c
   return true;
 }
 
+// row geometry in sliced-ELL: first entry of row r and the slice width
+__device__ __forceinline__ void sell_row(const int32_t* __restrict__ sptr, int64_t r, int64_t& base, int& w) {
+  const int32_t s0 = __ldg(sptr + (r >> 5)), s1 = __ldg(sptr + (r >> 5) + 1);
+  base = (int64_t)s0 + (r & 31);
+  w = (s1 - s0) >> 5;
+}
+
 // ---------------------------------------------------------------------------
 // setup kernels
 __global__ void k_csr_to_sell(int64_t n, const int32_t* __restrict__ sptr, const int32_t* __restrict__ rowptr,
@@ -109,21 +122,12 @@ cudaError_t launch_csr_to_sell(const Sell& A, int64_t n, const int32_t* rowptr, 
 }
 
 // s_i = rsqrt(K_ii) in FP32; flags a non-positive or non-finite diagonal
-template <bool D16>
-__global__ void k_scale_diag(int64_t n, const int32_t* __restrict__ sptr, const void* __restrict__ col,
-                             const double* __restrict__ val, const int32_t* __restrict__ diagpos,
-                             float* __restrict__ s, int* __restrict__ bad) {
+__global__ void k_scale_diag(int64_t n, const int32_t* __restrict__ sptr, const double* __restrict__ val,
+                             const int32_t* __restrict__ diagpos, float* __restrict__ s, int* __restrict__ bad) {
   const int64_t r = gtid();
   if (r >= n) return;
   const int64_t base = (int64_t)sptr[r >> 5] + (r & 31);
-  const int w = (sptr[(r >> 5) + 1] - sptr[r >> 5]) >> 5;
-  double d = 0.0;
-  if (diagpos) {
-    d = val[base + 32 * (int64_t)diagpos[r]];
-  } else {
-    for (int k = 0; k < w; k++)
-      if (colof<D16>(col, base + 32 * (int64_t)k, r) == r) d += val[base + 32 * (int64_t)k];
-  }
+  const double d = val[base + 32 * (int64_t)diagpos[r]];
   const float df = (float)d;
   if (!(df > 0.0f) || !isfinite(df)) {
     atomicExch(bad, 1);
@@ -133,20 +137,37 @@ __global__ void k_scale_diag(int64_t n, const int32_t* __restrict__ sptr, const 
   s[r] = rsqrtf(df);
 }
 
+// val64 <- s_i K_ij s_j (FP64, in place, standard form).  The difference-form copies
+// (FP64 valD for residuals, FP32 val32 for the inner iteration) hold w_ij = s_i K_ij
+// in off-diagonal slots and d_i = s_i^2 sum_j K_ij (the row sum, zero for rows of a
+// pure Laplacian) in the diagonal slot, so that
+//     (K~ x)_i = d_i x_i + sum_{j != i} w_ij (s_j x_j - s_i x_i)
+// rounds in proportion to the differences s_j x_j - s_i x_i.  Smooth error modes,
+// whose eigenvalues are far below FP32 resolution relative to the diagonal, keep
+// their accuracy; a plain FP32 copy of K~ loses them once cond(K~) * 2^-24 ~ 1.
 template <bool D16>
 __global__ void k_scale_values(int64_t n, const int32_t* __restrict__ sptr, const void* __restrict__ col,
-                               double* __restrict__ val, float* __restrict__ val32, const float* __restrict__ s) {
+                               double* __restrict__ val, double* __restrict__ valD, float* __restrict__ val32,
+                               const float* __restrict__ s, const int32_t* __restrict__ diagpos) {
   const int64_t r = gtid();
   if (r >= n) return;
-  const int64_t base = (int64_t)sptr[r >> 5] + (r & 31);
-  const int w = (sptr[(r >> 5) + 1] - sptr[r >> 5]) >> 5;
+  int64_t base;
+  int w;
+  sell_row(sptr, r, base, w);
   const double si = (double)s[r];
+  double rowsum = 0.0;
   for (int k = 0; k < w; k++) {
     const int64_t idx = base + 32 * (int64_t)k;
-    const double v = si * val[idx] * (double)s[colof<D16>(col, idx, r)];
-    val[idx] = v;
-    val32[idx] = (float)v;
+    const double v = val[idx];
+    rowsum += v;
+    const double t = si * v;
+    val[idx] = t * (double)s[colof<D16>(col, idx, r)];
+    valD[idx] = t;
+    val32[idx] = (float)t;
   }
+  const double d = si * si * rowsum;
+  valD[base + 32 * (int64_t)diagpos[r]] = d;
+  val32[base + 32 * (int64_t)diagpos[r]] = (float)d;
 }
 
 // ---------------------------------------------------------------------------
@@ -171,28 +192,35 @@ __global__ void __launch_bounds__(kT) k_init(int64_t n, const double* __restrict
   }
 }
 
-// FP64 residual r = b~ - K~ y.  mode 0: FP64 CG start (p = r, rho = r.r);
-// mode 1: mixed reliable update (r32 = (float) r, re-orthogonalise p, new coefficients);
+// FP64 residual r = b~ - K~ y, evaluated in difference form (see k_scale_values) so
+// that its rounding follows the differences of the solution rather than its size.
+// mode 0: FP64 CG start (r64 = p64 = r, rho = r.r);
+// mode 1: mixed residual replacement (r32 = (float) r, re-orthogonalise p, new coefficients);
 // mode 2: final check only (rr64).
 template <bool D16>
 __global__ void __launch_bounds__(kT) k_residual64(int64_t n, const int32_t* __restrict__ sptr,
-                                                   const void* __restrict__ col, const double* __restrict__ val,
-                                                   const double* __restrict__ b, const double* __restrict__ y,
-                                                   double* __restrict__ r64, double* __restrict__ p64,
-                                                   float* __restrict__ r32, const float* __restrict__ pa,
-                                                   const float* __restrict__ pb, CgState* st, double* partials,
-                                                   int mode, int force) {
+                                                   const void* __restrict__ col, const double* __restrict__ valD,
+                                                   const float* __restrict__ sc, const double* __restrict__ b,
+                                                   const double* __restrict__ y, double* __restrict__ r64,
+                                                   double* __restrict__ p64, float* __restrict__ r32,
+                                                   const float* __restrict__ pa, const float* __restrict__ pb,
+                                                   CgState* st, double* partials, int mode, int force) {
   if (!force && st->done != 3) return;
   const int it = st->iters;
   const float* plat = (it & 1) ? pb : pa;
   double a0 = 0.0, a1 = 0.0, a2 = 0.0;
   for (int64_t r = gtid(); r < n; r += gstride()) {
-    const int64_t base = (int64_t)sptr[r >> 5] + (r & 31);
-    const int w = (sptr[(r >> 5) + 1] - sptr[r >> 5]) >> 5;
+    int64_t base;
+    int w;
+    sell_row(sptr, r, base, w);
+    const double yr = y[r];
+    const double zr = (double)sc[r] * yr;
     double s = 0.0;
     for (int k = 0; k < w; k++) {
       const int64_t idx = base + 32 * (int64_t)k;
-      s = fma(val[idx], y[colof<D16>(col, idx, r)], s);
+      const int j = colof<D16>(col, idx, r);
+      const double t = (j == r) ? yr : fma((double)sc[j], y[j], -zr);
+      s = fma(valD[idx], t, s);
     }
     const double ri = b[r] - s;
     a0 = fma(ri, ri, a0);
@@ -219,6 +247,15 @@ __global__ void __launch_bounds__(kT) k_residual64(int64_t n, const int32_t* __r
       st->done = 1;
       return;
     }
+    // The FP64 residual of an FP64 iterate cannot fall below about 2^-53 |K~| |y|
+    // (rounding of y itself, amplified by the largest eigenvalues).  When the FP32
+    // residual has met rtol twice in a row and the FP64 residual improved less than
+    // 4x in between, the iterate is at that attainable accuracy: stop there.
+    if (mode == 1 && st->final_req && st->last_rr64 > 0.0 && rr > 0.0625 * st->last_rr64) {
+      st->floor_hit = 1;
+      st->done = 1;
+      return;
+    }
     if (st->iters >= st->max_iter) {
       st->done = 4;
       return;
@@ -228,6 +265,8 @@ __global__ void __launch_bounds__(kT) k_residual64(int64_t n, const int32_t* __r
       st->done = 0;
       return;
     }
+    if (st->final_req) st->last_rr64 = rr;
+    st->final_req = 0;
     const double rn = tot[1];
     if (st->updates == 0) {
       st->ar = 1.0;
@@ -247,26 +286,82 @@ __global__ void __launch_bounds__(kT) k_residual64(int64_t n, const int32_t* __r
 
 // ---------------------------------------------------------------------------
 // FP64 CG iteration
-template <bool D16>
-__global__ void __launch_bounds__(kT) k_cg64_spmv(int64_t n, const int32_t* __restrict__ sptr,
-                                                  const void* __restrict__ col, const double* __restrict__ val,
-                                                  const double* __restrict__ p, double* __restrict__ q, CgState* st,
-                                                  double* partials) {
+// Column pattern access of a sliced-ELL operator (see Sell::spat).
+struct SellPat {
+  const int32_t* spat;
+  const int16_t* pat;
+  int period;
+};
+
+// Matrix entries of one sliced-ELL row held in registers.  In a slice with a
+// uniform column pattern the gather indices come from the (warp-uniform, cached)
+// slice pattern and do not wait for per-row column loads.
+template <class V, bool D16, int MAXW>
+struct RowRegs {
+  V v[MAXW];
+  int j[MAXW];
+  int w;
+  __device__ __forceinline__ void load(const int32_t* __restrict__ sptr, const void* __restrict__ col,
+                                       const SellPat& sp, const V* __restrict__ val, int64_t r, int64_t n) {
+    int64_t base = 0;
+    w = 0;
+    int32_t so = -1;
+    if (r < n) {
+      sell_row(sptr, r, base, w);
+      so = __ldg(sp.spat + (r >> 5));
+    }
+    const int16_t* pp = sp.pat + (so < 0 ? 0 : so) + (sp.period == 2 ? (int)(r & 1) * w : 0);
+#pragma unroll
+    for (int k = 0; k < MAXW; k++) {
+      v[k] = k < w ? __ldg(val + base + 32 * k) : V(0);
+      int jk = (int)r;
+      if (k < w) jk = so >= 0 ? (int)r + (int)__ldg(pp + k) : colof<D16>(col, base + 32 * k, r);
+      j[k] = jk;
+    }
+  }
+};
+
+// q = K~ p (FP64, standard form) and p.q.  PF: software pipelining (the next row's
+// entries are loaded while the current row's gathers are in flight).
+template <bool D16, int MAXW, bool PF>
+__global__ void __launch_bounds__(kT, PF ? 4 : 1) k_cg64_spmv(int64_t n, const int32_t* __restrict__ sptr,
+                                                              const void* __restrict__ col, SellPat sp,
+                                                              const double* __restrict__ val,
+                                                              const double* __restrict__ p, double* __restrict__ q,
+                                                              CgState* st, double* partials) {
   if (st->done) return;
   double acc = 0.0;
-  for (int64_t r = gtid(); r < n; r += gstride()) {
-    const int64_t base = (int64_t)sptr[r >> 5] + (r & 31);
-    const int w = (sptr[(r >> 5) + 1] - sptr[r >> 5]) >> 5;
-    double s = 0.0;
-    for (int k = 0; k < w; k++) {
-      const int64_t idx = base + 32 * (int64_t)k;
-      s = fma(val[idx], p[colof<D16>(col, idx, r)], s);
+  if constexpr (MAXW > 0) {
+    RowRegs<double, D16, MAXW> cur, nxt;
+    int64_t r = gtid();
+    if (PF) cur.load(sptr, col, sp, val, r, n);
+    for (; r < n; r += gstride()) {
+      if (PF) nxt.load(sptr, col, sp, val, r + gstride(), n);
+      else cur.load(sptr, col, sp, val, r, n);
+      double s = 0.0;
+#pragma unroll
+      for (int k = 0; k < MAXW; k++)
+        if (k < cur.w) s = fma(cur.v[k], __ldg(p + cur.j[k]), s);
+      q[r] = s;
+      acc = fma(__ldg(p + r), s, acc);
+      if (PF) cur = nxt;
     }
-    q[r] = s;
-    acc = fma(p[r], s, acc);
+  } else {
+    for (int64_t r = gtid(); r < n; r += gstride()) {
+      int64_t base;
+      int w;
+      sell_row(sptr, r, base, w);
+      double s = 0.0;
+      for (int k = 0; k < w; k++) {
+        const int64_t idx = base + 32 * (int64_t)k;
+        s = fma(val[idx], p[colof<D16>(col, idx, r)], s);
+      }
+      q[r] = s;
+      acc = fma(p[r], s, acc);
+    }
   }
-  double v[1] = {acc}, tot[1];
-  if (reduce_grid<double, 1>(v, partials, &st->counter[0], tot) && threadIdx.x == 0) {
+  double v1[1] = {acc}, tot[1];
+  if (reduce_grid<double, 1>(v1, partials, &st->counter[0], tot) && threadIdx.x == 0) {
     const double pq = tot[0];
     if (!(pq > 0.0) || !isfinite(pq)) st->done = 2;
     else st->alpha = st->rho / pq;
@@ -279,7 +374,22 @@ __global__ void __launch_bounds__(kT) k_cg64_update(int64_t n, double* __restric
   if (st->done) return;
   const double a = st->alpha;
   double acc = 0.0;
-  for (int64_t i = gtid(); i < n; i += gstride()) {
+  const int64_t n2 = n >> 1;
+  for (int64_t v2 = gtid(); v2 < n2; v2 += gstride()) {
+    const double2 pp = __ldg(reinterpret_cast<const double2*>(p) + v2);
+    const double2 qq = __ldg(reinterpret_cast<const double2*>(q) + v2);
+    double2 yy = reinterpret_cast<double2*>(y)[v2];
+    double2 rr = reinterpret_cast<double2*>(r)[v2];
+    yy.x = fma(a, pp.x, yy.x);
+    yy.y = fma(a, pp.y, yy.y);
+    rr.x = fma(-a, qq.x, rr.x);
+    rr.y = fma(-a, qq.y, rr.y);
+    reinterpret_cast<double2*>(y)[v2] = yy;
+    reinterpret_cast<double2*>(r)[v2] = rr;
+    acc = fma(rr.x, rr.x, acc);
+    acc = fma(rr.y, rr.y, acc);
+  }
+  for (int64_t i = 2 * n2 + gtid(); i < n; i += gstride()) {
     y[i] = fma(a, p[i], y[i]);
     const double ri = fma(-a, q[i], r[i]);
     r[i] = ri;
@@ -304,69 +414,161 @@ __global__ void __launch_bounds__(kT) k_cg64_p(int64_t n, const double* __restri
                                                const CgState* st) {
   if (st->done) return;
   const double bt = st->beta;
-  for (int64_t i = gtid(); i < n; i += gstride()) p[i] = fma(bt, p[i], r[i]);
+  const int64_t n2 = n >> 1;
+  for (int64_t v2 = gtid(); v2 < n2; v2 += gstride()) {
+    const double2 rr = __ldg(reinterpret_cast<const double2*>(r) + v2);
+    double2 pp = reinterpret_cast<double2*>(p)[v2];
+    pp.x = fma(bt, pp.x, rr.x);
+    pp.y = fma(bt, pp.y, rr.y);
+    reinterpret_cast<double2*>(p)[v2] = pp;
+  }
+  for (int64_t i = 2 * n2 + gtid(); i < n; i += gstride()) p[i] = fma(bt, p[i], r[i]);
 }
 
 // ---------------------------------------------------------------------------
 // FP32 inner iteration of the mixed solve.  The two p buffers alternate: the
 // iteration with counter it reads p_old = P[it&1] and writes p_new = P[(it+1)&1],
-// P = {pa, pb}.
-template <bool D16>
-__global__ void __launch_bounds__(kT) k_cg32_spmv(int64_t n, const int32_t* __restrict__ sptr,
-                                                  const void* __restrict__ col, const float* __restrict__ val,
-                                                  const float* __restrict__ r, float* pa, float* pb,
-                                                  float* __restrict__ q, CgState* st, float* partials) {
+// P = {pa, pb}.  The SpMV uses the difference form of k_scale_values: the diagonal
+// slot (and zero padding, column = row) multiplies p_i, an off-diagonal slot
+// multiplies s_j p_j - s_i p_i.
+template <bool D16, int MAXW, bool PF>
+__global__ void __launch_bounds__(kT, PF ? 4 : 1) k_cg32_spmv(int64_t n, const int32_t* __restrict__ sptr,
+                                                              const void* __restrict__ col, SellPat sp,
+                                                              const float* __restrict__ val,
+                                                              const float* __restrict__ sc,
+                                                              const float* __restrict__ r, float* pa, float* pb,
+                                                              float* __restrict__ q, CgState* st, double* partials) {
   if (st->done) return;
   const int it = st->iters;
   const float* __restrict__ pold = (it & 1) ? pb : pa;
   float* __restrict__ pnew = (it & 1) ? pa : pb;
   const float ar = (float)st->ar, ap = (float)st->ap;
   float acc = 0.0f;
-  for (int64_t row = gtid(); row < n; row += gstride()) {
-    const int64_t base = (int64_t)sptr[row >> 5] + (row & 31);
-    const int w = (sptr[(row >> 5) + 1] - sptr[row >> 5]) >> 5;
-    float s = 0.0f;
-    for (int k = 0; k < w; k++) {
-      const int64_t idx = base + 32 * (int64_t)k;
-      const int64_t j = colof<D16>(col, idx, row);
-      const float pj = fmaf(ap, pold[j], ar * r[j]);
-      s = fmaf(val[idx], pj, s);
+  if constexpr (MAXW > 0) {
+    RowRegs<float, D16, MAXW> cur, nxt;
+    int64_t row = gtid();
+    if (PF) cur.load(sptr, col, sp, val, row, n);
+    for (; row < n; row += gstride()) {
+      if (PF) nxt.load(sptr, col, sp, val, row + gstride(), n);
+      else cur.load(sptr, col, sp, val, row, n);
+      const float pr = fmaf(ap, __ldg(pold + row), ar * __ldg(r + row));
+      const float zr = __ldg(sc + row) * pr;
+      float s = 0.0f;
+#pragma unroll
+      for (int k = 0; k < MAXW; k++) {
+        if (k < cur.w) {
+          const int j = cur.j[k];
+          const float pj = fmaf(ap, __ldg(pold + j), ar * __ldg(r + j));
+          const float t = (j == row) ? pr : fmaf(__ldg(sc + j), pj, -zr);
+          s = fmaf(cur.v[k], t, s);
+        }
+      }
+      pnew[row] = pr;
+      q[row] = s;
+      acc = fmaf(pr, s, acc);
+      if (PF) cur = nxt;
     }
-    const float pr = fmaf(ap, pold[row], ar * r[row]);
-    pnew[row] = pr;
-    q[row] = s;
-    acc = fmaf(pr, s, acc);
+  } else {
+    for (int64_t row = gtid(); row < n; row += gstride()) {
+      int64_t base;
+      int w;
+      sell_row(sptr, row, base, w);
+      const float pr = fmaf(ap, pold[row], ar * r[row]);
+      const float zr = sc[row] * pr;
+      float s = 0.0f;
+      for (int k = 0; k < w; k++) {
+        const int64_t idx = base + 32 * (int64_t)k;
+        const int j = colof<D16>(col, idx, row);
+        const float pj = fmaf(ap, pold[j], ar * r[j]);
+        const float t = (j == row) ? pr : fmaf(sc[j], pj, -zr);
+        s = fmaf(val[idx], t, s);
+      }
+      pnew[row] = pr;
+      q[row] = s;
+      acc = fmaf(pr, s, acc);
+    }
   }
-  float v[1] = {acc}, tot[1];
-  if (reduce_grid<float, 1>(v, partials, &st->counter[0], tot) && threadIdx.x == 0) {
-    const double pq = (double)tot[0];
+  // per-thread partials in FP32, combined across threads and blocks in FP64
+  double v1[1] = {(double)acc}, tot[1];
+  if (reduce_grid<double, 1>(v1, partials, &st->counter[0], tot) && threadIdx.x == 0) {
+    const double pq = tot[0];
     if (!(pq > 0.0) || !isfinite(pq)) st->done = 2;
     else st->alpha = st->rho / pq;
   }
 }
 
-__global__ void __launch_bounds__(kT) k_cg32_update(int64_t n, float* __restrict__ y, float* __restrict__ r,
-                                                    const float* pa, const float* pb, const float* __restrict__ q,
-                                                    CgState* st, float* partials) {
+// x/r update of the mixed iteration: residual and its norm in FP32; the solution
+// correction y += alpha p accumulated in an FP32 hi+lo pair with error-free
+// transformations (two-product, two-sum), i.e. about 48 bits without FP64
+// instructions.  A plain FP32 accumulator would add rounding noise of size
+// 2^-24 |y| that the operator amplifies by its largest eigenvalue.
+// (h, l) += a * p as an unevaluated FP32 pair: two-product of a*p, two-sum with h,
+// renormalisation.  Explicitly rounded intrinsics keep the compiler from fusing
+// or reassociating the error terms.
+__device__ __forceinline__ void df_axpy(float& h, float& l, float a, float p) {
+  const float ph = __fmul_rn(a, p);
+  const float pl = fmaf(a, p, -ph);
+  const float s = __fadd_rn(h, ph);
+  const float bb = __fsub_rn(s, h);
+  float e = __fadd_rn(__fsub_rn(h, __fsub_rn(s, bb)), __fsub_rn(ph, bb));
+  e = __fadd_rn(e, __fadd_rn(l, pl));
+  const float hi = __fadd_rn(s, e);
+  l = __fsub_rn(e, __fsub_rn(hi, s));
+  h = hi;
+}
+
+__global__ void __launch_bounds__(kT) k_cg32_update(int64_t n, float* __restrict__ yh, float* __restrict__ yl,
+                                                    float* __restrict__ r, const float* pa, const float* pb,
+                                                    const float* __restrict__ q, CgState* st, double* partials) {
   if (st->done) return;
   const int it = st->iters;
   const float* __restrict__ pnew = (it & 1) ? pa : pb;
   const float a = (float)st->alpha;
   float acc = 0.0f;
-  for (int64_t i = gtid(); i < n; i += gstride()) {
-    y[i] = fmaf(a, pnew[i], y[i]);
+  // four entries per thread and step (16-byte loads and stores), then the tail
+  const int64_t n4 = n >> 2;
+  for (int64_t v4 = gtid(); v4 < n4; v4 += gstride()) {
+    const float4 p = __ldg(reinterpret_cast<const float4*>(pnew) + v4);
+    const float4 qq = __ldg(reinterpret_cast<const float4*>(q) + v4);
+    float4 h = reinterpret_cast<float4*>(yh)[v4];
+    float4 l = reinterpret_cast<float4*>(yl)[v4];
+    float4 rr = reinterpret_cast<float4*>(r)[v4];
+    df_axpy(h.x, l.x, a, p.x);
+    df_axpy(h.y, l.y, a, p.y);
+    df_axpy(h.z, l.z, a, p.z);
+    df_axpy(h.w, l.w, a, p.w);
+    rr.x = fmaf(-a, qq.x, rr.x);
+    rr.y = fmaf(-a, qq.y, rr.y);
+    rr.z = fmaf(-a, qq.z, rr.z);
+    rr.w = fmaf(-a, qq.w, rr.w);
+    reinterpret_cast<float4*>(yh)[v4] = h;
+    reinterpret_cast<float4*>(yl)[v4] = l;
+    reinterpret_cast<float4*>(r)[v4] = rr;
+    acc = fmaf(rr.x, rr.x, acc);
+    acc = fmaf(rr.y, rr.y, acc);
+    acc = fmaf(rr.z, rr.z, acc);
+    acc = fmaf(rr.w, rr.w, acc);
+  }
+  for (int64_t i = 4 * n4 + gtid(); i < n; i += gstride()) {
+    float h = yh[i], l = yl[i];
+    df_axpy(h, l, a, pnew[i]);
+    yh[i] = h;
+    yl[i] = l;
     const float ri = fmaf(-a, q[i], r[i]);
     r[i] = ri;
     acc = fmaf(ri, ri, acc);
   }
-  float v[1] = {acc}, tot[1];
-  if (reduce_grid<float, 1>(v, partials + gridDim.x, &st->counter[2], tot) && threadIdx.x == 0) {
-    const double rn = (double)tot[0];
+  double v[1] = {(double)acc}, tot[1];
+  if (reduce_grid<double, 1>(v, partials + gridDim.x, &st->counter[2], tot) && threadIdx.x == 0) {
+    const double rn = tot[0];
     st->iters = it + 1;
     st->rho_new = rn;
     if (!isfinite(rn)) st->done = 2;
-    else if (rn <= st->ru2 || rn <= st->stop2) st->done = 3;
-    else if (st->iters >= st->max_iter) st->done = 3;  // final FP64 check decides
+    else if (rn <= st->stop2) {
+      st->final_req = 1;
+      st->done = 3;
+    } else if (rn <= st->ru2) st->done = 3;
+    else if (st->iters >= st->max_iter) st->done = 3;  // the FP64 check decides
     else {
       const double beta = rn / st->rho;
       st->ar = 1.0;
@@ -376,20 +578,25 @@ __global__ void __launch_bounds__(kT) k_cg32_update(int64_t n, float* __restrict
   }
 }
 
-// fold the FP32 iterate into the FP64 solution: y64 += y32, y32 = 0
-__global__ void __launch_bounds__(kT) k_fold(int64_t n, double* __restrict__ y64, float* __restrict__ y32,
-                                             const CgState* st, int force) {
+// fold the correction into the FP64 solution: y64 += hi + lo, hi = lo = 0
+__global__ void __launch_bounds__(kT) k_fold(int64_t n, double* __restrict__ y64, float* __restrict__ yh,
+                                             float* __restrict__ yl, const CgState* st, int force) {
   if (!force && st->done != 3) return;
   for (int64_t i = gtid(); i < n; i += gstride()) {
-    y64[i] += (double)y32[i];
-    y32[i] = 0.0f;
+    y64[i] += (double)yh[i] + (double)yl[i];
+    yh[i] = 0.0f;
+    yl[i] = 0.0f;
   }
 }
 
+// u = S y; rows tagged 1 (Dirichlet) get their prescribed value exactly (or 0)
 __global__ void k_unscale(int64_t n, const double* __restrict__ y, const float* __restrict__ s,
+                          const uint8_t* __restrict__ fix, const double* __restrict__ fixval,
                           double* __restrict__ u) {
   const int64_t i = gtid();
-  if (i < n) u[i] = (double)s[i] * y[i];
+  if (i >= n) return;
+  if (fix && fix[i] == 1) u[i] = fixval ? fixval[i] : 0.0;
+  else u[i] = (double)s[i] * y[i];
 }
 
 // y = K x = S^-1 K~ S^-1 x
@@ -399,18 +606,42 @@ __global__ void k_apply(int64_t n, const int32_t* __restrict__ sptr, const void*
                         double* __restrict__ y) {
   const int64_t r = gtid();
   if (r >= n) return;
-  const int64_t base = (int64_t)sptr[r >> 5] + (r & 31);
-  const int w = (sptr[(r >> 5) + 1] - sptr[r >> 5]) >> 5;
+  int64_t base;
+  int w;
+  sell_row(sptr, r, base, w);
   double acc = 0.0;
   for (int k = 0; k < w; k++) {
     const int64_t idx = base + 32 * (int64_t)k;
-    const int64_t j = colof<D16>(col, idx, r);
+    const int j = colof<D16>(col, idx, r);
     acc = fma(val[idx], x[j] / (double)s[j], acc);
   }
   y[r] = acc / (double)s[r];
 }
 
 // ---------------------------------------------------------------------------
+// dispatch on the column format and the widest slice
+#define ADFEM_SELL_DISPATCH_PF(A, KERNEL, PF, GRID, STREAM, ...)                           \
+  do {                                                                                     \
+    if ((A).delta16) {                                                                     \
+      if ((A).maxw <= 8) KERNEL<true, 8, PF><<<GRID, kT, 0, STREAM>>>(__VA_ARGS__);        \
+      else if ((A).maxw <= 16) KERNEL<true, 16, PF><<<GRID, kT, 0, STREAM>>>(__VA_ARGS__); \
+      else KERNEL<true, 0, PF><<<GRID, kT, 0, STREAM>>>(__VA_ARGS__);                      \
+    } else {                                                                               \
+      if ((A).maxw <= 8) KERNEL<false, 8, PF><<<GRID, kT, 0, STREAM>>>(__VA_ARGS__);       \
+      else if ((A).maxw <= 16) KERNEL<false, 16, PF><<<GRID, kT, 0, STREAM>>>(__VA_ARGS__); \
+      else KERNEL<false, 0, PF><<<GRID, kT, 0, STREAM>>>(__VA_ARGS__);                     \
+    }                                                                                      \
+  } while (0)
+#define ADFEM_SELL_DISPATCH(S, KERNEL, GRID, STREAM, ...)                                  \
+  do {                                                                                     \
+    if ((S).prefetch) ADFEM_SELL_DISPATCH_PF(*(S).A, KERNEL, true, GRID, STREAM, __VA_ARGS__); \
+    else ADFEM_SELL_DISPATCH_PF(*(S).A, KERNEL, false, GRID, STREAM, __VA_ARGS__);         \
+  } while (0)
+
+static SellPat sell_pat(const Sell& A) {
+  return SellPat{A.spat.as<int32_t>(), A.pat.as<int16_t>(), A.pat_period};
+}
+
 Solver::~Solver() {
   if (g64) cudaGraphExecDestroy(g64);
   if (g32) cudaGraphExecDestroy(g32);
@@ -421,6 +652,15 @@ Solver::~Solver() {
   if (h_state) cudaFreeHost(h_state);
 }
 
+template <class F>
+static int resident_grid(F kernel, int sms, int64_t need, int* grid) {
+  int per = 0;
+  ADFEM_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kernel, kT, 0));
+  per = std::max(1, std::min(per, kMaxBlocksPerSM));
+  *grid = (int)std::max<int64_t>(1, std::min<int64_t>(need, (int64_t)sms * per));
+  return ADFEM_OK;
+}
+
 int Solver::init(const Sell* A_, int64_t n_) {
   A = A_;
   n = n_;
@@ -428,10 +668,36 @@ int Solver::init(const Sell* A_, int64_t n_) {
   ADFEM_CUDA(cudaGetDevice(&dev));
   ADFEM_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
   const int64_t need = (n + kT - 1) / kT;
-  grid = (int)std::max<int64_t>(1, std::min<int64_t>(need, (int64_t)sms * kBlocksPerSM));
+  // one grid for all grid-stride vector kernels: the smallest resident grid among them
+  {
+    int g = 0;
+    ADFEM_TRY(resident_grid(k_cg32_update, sms, need, &grid));
+    ADFEM_TRY(resident_grid(k_cg64_update, sms, need, &g));
+    grid = std::min(grid, g);
+    ADFEM_TRY(resident_grid(k_cg64_p, sms, need, &g));
+    grid = std::min(grid, g);
+    ADFEM_TRY(resident_grid(k_fold, sms, need, &g));
+    grid = std::min(grid, g);
+    ADFEM_TRY(resident_grid(k_init, sms, need, &g));
+    grid = std::min(grid, g);
+    ADFEM_TRY(resident_grid(k_residual64<true>, sms, need, &g));
+    grid = std::min(grid, g);
+  }
+  const char* pf = std::getenv("ADFEM_SPMV_PREFETCH");
+  prefetch = pf && pf[0] == '1';
+  int g2 = 0, g3 = 0;
+  const bool w8 = A->maxw <= 8;
+  if (prefetch) {
+    ADFEM_TRY(resident_grid(w8 ? k_cg32_spmv<true, 8, true> : k_cg32_spmv<true, 16, true>, sms, need, &g2));
+    ADFEM_TRY(resident_grid(w8 ? k_cg64_spmv<true, 8, true> : k_cg64_spmv<true, 16, true>, sms, need, &g3));
+  } else {
+    ADFEM_TRY(resident_grid(w8 ? k_cg32_spmv<true, 8, false> : k_cg32_spmv<true, 16, false>, sms, need, &g2));
+    ADFEM_TRY(resident_grid(w8 ? k_cg64_spmv<true, 8, false> : k_cg64_spmv<true, 16, false>, sms, need, &g3));
+  }
+  grid_spmv = std::min(g2, g3);
   ADFEM_TRY(state.alloc(sizeof(CgState)));
   ADFEM_CUDA(cudaMemset(state.p, 0, sizeof(CgState)));
-  ADFEM_TRY(partials.alloc(sizeof(double) * 4 * (size_t)grid));
+  ADFEM_TRY(partials.alloc(sizeof(double) * 4 * (size_t)std::max(grid, grid_spmv)));
   const size_t n8 = sizeof(double) * (size_t)n, n4 = sizeof(float) * (size_t)n;
   ADFEM_TRY(s32.alloc(n4));
   ADFEM_TRY(b.alloc(n8));
@@ -439,11 +705,12 @@ int Solver::init(const Sell* A_, int64_t n_) {
   ADFEM_TRY(r64.alloc(n8));
   ADFEM_TRY(p64.alloc(n8));
   ADFEM_TRY(q64.alloc(n8));
-  ADFEM_TRY(y32.alloc(n4));
   ADFEM_TRY(r32.alloc(n4));
   ADFEM_TRY(pa32.alloc(n4));
   ADFEM_TRY(pb32.alloc(n4));
   ADFEM_TRY(q32.alloc(n4));
+  ADFEM_TRY(yh32.alloc(n4));
+  ADFEM_TRY(yl32.alloc(n4));
   if (!h_state) ADFEM_CUDA(cudaMallocHost(&h_state, 2 * sizeof(CgState)));
   if (!stream) ADFEM_CUDA(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
   for (auto& e : ev)
@@ -454,21 +721,21 @@ int Solver::init(const Sell* A_, int64_t n_) {
 int solver_prepare(Solver& S, const int32_t* diagpos_dev, cudaStream_t user) {
   const Sell& A = *S.A;
   S.prepared = false;
+  if (!diagpos_dev) return fail(ADFEM_ERR_INVALID, "solver_prepare: diagonal positions required");
   DevBuf bad;
   ADFEM_TRY(bad.alloc(sizeof(int)));
   ADFEM_CUDA(cudaMemsetAsync(bad.p, 0, sizeof(int), user));
   const unsigned nb = (unsigned)((S.n + kT - 1) / kT);
-  if (A.delta16) {
-    k_scale_diag<true><<<nb, kT, 0, user>>>(S.n, A.sptr.as<int32_t>(), A.col.p, A.val64.as<double>(), diagpos_dev,
-                                            S.s32.as<float>(), bad.as<int>());
+  k_scale_diag<<<nb, kT, 0, user>>>(S.n, A.sptr.as<int32_t>(), A.val64.as<double>(), diagpos_dev, S.s32.as<float>(),
+                                    bad.as<int>());
+  if (A.delta16)
     k_scale_values<true><<<nb, kT, 0, user>>>(S.n, A.sptr.as<int32_t>(), A.col.p, A.val64.as<double>(),
-                                              A.val32.as<float>(), S.s32.as<float>());
-  } else {
-    k_scale_diag<false><<<nb, kT, 0, user>>>(S.n, A.sptr.as<int32_t>(), A.col.p, A.val64.as<double>(), diagpos_dev,
-                                             S.s32.as<float>(), bad.as<int>());
+                                              A.valD64.as<double>(), A.val32.as<float>(), S.s32.as<float>(),
+                                              diagpos_dev);
+  else
     k_scale_values<false><<<nb, kT, 0, user>>>(S.n, A.sptr.as<int32_t>(), A.col.p, A.val64.as<double>(),
-                                               A.val32.as<float>(), S.s32.as<float>());
-  }
+                                               A.valD64.as<double>(), A.val32.as<float>(), S.s32.as<float>(),
+                                               diagpos_dev);
   ADFEM_CUDA(cudaGetLastError());
   int hbad = 0;
   ADFEM_CUDA(cudaMemcpyAsync(&hbad, bad.p, sizeof(int), cudaMemcpyDeviceToHost, user));
@@ -525,12 +792,8 @@ static void enqueue_cg64(Solver& S, cudaStream_t st, Timer* tm = nullptr) {
   auto* cs = S.state.as<CgState>();
   auto* part = S.partials.as<double>();
   tm->run(0, st, [&] {
-    if (A.delta16)
-      k_cg64_spmv<true><<<S.grid, kT, 0, st>>>(S.n, sp, A.col.p, A.val64.as<double>(), S.p64.as<double>(),
-                                               S.q64.as<double>(), cs, part);
-    else
-      k_cg64_spmv<false><<<S.grid, kT, 0, st>>>(S.n, sp, A.col.p, A.val64.as<double>(), S.p64.as<double>(),
-                                                S.q64.as<double>(), cs, part);
+    ADFEM_SELL_DISPATCH(S, k_cg64_spmv, S.grid_spmv, st, S.n, sp, A.col.p, sell_pat(A), A.val64.as<double>(),
+                        S.p64.as<double>(), S.q64.as<double>(), cs, part);
   });
   tm->run(1, st, [&] {
     k_cg64_update<<<S.grid, kT, 0, st>>>(S.n, S.y64.as<double>(), S.r64.as<double>(), S.p64.as<double>(),
@@ -545,16 +808,18 @@ static void enqueue_residual(Solver& S, cudaStream_t st, int mode, int force, Ti
   const Sell& A = *S.A;
   auto* sp = A.sptr.as<int32_t>();
   tm->run(3, st, [&] {
-  if (A.delta16)
-    k_residual64<true><<<S.grid, kT, 0, st>>>(S.n, sp, A.col.p, A.val64.as<double>(), S.b.as<double>(),
-                                              S.y64.as<double>(), S.r64.as<double>(), S.p64.as<double>(),
-                                              S.r32.as<float>(), S.pa32.as<float>(), S.pb32.as<float>(),
-                                              S.state.as<CgState>(), S.partials.as<double>(), mode, force);
-  else
-    k_residual64<false><<<S.grid, kT, 0, st>>>(S.n, sp, A.col.p, A.val64.as<double>(), S.b.as<double>(),
-                                               S.y64.as<double>(), S.r64.as<double>(), S.p64.as<double>(),
-                                               S.r32.as<float>(), S.pa32.as<float>(), S.pb32.as<float>(),
-                                               S.state.as<CgState>(), S.partials.as<double>(), mode, force);
+    if (A.delta16)
+      k_residual64<true><<<S.grid, kT, 0, st>>>(S.n, sp, A.col.p, A.valD64.as<double>(), S.s32.as<float>(),
+                                                S.b.as<double>(), S.y64.as<double>(), S.r64.as<double>(),
+                                                S.p64.as<double>(), S.r32.as<float>(), S.pa32.as<float>(),
+                                                S.pb32.as<float>(), S.state.as<CgState>(), S.partials.as<double>(),
+                                                mode, force);
+    else
+      k_residual64<false><<<S.grid, kT, 0, st>>>(S.n, sp, A.col.p, A.valD64.as<double>(), S.s32.as<float>(),
+                                                 S.b.as<double>(), S.y64.as<double>(), S.r64.as<double>(),
+                                                 S.p64.as<double>(), S.r32.as<float>(), S.pa32.as<float>(),
+                                                 S.pb32.as<float>(), S.state.as<CgState>(), S.partials.as<double>(),
+                                                 mode, force);
   });
 }
 
@@ -564,26 +829,25 @@ static void enqueue_cg32(Solver& S, cudaStream_t st, Timer* tm = nullptr) {
   const Sell& A = *S.A;
   auto* sp = A.sptr.as<int32_t>();
   auto* cs = S.state.as<CgState>();
-  auto* part = reinterpret_cast<float*>(S.partials.p);
+  auto* part = S.partials.as<double>();
   tm->run(0, st, [&] {
-    if (A.delta16)
-      k_cg32_spmv<true><<<S.grid, kT, 0, st>>>(S.n, sp, A.col.p, A.val32.as<float>(), S.r32.as<float>(),
-                                               S.pa32.as<float>(), S.pb32.as<float>(), S.q32.as<float>(), cs, part);
-    else
-      k_cg32_spmv<false><<<S.grid, kT, 0, st>>>(S.n, sp, A.col.p, A.val32.as<float>(), S.r32.as<float>(),
-                                                S.pa32.as<float>(), S.pb32.as<float>(), S.q32.as<float>(), cs, part);
+    ADFEM_SELL_DISPATCH(S, k_cg32_spmv, S.grid_spmv, st, S.n, sp, A.col.p, sell_pat(A), A.val32.as<float>(),
+                        S.s32.as<float>(), S.r32.as<float>(), S.pa32.as<float>(), S.pb32.as<float>(),
+                        S.q32.as<float>(), cs, part);
   });
   tm->run(1, st, [&] {
-    k_cg32_update<<<S.grid, kT, 0, st>>>(S.n, S.y32.as<float>(), S.r32.as<float>(), S.pa32.as<float>(),
-                                         S.pb32.as<float>(), S.q32.as<float>(), cs, part);
+    k_cg32_update<<<S.grid, kT, 0, st>>>(S.n, S.yh32.as<float>(), S.yl32.as<float>(), S.r32.as<float>(),
+                                         S.pa32.as<float>(), S.pb32.as<float>(), S.q32.as<float>(), cs, part);
   });
 }
 
+// fold + FP64 residual replacement of the mixed solve (both return at entry unless due)
 static void enqueue_reliable_update(Solver& S, cudaStream_t st, int force, Timer* tm = nullptr) {
   Timer none;
   if (!tm) tm = &none;
   tm->run(2, st, [&] {
-    k_fold<<<S.grid, kT, 0, st>>>(S.n, S.y64.as<double>(), S.y32.as<float>(), S.state.as<CgState>(), force);
+    k_fold<<<S.grid, kT, 0, st>>>(S.n, S.y64.as<double>(), S.yh32.as<float>(), S.yl32.as<float>(),
+                                  S.state.as<CgState>(), force);
   });
   enqueue_residual(S, st, 1, force, tm);
 }
@@ -616,8 +880,9 @@ static int capture_chunk(Solver& S, bool mixed, int chunk, cudaGraphExec_t* out)
   return ADFEM_OK;
 }
 
-int solver_solve(Solver& S, const double* rhs, double* u, const uint8_t* zero_rows, const adfem_solver_opts& o,
-                 adfem_solver_stats* stats, cudaStream_t user, SolveProfile* prof) {
+int solver_solve(Solver& S, const double* rhs, double* u, const uint8_t* zero_rows, const uint8_t* fix_rows,
+                 const double* fix_vals, const adfem_solver_opts& o, adfem_solver_stats* stats, cudaStream_t user,
+                 SolveProfile* prof) {
   if (!S.prepared) return fail(ADFEM_ERR_INVALID, "solver: operator not prepared");
   const bool mixed = o.precision == ADFEM_PREC_MIXED;
   if (o.precision != ADFEM_PREC_FP64 && !mixed) return fail(ADFEM_ERR_INVALID, "solver: unknown precision");
@@ -653,9 +918,10 @@ int solver_solve(Solver& S, const double* rhs, double* u, const uint8_t* zero_ro
                                 o.rtol * o.rtol);
   ADFEM_CUDA(cudaGetLastError());
   if (mixed) {
-    ADFEM_CUDA(cudaMemsetAsync(S.y32.p, 0, sizeof(float) * S.n, st));
     ADFEM_CUDA(cudaMemsetAsync(S.pa32.p, 0, sizeof(float) * S.n, st));
     ADFEM_CUDA(cudaMemsetAsync(S.pb32.p, 0, sizeof(float) * S.n, st));
+    ADFEM_CUDA(cudaMemsetAsync(S.yh32.p, 0, sizeof(float) * S.n, st));
+    ADFEM_CUDA(cudaMemsetAsync(S.yl32.p, 0, sizeof(float) * S.n, st));
     enqueue_residual(S, st, 1, 1);
   } else {
     enqueue_residual(S, st, 0, 1);
@@ -704,12 +970,18 @@ int solver_solve(Solver& S, const double* rhs, double* u, const uint8_t* zero_ro
       slot = 1 - slot;
     }
   }
-  // final FP64 residual (the mixed path's stop test already is one; recompute for both)
-  if (mixed) k_fold<<<S.grid, kT, 0, st>>>(S.n, S.y64.as<double>(), S.y32.as<float>(), S.state.as<CgState>(), 1);
+  // final fold (mixed), FP64 residual (difference form) for the report, then u = S y
+  // with the Dirichlet rows set exactly
+  if (mixed) {
+    k_fold<<<S.grid, kT, 0, st>>>(S.n, S.y64.as<double>(), S.yh32.as<float>(), S.yl32.as<float>(),
+                                  S.state.as<CgState>(), 1);
+    launches += 1;
+  }
   enqueue_residual(S, st, 2, 1);
-  k_unscale<<<(unsigned)((S.n + kT - 1) / kT), kT, 0, st>>>(S.n, S.y64.as<double>(), S.s32.as<float>(), u);
+  k_unscale<<<(unsigned)((S.n + kT - 1) / kT), kT, 0, st>>>(S.n, S.y64.as<double>(), S.s32.as<float>(), fix_rows,
+                                                           fix_vals, u);
   ADFEM_CUDA(cudaGetLastError());
-  launches += mixed ? 3 : 2;
+  launches += 2;
   ADFEM_CUDA(cudaMemcpyAsync(&S.h_state[0], S.state.p, sizeof(CgState), cudaMemcpyDeviceToHost, st));
   ADFEM_CUDA(cudaEventRecord(S.ev[3], st));
   ADFEM_CUDA(cudaEventSynchronize(S.ev[3]));

@@ -20,19 +20,25 @@ struct CgState {
   int max_iter;
   int done;            // 0 running, 1 converged, 2 breakdown, 3 residual replacement due, 4 max_iter
   int updates;         // residual replacements done (mixed)
+  int final_req;       // mixed: the last replacement was requested because the FP32 residual met rtol
+  int floor_hit;       // mixed: stopped at the attainable accuracy of the FP64 residual
+  double last_rr64;    // mixed: FP64 residual norm^2 at the previous replacement
   unsigned counter[4]; // last-block arrival counters (returned to 0 by the last block)
 };
 
 struct Solver {
   int64_t n = 0;
-  int grid = 0;            // blocks of the reduction kernels (grid-stride)
+  int grid = 0;            // blocks of the grid-stride kernels (resident blocks per SM x SMs)
+  int grid_spmv = 0;       // same for the unrolled SpMV kernels (higher register use)
+  bool prefetch = false;   // SpMV software pipelining (ADFEM_SPMV_PREFETCH=1)
   const Sell* A = nullptr; // sliced-ELL operator (val64 scaled in place, val32 scaled copy)
   DevBuf s32;              // Jacobi scaling s_i = 1/sqrt(K_ii) (float, exact in double)
   DevBuf state;            // CgState
   DevBuf partials;         // 4 * grid doubles
   DevBuf b;                // scaled rhs (FP64)
   DevBuf y64, r64, p64, q64;
-  DevBuf y32, r32, pa32, pb32, q32;
+  DevBuf r32, pa32, pb32, q32;
+  DevBuf yh32, yl32;       // mixed: solution correction since the last fold, as an FP32 hi+lo pair
   CgState* h_state = nullptr;  // pinned, 2 slots
   cudaStream_t stream = nullptr;
   cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
@@ -44,8 +50,8 @@ struct Solver {
   int init(const Sell* A, int64_t n);
 };
 
-// scale the operator: s_i = rsqrt(K_ii) (FP32), val64 <- s_i K_ij s_j, val32 <- (float) val64.
-// diagpos: entry index k of the diagonal within row i (null: search by column).
+// scale the operator: s_i = rsqrt(K_ii) (FP32), val64 <- s_i K_ij s_j, val32 <- the FP32
+// difference-form copy (see k_scale_values).  diagpos: entry index k of the diagonal in row i.
 int solver_prepare(Solver& S, const int32_t* diagpos_dev, cudaStream_t user);
 // Per-kernel timing of a profiled solve: 0 SpMV+dot, 1 update+dot, 2 p update / fold,
 // 3 FP64 residual.
@@ -56,14 +62,16 @@ struct SolveProfile {
 // Solve K u = rhs (rhs, u unscaled, device).  zero_rows (optional, uint8 tags == 1): rows
 // whose rhs is replaced by 0 (adjoint solves).  With prof != null every kernel is launched
 // on its own between two CUDA events (no graph) and timed.
-int solver_solve(Solver& S, const double* rhs, double* u, const uint8_t* zero_rows, const adfem_solver_opts& o,
-                 adfem_solver_stats* stats, cudaStream_t user, SolveProfile* prof = nullptr);
+// fix_rows (optional, tags == 1) get u = fix_vals (or 0 when fix_vals is null) exactly.
+int solver_solve(Solver& S, const double* rhs, double* u, const uint8_t* zero_rows, const uint8_t* fix_rows,
+                 const double* fix_vals, const adfem_solver_opts& o, adfem_solver_stats* stats, cudaStream_t user,
+                 SolveProfile* prof = nullptr);
 // y = K x with the unscaled operator (via the scaled copy)
 int solver_apply(Solver& S, const double* x, double* y, cudaStream_t user);
 
 // Fill sliced-ELL values from CSR values (same pattern).
 cudaError_t launch_csr_to_sell(const Sell& A, int64_t n, const int32_t* rowptr, const double* csr, double* sell,
                                cudaStream_t st);
-int sell_build_pattern(int64_t n, const int32_t* rowptr, const int32_t* colind, Sell& s);
+int sell_build_pattern(int64_t n, const int32_t* rowptr, const int32_t* colind, Sell& s, int period);
 
 }  // namespace adfem

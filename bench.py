@@ -38,7 +38,7 @@ METRIC = "solves/s & grads/s at 4M DOF, mixed vs FP64 @1e-10; serve p50/p99 ms"
 UNIT = "solves/s"
 # FP64 Jacobi-CG iterations this workload needs at the default rtol on GB300; the
 # reference arm scales its per-iteration CPU time by this count.
-FP64_ITERS_DEFAULT = 9000
+FP64_ITERS_DEFAULT = 14346
 
 
 def peaks():
@@ -246,6 +246,20 @@ def run_ours(args, rank, world, dist):
     n = mesh.ndof
     S = A.PoissonSystem(mesh)
     S.set_dirichlet(bd)
+    if args.trace_iters > 0:
+        # short run of the same step for profiler captures: one assembly, then the
+        # mixed and the FP64 solve stopped after trace_iters iterations
+        S.assemble(kappa, f)
+        u = torch.zeros(n, dtype=torch.float64, device="cuda")
+        for prec in ("mixed", "fp64"):
+            try:
+                S.solve(u, precision=prec, rtol=args.rtol, max_iter=args.trace_iters, chunk=8)
+            except A.AdFemError as e:
+                if e.status != 4:
+                    raise
+        torch.cuda.synchronize()
+        print(json.dumps({"trace_iters": args.trace_iters, "m": args.m}))
+        return 0
 
     def barrier():
         if dist is not None:
@@ -259,7 +273,7 @@ def run_ours(args, rank, world, dist):
 
     def step(prec, u):
         S.assemble(kappa, f)
-        S.solve(u, precision=prec, rtol=args.rtol)
+        S.solve(u, precision=prec, rtol=args.rtol if prec == "mixed" else args.rtol_fp64)
         return S.last_stats
 
     u = torch.zeros(n, dtype=torch.float64, device="cuda")
@@ -400,7 +414,8 @@ def run_ours(args, rank, world, dist):
             "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic",
             "config": {"workload": "poisson-2000x2000-jittered-4M-dof-contrast1e3", "m": args.m, "dof": n,
-                       "nnz": int(mesh.pattern()[1].size), "rtol": args.rtol, "precision": "mixed",
+                       "nnz": int(mesh.pattern()[1].size), "rtol_mixed": args.rtol, "rtol_fp64": args.rtol_fp64,
+                       "precision": "mixed",
                        "parallelism": "replicas" if world > 1 else "single",
                        "l2": "working set > L2 (no flush needed)", "kappa_sigma": sigma},
             "mixed": {"solves_per_s": value, "iters": [s[0] for s in mixed_stats],
@@ -434,7 +449,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--m", type=int, default=2000)
-    ap.add_argument("--rtol", type=float, default=1e-11)
+    ap.add_argument("--rtol", type=float, default=3e-10, help="mixed-precision stopping tolerance")
+    ap.add_argument("--rtol-fp64", type=float, default=1e-9, help="FP64 CG stopping tolerance")
     ap.add_argument("--ref-rtol", type=float, default=1e-14)
     ap.add_argument("--fp64-steps", type=int, default=2)
     ap.add_argument("--grad-steps", type=int, default=2)
@@ -442,6 +458,8 @@ def main():
     ap.add_argument("--ref-iters", type=int, default=10)
     ap.add_argument("--fp64-iters", type=int, default=FP64_ITERS_DEFAULT)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--trace-iters", type=int, default=0,
+                    help="profiling aid: run one truncated step (this many CG iterations) and exit")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
