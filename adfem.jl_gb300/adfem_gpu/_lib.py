@@ -115,6 +115,7 @@ SIGNATURES = {
     "adfem_system_solve_profiled_d": (c_i, [c_p, c_p, ctypes.POINTER(SolverOpts), ctypes.POINTER(SolverStats), c_p,
                                             c_p, c_p]),
     "adfem_poisson_solve": (c_i, [c_p, c_p, c_p, c_p, ctypes.POINTER(SolverOpts), ctypes.POINTER(SolverStats)]),
+    "adfem_csr_pcg_noalloc_d": (c_i, [c_i, c_p, c_p, c_p, c_p, c_p, c_d, c_i, c_p, c_p, c_p]),
 }
 
 

@@ -278,6 +278,22 @@ ADFEM_API int adfem_system_solve_profiled_d(adfem_system *sys, double *u_d, cons
                                             adfem_solver_stats *stats, double *kernel_ms, long long *launches,
                                             void *stream);
 
+/* No counterpart in the reference.  Allocation-free FP64 Jacobi-CG on a caller-owned
+ * device CSR matrix (0-based rowptr[n+1], colind[nnz], vals[nnz], symmetric positive
+ * definite), for callers that cannot call cudaMalloc -- e.g. code running inside a
+ * TensorFlow/ADCME custom op or a CUDA.jl task, where the framework's pool owns the
+ * device memory and an allocation could fail or synchronise the device.  All scratch
+ * lives in a fixed static device array: n must not exceed 131072 rows (larger n
+ * returns ADFEM_ERR_INVALID).  No cudaMalloc/cudaFree or allocating library call is
+ * made.  The first call on a device looks up the array's device address, so it should
+ * come before any stream capture.  Calls share the array: calls that overlap on the
+ * GPU race and must be serialised by the caller.  u_d receives the solution (the
+ * iteration starts from zero); iterations/relres (optional) receive the CG count and
+ * the final recursive ||r||/||b||. */
+ADFEM_API int adfem_csr_pcg_noalloc_d(int n, const int *rowptr_d, const int *colind_d, const double *vals_d,
+                                      const double *rhs_d, double *u_d, double rtol, int max_iter, int *iterations,
+                                      double *relres, void *stream);
+
 /* One host-buffer call for the whole Poisson forward path: upload kappa and f,
  * assemble, impose u = bdval on bd, solve, download u.  The end-to-end entry a Julia
  * caller uses for `K\F` after compute_fem_laplace_matrix1 / compute_fem_source_term1 /
