@@ -331,8 +331,9 @@ def solver_opts(precision: str = "fp64", rtol: float = 1e-12, max_iter: int = 20
     return o
 
 
-def solve(K, F, precision: str = "fp64", rtol: float = 1e-12, max_iter: int = 200000, return_stats: bool = False):
-    """``K\\F`` for a symmetric positive definite sparse K (GPU Jacobi-CG)."""
+def solve(K, F, precision: str = "fp64", rtol: float = 1e-12, max_iter: int = 200000, return_stats: bool = False,
+          u0=None):
+    """``K\\F`` for a symmetric positive definite sparse K (GPU Jacobi-CG); ``u0`` warm-starts."""
     K = sp.csc_matrix(K)
     K.sort_indices()
     n = K.shape[0]
@@ -340,8 +341,8 @@ def solve(K, F, precision: str = "fp64", rtol: float = 1e-12, max_iter: int = 20
     rv = _c(K.indices, np.int64) + 1
     nz = _c(K.data, np.float64)
     F = _c(F, np.float64)
-    u = np.zeros(n)
-    o = solver_opts(precision, rtol, max_iter)
+    u = np.zeros(n) if u0 is None else np.array(u0, dtype=np.float64, copy=True)
+    o = solver_opts(precision, rtol, max_iter, warm_start=u0 is not None)
     st = SolverStats()
     check(_lib_().adfem_csc_solve(n, ptr(cp), ptr(rv), ptr(nz), ptr(F), ptr(u), ctypes.byref(o), ctypes.byref(st)),
           "solve")

@@ -30,6 +30,11 @@ class SolverStats(ctypes.Structure):
                 ("launches", c_ll)]
 
 
+class SolverInfo(ctypes.Structure):
+    _fields_ = [("rows", c_ll), ("stored", c_ll), ("uniform_entries", c_ll), ("slices", c_ll), ("band", c_ll),
+                ("banded", c_i), ("blocks", c_i), ("rows_per_block", c_ll), ("ring", c_i)]
+
+
 OK = 0
 ERR_INVALID = 1
 ERR_CUDA = 2
@@ -114,6 +119,7 @@ SIGNATURES = {
     "adfem_system_rhs_d": (c_i, [c_p, c_p, c_p]),
     "adfem_system_solve_profiled_d": (c_i, [c_p, c_p, ctypes.POINTER(SolverOpts), ctypes.POINTER(SolverStats), c_p,
                                             c_p, c_p]),
+    "adfem_system_solver_info": (c_i, [c_p, ctypes.POINTER(SolverInfo)]),
     "adfem_poisson_solve": (c_i, [c_p, c_p, c_p, c_p, ctypes.POINTER(SolverOpts), ctypes.POINTER(SolverStats)]),
     "adfem_csr_pcg_noalloc_d": (c_i, [c_i, c_p, c_p, c_p, c_p, c_p, c_d, c_i, c_p, c_p, c_p]),
 }

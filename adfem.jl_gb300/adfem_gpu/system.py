@@ -112,6 +112,12 @@ class _System:
         check(_lib.load().adfem_system_rhs_d(self._h, ptr(r), _cur_stream()), "system_rhs")
         return r
 
+    def solver_info(self):
+        """Operator layout and the mixed iteration used (dict of adfem_solver_info)."""
+        info = _lib.SolverInfo()
+        check(_lib.load().adfem_system_solver_info(self._h, ctypes.byref(info)), "system_solver_info")
+        return {name: getattr(info, name) for name, _ in info._fields_}
+
 
 class PoissonSystem(_System):
     """-div(kappa grad u) = f on a P1 mesh with u = bdval on the Dirichlet nodes."""

@@ -72,6 +72,7 @@ struct Sell {
   int64_t nslices = 0;  // ceil(n / 32)
   int64_t nent = 0;     // stored entries incl. padding
   int maxw = 0;         // widest slice
+  int64_t band = 0;     // max |col - row| over all stored entries
   bool delta16 = false; // column stored as int16 delta to the row, else int32 column
   DevBuf sptr;          // int32 [nslices + 1]  (units of entries)
   DevBuf col;           // int16 [nent] (delta) or int32 [nent]
@@ -85,6 +86,7 @@ struct Sell {
   DevBuf pat;           // int16 pool
   int pat_period = 1;
   int64_t uniform_slices = 0;
+  int64_t uniform_entries = 0;  // stored entries of the uniform slices
   DevBuf val64;         // double [nent]  (Jacobi-scaled, standard form)
   DevBuf valD64;        // double [nent]  (Jacobi-scaled, difference form, for FP64 residuals)
   DevBuf val32;         // float  [nent]

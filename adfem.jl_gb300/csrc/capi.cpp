@@ -735,6 +735,22 @@ int adfem_system_solve_profiled_d(adfem_system* sys, double* u_d, const adfem_so
   return r;
 }
 
+int adfem_system_solver_info(const adfem_system* sys, adfem_solver_info* info) {
+  if (!sys || !info) return fail(ADFEM_ERR_INVALID, "null argument");
+  const Sell& A = sys->A;
+  const Solver& sv = sys->solver;
+  info->rows = A.n;
+  info->stored = A.nent;
+  info->uniform_entries = A.uniform_entries;
+  info->slices = A.nslices;
+  info->band = A.band;
+  info->banded = sv.zcg ? 1 : 0;
+  info->blocks = sv.zcg ? sv.zgrid : 0;
+  info->rows_per_block = sv.zcg ? sv.zL : 0;
+  info->ring = sv.zcg ? sv.zW : 0;
+  return ADFEM_OK;
+}
+
 int adfem_system_adjoint_d(adfem_system* sys, const double* g_d, double* lam_d, const adfem_solver_opts* opts,
                            adfem_solver_stats* stats, void* stream) {
   if (!sys || !g_d || !lam_d) return fail(ADFEM_ERR_INVALID, "null argument");

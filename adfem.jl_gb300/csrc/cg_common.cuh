@@ -1,0 +1,151 @@
+// Device helpers shared by the CG kernels (solver.cu, zcg.cu): thread indexing,
+// sliced-ELL row access, deterministic block/grid reductions, the FP32 hi+lo axpy
+// and the residual-replacement bookkeeping of the mixed solves.
+#pragma once
+#include "solver.cuh"
+
+namespace adfem {
+
+static constexpr int kT = 256;
+
+__device__ __forceinline__ int64_t gtid() { return (int64_t)blockIdx.x * blockDim.x + threadIdx.x; }
+__device__ __forceinline__ int64_t gstride() { return (int64_t)gridDim.x * blockDim.x; }
+
+template <bool D16>
+__device__ __forceinline__ int colof(const void* c, int64_t idx, int64_t r) {
+  if constexpr (D16) return (int)(r + (int64_t)__ldg(reinterpret_cast<const int16_t*>(c) + idx));
+  else return __ldg(reinterpret_cast<const int32_t*>(c) + idx);
+}
+
+template <class T>
+__device__ __forceinline__ T warp_sum(T v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+// Deterministic block sum of NV values over a block of BT threads; the totals end up
+// in thread 0.
+template <class T, int NV, int BT = kT>
+__device__ __forceinline__ void block_sum(T (&v)[NV]) {
+  static_assert(BT % 32 == 0 && BT <= 1024, "block size");
+  __shared__ T sh[NV][BT / 32];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+  for (int j = 0; j < NV; j++) v[j] = warp_sum(v[j]);
+  if (lane == 0)
+#pragma unroll
+    for (int j = 0; j < NV; j++) sh[j][wid] = v[j];
+  __syncthreads();
+  if (wid == 0) {
+#pragma unroll
+    for (int j = 0; j < NV; j++) {
+      T x = lane < (BT / 32) ? sh[j][lane] : T(0);
+      v[j] = warp_sum(x);
+    }
+  }
+  __syncthreads();
+}
+
+// Publish this block's partial sums; the last block to arrive sums all partials in
+// block order into tot (valid in thread 0) and returns true (block-uniform).
+template <class T, int NV, int BT = kT>
+__device__ __forceinline__ bool reduce_grid(T (&v)[NV], T* partials, unsigned* counter, T (&tot)[NV]) {
+  __shared__ bool last;
+  block_sum<T, NV, BT>(v);
+  if (threadIdx.x == 0) {
+#pragma unroll
+    for (int j = 0; j < NV; j++) partials[j * gridDim.x + blockIdx.x] = v[j];
+    __threadfence();
+    const unsigned prev = atomicAdd(counter, 1u);
+    last = (prev == gridDim.x - 1);
+  }
+  __syncthreads();
+  if (!last) return false;
+  __threadfence();
+  T s[NV];
+#pragma unroll
+  for (int j = 0; j < NV; j++) s[j] = T(0);
+  for (int b = threadIdx.x; b < (int)gridDim.x; b += blockDim.x)
+#pragma unroll
+    for (int j = 0; j < NV; j++) s[j] += __ldcg(partials + j * gridDim.x + b);
+  block_sum<T, NV, BT>(s);
+  if (threadIdx.x == 0) {
+#pragma unroll
+    for (int j = 0; j < NV; j++) tot[j] = s[j];
+    *counter = 0u;
+  }
+  return true;
+}
+
+// row geometry in sliced-ELL: first entry of row r and the slice width
+__device__ __forceinline__ void sell_row(const int32_t* __restrict__ sptr, int64_t r, int64_t& base, int& w) {
+  const int32_t s0 = __ldg(sptr + (r >> 5)), s1 = __ldg(sptr + (r >> 5) + 1);
+  base = (int64_t)s0 + (r & 31);
+  w = (s1 - s0) >> 5;
+}
+
+// (h, l) += a * p as an unevaluated FP32 pair: two-product of a*p, two-sum with h,
+// renormalisation.  Explicitly rounded intrinsics keep the compiler from fusing
+// or reassociating the error terms.
+__device__ __forceinline__ void df_axpy(float& h, float& l, float a, float p) {
+  const float ph = __fmul_rn(a, p);
+  const float pl = fmaf(a, p, -ph);
+  const float s = __fadd_rn(h, ph);
+  const float bb = __fsub_rn(s, h);
+  float e = __fadd_rn(__fsub_rn(h, __fsub_rn(s, bb)), __fsub_rn(ph, bb));
+  e = __fadd_rn(e, __fadd_rn(l, pl));
+  const float hi = __fadd_rn(s, e);
+  l = __fsub_rn(e, __fsub_rn(hi, s));
+  h = hi;
+}
+
+// Bookkeeping after an FP64 residual evaluation of a mixed solve (thread 0 of the
+// last block).  rr: FP64 residual norm^2 (scaled), rn: norm^2 of its FP32 copy, rp:
+// (FP32 residual, current direction) in the same inner product.  mode 1 replaces the
+// recurrence residual; mode 2 only records rr.
+__device__ __forceinline__ void replacement_step(CgState* st, double rr, double rn, double rp, int mode) {
+  st->rr64 = rr;
+  if (mode == 2) return;
+  if (!isfinite(rr)) {
+    st->done = 2;
+    return;
+  }
+  if (rr <= st->stop2) {
+    st->done = 1;
+    return;
+  }
+  // The FP64 residual of an FP64 iterate cannot fall below about 2^-53 |K| |y|
+  // (rounding of y itself, amplified by the largest eigenvalues).  When the FP32
+  // residual has met rtol twice in a row and the FP64 residual improved less than
+  // 4x in between, the iterate is at that attainable accuracy: stop there.
+  if (st->final_req && st->last_rr64 > 0.0 && rr > 0.0625 * st->last_rr64) {
+    st->floor_hit = 1;
+    st->done = 1;
+    return;
+  }
+  if (st->iters >= st->max_iter) {
+    st->done = 4;
+    return;
+  }
+  if (st->final_req) st->last_rr64 = rr;
+  st->final_req = 0;
+  if (st->updates == 0) {
+    st->ar = 1.0;
+    st->ap = 0.0;
+  } else {
+    // re-orthogonalise the direction against the new residual: p <- p - c r, folded
+    // into the next direction update p_new = r + beta p = (1 - beta c) r + beta p
+    const double c = rp / rn;
+    const double beta = rn / st->rho;
+    st->ar = 1.0 - beta * c;
+    st->ap = beta;
+  }
+  st->alpha = 0.0;
+  st->updates += 1;
+  st->rho = rn;
+  st->ru2 = st->delta2 * rn;
+  st->done = 0;
+}
+
+}  // namespace adfem

@@ -102,6 +102,7 @@ int sell_build_pattern(int64_t n, const int32_t* rowptr, const int32_t* colind, 
   }
   s.nent = sptr[s.nslices];
   s.maxw = maxw;
+  s.band = maxd;
   s.delta16 = maxd <= 32767;
   ADFEM_TRY(upload(s.sptr, sptr.data(), sptr.size()));
   if (s.delta16) {
@@ -135,6 +136,7 @@ int sell_build_pattern(int64_t n, const int32_t* rowptr, const int32_t* colind, 
   // slice-uniform patterns
   s.pat_period = period;
   s.uniform_slices = 0;
+  s.uniform_entries = 0;
   std::vector<int32_t> spat(std::max<int64_t>(s.nslices, 1), -1);
   std::vector<int16_t> pool;
   if (s.delta16 && (period == 1 || period == 2)) {
@@ -172,6 +174,7 @@ int sell_build_pattern(int64_t n, const int32_t* rowptr, const int32_t* colind, 
       }
       spat[sl] = off;
       s.uniform_slices++;
+      s.uniform_entries += 32 * (int64_t)w;
     }
   }
   if (pool.empty()) pool.push_back(0);

@@ -23,87 +23,11 @@
 #include <cstdlib>
 #include <cstring>
 
-#include "solver.cuh"
+#include "cg_common.cuh"
 
 namespace adfem {
 
-static constexpr int kT = 256;
 static constexpr int kMaxBlocksPerSM = 8;
-
-__device__ __forceinline__ int64_t gtid() { return (int64_t)blockIdx.x * blockDim.x + threadIdx.x; }
-__device__ __forceinline__ int64_t gstride() { return (int64_t)gridDim.x * blockDim.x; }
-
-template <bool D16>
-__device__ __forceinline__ int colof(const void* c, int64_t idx, int64_t r) {
-  if constexpr (D16) return (int)(r + (int64_t)__ldg(reinterpret_cast<const int16_t*>(c) + idx));
-  else return __ldg(reinterpret_cast<const int32_t*>(c) + idx);
-}
-
-template <class T>
-__device__ __forceinline__ T warp_sum(T v) {
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-  return v;
-}
-
-// Deterministic block sum of NV values; the totals end up in thread 0.
-template <class T, int NV>
-__device__ __forceinline__ void block_sum(T (&v)[NV]) {
-  __shared__ T sh[NV][kT / 32];
-  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-#pragma unroll
-  for (int j = 0; j < NV; j++) v[j] = warp_sum(v[j]);
-  if (lane == 0)
-#pragma unroll
-    for (int j = 0; j < NV; j++) sh[j][wid] = v[j];
-  __syncthreads();
-  if (wid == 0) {
-#pragma unroll
-    for (int j = 0; j < NV; j++) {
-      T x = lane < (kT / 32) ? sh[j][lane] : T(0);
-      v[j] = warp_sum(x);
-    }
-  }
-  __syncthreads();
-}
-
-// Publish this block's partial sums; the last block to arrive sums all partials in
-// block order into tot (valid in thread 0) and returns true (block-uniform).
-template <class T, int NV>
-__device__ __forceinline__ bool reduce_grid(T (&v)[NV], T* partials, unsigned* counter, T (&tot)[NV]) {
-  __shared__ bool last;
-  block_sum<T, NV>(v);
-  if (threadIdx.x == 0) {
-#pragma unroll
-    for (int j = 0; j < NV; j++) partials[j * gridDim.x + blockIdx.x] = v[j];
-    __threadfence();
-    const unsigned prev = atomicAdd(counter, 1u);
-    last = (prev == gridDim.x - 1);
-  }
-  __syncthreads();
-  if (!last) return false;
-  __threadfence();
-  T s[NV];
-#pragma unroll
-  for (int j = 0; j < NV; j++) s[j] = T(0);
-  for (int b = threadIdx.x; b < (int)gridDim.x; b += blockDim.x)
-#pragma unroll
-    for (int j = 0; j < NV; j++) s[j] += __ldcg(partials + j * gridDim.x + b);
-  block_sum<T, NV>(s);
-  if (threadIdx.x == 0) {
-#pragma unroll
-    for (int j = 0; j < NV; j++) tot[j] = s[j];
-    *counter = 0u;
-  }
-  return true;
-}
-
-// row geometry in sliced-ELL: first entry of row r and the slice width
-__device__ __forceinline__ void sell_row(const int32_t* __restrict__ sptr, int64_t r, int64_t& base, int& w) {
-  const int32_t s0 = __ldg(sptr + (r >> 5)), s1 = __ldg(sptr + (r >> 5) + 1);
-  base = (int64_t)s0 + (r & 31);
-  w = (s1 - s0) >> 5;
-}
 
 // ---------------------------------------------------------------------------
 // setup kernels
@@ -237,50 +161,18 @@ __global__ void __launch_bounds__(kT) k_residual64(int64_t n, const int32_t* __r
   double v[3] = {a0, a1, a2}, tot[3];
   if (reduce_grid<double, 3>(v, partials, &st->counter[1], tot) && threadIdx.x == 0) {
     const double rr = tot[0];
+    if (mode != 0) {
+      replacement_step(st, rr, tot[1], tot[2], mode);
+      return;
+    }
     st->rr64 = rr;
-    if (mode == 2) return;
-    if (!isfinite(rr)) {
-      st->done = 2;
-      return;
-    }
-    if (rr <= st->stop2) {
-      st->done = 1;
-      return;
-    }
-    // The FP64 residual of an FP64 iterate cannot fall below about 2^-53 |K~| |y|
-    // (rounding of y itself, amplified by the largest eigenvalues).  When the FP32
-    // residual has met rtol twice in a row and the FP64 residual improved less than
-    // 4x in between, the iterate is at that attainable accuracy: stop there.
-    if (mode == 1 && st->final_req && st->last_rr64 > 0.0 && rr > 0.0625 * st->last_rr64) {
-      st->floor_hit = 1;
-      st->done = 1;
-      return;
-    }
-    if (st->iters >= st->max_iter) {
-      st->done = 4;
-      return;
-    }
-    if (mode == 0) {
+    if (!isfinite(rr)) st->done = 2;
+    else if (rr <= st->stop2) st->done = 1;
+    else if (st->iters >= st->max_iter) st->done = 4;
+    else {
       st->rho = rr;
       st->done = 0;
-      return;
     }
-    if (st->final_req) st->last_rr64 = rr;
-    st->final_req = 0;
-    const double rn = tot[1];
-    if (st->updates == 0) {
-      st->ar = 1.0;
-      st->ap = 0.0;
-    } else {
-      const double c = tot[2] / rn;
-      const double beta = rn / st->rho;
-      st->ar = 1.0 - beta * c;
-      st->ap = beta;
-    }
-    st->updates += 1;
-    st->rho = rn;
-    st->ru2 = st->delta2 * rn;
-    st->done = 0;
   }
 }
 
@@ -502,21 +394,6 @@ __global__ void __launch_bounds__(kT, PF ? 4 : 1) k_cg32_spmv(int64_t n, const i
 // transformations (two-product, two-sum), i.e. about 48 bits without FP64
 // instructions.  A plain FP32 accumulator would add rounding noise of size
 // 2^-24 |y| that the operator amplifies by its largest eigenvalue.
-// (h, l) += a * p as an unevaluated FP32 pair: two-product of a*p, two-sum with h,
-// renormalisation.  Explicitly rounded intrinsics keep the compiler from fusing
-// or reassociating the error terms.
-__device__ __forceinline__ void df_axpy(float& h, float& l, float a, float p) {
-  const float ph = __fmul_rn(a, p);
-  const float pl = fmaf(a, p, -ph);
-  const float s = __fadd_rn(h, ph);
-  const float bb = __fsub_rn(s, h);
-  float e = __fadd_rn(__fsub_rn(h, __fsub_rn(s, bb)), __fsub_rn(ph, bb));
-  e = __fadd_rn(e, __fadd_rn(l, pl));
-  const float hi = __fadd_rn(s, e);
-  l = __fsub_rn(e, __fsub_rn(hi, s));
-  h = hi;
-}
-
 __global__ void __launch_bounds__(kT) k_cg32_update(int64_t n, float* __restrict__ yh, float* __restrict__ yl,
                                                     float* __restrict__ r, const float* pa, const float* pb,
                                                     const float* __restrict__ q, CgState* st, double* partials) {
@@ -645,6 +522,7 @@ static SellPat sell_pat(const Sell& A) {
 Solver::~Solver() {
   if (g64) cudaGraphExecDestroy(g64);
   if (g32) cudaGraphExecDestroy(g32);
+  if (gz) cudaGraphExecDestroy(gz);
   for (auto& e : ev)
     if (e) cudaEventDestroy(e);
   for (auto& e : pev) cudaEventDestroy(e);
@@ -695,9 +573,10 @@ int Solver::init(const Sell* A_, int64_t n_) {
     ADFEM_TRY(resident_grid(w8 ? k_cg64_spmv<true, 8, false> : k_cg64_spmv<true, 16, false>, sms, need, &g3));
   }
   grid_spmv = std::min(g2, g3);
+  ADFEM_TRY(zcg_plan(*this, sms));
   ADFEM_TRY(state.alloc(sizeof(CgState)));
   ADFEM_CUDA(cudaMemset(state.p, 0, sizeof(CgState)));
-  ADFEM_TRY(partials.alloc(sizeof(double) * 4 * (size_t)std::max(grid, grid_spmv)));
+  ADFEM_TRY(partials.alloc(sizeof(double) * 4 * (size_t)std::max(std::max(grid, grid_spmv), zgrid)));
   const size_t n8 = sizeof(double) * (size_t)n, n4 = sizeof(float) * (size_t)n;
   ADFEM_TRY(s32.alloc(n4));
   ADFEM_TRY(b.alloc(n8));
@@ -726,6 +605,7 @@ int solver_prepare(Solver& S, const int32_t* diagpos_dev, cudaStream_t user) {
   ADFEM_TRY(bad.alloc(sizeof(int)));
   ADFEM_CUDA(cudaMemsetAsync(bad.p, 0, sizeof(int), user));
   const unsigned nb = (unsigned)((S.n + kT - 1) / kT);
+  if (S.zcg) ADFEM_TRY(zcg_prepare(S, diagpos_dev, bad.as<int>(), user));  // reads the unscaled values
   k_scale_diag<<<nb, kT, 0, user>>>(S.n, A.sptr.as<int32_t>(), A.val64.as<double>(), diagpos_dev, S.s32.as<float>(),
                                     bad.as<int>());
   if (A.delta16)
@@ -852,26 +732,49 @@ static void enqueue_reliable_update(Solver& S, cudaStream_t st, int force, Timer
   enqueue_residual(S, st, 1, force, tm);
 }
 
-static int chunk_launches(bool mixed, int chunk) {
-  if (!mixed) return 3 * chunk;
+// The three iteration schemes: FP64 CG, the scaled two-kernel mixed iteration, and the
+// banded one-kernel mixed iteration (zcg.cu).
+enum class Path { FP64, MIXED, BANDED };
+
+// fold + FP64 residual replacement of the banded path (both return at entry unless due)
+static void enqueue_zreliable_update(Solver& S, cudaStream_t st, int force, Timer* tm = nullptr) {
+  Timer none;
+  if (!tm) tm = &none;
+  tm->run(2, st, [&] {
+    k_fold<<<S.grid, kT, 0, st>>>(S.n, S.y64.as<double>(), S.yh32.as<float>(), S.yl32.as<float>(),
+                                  S.state.as<CgState>(), force);
+  });
+  tm->run(3, st, [&] { zcg_enqueue_residual(S, st, 1, force); });
+}
+
+// iteration i of a chunk of `chunk` (the replacement check follows every 8th and the last)
+static void enqueue_iteration(Solver& S, Path path, int i, int chunk, cudaStream_t st, Timer* tm = nullptr) {
+  const bool check = (i + 1) % 8 == 0 || i + 1 == chunk;
+  if (path == Path::FP64) {
+    enqueue_cg64(S, st, tm);
+  } else if (path == Path::MIXED) {
+    enqueue_cg32(S, st, tm);
+    if (check) enqueue_reliable_update(S, st, 0, tm);
+  } else {
+    if (tm) tm->run(0, st, [&] { zcg_enqueue_iter(S, st); });
+    else zcg_enqueue_iter(S, st);
+    if (check) enqueue_zreliable_update(S, st, 0, tm);
+  }
+}
+
+static int chunk_launches(Path path, int chunk) {
+  if (path == Path::FP64) return 3 * chunk;
   int ru = 0;
   for (int i = 0; i < chunk; i++)
     if ((i + 1) % 8 == 0 || i + 1 == chunk) ru++;
-  return 2 * chunk + 2 * ru;
+  return (path == Path::MIXED ? 2 : 1) * chunk + 2 * ru;
 }
 
 // capture `chunk` iterations into a graph (kernels read all scalars from device state)
-static int capture_chunk(Solver& S, bool mixed, int chunk, cudaGraphExec_t* out) {
+static int capture_chunk(Solver& S, Path path, int chunk, cudaGraphExec_t* out) {
   cudaGraph_t g = nullptr;
   ADFEM_CUDA(cudaStreamBeginCapture(S.stream, cudaStreamCaptureModeThreadLocal));
-  for (int i = 0; i < chunk; i++) {
-    if (mixed) {
-      enqueue_cg32(S, S.stream);
-      if ((i + 1) % 8 == 0 || i + 1 == chunk) enqueue_reliable_update(S, S.stream, 0);
-    } else {
-      enqueue_cg64(S, S.stream);
-    }
-  }
+  for (int i = 0; i < chunk; i++) enqueue_iteration(S, path, i, chunk, S.stream);
   cudaError_t e = cudaStreamEndCapture(S.stream, &g);
   if (e != cudaSuccess) return cuda_fail(e, "cudaStreamEndCapture");
   e = cudaGraphInstantiate(out, g, 0);
@@ -888,16 +791,17 @@ int solver_solve(Solver& S, const double* rhs, double* u, const uint8_t* zero_ro
   if (o.precision != ADFEM_PREC_FP64 && !mixed) return fail(ADFEM_ERR_INVALID, "solver: unknown precision");
   if (!(o.rtol > 0.0) || o.max_iter < 1) return fail(ADFEM_ERR_INVALID, "solver: rtol must be > 0, max_iter >= 1");
   const int chunk = std::max(1, std::min(o.chunk > 0 ? o.chunk : 32, 512));
+  const Path path = !mixed ? Path::FP64 : (S.zcg ? Path::BANDED : Path::MIXED);
   cudaStream_t st = S.stream;
-  cudaGraphExec_t* gx = mixed ? &S.g32 : &S.g64;
-  int* gc = mixed ? &S.g32_chunk : &S.g64_chunk;
+  cudaGraphExec_t* gx = path == Path::FP64 ? &S.g64 : (path == Path::MIXED ? &S.g32 : &S.gz);
+  int* gc = path == Path::FP64 ? &S.g64_chunk : (path == Path::MIXED ? &S.g32_chunk : &S.gz_chunk);
   if (!prof) {
     if (*gx && *gc != chunk) {
       cudaGraphExecDestroy(*gx);
       *gx = nullptr;
     }
     if (!*gx) {
-      ADFEM_TRY(capture_chunk(S, mixed, chunk, gx));
+      ADFEM_TRY(capture_chunk(S, path, chunk, gx));
       *gc = chunk;
     }
   }
@@ -913,18 +817,24 @@ int solver_solve(Solver& S, const double* rhs, double* u, const uint8_t* zero_ro
   init.delta2 = dl * dl;
   init.done = 3;  // lets the forced residual kernel run in mixed mode
   ADFEM_CUDA(cudaMemcpyAsync(S.state.p, &init, sizeof(CgState), cudaMemcpyHostToDevice, st));
-  k_init<<<S.grid, kT, 0, st>>>(S.n, rhs, zero_rows, S.s32.as<float>(), o.warm_start ? u : nullptr,
-                                S.b.as<double>(), S.y64.as<double>(), S.state.as<CgState>(), S.partials.as<double>(),
-                                o.rtol * o.rtol);
-  ADFEM_CUDA(cudaGetLastError());
-  if (mixed) {
-    ADFEM_CUDA(cudaMemsetAsync(S.pa32.p, 0, sizeof(float) * S.n, st));
-    ADFEM_CUDA(cudaMemsetAsync(S.pb32.p, 0, sizeof(float) * S.n, st));
-    ADFEM_CUDA(cudaMemsetAsync(S.yh32.p, 0, sizeof(float) * S.n, st));
-    ADFEM_CUDA(cudaMemsetAsync(S.yl32.p, 0, sizeof(float) * S.n, st));
-    enqueue_residual(S, st, 1, 1);
+  if (path == Path::BANDED) {
+    ADFEM_TRY(zcg_clear(S, st));
+    zcg_enqueue_init(S, st, rhs, zero_rows, o.warm_start ? u : nullptr, o.rtol * o.rtol);
+    zcg_enqueue_residual(S, st, 1, 1);
   } else {
-    enqueue_residual(S, st, 0, 1);
+    k_init<<<S.grid, kT, 0, st>>>(S.n, rhs, zero_rows, S.s32.as<float>(), o.warm_start ? u : nullptr,
+                                  S.b.as<double>(), S.y64.as<double>(), S.state.as<CgState>(), S.partials.as<double>(),
+                                  o.rtol * o.rtol);
+    ADFEM_CUDA(cudaGetLastError());
+    if (mixed) {
+      ADFEM_CUDA(cudaMemsetAsync(S.pa32.p, 0, sizeof(float) * S.n, st));
+      ADFEM_CUDA(cudaMemsetAsync(S.pb32.p, 0, sizeof(float) * S.n, st));
+      ADFEM_CUDA(cudaMemsetAsync(S.yh32.p, 0, sizeof(float) * S.n, st));
+      ADFEM_CUDA(cudaMemsetAsync(S.yl32.p, 0, sizeof(float) * S.n, st));
+      enqueue_residual(S, st, 1, 1);
+    } else {
+      enqueue_residual(S, st, 0, 1);
+    }
   }
   ADFEM_CUDA(cudaGetLastError());
   launches += 2;
@@ -936,15 +846,8 @@ int solver_solve(Solver& S, const double* rhs, double* u, const uint8_t* zero_ro
     tm.S = &S;
     tm.prof = prof;
     for (;;) {
-      for (int i = 0; i < chunk; i++) {
-        if (mixed) {
-          enqueue_cg32(S, st, &tm);
-          if ((i + 1) % 8 == 0 || i + 1 == chunk) enqueue_reliable_update(S, st, 0, &tm);
-        } else {
-          enqueue_cg64(S, st, &tm);
-        }
-      }
-      launches += chunk_launches(mixed, chunk);
+      for (int i = 0; i < chunk; i++) enqueue_iteration(S, path, i, chunk, st, &tm);
+      launches += chunk_launches(path, chunk);
       ADFEM_CUDA(cudaGetLastError());
       ADFEM_CUDA(cudaMemcpyAsync(&S.h_state[0], S.state.p, sizeof(CgState), cudaMemcpyDeviceToHost, st));
       ADFEM_CUDA(cudaStreamSynchronize(st));
@@ -958,10 +861,10 @@ int solver_solve(Solver& S, const double* rhs, double* u, const uint8_t* zero_ro
     ADFEM_CUDA(cudaGraphLaunch(*gx, st));
     ADFEM_CUDA(cudaMemcpyAsync(&S.h_state[0], S.state.p, sizeof(CgState), cudaMemcpyDeviceToHost, st));
     ADFEM_CUDA(cudaEventRecord(S.ev[2], st));
-    launches += chunk_launches(mixed, chunk);
+    launches += chunk_launches(path, chunk);
     for (;;) {
       ADFEM_CUDA(cudaGraphLaunch(*gx, st));
-      launches += chunk_launches(mixed, chunk);
+      launches += chunk_launches(path, chunk);
       ADFEM_CUDA(cudaMemcpyAsync(&S.h_state[1 - slot], S.state.p, sizeof(CgState), cudaMemcpyDeviceToHost, st));
       ADFEM_CUDA(cudaEventRecord(S.ev[2 + (1 - slot)], st));
       ADFEM_CUDA(cudaEventSynchronize(S.ev[2 + slot]));
@@ -977,9 +880,14 @@ int solver_solve(Solver& S, const double* rhs, double* u, const uint8_t* zero_ro
                                   S.state.as<CgState>(), 1);
     launches += 1;
   }
-  enqueue_residual(S, st, 2, 1);
-  k_unscale<<<(unsigned)((S.n + kT - 1) / kT), kT, 0, st>>>(S.n, S.y64.as<double>(), S.s32.as<float>(), fix_rows,
-                                                           fix_vals, u);
+  if (path == Path::BANDED) {
+    zcg_enqueue_residual(S, st, 2, 1);
+    zcg_enqueue_unscale(S, st, fix_rows, fix_vals, u);
+  } else {
+    enqueue_residual(S, st, 2, 1);
+    k_unscale<<<(unsigned)((S.n + kT - 1) / kT), kT, 0, st>>>(S.n, S.y64.as<double>(), S.s32.as<float>(), fix_rows,
+                                                             fix_vals, u);
+  }
   ADFEM_CUDA(cudaGetLastError());
   launches += 2;
   ADFEM_CUDA(cudaMemcpyAsync(&S.h_state[0], S.state.p, sizeof(CgState), cudaMemcpyDeviceToHost, st));

@@ -46,6 +46,24 @@ struct Solver {
   std::vector<cudaEvent_t> pev;  // event pool of profiled solves
   int g64_chunk = 0, g32_chunk = 0;
   bool prepared = false;
+  // banded mixed path (zcg.cu): used by mixed solves when the band fits the ring
+  bool zcg = false;
+  int zH = 0, zgrid = 0;
+  int zS = 0;              // rows per super-tile
+  int zK = 0;              // super-tiles per block
+  int zW = 0;              // shared-memory positions per super-tile (zS + 2 zH)
+  int64_t zL = 0;
+  size_t zsmem = 0;
+  DevBuf z1, zq1;          // second buffers of the Z and q^ ping-pong pairs (first: r32, q32)
+  DevBuf dz32;             // fp32(K_ii)
+  DevBuf valz64, valz32;   // difference-form copies of K (physical scale; FP32 in the fixed-width layout)
+  DevBuf colz16;           // per-entry column deltas of the fixed-width layout
+  DevBuf zpid32, zpool32;  // per-slice pattern id, distinct padded column patterns
+  int znpool = 0;          // ints in zpool32
+  int zw = 0;              // fixed slice width (widest slice)
+  int zps = 0;             // pattern row stride (8 or 16, the kernel's unrolled width)
+  cudaGraphExec_t gz = nullptr;
+  int gz_chunk = 0;
   ~Solver();
   int init(const Sell* A, int64_t n);
 };
@@ -68,6 +86,18 @@ int solver_solve(Solver& S, const double* rhs, double* u, const uint8_t* zero_ro
                  SolveProfile* prof = nullptr);
 // y = K x with the unscaled operator (via the scaled copy)
 int solver_apply(Solver& S, const double* x, double* y, cudaStream_t user);
+
+// Banded mixed path (zcg.cu).  zcg_plan decides whether the operator's band fits
+// the shared-memory ring and allocates the path's buffers; zcg_prepare derives its
+// operator copies from the unscaled FP64 values (before they are scaled in place).
+int zcg_plan(Solver& S, int sms);
+int zcg_prepare(Solver& S, const int32_t* diagpos_dev, int* bad_dev, cudaStream_t st);
+int zcg_clear(Solver& S, cudaStream_t st);
+void zcg_enqueue_init(Solver& S, cudaStream_t st, const double* rhs, const uint8_t* zero_rows, const double* u0,
+                      double rtol2);
+void zcg_enqueue_iter(Solver& S, cudaStream_t st);
+void zcg_enqueue_residual(Solver& S, cudaStream_t st, int mode, int force);
+void zcg_enqueue_unscale(Solver& S, cudaStream_t st, const uint8_t* fix, const double* fixval, double* u);
 
 // Fill sliced-ELL values from CSR values (same pattern).
 cudaError_t launch_csr_to_sell(const Sell& A, int64_t n, const int32_t* rowptr, const double* csr, double* sell,

@@ -1,0 +1,530 @@
+// Mixed-precision Jacobi-PCG for banded operators, one kernel per iteration (sm_103a).
+//
+// Vectors are kept in the physical space of K (the operator is not Jacobi-scaled):
+//   Z  = D^-1 r   preconditioned residual (FP32),
+//   P             search direction (FP32),
+//   q^ = D^-1 K P (FP32),
+//   Y             solution correction since the last fold (FP32 hi+lo pair),
+//   D  = fp32(diag K), used as the Jacobi preconditioner everywhere (also by the FP64
+//        residual), so the preconditioner is exactly consistent across precisions.
+// K P is evaluated in difference form, (K P)_i = rowsum_i P_i + sum_{j!=i} K_ij (P_j - P_i),
+// from an FP32 copy whose diagonal slot holds the FP64 row sum rounded once.
+//
+// Launch k of the iteration, for the rows of each block's contiguous range:
+//   Z_k = Z_{k-1} - a_{k-1} q^_{k-1}   and   Y += a_{k-1} P_{k-1}   (lagged updates),
+//   P_k = ar Z_k + ap P_{k-1}          (ar = 1, ap = beta_{k-1}; other values after a
+//                                       residual replacement re-orthogonalise P),
+//   q_k = K P_k,  q^_k = q_k / D,
+//   rho_k = sum D Z_k^2,  P_k.q_k,  Z_k.q_k,  q_k.q^_k   (one grid reduction).
+// The last block sets a_k = rho_k / P.q and beta_k from the one-step estimate
+//   rho_{k+1} ~ rho_k - 2 a_k Z.q + a_k^2 q.q^   (the algebra of Z_{k+1} = Z_k - a_k q^).
+// rho_{k+1} is then computed directly by launch k+1, so the estimate never compounds.
+// Z.q = P.q - ap P_{k-1}.q; with ar = 1 the second term vanishes by the conjugacy of
+// successive directions and is not formed; after a residual replacement (ar != 1) it is.
+// When rho_k meets the replacement or stopping threshold, launch k's direction work is
+// discarded (the iteration counter does not advance): Y and Z_k are consistent, the
+// FP64 residual replaces Z_k, and the iteration is redone from there with a = 0.
+//
+// Gathers: the columns of row i lie in [i - H, i + H] (H = matrix band).  A block owns a
+// contiguous row range and works through it in super-tiles of at most S rows (one for
+// the usual sizes).  Phase 1 streams the positions [lo - H, hi + H) of the super-tile
+// (Z, q^, P of the previous iteration), forms P_k into shared memory and updates Z, P
+// and Y of its own rows; after one barrier, phase 2 streams the matrix rows of the
+// super-tile and gathers P_k from shared memory.  Neither phase has a barrier inside,
+// so every warp keeps its loads in flight independently.  Halo positions belong to
+// neighbouring blocks and are recomputed there bit-identically; the Z, P and q^ buffers
+// are ping-pong pairs, so halos always read the previous iteration's values.
+#include <cstdlib>
+#include <vector>
+
+#include "cg_common.cuh"
+
+namespace adfem {
+
+struct ZcgArgs {
+  int64_t n;
+  int64_t L;          // rows per block (multiple of 32)
+  int S;              // rows per super-tile (multiple of 32)
+  int H;              // band: |col - row| <= H
+  int period;         // slice pattern period
+  int zw;             // fixed slice width of the banded layout
+  const int32_t* zpid;  // per slice: id of its column pattern in `pool`, or -1 (per-entry deltas in colz)
+  const int32_t* pool;  // [pattern id][period][MAXW] column deltas, padded with 0 (copied to shared memory)
+  int npool;            // ints in pool
+  const int16_t* colz;  // fixed-width sliced-ELL column deltas
+  const float* val;   // fixed-width sliced-ELL values, FP32 difference form, physical scale
+  const float* dz;    // fp32(K_ii)
+  float* z[2];
+  float* p[2];
+  float* q[2];
+  float* yh;
+  float* yl;
+  CgState* st;
+  double* partials;
+};
+
+// Positions and row indices are 32-bit (the plan requires n and the fixed-width layout
+// to stay below 2^31).  A warp's 32 rows are one slice (block ranges and super-tiles are
+// multiples of 32 rows), so the pattern/no-pattern branch is warp-uniform.
+template <int MAXW, int BT, int U1>
+__global__ void __launch_bounds__(BT, 2) k_zcg_iter(ZcgArgs A) {
+  static_assert(MAXW % 4 == 0, "pattern rows are loaded as int4");
+  CgState* st = A.st;
+  if (st->done) return;
+  extern __shared__ float zsm[];
+  int* spool = reinterpret_cast<int*>(zsm);           // column patterns (16-byte aligned)
+  float* sP = zsm + ((A.npool + 3) & ~3);             // P_k of the super-tile's positions
+  for (int j = threadIdx.x; j < A.npool; j += BT) spool[j] = __ldg(A.pool + j);
+  const int it = st->iters;
+  const int cur = it & 1, nxt = cur ^ 1;
+  const float* __restrict__ zprev = A.z[cur];
+  const float* __restrict__ pprev = A.p[cur];
+  const float* __restrict__ qprev = A.q[cur];
+  float* __restrict__ znew = A.z[nxt];
+  float* __restrict__ pnew = A.p[nxt];
+  float* __restrict__ qnew = A.q[nxt];
+  float* __restrict__ yh = A.yh;
+  float* __restrict__ yl = A.yl;
+  const float a = (float)st->alpha, ar = (float)st->ar, ap = (float)st->ap;
+  const bool full_zq = ar != 1.0f;  // uniform
+  const int tid = threadIdx.x;
+  const int zw = A.zw;
+  const int n = (int)A.n;
+  const int blo = (int)blockIdx.x * (int)A.L;
+  const int bhi = min(blo + (int)A.L, n);
+  float pq = 0.f, pkq = 0.f, qq = 0.f, rr = 0.f;
+
+  for (int lo = blo; lo < bhi; lo += A.S) {
+    const int hi = min(lo + A.S, bhi);
+    const int wlo = max(lo - A.H, 0);
+    const int whi = min(hi + A.H, n);
+    if (lo != blo) __syncthreads();  // the previous super-tile's gathers are done
+    // ---- phase 1: P_k for [wlo, whi) into shared memory; Z, P, Y of own rows.  All loads
+    // of a trip (U1 positions per thread) are issued before any store.
+    struct In {
+      float zp, qp, pp, h, l, d;
+      bool own;
+    };
+    auto fetch1 = [&](int pos, In& x) {
+      x.own = pos >= lo && pos < hi;
+      x.zp = __ldg(zprev + pos);
+      x.qp = __ldg(qprev + pos);
+      x.pp = __ldg(pprev + pos);
+      x.h = x.own ? yh[pos] : 0.f;
+      x.l = x.own ? yl[pos] : 0.f;
+      x.d = x.own ? __ldg(A.dz + pos) : 0.f;
+    };
+    auto commit = [&](int pos, In& x) {
+      const float zk = fmaf(-a, x.qp, x.zp);
+      const float pk = fmaf(ap, x.pp, __fmul_rn(ar, zk));
+      sP[pos - wlo] = pk;
+      if (x.own) {
+        znew[pos] = zk;
+        pnew[pos] = pk;
+        df_axpy(x.h, x.l, a, x.pp);
+        yh[pos] = x.h;
+        yl[pos] = x.l;
+        rr = fmaf(__fmul_rn(x.d, zk), zk, rr);
+      }
+    };
+    int pos = wlo + tid;
+    for (; pos + (U1 - 1) * BT < whi; pos += U1 * BT) {
+      In x[U1];
+#pragma unroll
+      for (int u = 0; u < U1; u++) fetch1(pos + u * BT, x[u]);
+#pragma unroll
+      for (int u = 0; u < U1; u++) commit(pos + u * BT, x[u]);
+    }
+    for (; pos < whi; pos += BT) {
+      In x0;
+      fetch1(pos, x0);
+      commit(pos, x0);
+    }
+    __syncthreads();
+    // ---- phase 2: q = K P_k for the rows [lo, hi)
+    auto row = [&](int i, const float (&v)[MAXW], float d, int pid) {
+      const float Pi = sP[i - wlo];
+      int dl[MAXW];
+      if (pid >= 0) {
+        // the slice's column pattern (int32, padded with 0 to MAXW per row parity)
+        const int4* pv = reinterpret_cast<const int4*>(spool) + (pid * A.period + (A.period == 2 ? (i & 1) : 0)) *
+                                                                     (MAXW / 4);
+#pragma unroll
+        for (int h = 0; h < MAXW / 4; h++) {
+          const int4 x = pv[h];
+          dl[4 * h] = x.x;
+          dl[4 * h + 1] = x.y;
+          dl[4 * h + 2] = x.z;
+          dl[4 * h + 3] = x.w;
+        }
+      } else {
+        const int base = (i >> 5) * (32 * zw) + (i & 31);
+#pragma unroll
+        for (int k = 0; k < MAXW; k++) dl[k] = k < zw ? (int)__ldg(A.colz + base + 32 * k) : 0;
+      }
+      float s = 0.f;
+#pragma unroll
+      for (int k = 0; k < MAXW; k++) {
+        const float tv = dl[k] == 0 ? Pi : __fsub_rn(sP[i + dl[k] - wlo], Pi);
+        s = fmaf(v[k], tv, s);
+      }
+      const float qh = __fdiv_rn(s, d);
+      qnew[i] = qh;
+      pq = fmaf(Pi, s, pq);
+      qq = fmaf(s, qh, qq);
+      if (full_zq) pkq = fmaf(__ldg(pprev + i), s, pkq);
+    };
+    // fixed-width layout: entry k of row i at (i>>5)*32*zw + 32k + (i&31) (padding: value 0,
+    // delta 0), so the loads of a row depend on nothing but i
+    auto fetch = [&](int i, float (&v)[MAXW], float& d, int& pid) {
+      const int base = (i >> 5) * (32 * zw) + (i & 31);
+#pragma unroll
+      for (int k = 0; k < MAXW; k++) v[k] = k < zw ? __ldg(A.val + base + 32 * k) : 0.f;
+      d = __ldg(A.dz + i);
+      pid = __ldg(A.zpid + (i >> 5));
+    };
+    int i = lo + tid;
+    for (; i + BT < hi; i += 2 * BT) {  // two rows per thread and trip
+      float v0[MAXW], v1[MAXW], d0, d1;
+      int g0, g1;
+      fetch(i, v0, d0, g0);
+      fetch(i + BT, v1, d1, g1);
+      row(i, v0, d0, g0);
+      row(i + BT, v1, d1, g1);
+    }
+    if (i < hi) {
+      float v0[MAXW], d0;
+      int g0;
+      fetch(i, v0, d0, g0);
+      row(i, v0, d0, g0);
+    }
+  }
+
+  double v[4] = {(double)pq, (double)pkq, (double)qq, (double)rr}, tot[4];
+  if (reduce_grid<double, 4, BT>(v, A.partials, &st->counter[0], tot) && threadIdx.x == 0) {
+    const double pqd = tot[0], qqd = tot[2], rho = tot[3];
+    const double zqd = (full_zq && st->ar != 0.0) ? (pqd - st->ap * tot[1]) / st->ar : pqd;
+    if (!isfinite(rho) || !isfinite(pqd)) {
+      st->done = 2;
+    } else if (rho <= st->stop2) {
+      st->final_req = 1;
+      st->done = 3;
+    } else if (rho <= st->ru2 || it >= st->max_iter) {
+      st->done = 3;  // the FP64 residual decides
+    } else if (!(pqd > 0.0)) {
+      st->done = 2;
+    } else {
+      const double al = rho / pqd;
+      const double est = rho - 2.0 * al * zqd + al * al * qqd;
+      st->alpha = al;
+      st->ar = 1.0;
+      st->ap = fmax(est, 0.0) / rho;
+      st->rho = rho;
+      st->iters = it + 1;
+    }
+  }
+}
+
+// Operator copies for the banded path from the unscaled FP64 sliced-ELL values:
+// difference form (off-diagonal K_ij, diagonal slot = row sum) in FP64 (sliced-ELL
+// layout, for the FP64 residual) and FP32 (fixed-width layout of width zw, whose
+// padding stays 0), and the FP32 diagonal.  Flags a non-positive or non-finite diagonal.
+__global__ void k_zprep(int64_t n, const int32_t* __restrict__ sptr, const double* __restrict__ val,
+                        const int32_t* __restrict__ diagpos, int zw, double* __restrict__ valz64,
+                        float* __restrict__ valz32, float* __restrict__ dz, int* __restrict__ bad) {
+  const int64_t r = gtid();
+  if (r >= n) return;
+  int64_t base;
+  int w;
+  sell_row(sptr, r, base, w);
+  const int64_t fbase = ((r >> 5) * 32) * zw + (r & 31);
+  double rs = 0.0;
+  for (int k = 0; k < w; k++) rs += val[base + 32 * (int64_t)k];
+  const int dp = diagpos[r];
+  for (int k = 0; k < w; k++) {
+    const int64_t idx = base + 32 * (int64_t)k;
+    const double v = k == dp ? rs : val[idx];
+    valz64[idx] = v;
+    valz32[fbase + 32 * (int64_t)k] = (float)v;
+  }
+  float d = (float)val[base + 32 * (int64_t)dp];
+  if (!(d > 0.0f) || !isfinite(d)) {
+    atomicExch(bad, 1);
+    d = 1.0f;
+  }
+  dz[r] = d;
+}
+
+// b = rhs (rows tagged 1 in zero_rows get 0), y0 = u0 or 0, ||b||_{D^-1}^2 and the
+// stopping threshold.
+__global__ void __launch_bounds__(kT) k_zinit(int64_t n, const double* __restrict__ rhs, const uint8_t* zero_rows,
+                                              const float* __restrict__ dz, const double* __restrict__ u0,
+                                              double* __restrict__ b, double* __restrict__ y, CgState* st,
+                                              double* partials, double rtol2) {
+  double acc = 0.0;
+  for (int64_t i = gtid(); i < n; i += gstride()) {
+    const double bi = (zero_rows && zero_rows[i] == 1) ? 0.0 : rhs[i];
+    b[i] = bi;
+    y[i] = u0 ? u0[i] : 0.0;
+    acc = fma(bi, bi / (double)dz[i], acc);
+  }
+  double v[1] = {acc}, tot[1];
+  if (reduce_grid<double, 1>(v, partials, &st->counter[0], tot) && threadIdx.x == 0) {
+    st->bnorm2 = tot[0];
+    st->stop2 = rtol2 * tot[0];
+  }
+}
+
+// FP64 residual r = b - K y in difference form; mode 1 also replaces Z (the buffer the
+// next iteration reads) by fp32(r / D) and supplies the re-orthogonalisation dot with
+// the direction that iteration starts from; mode 2 only records ||r||_{D^-1}^2.
+__global__ void __launch_bounds__(kT) k_zres64(int64_t n, const int32_t* __restrict__ sptr,
+                                               const int16_t* __restrict__ col, const double* __restrict__ valz,
+                                               const float* __restrict__ dz, const double* __restrict__ b,
+                                               const double* __restrict__ y, float* z0, float* z1, const float* p0,
+                                               const float* p1, CgState* st, double* partials, int mode, int force) {
+  if (!force && st->done != 3) return;
+  const int it = st->iters;
+  float* zc = (it & 1) ? z1 : z0;
+  const float* pc = (it & 1) ? p1 : p0;
+  double a0 = 0.0, a1 = 0.0, a2 = 0.0;
+  for (int64_t r = gtid(); r < n; r += gstride()) {
+    int64_t base;
+    int w;
+    sell_row(sptr, r, base, w);
+    const double yr = y[r];
+    double s = 0.0;
+    for (int k = 0; k < w; k++) {
+      const int64_t idx = base + 32 * (int64_t)k;
+      const int dl = (int)__ldg(col + idx);
+      const double t = dl == 0 ? yr : y[r + dl] - yr;
+      s = fma(valz[idx], t, s);
+    }
+    const double ri = b[r] - s;
+    const double di = (double)dz[r];
+    const double zt = ri / di;
+    a0 = fma(ri, zt, a0);
+    if (mode == 1) {
+      const float zf = (float)zt;
+      zc[r] = zf;
+      const double dzf = di * (double)zf;
+      a1 = fma(dzf, (double)zf, a1);
+      a2 = fma(dzf, (double)pc[r], a2);
+    }
+  }
+  double v[3] = {a0, a1, a2}, tot[3];
+  if (reduce_grid<double, 3>(v, partials, &st->counter[1], tot) && threadIdx.x == 0)
+    replacement_step(st, tot[0], tot[1], tot[2], mode);
+}
+
+// Per-entry column deltas of the fixed-width layout (once per operator pattern);
+// padding stays 0.
+__global__ void k_zlayout(int64_t n, const int32_t* __restrict__ sptr, const int16_t* __restrict__ col, int zw,
+                          int16_t* __restrict__ colz) {
+  const int64_t r = gtid();
+  if (r >= n) return;
+  int64_t base;
+  int w;
+  sell_row(sptr, r, base, w);
+  const int64_t fbase = ((r >> 5) * 32) * zw + (r & 31);
+  for (int k = 0; k < w; k++) colz[fbase + 32 * (int64_t)k] = col[base + 32 * (int64_t)k];
+}
+
+// u = y; rows tagged 1 get their prescribed value exactly (or 0)
+__global__ void k_zunscale(int64_t n, const double* __restrict__ y, const uint8_t* __restrict__ fix,
+                           const double* __restrict__ fixval, double* __restrict__ u) {
+  const int64_t i = gtid();
+  if (i >= n) return;
+  u[i] = (fix && fix[i] == 1) ? (fixval ? fixval[i] : 0.0) : y[i];
+}
+
+// ---------------------------------------------------------------------------
+static constexpr int kZBT = 512;                     // threads per block
+static constexpr int kZU1 = 4;                       // phase-1 positions per thread and trip
+static constexpr size_t kZSmemBlock = 100 * 1024;    // shared memory per block (two blocks per SM)
+
+// Distinct slice column patterns (at most kZMaxPatterns; further slices use their
+// per-entry deltas), padded to the kernel's unrolled width per row parity, and the
+// pattern id of every slice.  Built on the host from the operator's pattern pool.
+static constexpr int kZMaxPatterns = 32;
+
+template <class T>
+static int zupload(DevBuf& b, const T* src, size_t count) {
+  ADFEM_TRY(b.alloc(sizeof(T) * count));
+  ADFEM_CUDA(cudaMemcpy(b.p, src, sizeof(T) * count, cudaMemcpyHostToDevice));
+  return ADFEM_OK;
+}
+
+static int zcg_build_pool(Solver& S) {
+  const Sell& A = *S.A;
+  const int64_t ns = A.nslices;
+  const int period = A.pat_period;
+  std::vector<int32_t> spat(std::max<int64_t>(ns, 1)), sptr(ns + 1);
+  std::vector<int16_t> pat(A.pat.bytes / sizeof(int16_t));
+  ADFEM_CUDA(cudaMemcpy(spat.data(), A.spat.p, sizeof(int32_t) * spat.size(), cudaMemcpyDeviceToHost));
+  ADFEM_CUDA(cudaMemcpy(sptr.data(), A.sptr.p, sizeof(int32_t) * sptr.size(), cudaMemcpyDeviceToHost));
+  if (!pat.empty()) ADFEM_CUDA(cudaMemcpy(pat.data(), A.pat.p, A.pat.bytes, cudaMemcpyDeviceToHost));
+  std::vector<int32_t> zpid(std::max<int64_t>(ns, 1), -1), pool;
+  std::vector<int32_t> offs;  // pool offset of each pattern id
+  for (int64_t sl = 0; sl < ns; sl++) {
+    const int32_t so = spat[sl];
+    if (so < 0) continue;
+    const int w = (sptr[sl + 1] - sptr[sl]) / 32;
+    int id = -1;
+    for (size_t j = 0; j < offs.size(); j++)
+      if (offs[j] == so) id = (int)j;
+    if (id < 0) {
+      if ((int)offs.size() >= kZMaxPatterns || (size_t)so + (size_t)period * w > pat.size()) continue;
+      id = (int)offs.size();
+      offs.push_back(so);
+      for (int q = 0; q < period; q++)
+        for (int k = 0; k < S.zps; k++) pool.push_back(k < w ? (int32_t)pat[so + q * w + k] : 0);
+    }
+    zpid[sl] = id;
+  }
+  if (pool.empty()) pool.assign(4, 0);
+  S.znpool = (int)pool.size();
+  ADFEM_TRY(zupload(S.zpid32, zpid.data(), zpid.size()));
+  ADFEM_TRY(zupload(S.zpool32, pool.data(), pool.size()));
+  return ADFEM_OK;
+}
+
+template <int MAXW>
+static int zcg_configure(Solver& S, int sms) {
+  auto kern = k_zcg_iter<MAXW, kZBT, kZU1>;
+  ADFEM_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)S.zsmem));
+  int per = 0;
+  ADFEM_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kern, kZBT, S.zsmem));
+  if (per < 1) return fail(ADFEM_ERR_CUDA, "banded CG kernel cannot be resident");
+  const int64_t want = (int64_t)sms * per;
+  // at least one band width of rows per block, so that halos stay below twice the rows
+  int64_t L = (S.n + want - 1) / want;
+  L = std::max<int64_t>(std::max<int64_t>(L, S.zH), 32);
+  L = (L + 31) / 32 * 32;
+  S.zL = L;
+  S.zgrid = (int)((S.n + L - 1) / L);
+  S.zK = (int)((L + S.zS - 1) / S.zS);
+  return ADFEM_OK;
+}
+
+int zcg_plan(Solver& S, int sms) {
+  const Sell& A = *S.A;
+  S.zcg = false;
+  const char* env = std::getenv("ADFEM_ZCG");
+  if (env && env[0] == '0') return ADFEM_OK;
+  if (!A.delta16 || A.maxw > 16 || A.maxw < 1 || A.band > 32767 || S.n < 1) return ADFEM_OK;
+  // 32-bit positions and fixed-width indices
+  if (A.nslices * 32 * (int64_t)A.maxw >= INT32_MAX || S.n + A.band >= INT32_MAX) return ADFEM_OK;
+  const int H = (int)A.band;
+  S.zw = A.maxw;
+  S.zps = S.zw <= 8 ? 8 : 16;
+  ADFEM_TRY(zcg_build_pool(S));
+  const size_t pool_bytes = sizeof(int32_t) * (size_t)((S.znpool + 3) & ~3);
+  // super-tile rows: the whole per-block range when it fits beside its 2H halo, else the
+  // largest multiple of 32 that does; a halo larger than the rows it serves is not worth it
+  const int64_t per_block = ((S.n + 2 * (int64_t)sms - 1) / (2 * (int64_t)sms) + 31) / 32 * 32;
+  const int64_t room = (int64_t)((kZSmemBlock - pool_bytes) / sizeof(float)) - 2 * (int64_t)H;
+  int64_t smax = room / 32 * 32;
+  if (smax < std::max<int64_t>(1024, 2 * (int64_t)H)) return ADFEM_OK;  // scaled two-kernel path
+  // ADFEM_ZCG_SMAX caps the super-tile rows (a test hook for ranges split into several)
+  if (const char* cap = std::getenv("ADFEM_ZCG_SMAX")) {
+    const int64_t c = std::atoll(cap) / 32 * 32;
+    if (c >= 32) smax = std::min(smax, c);
+  }
+  S.zS = (int)std::min<int64_t>(std::max<int64_t>(per_block, ((int64_t)H + 31) / 32 * 32), smax);
+  S.zH = H;
+  S.zW = S.zS + 2 * H;
+  S.zsmem = pool_bytes + sizeof(float) * (size_t)S.zW;
+  if (A.maxw <= 8) ADFEM_TRY(zcg_configure<8>(S, sms));
+  else ADFEM_TRY(zcg_configure<16>(S, sms));
+  const size_t n4 = sizeof(float) * (size_t)S.n;
+  ADFEM_TRY(S.z1.alloc(n4));
+  ADFEM_TRY(S.zq1.alloc(n4));
+  ADFEM_TRY(S.dz32.alloc(n4));
+  // FP64 copy in the sliced-ELL layout; FP32 copy and column deltas in the fixed-width layout
+  const size_t ne = (size_t)std::max<int64_t>(A.nent, 1);
+  const size_t nf = (size_t)std::max<int64_t>(A.nslices, 1) * 32 * (size_t)S.zw;
+  ADFEM_TRY(S.valz64.alloc(sizeof(double) * ne));
+  ADFEM_TRY(S.valz32.alloc(sizeof(float) * nf));
+  ADFEM_TRY(S.colz16.alloc(sizeof(int16_t) * nf));
+  ADFEM_CUDA(cudaMemset(S.valz64.p, 0, sizeof(double) * ne));
+  ADFEM_CUDA(cudaMemset(S.valz32.p, 0, sizeof(float) * nf));
+  ADFEM_CUDA(cudaMemset(S.colz16.p, 0, sizeof(int16_t) * nf));
+  k_zlayout<<<(unsigned)((S.n + kT - 1) / kT), kT>>>(S.n, A.sptr.as<int32_t>(), A.col.as<int16_t>(), S.zw,
+                                                     S.colz16.as<int16_t>());
+  ADFEM_CUDA(cudaGetLastError());
+  ADFEM_CUDA(cudaDeviceSynchronize());
+  S.zcg = true;
+  return ADFEM_OK;
+}
+
+int zcg_prepare(Solver& S, const int32_t* diagpos_dev, int* bad_dev, cudaStream_t st) {
+  const Sell& A = *S.A;
+  const unsigned nb = (unsigned)((S.n + kT - 1) / kT);
+  k_zprep<<<nb, kT, 0, st>>>(S.n, A.sptr.as<int32_t>(), A.val64.as<double>(), diagpos_dev, S.zw,
+                             S.valz64.as<double>(), S.valz32.as<float>(), S.dz32.as<float>(), bad_dev);
+  ADFEM_CUDA(cudaGetLastError());
+  return ADFEM_OK;
+}
+
+static ZcgArgs zcg_args(Solver& S) {
+  const Sell& A = *S.A;
+  ZcgArgs z;
+  z.n = S.n;
+  z.L = S.zL;
+  z.S = S.zS;
+  z.H = S.zH;
+  z.period = A.pat_period;
+  z.zw = S.zw;
+  z.zpid = S.zpid32.as<int32_t>();
+  z.pool = S.zpool32.as<int32_t>();
+  z.npool = S.znpool;
+  z.colz = S.colz16.as<int16_t>();
+  z.val = S.valz32.as<float>();
+  z.dz = S.dz32.as<float>();
+  z.z[0] = S.r32.as<float>();
+  z.z[1] = S.z1.as<float>();
+  z.p[0] = S.pa32.as<float>();
+  z.p[1] = S.pb32.as<float>();
+  z.q[0] = S.q32.as<float>();
+  z.q[1] = S.zq1.as<float>();
+  z.yh = S.yh32.as<float>();
+  z.yl = S.yl32.as<float>();
+  z.st = S.state.as<CgState>();
+  z.partials = S.partials.as<double>();
+  return z;
+}
+
+void zcg_enqueue_iter(Solver& S, cudaStream_t st) {
+  const ZcgArgs z = zcg_args(S);
+  if (S.A->maxw <= 8) k_zcg_iter<8, kZBT, kZU1><<<S.zgrid, kZBT, S.zsmem, st>>>(z);
+  else k_zcg_iter<16, kZBT, kZU1><<<S.zgrid, kZBT, S.zsmem, st>>>(z);
+}
+
+void zcg_enqueue_init(Solver& S, cudaStream_t st, const double* rhs, const uint8_t* zero_rows, const double* u0,
+                      double rtol2) {
+  k_zinit<<<S.grid, kT, 0, st>>>(S.n, rhs, zero_rows, S.dz32.as<float>(), u0, S.b.as<double>(), S.y64.as<double>(),
+                                 S.state.as<CgState>(), S.partials.as<double>(), rtol2);
+}
+
+void zcg_enqueue_residual(Solver& S, cudaStream_t st, int mode, int force) {
+  const Sell& A = *S.A;
+  k_zres64<<<S.grid, kT, 0, st>>>(S.n, A.sptr.as<int32_t>(), A.col.as<int16_t>(), S.valz64.as<double>(),
+                                  S.dz32.as<float>(), S.b.as<double>(), S.y64.as<double>(), S.r32.as<float>(),
+                                  S.z1.as<float>(), S.pa32.as<float>(), S.pb32.as<float>(), S.state.as<CgState>(),
+                                  S.partials.as<double>(), mode, force);
+}
+
+void zcg_enqueue_unscale(Solver& S, cudaStream_t st, const uint8_t* fix, const double* fixval, double* u) {
+  k_zunscale<<<(unsigned)((S.n + kT - 1) / kT), kT, 0, st>>>(S.n, S.y64.as<double>(), fix, fixval, u);
+}
+
+// buffers the banded path zeroes before a solve
+int zcg_clear(Solver& S, cudaStream_t st) {
+  const size_t n4 = sizeof(float) * (size_t)S.n;
+  for (DevBuf* b : {&S.r32, &S.z1, &S.pa32, &S.pb32, &S.q32, &S.zq1, &S.yh32, &S.yl32})
+    ADFEM_CUDA(cudaMemsetAsync(b->p, 0, n4, st));
+  return ADFEM_OK;
+}
+
+}  // namespace adfem

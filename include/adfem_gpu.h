@@ -272,11 +272,27 @@ ADFEM_API int adfem_system_apply_d(adfem_system *sys, const double *x_d, double 
 ADFEM_API int adfem_system_rhs_d(adfem_system *sys, double *rhs_d, void *stream);
 /* Same solve as adfem_system_solve_d, launched kernel by kernel (no graph) with a CUDA
  * event pair around every launch on the solver's stream, for measurement.  kernel_ms[j]
- * and launches[j] receive the summed duration and launch count of: 0 SpMV+dot,
- * 1 vector update+dot, 2 p update (FP64) / fold (mixed), 3 FP64 residual. */
+ * and launches[j] receive the summed duration and launch count of: 0 SpMV+dot (the whole
+ * iteration on the banded mixed path), 1 vector update+dot, 2 p update (FP64) / fold
+ * (mixed), 3 FP64 residual. */
 ADFEM_API int adfem_system_solve_profiled_d(adfem_system *sys, double *u_d, const adfem_solver_opts *opts,
                                             adfem_solver_stats *stats, double *kernel_ms, long long *launches,
                                             void *stream);
+
+/* Layout of a system's solver operator and the mixed-precision iteration it uses (no
+ * counterpart in the reference; for traffic models and tests). */
+typedef struct adfem_solver_info {
+  long long rows;             /* solver DOFs */
+  long long stored;           /* sliced-ELL entries, padding included */
+  long long uniform_entries;  /* entries in slices whose column pattern is stored once */
+  long long slices;           /* 32-row slices */
+  long long band;             /* max |col - row| */
+  int banded;                 /* 1: one-kernel banded mixed iteration, 0: scaled two-kernel iteration */
+  int blocks;                 /* blocks of the banded iteration kernel (0 if not banded) */
+  long long rows_per_block;   /* contiguous rows per block (0 if not banded) */
+  int ring;                   /* shared-memory positions per super-tile: rows + 2 band (0 if not banded) */
+} adfem_solver_info;
+ADFEM_API int adfem_system_solver_info(const adfem_system *sys, adfem_solver_info *info);
 
 /* No counterpart in the reference.  Allocation-free FP64 Jacobi-CG on a caller-owned
  * device CSR matrix (0-based rowptr[n+1], colind[nnz], vals[nnz], symmetric positive
