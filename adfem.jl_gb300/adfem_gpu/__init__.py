@@ -349,6 +349,7 @@ def solve(K, F, precision: str = "fp64", rtol: float = 1e-12, max_iter: int = 20
     return (u, st) if return_stats else u
 
 
+from .server import Server  # noqa: E402
 from .system import ElasticitySystem, PoissonSystem  # noqa: E402
 
-__all__ += ["PoissonSystem", "ElasticitySystem"]
+__all__ += ["PoissonSystem", "ElasticitySystem", "Server"]

@@ -35,6 +35,28 @@ class SolverInfo(ctypes.Structure):
                 ("banded", c_i), ("blocks", c_i), ("rows_per_block", c_ll), ("ring", c_i)]
 
 
+class ServerConfig(ctypes.Structure):
+    _fields_ = [("hbm_budget_bytes", c_ll), ("workers", c_i), ("max_queue", c_i), ("opts", SolverOpts)]
+
+
+class Request(ctypes.Structure):
+    _fields_ = [("mesh", c_p), ("kind", c_i), ("in_", c_p * 4), ("bd", c_p), ("nbd", c_ll), ("bdval", c_p),
+                ("obs", c_p), ("nobs", c_ll), ("uobs", c_p), ("u", c_p), ("grad", c_p), ("deadline_ms", c_d),
+                ("warm_start", c_i), ("precision", c_i)]
+
+
+class Response(ctypes.Structure):
+    _fields_ = [("status", c_i), ("iterations", c_i), ("adjoint_iterations", c_i), ("relres", c_d), ("loss", c_d),
+                ("queue_ms", c_d), ("run_ms", c_d), ("total_ms", c_d), ("message", ctypes.c_char * 160)]
+
+
+class ServerStats(ctypes.Structure):
+    _fields_ = [("submitted", c_ll), ("completed", c_ll), ("rejected", c_ll), ("timeouts", c_ll), ("failed", c_ll),
+                ("cache_hits", c_ll), ("cache_misses", c_ll), ("evictions", c_ll), ("resident_systems", c_ll),
+                ("device_bytes", c_ll), ("p50_ms", c_d), ("p99_ms", c_d), ("mean_ms", c_d), ("max_ms", c_d),
+                ("p50_queue_ms", c_d), ("p99_queue_ms", c_d)]
+
+
 OK = 0
 ERR_INVALID = 1
 ERR_CUDA = 2
@@ -120,6 +142,13 @@ SIGNATURES = {
     "adfem_system_solve_profiled_d": (c_i, [c_p, c_p, ctypes.POINTER(SolverOpts), ctypes.POINTER(SolverStats), c_p,
                                             c_p, c_p]),
     "adfem_system_solver_info": (c_i, [c_p, ctypes.POINTER(SolverInfo)]),
+    "adfem_server_config_default": (None, [ctypes.POINTER(ServerConfig)]),
+    "adfem_server_create": (c_i, [ctypes.POINTER(ServerConfig), c_pp]),
+    "adfem_server_destroy": (c_i, [c_p]),
+    "adfem_server_submit": (c_i, [c_p, ctypes.POINTER(Request), ctypes.POINTER(c_ll)]),
+    "adfem_server_wait": (c_i, [c_p, c_ll, c_d, ctypes.POINTER(Response)]),
+    "adfem_server_get_stats": (c_i, [c_p, ctypes.POINTER(ServerStats)]),
+    "adfem_server_reset_stats": (c_i, [c_p]),
     "adfem_poisson_solve": (c_i, [c_p, c_p, c_p, c_p, ctypes.POINTER(SolverOpts), ctypes.POINTER(SolverStats)]),
     "adfem_csr_pcg_noalloc_d": (c_i, [c_i, c_p, c_p, c_p, c_p, c_p, c_d, c_i, c_p, c_p, c_p]),
 }

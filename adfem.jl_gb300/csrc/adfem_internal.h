@@ -42,15 +42,16 @@ struct DevBuf {
   DevBuf(const DevBuf&) = delete;
   DevBuf& operator=(const DevBuf&) = delete;
   ~DevBuf() { release(); }
-  void release() {
-    if (p) cudaFree(p);
-    p = nullptr;
-    bytes = 0;
-  }
+  void release();
   int alloc(size_t nbytes);  // (re)allocates only when larger storage is needed
   template <class T>
   T* as() const { return reinterpret_cast<T*>(p); }
 };
+
+// cudaMalloc and cudaFree may synchronize the device, which invalidates a CUDA-graph
+// capture running in another thread; the library's allocations and its graph captures
+// therefore take this lock (held briefly: a capture records a few dozen launches).
+std::mutex& device_alloc_mutex();
 
 // ---------------------------------------------------------------------------
 // Packed node->element incidence record.  For node i, each incident element e in
@@ -177,5 +178,11 @@ cudaError_t launch_stiffness_rows(const Mesh& m, const double* Dbar, double* val
                                   cudaStream_t st);
 cudaError_t launch_stiffness_coo(const Mesh& m, const double* D, long long* indices, double* vv, cudaStream_t st);
 cudaError_t launch_stiffness_coo_backward(const Mesh& m, const double* grad_vv, double* grad_D, cudaStream_t st);
+
+// Device bytes held by a resident system (operator copies, Dirichlet data, solver
+// vectors) -- what the serving loop counts against its HBM budget.
+size_t system_device_bytes(const adfem_system* s);
+// Mesh behind a handle (sizes for admission estimates).
+const Mesh* mesh_of(const adfem_mesh* h);
 
 }  // namespace adfem

@@ -114,6 +114,27 @@ int system_set_bd(adfem_system* s, const long long* bd, long long nbd, const dou
 
 }  // namespace
 
+namespace adfem {
+
+size_t system_device_bytes(const adfem_system* s) {
+  size_t b = 0;
+  const Sell& A = s->A;
+  for (const DevBuf* d : {&A.sptr, &A.col, &A.spat, &A.pat, &A.val64, &A.valD64, &A.val32, &s->diagpos, &s->isbd,
+                          &s->bdval, &s->rhs, &s->sigma, &s->src3, &s->srcy3, &s->Dbar, &s->t0, &s->t1, &s->t2,
+                          &s->in0, &s->in1})
+    b += d->bytes;
+  const Solver& v = s->solver;
+  for (const DevBuf* d : {&v.s32, &v.state, &v.partials, &v.b, &v.y64, &v.r64, &v.p64, &v.q64, &v.r32, &v.pa32,
+                          &v.pb32, &v.q32, &v.yh32, &v.yl32, &v.z1, &v.zq1, &v.dz32, &v.valz64, &v.valz32,
+                          &v.colz16, &v.zpid32, &v.zpool32})
+    b += d->bytes;
+  return b;
+}
+
+const Mesh* mesh_of(const adfem_mesh* h) { return h ? h->m : nullptr; }
+
+}  // namespace adfem
+
 extern "C" {
 
 const char* adfem_status_string(int st) {

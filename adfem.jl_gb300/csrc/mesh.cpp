@@ -25,10 +25,25 @@ int cuda_fail(cudaError_t e, const char* what) {
   return e == cudaErrorMemoryAllocation ? ADFEM_ERR_NOMEM : ADFEM_ERR_CUDA;
 }
 
+std::mutex& device_alloc_mutex() {
+  static std::mutex mu;
+  return mu;
+}
+
+void DevBuf::release() {
+  if (p) {
+    std::lock_guard<std::mutex> lk(device_alloc_mutex());
+    cudaFree(p);
+  }
+  p = nullptr;
+  bytes = 0;
+}
+
 int DevBuf::alloc(size_t nb) {
   if (p && nb <= bytes) return ADFEM_OK;
   release();
   if (nb == 0) return ADFEM_OK;
+  std::lock_guard<std::mutex> lk(device_alloc_mutex());
   cudaError_t e = cudaMalloc(&p, nb);
   if (e != cudaSuccess) {
     p = nullptr;

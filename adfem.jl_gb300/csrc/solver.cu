@@ -22,6 +22,7 @@
 #include <cmath>
 #include <cstdlib>
 #include <cstring>
+#include <thread>
 
 #include "cg_common.cuh"
 
@@ -527,7 +528,10 @@ Solver::~Solver() {
     if (e) cudaEventDestroy(e);
   for (auto& e : pev) cudaEventDestroy(e);
   if (stream) cudaStreamDestroy(stream);
-  if (h_state) cudaFreeHost(h_state);
+  if (h_state) {
+    std::lock_guard<std::mutex> lk(device_alloc_mutex());
+    cudaFreeHost(h_state);
+  }
 }
 
 template <class F>
@@ -590,7 +594,10 @@ int Solver::init(const Sell* A_, int64_t n_) {
   ADFEM_TRY(q32.alloc(n4));
   ADFEM_TRY(yh32.alloc(n4));
   ADFEM_TRY(yl32.alloc(n4));
-  if (!h_state) ADFEM_CUDA(cudaMallocHost(&h_state, 2 * sizeof(CgState)));
+  if (!h_state) {
+    std::lock_guard<std::mutex> lk(device_alloc_mutex());
+    ADFEM_CUDA(cudaMallocHost(&h_state, 2 * sizeof(CgState)));
+  }
   if (!stream) ADFEM_CUDA(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
   for (auto& e : ev)
     if (!e) ADFEM_CUDA(cudaEventCreate(&e));
@@ -771,16 +778,32 @@ static int chunk_launches(Path path, int chunk) {
 }
 
 // capture `chunk` iterations into a graph (kernels read all scalars from device state)
+// A capture can be invalidated by work another host thread does at the same time that
+// has to synchronise the device (allocations take device_alloc_mutex for that reason;
+// first-use loading of kernel code is another such event); such a capture is retried.
 static int capture_chunk(Solver& S, Path path, int chunk, cudaGraphExec_t* out) {
-  cudaGraph_t g = nullptr;
-  ADFEM_CUDA(cudaStreamBeginCapture(S.stream, cudaStreamCaptureModeThreadLocal));
-  for (int i = 0; i < chunk; i++) enqueue_iteration(S, path, i, chunk, S.stream);
-  cudaError_t e = cudaStreamEndCapture(S.stream, &g);
-  if (e != cudaSuccess) return cuda_fail(e, "cudaStreamEndCapture");
-  e = cudaGraphInstantiate(out, g, 0);
-  cudaGraphDestroy(g);
-  if (e != cudaSuccess) return cuda_fail(e, "cudaGraphInstantiate");
-  return ADFEM_OK;
+  cudaError_t e = cudaSuccess;
+  for (int attempt = 0; attempt < 8; attempt++) {
+    cudaGraph_t g = nullptr;
+    {
+      std::lock_guard<std::mutex> lk(device_alloc_mutex());
+      ADFEM_CUDA(cudaStreamBeginCapture(S.stream, cudaStreamCaptureModeThreadLocal));
+      for (int i = 0; i < chunk; i++) enqueue_iteration(S, path, i, chunk, S.stream);
+      e = cudaStreamEndCapture(S.stream, &g);
+    }
+    if (e == cudaErrorStreamCaptureInvalidated || e == cudaErrorStreamCaptureUnjoined) {
+      if (g) cudaGraphDestroy(g);
+      cudaGetLastError();  // the launches of the invalidated capture reported it too
+      std::this_thread::yield();
+      continue;
+    }
+    if (e != cudaSuccess) return cuda_fail(e, "cudaStreamEndCapture");
+    e = cudaGraphInstantiate(out, g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaGraphInstantiate");
+    return ADFEM_OK;
+  }
+  return cuda_fail(e, "cudaStreamEndCapture (retried)");
 }
 
 int solver_solve(Solver& S, const double* rhs, double* u, const uint8_t* zero_rows, const uint8_t* fix_rows,

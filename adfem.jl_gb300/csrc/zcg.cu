@@ -35,6 +35,7 @@
 // neighbouring blocks and are recomputed there bit-identically; the Z, P and q^ buffers
 // are ping-pong pairs, so halos always read the previous iteration's values.
 #include <cstdlib>
+#include <mutex>
 #include <vector>
 
 #include "cg_common.cuh"
@@ -392,7 +393,17 @@ static int zcg_build_pool(Solver& S) {
 template <int MAXW>
 static int zcg_configure(Solver& S, int sms) {
   auto kern = k_zcg_iter<MAXW, kZBT, kZU1>;
-  ADFEM_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)S.zsmem));
+  // The shared-memory limit is raised once per process to the most any plan uses:
+  // changing a kernel's attributes while another thread captures a graph with that
+  // kernel invalidates the capture.
+  static std::once_flag once;
+  static cudaError_t set_err = cudaSuccess;
+  std::call_once(once, [&] {
+    std::lock_guard<std::mutex> lk(device_alloc_mutex());
+    set_err = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kZSmemBlock);
+  });
+  if (set_err != cudaSuccess) return cuda_fail(set_err, "cudaFuncSetAttribute");
+  if (S.zsmem > kZSmemBlock) return fail(ADFEM_ERR_INVALID, "banded CG plan exceeds its shared-memory limit");
   int per = 0;
   ADFEM_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kern, kZBT, S.zsmem));
   if (per < 1) return fail(ADFEM_ERR_CUDA, "banded CG kernel cannot be resident");
@@ -453,7 +464,9 @@ int zcg_plan(Solver& S, int sms) {
   k_zlayout<<<(unsigned)((S.n + kT - 1) / kT), kT>>>(S.n, A.sptr.as<int32_t>(), A.col.as<int16_t>(), S.zw,
                                                      S.colz16.as<int16_t>());
   ADFEM_CUDA(cudaGetLastError());
-  ADFEM_CUDA(cudaDeviceSynchronize());
+  // legacy-stream sync, not a device-wide one: other threads may be capturing graphs on
+  // their (non-blocking) solver streams
+  ADFEM_CUDA(cudaStreamSynchronize(0));
   S.zcg = true;
   return ADFEM_OK;
 }

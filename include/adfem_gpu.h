@@ -310,6 +310,78 @@ ADFEM_API int adfem_csr_pcg_noalloc_d(int n, const int *rowptr_d, const int *col
                                       const double *rhs_d, double *u_d, double rtol, int max_iter, int *iterations,
                                       double *relres, void *stream);
 
+/* ---- serving loop (no counterpart in the reference, which holds one global mesh,
+ * deps/MFEM/API.cpp:6-10) ----
+ * A request = one forward solve on a caller-owned mesh (Poisson or plane-strain
+ * elasticity, the fields at the Gauss points, Dirichlet DOFs), optionally with a
+ * misfit L = sum (u[obs] - uobs)^2 whose gradient with respect to the field
+ * (kappa or E) is returned through the adjoint.  Worker threads, each with its own
+ * CUDA stream, take requests in arrival order and run them on resident systems kept
+ * per (mesh, kind) and reused (operator pattern, solver buffers and captured CUDA
+ * graphs stay on the device); a new request starts as soon as a worker frees, so
+ * requests of any size run concurrently.  Every request runs its own fixed-grid,
+ * fixed-order kernels: its results do not depend on what else is in flight.
+ * Admission: resident systems and worker buffers are counted against an HBM budget;
+ * idle systems are evicted least-recently-used; a request that cannot fit even in an
+ * empty server is rejected with ADFEM_ERR_BUSY, as is a submit to a full queue. */
+typedef struct adfem_server adfem_server;
+typedef struct adfem_server_config {
+  long long hbm_budget_bytes; /* device bytes for resident systems and worker buffers; 0: 80% of free memory */
+  int workers;                /* concurrent requests (one CUDA stream each); 0: 8 */
+  int max_queue;              /* pending requests accepted; 0: 65536 */
+  adfem_solver_opts opts;     /* solver options of every request (precision per request may override) */
+} adfem_server_config;
+ADFEM_API void adfem_server_config_default(adfem_server_config *cfg);
+
+typedef struct adfem_request {
+  adfem_mesh *mesh;          /* caller-owned, must outlive the request */
+  int kind;                  /* ADFEM_SYS_POISSON or ADFEM_SYS_ELASTICITY */
+  const double *in[4];       /* host, ngauss each: Poisson {kappa, f}; elasticity {E, nu, fx, fy} */
+  const long long *bd;       /* Dirichlet DOF ids, 1-based (elasticity: [x; y] ordering) */
+  long long nbd;
+  const double *bdval;       /* NULL: all zero */
+  const long long *obs;      /* optional observation DOF ids (1-based): misfit + gradient */
+  long long nobs;
+  const double *uobs;        /* observed values at obs */
+  double *u;                 /* host out, ndof */
+  double *grad;              /* host out, ngauss: dL/dkappa or dL/dE (required with obs) */
+  double deadline_ms;        /* from submission; a request not started by then gets ADFEM_ERR_TIMEOUT; 0: none */
+  int warm_start;            /* start from the last solution computed on the same resident system */
+  int precision;             /* ADFEM_PREC_FP64 / ADFEM_PREC_MIXED, or -1 for the server's */
+} adfem_request;
+
+typedef struct adfem_response {
+  int status;                /* ADFEM_OK or the failure status */
+  int iterations;            /* forward CG iterations */
+  int adjoint_iterations;    /* 0 without observations */
+  double relres;             /* forward FP64 relative residual */
+  double loss;               /* misfit, 0 without observations */
+  double queue_ms;           /* submission to start */
+  double run_ms;             /* start to completion */
+  double total_ms;           /* submission to completion */
+  char message[160];         /* failure message ("" on success) */
+} adfem_response;
+
+typedef struct adfem_server_stats {
+  long long submitted, completed, rejected, timeouts, failed;
+  long long cache_hits, cache_misses, evictions;
+  long long resident_systems, device_bytes;
+  double p50_ms, p99_ms, mean_ms, max_ms;  /* total latency of completed requests */
+  double p50_queue_ms, p99_queue_ms;
+} adfem_server_stats;
+
+ADFEM_API int adfem_server_create(const adfem_server_config *cfg, adfem_server **out);
+/* Stops accepting requests, finishes the queued ones, releases all resident systems. */
+ADFEM_API int adfem_server_destroy(adfem_server *srv);
+/* Queue a request (the request struct is copied; the arrays it points to must stay
+ * valid until the request completes).  ticket receives its id. */
+ADFEM_API int adfem_server_submit(adfem_server *srv, const adfem_request *req, long long *ticket);
+/* Wait up to timeout_ms (< 0: forever) for a request; ADFEM_OK with the response once
+ * it completed (the ticket is then released), ADFEM_ERR_TIMEOUT if still running. */
+ADFEM_API int adfem_server_wait(adfem_server *srv, long long ticket, double timeout_ms, adfem_response *resp);
+ADFEM_API int adfem_server_get_stats(adfem_server *srv, adfem_server_stats *stats);
+ADFEM_API int adfem_server_reset_stats(adfem_server *srv);
+
 /* One host-buffer call for the whole Poisson forward path: upload kappa and f,
  * assemble, impose u = bdval on bd, solve, download u.  The end-to-end entry a Julia
  * caller uses for `K\F` after compute_fem_laplace_matrix1 / compute_fem_source_term1 /
