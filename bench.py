@@ -13,7 +13,10 @@ of matrix and vectors) is larger than L2 (129 MB), so no flush is needed.
 
 Printed: one JSON line (rank 0) with value = solves/s over all ranks, the
 FP64-CG comparison, grads/s, roofline of the dominant kernel, the end-to-end
-rate through the host-buffer C ABI call, the CPU baseline and SM clocks.
+rate through the host-buffer C ABI call, the CPU baseline, SM clocks and the
+serving workload ("serve": a stream of independent Poisson/elasticity requests of
+16x16 to 1024x1024 cells through the library's request server, saturation
+throughput and p50/p99 latency under open-loop Poisson arrivals).
 ``--impl reference`` times the CPU restatement of the reference path instead.
 """
 from __future__ import annotations
@@ -37,7 +40,7 @@ sys.path.insert(0, os.path.join(ROOT, "oracle"))
 METRIC = "solves/s & grads/s at 4M DOF, mixed vs FP64 @1e-10; serve p50/p99 ms"
 UNIT = "solves/s"
 # FP64 Jacobi-CG iterations this workload needs at the default rtol on GB300; the
-# reference arm scales its per-iteration CPU time by this count.
+# reference arm times a bounded number of CPU iterations and scales to this count.
 FP64_ITERS_DEFAULT = 14346
 
 
@@ -258,6 +261,125 @@ def run_reference(args, rank, world):
     return 0
 
 
+# ----------------------------------------------------------------------------- serving (C5)
+SERVE_SIZES = sorted({int(round(16 * 2 ** (k / 4))) for k in range(25)})  # 16 .. 1024, ratio 2^(1/4)
+
+
+class ServeCatalog:
+    """Meshes and input fields of the serving workload, prepared before any timing: per
+    mesh size m (jittered m x m square, seed 0) the Dirichlet sets (Poisson: boundary;
+    elasticity: left edge clamped in x and y), 1% observation DOFs, the shared fields
+    (f = 1e5(x+y); nu = 0.3, body force (0, -1e6)) and two seeded variants of kappa =
+    1 + exp(0.5 G) and E = 1e9 exp(0.3 G) (G a unit-variance Fourier field)."""
+
+    def __init__(self, A, sizes, variants=2):
+        import torch
+        from adfem_gpu import synth
+
+        self.sizes = sizes
+        self.items = {}
+        for m in sizes:
+            coords, elems = synth.jittered_square(m, seed=0)
+            mesh = A.Mesh(coords, elems)
+            g = torch.tensor(A.gauss_nodes(mesh), device="cuda")
+            ng = g.shape[0]
+            nv = mesh.nnode
+            left = synth.left_edge_nodes(coords) + 1
+            rng = np.random.default_rng(m)
+            it = {"mesh": mesh, "ndof": (nv, 2 * nv),
+                  "bd": (A.bcnode(mesh), np.concatenate([left, left + nv])),
+                  "f": (1e5 * (g[:, 0] + g[:, 1])).cpu().numpy(),
+                  "nu": np.full(ng, 0.3), "fx": np.zeros(ng), "fy": np.full(ng, -1e6),
+                  "kappa": [], "E": [], "obs": []}
+            for v in range(variants):
+                G = synth.fourier_field(g[:, 0], g[:, 1], seed=1000 * m + v)
+                it["kappa"].append((1.0 + torch.exp(0.5 * G)).cpu().numpy())
+                it["E"].append((1e9 * torch.exp(0.3 * G)).cpu().numpy())
+            for nd in it["ndof"]:
+                ob = np.sort(rng.choice(np.arange(1, nd + 1), max(1, nd // 100), replace=False))
+                it["obs"].append((ob, 1e-3 * rng.standard_normal(ob.size)))
+            self.items[m] = it
+
+    def requests(self, count, seed):
+        """(m, kind, variant, with_gradient) for `count` requests with per-request draws."""
+        rng = np.random.default_rng(seed)
+        lo, hi = math.log(16), math.log(1024)
+        out = []
+        for _ in range(count):
+            mc = math.exp(rng.uniform(lo, hi))
+            m = min(self.sizes, key=lambda s: abs(math.log(s) - math.log(mc)))
+            kind = 0 if rng.random() < 0.8 else 1
+            out.append((m, kind, int(rng.integers(0, 2)), bool(rng.random() < 0.5)))
+        return out
+
+    def submit(self, srv, req):
+        m, kind, v, grad = req
+        it = self.items[m]
+        fields = (it["kappa"][v], it["f"]) if kind == 0 else (it["E"][v], it["nu"], it["fx"], it["fy"])
+        ob, uo = it["obs"][kind] if grad else (None, None)
+        return srv.submit(it["mesh"], kind, fields, it["bd"][kind], obs=ob, uobs=uo)
+
+    def dof(self, req):
+        return self.items[req[0]]["ndof"][req[1]]
+
+
+def run_serve(A, args):
+    """C5 serving workload through adfem_gpu.Server: a warm-up pass over every (size,
+    kind), a saturation run (all requests queued at once) and an open-loop sweep with
+    Poisson arrivals at fractions of the saturation throughput."""
+    t0 = time.perf_counter()
+    cat = ServeCatalog(A, SERVE_SIZES)
+    setup_s = time.perf_counter() - t0
+    with A.Server(workers=args.serve_workers, precision="mixed", rtol=args.serve_rtol) as srv:
+        warm = [(m, k, 0, True) for m in SERVE_SIZES for k in (0, 1)]
+        for t in [cat.submit(srv, r) for r in warm]:
+            srv.wait(t)
+        # saturation: every request queued at t = 0
+        reqs = cat.requests(args.serve_requests, seed=11)
+        srv.reset_stats()
+        ts = time.perf_counter()
+        tickets = [cat.submit(srv, r) for r in reqs]
+        resps = [srv.wait(t)[0] for t in tickets]
+        wall = time.perf_counter() - ts
+        st = srv.stats()
+        bad = sum(1 for r in resps if r["status"] != 0)
+        sat = {"requests": len(reqs), "wall_s": wall, "throughput_req_s": len(reqs) / wall,
+               "dof_per_s": sum(cat.dof(r) for r in reqs) / wall, "p50_ms": st["p50_ms"], "p99_ms": st["p99_ms"],
+               "failed": bad, "gradients": sum(1 for r in reqs if r[3])}
+        # open loop: exponential inter-arrival gaps at a fraction of the saturation rate
+        sweep = []
+        for frac in args.serve_loads:
+            rate = frac * sat["throughput_req_s"]
+            sub = cat.requests(args.serve_sweep_requests, seed=int(100 * frac))
+            gaps = np.random.default_rng(int(1000 * frac)).exponential(1.0 / rate, len(sub))
+            srv.reset_stats()
+            ts = time.perf_counter()
+            nxt = ts
+            tickets = []
+            for r, gap in zip(sub, gaps):
+                nxt += gap
+                dt = nxt - time.perf_counter()
+                if dt > 0:
+                    time.sleep(dt)
+                tickets.append(cat.submit(srv, r))
+            rs = [srv.wait(t)[0] for t in tickets]
+            wall = time.perf_counter() - ts
+            s = srv.stats()
+            sweep.append({"offered_req_s": rate, "load": frac, "achieved_req_s": len(sub) / wall,
+                          "p50_ms": s["p50_ms"], "p99_ms": s["p99_ms"], "p50_queue_ms": s["p50_queue_ms"],
+                          "failed": sum(1 for r in rs if r["status"] != 0)})
+        cache = srv.stats()
+    ref = min(sweep, key=lambda x: abs(x["load"] - 0.5)) if sweep else None
+    return {"workload": "C5 mix: 80/20 Poisson/elasticity, m log-uniform in [16,1024] rounded to %d sizes "
+                        "(ratio 2^(1/4)), 50%% with a misfit gradient (1%% observations), seeded fields"
+                        % len(SERVE_SIZES),
+            "workers": args.serve_workers, "rtol": args.serve_rtol, "precision": "mixed",
+            "p50_ms": ref["p50_ms"] if ref else sat["p50_ms"], "p99_ms": ref["p99_ms"] if ref else sat["p99_ms"],
+            "latency_at_load": ref["load"] if ref else 1.0,
+            "saturation": sat, "sweep": sweep, "setup_s": setup_s,
+            "resident_systems": cache["resident_systems"], "device_bytes": cache["device_bytes"]}
+
+
 # ----------------------------------------------------------------------------- our arm
 def run_ours(args, rank, world, dist):
     import torch
@@ -423,6 +545,9 @@ def run_ours(args, rank, world, dist):
     e2e_value = world * args.steps / e2e_s
     err_e2e = float(_np.max(_np.abs(uh.numpy() - u_ref.cpu().numpy())) / float(u_ref.abs().max()))
 
+    # ------------------------------------------------------------------ serving (C5)
+    serve = run_serve(A, args) if args.serve_requests > 0 else None
+
     # ------------------------------------------------------------------ CPU baseline (rank 0, N=1)
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
@@ -466,6 +591,7 @@ def run_ours(args, rank, world, dist):
             "gpu_launches": launches,
             "clocks": clocks,
             "cpu_baseline": cpu,
+            "serve": serve,
         }
         print(json.dumps(line), flush=True)
     return 0
@@ -487,6 +613,12 @@ def main():
     ap.add_argument("--ref-iters", type=int, default=10)
     ap.add_argument("--fp64-iters", type=int, default=FP64_ITERS_DEFAULT)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--serve-requests", type=int, default=300,
+                    help="serving workload: requests of the saturation run (0 skips serving)")
+    ap.add_argument("--serve-sweep-requests", type=int, default=150)
+    ap.add_argument("--serve-loads", type=float, nargs="*", default=[0.5, 0.8])
+    ap.add_argument("--serve-workers", type=int, default=8)
+    ap.add_argument("--serve-rtol", type=float, default=1e-9)
     ap.add_argument("--trace-iters", type=int, default=0,
                     help="profiling aid: run one truncated step (this many CG iterations) and exit")
     args = ap.parse_args()
