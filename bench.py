@@ -380,6 +380,133 @@ def run_serve(A, args):
             "resident_systems": cache["resident_systems"], "device_bytes": cache["device_bytes"]}
 
 
+# ----------------------------------------------------------------------------- C2, C4
+def run_c2(A, args):
+    """Inverse Poisson at m x m cells (C2, m = 1000: 1,002,001 DOF, 6M Gauss points).
+    kappa_true = 1 + exp(0.5 G) (G: unit-variance 64-mode Fourier field, seed 1), f = 1e5(x+y),
+    u = 0 on the boundary; observations at 1% of the nodes (seed 3) of the true solution
+    plus N(0, 1e-3^2) noise (seed 4); L = sum (u[obs] - uobs)^2.  The gradient dL/dkappa at
+    all Gauss points is taken at the iterate kappa0 = kappa_true (1 + 0.1 G2) (G2 seed 5)
+    by one mixed forward and one mixed adjoint solve; grads/s is timed over `c2_steps`
+    such gradients.  Check: central differences of L (FP64 solves, rtol 1e-13) along
+    `c2_dirs` random unit directions d with step eps = 1e-4 ||kappa0||, against d.grad
+    from an FP64 adjoint."""
+    import torch
+    from adfem_gpu import synth
+
+    m = args.c2_m
+    coords, elems = synth.jittered_square(m, seed=0)
+    mesh = A.Mesh(coords, elems)
+    g = torch.tensor(A.gauss_nodes(mesh), device="cuda")
+    G = synth.fourier_field(g[:, 0], g[:, 1], seed=1)
+    G2 = synth.fourier_field(g[:, 0], g[:, 1], seed=5)
+    kap_true = (1.0 + torch.exp(0.5 * G)).contiguous()
+    kap0 = (kap_true * (1.0 + 0.1 * G2)).contiguous()
+    f = (1e5 * (g[:, 0] + g[:, 1])).contiguous()
+    S = A.PoissonSystem(mesh)
+    S.set_dirichlet(A.bcnode(mesh))
+    S.assemble(kap_true, f)
+    u_true = S.solve(precision="fp64", rtol=1e-13)
+    obs = torch.tensor(synth.observation_nodes(mesh.nnode, seed=3), device="cuda")
+    noise = torch.randn(obs.numel(), dtype=torch.float64, device="cuda",
+                        generator=torch.Generator(device="cuda").manual_seed(4))
+    uobs = u_true[obs] + 1e-3 * noise
+
+    def loss_grad(kap, precision, rtol, grad=True):
+        S.assemble(kap, f)
+        u = S.solve(precision=precision, rtol=rtol)
+        r = u[obs] - uobs
+        L = float((r * r).sum())
+        if not grad:
+            return L, None
+        gu = torch.zeros_like(u)
+        gu[obs] = 2 * r
+        lam = S.adjoint(gu, precision=precision, rtol=rtol)
+        return L, S.grad_kappa(u, lam)
+
+    loss_grad(kap0, "mixed", args.rtol)  # warm-up (graph capture)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(args.c2_steps):
+        L, gk = loss_grad(kap0, "mixed", args.rtol)
+    torch.cuda.synchronize()
+    grads_s = args.c2_steps / (time.perf_counter() - t0)
+    # finite-difference check of the adjoint gradient (FP64 solves)
+    L0, g64 = loss_grad(kap0, "fp64", 1e-13)
+    eps = 1e-4 * float(kap0.norm())
+    gen = torch.Generator(device="cuda").manual_seed(6)
+    errs = []
+    for _ in range(args.c2_dirs):
+        d = torch.randn(kap0.numel(), dtype=torch.float64, device="cuda", generator=gen)
+        d /= d.norm()
+        lp, _ = loss_grad(kap0 + eps * d, "fp64", 1e-13, grad=False)
+        lm, _ = loss_grad(kap0 - eps * d, "fp64", 1e-13, grad=False)
+        fd = (lp - lm) / (2 * eps)
+        an = float((g64 * d).sum())
+        errs.append(abs(fd - an) / max(abs(an), 1e-300))
+    return {"workload": "inverse Poisson %dx%d jittered, %d DOF, %d Gauss-point parameters, 1%% observations"
+                        % (m, m, mesh.nnode, kap0.numel()),
+            "grads_per_s": grads_s, "loss": L, "grad_mixed_vs_fp64_rel": float((gk - g64).norm() / g64.norm()),
+            "fd_check": {"directions": args.c2_dirs, "eps": eps, "max_rel_err": max(errs) if errs else None,
+                         "median_rel_err": statistics.median(errs) if errs else None}}
+
+
+def run_c4(A, args):
+    """Plane-strain elasticity at m x m cells, 2 DOF per node (C4, m = 1000: 2,004,002 DOF).
+    E = 1e9 exp(0.3 G) (G: unit-variance Fourier field, seed 2), nu = 0.3 with the
+    reference's plane-strain matrix, body force (0, -1e6), nodes on x = 0 clamped in both
+    components.  FP64 and mixed solves/s (each against an FP64 reference at rtol 1e-12)
+    and grads/s of a misfit at 1% of the DOFs with respect to E at every Gauss point."""
+    import torch
+    from adfem_gpu import synth
+
+    m = args.c4_m
+    coords, elems = synth.jittered_square(m, seed=0)
+    mesh = A.Mesh(coords, elems)
+    g = torch.tensor(A.gauss_nodes(mesh), device="cuda")
+    ng = g.shape[0]
+    E = (1e9 * torch.exp(0.3 * synth.fourier_field(g[:, 0], g[:, 1], seed=2))).contiguous()
+    nu = torch.full((ng,), 0.3, dtype=torch.float64, device="cuda")
+    fx = torch.zeros(ng, dtype=torch.float64, device="cuda")
+    fy = torch.full((ng,), -1e6, dtype=torch.float64, device="cuda")
+    S = A.ElasticitySystem(mesh)
+    left = synth.left_edge_nodes(coords) + 1
+    S.set_dirichlet(np.concatenate([left, left + mesh.nnode]))
+    S.assemble(E, nu, fx, fy)
+    u_ref = S.solve(precision="fp64", rtol=1e-12)
+    ref_iters = S.last_stats.iterations
+    out = {"workload": "plane-strain elasticity %dx%d jittered, %d DOF, left edge clamped" % (m, m, 2 * mesh.nnode),
+           "fp64_reference": {"rtol": 1e-12, "iters": ref_iters}}
+    u = torch.zeros_like(u_ref)
+    for prec, rtol in (("fp64", args.rtol_fp64), ("mixed", args.rtol)):
+        S.solve(u, precision=prec, rtol=rtol)  # warm-up (graph capture)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(args.c4_steps):
+            S.assemble(E, nu, fx, fy)
+            S.solve(u, precision=prec, rtol=rtol)
+        torch.cuda.synchronize()
+        out[prec] = {"solves_per_s": args.c4_steps / (time.perf_counter() - t0), "rtol": rtol,
+                     "iters": S.last_stats.iterations,
+                     "rel_err_vs_fp64_ref": float((u - u_ref).abs().max() / u_ref.abs().max())}
+    out["speedup_mixed_over_fp64"] = out["mixed"]["solves_per_s"] / out["fp64"]["solves_per_s"]
+    obs = torch.tensor(synth.observation_nodes(2 * mesh.nnode, seed=7), device="cuda")
+    uobs = u_ref[obs] * 1.01
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(args.c4_steps):
+        S.assemble(E, nu, fx, fy)
+        S.solve(u, precision="mixed", rtol=args.rtol)
+        gu = torch.zeros_like(u)
+        gu[obs] = 2 * (u[obs] - uobs)
+        lam = S.adjoint(gu, precision="mixed", rtol=args.rtol)
+        gE = S.grad_E(u, lam, E, nu)
+    torch.cuda.synchronize()
+    out["grads_per_s"] = args.c4_steps / (time.perf_counter() - t0)
+    out["grad_norm"] = float(gE.norm())
+    return out
+
+
 # ----------------------------------------------------------------------------- our arm
 def run_ours(args, rank, world, dist):
     import torch
@@ -547,6 +674,8 @@ def run_ours(args, rank, world, dist):
 
     # ------------------------------------------------------------------ serving (C5)
     serve = run_serve(A, args) if args.serve_requests > 0 else None
+    c2 = run_c2(A, args) if args.c2_m > 0 else None
+    c4 = run_c4(A, args) if args.c4_m > 0 else None
 
     # ------------------------------------------------------------------ CPU baseline (rank 0, N=1)
     cpu = None
@@ -592,6 +721,8 @@ def run_ours(args, rank, world, dist):
             "clocks": clocks,
             "cpu_baseline": cpu,
             "serve": serve,
+            "inverse_poisson_1M": c2,
+            "elasticity_2M": c4,
         }
         print(json.dumps(line), flush=True)
     return 0
@@ -619,6 +750,11 @@ def main():
     ap.add_argument("--serve-loads", type=float, nargs="*", default=[0.5, 0.8])
     ap.add_argument("--serve-workers", type=int, default=8)
     ap.add_argument("--serve-rtol", type=float, default=1e-9)
+    ap.add_argument("--c2-m", type=int, default=1000, help="inverse Poisson cells per side (0 skips)")
+    ap.add_argument("--c2-steps", type=int, default=2)
+    ap.add_argument("--c2-dirs", type=int, default=32, help="finite-difference directions of the gradient check")
+    ap.add_argument("--c4-m", type=int, default=1000, help="elasticity cells per side (0 skips)")
+    ap.add_argument("--c4-steps", type=int, default=1)
     ap.add_argument("--trace-iters", type=int, default=0,
                     help="profiling aid: run one truncated step (this many CG iterations) and exit")
     args = ap.parse_args()
