@@ -62,6 +62,7 @@ struct Solver {
   int znpool = 0;          // ints in zpool32
   int zw = 0;              // fixed slice width (widest slice)
   int zps = 0;             // pattern row stride (8 or 16, the kernel's unrolled width)
+  bool zblock2 = false;    // interleaved 2-DOF operator in block difference form
   cudaGraphExec_t gz = nullptr;
   int gz_chunk = 0;
   ~Solver();

@@ -67,7 +67,11 @@ struct ZcgArgs {
 // Positions and row indices are 32-bit (the plan requires n and the fixed-width layout
 // to stay below 2^31).  A warp's 32 rows are one slice (block ranges and super-tiles are
 // multiples of 32 rows), so the pattern/no-pattern branch is warp-uniform.
-template <int MAXW, int BT, int U1>
+// B2: block difference form of an interleaved 2-DOF operator (rows 2a, 2a+1 are the x, y
+// DOFs of node a): each neighbour is differenced against the value of the same component
+// at row i's node, the same-component row sum sits in the diagonal slot and the
+// other-component row sum in the slot of the partner DOF i^1 (see k_zprep).
+template <int MAXW, int BT, int U1, bool B2>
 __global__ void __launch_bounds__(BT, 2) k_zcg_iter(ZcgArgs A) {
   static_assert(MAXW % 4 == 0, "pattern rows are loaded as int4");
   CgState* st = A.st;
@@ -145,6 +149,8 @@ __global__ void __launch_bounds__(BT, 2) k_zcg_iter(ZcgArgs A) {
     // ---- phase 2: q = K P_k for the rows [lo, hi)
     auto row = [&](int i, const float (&v)[MAXW], float d, int pid) {
       const float Pi = sP[i - wlo];
+      const float Pp = B2 ? sP[(i ^ 1) - wlo] : Pi;  // partner DOF (B2: rows come in even/odd pairs)
+      const int dpart = (i & 1) ? -1 : 1;            // column delta of the partner DOF
       int dl[MAXW];
       if (pid >= 0) {
         // the slice's column pattern (int32, padded with 0 to MAXW per row parity)
@@ -166,7 +172,10 @@ __global__ void __launch_bounds__(BT, 2) k_zcg_iter(ZcgArgs A) {
       float s = 0.f;
 #pragma unroll
       for (int k = 0; k < MAXW; k++) {
-        const float tv = dl[k] == 0 ? Pi : __fsub_rn(sP[i + dl[k] - wlo], Pi);
+        float tv;
+        if (dl[k] == 0) tv = Pi;
+        else if (B2 && dl[k] == dpart) tv = Pp;
+        else tv = __fsub_rn(sP[i + dl[k] - wlo], (B2 && (dl[k] & 1)) ? Pp : Pi);
         s = fmaf(v[k], tv, s);
       }
       const float qh = __fdiv_rn(s, d);
@@ -229,22 +238,32 @@ __global__ void __launch_bounds__(BT, 2) k_zcg_iter(ZcgArgs A) {
 // Operator copies for the banded path from the unscaled FP64 sliced-ELL values:
 // difference form (off-diagonal K_ij, diagonal slot = row sum) in FP64 (sliced-ELL
 // layout, for the FP64 residual) and FP32 (fixed-width layout of width zw, whose
-// padding stays 0), and the FP32 diagonal.  Flags a non-positive or non-finite diagonal.
-__global__ void k_zprep(int64_t n, const int32_t* __restrict__ sptr, const double* __restrict__ val,
-                        const int32_t* __restrict__ diagpos, int zw, double* __restrict__ valz64,
-                        float* __restrict__ valz32, float* __restrict__ dz, int* __restrict__ bad) {
+// padding stays 0), and the FP32 diagonal.  With block2 (interleaved 2-DOF operator)
+// the diagonal slot holds the row sum over same-component columns and the partner
+// slot (column i^1) the sum over other-component columns: the two sums vanish in
+// interior rows (rigid translations), which keeps FP32 rounding relative to the
+// component-wise differences.  Flags a non-positive or non-finite diagonal.
+__global__ void k_zprep(int64_t n, const int32_t* __restrict__ sptr, const int16_t* __restrict__ col,
+                        const double* __restrict__ val, const int32_t* __restrict__ diagpos, int zw, int block2,
+                        double* __restrict__ valz64, float* __restrict__ valz32, float* __restrict__ dz,
+                        int* __restrict__ bad) {
   const int64_t r = gtid();
   if (r >= n) return;
   int64_t base;
   int w;
   sell_row(sptr, r, base, w);
   const int64_t fbase = ((r >> 5) * 32) * zw + (r & 31);
-  double rs = 0.0;
-  for (int k = 0; k < w; k++) rs += val[base + 32 * (int64_t)k];
+  const int dpart = (r & 1) ? -1 : 1;
+  double rs = 0.0, ro = 0.0;  // same-component / other-component row sums
+  for (int k = 0; k < w; k++) {
+    const double v = val[base + 32 * (int64_t)k];
+    if (block2 && (col[base + 32 * (int64_t)k] & 1)) ro += v;
+    else rs += v;
+  }
   const int dp = diagpos[r];
   for (int k = 0; k < w; k++) {
     const int64_t idx = base + 32 * (int64_t)k;
-    const double v = k == dp ? rs : val[idx];
+    const double v = k == dp ? rs : ((block2 && col[idx] == dpart) ? ro : val[idx]);
     valz64[idx] = v;
     valz32[fbase + 32 * (int64_t)k] = (float)v;
   }
@@ -281,7 +300,7 @@ __global__ void __launch_bounds__(kT) k_zinit(int64_t n, const double* __restric
 // the direction that iteration starts from; mode 2 only records ||r||_{D^-1}^2.
 __global__ void __launch_bounds__(kT) k_zres64(int64_t n, const int32_t* __restrict__ sptr,
                                                const int16_t* __restrict__ col, const double* __restrict__ valz,
-                                               const float* __restrict__ dz, const double* __restrict__ b,
+                                               int block2, const float* __restrict__ dz, const double* __restrict__ b,
                                                const double* __restrict__ y, float* z0, float* z1, const float* p0,
                                                const float* p1, CgState* st, double* partials, int mode, int force) {
   if (!force && st->done != 3) return;
@@ -294,11 +313,16 @@ __global__ void __launch_bounds__(kT) k_zres64(int64_t n, const int32_t* __restr
     int w;
     sell_row(sptr, r, base, w);
     const double yr = y[r];
+    const int dpart = (r & 1) ? -1 : 1;
+    const double yp = block2 ? y[r ^ 1] : yr;
     double s = 0.0;
     for (int k = 0; k < w; k++) {
       const int64_t idx = base + 32 * (int64_t)k;
       const int dl = (int)__ldg(col + idx);
-      const double t = dl == 0 ? yr : y[r + dl] - yr;
+      double t;
+      if (dl == 0) t = yr;
+      else if (block2 && dl == dpart) t = yp;
+      else t = y[r + dl] - ((block2 && (dl & 1)) ? yp : yr);
       s = fma(valz[idx], t, s);
     }
     const double ri = b[r] - s;
@@ -319,16 +343,24 @@ __global__ void __launch_bounds__(kT) k_zres64(int64_t n, const int32_t* __restr
 }
 
 // Per-entry column deltas of the fixed-width layout (once per operator pattern);
-// padding stays 0.
+// padding stays 0.  no_partner is set when a row lacks the entry of its partner DOF
+// (column r^1), which the block difference form of 2-DOF operators needs.
 __global__ void k_zlayout(int64_t n, const int32_t* __restrict__ sptr, const int16_t* __restrict__ col, int zw,
-                          int16_t* __restrict__ colz) {
+                          int16_t* __restrict__ colz, int* __restrict__ no_partner) {
   const int64_t r = gtid();
   if (r >= n) return;
   int64_t base;
   int w;
   sell_row(sptr, r, base, w);
   const int64_t fbase = ((r >> 5) * 32) * zw + (r & 31);
-  for (int k = 0; k < w; k++) colz[fbase + 32 * (int64_t)k] = col[base + 32 * (int64_t)k];
+  const int dpart = (r & 1) ? -1 : 1;
+  bool found = false;
+  for (int k = 0; k < w; k++) {
+    const int16_t d = col[base + 32 * (int64_t)k];
+    colz[fbase + 32 * (int64_t)k] = d;
+    found |= d == dpart;
+  }
+  if (!found || (r ^ 1) >= n) atomicExch(no_partner, 1);
 }
 
 // u = y; rows tagged 1 get their prescribed value exactly (or 0)
@@ -390,9 +422,9 @@ static int zcg_build_pool(Solver& S) {
   return ADFEM_OK;
 }
 
-template <int MAXW>
+template <int MAXW, bool B2>
 static int zcg_configure(Solver& S, int sms) {
-  auto kern = k_zcg_iter<MAXW, kZBT, kZU1>;
+  auto kern = k_zcg_iter<MAXW, kZBT, kZU1, B2>;
   // The shared-memory limit is raised once per process to the most any plan uses:
   // changing a kernel's attributes while another thread captures a graph with that
   // kernel invalidates the capture.
@@ -446,8 +478,11 @@ int zcg_plan(Solver& S, int sms) {
   S.zH = H;
   S.zW = S.zS + 2 * H;
   S.zsmem = pool_bytes + sizeof(float) * (size_t)S.zW;
-  if (A.maxw <= 8) ADFEM_TRY(zcg_configure<8>(S, sms));
-  else ADFEM_TRY(zcg_configure<16>(S, sms));
+  // (the block form is decided after the layout pass below; both 16-wide variants have
+  // the same resources, so the plan is made with the plain one)
+  if (A.maxw <= 8) ADFEM_TRY((zcg_configure<8, false>(S, sms)));
+  else ADFEM_TRY((zcg_configure<16, false>(S, sms)));
+  if (A.maxw > 8) ADFEM_TRY((zcg_configure<16, true>(S, sms)));
   const size_t n4 = sizeof(float) * (size_t)S.n;
   ADFEM_TRY(S.z1.alloc(n4));
   ADFEM_TRY(S.zq1.alloc(n4));
@@ -461,12 +496,18 @@ int zcg_plan(Solver& S, int sms) {
   ADFEM_CUDA(cudaMemset(S.valz64.p, 0, sizeof(double) * ne));
   ADFEM_CUDA(cudaMemset(S.valz32.p, 0, sizeof(float) * nf));
   ADFEM_CUDA(cudaMemset(S.colz16.p, 0, sizeof(int16_t) * nf));
+  DevBuf flag;
+  ADFEM_TRY(flag.alloc(sizeof(int)));
+  ADFEM_CUDA(cudaMemset(flag.p, 0, sizeof(int)));
   k_zlayout<<<(unsigned)((S.n + kT - 1) / kT), kT>>>(S.n, A.sptr.as<int32_t>(), A.col.as<int16_t>(), S.zw,
-                                                     S.colz16.as<int16_t>());
+                                                     S.colz16.as<int16_t>(), flag.as<int>());
   ADFEM_CUDA(cudaGetLastError());
   // legacy-stream sync, not a device-wide one: other threads may be capturing graphs on
   // their (non-blocking) solver streams
   ADFEM_CUDA(cudaStreamSynchronize(0));
+  int no_partner = 0;
+  ADFEM_CUDA(cudaMemcpy(&no_partner, flag.p, sizeof(int), cudaMemcpyDeviceToHost));
+  S.zblock2 = A.pat_period == 2 && !no_partner && A.maxw > 8;
   S.zcg = true;
   return ADFEM_OK;
 }
@@ -474,8 +515,9 @@ int zcg_plan(Solver& S, int sms) {
 int zcg_prepare(Solver& S, const int32_t* diagpos_dev, int* bad_dev, cudaStream_t st) {
   const Sell& A = *S.A;
   const unsigned nb = (unsigned)((S.n + kT - 1) / kT);
-  k_zprep<<<nb, kT, 0, st>>>(S.n, A.sptr.as<int32_t>(), A.val64.as<double>(), diagpos_dev, S.zw,
-                             S.valz64.as<double>(), S.valz32.as<float>(), S.dz32.as<float>(), bad_dev);
+  k_zprep<<<nb, kT, 0, st>>>(S.n, A.sptr.as<int32_t>(), A.col.as<int16_t>(), A.val64.as<double>(), diagpos_dev,
+                             S.zw, S.zblock2 ? 1 : 0, S.valz64.as<double>(), S.valz32.as<float>(),
+                             S.dz32.as<float>(), bad_dev);
   ADFEM_CUDA(cudaGetLastError());
   return ADFEM_OK;
 }
@@ -510,8 +552,9 @@ static ZcgArgs zcg_args(Solver& S) {
 
 void zcg_enqueue_iter(Solver& S, cudaStream_t st) {
   const ZcgArgs z = zcg_args(S);
-  if (S.A->maxw <= 8) k_zcg_iter<8, kZBT, kZU1><<<S.zgrid, kZBT, S.zsmem, st>>>(z);
-  else k_zcg_iter<16, kZBT, kZU1><<<S.zgrid, kZBT, S.zsmem, st>>>(z);
+  if (S.A->maxw <= 8) k_zcg_iter<8, kZBT, kZU1, false><<<S.zgrid, kZBT, S.zsmem, st>>>(z);
+  else if (S.zblock2) k_zcg_iter<16, kZBT, kZU1, true><<<S.zgrid, kZBT, S.zsmem, st>>>(z);
+  else k_zcg_iter<16, kZBT, kZU1, false><<<S.zgrid, kZBT, S.zsmem, st>>>(z);
 }
 
 void zcg_enqueue_init(Solver& S, cudaStream_t st, const double* rhs, const uint8_t* zero_rows, const double* u0,
@@ -523,7 +566,7 @@ void zcg_enqueue_init(Solver& S, cudaStream_t st, const double* rhs, const uint8
 void zcg_enqueue_residual(Solver& S, cudaStream_t st, int mode, int force) {
   const Sell& A = *S.A;
   k_zres64<<<S.grid, kT, 0, st>>>(S.n, A.sptr.as<int32_t>(), A.col.as<int16_t>(), S.valz64.as<double>(),
-                                  S.dz32.as<float>(), S.b.as<double>(), S.y64.as<double>(), S.r32.as<float>(),
+                                  S.zblock2 ? 1 : 0, S.dz32.as<float>(), S.b.as<double>(), S.y64.as<double>(), S.r32.as<float>(),
                                   S.z1.as<float>(), S.pa32.as<float>(), S.pb32.as<float>(), S.state.as<CgState>(),
                                   S.partials.as<double>(), mode, force);
 }
