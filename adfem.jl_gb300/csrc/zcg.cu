@@ -64,6 +64,32 @@ struct ZcgArgs {
   double* partials;
 };
 
+// L2 policies.  The matrix is read once per iteration: it is streamed with evict-first,
+// so that the vectors the next iteration reads again (Z, P, q^, Y, D, about as large as
+// L2) stay cached, and those vectors are stored with evict-last (ADFEM_ZCG_KEEP_STORES=0
+// at build time turns that off).
+#ifndef ADFEM_ZCG_KEEP_STORES
+#define ADFEM_ZCG_KEEP_STORES 1
+#endif
+__device__ __forceinline__ uint64_t l2_evict_first_policy() {
+  uint64_t p;
+  asm volatile("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(p));
+  return p;
+}
+__device__ __forceinline__ uint64_t l2_evict_last_policy() {
+  uint64_t p;
+  asm volatile("createpolicy.fractional.L2::evict_last.b64 %0, 1.0;" : "=l"(p));
+  return p;
+}
+__device__ __forceinline__ void st_keep(float* a, float v, uint64_t pol) {
+  asm volatile("st.global.L2::cache_hint.f32 [%0], %1, %2;" ::"l"(a), "f"(v), "l"(pol) : "memory");
+}
+__device__ __forceinline__ float ld_stream(const float* a, uint64_t pol) {
+  float v;
+  asm volatile("ld.global.nc.L1::no_allocate.L2::cache_hint.f32 %0, [%1], %2;" : "=f"(v) : "l"(a), "l"(pol));
+  return v;
+}
+
 // Positions and row indices are 32-bit (the plan requires n and the fixed-width layout
 // to stay below 2^31).  A warp's 32 rows are one slice (block ranges and super-tiles are
 // multiples of 32 rows), so the pattern/no-pattern branch is warp-uniform.
@@ -92,6 +118,8 @@ __global__ void __launch_bounds__(BT, 2) k_zcg_iter(ZcgArgs A) {
   float* __restrict__ yl = A.yl;
   const float a = (float)st->alpha, ar = (float)st->ar, ap = (float)st->ap;
   const bool full_zq = ar != 1.0f;  // uniform
+  const uint64_t pol = l2_evict_first_policy();
+  const uint64_t keep = ADFEM_ZCG_KEEP_STORES ? l2_evict_last_policy() : 0;
   const int tid = threadIdx.x;
   const int zw = A.zw;
   const int n = (int)A.n;
@@ -124,11 +152,18 @@ __global__ void __launch_bounds__(BT, 2) k_zcg_iter(ZcgArgs A) {
       const float pk = fmaf(ap, x.pp, __fmul_rn(ar, zk));
       sP[pos - wlo] = pk;
       if (x.own) {
-        znew[pos] = zk;
-        pnew[pos] = pk;
         df_axpy(x.h, x.l, a, x.pp);
-        yh[pos] = x.h;
-        yl[pos] = x.l;
+        if constexpr (ADFEM_ZCG_KEEP_STORES) {
+          st_keep(znew + pos, zk, keep);
+          st_keep(pnew + pos, pk, keep);
+          st_keep(yh + pos, x.h, keep);
+          st_keep(yl + pos, x.l, keep);
+        } else {
+          znew[pos] = zk;
+          pnew[pos] = pk;
+          yh[pos] = x.h;
+          yl[pos] = x.l;
+        }
         rr = fmaf(__fmul_rn(x.d, zk), zk, rr);
       }
     };
@@ -179,7 +214,8 @@ __global__ void __launch_bounds__(BT, 2) k_zcg_iter(ZcgArgs A) {
         s = fmaf(v[k], tv, s);
       }
       const float qh = __fdiv_rn(s, d);
-      qnew[i] = qh;
+      if constexpr (ADFEM_ZCG_KEEP_STORES) st_keep(qnew + i, qh, keep);
+      else qnew[i] = qh;
       pq = fmaf(Pi, s, pq);
       qq = fmaf(s, qh, qq);
       if (full_zq) pkq = fmaf(__ldg(pprev + i), s, pkq);
@@ -189,7 +225,7 @@ __global__ void __launch_bounds__(BT, 2) k_zcg_iter(ZcgArgs A) {
     auto fetch = [&](int i, float (&v)[MAXW], float& d, int& pid) {
       const int base = (i >> 5) * (32 * zw) + (i & 31);
 #pragma unroll
-      for (int k = 0; k < MAXW; k++) v[k] = k < zw ? __ldg(A.val + base + 32 * k) : 0.f;
+      for (int k = 0; k < MAXW; k++) v[k] = k < zw ? ld_stream(A.val + base + 32 * k, pol) : 0.f;
       d = __ldg(A.dz + i);
       pid = __ldg(A.zpid + (i >> 5));
     };
@@ -508,6 +544,7 @@ int zcg_plan(Solver& S, int sms) {
   int no_partner = 0;
   ADFEM_CUDA(cudaMemcpy(&no_partner, flag.p, sizeof(int), cudaMemcpyDeviceToHost));
   S.zblock2 = A.pat_period == 2 && !no_partner && A.maxw > 8;
+
   S.zcg = true;
   return ADFEM_OK;
 }
