@@ -107,6 +107,9 @@ __device__ __forceinline__ void df_axpy(float& h, float& l, float a, float p) {
 __device__ __forceinline__ void replacement_step(CgState* st, double rr, double rn, double rp, int mode) {
   st->rr64 = rr;
   if (mode == 2) return;
+  // the solution correction has just been folded: no update term is pending any more
+  st->alpha = 0.0;
+  st->alpha_prev = 0.0;
   if (!isfinite(rr)) {
     st->done = 2;
     return;
@@ -141,7 +144,6 @@ __device__ __forceinline__ void replacement_step(CgState* st, double rr, double 
     st->ar = 1.0 - beta * c;
     st->ap = beta;
   }
-  st->alpha = 0.0;
   st->updates += 1;
   st->rho = rn;
   st->ru2 = st->delta2 * rn;

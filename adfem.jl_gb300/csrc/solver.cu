@@ -747,10 +747,7 @@ enum class Path { FP64, MIXED, BANDED };
 static void enqueue_zreliable_update(Solver& S, cudaStream_t st, int force, Timer* tm = nullptr) {
   Timer none;
   if (!tm) tm = &none;
-  tm->run(2, st, [&] {
-    k_fold<<<S.grid, kT, 0, st>>>(S.n, S.y64.as<double>(), S.yh32.as<float>(), S.yl32.as<float>(),
-                                  S.state.as<CgState>(), force);
-  });
+  tm->run(2, st, [&] { zcg_enqueue_fold(S, st, force); });
   tm->run(3, st, [&] { zcg_enqueue_residual(S, st, 1, force); });
 }
 
@@ -898,7 +895,10 @@ int solver_solve(Solver& S, const double* rhs, double* u, const uint8_t* zero_ro
   }
   // final fold (mixed), FP64 residual (difference form) for the report, then u = S y
   // with the Dirichlet rows set exactly
-  if (mixed) {
+  if (path == Path::BANDED) {
+    zcg_enqueue_fold(S, st, 1);
+    launches += 1;
+  } else if (mixed) {
     k_fold<<<S.grid, kT, 0, st>>>(S.n, S.y64.as<double>(), S.yh32.as<float>(), S.yl32.as<float>(),
                                   S.state.as<CgState>(), 1);
     launches += 1;

@@ -10,6 +10,7 @@ struct CgState {
   double rho;          // current (recursive) r.r
   double rho_new;      // r.r computed by the last update step
   double alpha, beta;  // CG coefficients
+  double alpha_prev;   // banded mixed path: alpha of the iteration before (two-step solution update)
   double ar, ap;       // mixed: p_new = ar*r + ap*p_old
   double bnorm2;       // ||b~||^2
   double stop2;        // stop when ||r||^2 <= stop2 (= rtol^2 ||b~||^2)
@@ -98,6 +99,7 @@ void zcg_enqueue_init(Solver& S, cudaStream_t st, const double* rhs, const uint8
                       double rtol2);
 void zcg_enqueue_iter(Solver& S, cudaStream_t st);
 void zcg_enqueue_residual(Solver& S, cudaStream_t st, int mode, int force);
+void zcg_enqueue_fold(Solver& S, cudaStream_t st, int force);
 void zcg_enqueue_unscale(Solver& S, cudaStream_t st, const uint8_t* fix, const double* fixval, double* u);
 
 // Fill sliced-ELL values from CSR values (same pattern).

@@ -11,7 +11,9 @@
 // from an FP32 copy whose diagonal slot holds the FP64 row sum rounded once.
 //
 // Launch k of the iteration, for the rows of each block's contiguous range:
-//   Z_k = Z_{k-1} - a_{k-1} q^_{k-1}   and   Y += a_{k-1} P_{k-1}   (lagged updates),
+//   Z_k = Z_{k-1} - a_{k-1} q^_{k-1}   (lagged update),
+//   Y += a_{k-2} P_{k-2} + a_{k-1} P_{k-1}   on even k only (P_{k-2} is still in the buffer
+//        launch k overwrites; a fold after an odd k adds the pending a_{k-1} P_{k-1}),
 //   P_k = ar Z_k + ap P_{k-1}          (ar = 1, ap = beta_{k-1}; other values after a
 //                                       residual replacement re-orthogonalise P),
 //   q_k = K P_k,  q^_k = q_k / D,
@@ -97,7 +99,7 @@ __device__ __forceinline__ float ld_stream(const float* a, uint64_t pol) {
 // DOFs of node a): each neighbour is differenced against the value of the same component
 // at row i's node, the same-component row sum sits in the diagonal slot and the
 // other-component row sum in the slot of the partner DOF i^1 (see k_zprep).
-template <int MAXW, int BT, int U1, bool B2>
+template <int MAXW, int BT, int U1, int U2, bool B2>
 __global__ void __launch_bounds__(BT, 2) k_zcg_iter(ZcgArgs A) {
   static_assert(MAXW % 4 == 0, "pattern rows are loaded as int4");
   CgState* st = A.st;
@@ -117,6 +119,8 @@ __global__ void __launch_bounds__(BT, 2) k_zcg_iter(ZcgArgs A) {
   float* __restrict__ yh = A.yh;
   float* __restrict__ yl = A.yl;
   const float a = (float)st->alpha, ar = (float)st->ar, ap = (float)st->ap;
+  const float a2 = (float)st->alpha_prev;
+  const bool ydo = (it & 1) == 0;   // the two-step solution update runs on even iterations
   const bool full_zq = ar != 1.0f;  // uniform
   const uint64_t pol = l2_evict_first_policy();
   const uint64_t keep = ADFEM_ZCG_KEEP_STORES ? l2_evict_last_policy() : 0;
@@ -135,7 +139,7 @@ __global__ void __launch_bounds__(BT, 2) k_zcg_iter(ZcgArgs A) {
     // ---- phase 1: P_k for [wlo, whi) into shared memory; Z, P, Y of own rows.  All loads
     // of a trip (U1 positions per thread) are issued before any store.
     struct In {
-      float zp, qp, pp, h, l, d;
+      float zp, qp, pp, p2, h, l, d;
       bool own;
     };
     auto fetch1 = [&](int pos, In& x) {
@@ -143,8 +147,10 @@ __global__ void __launch_bounds__(BT, 2) k_zcg_iter(ZcgArgs A) {
       x.zp = __ldg(zprev + pos);
       x.qp = __ldg(qprev + pos);
       x.pp = __ldg(pprev + pos);
-      x.h = x.own ? yh[pos] : 0.f;
-      x.l = x.own ? yl[pos] : 0.f;
+      const bool yupd = x.own && ydo;
+      x.p2 = yupd ? pnew[pos] : 0.f;  // P_{k-2}, read before this thread overwrites it with P_k
+      x.h = yupd ? yh[pos] : 0.f;
+      x.l = yupd ? yl[pos] : 0.f;
       x.d = x.own ? __ldg(A.dz + pos) : 0.f;
     };
     auto commit = [&](int pos, In& x) {
@@ -152,17 +158,23 @@ __global__ void __launch_bounds__(BT, 2) k_zcg_iter(ZcgArgs A) {
       const float pk = fmaf(ap, x.pp, __fmul_rn(ar, zk));
       sP[pos - wlo] = pk;
       if (x.own) {
-        df_axpy(x.h, x.l, a, x.pp);
         if constexpr (ADFEM_ZCG_KEEP_STORES) {
           st_keep(znew + pos, zk, keep);
           st_keep(pnew + pos, pk, keep);
-          st_keep(yh + pos, x.h, keep);
-          st_keep(yl + pos, x.l, keep);
         } else {
           znew[pos] = zk;
           pnew[pos] = pk;
-          yh[pos] = x.h;
-          yl[pos] = x.l;
+        }
+        if (ydo) {
+          df_axpy(x.h, x.l, a2, x.p2);
+          df_axpy(x.h, x.l, a, x.pp);
+          if constexpr (ADFEM_ZCG_KEEP_STORES) {
+            st_keep(yh + pos, x.h, keep);
+            st_keep(yl + pos, x.l, keep);
+          } else {
+            yh[pos] = x.h;
+            yl[pos] = x.l;
+          }
         }
         rr = fmaf(__fmul_rn(x.d, zk), zk, rr);
       }
@@ -230,15 +242,15 @@ __global__ void __launch_bounds__(BT, 2) k_zcg_iter(ZcgArgs A) {
       pid = __ldg(A.zpid + (i >> 5));
     };
     int i = lo + tid;
-    for (; i + BT < hi; i += 2 * BT) {  // two rows per thread and trip
-      float v0[MAXW], v1[MAXW], d0, d1;
-      int g0, g1;
-      fetch(i, v0, d0, g0);
-      fetch(i + BT, v1, d1, g1);
-      row(i, v0, d0, g0);
-      row(i + BT, v1, d1, g1);
+    for (; i + (U2 - 1) * BT < hi; i += U2 * BT) {  // U2 rows per thread and trip, loads first
+      float v[U2][MAXW], d[U2];
+      int pid[U2];
+#pragma unroll
+      for (int u = 0; u < U2; u++) fetch(i + u * BT, v[u], d[u], pid[u]);
+#pragma unroll
+      for (int u = 0; u < U2; u++) row(i + u * BT, v[u], d[u], pid[u]);
     }
-    if (i < hi) {
+    for (; i < hi; i += BT) {
       float v0[MAXW], d0;
       int g0;
       fetch(i, v0, d0, g0);
@@ -262,6 +274,7 @@ __global__ void __launch_bounds__(BT, 2) k_zcg_iter(ZcgArgs A) {
     } else {
       const double al = rho / pqd;
       const double est = rho - 2.0 * al * zqd + al * al * qqd;
+      st->alpha_prev = st->alpha;
       st->alpha = al;
       st->ar = 1.0;
       st->ap = fmax(est, 0.0) / rho;
@@ -399,6 +412,24 @@ __global__ void k_zlayout(int64_t n, const int32_t* __restrict__ sptr, const int
   if (!found || (r ^ 1) >= n) atomicExch(no_partner, 1);
 }
 
+// Fold the FP32 hi+lo correction into the FP64 solution: y += Yh + Yl, plus the update
+// term a_{k-1} P_{k-1} that is still pending when the last launch had an odd iteration
+// counter (the two-step update of Y runs on even ones); Yh = Yl = 0.  Runs when a
+// residual replacement is due (done == 3) or when forced.
+__global__ void __launch_bounds__(kT) k_zfold(int64_t n, double* __restrict__ y64, float* __restrict__ yh,
+                                              float* __restrict__ yl, const float* __restrict__ p0,
+                                              const float* __restrict__ p1, const CgState* st, int force) {
+  if (!force && st->done != 3) return;
+  const int it = st->iters;
+  const double a = (it & 1) ? (double)(float)st->alpha : 0.0;  // the FP32 alpha the iteration used
+  const float* __restrict__ pp = (it & 1) ? p1 : p0;
+  for (int64_t i = gtid(); i < n; i += gstride()) {
+    y64[i] += (double)yh[i] + (double)yl[i] + a * (double)pp[i];
+    yh[i] = 0.0f;
+    yl[i] = 0.0f;
+  }
+}
+
 // u = y; rows tagged 1 get their prescribed value exactly (or 0)
 __global__ void k_zunscale(int64_t n, const double* __restrict__ y, const uint8_t* __restrict__ fix,
                            const double* __restrict__ fixval, double* __restrict__ u) {
@@ -409,7 +440,14 @@ __global__ void k_zunscale(int64_t n, const double* __restrict__ y, const uint8_
 
 // ---------------------------------------------------------------------------
 static constexpr int kZBT = 512;                     // threads per block
-static constexpr int kZU1 = 4;                       // phase-1 positions per thread and trip
+#ifndef ADFEM_ZCG_U1
+#define ADFEM_ZCG_U1 4
+#endif
+#ifndef ADFEM_ZCG_U2
+#define ADFEM_ZCG_U2 2
+#endif
+static constexpr int kZU1 = ADFEM_ZCG_U1;            // phase-1 positions per thread and trip
+static constexpr int kZU2 = ADFEM_ZCG_U2;            // phase-2 matrix rows per thread and trip
 static constexpr size_t kZSmemBlock = 100 * 1024;    // shared memory per block (two blocks per SM)
 
 // Distinct slice column patterns (at most kZMaxPatterns; further slices use their
@@ -460,7 +498,7 @@ static int zcg_build_pool(Solver& S) {
 
 template <int MAXW, bool B2>
 static int zcg_configure(Solver& S, int sms) {
-  auto kern = k_zcg_iter<MAXW, kZBT, kZU1, B2>;
+  auto kern = k_zcg_iter<MAXW, kZBT, kZU1, kZU2, B2>;
   // The shared-memory limit is raised once per process to the most any plan uses:
   // changing a kernel's attributes while another thread captures a graph with that
   // kernel invalidates the capture.
@@ -589,9 +627,9 @@ static ZcgArgs zcg_args(Solver& S) {
 
 void zcg_enqueue_iter(Solver& S, cudaStream_t st) {
   const ZcgArgs z = zcg_args(S);
-  if (S.A->maxw <= 8) k_zcg_iter<8, kZBT, kZU1, false><<<S.zgrid, kZBT, S.zsmem, st>>>(z);
-  else if (S.zblock2) k_zcg_iter<16, kZBT, kZU1, true><<<S.zgrid, kZBT, S.zsmem, st>>>(z);
-  else k_zcg_iter<16, kZBT, kZU1, false><<<S.zgrid, kZBT, S.zsmem, st>>>(z);
+  if (S.A->maxw <= 8) k_zcg_iter<8, kZBT, kZU1, kZU2, false><<<S.zgrid, kZBT, S.zsmem, st>>>(z);
+  else if (S.zblock2) k_zcg_iter<16, kZBT, kZU1, kZU2, true><<<S.zgrid, kZBT, S.zsmem, st>>>(z);
+  else k_zcg_iter<16, kZBT, kZU1, kZU2, false><<<S.zgrid, kZBT, S.zsmem, st>>>(z);
 }
 
 void zcg_enqueue_init(Solver& S, cudaStream_t st, const double* rhs, const uint8_t* zero_rows, const double* u0,
@@ -606,6 +644,11 @@ void zcg_enqueue_residual(Solver& S, cudaStream_t st, int mode, int force) {
                                   S.zblock2 ? 1 : 0, S.dz32.as<float>(), S.b.as<double>(), S.y64.as<double>(), S.r32.as<float>(),
                                   S.z1.as<float>(), S.pa32.as<float>(), S.pb32.as<float>(), S.state.as<CgState>(),
                                   S.partials.as<double>(), mode, force);
+}
+
+void zcg_enqueue_fold(Solver& S, cudaStream_t st, int force) {
+  k_zfold<<<S.grid, kT, 0, st>>>(S.n, S.y64.as<double>(), S.yh32.as<float>(), S.yl32.as<float>(),
+                                 S.pa32.as<float>(), S.pb32.as<float>(), S.state.as<CgState>(), force);
 }
 
 void zcg_enqueue_unscale(Solver& S, cudaStream_t st, const uint8_t* fix, const double* fixval, double* u) {

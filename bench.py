@@ -134,12 +134,13 @@ def spmv32_bytes(mesh_nent, n, nslices):
 
 
 def zcg_bytes(info):
-    """Algorithmic bytes of one banded mixed iteration (k_zcg_iter): per row Z, q^, P of
-    the previous iteration read (12 B), Z, P, q^ written (12 B), the Y hi+lo pair read and
-    written (16 B) and the diagonal (4 B); per stored entry its FP32 value (4 B) plus the
-    int16 column delta outside slices with a stored pattern (2 B); slice pointer and
-    pattern index per slice (8 B).  Halo re-reads are not counted."""
-    return (44 * info["rows"] + 4 * info["stored"] + 2 * (info["stored"] - info["uniform_entries"])
+    """Algorithmic bytes of one banded mixed iteration (k_zcg_iter), averaged over an even
+    and an odd launch: per row Z, q^, P of the previous iteration read (12 B), Z, P, q^
+    written (12 B), the diagonal (4 B), and the Y hi+lo pair read and written with
+    P_{k-2} read on even launches only (20 B every other launch: 10 B); per stored entry
+    its FP32 value (4 B) plus the int16 column delta outside slices with a stored pattern
+    (2 B); slice pointer and pattern index per slice (8 B).  Halo re-reads are not counted."""
+    return (38 * info["rows"] + 4 * info["stored"] + 2 * (info["stored"] - info["uniform_entries"])
             + 8 * info["slices"])
 
 
