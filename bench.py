@@ -262,6 +262,30 @@ def run_reference(args, rank, world):
     return 0
 
 
+# ----------------------------------------------------------------------------- replicas
+def max_over_ranks(dist, x):
+    """Largest value of x over all ranks (the slowest replica sets the job's time); the
+    tensor lives on the GPU for NCCL and on the CPU for gloo."""
+    if dist is None:
+        return float(x)
+    import torch
+
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([float(x)], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def shard(items, rank, world):
+    """Request-level dispatch to replicas: rank r takes items r, r + world, ..."""
+    return items[rank::world]
+
+
+def replica_rate(world, units_per_rank, seconds):
+    """Whole-job rate: all ranks' units over the slowest rank's time."""
+    return world * units_per_rank / seconds
+
+
 # ----------------------------------------------------------------------------- serving (C5)
 SERVE_SIZES = sorted({int(round(16 * 2 ** (k / 4))) for k in range(25)})  # 16 .. 1024, ratio 2^(1/4)
 
@@ -324,10 +348,13 @@ class ServeCatalog:
         return self.items[req[0]]["ndof"][req[1]]
 
 
-def run_serve(A, args):
+def run_serve(A, args, rank=0, world=1, dist=None):
     """C5 serving workload through adfem_gpu.Server: a warm-up pass over every (size,
     kind), a saturation run (all requests queued at once) and an open-loop sweep with
-    Poisson arrivals at fractions of the saturation throughput."""
+    Poisson arrivals at fractions of the saturation throughput.  With several ranks each
+    runs a server replica on its GPU and takes its share of every request stream
+    (`shard`); throughput is all requests over the slowest replica's time, latency
+    percentiles are rank 0's."""
     t0 = time.perf_counter()
     cat = ServeCatalog(A, SERVE_SIZES)
     setup_s = time.perf_counter() - t0
@@ -336,23 +363,24 @@ def run_serve(A, args):
         for t in [cat.submit(srv, r) for r in warm]:
             srv.wait(t)
         # saturation: every request queued at t = 0
-        reqs = cat.requests(args.serve_requests, seed=11)
+        reqs = shard(cat.requests(args.serve_requests, seed=11), rank, world)
         srv.reset_stats()
         ts = time.perf_counter()
         tickets = [cat.submit(srv, r) for r in reqs]
         resps = [srv.wait(t)[0] for t in tickets]
-        wall = time.perf_counter() - ts
+        wall = max_over_ranks(dist, time.perf_counter() - ts)
         st = srv.stats()
         bad = sum(1 for r in resps if r["status"] != 0)
-        sat = {"requests": len(reqs), "wall_s": wall, "throughput_req_s": len(reqs) / wall,
-               "dof_per_s": sum(cat.dof(r) for r in reqs) / wall, "p50_ms": st["p50_ms"], "p99_ms": st["p99_ms"],
+        sat = {"requests": args.serve_requests, "wall_s": wall,
+               "throughput_req_s": replica_rate(world, len(reqs), wall),
+               "dof_per_s": replica_rate(world, sum(cat.dof(r) for r in reqs), wall), "p50_ms": st["p50_ms"], "p99_ms": st["p99_ms"],
                "failed": bad, "gradients": sum(1 for r in reqs if r[3])}
         # open loop: exponential inter-arrival gaps at a fraction of the saturation rate
         sweep = []
         for frac in args.serve_loads:
             rate = frac * sat["throughput_req_s"]
-            sub = cat.requests(args.serve_sweep_requests, seed=int(100 * frac))
-            gaps = np.random.default_rng(int(1000 * frac)).exponential(1.0 / rate, len(sub))
+            sub = shard(cat.requests(args.serve_sweep_requests, seed=int(100 * frac)), rank, world)
+            gaps = np.random.default_rng(int(1000 * frac) + rank).exponential(world / rate, len(sub))
             srv.reset_stats()
             ts = time.perf_counter()
             nxt = ts
@@ -364,9 +392,9 @@ def run_serve(A, args):
                     time.sleep(dt)
                 tickets.append(cat.submit(srv, r))
             rs = [srv.wait(t)[0] for t in tickets]
-            wall = time.perf_counter() - ts
+            wall = max_over_ranks(dist, time.perf_counter() - ts)
             s = srv.stats()
-            sweep.append({"offered_req_s": rate, "load": frac, "achieved_req_s": len(sub) / wall,
+            sweep.append({"offered_req_s": rate, "load": frac, "achieved_req_s": replica_rate(world, len(sub), wall),
                           "p50_ms": s["p50_ms"], "p99_ms": s["p99_ms"], "p50_queue_ms": s["p50_queue_ms"],
                           "failed": sum(1 for r in rs if r["status"] != 0)})
         cache = srv.stats()
@@ -567,13 +595,9 @@ def run_ours(args, rank, world, dist):
     e1.record()
     barrier()
     clocks = clk.stop()
-    ms = e0.elapsed_time(e1)
-    if dist is not None:
-        t = torch.tensor([ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
+    ms = max_over_ranks(dist, e0.elapsed_time(e1))
     err_mixed = float((u - u_ref).abs().max() / u_ref.abs().max())
-    value = world * args.steps / (ms / 1000.0)
+    value = replica_rate(world, args.steps, ms / 1000.0)
 
     # ------------------------------------------------------------------ FP64 CG comparison
     u64 = torch.zeros_like(u)
@@ -590,7 +614,8 @@ def run_ours(args, rank, world, dist):
     barrier()
     ms64 = f0.elapsed_time(f1)
     err_fp64 = float((u64 - u_ref).abs().max() / u_ref.abs().max())
-    fp64_value = world * args.fp64_steps / (ms64 / 1000.0)
+    ms64 = max_over_ranks(dist, ms64)
+    fp64_value = replica_rate(world, args.fp64_steps, ms64 / 1000.0)
 
     # ------------------------------------------------------------------ grads/s (mixed)
     from adfem_gpu import synth
@@ -610,7 +635,7 @@ def run_ours(args, rank, world, dist):
         gk = S.grad_kappa(u, lam)
     g1.record()
     barrier()
-    grads_value = world * args.grad_steps / (g0.elapsed_time(g1) / 1000.0)
+    grads_value = replica_rate(world, args.grad_steps, max_over_ranks(dist, g0.elapsed_time(g1)) / 1000.0)
 
     # ------------------------------------------------------------------ roofline (profiled solve)
     import ctypes
@@ -665,16 +690,12 @@ def run_ours(args, rank, world, dist):
         _lib.check(_lib.load().adfem_poisson_solve(S.handle, _lib.ptr(kh), _lib.ptr(fh), _lib.ptr(uh),
                                                    ctypes.byref(o), ctypes.byref(est)))
     barrier()
-    e2e_s = time.perf_counter() - t0
-    if dist is not None:
-        t = torch.tensor([e2e_s], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_s = float(t.item())
-    e2e_value = world * args.steps / e2e_s
+    e2e_s = max_over_ranks(dist, time.perf_counter() - t0)
+    e2e_value = replica_rate(world, args.steps, e2e_s)
     err_e2e = float(_np.max(_np.abs(uh.numpy() - u_ref.cpu().numpy())) / float(u_ref.abs().max()))
 
     # ------------------------------------------------------------------ serving (C5)
-    serve = run_serve(A, args) if args.serve_requests > 0 else None
+    serve = run_serve(A, args, rank, world, dist) if args.serve_requests > 0 else None
     c2 = run_c2(A, args) if args.c2_m > 0 else None
     c4 = run_c4(A, args) if args.c4_m > 0 else None
 
