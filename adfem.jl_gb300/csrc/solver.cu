@@ -29,6 +29,8 @@
 namespace adfem {
 
 static constexpr int kMaxBlocksPerSM = 8;
+// systems up to this many rows run their solver stream at the highest priority
+static constexpr int64_t kSmallSystemRows = 1 << 17;
 
 // ---------------------------------------------------------------------------
 // setup kernels
@@ -598,7 +600,16 @@ int Solver::init(const Sell* A_, int64_t n_) {
     std::lock_guard<std::mutex> lk(device_alloc_mutex());
     ADFEM_CUDA(cudaMallocHost(&h_state, 2 * sizeof(CgState)));
   }
-  if (!stream) ADFEM_CUDA(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
+  if (!stream) {
+    // Small systems get the highest stream priority: when solves of different sizes run
+    // concurrently (the request server), the block scheduler then starts a small solve's
+    // short kernels as soon as SMs free up instead of queueing them behind the whole-GPU
+    // kernels of large solves.  Priorities change scheduling only, never results.
+    int least = 0, greatest = 0;
+    ADFEM_CUDA(cudaDeviceGetStreamPriorityRange(&least, &greatest));
+    const int prio = n <= kSmallSystemRows ? greatest : least;
+    ADFEM_CUDA(cudaStreamCreateWithPriority(&stream, cudaStreamNonBlocking, prio));
+  }
   for (auto& e : ev)
     if (!e) ADFEM_CUDA(cudaEventCreate(&e));
   return ADFEM_OK;
