@@ -126,7 +126,7 @@ size_t system_device_bytes(const adfem_system* s) {
   const Solver& v = s->solver;
   for (const DevBuf* d : {&v.s32, &v.state, &v.partials, &v.b, &v.y64, &v.r64, &v.p64, &v.q64, &v.r32, &v.pa32,
                           &v.pb32, &v.q32, &v.yh32, &v.yl32, &v.z1, &v.zq1, &v.dz32, &v.valz64, &v.valz32,
-                          &v.colz16, &v.zpid32, &v.zpool32})
+                          &v.colz16, &v.zpid32, &v.zpool32, &v.bz32})
     b += d->bytes;
   return b;
 }

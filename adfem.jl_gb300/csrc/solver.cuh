@@ -63,7 +63,8 @@ struct Solver {
   int znpool = 0;          // ints in zpool32
   int zw = 0;              // fixed slice width (widest slice)
   int zps = 0;             // pattern row stride (8 or 16, the kernel's unrolled width)
-  bool zblock2 = false;    // interleaved 2-DOF operator in block difference form
+  bool zblock2 = false;    // interleaved 2-DOF operator: block difference form, node-block Jacobi
+  DevBuf bz32;             // zblock2: per row {K_ii, K_(i,i^1)} (FP32)
   cudaGraphExec_t gz = nullptr;
   int gz_chunk = 0;
   ~Solver();

@@ -57,6 +57,7 @@ struct ZcgArgs {
   const int16_t* colz;  // fixed-width sliced-ELL column deltas
   const float* val;   // fixed-width sliced-ELL values, FP32 difference form, physical scale
   const float* dz;    // fp32(K_ii)
+  const float2* bz;   // B2: per row {K_ii, K_(i,i^1)} in FP32, the row of its node's 2x2 block
   float* z[2];
   float* p[2];
   float* q[2];
@@ -65,6 +66,10 @@ struct ZcgArgs {
   CgState* st;
   double* partials;
 };
+
+// Lanes of the current node pair (rows 2a, 2a+1 sit in lanes 2j, 2j+1 of a warp): the
+// block-Jacobi shuffles name exactly these two lanes, which always execute them together.
+__device__ __forceinline__ unsigned pair_mask() { return 3u << (threadIdx.x & 30); }
 
 // L2 policies.  The matrix is read once per iteration: it is streamed with evict-first,
 // so that the vectors the next iteration reads again (Z, P, q^, Y, D, about as large as
@@ -98,7 +103,10 @@ __device__ __forceinline__ float ld_stream(const float* a, uint64_t pol) {
 // B2: block difference form of an interleaved 2-DOF operator (rows 2a, 2a+1 are the x, y
 // DOFs of node a): each neighbour is differenced against the value of the same component
 // at row i's node, the same-component row sum sits in the diagonal slot and the
-// other-component row sum in the slot of the partner DOF i^1 (see k_zprep).
+// other-component row sum in the slot of the partner DOF i^1 (see k_zprep).  The
+// preconditioner is then the node-block Jacobi M = blockdiag(K_aa) (2x2 per node): a row
+// and its partner are neighbouring lanes of one warp (block ranges, windows and tiles
+// start at even rows), so M and M^-1 are applied with one lane shuffle.
 template <int MAXW, int BT, int U1, int U2, bool B2>
 __global__ void __launch_bounds__(BT, 2) k_zcg_iter(ZcgArgs A) {
   static_assert(MAXW % 4 == 0, "pattern rows are loaded as int4");
@@ -133,13 +141,14 @@ __global__ void __launch_bounds__(BT, 2) k_zcg_iter(ZcgArgs A) {
 
   for (int lo = blo; lo < bhi; lo += A.S) {
     const int hi = min(lo + A.S, bhi);
-    const int wlo = max(lo - A.H, 0);
-    const int whi = min(hi + A.H, n);
+    // (B2: the window starts and ends at even positions, so lane pairs hold node pairs)
+    const int wlo = B2 ? (max(lo - A.H, 0) & ~1) : max(lo - A.H, 0);
+    const int whi = B2 ? min((hi + A.H + 1) & ~1, n) : min(hi + A.H, n);
     if (lo != blo) __syncthreads();  // the previous super-tile's gathers are done
     // ---- phase 1: P_k for [wlo, whi) into shared memory; Z, P, Y of own rows.  All loads
     // of a trip (U1 positions per thread) are issued before any store.
     struct In {
-      float zp, qp, pp, p2, h, l, d;
+      float zp, qp, pp, p2, h, l, d, c;
       bool own;
     };
     auto fetch1 = [&](int pos, In& x) {
@@ -151,11 +160,20 @@ __global__ void __launch_bounds__(BT, 2) k_zcg_iter(ZcgArgs A) {
       x.p2 = yupd ? pnew[pos] : 0.f;  // P_{k-2}, read before this thread overwrites it with P_k
       x.h = yupd ? yh[pos] : 0.f;
       x.l = yupd ? yl[pos] : 0.f;
-      x.d = x.own ? __ldg(A.dz + pos) : 0.f;
+      if constexpr (B2) {
+        const float2 b = x.own ? __ldg(A.bz + pos) : make_float2(0.f, 0.f);
+        x.d = b.x;
+        x.c = b.y;
+      } else {
+        x.d = x.own ? __ldg(A.dz + pos) : 0.f;
+        x.c = 0.f;
+      }
     };
     auto commit = [&](int pos, In& x) {
       const float zk = fmaf(-a, x.qp, x.zp);
       const float pk = fmaf(ap, x.pp, __fmul_rn(ar, zk));
+      // B2: the partner DOF's Z_k (lane pairs move together through the window)
+      const float zpart = B2 ? __shfl_xor_sync(pair_mask(), zk, 1) : 0.f;
       sP[pos - wlo] = pk;
       if (x.own) {
         if constexpr (ADFEM_ZCG_KEEP_STORES) {
@@ -176,7 +194,8 @@ __global__ void __launch_bounds__(BT, 2) k_zcg_iter(ZcgArgs A) {
             yl[pos] = x.l;
           }
         }
-        rr = fmaf(__fmul_rn(x.d, zk), zk, rr);
+        // rho_k = Z_k . M Z_k
+        rr = B2 ? fmaf(fmaf(x.d, zk, __fmul_rn(x.c, zpart)), zk, rr) : fmaf(__fmul_rn(x.d, zk), zk, rr);
       }
     };
     int pos = wlo + tid;
@@ -194,7 +213,7 @@ __global__ void __launch_bounds__(BT, 2) k_zcg_iter(ZcgArgs A) {
     }
     __syncthreads();
     // ---- phase 2: q = K P_k for the rows [lo, hi)
-    auto row = [&](int i, const float (&v)[MAXW], float d, int pid) {
+    auto row = [&](int i, const float (&v)[MAXW], float d, float c, int pid) {
       const float Pi = sP[i - wlo];
       const float Pp = B2 ? sP[(i ^ 1) - wlo] : Pi;  // partner DOF (B2: rows come in even/odd pairs)
       const int dpart = (i & 1) ? -1 : 1;            // column delta of the partner DOF
@@ -225,7 +244,17 @@ __global__ void __launch_bounds__(BT, 2) k_zcg_iter(ZcgArgs A) {
         else tv = __fsub_rn(sP[i + dl[k] - wlo], (B2 && (dl[k] & 1)) ? Pp : Pi);
         s = fmaf(v[k], tv, s);
       }
-      const float qh = __fdiv_rn(s, d);
+      float qh;
+      if constexpr (B2) {
+        // q^ = M^-1 q with the node's 2x2 block [d c; c dp] (partner row in the next lane)
+        const unsigned msk = pair_mask();
+        const float qpart = __shfl_xor_sync(msk, s, 1);
+        const float dp = __shfl_xor_sync(msk, d, 1);
+        const float det = __fsub_rn(__fmul_rn(d, dp), __fmul_rn(c, c));
+        qh = __fdiv_rn(__fsub_rn(__fmul_rn(dp, s), __fmul_rn(c, qpart)), det);
+      } else {
+        qh = __fdiv_rn(s, d);
+      }
       if constexpr (ADFEM_ZCG_KEEP_STORES) st_keep(qnew + i, qh, keep);
       else qnew[i] = qh;
       pq = fmaf(Pi, s, pq);
@@ -234,27 +263,34 @@ __global__ void __launch_bounds__(BT, 2) k_zcg_iter(ZcgArgs A) {
     };
     // fixed-width layout: entry k of row i at (i>>5)*32*zw + 32k + (i&31) (padding: value 0,
     // delta 0), so the loads of a row depend on nothing but i
-    auto fetch = [&](int i, float (&v)[MAXW], float& d, int& pid) {
+    auto fetch = [&](int i, float (&v)[MAXW], float& d, float& c, int& pid) {
       const int base = (i >> 5) * (32 * zw) + (i & 31);
 #pragma unroll
       for (int k = 0; k < MAXW; k++) v[k] = k < zw ? ld_stream(A.val + base + 32 * k, pol) : 0.f;
-      d = __ldg(A.dz + i);
+      if constexpr (B2) {
+        const float2 b = __ldg(A.bz + i);
+        d = b.x;
+        c = b.y;
+      } else {
+        d = __ldg(A.dz + i);
+        c = 0.f;
+      }
       pid = __ldg(A.zpid + (i >> 5));
     };
     int i = lo + tid;
     for (; i + (U2 - 1) * BT < hi; i += U2 * BT) {  // U2 rows per thread and trip, loads first
-      float v[U2][MAXW], d[U2];
+      float v[U2][MAXW], d[U2], c[U2];
       int pid[U2];
 #pragma unroll
-      for (int u = 0; u < U2; u++) fetch(i + u * BT, v[u], d[u], pid[u]);
+      for (int u = 0; u < U2; u++) fetch(i + u * BT, v[u], d[u], c[u], pid[u]);
 #pragma unroll
-      for (int u = 0; u < U2; u++) row(i + u * BT, v[u], d[u], pid[u]);
+      for (int u = 0; u < U2; u++) row(i + u * BT, v[u], d[u], c[u], pid[u]);
     }
     for (; i < hi; i += BT) {
-      float v0[MAXW], d0;
+      float v0[MAXW], d0, c0;
       int g0;
-      fetch(i, v0, d0, g0);
-      row(i, v0, d0, g0);
+      fetch(i, v0, d0, c0, g0);
+      row(i, v0, d0, c0, g0);
     }
   }
 
@@ -295,7 +331,7 @@ __global__ void __launch_bounds__(BT, 2) k_zcg_iter(ZcgArgs A) {
 __global__ void k_zprep(int64_t n, const int32_t* __restrict__ sptr, const int16_t* __restrict__ col,
                         const double* __restrict__ val, const int32_t* __restrict__ diagpos, int zw, int block2,
                         double* __restrict__ valz64, float* __restrict__ valz32, float* __restrict__ dz,
-                        int* __restrict__ bad) {
+                        float2* __restrict__ bz, int* __restrict__ bad) {
   const int64_t r = gtid();
   if (r >= n) return;
   int64_t base;
@@ -322,20 +358,39 @@ __global__ void k_zprep(int64_t n, const int32_t* __restrict__ sptr, const int16
     d = 1.0f;
   }
   dz[r] = d;
+  if (block2) {
+    // the row of the node's 2x2 block: {K_ii, K_(i,i^1)}; the partner row is the next
+    // lane (n is even), so the block's determinant is checked here too
+    float c = 0.0f;
+    for (int k = 0; k < w; k++)
+      if (col[base + 32 * (int64_t)k] == dpart) c = (float)val[base + 32 * (int64_t)k];
+    const unsigned pm = pair_mask();
+    const float dpp = __shfl_xor_sync(pm, d, 1);
+    c = __shfl_sync(pm, c, threadIdx.x & 30);  // both rows take K_(2a,2a+1): an exactly symmetric block
+    if (!(__fsub_rn(__fmul_rn(d, dpp), __fmul_rn(c, c)) > 0.0f) || !isfinite(c)) atomicExch(bad, 1);
+    bz[r] = make_float2(d, c);
+  }
 }
 
 // b = rhs (rows tagged 1 in zero_rows get 0), y0 = u0 or 0, ||b||_{D^-1}^2 and the
 // stopping threshold.
 __global__ void __launch_bounds__(kT) k_zinit(int64_t n, const double* __restrict__ rhs, const uint8_t* zero_rows,
-                                              const float* __restrict__ dz, const double* __restrict__ u0,
-                                              double* __restrict__ b, double* __restrict__ y, CgState* st,
-                                              double* partials, double rtol2) {
+                                              const float* __restrict__ dz, const float2* __restrict__ bz,
+                                              const double* __restrict__ u0, double* __restrict__ b,
+                                              double* __restrict__ y, CgState* st, double* partials, double rtol2) {
   double acc = 0.0;
   for (int64_t i = gtid(); i < n; i += gstride()) {
     const double bi = (zero_rows && zero_rows[i] == 1) ? 0.0 : rhs[i];
     b[i] = bi;
     y[i] = u0 ? u0[i] : 0.0;
-    acc = fma(bi, bi / (double)dz[i], acc);
+    if (bz) {  // node-block preconditioner: b . M^-1 b (the partner row is the next lane)
+      const unsigned msk = pair_mask();
+      const float2 m = bz[i];
+      const double d = m.x, c = m.y, dp = __shfl_xor_sync(msk, d, 1), bp = __shfl_xor_sync(msk, bi, 1);
+      acc = fma(bi, (dp * bi - c * bp) / (d * dp - c * c), acc);
+    } else {
+      acc = fma(bi, bi / (double)dz[i], acc);
+    }
   }
   double v[1] = {acc}, tot[1];
   if (reduce_grid<double, 1>(v, partials, &st->counter[0], tot) && threadIdx.x == 0) {
@@ -349,7 +404,8 @@ __global__ void __launch_bounds__(kT) k_zinit(int64_t n, const double* __restric
 // the direction that iteration starts from; mode 2 only records ||r||_{D^-1}^2.
 __global__ void __launch_bounds__(kT) k_zres64(int64_t n, const int32_t* __restrict__ sptr,
                                                const int16_t* __restrict__ col, const double* __restrict__ valz,
-                                               int block2, const float* __restrict__ dz, const double* __restrict__ b,
+                                               int block2, const float* __restrict__ dz,
+                                               const float2* __restrict__ bz, const double* __restrict__ b,
                                                const double* __restrict__ y, float* z0, float* z1, const float* p0,
                                                const float* p1, CgState* st, double* partials, int mode, int force) {
   if (!force && st->done != 3) return;
@@ -375,15 +431,33 @@ __global__ void __launch_bounds__(kT) k_zres64(int64_t n, const int32_t* __restr
       s = fma(valz[idx], t, s);
     }
     const double ri = b[r] - s;
-    const double di = (double)dz[r];
-    const double zt = ri / di;
-    a0 = fma(ri, zt, a0);
-    if (mode == 1) {
-      const float zf = (float)zt;
-      zc[r] = zf;
-      const double dzf = di * (double)zf;
-      a1 = fma(dzf, (double)zf, a1);
-      a2 = fma(dzf, (double)pc[r], a2);
+    if (block2) {
+      // node-block preconditioner: z = M^-1 r with the FP32 block the iteration uses (the
+      // partner row is the next lane; both rows of a node are in range together)
+      const unsigned msk = pair_mask();
+      const float2 m = bz[r];
+      const double d = m.x, c = m.y, dp = __shfl_xor_sync(msk, d, 1), rp = __shfl_xor_sync(msk, ri, 1);
+      const double zt = (dp * ri - c * rp) / (d * dp - c * c);
+      a0 = fma(ri, zt, a0);
+      if (mode == 1) {
+        const float zf = (float)zt;
+        zc[r] = zf;
+        const double zd = (double)zf, zp = __shfl_xor_sync(msk, zd, 1);
+        const double mz = fma(d, zd, c * zp);  // (M Z)_r
+        a1 = fma(mz, zd, a1);
+        a2 = fma(mz, (double)pc[r], a2);
+      }
+    } else {
+      const double di = (double)dz[r];
+      const double zt = ri / di;
+      a0 = fma(ri, zt, a0);
+      if (mode == 1) {
+        const float zf = (float)zt;
+        zc[r] = zf;
+        const double dzf = di * (double)zf;
+        a1 = fma(dzf, (double)zf, a1);
+        a2 = fma(dzf, (double)pc[r], a2);
+      }
     }
   }
   double v[3] = {a0, a1, a2}, tot[3];
@@ -540,7 +614,7 @@ int zcg_plan(Solver& S, int sms) {
   // super-tile rows: the whole per-block range when it fits beside its 2H halo, else the
   // largest multiple of 32 that does; a halo larger than the rows it serves is not worth it
   const int64_t per_block = ((S.n + 2 * (int64_t)sms - 1) / (2 * (int64_t)sms) + 31) / 32 * 32;
-  const int64_t room = (int64_t)((kZSmemBlock - pool_bytes) / sizeof(float)) - 2 * (int64_t)H;
+  const int64_t room = (int64_t)((kZSmemBlock - pool_bytes) / sizeof(float)) - 2 * (int64_t)H - 2;
   int64_t smax = room / 32 * 32;
   if (smax < std::max<int64_t>(1024, 2 * (int64_t)H)) return ADFEM_OK;  // scaled two-kernel path
   // ADFEM_ZCG_SMAX caps the super-tile rows (a test hook for ranges split into several)
@@ -550,7 +624,7 @@ int zcg_plan(Solver& S, int sms) {
   }
   S.zS = (int)std::min<int64_t>(std::max<int64_t>(per_block, ((int64_t)H + 31) / 32 * 32), smax);
   S.zH = H;
-  S.zW = S.zS + 2 * H;
+  S.zW = S.zS + 2 * H + 2;  // (+2: windows of 2-DOF operators are widened to even ends)
   S.zsmem = pool_bytes + sizeof(float) * (size_t)S.zW;
   // (the block form is decided after the layout pass below; both 16-wide variants have
   // the same resources, so the plan is made with the plain one)
@@ -582,6 +656,7 @@ int zcg_plan(Solver& S, int sms) {
   int no_partner = 0;
   ADFEM_CUDA(cudaMemcpy(&no_partner, flag.p, sizeof(int), cudaMemcpyDeviceToHost));
   S.zblock2 = A.pat_period == 2 && !no_partner && A.maxw > 8;
+  if (S.zblock2) ADFEM_TRY(S.bz32.alloc(sizeof(float2) * (size_t)S.n));
 
   S.zcg = true;
   return ADFEM_OK;
@@ -592,7 +667,7 @@ int zcg_prepare(Solver& S, const int32_t* diagpos_dev, int* bad_dev, cudaStream_
   const unsigned nb = (unsigned)((S.n + kT - 1) / kT);
   k_zprep<<<nb, kT, 0, st>>>(S.n, A.sptr.as<int32_t>(), A.col.as<int16_t>(), A.val64.as<double>(), diagpos_dev,
                              S.zw, S.zblock2 ? 1 : 0, S.valz64.as<double>(), S.valz32.as<float>(),
-                             S.dz32.as<float>(), bad_dev);
+                             S.dz32.as<float>(), S.zblock2 ? S.bz32.as<float2>() : nullptr, bad_dev);
   ADFEM_CUDA(cudaGetLastError());
   return ADFEM_OK;
 }
@@ -612,6 +687,7 @@ static ZcgArgs zcg_args(Solver& S) {
   z.colz = S.colz16.as<int16_t>();
   z.val = S.valz32.as<float>();
   z.dz = S.dz32.as<float>();
+  z.bz = S.zblock2 ? S.bz32.as<float2>() : nullptr;
   z.z[0] = S.r32.as<float>();
   z.z[1] = S.z1.as<float>();
   z.p[0] = S.pa32.as<float>();
@@ -634,14 +710,15 @@ void zcg_enqueue_iter(Solver& S, cudaStream_t st) {
 
 void zcg_enqueue_init(Solver& S, cudaStream_t st, const double* rhs, const uint8_t* zero_rows, const double* u0,
                       double rtol2) {
-  k_zinit<<<S.grid, kT, 0, st>>>(S.n, rhs, zero_rows, S.dz32.as<float>(), u0, S.b.as<double>(), S.y64.as<double>(),
-                                 S.state.as<CgState>(), S.partials.as<double>(), rtol2);
+  k_zinit<<<S.grid, kT, 0, st>>>(S.n, rhs, zero_rows, S.dz32.as<float>(), S.zblock2 ? S.bz32.as<float2>() : nullptr,
+                                 u0, S.b.as<double>(), S.y64.as<double>(), S.state.as<CgState>(),
+                                 S.partials.as<double>(), rtol2);
 }
 
 void zcg_enqueue_residual(Solver& S, cudaStream_t st, int mode, int force) {
   const Sell& A = *S.A;
   k_zres64<<<S.grid, kT, 0, st>>>(S.n, A.sptr.as<int32_t>(), A.col.as<int16_t>(), S.valz64.as<double>(),
-                                  S.zblock2 ? 1 : 0, S.dz32.as<float>(), S.b.as<double>(), S.y64.as<double>(), S.r32.as<float>(),
+                                  S.zblock2 ? 1 : 0, S.dz32.as<float>(), S.zblock2 ? S.bz32.as<float2>() : nullptr, S.b.as<double>(), S.y64.as<double>(), S.r32.as<float>(),
                                   S.z1.as<float>(), S.pa32.as<float>(), S.pb32.as<float>(), S.state.as<CgState>(),
                                   S.partials.as<double>(), mode, force);
 }
