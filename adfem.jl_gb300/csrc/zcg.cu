@@ -108,7 +108,7 @@ __device__ __forceinline__ float ld_stream(const float* a, uint64_t pol) {
 // and its partner are neighbouring lanes of one warp (block ranges, windows and tiles
 // start at even rows), so M and M^-1 are applied with one lane shuffle.
 template <int MAXW, int BT, int U1, int U2, bool B2>
-__global__ void __launch_bounds__(BT, 2) k_zcg_iter(ZcgArgs A) {
+__global__ void __launch_bounds__(BT, 1024 / BT) k_zcg_iter(ZcgArgs A) {
   static_assert(MAXW % 4 == 0, "pattern rows are loaded as int4");
   CgState* st = A.st;
   if (st->done) return;
@@ -513,7 +513,11 @@ __global__ void k_zunscale(int64_t n, const double* __restrict__ y, const uint8_
 }
 
 // ---------------------------------------------------------------------------
-static constexpr int kZBT = 512;                     // threads per block
+#ifndef ADFEM_ZCG_BT
+#define ADFEM_ZCG_BT 512
+#endif
+static constexpr int kZBT = ADFEM_ZCG_BT;            // threads per block
+static constexpr int kZPerSM = 1024 / kZBT;          // resident blocks per SM (1024 threads)
 #ifndef ADFEM_ZCG_U1
 #define ADFEM_ZCG_U1 4
 #endif
@@ -522,7 +526,7 @@ static constexpr int kZBT = 512;                     // threads per block
 #endif
 static constexpr int kZU1 = ADFEM_ZCG_U1;            // phase-1 positions per thread and trip
 static constexpr int kZU2 = ADFEM_ZCG_U2;            // phase-2 matrix rows per thread and trip
-static constexpr size_t kZSmemBlock = 100 * 1024;    // shared memory per block (two blocks per SM)
+static constexpr size_t kZSmemBlock = (kZPerSM >= 2 ? 100 : 200) * 1024;  // shared memory per block
 
 // Distinct slice column patterns (at most kZMaxPatterns; further slices use their
 // per-entry deltas), padded to the kernel's unrolled width per row parity, and the
@@ -613,7 +617,7 @@ int zcg_plan(Solver& S, int sms) {
   const size_t pool_bytes = sizeof(int32_t) * (size_t)((S.znpool + 3) & ~3);
   // super-tile rows: the whole per-block range when it fits beside its 2H halo, else the
   // largest multiple of 32 that does; a halo larger than the rows it serves is not worth it
-  const int64_t per_block = ((S.n + 2 * (int64_t)sms - 1) / (2 * (int64_t)sms) + 31) / 32 * 32;
+  const int64_t per_block = ((S.n + kZPerSM * (int64_t)sms - 1) / (kZPerSM * (int64_t)sms) + 31) / 32 * 32;
   const int64_t room = (int64_t)((kZSmemBlock - pool_bytes) / sizeof(float)) - 2 * (int64_t)H - 2;
   int64_t smax = room / 32 * 32;
   if (smax < std::max<int64_t>(1024, 2 * (int64_t)H)) return ADFEM_OK;  // scaled two-kernel path
