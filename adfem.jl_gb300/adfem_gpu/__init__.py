@@ -1,4 +1,4 @@
-"""adfem_gpu -- GB300 implementation of AdFem.jl's P1-triangle forward/adjoint path.
+"""adfem_gpu -- GB300 implementation of AdFem.jl's triangle-element forward/adjoint path.
 
 This module mirrors the Julia operator API of AdFem on top of the C ABI of
 libadfem_gpu.so (include/adfem_gpu.h): the same function names, argument
@@ -14,6 +14,8 @@ only converts arguments.
     compute_fem_source_term(f1, f2, mesh)        src/MFEM/MCore.jl:87-94
     compute_fem_stiffness_matrix(D, mesh)        src/MFEM/MCore.jl:287-315
     compute_plane_strain_matrix(E, nu)           src/Core.jl:777-785
+    compute_fem_mass_matrix1(rho, mesh)          src/MFEM/MCore.jl:170-193
+    fem_to_gauss_points / dof_to_gauss_points    src/MFEM/MUtils.jl:231-275
     bcnode(mesh)                                 src/MFEM/MCore.jl:439-450
     impose_Dirichlet_boundary_conditions(...)    src/MFEM/MUtils.jl:184-199
     solve(K, F)  (K\\F)                          README.md:54
@@ -33,8 +35,13 @@ __all__ = [
     "compute_fem_laplace_matrix1", "compute_fem_source_term1", "compute_fem_source_term",
     "compute_fem_stiffness_matrix", "compute_plane_strain_matrix", "compute_plane_stress_matrix",
     "impose_Dirichlet_boundary_conditions", "impose_Dirichlet_coo", "impose_Dirichlet_coo_backward",
-    "solve", "solver_opts",
+    "solve", "solver_opts", "get_connectivity", "gauss_weights", "dof_nodes", "eval_f_on_gauss_pts",
+    "eval_f_on_fem_pts", "eval_f_on_dof_pts", "compute_fem_mass_matrix1", "compute_fem_mass_matrix",
+    "fem_to_gauss_points", "dof_to_gauss_points", "P1", "P2",
 ]
+
+P1 = 1
+P2 = 2
 
 
 def _lib_():
@@ -46,18 +53,19 @@ def _c(a, dt):
 
 
 class Mesh:
-    """P1 triangle mesh resident on the GPU (mirror of AdFem's ``Mesh``).
+    """Triangle mesh resident on the GPU (mirror of AdFem's ``Mesh``).
 
-    ``coords``: (nnode, 2) float; ``elems``: (nelem, 3) 1-based vertex ids.  Only
-    degree 1 (P1) with the order-2 rule is supported; anything else raises
+    ``coords``: (nnode, 2) float; ``elems``: (nelem, 3) 1-based vertex ids.  Degree 1
+    (P1, order-2 rule) and degree 2 (P2, order-4 rule) are supported (``order=-1``
+    selects these defaults, src/MFEM/MFEM.jl:71-77); BDM1 and other orders raise
     ``AdFemError`` with status ``ERR_UNSUPPORTED``.
     """
 
     def __init__(self, coords, elems, order: int = -1, degree: int = 1, lorder: int = -1):
-        if degree != 1:
-            raise AdFemError(_lib.ERR_UNSUPPORTED, "only degree 1 (P1) elements are implemented")
-        if order not in (-1, 2):
-            raise AdFemError(_lib.ERR_UNSUPPORTED, "only the order-2 triangle rule is implemented")
+        if degree not in (1, 2):
+            raise AdFemError(_lib.ERR_UNSUPPORTED, "degree 1 (P1) and 2 (P2) elements are implemented")
+        if order not in (-1, 2 * degree):
+            raise AdFemError(_lib.ERR_UNSUPPORTED, "P1 uses the order-2 rule and P2 the order-4 rule")
         L = _lib_()
         coords = _c(coords, np.float64)
         elems = np.asarray(elems)
@@ -68,18 +76,24 @@ class Mesh:
         xyz[:, :2] = coords
         e0 = _c(elems - 1, np.int32)
         h = ctypes.c_void_p()
-        check(L.adfem_mesh_create(ptr(xyz), nv, ptr(e0), ne, 1, ctypes.byref(h)), "Mesh")
+        check(L.adfem_mesh_create(ptr(xyz), nv, ptr(e0), ne, degree, ctypes.byref(h)), "Mesh")
         self._h = h
         self.nodes = coords
         self.nnode = nv
         self.nelem = ne
-        self.ndof = nv
-        self.elem_ndof = 3
+        self.degree = degree
+        self.elem_type = P1 if degree == 1 else P2
+        nd, ndof = ctypes.c_int(), ctypes.c_longlong()
+        check(L.adfem_mesh_space(h, None, ctypes.byref(nd), None, ctypes.byref(ndof), None))
+        self.ndof = ndof.value
+        self.elem_ndof = nd.value
         self.lorder = 6 if lorder == -1 else lorder
         el = np.empty(3 * ne, np.int64)
         check(L.adfem_mesh_elements(h, ptr(el)))
         self.elems = el.reshape(ne, 3)
-        self.conn = self.elems
+        conn = np.empty(self.elem_ndof * ne, np.int64)
+        check(L.adfem_mesh_connectivity(h, ptr(conn)))
+        self.conn = conn.reshape(ne, self.elem_ndof)
         nedge = ctypes.c_longlong()
         check(L.adfem_mesh_edges(h, None, ctypes.byref(nedge)))
         ed = np.empty(2 * nedge.value, np.int64)
@@ -90,7 +104,7 @@ class Mesh:
         self._pattern_el = None
 
     @classmethod
-    def rectangle(cls, m: int, n: int, h: float, version: int = 1):
+    def rectangle(cls, m: int, n: int, h: float, version: int = 1, degree: int = 1):
         """``Mesh(m, n, h)``: m x n cells of size h, nodes x-fastest (MFEM.jl:134-170)."""
         if version not in (1, 2):
             raise AdFemError(_lib.ERR_UNSUPPORTED, "versions 1 and 2 are implemented")
@@ -108,7 +122,7 @@ class Mesh:
         else:
             el[0::2] = np.stack([a, d, c], 1)
             el[1::2] = np.stack([a, b, d], 1)
-        return cls(coords, el + 1)
+        return cls(coords, el + 1, degree=degree)
 
     @property
     def handle(self):
@@ -131,7 +145,7 @@ class Mesh:
             L = _lib_()
             nnz = ctypes.c_longlong()
             check(L.adfem_mesh_sizes(self._h, None, None, None, ctypes.byref(nnz)))
-            cp = np.empty(self.nnode + 1, np.int64)
+            cp = np.empty(self.ndof + 1, np.int64)
             rv = np.empty(nnz.value, np.int64)
             check(L.adfem_mesh_pattern(self._h, ptr(cp), ptr(rv)))
             self._pattern = (cp, rv)
@@ -141,7 +155,7 @@ class Mesh:
         if self._pattern_el is None:
             L = _lib_()
             cp0, rv0 = self.pattern()
-            cp = np.empty(2 * self.nnode + 1, np.int64)
+            cp = np.empty(2 * self.ndof + 1, np.int64)
             rv = np.empty(4 * rv0.size, np.int64)
             check(L.adfem_mesh_pattern_elasticity(self._h, ptr(cp), ptr(rv)))
             self._pattern_el = (cp, rv)
@@ -152,7 +166,40 @@ class Mesh:
 
 
 def get_ngauss(mesh: Mesh) -> int:
-    return 3 * mesh.nelem
+    return (3 if mesh.degree == 1 else 6) * mesh.nelem
+
+
+def get_connectivity(mesh: Mesh):
+    """ne x elem_ndof DOFs, 1-based: vertices, then nnode + edge for P2 (mfem_get_connectivity)."""
+    return mesh.conn
+
+
+def gauss_weights(mesh: Mesh):
+    w = np.empty(get_ngauss(mesh))
+    check(_lib_().adfem_mesh_gauss_weights(mesh.handle, ptr(w)))
+    return w
+
+
+def dof_nodes(mesh: Mesh):
+    """Coordinates of the DOFs: the vertices, then (P2) the edge midpoints."""
+    if mesh.degree == 1:
+        return mesh.nodes
+    mid = 0.5 * (mesh.nodes[mesh.edges[:, 0] - 1] + mesh.nodes[mesh.edges[:, 1] - 1])
+    return np.concatenate([mesh.nodes, mid])
+
+
+def eval_f_on_gauss_pts(f, mesh: Mesh):
+    g = gauss_nodes(mesh)
+    return np.asarray(f(g[:, 0], g[:, 1]), dtype=np.float64)
+
+
+def eval_f_on_fem_pts(f, mesh: Mesh):
+    return np.asarray(f(mesh.nodes[:, 0], mesh.nodes[:, 1]), dtype=np.float64)
+
+
+def eval_f_on_dof_pts(f, mesh: Mesh):
+    x = dof_nodes(mesh)
+    return np.asarray(f(x[:, 0], x[:, 1]), dtype=np.float64)
 
 
 def get_area(mesh: Mesh):
@@ -173,7 +220,8 @@ def fem_nodes(mesh: Mesh):
 
 
 def bcnode(mesh: Mesh):
-    """Boundary node ids, 1-based, ascending (the reference returns Julia Set order)."""
+    """Boundary DOFs, 1-based: ascending vertices (the reference returns Julia Set order),
+    then for P2 the DOFs of the boundary edges."""
     L = _lib_()
     n = ctypes.c_longlong()
     check(L.adfem_mesh_bcnode(mesh.handle, None, ctypes.byref(n)))
@@ -230,6 +278,44 @@ def compute_fem_stiffness_matrix(D, mesh: Mesh):
     nz = np.empty(rv.size)
     check(_lib_().adfem_stiffness_csc(mesh.handle, ptr(D), D.size, ptr(nz)), "compute_fem_stiffness_matrix")
     return _csc(nz, cp, rv, 2 * mesh.ndof)
+
+
+def compute_fem_mass_matrix1(rho, mesh: Mesh | None = None):
+    """Mass matrix sum_k rho_k w_k phi phi^T (SparseMatrixCSC arm), rho at the Gauss points;
+    ``compute_fem_mass_matrix1(mesh)`` uses rho = 1 (MCore.jl:170-181)."""
+    if mesh is None and isinstance(rho, Mesh):
+        mesh, rho = rho, np.ones(get_ngauss(rho))
+    rho = _c(rho, np.float64).ravel()
+    if rho.size != get_ngauss(mesh):
+        raise AdFemError(_lib.ERR_INVALID, "length(rho) must equal get_ngauss(mesh)")
+    cp, rv = mesh.pattern()
+    nz = np.empty(rv.size)
+    check(_lib_().adfem_mass_csc(mesh.handle, ptr(rho), rho.size, ptr(nz)), "compute_fem_mass_matrix1")
+    return _csc(nz, cp, rv, mesh.ndof)
+
+
+def compute_fem_mass_matrix(rho, mesh: Mesh | None = None):
+    """[M 0; 0 M] for the two displacement components (MCore.jl:183-193)."""
+    M = compute_fem_mass_matrix1(rho, mesh)
+    return sp.block_diag([M, M], format="csc")
+
+
+def fem_to_gauss_points(u, mesh: Mesh):
+    """Nodal values (length nnode) at the Gauss points through the P1 shape (MUtils.jl:231-246)."""
+    u = _c(u, np.float64).ravel()
+    out = np.empty(get_ngauss(mesh))
+    check(_lib_().adfem_fem_to_gauss(mesh.handle, ptr(u), u.size, ptr(out)), "fem_to_gauss_points")
+    return out
+
+
+def dof_to_gauss_points(u, mesh: Mesh):
+    """DOF values (length ndof) at the Gauss points through every basis function (MUtils.jl:256-270)."""
+    u = _c(u, np.float64).ravel()
+    if u.size != mesh.ndof:
+        raise AdFemError(_lib.ERR_INVALID, "length(u) must equal mesh.ndof")
+    out = np.empty(get_ngauss(mesh))
+    check(_lib_().adfem_dof_to_gauss(mesh.handle, ptr(u), u.size, ptr(out)), "dof_to_gauss_points")
+    return out
 
 
 def _plane(E, nu, fn):

@@ -93,6 +93,14 @@ SIGNATURES = {
     "FemLaplaceScalar_backward": (None, [c_p, c_p, c_p, c_p, c_p]),
     "FemSourceScalar_backward": (None, [c_p, c_p, c_p, c_p]),
     "ComputeFemStiffnessMatrixMfem_backward": (None, [c_p, c_p]),
+    "ComputeFemMassMatrix1_forward": (None, [c_p, c_p, c_p]),
+    "ComputeFemMassMatrix1_backward": (None, [c_p, c_p, c_p, c_p]),
+    "FemToGaussPointsMfem_Julia": (None, [c_p, c_p]),
+    "FemToGaussPointsMfem_forward": (None, [c_p, c_p]),
+    "FemToGaussPointsMfem_backward": (None, [c_p, c_p, c_p, c_p]),
+    "DofToGaussPointsMfem_forward_Julia": (None, [c_p, c_p]),
+    "DofToGaussPointsMfem_forward": (None, [c_p, c_p]),
+    "DofToGaussPointsMfem_backward": (None, [c_p, c_p, c_p, c_p]),
     "PlaneStrainMatrix_forward": (None, [c_p, c_p, c_p, c_i]),
     "PlaneStrainMatrix_backward": (None, [c_p, c_p, c_p, c_p, c_p, c_i]),
     "PlaneStressMatrix_forward": (None, [c_p, c_p, c_p, c_i]),
@@ -109,6 +117,19 @@ SIGNATURES = {
     "adfem_mesh_elements": (c_i, [c_p, c_p]),
     "adfem_mesh_area": (c_i, [c_p, c_p]),
     "adfem_mesh_edges": (c_i, [c_p, c_p, c_p]),
+    "adfem_mesh_space": (c_i, [c_p, c_p, c_p, c_p, c_p, c_p]),
+    "adfem_mesh_connectivity": (c_i, [c_p, c_p]),
+    "adfem_mesh_gauss_weights": (c_i, [c_p, c_p]),
+    "adfem_mass_csc": (c_i, [c_p, c_p, c_ll, c_p]),
+    "adfem_mass_csr_d": (c_i, [c_p, c_p, c_p, c_p]),
+    "adfem_mass_coo_d": (c_i, [c_p, c_p, c_p, c_p, c_p]),
+    "adfem_mass_coo_backward_d": (c_i, [c_p, c_p, c_p, c_p]),
+    "adfem_fem_to_gauss": (c_i, [c_p, c_p, c_ll, c_p]),
+    "adfem_dof_to_gauss": (c_i, [c_p, c_p, c_ll, c_p]),
+    "adfem_fem_to_gauss_d": (c_i, [c_p, c_p, c_p, c_p]),
+    "adfem_fem_to_gauss_backward_d": (c_i, [c_p, c_p, c_p, c_ll, c_i, c_p]),
+    "adfem_dof_to_gauss_d": (c_i, [c_p, c_p, c_p, c_p]),
+    "adfem_dof_to_gauss_backward_d": (c_i, [c_p, c_p, c_p, c_ll, c_i, c_p]),
     "adfem_laplace_csc": (c_i, [c_p, c_p, c_ll, c_p]),
     "adfem_laplace_csr_d": (c_i, [c_p, c_p, c_p, c_p]),
     "adfem_laplace_coo_d": (c_i, [c_p, c_p, c_p, c_p, c_p]),

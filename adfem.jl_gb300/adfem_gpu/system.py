@@ -174,21 +174,25 @@ class ElasticitySystem(_System):
 
 
 # --------------------------------------------------------------- device operators
+def _ng(mesh):
+    return (3 if mesh.degree == 1 else 6) * mesh.nelem
+
+
 def laplace_coo(mesh, kappa):
-    """FemLaplaceScalar forward on the device: (indices (N,2) int64, vv (N,)), N = 9 ngauss."""
+    """FemLaplaceScalar forward on the device: (indices (N,2) int64, vv (N,)), N = elem_ndof^2 ngauss."""
     torch = _torch()
-    ng = 3 * mesh.nelem
+    ng, nd2 = _ng(mesh), mesh.elem_ndof ** 2
     _dev(kappa, ng, "kappa")
-    idx = torch.empty((9 * ng, 2), dtype=torch.int64, device="cuda")
-    vv = torch.empty(9 * ng, dtype=torch.float64, device="cuda")
+    idx = torch.empty((nd2 * ng, 2), dtype=torch.int64, device="cuda")
+    vv = torch.empty(nd2 * ng, dtype=torch.float64, device="cuda")
     check(_lib.load().adfem_laplace_coo_d(mesh.handle, ptr(kappa), ptr(idx), ptr(vv), _cur_stream()), "laplace_coo")
     return idx, vv
 
 
 def laplace_coo_backward(mesh, grad_vv):
     torch = _torch()
-    ng = 3 * mesh.nelem
-    _dev(grad_vv, 9 * ng, "grad_vv")
+    ng = _ng(mesh)
+    _dev(grad_vv, mesh.elem_ndof ** 2 * ng, "grad_vv")
     g = torch.empty(ng, dtype=torch.float64, device="cuda")
     check(_lib.load().adfem_laplace_coo_backward_d(mesh.handle, ptr(grad_vv), ptr(g), _cur_stream()), "laplace bwd")
     return g
@@ -197,15 +201,44 @@ def laplace_coo_backward(mesh, grad_vv):
 def laplace_csr(mesh, kappa):
     torch = _torch()
     cp, rv = mesh.pattern()
-    _dev(kappa, 3 * mesh.nelem, "kappa")
+    _dev(kappa, _ng(mesh), "kappa")
     v = torch.empty(rv.size, dtype=torch.float64, device="cuda")
     check(_lib.load().adfem_laplace_csr_d(mesh.handle, ptr(kappa), ptr(v), _cur_stream()), "laplace_csr")
     return v
 
 
+def mass_coo(mesh, rho):
+    """ComputeFemMassMatrix1 forward on the device (elem_ndof^2 entries per Gauss point)."""
+    torch = _torch()
+    ng, nd2 = _ng(mesh), mesh.elem_ndof ** 2
+    _dev(rho, ng, "rho")
+    idx = torch.empty((nd2 * ng, 2), dtype=torch.int64, device="cuda")
+    vv = torch.empty(nd2 * ng, dtype=torch.float64, device="cuda")
+    check(_lib.load().adfem_mass_coo_d(mesh.handle, ptr(rho), ptr(idx), ptr(vv), _cur_stream()), "mass_coo")
+    return idx, vv
+
+
+def mass_coo_backward(mesh, grad_vv):
+    torch = _torch()
+    ng = _ng(mesh)
+    _dev(grad_vv, mesh.elem_ndof ** 2 * ng, "grad_vv")
+    g = torch.empty(ng, dtype=torch.float64, device="cuda")
+    check(_lib.load().adfem_mass_coo_backward_d(mesh.handle, ptr(grad_vv), ptr(g), _cur_stream()), "mass bwd")
+    return g
+
+
+def mass_csr(mesh, rho):
+    torch = _torch()
+    cp, rv = mesh.pattern()
+    _dev(rho, _ng(mesh), "rho")
+    v = torch.empty(rv.size, dtype=torch.float64, device="cuda")
+    check(_lib.load().adfem_mass_csr_d(mesh.handle, ptr(rho), ptr(v), _cur_stream()), "mass_csr")
+    return v
+
+
 def source(mesh, f, rhs=None, accumulate=False):
     torch = _torch()
-    _dev(f, 3 * mesh.nelem, "f")
+    _dev(f, _ng(mesh), "f")
     if rhs is None:
         rhs = torch.zeros(mesh.ndof, dtype=torch.float64, device="cuda")
     check(_lib.load().adfem_source_d(mesh.handle, ptr(f), ptr(rhs), int(accumulate), _cur_stream()), "source")
@@ -215,25 +248,25 @@ def source(mesh, f, rhs=None, accumulate=False):
 def source_backward(mesh, grad_rhs):
     torch = _torch()
     _dev(grad_rhs, mesh.ndof, "grad_rhs")
-    g = torch.empty(3 * mesh.nelem, dtype=torch.float64, device="cuda")
+    g = torch.empty(_ng(mesh), dtype=torch.float64, device="cuda")
     check(_lib.load().adfem_source_backward_d(mesh.handle, ptr(grad_rhs), ptr(g), _cur_stream()), "source bwd")
     return g
 
 
 def stiffness_coo(mesh, D):
     torch = _torch()
-    ng = 3 * mesh.nelem
+    ng, n4 = _ng(mesh), 4 * mesh.elem_ndof ** 2
     _dev(D, 9 * ng, "D")
-    idx = torch.empty((36 * ng, 2), dtype=torch.int64, device="cuda")
-    vv = torch.empty(36 * ng, dtype=torch.float64, device="cuda")
+    idx = torch.empty((n4 * ng, 2), dtype=torch.int64, device="cuda")
+    vv = torch.empty(n4 * ng, dtype=torch.float64, device="cuda")
     check(_lib.load().adfem_stiffness_coo_d(mesh.handle, ptr(D), ptr(idx), ptr(vv), _cur_stream()), "stiffness_coo")
     return idx, vv
 
 
 def stiffness_coo_backward(mesh, grad_vv):
     torch = _torch()
-    ng = 3 * mesh.nelem
-    _dev(grad_vv, 36 * ng, "grad_vv")
+    ng = _ng(mesh)
+    _dev(grad_vv, 4 * mesh.elem_ndof ** 2 * ng, "grad_vv")
     g = torch.empty(9 * ng, dtype=torch.float64, device="cuda")
     check(_lib.load().adfem_stiffness_coo_backward_d(mesh.handle, ptr(grad_vv), ptr(g), _cur_stream()), "stiff bwd")
     return g
@@ -242,10 +275,50 @@ def stiffness_coo_backward(mesh, grad_vv):
 def stiffness_csr(mesh, D):
     torch = _torch()
     cp, rv = mesh.pattern_elasticity()
-    _dev(D, 27 * mesh.nelem, "D")
+    _dev(D, 9 * _ng(mesh), "D")
     v = torch.empty(rv.size, dtype=torch.float64, device="cuda")
     check(_lib.load().adfem_stiffness_csr_d(mesh.handle, ptr(D), ptr(v), _cur_stream()), "stiffness_csr")
     return v
+
+
+def fem_to_gauss(mesh, u):
+    """fem_to_gauss_points on the device: nodal values (nnode) -> Gauss points."""
+    torch = _torch()
+    _dev(u, None, "u")
+    out = torch.empty(_ng(mesh), dtype=torch.float64, device="cuda")
+    check(_lib.load().adfem_fem_to_gauss_d(mesh.handle, ptr(u), ptr(out), _cur_stream()), "fem_to_gauss")
+    return out
+
+
+def fem_to_gauss_backward(mesh, grad_out, nu=None, grad_u=None):
+    """Transpose of fem_to_gauss: writes nu entries, or adds into grad_u when given."""
+    torch = _torch()
+    _dev(grad_out, _ng(mesh), "grad_out")
+    acc = grad_u is not None
+    if grad_u is None:
+        grad_u = torch.empty(mesh.nnode if nu is None else nu, dtype=torch.float64, device="cuda")
+    check(_lib.load().adfem_fem_to_gauss_backward_d(mesh.handle, ptr(grad_out), ptr(grad_u), grad_u.numel(),
+                                                    int(acc), _cur_stream()), "fem_to_gauss backward")
+    return grad_u
+
+
+def dof_to_gauss(mesh, u):
+    torch = _torch()
+    _dev(u, mesh.ndof, "u")
+    out = torch.empty(_ng(mesh), dtype=torch.float64, device="cuda")
+    check(_lib.load().adfem_dof_to_gauss_d(mesh.handle, ptr(u), ptr(out), _cur_stream()), "dof_to_gauss")
+    return out
+
+
+def dof_to_gauss_backward(mesh, grad_out, grad_u=None):
+    torch = _torch()
+    _dev(grad_out, _ng(mesh), "grad_out")
+    acc = grad_u is not None
+    if grad_u is None:
+        grad_u = torch.empty(mesh.ndof, dtype=torch.float64, device="cuda")
+    check(_lib.load().adfem_dof_to_gauss_backward_d(mesh.handle, ptr(grad_out), ptr(grad_u), grad_u.numel(),
+                                                    int(acc), _cur_stream()), "dof_to_gauss backward")
+    return grad_u
 
 
 def plane_strain(E, nu, mode=0):

@@ -93,10 +93,39 @@ struct Sell {
   DevBuf val32;         // float  [nent]
 };
 
-// Device-resident P1 mesh: geometry, incidence, scalar CSR pattern and the
-// sliced-ELL copy of that pattern.
+// Degree-generic Lagrange space on a triangle mesh (P1 or P2), used by the generic
+// element kernels (generic.cu): element DOFs, the DOF graph pattern and the
+// DOF->element incidence.  P2 DOFs are the vertices, then nv + edge for the edge
+// midpoints; an element lists its vertices, then its local edges (0,1), (1,2), (2,0).
+// Incidence record s of DOF i (ascending element order) is {e, a, o0 | o1 << 10 |
+// o2 << 20, o3 | o4 << 10 | o5 << 20}: element, local index of i in e, and the
+// position within row i of the column of each local DOF b of e.
+struct Space {
+  int degree = 1;
+  int nd = 3;            // DOFs per element
+  int ng = 3;            // Gauss points per element
+  int64_t ndof = 0, nnz = 0;
+  int maxrow = 0;
+  std::vector<int32_t> dof;      // nd * ne
+  std::vector<int32_t> rowptr;   // ndof + 1
+  std::vector<int32_t> colind;   // nnz
+  DevBuf d_dof;      // int32 [nd * ne]
+  DevBuf d_area;     // double [ne]
+  DevBuf d_rowptr;   // int32 [ndof + 1]
+  DevBuf d_colind;   // int32 [nnz]
+  DevBuf d_inc_ptr;  // int32 [ndof + 1]
+  DevBuf d_inc;      // uint4 [nd * ne]
+  DevBuf d_ke;       // element matrices (scratch of the summed-operator kernels)
+};
+__host__ __device__ inline unsigned space_off(uint4 r, int b) {
+  return ((b < 3 ? r.z : r.w) >> (10 * (b % 3))) & 1023u;
+}
+
+// Device-resident triangle mesh: P1 geometry, incidence, scalar CSR pattern and the
+// sliced-ELL copy of that pattern; degree-2 meshes add a P2 space.
 struct Mesh {
   int64_t nv = 0, ne = 0;
+  int degree = 1;       // element degree the mesh was created with (1 or 2)
   int64_t nnz = 0;      // scalar CSR pattern entries
   int maxrow = 0;       // longest scalar row
   int maxinc = 0;       // largest node valence (incident elements)
@@ -112,7 +141,9 @@ struct Mesh {
   std::vector<int32_t> inc_ptr;  // nv+1
   std::vector<uint32_t> inc;     // 2 * 3ne (x,y pairs)
   std::vector<int64_t> edges;    // 2*nedges, 1-based (min block then max block); filled lazily
+  std::vector<int32_t> eedge;    // 3*ne edge of each local edge (0,1), (1,2), (2,0); with edges
   int64_t nedges = -1;
+  std::unique_ptr<Space> space[3];  // [degree], built on first use
 
   // device copies
   DevBuf d_xy;       // double2 [nv]
@@ -128,7 +159,7 @@ struct Mesh {
   Sell sell;         // scalar pattern in sliced-ELL (values unused here)
   DevBuf d_sell2;    // (built lazily) interleaved 2-dof pattern: see Elasticity
 
-  // per-mesh scratch reused by the host-pointer entry points
+  // per-mesh scratch reused by the host-pointer entry points (mu also guards space[])
   std::mutex mu;
   DevBuf s_in0, s_in1, s_out0, s_out1, s_el0, s_el1;
 };
@@ -136,9 +167,22 @@ struct Mesh {
 // Build a mesh from xyz triples (z ignored) and 0-based triangles.  Host work
 // (orientation fix, geometry, incidence, pattern) then upload.
 int mesh_build(const double* xyz, int64_t nv, const int32_t* elems0, int64_t ne, Mesh** out);
-int mesh_edges(Mesh* m);  // fills m->edges / nedges (first-appearance numbering)
-int64_t mesh_bcnode(const Mesh* m, int64_t* out1);  // ascending 1-based boundary nodes
-void mesh_gauss(const Mesh* m, double* x, double* y);  // 3 points per element
+int mesh_edges(Mesh* m);  // fills m->edges / eedge / nedges (first-appearance numbering)
+// Boundary DOFs, 1-based: ascending boundary vertices; for degree-2 meshes followed by
+// the ascending DOFs of boundary edges
+int64_t mesh_bcnode(Mesh* m, int64_t* out1);
+// Gauss points per element (3 for the order-2 rule of P1, 6 for the order-4 rule of P2)
+inline int mesh_ng(const Mesh& m) { return m.degree == 2 ? 6 : 3; }
+inline int64_t mesh_ngauss(const Mesh& m) { return (int64_t)mesh_ng(m) * m.ne; }
+// DOFs of the mesh's own space (nv, or nv + nedges for P2)
+int64_t mesh_ndof(Mesh* m);
+void mesh_gauss(const Mesh* m, double* x, double* y);      // mesh_ng points per element
+void mesh_gauss_weights(const Mesh* m, double* w);          // ip.weight * area / 0.5
+// The space of the given degree on m, built on first use (host work + upload); the
+// caller holds m->mu.
+int mesh_space(Mesh* m, int degree, Space** out);
+// Triangle rules: reference coordinates and weights of point k (order 2 or 4)
+void rule_point(int degree, int k, double* xi, double* eta, double* w);
 
 // ---------------------------------------------------------------------------
 // kernels (launchers; every launcher returns cudaError_t from cudaGetLastError)
@@ -178,6 +222,39 @@ cudaError_t launch_stiffness_rows(const Mesh& m, const double* Dbar, double* val
                                   cudaStream_t st);
 cudaError_t launch_stiffness_coo(const Mesh& m, const double* D, long long* indices, double* vv, cudaStream_t st);
 cudaError_t launch_stiffness_coo_backward(const Mesh& m, const double* grad_vv, double* grad_D, cudaStream_t st);
+
+// degree-generic element kernels (generic.cu), on a Space of degree 1 or 2.  Per-point
+// inputs hold sp.ng values per element (9 per point for D), element-major.
+enum class GenOp { LAPLACE = 0, MASS = 1 };
+// unsummed COO of the reference op: nd*nd entries per Gauss point (Laplace, mass)
+cudaError_t launch_gen_coo(const Mesh& m, const Space& sp, GenOp op, const double* coef, long long* indices,
+                           double* vv, cudaStream_t st);
+cudaError_t launch_gen_coo_backward(const Mesh& m, const Space& sp, GenOp op, const double* grad_vv, double* grad_coef,
+                                    cudaStream_t st);
+// 4 nd^2 entries per Gauss point, DOFs [dof; dof + ndof]
+cudaError_t launch_gen_stiffness_coo(const Mesh& m, const Space& sp, const double* D, long long* indices, double* vv,
+                                     cudaStream_t st);
+cudaError_t launch_gen_stiffness_coo_backward(const Mesh& m, const Space& sp, const double* grad_vv, double* grad_D,
+                                              cudaStream_t st);
+// summed operator values in the space's CSR pattern (transpose: CSC of the same
+// symmetric pattern); ke: scratch of nd*nd doubles per element
+cudaError_t launch_gen_matrix(const Mesh& m, const Space& sp, GenOp op, const double* coef, double* ke, double* vals,
+                              bool transpose, cudaStream_t st);
+// summed elasticity operator in the [x; y] block pattern (rows 2 ndof, 4 nnz entries);
+// ke: scratch of 4 nd^2 doubles per element
+cudaError_t launch_gen_stiffness_matrix(const Mesh& m, const Space& sp, const double* D, double* ke, double* vals,
+                                        bool transpose, cudaStream_t st);
+cudaError_t launch_gen_source(const Mesh& m, const Space& sp, const double* f, double* rhs, bool accumulate,
+                              cudaStream_t st);
+cudaError_t launch_gen_source_backward(const Mesh& m, const Space& sp, const double* grad_rhs, double* grad_f,
+                                       cudaStream_t st);
+// values at the Gauss points of the mesh's rule: through the P1 shape of the vertices
+// (vertex_only, fem_to_gauss_points) or through all DOFs of sp (dof_to_gauss_points)
+cudaError_t launch_gen_to_gauss(const Mesh& m, const Space& sp, bool vertex_only, const double* u, double* out,
+                                cudaStream_t st);
+// transposes of the above: grad_u (+)= ...; vertex_only writes entries [0, nv) only
+cudaError_t launch_gen_to_gauss_backward(const Mesh& m, const Space& sp, bool vertex_only, const double* grad_out,
+                                         double* grad_u, bool accumulate, cudaStream_t st);
 
 // Device bytes held by a resident system (operator copies, Dirichlet data, solver
 // vectors) -- what the serving loop counts against its HBM budget.

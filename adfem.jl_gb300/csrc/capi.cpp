@@ -69,6 +69,12 @@ int kerr(cudaError_t e, const char* what) {
   return ADFEM_OK;
 }
 
+// The space of the given degree on m (built on first use under m.mu).
+int get_space(Mesh& m, int degree, Space** sp) {
+  std::lock_guard<std::mutex> lk(m.mu);
+  return mesh_space(&m, degree, sp);
+}
+
 void legacy_report(int st, const char* fn) {
   if (st != ADFEM_OK) std::fprintf(stderr, "libadfem_gpu: %s failed: %s\n", fn, last_error_cstr());
 }
@@ -161,10 +167,16 @@ int adfem_mesh_create(const double* xyz, long long nv, const int* elems0, long l
                       adfem_mesh** out) {
   if (!out) return fail(ADFEM_ERR_INVALID, "null output handle");
   *out = nullptr;
-  if (degree != 1) return fail(ADFEM_ERR_UNSUPPORTED, "only P1 (degree 1) elements are implemented");
+  if (degree != 1 && degree != 2) return fail(ADFEM_ERR_UNSUPPORTED, "element degree must be 1 (P1) or 2 (P2)");
   Mesh* m = nullptr;
   ADFEM_TRY(mesh_build(xyz, nv, reinterpret_cast<const int32_t*>(elems0), ne, &m));
-  *out = new adfem_mesh{m};
+  std::unique_ptr<Mesh> own(m);
+  m->degree = degree;
+  if (degree == 2) {
+    Space* sp = nullptr;
+    ADFEM_TRY(get_space(*m, 2, &sp));
+  }
+  *out = new adfem_mesh{own.release()};
   return ADFEM_OK;
 }
 
@@ -186,8 +198,37 @@ int adfem_mesh_sizes(const adfem_mesh* mesh, long long* nv, long long* ne, long 
   if (!mesh) return fail(ADFEM_ERR_INVALID, "null mesh");
   if (nv) *nv = mesh->m->nv;
   if (ne) *ne = mesh->m->ne;
-  if (ngauss) *ngauss = 3 * mesh->m->ne;
-  if (nnz) *nnz = mesh->m->nnz;
+  if (ngauss) *ngauss = mesh_ngauss(*mesh->m);
+  if (nnz) *nnz = mesh->m->degree == 2 ? mesh->m->space[2]->nnz : mesh->m->nnz;
+  return ADFEM_OK;
+}
+
+int adfem_mesh_space(const adfem_mesh* mesh, int* degree, int* elem_ndof, int* ngauss_elem, long long* ndof,
+                     long long* nnz) {
+  if (!mesh) return fail(ADFEM_ERR_INVALID, "null mesh");
+  Mesh& m = *mesh->m;
+  Space* sp = nullptr;
+  ADFEM_TRY(get_space(m, m.degree, &sp));
+  if (degree) *degree = m.degree;
+  if (elem_ndof) *elem_ndof = sp->nd;
+  if (ngauss_elem) *ngauss_elem = sp->ng;
+  if (ndof) *ndof = sp->ndof;
+  if (nnz) *nnz = sp->nnz;
+  return ADFEM_OK;
+}
+
+int adfem_mesh_connectivity(const adfem_mesh* mesh, long long* conn1) {
+  if (!mesh || !conn1) return fail(ADFEM_ERR_INVALID, "null argument");
+  Mesh& m = *mesh->m;
+  Space* sp = nullptr;
+  ADFEM_TRY(get_space(m, m.degree, &sp));
+  for (size_t k = 0; k < sp->dof.size(); k++) conn1[k] = (long long)sp->dof[k] + 1;
+  return ADFEM_OK;
+}
+
+int adfem_mesh_gauss_weights(const adfem_mesh* mesh, double* w) {
+  if (!mesh || !w) return fail(ADFEM_ERR_INVALID, "null argument");
+  mesh_gauss_weights(mesh->m, w);
   return ADFEM_OK;
 }
 
@@ -208,23 +249,28 @@ adfem_mesh* adfem_current_mesh(void) {
 
 int adfem_mesh_pattern(const adfem_mesh* mesh, long long* colptr1, long long* rowval1) {
   if (!mesh || !colptr1 || !rowval1) return fail(ADFEM_ERR_INVALID, "null argument");
-  const Mesh& m = *mesh->m;
-  for (int64_t i = 0; i <= m.nv; i++) colptr1[i] = (long long)m.rowptr[i] + 1;
-  for (int64_t k = 0; k < m.nnz; k++) rowval1[k] = (long long)m.colind[k] + 1;
+  Mesh& m = *mesh->m;
+  Space* sp = nullptr;
+  ADFEM_TRY(get_space(m, m.degree, &sp));
+  for (int64_t i = 0; i <= sp->ndof; i++) colptr1[i] = (long long)sp->rowptr[i] + 1;
+  for (int64_t k = 0; k < sp->nnz; k++) rowval1[k] = (long long)sp->colind[k] + 1;
   return ADFEM_OK;
 }
 
 int adfem_mesh_pattern_elasticity(const adfem_mesh* mesh, long long* colptr1, long long* rowval1) {
   if (!mesh || !colptr1 || !rowval1) return fail(ADFEM_ERR_INVALID, "null argument");
-  const Mesh& m = *mesh->m;
+  Mesh& m = *mesh->m;
+  Space* sp = nullptr;
+  ADFEM_TRY(get_space(m, m.degree, &sp));
+  const int64_t n = sp->ndof;
   long long z = 0;
   for (int c = 0; c < 2; c++)
-    for (int64_t i = 0; i < m.nv; i++) {
-      colptr1[c * m.nv + i] = z + 1;
+    for (int64_t i = 0; i < n; i++) {
+      colptr1[c * n + i] = z + 1;
       for (int cc = 0; cc < 2; cc++)
-        for (int32_t k = m.rowptr[i]; k < m.rowptr[i + 1]; k++) rowval1[z++] = (long long)m.colind[k] + cc * m.nv + 1;
+        for (int32_t k = sp->rowptr[i]; k < sp->rowptr[i + 1]; k++) rowval1[z++] = (long long)sp->colind[k] + cc * n + 1;
     }
-  colptr1[2 * m.nv] = z + 1;
+  colptr1[2 * n] = z + 1;
   return ADFEM_OK;
 }
 
@@ -238,6 +284,135 @@ int adfem_mesh_gauss_nodes(const adfem_mesh* mesh, double* x, double* y) {
   if (!mesh || !x || !y) return fail(ADFEM_ERR_INVALID, "null argument");
   mesh_gauss(mesh->m, x, y);
   return ADFEM_OK;
+}
+
+// ------------------------------------------------------------------ generic (P2) ops
+namespace {
+Space* p2_space(Mesh& m) { return m.degree == 2 ? m.space[2].get() : nullptr; }
+
+int gen_matrix_d(Mesh& m, Space& sp, GenOp op, const double* coef_d, double* vals_d, bool transpose,
+                 cudaStream_t st) {
+  std::lock_guard<std::mutex> lk(m.mu);
+  ADFEM_TRY(sp.d_ke.alloc(sizeof(double) * (size_t)sp.nd * sp.nd * m.ne));
+  ADFEM_TRY(kerr(launch_gen_matrix(m, sp, op, coef_d, sp.d_ke.as<double>(), vals_d, transpose, st), "matrix"));
+  ADFEM_CUDA(cudaStreamSynchronize(st));
+  return ADFEM_OK;
+}
+
+int gen_stiffness_d(Mesh& m, Space& sp, const double* D_d, double* vals_d, bool transpose, cudaStream_t st) {
+  std::lock_guard<std::mutex> lk(m.mu);
+  ADFEM_TRY(sp.d_ke.alloc(sizeof(double) * 4 * (size_t)sp.nd * sp.nd * m.ne));
+  ADFEM_TRY(kerr(launch_gen_stiffness_matrix(m, sp, D_d, sp.d_ke.as<double>(), vals_d, transpose, st), "stiffness"));
+  ADFEM_CUDA(cudaStreamSynchronize(st));
+  return ADFEM_OK;
+}
+
+// host-pointer summed operator: per-point input of len values -> nnz_mult * nnz values
+int gen_matrix_host(adfem_mesh* mesh, int which, const double* in, long long nin, double* nzval) {
+  Mesh& m = *mesh->m;
+  Space* sp = nullptr;
+  ADFEM_TRY(get_space(m, m.degree, &sp));
+  const int64_t ng = mesh_ngauss(m);
+  const int64_t want = which == 2 ? 9 * ng : ng;
+  if (nin != want)
+    return fail(ADFEM_ERR_INVALID, which == 2 ? "D must hold a 3x3 matrix per Gauss point"
+                                              : "the coefficient must have one value per Gauss point");
+  const size_t nv = (which == 2 ? 4 : 1) * (size_t)sp->nnz;
+  DevBuf k, v;
+  ADFEM_TRY(to_dev(k, in, (size_t)nin));
+  ADFEM_TRY(v.alloc(sizeof(double) * nv));
+  if (which == 2) ADFEM_TRY(gen_stiffness_d(m, *sp, k.as<double>(), v.as<double>(), true, nullptr));
+  else ADFEM_TRY(gen_matrix_d(m, *sp, which == 0 ? GenOp::LAPLACE : GenOp::MASS, k.as<double>(), v.as<double>(), true,
+                              nullptr));
+  return to_host(nzval, v, nv);
+}
+}  // namespace
+
+int adfem_mass_csr_d(adfem_mesh* mesh, const double* rho_d, double* vals_d, void* stream) {
+  if (!mesh || !rho_d || !vals_d) return fail(ADFEM_ERR_INVALID, "null argument");
+  Mesh& m = *mesh->m;
+  Space* sp = nullptr;
+  ADFEM_TRY(get_space(m, m.degree, &sp));
+  return gen_matrix_d(m, *sp, GenOp::MASS, rho_d, vals_d, false, S(stream));
+}
+
+int adfem_mass_csc(adfem_mesh* mesh, const double* rho, long long nrho, double* nzval) {
+  if (!mesh || !rho || !nzval) return fail(ADFEM_ERR_INVALID, "null argument");
+  return gen_matrix_host(mesh, 1, rho, nrho, nzval);
+}
+
+int adfem_mass_coo_d(adfem_mesh* mesh, const double* rho_d, long long* indices_d, double* vv_d, void* stream) {
+  if (!mesh || !rho_d || !indices_d || !vv_d) return fail(ADFEM_ERR_INVALID, "null argument");
+  Mesh& m = *mesh->m;
+  Space* sp = nullptr;
+  ADFEM_TRY(get_space(m, m.degree, &sp));
+  return kerr(launch_gen_coo(m, *sp, GenOp::MASS, rho_d, indices_d, vv_d, S(stream)), "mass coo");
+}
+
+int adfem_mass_coo_backward_d(adfem_mesh* mesh, const double* grad_vv_d, double* grad_rho_d, void* stream) {
+  if (!mesh || !grad_vv_d || !grad_rho_d) return fail(ADFEM_ERR_INVALID, "null argument");
+  Mesh& m = *mesh->m;
+  Space* sp = nullptr;
+  ADFEM_TRY(get_space(m, m.degree, &sp));
+  return kerr(launch_gen_coo_backward(m, *sp, GenOp::MASS, grad_vv_d, grad_rho_d, S(stream)), "mass coo backward");
+}
+
+static int to_gauss_d(adfem_mesh* mesh, bool vertex_only, const double* u_d, double* out_d, void* stream) {
+  if (!mesh || !u_d || !out_d) return fail(ADFEM_ERR_INVALID, "null argument");
+  Mesh& m = *mesh->m;
+  Space* sp = nullptr;
+  ADFEM_TRY(get_space(m, m.degree, &sp));
+  return kerr(launch_gen_to_gauss(m, *sp, vertex_only, u_d, out_d, S(stream)), "to gauss");
+}
+
+static int to_gauss_backward_d(adfem_mesh* mesh, bool vertex_only, const double* g_d, double* gu_d, long long nu,
+                               int accumulate, void* stream) {
+  if (!mesh || !g_d || !gu_d) return fail(ADFEM_ERR_INVALID, "null argument");
+  Mesh& m = *mesh->m;
+  Space* sp = nullptr;
+  ADFEM_TRY(get_space(m, m.degree, &sp));
+  const int64_t rows = vertex_only ? m.nv : sp->ndof;
+  if (nu < rows) return fail(ADFEM_ERR_INVALID, "grad_u is shorter than the values it interpolates");
+  ADFEM_TRY(kerr(launch_gen_to_gauss_backward(m, *sp, vertex_only, g_d, gu_d, accumulate != 0, S(stream)),
+                 "to gauss backward"));
+  if (!accumulate && nu > rows)
+    ADFEM_CUDA(cudaMemsetAsync(gu_d + rows, 0, sizeof(double) * (size_t)(nu - rows), S(stream)));
+  return ADFEM_OK;
+}
+
+int adfem_fem_to_gauss_d(adfem_mesh* mesh, const double* u_d, double* out_d, void* stream) {
+  return to_gauss_d(mesh, true, u_d, out_d, stream);
+}
+int adfem_fem_to_gauss_backward_d(adfem_mesh* mesh, const double* grad_out_d, double* grad_u_d, long long nu,
+                                  int accumulate, void* stream) {
+  return to_gauss_backward_d(mesh, true, grad_out_d, grad_u_d, nu, accumulate, stream);
+}
+int adfem_dof_to_gauss_d(adfem_mesh* mesh, const double* u_d, double* out_d, void* stream) {
+  return to_gauss_d(mesh, false, u_d, out_d, stream);
+}
+int adfem_dof_to_gauss_backward_d(adfem_mesh* mesh, const double* grad_out_d, double* grad_u_d, long long nu,
+                                  int accumulate, void* stream) {
+  return to_gauss_backward_d(mesh, false, grad_out_d, grad_u_d, nu, accumulate, stream);
+}
+
+static int to_gauss_host(adfem_mesh* mesh, bool vertex_only, const double* u, long long nu, double* out) {
+  if (!mesh || !u || !out) return fail(ADFEM_ERR_INVALID, "null argument");
+  Mesh& m = *mesh->m;
+  Space* sp = nullptr;
+  ADFEM_TRY(get_space(m, m.degree, &sp));
+  if (nu < (vertex_only ? m.nv : sp->ndof)) return fail(ADFEM_ERR_INVALID, "u is shorter than the mesh's values");
+  DevBuf du, dout;
+  ADFEM_TRY(to_dev(du, u, (size_t)nu));
+  ADFEM_TRY(dout.alloc(sizeof(double) * (size_t)mesh_ngauss(m)));
+  ADFEM_TRY(to_gauss_d(mesh, vertex_only, du.as<double>(), dout.as<double>(), nullptr));
+  return to_host(out, dout, (size_t)mesh_ngauss(m));
+}
+
+int adfem_fem_to_gauss(adfem_mesh* mesh, const double* u, long long nu, double* out) {
+  return to_gauss_host(mesh, true, u, nu, out);
+}
+int adfem_dof_to_gauss(adfem_mesh* mesh, const double* u, long long nu, double* out) {
+  return to_gauss_host(mesh, false, u, nu, out);
 }
 
 int adfem_mesh_elements(const adfem_mesh* mesh, long long* elems1) {
@@ -264,6 +439,7 @@ int adfem_mesh_edges(const adfem_mesh* mesh, long long* out, long long* nedges) 
 int adfem_laplace_csr_d(adfem_mesh* mesh, const double* kappa_d, double* vals_d, void* stream) {
   if (!mesh || !kappa_d || !vals_d) return fail(ADFEM_ERR_INVALID, "null argument");
   Mesh& m = *mesh->m;
+  if (Space* sp = p2_space(m)) return gen_matrix_d(m, *sp, GenOp::LAPLACE, kappa_d, vals_d, false, S(stream));
   std::lock_guard<std::mutex> lk(m.mu);
   ADFEM_TRY(m.s_el0.alloc(sizeof(double) * m.ne));
   ADFEM_TRY(kerr(launch_element_prepass(m, kappa_d, nullptr, m.s_el0.as<double>(), nullptr, S(stream)), "prepass"));
@@ -275,6 +451,7 @@ int adfem_laplace_csr_d(adfem_mesh* mesh, const double* kappa_d, double* vals_d,
 int adfem_laplace_csc(adfem_mesh* mesh, const double* kappa, long long nkappa, double* nzval) {
   if (!mesh || !kappa || !nzval) return fail(ADFEM_ERR_INVALID, "null argument");
   Mesh& m = *mesh->m;
+  if (m.degree == 2) return gen_matrix_host(mesh, 0, kappa, nkappa, nzval);
   if (nkappa != 3 * m.ne) return fail(ADFEM_ERR_INVALID, "kappa must have one value per Gauss point (3 per element)");
   DevBuf k, v;
   ADFEM_TRY(to_dev(k, kappa, (size_t)nkappa));
@@ -285,12 +462,17 @@ int adfem_laplace_csc(adfem_mesh* mesh, const double* kappa, long long nkappa, d
 
 int adfem_laplace_coo_d(adfem_mesh* mesh, const double* kappa_d, long long* indices_d, double* vv_d, void* stream) {
   if (!mesh || !kappa_d || !indices_d || !vv_d) return fail(ADFEM_ERR_INVALID, "null argument");
+  if (Space* sp = p2_space(*mesh->m))
+    return kerr(launch_gen_coo(*mesh->m, *sp, GenOp::LAPLACE, kappa_d, indices_d, vv_d, S(stream)), "laplace coo");
   ADFEM_TRY(kerr(launch_laplace_coo(*mesh->m, kappa_d, indices_d, vv_d, S(stream)), "laplace coo"));
   return ADFEM_OK;
 }
 
 int adfem_laplace_coo_backward_d(adfem_mesh* mesh, const double* grad_vv_d, double* grad_kappa_d, void* stream) {
   if (!mesh || !grad_vv_d || !grad_kappa_d) return fail(ADFEM_ERR_INVALID, "null argument");
+  if (Space* sp = p2_space(*mesh->m))
+    return kerr(launch_gen_coo_backward(*mesh->m, *sp, GenOp::LAPLACE, grad_vv_d, grad_kappa_d, S(stream)),
+                "laplace coo backward");
   ADFEM_TRY(kerr(launch_laplace_coo_backward(*mesh->m, grad_vv_d, grad_kappa_d, S(stream)), "laplace coo backward"));
   return ADFEM_OK;
 }
@@ -299,6 +481,11 @@ int adfem_laplace_coo_backward_d(adfem_mesh* mesh, const double* grad_vv_d, doub
 int adfem_source_d(adfem_mesh* mesh, const double* f_d, double* rhs_d, int accumulate, void* stream) {
   if (!mesh || !f_d || !rhs_d) return fail(ADFEM_ERR_INVALID, "null argument");
   Mesh& m = *mesh->m;
+  if (Space* sp = p2_space(m)) {
+    ADFEM_TRY(kerr(launch_gen_source(m, *sp, f_d, rhs_d, accumulate != 0, S(stream)), "source"));
+    ADFEM_CUDA(cudaStreamSynchronize(S(stream)));
+    return ADFEM_OK;
+  }
   std::lock_guard<std::mutex> lk(m.mu);
   ADFEM_TRY(m.s_el1.alloc(sizeof(double) * 3 * m.ne));
   ADFEM_TRY(kerr(launch_element_prepass(m, nullptr, f_d, nullptr, m.s_el1.as<double>(), S(stream)), "prepass"));
@@ -310,17 +497,20 @@ int adfem_source_d(adfem_mesh* mesh, const double* f_d, double* rhs_d, int accum
 int adfem_source(adfem_mesh* mesh, const double* f, long long nf, double* rhs, int accumulate) {
   if (!mesh || !f || !rhs) return fail(ADFEM_ERR_INVALID, "null argument");
   Mesh& m = *mesh->m;
-  if (nf != 3 * m.ne) return fail(ADFEM_ERR_INVALID, "f must have one value per Gauss point (3 per element)");
+  if (nf != mesh_ngauss(m)) return fail(ADFEM_ERR_INVALID, "f must have one value per Gauss point");
+  const size_t n = (size_t)mesh_ndof(&m);
   DevBuf fd, r;
   ADFEM_TRY(to_dev(fd, f, (size_t)nf));
-  if (accumulate) ADFEM_TRY(to_dev(r, rhs, (size_t)m.nv));
-  else ADFEM_TRY(r.alloc(sizeof(double) * m.nv));
+  if (accumulate) ADFEM_TRY(to_dev(r, rhs, n));
+  else ADFEM_TRY(r.alloc(sizeof(double) * n));
   ADFEM_TRY(adfem_source_d(mesh, fd.as<double>(), r.as<double>(), accumulate, nullptr));
-  return to_host(rhs, r, (size_t)m.nv);
+  return to_host(rhs, r, n);
 }
 
 int adfem_source_backward_d(adfem_mesh* mesh, const double* grad_rhs_d, double* grad_f_d, void* stream) {
   if (!mesh || !grad_rhs_d || !grad_f_d) return fail(ADFEM_ERR_INVALID, "null argument");
+  if (Space* sp = p2_space(*mesh->m))
+    return kerr(launch_gen_source_backward(*mesh->m, *sp, grad_rhs_d, grad_f_d, S(stream)), "source backward");
   ADFEM_TRY(kerr(launch_source_backward(*mesh->m, grad_rhs_d, grad_f_d, S(stream)), "source backward"));
   return ADFEM_OK;
 }
@@ -329,6 +519,7 @@ int adfem_source_backward_d(adfem_mesh* mesh, const double* grad_rhs_d, double* 
 int adfem_stiffness_csr_d(adfem_mesh* mesh, const double* D_d, double* vals_d, void* stream) {
   if (!mesh || !D_d || !vals_d) return fail(ADFEM_ERR_INVALID, "null argument");
   Mesh& m = *mesh->m;
+  if (Space* sp = p2_space(m)) return gen_stiffness_d(m, *sp, D_d, vals_d, false, S(stream));
   std::lock_guard<std::mutex> lk(m.mu);
   ADFEM_TRY(m.s_el0.alloc(sizeof(double) * 9 * m.ne));
   ADFEM_TRY(kerr(launch_stiffness_prepass(m, D_d, m.s_el0.as<double>(), S(stream)), "stiffness prepass"));
@@ -340,6 +531,7 @@ int adfem_stiffness_csr_d(adfem_mesh* mesh, const double* D_d, double* vals_d, v
 int adfem_stiffness_csc(adfem_mesh* mesh, const double* D, long long nD, double* nzval) {
   if (!mesh || !D || !nzval) return fail(ADFEM_ERR_INVALID, "null argument");
   Mesh& m = *mesh->m;
+  if (m.degree == 2) return gen_matrix_host(mesh, 2, D, nD, nzval);
   if (nD != 27 * m.ne) return fail(ADFEM_ERR_INVALID, "D must hold a 3x3 matrix per Gauss point (27 per element)");
   DevBuf dd, v;
   ADFEM_TRY(to_dev(dd, D, (size_t)nD));
@@ -355,12 +547,17 @@ int adfem_stiffness_csc(adfem_mesh* mesh, const double* D, long long nD, double*
 
 int adfem_stiffness_coo_d(adfem_mesh* mesh, const double* D_d, long long* indices_d, double* vv_d, void* stream) {
   if (!mesh || !D_d || !indices_d || !vv_d) return fail(ADFEM_ERR_INVALID, "null argument");
+  if (Space* sp = p2_space(*mesh->m))
+    return kerr(launch_gen_stiffness_coo(*mesh->m, *sp, D_d, indices_d, vv_d, S(stream)), "stiffness coo");
   ADFEM_TRY(kerr(launch_stiffness_coo(*mesh->m, D_d, indices_d, vv_d, S(stream)), "stiffness coo"));
   return ADFEM_OK;
 }
 
 int adfem_stiffness_coo_backward_d(adfem_mesh* mesh, const double* grad_vv_d, double* grad_D_d, void* stream) {
   if (!mesh || !grad_vv_d || !grad_D_d) return fail(ADFEM_ERR_INVALID, "null argument");
+  if (Space* sp = p2_space(*mesh->m))
+    return kerr(launch_gen_stiffness_coo_backward(*mesh->m, *sp, grad_vv_d, grad_D_d, S(stream)),
+                "stiffness coo backward");
   ADFEM_TRY(kerr(launch_stiffness_coo_backward(*mesh->m, grad_vv_d, grad_D_d, S(stream)), "stiffness coo backward"));
   return ADFEM_OK;
 }
@@ -614,6 +811,9 @@ int adfem_system_create(adfem_mesh* mesh, int kind, adfem_system** out) {
   if (!mesh || !out) return fail(ADFEM_ERR_INVALID, "null argument");
   if (kind != ADFEM_SYS_POISSON && kind != ADFEM_SYS_ELASTICITY) return fail(ADFEM_ERR_INVALID, "unknown kind");
   *out = nullptr;
+  if (mesh->m->degree != 1)
+    return fail(ADFEM_ERR_UNSUPPORTED, "resident systems are built on P1 meshes (assemble P2 operators and use "
+                                       "adfem_csc_solve)");
   std::unique_ptr<adfem_system> s(new adfem_system());
   s->mesh = mesh;
   s->kind = kind;
@@ -868,13 +1068,14 @@ int adfem_poisson_solve(adfem_system* sys, const double* kappa, const double* f,
 long long* init_nnfem_mesh(double* vertices, int num_vertices, int* element_indices, int num_elements, int order,
                            int lorder, int degree, long long* nedges) {
   (void)lorder;
-  if (degree != 1 || (order != 2 && order != -1)) {
-    fail(ADFEM_ERR_UNSUPPORTED, "only P1 elements with the order-2 triangle rule are implemented");
+  const bool ok = (degree == 1 && (order == 2 || order == -1)) || (degree == 2 && (order == 4 || order == -1));
+  if (!ok) {
+    fail(ADFEM_ERR_UNSUPPORTED, "implemented: P1 elements with the order-2 triangle rule, P2 with the order-4 rule");
     legacy_report(ADFEM_ERR_UNSUPPORTED, "init_nnfem_mesh");
     return nullptr;
   }
   adfem_mesh* h = nullptr;
-  int st = adfem_mesh_create(vertices, num_vertices, element_indices, num_elements, 1, &h);
+  int st = adfem_mesh_create(vertices, num_vertices, element_indices, num_elements, degree, &h);
   if (st != ADFEM_OK) {
     legacy_report(st, "init_nnfem_mesh");
     return nullptr;
@@ -908,7 +1109,7 @@ long long* init_nnfem_mesh(double* vertices, int num_vertices, int* element_indi
 
 int mfem_get_ngauss(void) {
   LEGACY_MESH("mfem_get_ngauss", 0);
-  return (int)(3 * m->ne);
+  return (int)mesh_ngauss(*m);
 }
 void mfem_get_gauss(double* x, double* y) {
   LEGACY_MESH("mfem_get_gauss", );
@@ -916,8 +1117,7 @@ void mfem_get_gauss(double* x, double* y) {
 }
 void mfem_get_gauss_weights(double* w) {
   LEGACY_MESH("mfem_get_gauss_weights", );
-  for (int64_t e = 0; e < m->ne; e++)
-    for (int k = 0; k < 3; k++) w[3 * e + k] = (1.0 / 6.0) * m->area[e] / 0.5;
+  mesh_gauss_weights(m, w);
 }
 void mfem_get_area(double* a) {
   LEGACY_MESH("mfem_get_area", );
@@ -925,15 +1125,16 @@ void mfem_get_area(double* a) {
 }
 int mfem_get_elem_ndof(void) {
   LEGACY_MESH("mfem_get_elem_ndof", 0);
-  return 3;
+  return m->degree == 2 ? 6 : 3;
 }
 int mfem_get_ndof(void) {
   LEGACY_MESH("mfem_get_ndof", 0);
-  return (int)m->nv;
+  return (int)mesh_ndof(m);
 }
 void mfem_get_connectivity(long long* conn) {
   LEGACY_MESH("mfem_get_connectivity", );
-  for (int64_t e = 0; e < 3 * m->ne; e++) conn[e] = (long long)m->elem[e] + 1;
+  adfem_mesh h{m};
+  legacy_report(adfem_mesh_connectivity(&h, conn), "mfem_get_connectivity");
 }
 void mfem_get_element_to_vertices(long long* elems) {
   LEGACY_MESH("mfem_get_element_to_vertices", );
@@ -941,13 +1142,17 @@ void mfem_get_element_to_vertices(long long* elems) {
     for (int k = 0; k < 3; k++) elems[k * m->ne + e] = (long long)m->elem[3 * e + k] + 1;
 }
 
+// DOFs per element of the current mesh
+static size_t elem_nd(const Mesh* m) { return m->degree == 2 ? 6 : 3; }
+
 static int legacy_laplace_coo(Mesh* m, long long* indices, double* vv, const double* kappa) {
-  const size_t ng = 3 * (size_t)m->ne, N = 9 * ng;
+  const size_t ng = (size_t)mesh_ngauss(*m), N = elem_nd(m) * elem_nd(m) * ng;
   DevBuf k, idx, v;
   ADFEM_TRY(to_dev(k, kappa, ng));
   ADFEM_TRY(idx.alloc(sizeof(long long) * 2 * N));
   ADFEM_TRY(v.alloc(sizeof(double) * N));
-  ADFEM_TRY(kerr(launch_laplace_coo(*m, k.as<double>(), idx.as<long long>(), v.as<double>(), nullptr), "laplace coo"));
+  adfem_mesh h{m};
+  ADFEM_TRY(adfem_laplace_coo_d(&h, k.as<double>(), idx.as<long long>(), v.as<double>(), nullptr));
   ADFEM_TRY(to_host(indices, idx, 2 * N));
   return to_host(vv, v, N);
 }
@@ -960,17 +1165,17 @@ void FemLaplaceScalar_forward_Julia(long long* indices, double* vv, const double
 void FemSourceScalar_forward_Julia(double* rhs, const double* f) {
   LEGACY_MESH("FemSourceScalar_forward_Julia", );
   adfem_mesh h{m};
-  legacy_report(adfem_source(&h, f, 3 * m->ne, rhs, 1), "FemSourceScalar_forward_Julia");
+  legacy_report(adfem_source(&h, f, mesh_ngauss(*m), rhs, 1), "FemSourceScalar_forward_Julia");
 }
 
 static int legacy_stiffness_coo(Mesh* m, long long* indices, double* vv, const double* hmat) {
-  const size_t ng = 3 * (size_t)m->ne, N = 36 * ng;
+  const size_t ng = (size_t)mesh_ngauss(*m), N = 4 * elem_nd(m) * elem_nd(m) * ng;
   DevBuf d, idx, v;
   ADFEM_TRY(to_dev(d, hmat, 9 * ng));
   ADFEM_TRY(idx.alloc(sizeof(long long) * 2 * N));
   ADFEM_TRY(v.alloc(sizeof(double) * N));
-  ADFEM_TRY(kerr(launch_stiffness_coo(*m, d.as<double>(), idx.as<long long>(), v.as<double>(), nullptr),
-                 "stiffness coo"));
+  adfem_mesh h{m};
+  ADFEM_TRY(adfem_stiffness_coo_d(&h, d.as<double>(), idx.as<long long>(), v.as<double>(), nullptr));
   ADFEM_TRY(to_host(indices, idx, 2 * N));
   return to_host(vv, v, N);
 }
@@ -981,11 +1186,12 @@ void ComputeFemStiffnessMatrixMfem_forward_Julia(long long* indices, double* vv,
 }
 
 static int legacy_laplace_backward(Mesh* m, double* grad_kappa, const double* grad_vv) {
-  const size_t ng = 3 * (size_t)m->ne;
+  const size_t ng = (size_t)mesh_ngauss(*m);
   DevBuf g, o;
-  ADFEM_TRY(to_dev(g, grad_vv, 9 * ng));
+  ADFEM_TRY(to_dev(g, grad_vv, elem_nd(m) * elem_nd(m) * ng));
   ADFEM_TRY(o.alloc(sizeof(double) * ng));
-  ADFEM_TRY(kerr(launch_laplace_coo_backward(*m, g.as<double>(), o.as<double>(), nullptr), "laplace backward"));
+  adfem_mesh h{m};
+  ADFEM_TRY(adfem_laplace_coo_backward_d(&h, g.as<double>(), o.as<double>(), nullptr));
   return to_host(grad_kappa, o, ng);
 }
 
@@ -999,11 +1205,12 @@ void FemLaplaceScalar_backward(double* grad_kappa, const double* grad_vv, const 
 }
 
 static int legacy_source_backward(Mesh* m, double* grad_f, const double* grad_rhs) {
-  const size_t ng = 3 * (size_t)m->ne;
+  const size_t ng = (size_t)mesh_ngauss(*m);
   DevBuf g, o;
-  ADFEM_TRY(to_dev(g, grad_rhs, (size_t)m->nv));
+  ADFEM_TRY(to_dev(g, grad_rhs, (size_t)mesh_ndof(m)));
   ADFEM_TRY(o.alloc(sizeof(double) * ng));
-  ADFEM_TRY(kerr(launch_source_backward(*m, g.as<double>(), o.as<double>(), nullptr), "source backward"));
+  adfem_mesh h{m};
+  ADFEM_TRY(adfem_source_backward_d(&h, g.as<double>(), o.as<double>(), nullptr));
   return to_host(grad_f, o, ng);
 }
 
@@ -1015,17 +1222,105 @@ void FemSourceScalar_backward(double* grad_f, const double* grad_rhs, const doub
 }
 
 static int legacy_stiffness_backward(Mesh* m, double* grad_hmat, const double* grad_vv) {
-  const size_t ng = 3 * (size_t)m->ne;
+  const size_t ng = (size_t)mesh_ngauss(*m);
   DevBuf g, o;
-  ADFEM_TRY(to_dev(g, grad_vv, 36 * ng));
+  ADFEM_TRY(to_dev(g, grad_vv, 4 * elem_nd(m) * elem_nd(m) * ng));
   ADFEM_TRY(o.alloc(sizeof(double) * 9 * ng));
-  ADFEM_TRY(kerr(launch_stiffness_coo_backward(*m, g.as<double>(), o.as<double>(), nullptr), "stiffness backward"));
+  adfem_mesh h{m};
+  ADFEM_TRY(adfem_stiffness_coo_backward_d(&h, g.as<double>(), o.as<double>(), nullptr));
   return to_host(grad_hmat, o, 9 * ng);
 }
 
 void ComputeFemStiffnessMatrixMfem_backward(double* grad_hmat, const double* grad_vv) {
   LEGACY_MESH("ComputeFemStiffnessMatrixMfem_backward", );
   legacy_report(legacy_stiffness_backward(m, grad_hmat, grad_vv), "ComputeFemStiffnessMatrixMfem_backward");
+}
+
+// ComputeFemMassMatrix1 (deps/MFEM/ComputeFemMassMatrix1/ComputeFemMassMatrixMfem.h:4-55)
+static int legacy_mass_coo(Mesh* m, long long* indices, double* vv, const double* rho) {
+  const size_t ng = (size_t)mesh_ngauss(*m), N = elem_nd(m) * elem_nd(m) * ng;
+  DevBuf k, idx, v;
+  ADFEM_TRY(to_dev(k, rho, ng));
+  ADFEM_TRY(idx.alloc(sizeof(long long) * 2 * N));
+  ADFEM_TRY(v.alloc(sizeof(double) * N));
+  adfem_mesh h{m};
+  ADFEM_TRY(adfem_mass_coo_d(&h, k.as<double>(), idx.as<long long>(), v.as<double>(), nullptr));
+  ADFEM_TRY(to_host(indices, idx, 2 * N));
+  return to_host(vv, v, N);
+}
+
+void ComputeFemMassMatrix1_forward(long long* indices, double* vv, const double* rho) {
+  LEGACY_MESH("ComputeFemMassMatrix1_forward", );
+  legacy_report(legacy_mass_coo(m, indices, vv, rho), "ComputeFemMassMatrix1_forward");
+}
+
+static int legacy_mass_backward(Mesh* m, double* grad_rho, const double* grad_vv) {
+  const size_t ng = (size_t)mesh_ngauss(*m);
+  DevBuf g, o;
+  ADFEM_TRY(to_dev(g, grad_vv, elem_nd(m) * elem_nd(m) * ng));
+  ADFEM_TRY(o.alloc(sizeof(double) * ng));
+  adfem_mesh h{m};
+  ADFEM_TRY(adfem_mass_coo_backward_d(&h, g.as<double>(), o.as<double>(), nullptr));
+  return to_host(grad_rho, o, ng);
+}
+
+void ComputeFemMassMatrix1_backward(double* grad_rho, const double* grad_vv, const double* vv, const double* rho) {
+  (void)vv;
+  (void)rho;
+  LEGACY_MESH("ComputeFemMassMatrix1_backward", );
+  legacy_report(legacy_mass_backward(m, grad_rho, grad_vv), "ComputeFemMassMatrix1_backward");
+}
+
+// FemToGaussPoints / DofToGaussPoints (host pointers, current mesh).  The forward
+// functions read nv (vertex values) or ndof values of u; the backward functions add
+// into grad_u like the reference loops (the TF ops zero grad_u first).
+static int legacy_to_gauss(Mesh* m, bool vertex_only, double* out, const double* u) {
+  adfem_mesh h{m};
+  Space* sp = nullptr;
+  ADFEM_TRY(get_space(*m, m->degree, &sp));
+  return to_gauss_host(&h, vertex_only, u, vertex_only ? m->nv : sp->ndof, out);
+}
+
+static int legacy_to_gauss_backward(Mesh* m, bool vertex_only, double* grad_u, const double* grad_out) {
+  adfem_mesh h{m};
+  Space* sp = nullptr;
+  ADFEM_TRY(get_space(*m, m->degree, &sp));
+  const size_t n = vertex_only ? (size_t)m->nv : (size_t)sp->ndof, ng = (size_t)mesh_ngauss(*m);
+  DevBuf g, gu;
+  ADFEM_TRY(to_dev(g, grad_out, ng));
+  ADFEM_TRY(to_dev(gu, grad_u, n));
+  ADFEM_TRY(to_gauss_backward_d(&h, vertex_only, g.as<double>(), gu.as<double>(), (long long)n, 1, nullptr));
+  ADFEM_CUDA(cudaStreamSynchronize(nullptr));
+  return to_host(grad_u, gu, n);
+}
+
+void FemToGaussPointsMfem_Julia(double* out, const double* u) {
+  LEGACY_MESH("FemToGaussPointsMfem_Julia", );
+  legacy_report(legacy_to_gauss(m, true, out, u), "FemToGaussPointsMfem_Julia");
+}
+void FemToGaussPointsMfem_forward(double* out, const double* u) {
+  LEGACY_MESH("FemToGaussPointsMfem_forward", );
+  legacy_report(legacy_to_gauss(m, true, out, u), "FemToGaussPointsMfem_forward");
+}
+void FemToGaussPointsMfem_backward(double* grad_u, const double* grad_out, const double* out, const double* u) {
+  (void)out;
+  (void)u;
+  LEGACY_MESH("FemToGaussPointsMfem_backward", );
+  legacy_report(legacy_to_gauss_backward(m, true, grad_u, grad_out), "FemToGaussPointsMfem_backward");
+}
+void DofToGaussPointsMfem_forward_Julia(double* out, const double* u) {
+  LEGACY_MESH("DofToGaussPointsMfem_forward_Julia", );
+  legacy_report(legacy_to_gauss(m, false, out, u), "DofToGaussPointsMfem_forward_Julia");
+}
+void DofToGaussPointsMfem_forward(double* out, const double* u) {
+  LEGACY_MESH("DofToGaussPointsMfem_forward", );
+  legacy_report(legacy_to_gauss(m, false, out, u), "DofToGaussPointsMfem_forward");
+}
+void DofToGaussPointsMfem_backward(double* grad_u, const double* grad_out, const double* out, const double* u) {
+  (void)out;
+  (void)u;
+  LEGACY_MESH("DofToGaussPointsMfem_backward", );
+  legacy_report(legacy_to_gauss_backward(m, false, grad_u, grad_out), "DofToGaussPointsMfem_backward");
 }
 
 static int host_plane(int mode, const double* E, const double* nu, int N, double* out) {

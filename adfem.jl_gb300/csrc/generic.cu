@@ -1,0 +1,715 @@
+// Degree-generic element kernels for P1 and P2 Lagrange triangles: the reference's
+// element loops written over elem_ndof and the per-point tables h, hx, hy, w
+// (deps/MFEM/Common.cpp:46-126), for
+//   FemLaplaceScalar forward/backward   deps/MFEM/FemLaplace1/FemLaplaceScalar.h:3-54
+//   ComputeFemMassMatrix1 fwd/bwd       deps/MFEM/ComputeFemMassMatrix1/ComputeFemMassMatrixMfem.h:4-55
+//   FemSourceScalar forward/backward    deps/MFEM/FemSource1/FemSourceScalar.h:4-32
+//   ComputeFemStiffnessMatrixMfem       deps/MFEM/ComputeFemStiffnessMatrixMfem/ComputeFemStiffnessMatrixMfem.h:4-81
+//   FemToGaussPoints / DofToGaussPoints deps/MFEM/FemToGaussPoints/FemToGaussPointsMfem.h:5-34,
+//                                       deps/MFEM/DofToGaussPoints/DofToGaussPointsMfem.h:5-35
+// and the summed (SparseMatrixCSC) operators of the Laplace, mass and elasticity
+// matrices.  The P1 Laplace/source/stiffness path of P1 meshes has its own fused
+// kernels (assemble.cu, elastic.cu); these serve P2 meshes and the mass and
+// interpolation ops of both degrees.
+//
+// Layout: one thread per (Gauss point, local row) for the unsummed COO outputs, so a
+// warp writes one contiguous stretch of entries; one thread per DOF row for every
+// scatter (load vector, summed operators, interpolation transposes), walking the
+// DOF->element incidence in ascending element order, so results are deterministic
+// and no atomics are needed.  The per-point basis tables of the degree are built in
+// shared memory by every block from the rule (a few hundred flops).
+#include "adfem_internal.h"
+#include "cg_common.cuh"
+
+namespace adfem {
+namespace {
+
+constexpr int kGT = 256;
+
+// rule points (xi, eta, weight) on the reference triangle: order 2 (3 points, P1) and
+// order 4 (6 points, P2: the published Strang-Fix/Dunavant rule); same constants as
+// the host tables of mesh.cpp
+__constant__ double c_rule[2][6][3] = {
+    {{1.0 / 6.0, 1.0 / 6.0, 1.0 / 6.0},
+     {1.0 / 6.0, 2.0 / 3.0, 1.0 / 6.0},
+     {2.0 / 3.0, 1.0 / 6.0, 1.0 / 6.0},
+     {0.0, 0.0, 0.0},
+     {0.0, 0.0, 0.0},
+     {0.0, 0.0, 0.0}},
+    {{0.091576213509770743460, 0.091576213509770743460, 0.054975871827660933819},
+     {0.091576213509770743460, 0.81684757298045851308, 0.054975871827660933819},
+     {0.81684757298045851308, 0.091576213509770743460, 0.054975871827660933819},
+     {0.44594849091596488632, 0.44594849091596488632, 0.11169079483900573285},
+     {0.44594849091596488632, 0.10810301816807022736, 0.11169079483900573285},
+     {0.10810301816807022736, 0.44594849091596488632, 0.11169079483900573285}}};
+
+template <int DEG>
+struct Tab {
+  static constexpr int ND = DEG == 2 ? 6 : 3;  // DOFs per element
+  static constexpr int NG = DEG == 2 ? 6 : 3;  // Gauss points per element
+  double h[NG][ND];     // phi_r at point k
+  double t[NG][ND][3];  // d phi_r / d l_c at point k
+  double l[NG][3];      // barycentric coordinates of point k
+  double w[NG];         // rule weight of point k
+};
+
+// Lagrange basis in barycentric coordinates.  P1: phi_r = l_r.  P2 (nodes at the
+// vertices and edge midpoints, vertex functions first, then edges (0,1), (1,2),
+// (2,0)): phi_a = l_a (2 l_a - 1), phi_ab = 4 l_a l_b.
+template <int DEG>
+__device__ void tab_init(Tab<DEG>& T) {
+  constexpr int ND = Tab<DEG>::ND, NG = Tab<DEG>::NG;
+  for (int k = threadIdx.x; k < NG; k += blockDim.x) {
+    const double xi = c_rule[DEG - 1][k][0], eta = c_rule[DEG - 1][k][1];
+    const double l[3] = {1.0 - xi - eta, xi, eta};
+    T.w[k] = c_rule[DEG - 1][k][2];
+    for (int c = 0; c < 3; c++) T.l[k][c] = l[c];
+    for (int r = 0; r < ND; r++) T.t[k][r][0] = T.t[k][r][1] = T.t[k][r][2] = 0.0;
+    if (DEG == 1) {
+      for (int r = 0; r < 3; r++) {
+        T.h[k][r] = l[r];
+        T.t[k][r][r] = 1.0;
+      }
+    } else {
+      for (int a = 0; a < 3; a++) {
+        T.h[k][a] = l[a] * (2.0 * l[a] - 1.0);
+        T.t[k][a][a] = 4.0 * l[a] - 1.0;
+      }
+      for (int j = 0; j < 3; j++) {
+        const int a = j, b = (j + 1) % 3;
+        T.h[k][3 + j] = 4.0 * l[a] * l[b];
+        T.t[k][3 + j][a] = 4.0 * l[b];
+        T.t[k][3 + j][b] = 4.0 * l[a];
+      }
+    }
+  }
+  __syncthreads();
+}
+
+// physical gradient of basis r at point k: sum_c (d phi_r / d l_c) grad l_c
+template <int DEG>
+__device__ __forceinline__ void grad_at(const Tab<DEG>& T, int k, int r, const double2 (&g)[3], double& hx,
+                                        double& hy) {
+  const double t0 = T.t[k][r][0], t1 = T.t[k][r][1], t2 = T.t[k][r][2];
+  hx = t0 * g[0].x + t1 * g[1].x + t2 * g[2].x;
+  hy = t0 * g[0].y + t1 * g[1].y + t2 * g[2].y;
+}
+
+__device__ __forceinline__ void load_grad(const double2* __restrict__ grad, int64_t e, double2 (&g)[3]) {
+  g[0] = grad[3 * e];
+  g[1] = grad[3 * e + 1];
+  g[2] = grad[3 * e + 2];
+}
+
+// w_k = ip.weight * area / 0.5 (Common.cpp:116)
+template <int DEG>
+__device__ __forceinline__ double weight_at(const Tab<DEG>& T, int k, double area) {
+  return T.w[k] * area / 0.5;
+}
+
+int grid_for(int64_t n, int bt = kGT) {
+  int64_t b = (n + bt - 1) / bt;
+  return (int)std::max<int64_t>(1, std::min<int64_t>(b, 152 * 32));
+}
+
+// ---------------------------------------------------------------- unsummed COO
+template <int DEG, int OP>
+__global__ void __launch_bounds__(kGT) k_gen_coo(int64_t ne, const int32_t* __restrict__ dof,
+                                                 const double* __restrict__ area, const double2* __restrict__ grad,
+                                                 const double* __restrict__ coef, long long* __restrict__ idx,
+                                                 double* __restrict__ vv) {
+  constexpr int ND = Tab<DEG>::ND, NG = Tab<DEG>::NG;
+  __shared__ Tab<DEG> T;
+  tab_init(T);
+  const int64_t n = ne * NG * ND;
+  for (int64_t t = gtid(); t < n; t += gstride()) {
+    const int64_t gp = t / ND;
+    const int p = (int)(t - gp * ND);
+    const int64_t e = gp / NG;
+    const int k = (int)(gp - e * NG);
+    const double w = weight_at(T, k, area[e]);
+    const double c = coef[gp];
+    int32_t d[ND];
+#pragma unroll
+    for (int q = 0; q < ND; q++) d[q] = dof[ND * e + q];
+    const int32_t dp = dof[ND * e + p];
+    double2 g[3];
+    double px = 0.0, py = 0.0;
+    if (OP == (int)GenOp::LAPLACE) {
+      load_grad(grad, e, g);
+      grad_at(T, k, p, g, px, py);
+    }
+    const int64_t base = t * ND;
+#pragma unroll
+    for (int q = 0; q < ND; q++) {
+      double v;
+      if (OP == (int)GenOp::LAPLACE) {
+        double qx, qy;
+        grad_at(T, k, q, g, qx, qy);
+        v = (px * qx + py * qy) * c * w;
+      } else {
+        v = T.h[k][p] * T.h[k][q] * c * w;
+      }
+      reinterpret_cast<longlong2*>(idx)[base + q] = make_longlong2(dp, d[q]);
+      vv[base + q] = v;
+    }
+  }
+}
+
+// grad_coef[gp] = sum_pq grad_vv[gp, p, q] * (d N_pq / d coef): threads (gp, p) form
+// the row sums, the gp's first thread adds the rows in order
+template <int DEG, int OP>
+__global__ void __launch_bounds__(64 * Tab<DEG>::ND) k_gen_coo_backward(int64_t ne, const double* __restrict__ area,
+                                                                      const double2* __restrict__ grad,
+                                                                      const double* __restrict__ gv,
+                                                                      double* __restrict__ out) {
+  constexpr int ND = Tab<DEG>::ND, NG = Tab<DEG>::NG;
+  __shared__ Tab<DEG> T;
+  __shared__ double part[64 * ND];
+  tab_init(T);
+  const int64_t ngp = ne * NG;
+  const int64_t gp = (int64_t)blockIdx.x * 64 + threadIdx.x / ND;
+  const int p = threadIdx.x % ND;
+  double s = 0.0;
+  if (gp < ngp) {
+    const int64_t e = gp / NG;
+    const int k = (int)(gp - e * NG);
+    const double w = weight_at(T, k, area[e]);
+    const double* row = gv + (gp * ND + p) * ND;
+    if (OP == (int)GenOp::LAPLACE) {
+      double2 g[3];
+      load_grad(grad, e, g);
+      double px, py;
+      grad_at(T, k, p, g, px, py);
+#pragma unroll
+      for (int q = 0; q < ND; q++) {
+        double qx, qy;
+        grad_at(T, k, q, g, qx, qy);
+        s += row[q] * ((px * qx + py * qy) * w);
+      }
+    } else {
+#pragma unroll
+      for (int q = 0; q < ND; q++) s += T.h[k][p] * T.h[k][q] * w * row[q];
+    }
+  }
+  part[threadIdx.x] = s;
+  __syncthreads();
+  if (p == 0 && gp < ngp) {
+    double v = 0.0;
+#pragma unroll
+    for (int r = 0; r < ND; r++) v += part[threadIdx.x + r];
+    out[gp] = v;
+  }
+}
+
+// B = [hx 0; 0 hy; hy hx] (3 x 2 nd), ComputeFemStiffnessMatrixMfem.h:18-23: column l
+template <int ND>
+__device__ __forceinline__ void bcol(const double (&hx)[ND], const double (&hy)[ND], int l, double& b0, double& b1,
+                                     double& b2) {
+  if (l < ND) {
+    b0 = hx[l];
+    b1 = 0.0;
+    b2 = hy[l];
+  } else {
+    b0 = 0.0;
+    b1 = hy[l - ND];
+    b2 = hx[l - ND];
+  }
+}
+
+// elasticity COO: thread (gp, l) writes row l of B^T K B w (2 nd entries)
+template <int DEG>
+__global__ void __launch_bounds__(kGT) k_gen_stiffness_coo(int64_t ne, int64_t ndof, const int32_t* __restrict__ dof,
+                                                           const double* __restrict__ area,
+                                                           const double2* __restrict__ grad,
+                                                           const double* __restrict__ D, long long* __restrict__ idx,
+                                                           double* __restrict__ vv) {
+  constexpr int ND = Tab<DEG>::ND, NG = Tab<DEG>::NG, N2 = 2 * ND;
+  __shared__ Tab<DEG> T;
+  tab_init(T);
+  const int64_t n = ne * NG * N2;
+  for (int64_t t = gtid(); t < n; t += gstride()) {
+    const int64_t gp = t / N2;
+    const int l = (int)(t - gp * N2);
+    const int64_t e = gp / NG;
+    const int k = (int)(gp - e * NG);
+    const double w = weight_at(T, k, area[e]);
+    double2 g[3];
+    load_grad(grad, e, g);
+    double hx[ND], hy[ND];
+#pragma unroll
+    for (int r = 0; r < ND; r++) grad_at(T, k, r, g, hx[r], hy[r]);
+    const double* K = D + 9 * gp;
+    double b0, b1, b2;
+    bcol<ND>(hx, hy, l, b0, b1, b2);
+    double tq[3];
+#pragma unroll
+    for (int q = 0; q < 3; q++) tq[q] = b0 * K[q] + b1 * K[3 + q] + b2 * K[6 + q];
+    const long long dl = (long long)dof[ND * e + (l % ND)] + (l >= ND ? ndof : 0);
+    const int64_t base = t * N2;
+#pragma unroll
+    for (int c = 0; c < N2; c++) {
+      double c0, c1, c2;
+      bcol<ND>(hx, hy, c, c0, c1, c2);
+      const long long dc = (long long)dof[ND * e + (c % ND)] + (c >= ND ? ndof : 0);
+      reinterpret_cast<longlong2*>(idx)[base + c] = make_longlong2(dl, dc);
+      vv[base + c] = (tq[0] * c0 + tq[1] * c1 + tq[2] * c2) * w;
+    }
+  }
+}
+
+// grad_D[gp] = w B G B^T: thread (gp, l) reads row l of G and contributes
+// B[:, l] (G[l, :] B^T); the gp's threads then add the 2 nd rows, in order, for each of the nine entries
+template <int DEG>
+__global__ void __launch_bounds__(32 * 2 * Tab<DEG>::ND) k_gen_stiffness_coo_backward(
+    int64_t ne, const double* __restrict__ area, const double2* __restrict__ grad, const double* __restrict__ gv,
+    double* __restrict__ out) {
+  constexpr int ND = Tab<DEG>::ND, NG = Tab<DEG>::NG, N2 = 2 * ND;
+  __shared__ Tab<DEG> T;
+  __shared__ double part[32 * N2][9];
+  tab_init(T);
+  const int64_t ngp = ne * NG;
+  const int slot = threadIdx.x / N2;
+  const int64_t gp = (int64_t)blockIdx.x * 32 + slot;
+  const int l = threadIdx.x % N2;
+  double acc[9];
+#pragma unroll
+  for (int j = 0; j < 9; j++) acc[j] = 0.0;
+  double w = 0.0;
+  if (gp < ngp) {
+    const int64_t e = gp / NG;
+    const int k = (int)(gp - e * NG);
+    w = weight_at(T, k, area[e]);
+    double2 g[3];
+    load_grad(grad, e, g);
+    double hx[ND], hy[ND];
+#pragma unroll
+    for (int r = 0; r < ND; r++) grad_at(T, k, r, g, hx[r], hy[r]);
+    const double* row = gv + (gp * N2 + l) * N2;
+    double u[3] = {0.0, 0.0, 0.0};  // G[l, :] B^T
+#pragma unroll
+    for (int c = 0; c < N2; c++) {
+      double c0, c1, c2;
+      bcol<ND>(hx, hy, c, c0, c1, c2);
+      const double gl = row[c];
+      u[0] += gl * c0;
+      u[1] += gl * c1;
+      u[2] += gl * c2;
+    }
+    double b[3];
+    bcol<ND>(hx, hy, l, b[0], b[1], b[2]);
+#pragma unroll
+    for (int a = 0; a < 3; a++)
+#pragma unroll
+      for (int q = 0; q < 3; q++) acc[3 * a + q] = b[a] * u[q];
+  }
+#pragma unroll
+  for (int j = 0; j < 9; j++) part[threadIdx.x][j] = acc[j];
+  __syncthreads();
+  if (gp < ngp)
+    for (int j = l; j < 9; j += N2) {  // 2 nd threads per point write its 9 entries
+      double v = 0.0;
+      for (int r = 0; r < N2; r++) v += part[slot * N2 + r][j];
+      out[9 * gp + j] = v * w;
+    }
+}
+
+// ---------------------------------------------------------------- summed operators
+// element matrices: thread (e, p) forms row p of sum_k N_k (Laplace / mass)
+template <int DEG, int OP>
+__global__ void __launch_bounds__(kGT) k_gen_ke(int64_t ne, const double* __restrict__ area,
+                                                const double2* __restrict__ grad, const double* __restrict__ coef,
+                                                double* __restrict__ ke) {
+  constexpr int ND = Tab<DEG>::ND, NG = Tab<DEG>::NG;
+  __shared__ Tab<DEG> T;
+  tab_init(T);
+  const int64_t n = ne * ND;
+  for (int64_t t = gtid(); t < n; t += gstride()) {
+    const int64_t e = t / ND;
+    const int p = (int)(t - e * ND);
+    const double ar = area[e];
+    double2 g[3];
+    if (OP == (int)GenOp::LAPLACE) load_grad(grad, e, g);
+    double row[ND];
+#pragma unroll
+    for (int q = 0; q < ND; q++) row[q] = 0.0;
+#pragma unroll
+    for (int k = 0; k < NG; k++) {
+      const double cw = coef[NG * e + k];
+      const double w = weight_at(T, k, ar);
+      if (OP == (int)GenOp::LAPLACE) {
+        double px, py;
+        grad_at(T, k, p, g, px, py);
+#pragma unroll
+        for (int q = 0; q < ND; q++) {
+          double qx, qy;
+          grad_at(T, k, q, g, qx, qy);
+          row[q] += (px * qx + py * qy) * cw * w;
+        }
+      } else {
+#pragma unroll
+        for (int q = 0; q < ND; q++) row[q] += T.h[k][p] * T.h[k][q] * cw * w;
+      }
+    }
+#pragma unroll
+    for (int q = 0; q < ND; q++) ke[t * ND + q] = row[q];
+  }
+}
+
+// elasticity element matrices (2 nd x 2 nd): thread (e, l) forms row l of sum_k w B^T D_k B
+template <int DEG>
+__global__ void __launch_bounds__(kGT) k_gen_ke_stiffness(int64_t ne, const double* __restrict__ area,
+                                                          const double2* __restrict__ grad,
+                                                          const double* __restrict__ D, double* __restrict__ ke) {
+  constexpr int ND = Tab<DEG>::ND, NG = Tab<DEG>::NG, N2 = 2 * ND;
+  __shared__ Tab<DEG> T;
+  tab_init(T);
+  const int64_t n = ne * N2;
+  for (int64_t t = gtid(); t < n; t += gstride()) {
+    const int64_t e = t / N2;
+    const int l = (int)(t - e * N2);
+    const double ar = area[e];
+    double2 g[3];
+    load_grad(grad, e, g);
+    double row[N2];
+#pragma unroll
+    for (int c = 0; c < N2; c++) row[c] = 0.0;
+#pragma unroll 1
+    for (int k = 0; k < NG; k++) {
+      const double w = weight_at(T, k, ar);
+      double hx[ND], hy[ND];
+#pragma unroll
+      for (int r = 0; r < ND; r++) grad_at(T, k, r, g, hx[r], hy[r]);
+      const double* K = D + 9 * (NG * e + k);
+      double b0, b1, b2;
+      bcol<ND>(hx, hy, l, b0, b1, b2);
+      double tq[3];
+#pragma unroll
+      for (int q = 0; q < 3; q++) tq[q] = b0 * K[q] + b1 * K[3 + q] + b2 * K[6 + q];
+#pragma unroll
+      for (int c = 0; c < N2; c++) {
+        double c0, c1, c2;
+        bcol<ND>(hx, hy, c, c0, c1, c2);
+        row[c] += (tq[0] * c0 + tq[1] * c1 + tq[2] * c2) * w;
+      }
+    }
+#pragma unroll
+    for (int c = 0; c < N2; c++) ke[t * N2 + c] = row[c];
+  }
+}
+
+// scalar rows: vals[row i] = sum over incident elements of ke row (or column) a
+template <int DEG>
+__global__ void __launch_bounds__(kGT) k_gen_rows(int64_t ndof, const int32_t* __restrict__ rowptr,
+                                                  const int32_t* __restrict__ inc_ptr, const uint4* __restrict__ inc,
+                                                  const double* __restrict__ ke, double* __restrict__ vals,
+                                                  bool transpose) {
+  constexpr int ND = Tab<DEG>::ND;
+  for (int64_t i = gtid(); i < ndof; i += gstride()) {
+    const int64_t base = rowptr[i];
+    const int len = rowptr[i + 1] - rowptr[i];
+    for (int j = 0; j < len; j++) vals[base + j] = 0.0;
+    for (int32_t s = inc_ptr[i]; s < inc_ptr[i + 1]; s++) {
+      const uint4 r = inc[s];
+      const double* K = ke + (int64_t)r.x * ND * ND;
+#pragma unroll
+      for (int b = 0; b < ND; b++) {
+        const double v = transpose ? K[b * ND + r.y] : K[r.y * ND + b];
+        vals[base + space_off(r, b)] += v;
+      }
+    }
+  }
+}
+
+// [x; y] block rows of the elasticity operator: x-row i at 2 rowptr[i], y-row ndof + i
+// at 2 nnz + 2 rowptr[i]; within a row the x columns, then the y columns
+template <int DEG>
+__global__ void __launch_bounds__(kGT) k_gen_rows_block2(int64_t ndof, int64_t nnz, const int32_t* __restrict__ rowptr,
+                                                         const int32_t* __restrict__ inc_ptr,
+                                                         const uint4* __restrict__ inc, const double* __restrict__ ke,
+                                                         double* __restrict__ vals, bool transpose) {
+  constexpr int ND = Tab<DEG>::ND, N2 = 2 * ND;
+  for (int64_t i = gtid(); i < ndof; i += gstride()) {
+    const int len = rowptr[i + 1] - rowptr[i];
+    const int64_t rb[2] = {2 * (int64_t)rowptr[i], 2 * nnz + 2 * (int64_t)rowptr[i]};
+    for (int j = 0; j < 2 * len; j++) {
+      vals[rb[0] + j] = 0.0;
+      vals[rb[1] + j] = 0.0;
+    }
+    for (int32_t s = inc_ptr[i]; s < inc_ptr[i + 1]; s++) {
+      const uint4 r = inc[s];
+      const double* K = ke + (int64_t)r.x * N2 * N2;
+#pragma unroll
+      for (int rc = 0; rc < 2; rc++) {
+        const int li = (int)r.y + rc * ND;
+#pragma unroll
+        for (int b = 0; b < ND; b++) {
+          const int64_t pos = rb[rc] + space_off(r, b);
+#pragma unroll
+          for (int cc = 0; cc < 2; cc++) {
+            const int lj = b + cc * ND;
+            vals[pos + cc * len] += transpose ? K[lj * N2 + li] : K[li * N2 + lj];
+          }
+        }
+      }
+    }
+  }
+}
+
+// ---------------------------------------------------------------- load vector
+template <int DEG>
+__global__ void __launch_bounds__(kGT) k_gen_source(int64_t ndof, const int32_t* __restrict__ inc_ptr,
+                                                    const uint4* __restrict__ inc, const double* __restrict__ area,
+                                                    const double* __restrict__ f, double* __restrict__ rhs,
+                                                    bool accumulate) {
+  constexpr int NG = Tab<DEG>::NG;
+  __shared__ Tab<DEG> T;
+  tab_init(T);
+  for (int64_t i = gtid(); i < ndof; i += gstride()) {
+    double acc = accumulate ? rhs[i] : 0.0;
+    for (int32_t s = inc_ptr[i]; s < inc_ptr[i + 1]; s++) {
+      const uint4 r = inc[s];
+      const double ar = area[r.x];
+#pragma unroll
+      for (int k = 0; k < NG; k++) acc += f[(int64_t)r.x * NG + k] * T.h[k][r.y] * weight_at(T, k, ar);
+    }
+    rhs[i] = acc;
+  }
+}
+
+template <int DEG>
+__global__ void __launch_bounds__(kGT) k_gen_source_backward(int64_t ne, const int32_t* __restrict__ dof,
+                                                             const double* __restrict__ area,
+                                                             const double* __restrict__ grhs,
+                                                             double* __restrict__ gf) {
+  constexpr int ND = Tab<DEG>::ND, NG = Tab<DEG>::NG;
+  __shared__ Tab<DEG> T;
+  tab_init(T);
+  for (int64_t gp = gtid(); gp < ne * NG; gp += gstride()) {
+    const int64_t e = gp / NG;
+    const int k = (int)(gp - e * NG);
+    const double w = weight_at(T, k, area[e]);
+    double v = 0.0;
+#pragma unroll
+    for (int r = 0; r < ND; r++) v += T.h[k][r] * w * grhs[dof[ND * e + r]];
+    gf[gp] = v;
+  }
+}
+
+// ---------------------------------------------------------------- interpolation
+template <int DEG, bool VERT>
+__global__ void __launch_bounds__(kGT) k_gen_to_gauss(int64_t ne, const int4* __restrict__ conn,
+                                                      const int32_t* __restrict__ dof, const double* __restrict__ u,
+                                                      double* __restrict__ out) {
+  constexpr int ND = Tab<DEG>::ND, NG = Tab<DEG>::NG;
+  __shared__ Tab<DEG> T;
+  tab_init(T);
+  for (int64_t gp = gtid(); gp < ne * NG; gp += gstride()) {
+    const int64_t e = gp / NG;
+    const int k = (int)(gp - e * NG);
+    double v;
+    if (VERT) {
+      const int4 c = conn[e];
+      v = u[c.x] * T.l[k][0] + u[c.y] * T.l[k][1] + u[c.z] * T.l[k][2];
+    } else {
+      v = 0.0;
+#pragma unroll
+      for (int r = 0; r < ND; r++) v += u[dof[ND * e + r]] * T.h[k][r];
+    }
+    out[gp] = v;
+  }
+}
+
+// transposes: VERT walks the vertex->element incidence of the mesh (local vertex in
+// the low bits of the record), else the space's DOF->element incidence
+template <int DEG, bool VERT>
+__global__ void __launch_bounds__(kGT) k_gen_to_gauss_backward(int64_t nrow, const int32_t* __restrict__ inc_ptr,
+                                                               const void* __restrict__ incp,
+                                                               const double* __restrict__ gout,
+                                                               double* __restrict__ gu, bool accumulate) {
+  constexpr int NG = Tab<DEG>::NG;
+  __shared__ Tab<DEG> T;
+  tab_init(T);
+  for (int64_t i = gtid(); i < nrow; i += gstride()) {
+    double acc = accumulate ? gu[i] : 0.0;
+    for (int32_t s = inc_ptr[i]; s < inc_ptr[i + 1]; s++) {
+      int64_t e;
+      int a;
+      if (VERT) {
+        const uint2 r = reinterpret_cast<const uint2*>(incp)[s];
+        e = r.x;
+        a = (int)inc_a(r.y);
+      } else {
+        const uint4 r = reinterpret_cast<const uint4*>(incp)[s];
+        e = r.x;
+        a = (int)r.y;
+      }
+#pragma unroll
+      for (int k = 0; k < NG; k++) acc += gout[e * NG + k] * (VERT ? T.l[k][a] : T.h[k][a]);
+    }
+    gu[i] = acc;
+  }
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------- launchers
+#define GEN_DISPATCH(sp, KERNEL_CALL1, KERNEL_CALL2) \
+  do {                                               \
+    if ((sp).degree == 2) {                          \
+      KERNEL_CALL2;                                  \
+    } else {                                         \
+      KERNEL_CALL1;                                  \
+    }                                                \
+  } while (0)
+
+cudaError_t launch_gen_coo(const Mesh& m, const Space& sp, GenOp op, const double* coef, long long* indices,
+                           double* vv, cudaStream_t st) {
+  const int64_t n = m.ne * sp.ng * sp.nd;
+  const int g = grid_for(n);
+  const int32_t* dof = sp.d_dof.as<int32_t>();
+  const double* area = sp.d_area.as<double>();
+  const double2* grad = m.d_grad.as<double2>();
+  if (op == GenOp::LAPLACE)
+    GEN_DISPATCH(sp, (k_gen_coo<1, 0><<<g, kGT, 0, st>>>(m.ne, dof, area, grad, coef, indices, vv)),
+                 (k_gen_coo<2, 0><<<g, kGT, 0, st>>>(m.ne, dof, area, grad, coef, indices, vv)));
+  else
+    GEN_DISPATCH(sp, (k_gen_coo<1, 1><<<g, kGT, 0, st>>>(m.ne, dof, area, grad, coef, indices, vv)),
+                 (k_gen_coo<2, 1><<<g, kGT, 0, st>>>(m.ne, dof, area, grad, coef, indices, vv)));
+  return cudaGetLastError();
+}
+
+cudaError_t launch_gen_coo_backward(const Mesh& m, const Space& sp, GenOp op, const double* grad_vv, double* grad_coef,
+                                    cudaStream_t st) {
+  const int64_t ngp = m.ne * sp.ng;
+  if (ngp == 0) return cudaSuccess;
+  const int g = (int)((ngp + 63) / 64);
+  const double* area = sp.d_area.as<double>();
+  const double2* grad = m.d_grad.as<double2>();
+  if (op == GenOp::LAPLACE)
+    GEN_DISPATCH(sp, (k_gen_coo_backward<1, 0><<<g, 64 * 3, 0, st>>>(m.ne, area, grad, grad_vv, grad_coef)),
+                 (k_gen_coo_backward<2, 0><<<g, 64 * 6, 0, st>>>(m.ne, area, grad, grad_vv, grad_coef)));
+  else
+    GEN_DISPATCH(sp, (k_gen_coo_backward<1, 1><<<g, 64 * 3, 0, st>>>(m.ne, area, grad, grad_vv, grad_coef)),
+                 (k_gen_coo_backward<2, 1><<<g, 64 * 6, 0, st>>>(m.ne, area, grad, grad_vv, grad_coef)));
+  return cudaGetLastError();
+}
+
+cudaError_t launch_gen_stiffness_coo(const Mesh& m, const Space& sp, const double* D, long long* indices, double* vv,
+                                     cudaStream_t st) {
+  const int g = grid_for(m.ne * sp.ng * 2 * sp.nd);
+  const int32_t* dof = sp.d_dof.as<int32_t>();
+  const double* area = sp.d_area.as<double>();
+  const double2* grad = m.d_grad.as<double2>();
+  GEN_DISPATCH(sp, (k_gen_stiffness_coo<1><<<g, kGT, 0, st>>>(m.ne, sp.ndof, dof, area, grad, D, indices, vv)),
+               (k_gen_stiffness_coo<2><<<g, kGT, 0, st>>>(m.ne, sp.ndof, dof, area, grad, D, indices, vv)));
+  return cudaGetLastError();
+}
+
+cudaError_t launch_gen_stiffness_coo_backward(const Mesh& m, const Space& sp, const double* grad_vv, double* grad_D,
+                                              cudaStream_t st) {
+  const int64_t ngp = m.ne * sp.ng;
+  if (ngp == 0) return cudaSuccess;
+  const int g = (int)((ngp + 31) / 32);
+  const double* area = sp.d_area.as<double>();
+  const double2* grad = m.d_grad.as<double2>();
+  GEN_DISPATCH(sp, (k_gen_stiffness_coo_backward<1><<<g, 32 * 6, 0, st>>>(m.ne, area, grad, grad_vv, grad_D)),
+               (k_gen_stiffness_coo_backward<2><<<g, 32 * 12, 0, st>>>(m.ne, area, grad, grad_vv, grad_D)));
+  return cudaGetLastError();
+}
+
+cudaError_t launch_gen_matrix(const Mesh& m, const Space& sp, GenOp op, const double* coef, double* ke, double* vals,
+                              bool transpose, cudaStream_t st) {
+  const int g = grid_for(m.ne * sp.nd);
+  const double* area = sp.d_area.as<double>();
+  const double2* grad = m.d_grad.as<double2>();
+  if (op == GenOp::LAPLACE)
+    GEN_DISPATCH(sp, (k_gen_ke<1, 0><<<g, kGT, 0, st>>>(m.ne, area, grad, coef, ke)),
+                 (k_gen_ke<2, 0><<<g, kGT, 0, st>>>(m.ne, area, grad, coef, ke)));
+  else
+    GEN_DISPATCH(sp, (k_gen_ke<1, 1><<<g, kGT, 0, st>>>(m.ne, area, grad, coef, ke)),
+                 (k_gen_ke<2, 1><<<g, kGT, 0, st>>>(m.ne, area, grad, coef, ke)));
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  const int gr = grid_for(sp.ndof);
+  const int32_t* rp = sp.d_rowptr.as<int32_t>();
+  const int32_t* ip = sp.d_inc_ptr.as<int32_t>();
+  const uint4* inc = sp.d_inc.as<uint4>();
+  GEN_DISPATCH(sp, (k_gen_rows<1><<<gr, kGT, 0, st>>>(sp.ndof, rp, ip, inc, ke, vals, transpose)),
+               (k_gen_rows<2><<<gr, kGT, 0, st>>>(sp.ndof, rp, ip, inc, ke, vals, transpose)));
+  return cudaGetLastError();
+}
+
+cudaError_t launch_gen_stiffness_matrix(const Mesh& m, const Space& sp, const double* D, double* ke, double* vals,
+                                        bool transpose, cudaStream_t st) {
+  const int g = grid_for(m.ne * 2 * sp.nd);
+  const double* area = sp.d_area.as<double>();
+  const double2* grad = m.d_grad.as<double2>();
+  GEN_DISPATCH(sp, (k_gen_ke_stiffness<1><<<g, kGT, 0, st>>>(m.ne, area, grad, D, ke)),
+               (k_gen_ke_stiffness<2><<<g, kGT, 0, st>>>(m.ne, area, grad, D, ke)));
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  const int gr = grid_for(sp.ndof);
+  const int32_t* rp = sp.d_rowptr.as<int32_t>();
+  const int32_t* ip = sp.d_inc_ptr.as<int32_t>();
+  const uint4* inc = sp.d_inc.as<uint4>();
+  GEN_DISPATCH(sp, (k_gen_rows_block2<1><<<gr, kGT, 0, st>>>(sp.ndof, sp.nnz, rp, ip, inc, ke, vals, transpose)),
+               (k_gen_rows_block2<2><<<gr, kGT, 0, st>>>(sp.ndof, sp.nnz, rp, ip, inc, ke, vals, transpose)));
+  return cudaGetLastError();
+}
+
+cudaError_t launch_gen_source(const Mesh& m, const Space& sp, const double* f, double* rhs, bool accumulate,
+                              cudaStream_t st) {
+  const int g = grid_for(sp.ndof);
+  const int32_t* ip = sp.d_inc_ptr.as<int32_t>();
+  const uint4* inc = sp.d_inc.as<uint4>();
+  const double* area = sp.d_area.as<double>();
+  GEN_DISPATCH(sp, (k_gen_source<1><<<g, kGT, 0, st>>>(sp.ndof, ip, inc, area, f, rhs, accumulate)),
+               (k_gen_source<2><<<g, kGT, 0, st>>>(sp.ndof, ip, inc, area, f, rhs, accumulate)));
+  return cudaGetLastError();
+}
+
+cudaError_t launch_gen_source_backward(const Mesh& m, const Space& sp, const double* grad_rhs, double* grad_f,
+                                       cudaStream_t st) {
+  const int g = grid_for(m.ne * sp.ng);
+  const int32_t* dof = sp.d_dof.as<int32_t>();
+  const double* area = sp.d_area.as<double>();
+  GEN_DISPATCH(sp, (k_gen_source_backward<1><<<g, kGT, 0, st>>>(m.ne, dof, area, grad_rhs, grad_f)),
+               (k_gen_source_backward<2><<<g, kGT, 0, st>>>(m.ne, dof, area, grad_rhs, grad_f)));
+  return cudaGetLastError();
+}
+
+cudaError_t launch_gen_to_gauss(const Mesh& m, const Space& sp, bool vertex_only, const double* u, double* out,
+                                cudaStream_t st) {
+  const int g = grid_for(m.ne * sp.ng);
+  const int4* conn = m.d_conn.as<int4>();
+  const int32_t* dof = sp.d_dof.as<int32_t>();
+  if (vertex_only)
+    GEN_DISPATCH(sp, (k_gen_to_gauss<1, true><<<g, kGT, 0, st>>>(m.ne, conn, dof, u, out)),
+                 (k_gen_to_gauss<2, true><<<g, kGT, 0, st>>>(m.ne, conn, dof, u, out)));
+  else
+    GEN_DISPATCH(sp, (k_gen_to_gauss<1, false><<<g, kGT, 0, st>>>(m.ne, conn, dof, u, out)),
+                 (k_gen_to_gauss<2, false><<<g, kGT, 0, st>>>(m.ne, conn, dof, u, out)));
+  return cudaGetLastError();
+}
+
+cudaError_t launch_gen_to_gauss_backward(const Mesh& m, const Space& sp, bool vertex_only, const double* grad_out,
+                                         double* grad_u, bool accumulate, cudaStream_t st) {
+  if (vertex_only) {
+    const int g = grid_for(m.nv);
+    const int32_t* ip = m.d_inc_ptr.as<int32_t>();
+    const void* inc = m.d_inc.p;
+    GEN_DISPATCH(sp, (k_gen_to_gauss_backward<1, true><<<g, kGT, 0, st>>>(m.nv, ip, inc, grad_out, grad_u, accumulate)),
+                 (k_gen_to_gauss_backward<2, true><<<g, kGT, 0, st>>>(m.nv, ip, inc, grad_out, grad_u, accumulate)));
+  } else {
+    const int g = grid_for(sp.ndof);
+    const int32_t* ip = sp.d_inc_ptr.as<int32_t>();
+    const void* inc = sp.d_inc.p;
+    GEN_DISPATCH(sp,
+                 (k_gen_to_gauss_backward<1, false><<<g, kGT, 0, st>>>(sp.ndof, ip, inc, grad_out, grad_u, accumulate)),
+                 (k_gen_to_gauss_backward<2, false><<<g, kGT, 0, st>>>(sp.ndof, ip, inc, grad_out, grad_u, accumulate)));
+  }
+  return cudaGetLastError();
+}
+
+}  // namespace adfem

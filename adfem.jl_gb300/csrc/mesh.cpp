@@ -76,6 +76,26 @@ static void parallel_for(int64_t n, F f) {
 static const double QX[3] = {1.0 / 6.0, 1.0 / 6.0, 2.0 / 3.0};
 static const double QY[3] = {1.0 / 6.0, 2.0 / 3.0, 1.0 / 6.0};
 static const double QW = 1.0 / 6.0;
+// degree-4 rule (the order P2 meshes default to, src/MFEM/MFEM.jl:71-77): the published
+// 6-point Strang-Fix/Dunavant rule, orbits (a,a), (a,1-2a), (1-2a,a)
+static const double Q4X[6] = {0.091576213509770743460, 0.091576213509770743460, 0.81684757298045851308,
+                              0.44594849091596488632, 0.44594849091596488632, 0.10810301816807022736};
+static const double Q4Y[6] = {0.091576213509770743460, 0.81684757298045851308, 0.091576213509770743460,
+                              0.44594849091596488632, 0.10810301816807022736, 0.44594849091596488632};
+static const double Q4W[6] = {0.054975871827660933819, 0.054975871827660933819, 0.054975871827660933819,
+                              0.11169079483900573285, 0.11169079483900573285, 0.11169079483900573285};
+
+void rule_point(int degree, int k, double* xi, double* eta, double* w) {
+  if (degree == 2) {
+    *xi = Q4X[k];
+    *eta = Q4Y[k];
+    *w = Q4W[k];
+  } else {
+    *xi = QX[k];
+    *eta = QY[k];
+    *w = QW;
+  }
+}
 
 static double heron(double x0, double y0, double x1, double y1, double x2, double y2) {
   // deps/MFEM/Common.cpp:9-15
@@ -391,6 +411,15 @@ int mesh_edges(Mesh* m) {
         emax.push_back(hi + 1);
       }
     }
+  m->eedge.resize(3 * m->ne);
+  for (int64_t e = 0; e < m->ne; e++)
+    for (int l = 0; l < 3; l++) {
+      int32_t a = m->elem[3 * e + l], b = m->elem[3 * e + (l + 1) % 3];
+      int32_t lo = std::min(a, b), hi = std::max(a, b);
+      const int32_t* row = m->colind.data() + m->rowptr[lo];
+      int32_t len = m->rowptr[lo + 1] - m->rowptr[lo];
+      m->eedge[3 * e + l] = (int32_t)id[m->rowptr[lo] + (std::lower_bound(row, row + len, hi) - row)];
+    }
   m->nedges = (int64_t)emin.size();
   m->edges.resize(2 * m->nedges);
   std::copy(emin.begin(), emin.end(), m->edges.begin());
@@ -399,8 +428,10 @@ int mesh_edges(Mesh* m) {
 }
 
 // Boundary nodes: endpoints of edges shared by an odd number of elements
-// (the Set toggle of src/MFEM/MCore.jl:385-406), ascending, 1-based.
-int64_t mesh_bcnode(const Mesh* m, int64_t* out1) {
+// (the Set toggle of src/MFEM/MCore.jl:385-406), ascending, 1-based.  For P2 meshes
+// the DOFs of those edges follow (nv + edge, ascending), as bcnode(mesh) appends the
+// boundary edge DOFs for P2 elements (MCore.jl:439-450).
+int64_t mesh_bcnode(Mesh* m, int64_t* out1) {
   std::vector<int32_t> cnt(m->nnz, 0);
   for (int64_t i = 0; i < m->nv; i++)
     for (int32_t s = m->inc_ptr[i]; s < m->inc_ptr[i + 1]; s++) {
@@ -419,19 +450,142 @@ int64_t mesh_bcnode(const Mesh* m, int64_t* out1) {
       c++;
     }
   }
+  if (m->degree == 2 && mesh_edges(m) == ADFEM_OK) {
+    std::vector<int32_t> ecnt(m->nedges, 0);
+    for (int32_t j : m->eedge) ecnt[j]++;
+    for (int64_t j = 0; j < m->nedges; j++)
+      if (ecnt[j] & 1) {
+        if (out1) out1[c] = m->nv + j + 1;
+        c++;
+      }
+  }
   return c;
 }
 
+int64_t mesh_ndof(Mesh* m) {
+  if (m->degree != 2) return m->nv;
+  mesh_edges(m);
+  return m->nv + m->nedges;
+}
+
 void mesh_gauss(const Mesh* m, double* x, double* y) {
+  const int ng = mesh_ng(*m);
   for (int64_t e = 0; e < m->ne; e++) {
     const double* X = m->xy.data();
     int32_t v0 = m->elem[3 * e], v1 = m->elem[3 * e + 1], v2 = m->elem[3 * e + 2];
-    for (int k = 0; k < 3; k++) {
-      double l0 = 1.0 - QX[k] - QY[k], l1 = QX[k], l2 = QY[k];
-      x[3 * e + k] = X[2 * v0] * l0 + X[2 * v1] * l1 + X[2 * v2] * l2;
-      y[3 * e + k] = X[2 * v0 + 1] * l0 + X[2 * v1 + 1] * l1 + X[2 * v2 + 1] * l2;
+    for (int k = 0; k < ng; k++) {
+      double xi, eta, w;
+      rule_point(m->degree, k, &xi, &eta, &w);
+      double l0 = 1.0 - xi - eta, l1 = xi, l2 = eta;
+      x[ng * e + k] = X[2 * v0] * l0 + X[2 * v1] * l1 + X[2 * v2] * l2;
+      y[ng * e + k] = X[2 * v0 + 1] * l0 + X[2 * v1 + 1] * l1 + X[2 * v2 + 1] * l2;
     }
   }
+}
+
+void mesh_gauss_weights(const Mesh* m, double* wout) {
+  const int ng = mesh_ng(*m);
+  for (int64_t e = 0; e < m->ne; e++)
+    for (int k = 0; k < ng; k++) {
+      double xi, eta, w;
+      rule_point(m->degree, k, &xi, &eta, &w);
+      wout[ng * e + k] = w * m->area[e] / 0.5;  // Common.cpp:116
+    }
+}
+
+// Space of degree 1 or 2 (see Space in adfem_internal.h): element DOFs as
+// NNFEM_Mesh::init numbers them (Common.cpp:62-71), the DOF graph (full pattern of
+// sparse() on the unsummed COO) and the DOF->element incidence with slot offsets.
+int mesh_space(Mesh* m, int degree, Space** out) {
+  if (degree != 1 && degree != 2) return fail(ADFEM_ERR_UNSUPPORTED, "element degree must be 1 or 2");
+  if (m->space[degree]) {
+    *out = m->space[degree].get();
+    return ADFEM_OK;
+  }
+  if (degree == 2) ADFEM_TRY(mesh_edges(m));
+  std::unique_ptr<Space> sp(new Space());
+  const int nd = degree == 2 ? 6 : 3;
+  const int64_t ne = m->ne;
+  sp->degree = degree;
+  sp->nd = nd;
+  sp->ng = degree == 2 ? 6 : 3;
+  sp->ndof = degree == 2 ? m->nv + m->nedges : m->nv;
+  if (sp->ndof > INT32_MAX / 2 || nd * ne > INT32_MAX) return fail(ADFEM_ERR_UNSUPPORTED, "space: too many DOFs");
+  const int64_t ndof = sp->ndof;
+  sp->dof.resize(nd * ne);
+  for (int64_t e = 0; e < ne; e++) {
+    for (int a = 0; a < 3; a++) sp->dof[nd * e + a] = m->elem[3 * e + a];
+    if (degree == 2)
+      for (int j = 0; j < 3; j++) sp->dof[nd * e + 3 + j] = (int32_t)(m->nv + m->eedge[3 * e + j]);
+  }
+  std::vector<int32_t> inc_ptr(ndof + 1, 0);
+  for (int32_t d : sp->dof) inc_ptr[d + 1]++;
+  for (int64_t i = 0; i < ndof; i++) inc_ptr[i + 1] += inc_ptr[i];
+  std::vector<uint32_t> inc(4 * (size_t)nd * ne, 0u);
+  {
+    std::vector<int32_t> fill(inc_ptr.begin(), inc_ptr.end() - 1);
+    for (int64_t e = 0; e < ne; e++)
+      for (int a = 0; a < nd; a++) {
+        int32_t s = fill[sp->dof[nd * e + a]]++;
+        inc[4 * (size_t)s] = (uint32_t)e;
+        inc[4 * (size_t)s + 1] = (uint32_t)a;
+      }
+  }
+  std::vector<int32_t> rowlen(ndof);
+  parallel_for(ndof, [&](int64_t lo, int64_t hi) {
+    std::vector<int32_t> cand;
+    for (int64_t i = lo; i < hi; i++) {
+      cand.clear();
+      for (int32_t s = inc_ptr[i]; s < inc_ptr[i + 1]; s++) {
+        int64_t e = inc[4 * (size_t)s];
+        for (int b = 0; b < nd; b++) cand.push_back(sp->dof[nd * e + b]);
+      }
+      std::sort(cand.begin(), cand.end());
+      rowlen[i] = (int32_t)(std::unique(cand.begin(), cand.end()) - cand.begin());
+    }
+  });
+  sp->rowptr.assign(ndof + 1, 0);
+  for (int64_t i = 0; i < ndof; i++) {
+    sp->maxrow = std::max(sp->maxrow, rowlen[i]);
+    if ((int64_t)sp->rowptr[i] + rowlen[i] > INT32_MAX) return fail(ADFEM_ERR_UNSUPPORTED, "space: pattern too large");
+    sp->rowptr[i + 1] = sp->rowptr[i] + rowlen[i];
+  }
+  if (sp->maxrow > 1024) return fail(ADFEM_ERR_UNSUPPORTED, "space: a DOF row has more than 1024 entries");
+  sp->nnz = sp->rowptr[ndof];
+  sp->colind.resize(sp->nnz);
+  parallel_for(ndof, [&](int64_t lo, int64_t hi) {
+    std::vector<int32_t> cand;
+    for (int64_t i = lo; i < hi; i++) {
+      cand.clear();
+      for (int32_t s = inc_ptr[i]; s < inc_ptr[i + 1]; s++) {
+        int64_t e = inc[4 * (size_t)s];
+        for (int b = 0; b < nd; b++) cand.push_back(sp->dof[nd * e + b]);
+      }
+      std::sort(cand.begin(), cand.end());
+      cand.erase(std::unique(cand.begin(), cand.end()), cand.end());
+      std::copy(cand.begin(), cand.end(), sp->colind.begin() + sp->rowptr[i]);
+      for (int32_t s = inc_ptr[i]; s < inc_ptr[i + 1]; s++) {
+        int64_t e = inc[4 * (size_t)s];
+        uint32_t z = 0, w = 0;
+        for (int b = 0; b < nd; b++) {
+          uint32_t off = (uint32_t)(std::lower_bound(cand.begin(), cand.end(), sp->dof[nd * e + b]) - cand.begin());
+          if (b < 3) z |= off << (10 * b);
+          else w |= off << (10 * (b - 3));
+        }
+        inc[4 * (size_t)s + 2] = z;
+        inc[4 * (size_t)s + 3] = w;
+      }
+    }
+  });
+  ADFEM_TRY(upload(sp->d_dof, sp->dof.data(), sp->dof.size()));
+  ADFEM_TRY(upload(sp->d_area, m->area.data(), m->area.size()));
+  ADFEM_TRY(upload(sp->d_rowptr, sp->rowptr.data(), sp->rowptr.size()));
+  ADFEM_TRY(upload(sp->d_colind, sp->colind.data(), sp->colind.size()));
+  ADFEM_TRY(upload(sp->d_inc_ptr, inc_ptr.data(), inc_ptr.size()));
+  ADFEM_TRY(upload(sp->d_inc, inc.data(), inc.size()));
+  m->space[degree] = std::move(sp);
+  *out = m->space[degree].get();
+  return ADFEM_OK;
 }
 
 }  // namespace adfem

@@ -57,15 +57,18 @@ ADFEM_API const char *adfem_version(void);
 
 /* deps/MFEM/API.cpp:4-14 (init_nnfem_mesh); caller src/MFEM/MFEM.jl:95-97.
  * vertices: 3*num_vertices xyz triples (z ignored); element_indices: 3*num_elements
- * 0-based vertex ids.  Only degree 1 (P1) with order 2 (or -1) is implemented;
- * other degrees record ADFEM_ERR_UNSUPPORTED and return NULL.  Builds a new mesh,
+ * 0-based vertex ids.  Implemented: degree 1 (P1) with order 2 and degree 2 (P2) with
+ * order 4 (order -1 selects these defaults, MFEM.jl:71-77); other degrees (BDM1) and
+ * orders record ADFEM_ERR_UNSUPPORTED and return NULL.  Builds a new mesh,
  * makes it current (replacing the previous current mesh, with the same warning the
  * reference prints), writes the edge count and returns a malloc'ed array of
  * 2*nedges 1-based vertex ids (all minimum endpoints, then all maximum endpoints)
  * that the caller releases with free() (Julia: unsafe_wrap(..., own=true)). */
 ADFEM_API long long *init_nnfem_mesh(double *vertices, int num_vertices, int *element_indices, int num_elements,
                                      int order, int lorder, int degree, long long *nedges);
-/* deps/MFEM/API.cpp:17-65 -- getters on the current mesh */
+/* deps/MFEM/API.cpp:17-65 -- getters on the current mesh.  For P2 meshes: 6 Gauss
+ * points per element, elem_ndof 6, ndof = nnode + nedges, connectivity rows list the
+ * vertices, then nnode + edge of the local edges (0,1), (1,2), (2,0) (Common.cpp:62-71). */
 ADFEM_API int mfem_get_ngauss(void);
 ADFEM_API void mfem_get_gauss(double *x, double *y);
 ADFEM_API void mfem_get_gauss_weights(double *w);
@@ -76,14 +79,22 @@ ADFEM_API void mfem_get_connectivity(long long *conn);
 ADFEM_API void mfem_get_element_to_vertices(long long *elems);
 
 /* deps/MFEM/FemLaplace1/FemLaplaceScalar.h:59-61 (caller src/MFEM/MCore.jl:117).
- * Unsummed COO: 9 entries per Gauss point, indices 0-based (row,col) pairs. */
+ * Unsummed COO: elem_ndof^2 entries per Gauss point (9 for P1, 36 for P2), indices
+ * 0-based (row,col) pairs. */
 ADFEM_API void FemLaplaceScalar_forward_Julia(long long *indices, double *vv, const double *kappa);
 /* deps/MFEM/FemSource1/FemSourceScalar.h:35-37 (caller MCore.jl:80).  Accumulates
  * into rhs, which the caller pre-zeroes (MCore.jl:79). */
 ADFEM_API void FemSourceScalar_forward_Julia(double *rhs, const double *f);
 /* deps/MFEM/ComputeFemStiffnessMatrixMfem/ComputeFemStiffnessMatrixMfem.h:84-87
- * (caller MCore.jl:311-312).  hmat: 9 row-major entries per Gauss point. */
+ * (caller MCore.jl:311-312).  hmat: 9 row-major entries per Gauss point; 4 elem_ndof^2
+ * entries per Gauss point, DOFs [dof; dof + ndof]. */
 ADFEM_API void ComputeFemStiffnessMatrixMfem_forward_Julia(long long *indices, double *vv, const double *hmat);
+/* deps/MFEM/FemToGaussPoints/FemToGaussPointsMfem.h:36-49 (caller src/MFEM/MUtils.jl:241-246):
+ * out[ngauss] = nodal values u[nnode] through the P1 shape of the vertices. */
+ADFEM_API void FemToGaussPointsMfem_Julia(double *out, const double *u);
+/* deps/MFEM/DofToGaussPoints/DofToGaussPointsMfem.h:35-37 (caller MUtils.jl:264-270):
+ * out[ngauss] = DOF values u[ndof] through all element basis functions. */
+ADFEM_API void DofToGaussPointsMfem_forward_Julia(double *out, const double *u);
 
 /* Compute functions behind AdFem's TensorFlow custom ops, same argument order as
  * the reference MFEM:: functions, on the current mesh, host pointers. */
@@ -94,6 +105,21 @@ ADFEM_API void FemLaplaceScalar_backward(double *grad_kappa, const double *grad_
 ADFEM_API void FemSourceScalar_backward(double *grad_f, const double *grad_rhs, const double *rhs, const double *f);
 /* ComputeFemStiffnessMatrixMfem.h:50-81 */
 ADFEM_API void ComputeFemStiffnessMatrixMfem_backward(double *grad_hmat, const double *grad_vv);
+/* deps/MFEM/ComputeFemMassMatrix1/ComputeFemMassMatrixMfem.h:4-55 (op compute_fem_mass_matrix_mfem,
+ * caller src/MFEM/MCore.jl:170-177): elem_ndof^2 COO entries per Gauss point of
+ * phi_l phi_s rho w; the backward overwrites grad_rho. */
+ADFEM_API void ComputeFemMassMatrix1_forward(long long *indices, double *vv, const double *rho);
+ADFEM_API void ComputeFemMassMatrix1_backward(double *grad_rho, const double *grad_vv, const double *vv,
+                                              const double *rho);
+/* FemToGaussPointsMfem.h:5-34, DofToGaussPointsMfem.h:5-35 (ops fem_to_gauss_points_mfem,
+ * dof_to_gauss_points_mfem); the backward functions add into grad_u (nnode or ndof
+ * entries), as the reference loops do into a zeroed tensor. */
+ADFEM_API void FemToGaussPointsMfem_forward(double *out, const double *u);
+ADFEM_API void FemToGaussPointsMfem_backward(double *grad_u, const double *grad_out, const double *out,
+                                             const double *u);
+ADFEM_API void DofToGaussPointsMfem_forward(double *out, const double *u);
+ADFEM_API void DofToGaussPointsMfem_backward(double *grad_u, const double *grad_out, const double *out,
+                                             const double *u);
 /* deps/MFEM/PlaneStrainAndStress/PlaneStrainAndStress.h:5-78 (op plane_strain_and_stress,
  * mode 0 = strain with the reference's all-nine-entries formula, mode 1 = stress) */
 ADFEM_API void PlaneStrainMatrix_forward(double *out, const double *E, const double *nu, int N);
@@ -109,28 +135,38 @@ ADFEM_API void PlaneStressMatrix_backward(double *grad_nu, double *grad_E, const
 typedef struct adfem_mesh adfem_mesh;
 typedef struct adfem_system adfem_system;
 
-/* Same inputs as init_nnfem_mesh (src/MFEM/MFEM.jl:60-119).  degree must be 1. */
+/* Same inputs as init_nnfem_mesh (src/MFEM/MFEM.jl:60-119).  degree 1 (P1, order-2
+ * rule) or 2 (P2, order-4 rule). */
 ADFEM_API int adfem_mesh_create(const double *xyz, long long num_vertices, const int *elems0, long long num_elements,
                                 int degree, adfem_mesh **out);
 ADFEM_API int adfem_mesh_destroy(adfem_mesh *mesh);
-/* nv, ne, ngauss (=3 ne), scalar pattern nnz */
+/* nv, ne, ngauss (3 ne for P1, 6 ne for P2), nnz of the scalar DOF pattern */
 ADFEM_API int adfem_mesh_sizes(const adfem_mesh *mesh, long long *nv, long long *ne, long long *ngauss,
                                long long *nnz);
+/* Element degree, DOFs per element, Gauss points per element, DOF count (nnode, or
+ * nnode + nedges for P2) and scalar pattern nnz of the mesh's own space. */
+ADFEM_API int adfem_mesh_space(const adfem_mesh *mesh, int *degree, int *elem_ndof, int *ngauss_elem,
+                               long long *ndof, long long *nnz);
+/* mfem_get_connectivity: ne x elem_ndof DOFs, 1-based, row-major */
+ADFEM_API int adfem_mesh_connectivity(const adfem_mesh *mesh, long long *conn1);
+/* mfem_get_gauss_weights: ip.weight * area / 0.5 per Gauss point (Common.cpp:116) */
+ADFEM_API int adfem_mesh_gauss_weights(const adfem_mesh *mesh, double *w);
 /* Make a handle the "current mesh" of layer 1 (NULL clears it).  The library keeps
  * one current mesh like the reference's global mmesh (deps/MFEM/Common.cpp:7). */
 ADFEM_API int adfem_set_current_mesh(adfem_mesh *mesh);
 ADFEM_API adfem_mesh *adfem_current_mesh(void);
 /* 1-based CSC pattern of the scalar operator (Julia SparseMatrixCSC colptr/rowval).
  * Equal to the pattern of sparse(I,J,V) on the unsummed COO (src/MFEM/MCore.jl:119):
- * the full node graph, stored zeros included.  colptr: nv+1, rowval: nnz. */
+ * the full DOF graph, stored zeros included.  colptr: ndof+1, rowval: nnz. */
 ADFEM_API int adfem_mesh_pattern(const adfem_mesh *mesh, long long *colptr1, long long *rowval1);
-/* Same for the 2 nv x 2 nv elasticity operator in the reference's [x block; y block]
- * ordering (MCore.jl:314): colptr 2nv+1, rowval 4 nnz. */
+/* Same for the 2 ndof x 2 ndof elasticity operator in the reference's [x block; y block]
+ * ordering (MCore.jl:314): colptr 2ndof+1, rowval 4 nnz. */
 ADFEM_API int adfem_mesh_pattern_elasticity(const adfem_mesh *mesh, long long *colptr1, long long *rowval1);
 /* bcnode (src/MFEM/MCore.jl:439-450): nodes on edges used by exactly one element, 1-based,
- * ascending (the reference returns Julia Set order).  With out == NULL only *count is set. */
+ * ascending (the reference returns Julia Set order); for P2 meshes followed by the DOFs
+ * of those edges (nnode + edge, ascending).  With out == NULL only *count is set. */
 ADFEM_API int adfem_mesh_bcnode(const adfem_mesh *mesh, long long *out, long long *count);
-/* gauss_nodes (src/MFEM/MFEM.jl:226-232): 3 points per element, element-major */
+/* gauss_nodes (src/MFEM/MFEM.jl:226-232): 3 (P1) or 6 (P2) points per element, element-major */
 ADFEM_API int adfem_mesh_gauss_nodes(const adfem_mesh *mesh, double *x, double *y);
 /* Element vertices after the orientation fix, 1-based, row-major ne x 3 (the content
  * mfem_get_element_to_vertices writes back into Julia's mesh.elems, API.cpp:57-64). */
@@ -140,6 +176,30 @@ ADFEM_API int adfem_mesh_area(const adfem_mesh *mesh, double *area);
 /* Edge list as returned by init_nnfem_mesh (Common.cpp:133-139): 2*nedges 1-based ids,
  * minimum endpoints then maximum endpoints.  With out == NULL only *nedges is set. */
 ADFEM_API int adfem_mesh_edges(const adfem_mesh *mesh, long long *out, long long *nedges);
+
+/* ---- compute_fem_mass_matrix1 (src/MFEM/MCore.jl:170-181), ComputeFemMassMatrixMfem.h:4-55 ----
+ * rho: one value per Gauss point.  Summed operator in the adfem_mesh_pattern order
+ * (CSC, host) or its CSR rows on the device; unsummed COO (elem_ndof^2 per Gauss point)
+ * and its backward (grad_rho overwritten) on the device.  Every degree. */
+ADFEM_API int adfem_mass_csc(adfem_mesh *mesh, const double *rho, long long nrho, double *nzval);
+ADFEM_API int adfem_mass_csr_d(adfem_mesh *mesh, const double *rho_d, double *vals_d, void *stream);
+ADFEM_API int adfem_mass_coo_d(adfem_mesh *mesh, const double *rho_d, long long *indices_d, double *vv_d,
+                               void *stream);
+ADFEM_API int adfem_mass_coo_backward_d(adfem_mesh *mesh, const double *grad_vv_d, double *grad_rho_d, void *stream);
+
+/* ---- fem_to_gauss_points / dof_to_gauss_points (src/MFEM/MUtils.jl:231-275) ----
+ * fem: u holds nodal values (nu >= nnode; P1 shape of the vertices); dof: u holds DOF
+ * values (nu >= ndof; all basis functions).  out: ngauss values.  The backward of
+ * either writes (accumulate = 0; entries past the values used are zeroed) or adds
+ * (accumulate = 1) grad_u, nu entries. */
+ADFEM_API int adfem_fem_to_gauss(adfem_mesh *mesh, const double *u, long long nu, double *out);
+ADFEM_API int adfem_dof_to_gauss(adfem_mesh *mesh, const double *u, long long nu, double *out);
+ADFEM_API int adfem_fem_to_gauss_d(adfem_mesh *mesh, const double *u_d, double *out_d, void *stream);
+ADFEM_API int adfem_fem_to_gauss_backward_d(adfem_mesh *mesh, const double *grad_out_d, double *grad_u_d,
+                                            long long nu, int accumulate, void *stream);
+ADFEM_API int adfem_dof_to_gauss_d(adfem_mesh *mesh, const double *u_d, double *out_d, void *stream);
+ADFEM_API int adfem_dof_to_gauss_backward_d(adfem_mesh *mesh, const double *grad_out_d, double *grad_u_d,
+                                            long long nu, int accumulate, void *stream);
 
 /* ---- compute_fem_laplace_matrix1 (src/MFEM/MCore.jl:112-120), Array arm ----
  * kappa: ngauss values (host).  nzval: nnz values in the adfem_mesh_pattern order,
@@ -168,7 +228,7 @@ ADFEM_API int adfem_source_backward_d(adfem_mesh *mesh, const double *grad_rhs_d
 ADFEM_API int adfem_stiffness_csc(adfem_mesh *mesh, const double *D, long long nD, double *nzval);
 /* device variant: 0-based CSR values of the same pattern (transpose of the CSC values) */
 ADFEM_API int adfem_stiffness_csr_d(adfem_mesh *mesh, const double *D_d, double *vals_d, void *stream);
-/* graph-op arm (ComputeFemStiffnessMatrixMfem.h:4-48): unsummed COO, 36 per Gauss point */
+/* graph-op arm (ComputeFemStiffnessMatrixMfem.h:4-48): unsummed COO, 4 elem_ndof^2 per Gauss point */
 ADFEM_API int adfem_stiffness_coo_d(adfem_mesh *mesh, const double *D_d, long long *indices_d, double *vv_d,
                                     void *stream);
 ADFEM_API int adfem_stiffness_coo_backward_d(adfem_mesh *mesh, const double *grad_vv_d, double *grad_D_d,
@@ -239,6 +299,7 @@ ADFEM_API int adfem_csc_solve(long long n, const long long *colptr1, const long 
  * sliced-ELL form (FP64 and FP32 Jacobi-scaled copies) with its right-hand side and
  * CG work vectors, so repeated solves and adjoint solves reuse them. */
 enum { ADFEM_SYS_POISSON = 0, ADFEM_SYS_ELASTICITY = 1 };
+/* P1 meshes only (a P2 mesh gives ADFEM_ERR_UNSUPPORTED: assemble its operators and use adfem_csc_solve) */
 ADFEM_API int adfem_system_create(adfem_mesh *mesh, int kind, adfem_system **out);
 ADFEM_API int adfem_system_destroy(adfem_system *sys);
 /* Dirichlet data: bd 1-based DOF ids (for elasticity DOF ids in the [x; y] ordering,

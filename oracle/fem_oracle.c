@@ -1,5 +1,6 @@
 /*
- * fem_oracle.c -- CPU restatement of AdFem's P1-triangle forward/backward path.
+ * fem_oracle.c -- CPU restatement of AdFem's triangle forward/backward path (P1, and
+ * the P2 / mass-matrix / Gauss-point interpolation ops next to it).
  *
  * TEST INFRASTRUCTURE ONLY.  This file is the parity oracle: it is called by
  * tests/, by __graft_entry__.smoke() and by bench.py's CPU-baseline legs, and
@@ -103,7 +104,7 @@ int orc_mesh_geometry(int nv, const double *xyz, int ne, const int *elems0, int 
  * Returns nedges; writes edges when out != NULL.  O(ne log) via a per-vertex
  * adjacency scan (vertex valence is small).
  */
-i64 orc_mesh_edges(int nv, int ne, const int *elem, i64 *out) {
+static i64 edges_impl(int nv, int ne, const int *elem, i64 *out, int *eedge) {
   /* adjacency lists keyed by the smaller vertex */
   int *cnt = (int *)calloc((size_t)nv + 1, sizeof(int));
   for (int e = 0; e < ne; e++)
@@ -123,16 +124,17 @@ i64 orc_mesh_edges(int nv, int ne, const int *elem, i64 *out) {
     for (int l = 0; l < 3; l++) {
       int a = elem[3 * e + l], b = elem[3 * e + (l + 1) % 3];
       int lo = a < b ? a : b, hi = a < b ? b : a;
-      int found = 0;
+      i64 found = -1;
       for (int s = cnt[lo]; s < cnt[lo] + fill[lo]; s++)
-        if (nbr[s] == hi) { found = 1; break; }
-      if (!found) {
+        if (nbr[s] == hi) { found = id[s]; break; }
+      if (found < 0) {
         int s = cnt[lo] + fill[lo]++;
         nbr[s] = hi;
         id[s] = nedges;
         emin[nedges] = lo; emax[nedges] = hi;
-        nedges++;
+        found = nedges++;
       }
+      if (eedge) eedge[3 * e + l] = (int)found;
     }
   if (out) {
     for (i64 i = 0; i < nedges; i++) {
@@ -143,6 +145,12 @@ i64 orc_mesh_edges(int nv, int ne, const int *elem, i64 *out) {
   free(cnt); free(nbr); free(id); free(fill); free(emin); free(emax);
   return nedges;
 }
+
+i64 orc_mesh_edges(int nv, int ne, const int *elem, i64 *out) { return edges_impl(nv, ne, elem, out, NULL); }
+
+/* Element-to-edge map in the same numbering: eedge[3e + l] is the edge of local edge l
+ * ((0,1), (1,2), (2,0)), as mesh.GetElementEdges gives it in Common.cpp:68-71. */
+i64 orc_element_edges(int nv, int ne, const int *elem, int *eedge) { return edges_impl(nv, ne, elem, NULL, eedge); }
 
 /* FemLaplaceScalar_forward, deps/MFEM/FemLaplace1/FemLaplaceScalar.h:3-26 */
 void orc_laplace_coo(int ne, const int *elem, const double *w, const double *hx, const double *hy,
@@ -277,6 +285,323 @@ void orc_stiffness_coo_backward(int ne, const double *w, const double *hx, const
         }
     }
   }
+}
+
+/* ======================================================================
+ * Degree-generic element loops (P1 and P2 Lagrange triangles).
+ *
+ * The reference kernels are written over elem_ndof and elem->ngauss with per-point
+ * tables h, hx, hy, w and dof[] filled by NNFEM_Mesh::init (Common.cpp:46-126);
+ * the loops below restate them over tables of the same meaning:
+ *   nd = elem_ndof (3 or 6), ng = Gauss points per element (3 or 6),
+ *   dof[nd*e + r], w[ng*e + k], h/hx/hy[(ng*e + k)*nd + r], hs[(ng*e + k)*3 + a].
+ * ---------------------------------------------------------------------- */
+
+/* Degree-4 triangle rule (IntegrationRules::Get(TRIANGLE, 4), the order P2 meshes
+ * default to, src/MFEM/MFEM.jl:71-77): the published 6-point Strang-Fix/Dunavant rule,
+ * two orbits (a,a), (a,1-2a), (1-2a,a) with a = 0.0915762... (weight 0.0549758...)
+ * and a = 0.4459484... (weight 0.1116907...); weights sum to the reference area 1/2.
+ * Point order within the rule is not pinned by any reference test. */
+static const double Q4X[6] = {0.091576213509770743460, 0.091576213509770743460, 0.81684757298045851308,
+                              0.44594849091596488632, 0.44594849091596488632, 0.10810301816807022736};
+static const double Q4Y[6] = {0.091576213509770743460, 0.81684757298045851308, 0.091576213509770743460,
+                              0.44594849091596488632, 0.10810301816807022736, 0.44594849091596488632};
+static const double Q4W[6] = {0.054975871827660933819, 0.054975871827660933819, 0.054975871827660933819,
+                              0.11169079483900573285, 0.11169079483900573285, 0.11169079483900573285};
+
+/* Lagrange basis on the triangle in barycentric coordinates l[3] and its partial
+ * derivatives t[r][c] = d phi_r / d l_c.  P1: phi_r = l_r.  P2 (H1_FECollection(2):
+ * nodes at the vertices and edge midpoints, vertex functions first, then the edges
+ * (0,1), (1,2), (2,0)): phi_a = l_a (2 l_a - 1), phi_ab = 4 l_a l_b. */
+static void basis(int degree, const double l[3], double phi[6], double t[6][3]) {
+  for (int r = 0; r < 6; r++) t[r][0] = t[r][1] = t[r][2] = 0.0;
+  if (degree == 1) {
+    for (int r = 0; r < 3; r++) {
+      phi[r] = l[r];
+      t[r][r] = 1.0;
+    }
+    return;
+  }
+  for (int a = 0; a < 3; a++) {
+    phi[a] = l[a] * (2.0 * l[a] - 1.0);
+    t[a][a] = 4.0 * l[a] - 1.0;
+  }
+  static const int E0[3] = {0, 1, 2}, E1[3] = {1, 2, 0};
+  for (int j = 0; j < 3; j++) {
+    int a = E0[j], b = E1[j];
+    phi[3 + j] = 4.0 * l[a] * l[b];
+    t[3 + j][a] = 4.0 * l[b];
+    t[3 + j][b] = 4.0 * l[a];
+  }
+}
+
+/*
+ * Per-point tables of NNFEM_Mesh::init (Common.cpp:46-126) for degree 1 or 2:
+ *   elem, area, hx1, hy1 : outputs of orc_mesh_geometry (P1 gradients = grad l_a)
+ *   eedge                : orc_element_edges (needed for degree 2, else NULL)
+ * outputs: dof (nd per element: vertices, then nv + edge of each local edge,
+ * Common.cpp:62-71), w, h, hx, hy, hs (P1 shape at the point, Common.cpp:103-105) and
+ * the Gauss-point coordinates gx, gy.  Physical gradients follow the chain rule
+ * grad phi_r = sum_c (d phi_r / d l_c) grad l_c, which is what CalcPhysDShape
+ * evaluates through the inverse Jacobian.
+ */
+void orc_space_tables(int degree, int nv, const double *xyz, int ne, const int *elem, const int *eedge,
+                      const double *area, const double *hx1, const double *hy1, int *dof, double *w, double *h,
+                      double *hx, double *hy, double *hs, double *gx, double *gy) {
+  const int nd = degree == 2 ? 6 : 3, ng = degree == 2 ? 6 : 3;
+  for (int e = 0; e < ne; e++) {
+    for (int a = 0; a < 3; a++) dof[nd * e + a] = elem[3 * e + a];
+    if (degree == 2)
+      for (int j = 0; j < 3; j++) dof[nd * e + 3 + j] = nv + eedge[3 * e + j];
+    const int v0 = elem[3 * e], v1 = elem[3 * e + 1], v2 = elem[3 * e + 2];
+    for (int k = 0; k < ng; k++) {
+      const double xi = degree == 2 ? Q4X[k] : QX[k], eta = degree == 2 ? Q4Y[k] : QY[k];
+      const double qw = degree == 2 ? Q4W[k] : QW;
+      double l[3] = {1.0 - xi - eta, xi, eta};
+      double phi[6], t[6][3];
+      basis(degree, l, phi, t);
+      const i64 p = (i64)ng * e + k;
+      w[p] = qw * area[e] / 0.5;
+      gx[p] = xyz[3 * v0] * l[0] + xyz[3 * v1] * l[1] + xyz[3 * v2] * l[2];
+      gy[p] = xyz[3 * v0 + 1] * l[0] + xyz[3 * v1 + 1] * l[1] + xyz[3 * v2 + 1] * l[2];
+      for (int a = 0; a < 3; a++) hs[3 * p + a] = l[a];
+      for (int r = 0; r < nd; r++) {
+        h[nd * p + r] = phi[r];
+        hx[nd * p + r] = t[r][0] * hx1[3 * e] + t[r][1] * hx1[3 * e + 1] + t[r][2] * hx1[3 * e + 2];
+        hy[nd * p + r] = t[r][0] * hy1[3 * e] + t[r][1] * hy1[3 * e + 1] + t[r][2] * hy1[3 * e + 2];
+      }
+    }
+  }
+}
+
+/* FemLaplaceScalar_forward, FemLaplaceScalar.h:3-26, over elem_ndof */
+void orc_gen_laplace_coo(int ne, int nd, int ng, const int *dof, const double *w, const double *hx,
+                         const double *hy, const double *kappa, i64 *indices, double *vv) {
+  i64 nz = 0;
+  for (int e = 0; e < ne; e++)
+    for (int k = 0; k < ng; k++) {
+      const i64 p = (i64)ng * e + k;
+      for (int a = 0; a < nd; a++)
+        for (int b = 0; b < nd; b++) {
+          double dd = hx[nd * p + a] * hx[nd * p + b] + hy[nd * p + a] * hy[nd * p + b];
+          indices[2 * nz] = dof[nd * e + a];
+          indices[2 * nz + 1] = dof[nd * e + b];
+          vv[nz] = dd * kappa[p] * w[p];
+          nz++;
+        }
+    }
+}
+
+/* FemLaplaceScalar_backward, FemLaplaceScalar.h:28-54 */
+void orc_gen_laplace_coo_backward(int ne, int nd, int ng, const double *w, const double *hx, const double *hy,
+                                  const double *grad_vv, double *grad_kappa) {
+  i64 nz = 0;
+  for (int e = 0; e < ne; e++)
+    for (int k = 0; k < ng; k++) {
+      const i64 p = (i64)ng * e + k;
+      double v = 0.0;
+      for (int a = 0; a < nd; a++)
+        for (int b = 0; b < nd; b++) {
+          double dd = hx[nd * p + a] * hx[nd * p + b] + hy[nd * p + a] * hy[nd * p + b];
+          v += grad_vv[nz] * (dd * w[p]);
+          nz++;
+        }
+      grad_kappa[p] = v;
+    }
+}
+
+/* ComputeFemMassMatrix1_forward, deps/MFEM/ComputeFemMassMatrix1/ComputeFemMassMatrixMfem.h:4-29 */
+void orc_gen_mass_coo(int ne, int nd, int ng, const int *dof, const double *w, const double *h, const double *rho,
+                      i64 *indices, double *vv) {
+  i64 nz = 0;
+  for (int e = 0; e < ne; e++)
+    for (int k = 0; k < ng; k++) {
+      const i64 p = (i64)ng * e + k;
+      for (int a = 0; a < nd; a++)
+        for (int b = 0; b < nd; b++) {
+          indices[2 * nz] = dof[nd * e + a];
+          indices[2 * nz + 1] = dof[nd * e + b];
+          vv[nz] = h[nd * p + a] * h[nd * p + b] * rho[p] * w[p];
+          nz++;
+        }
+    }
+}
+
+/* ComputeFemMassMatrix1_backward, ComputeFemMassMatrixMfem.h:31-55 (grad_rho zeroed first,
+ * as the TF grad op does, ComputeFemMassMatrixMfem.cpp:139) */
+void orc_gen_mass_coo_backward(int ne, int nd, int ng, const double *w, const double *h, const double *grad_vv,
+                               double *grad_rho) {
+  i64 nz = 0;
+  for (int e = 0; e < ne; e++)
+    for (int k = 0; k < ng; k++) {
+      const i64 p = (i64)ng * e + k;
+      grad_rho[p] = 0.0;
+      for (int a = 0; a < nd; a++)
+        for (int b = 0; b < nd; b++) {
+          grad_rho[p] += h[nd * p + a] * h[nd * p + b] * w[p] * grad_vv[nz];
+          nz++;
+        }
+    }
+}
+
+/* FemSourceScalar_forward, FemSourceScalar.h:4-15, over elem_ndof (accumulates into rhs) */
+void orc_gen_source(int ne, int nd, int ng, const int *dof, const double *w, const double *h, const double *f,
+                    double *rhs) {
+  for (int e = 0; e < ne; e++)
+    for (int k = 0; k < ng; k++) {
+      const i64 p = (i64)ng * e + k;
+      for (int r = 0; r < nd; r++) rhs[dof[nd * e + r]] += f[p] * h[nd * p + r] * w[p];
+    }
+}
+
+/* FemSourceScalar_backward, FemSourceScalar.h:17-32 */
+void orc_gen_source_backward(int ne, int nd, int ng, const int *dof, const double *w, const double *h,
+                             const double *grad_rhs, double *grad_f) {
+  for (int e = 0; e < ne; e++)
+    for (int k = 0; k < ng; k++) {
+      const i64 p = (i64)ng * e + k;
+      grad_f[p] = 0.0;
+      for (int r = 0; r < nd; r++) grad_f[p] += h[nd * p + r] * w[p] * grad_rhs[dof[nd * e + r]];
+    }
+}
+
+/* ComputeFemStiffnessMatrixMfem_forward, ComputeFemStiffnessMatrixMfem.h:4-48, over
+ * elem_ndof: B = [hx 0; 0 hy; hy hx] (3 x 2nd), DOFs [dof; dof + ndof] */
+void orc_gen_stiffness_coo(int ne, int nd, int ng, int ndof, const int *dof, const double *w, const double *hx,
+                           const double *hy, const double *hmat, i64 *indices, double *vv) {
+  i64 nz = 0;
+  double B[3][12];
+  for (int e = 0; e < ne; e++)
+    for (int k = 0; k < ng; k++) {
+      const i64 p = (i64)ng * e + k;
+      for (int a = 0; a < 3; a++)
+        for (int c = 0; c < 2 * nd; c++) B[a][c] = 0.0;
+      for (int r = 0; r < nd; r++) {
+        B[0][r] = hx[nd * p + r];
+        B[1][r + nd] = hy[nd * p + r];
+        B[2][r] = hy[nd * p + r];
+        B[2][r + nd] = hx[nd * p + r];
+      }
+      const double *K = hmat + 9 * p;
+      double T[12][3];
+      for (int l = 0; l < 2 * nd; l++)
+        for (int q = 0; q < 3; q++) {
+          double acc = 0.0;
+          for (int a = 0; a < 3; a++) acc += B[a][l] * K[3 * a + q];
+          T[l][q] = acc;
+        }
+      for (int l = 0; l < 2 * nd; l++)
+        for (int c = 0; c < 2 * nd; c++) {
+          double acc = 0.0;
+          for (int q = 0; q < 3; q++) acc += T[l][q] * B[q][c];
+          indices[2 * nz] = dof[nd * e + (l % nd)] + (l >= nd ? ndof : 0);
+          indices[2 * nz + 1] = dof[nd * e + (c % nd)] + (c >= nd ? ndof : 0);
+          vv[nz] = acc * w[p];
+          nz++;
+        }
+    }
+}
+
+/* ComputeFemStiffnessMatrixMfem_backward, ComputeFemStiffnessMatrixMfem.h:50-81 */
+void orc_gen_stiffness_coo_backward(int ne, int nd, int ng, const double *w, const double *hx, const double *hy,
+                                    const double *grad_vv, double *grad_hmat) {
+  i64 nz = 0;
+  double B[3][12], T[3][12];
+  for (int e = 0; e < ne; e++)
+    for (int k = 0; k < ng; k++) {
+      const i64 p = (i64)ng * e + k;
+      for (int a = 0; a < 3; a++)
+        for (int c = 0; c < 2 * nd; c++) B[a][c] = 0.0;
+      for (int r = 0; r < nd; r++) {
+        B[0][r] = hx[nd * p + r];
+        B[1][r + nd] = hy[nd * p + r];
+        B[2][r] = hy[nd * p + r];
+        B[2][r + nd] = hx[nd * p + r];
+      }
+      const double *G = grad_vv + nz;
+      for (int a = 0; a < 3; a++)
+        for (int c = 0; c < 2 * nd; c++) {
+          double acc = 0.0;
+          for (int l = 0; l < 2 * nd; l++) acc += B[a][l] * G[2 * nd * l + c];
+          T[a][c] = acc;
+        }
+      for (int a = 0; a < 3; a++)
+        for (int q = 0; q < 3; q++) {
+          double acc = 0.0;
+          for (int c = 0; c < 2 * nd; c++) acc += T[a][c] * B[q][c];
+          grad_hmat[9 * p + 3 * a + q] = acc * w[p];
+        }
+      nz += 4 * nd * nd;
+    }
+}
+
+/* FemToGaussPointsMfem_forward / _backward, deps/MFEM/FemToGaussPoints/FemToGaussPointsMfem.h:5-34:
+ * nodal values through the P1 shape hs at each Gauss point.  The backward accumulates
+ * into grad_u (the TF op zeroes it first, FemToGaussPointsMfem.cpp:128). */
+void orc_fem_to_gauss(int ne, int ng, const int *elem, const double *hs, const double *u, double *out) {
+  for (int e = 0; e < ne; e++)
+    for (int k = 0; k < ng; k++) {
+      const i64 p = (i64)ng * e + k;
+      out[p] = u[elem[3 * e]] * hs[3 * p] + u[elem[3 * e + 1]] * hs[3 * p + 1] + u[elem[3 * e + 2]] * hs[3 * p + 2];
+    }
+}
+
+void orc_fem_to_gauss_backward(int ne, int ng, const int *elem, const double *hs, const double *grad_out,
+                               double *grad_u) {
+  for (int e = 0; e < ne; e++)
+    for (int k = 0; k < ng; k++) {
+      const i64 p = (i64)ng * e + k;
+      for (int a = 0; a < 3; a++) grad_u[elem[3 * e + a]] += grad_out[p] * hs[3 * p + a];
+    }
+}
+
+/* DofToGaussPointsMfem_forward / _backward, deps/MFEM/DofToGaussPoints/DofToGaussPointsMfem.h:5-35 */
+void orc_dof_to_gauss(int ne, int nd, int ng, const int *dof, const double *h, const double *u, double *out) {
+  for (int e = 0; e < ne; e++)
+    for (int k = 0; k < ng; k++) {
+      const i64 p = (i64)ng * e + k;
+      out[p] = 0.0;
+      for (int r = 0; r < nd; r++) out[p] += u[dof[nd * e + r]] * h[nd * p + r];
+    }
+}
+
+void orc_dof_to_gauss_backward(int ne, int nd, int ng, const int *dof, const double *h, const double *grad_out,
+                               double *grad_u) {
+  for (int e = 0; e < ne; e++)
+    for (int k = 0; k < ng; k++) {
+      const i64 p = (i64)ng * e + k;
+      for (int r = 0; r < nd; r++) grad_u[dof[nd * e + r]] += grad_out[p] * h[nd * p + r];
+    }
+}
+
+/* bcnode(mesh) for P2 (src/MFEM/MCore.jl:439-450): boundary vertices, then the DOFs of
+ * boundary edges (nv + edge).  Boundary edges are those used by one element
+ * (bcedge's toggle set, MCore.jl:385-406).  Both parts ascending, 1-based.
+ * Returns the count; writes out when non-NULL. */
+i64 orc_bcnode_p2(int nv, int ne, const int *elem, const int *eedge, i64 nedges, i64 *out) {
+  int *cnt = (int *)calloc((size_t)(nedges > 0 ? nedges : 1), sizeof(int));
+  char *bv = (char *)calloc((size_t)nv, 1);
+  for (int e = 0; e < ne; e++)
+    for (int l = 0; l < 3; l++) cnt[eedge[3 * e + l]]++;
+  for (int e = 0; e < ne; e++)
+    for (int l = 0; l < 3; l++)
+      if (cnt[eedge[3 * e + l]] & 1) {
+        bv[elem[3 * e + l]] = 1;
+        bv[elem[3 * e + (l + 1) % 3]] = 1;
+      }
+  i64 c = 0;
+  for (int i = 0; i < nv; i++)
+    if (bv[i]) {
+      if (out) out[c] = i + 1;
+      c++;
+    }
+  for (i64 j = 0; j < nedges; j++)
+    if (cnt[j] & 1) {
+      if (out) out[c] = nv + j + 1;
+      c++;
+    }
+  free(cnt); free(bv);
+  return c;
 }
 
 /*

@@ -1,4 +1,4 @@
-"""Parity oracle for the P1-triangle path -- TEST INFRASTRUCTURE ONLY.
+"""Parity oracle for the triangle-element path (P1, P2) -- TEST INFRASTRUCTURE ONLY.
 
 ctypes wrapper around ``fem_oracle.c`` (a serial C restatement of AdFem's
 deps/MFEM kernels, each function citing the reference file:line it follows),
@@ -63,6 +63,21 @@ def lib():
             "orc_dirichlet_csc": (_L, [_L, _P, _P, _P, _P, _P, _I, _P, _I, _P, _P, _P, _P]),
             "orc_bcnode": (_L, [_I, _I, _P, _P]),
             "orc_pcg": (_I, [_L, _P, _P, _P, _P, _P, _D, _I, _I, _P]),
+            "orc_element_edges": (_L, [_I, _I, _P, _P]),
+            "orc_space_tables": (None, [_I, _I, _P, _I, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P]),
+            "orc_gen_laplace_coo": (None, [_I, _I, _I, _P, _P, _P, _P, _P, _P, _P]),
+            "orc_gen_laplace_coo_backward": (None, [_I, _I, _I, _P, _P, _P, _P, _P]),
+            "orc_gen_mass_coo": (None, [_I, _I, _I, _P, _P, _P, _P, _P, _P]),
+            "orc_gen_mass_coo_backward": (None, [_I, _I, _I, _P, _P, _P, _P]),
+            "orc_gen_source": (None, [_I, _I, _I, _P, _P, _P, _P, _P]),
+            "orc_gen_source_backward": (None, [_I, _I, _I, _P, _P, _P, _P, _P]),
+            "orc_gen_stiffness_coo": (None, [_I, _I, _I, _I, _P, _P, _P, _P, _P, _P, _P]),
+            "orc_gen_stiffness_coo_backward": (None, [_I, _I, _I, _P, _P, _P, _P, _P]),
+            "orc_fem_to_gauss": (None, [_I, _I, _P, _P, _P, _P]),
+            "orc_fem_to_gauss_backward": (None, [_I, _I, _P, _P, _P, _P]),
+            "orc_dof_to_gauss": (None, [_I, _I, _I, _P, _P, _P, _P]),
+            "orc_dof_to_gauss_backward": (None, [_I, _I, _I, _P, _P, _P, _P]),
+            "orc_bcnode_p2": (_L, [_I, _I, _P, _P, _L, _P]),
         }
         for name, (res, args) in sig.items():
             f = getattr(L, name)
@@ -179,6 +194,164 @@ class OracleMesh:
         n = lib().orc_bcnode(self.nnode, self.nelem, _p(self.elem), None)
         out = np.empty(n, np.int64)
         lib().orc_bcnode(self.nnode, self.nelem, _p(self.elem), _p(out))
+        return out
+
+
+class OracleSpace:
+    """Restated NNFEM_Mesh tables for degree 1 (P1) or 2 (P2) Lagrange triangles.
+
+    Follows deps/MFEM/Common.cpp:46-126: element DOFs (vertices, then nnode + edge of
+    the local edges (0,1), (1,2), (2,0)), per-point weights, shape values and physical
+    gradients on the default rule of the degree (order 2: 3 points; order 4: 6
+    points).  The operator methods restate the reference loops over elem_ndof.
+    """
+
+    def __init__(self, coords, elems, degree: int = 1):
+        if degree not in (1, 2):
+            raise ValueError("degree must be 1 or 2")
+        self.p1 = OracleMesh(coords, elems)
+        m = self.p1
+        self.degree = degree
+        self.nnode, self.nelem = m.nnode, m.nelem
+        ne = self.nelem
+        self.eedge = np.empty((ne, 3), np.int32)
+        self.nedge = int(lib().orc_element_edges(self.nnode, ne, _p(m.elem), _p(self.eedge)))
+        nd = ng = 3 if degree == 1 else 6
+        self.nd, self.ng = nd, ng
+        self.ndof = self.nnode if degree == 1 else self.nnode + self.nedge
+        self.ngauss = ng * ne
+        xyz = np.zeros((self.nnode, 3))
+        xyz[:, :2] = m.coords
+        self.dof = np.empty((ne, nd), np.int32)
+        self.w = np.empty((ne, ng))
+        self.h = np.empty((ne, ng, nd))
+        self.hx = np.empty((ne, ng, nd))
+        self.hy = np.empty((ne, ng, nd))
+        self.hs = np.empty((ne, ng, 3))
+        self.gx = np.empty((ne, ng))
+        self.gy = np.empty((ne, ng))
+        lib().orc_space_tables(degree, self.nnode, _p(xyz), ne, _p(m.elem), _p(self.eedge), _p(m.area), _p(m.hx),
+                               _p(m.hy), _p(self.dof), _p(self.w), _p(self.h), _p(self.hx), _p(self.hy), _p(self.hs),
+                               _p(self.gx), _p(self.gy))
+
+    def gauss_nodes(self):
+        return np.stack([self.gx.ravel(), self.gy.ravel()], axis=1)
+
+    def connectivity1(self):
+        return self.dof.astype(np.int64) + 1
+
+    def dof_nodes(self):
+        """Coordinates of the DOFs: vertices, then edge midpoints (P2)."""
+        xy = self.p1.coords
+        if self.degree == 1:
+            return xy.copy()
+        mid = np.empty((self.nedge, 2))
+        for j in range(3):
+            a, b = self.p1.elem[:, j], self.p1.elem[:, (j + 1) % 3]
+            mid[self.eedge[:, j]] = 0.5 * (xy[a] + xy[b])
+        return np.concatenate([xy, mid])
+
+    def _args(self):
+        return self.nelem, self.nd, self.ng
+
+    def laplace_coo(self, kappa):
+        kappa = _c(kappa, np.float64)
+        N = self.nd * self.nd * self.ngauss
+        idx = np.empty(2 * N, np.int64)
+        vv = np.empty(N)
+        lib().orc_gen_laplace_coo(*self._args(), _p(self.dof), _p(self.w), _p(self.hx), _p(self.hy), _p(kappa),
+                                  _p(idx), _p(vv))
+        return idx.reshape(-1, 2), vv
+
+    def laplace_coo_backward(self, grad_vv):
+        g = _c(grad_vv, np.float64)
+        out = np.empty(self.ngauss)
+        lib().orc_gen_laplace_coo_backward(*self._args(), _p(self.w), _p(self.hx), _p(self.hy), _p(g), _p(out))
+        return out
+
+    def laplace_csc(self, kappa):
+        idx, vv = self.laplace_coo(kappa)
+        return coo_to_csc(idx, vv, self.ndof)
+
+    def mass_coo(self, rho):
+        rho = _c(rho, np.float64)
+        N = self.nd * self.nd * self.ngauss
+        idx = np.empty(2 * N, np.int64)
+        vv = np.empty(N)
+        lib().orc_gen_mass_coo(*self._args(), _p(self.dof), _p(self.w), _p(self.h), _p(rho), _p(idx), _p(vv))
+        return idx.reshape(-1, 2), vv
+
+    def mass_coo_backward(self, grad_vv):
+        g = _c(grad_vv, np.float64)
+        out = np.empty(self.ngauss)
+        lib().orc_gen_mass_coo_backward(*self._args(), _p(self.w), _p(self.h), _p(g), _p(out))
+        return out
+
+    def mass_csc(self, rho):
+        idx, vv = self.mass_coo(rho)
+        return coo_to_csc(idx, vv, self.ndof)
+
+    def source(self, f, rhs=None):
+        f = _c(f, np.float64)
+        out = np.zeros(self.ndof) if rhs is None else np.array(rhs, dtype=np.float64, copy=True)
+        lib().orc_gen_source(*self._args(), _p(self.dof), _p(self.w), _p(self.h), _p(f), _p(out))
+        return out
+
+    def source_backward(self, grad_rhs):
+        g = _c(grad_rhs, np.float64)
+        out = np.empty(self.ngauss)
+        lib().orc_gen_source_backward(*self._args(), _p(self.dof), _p(self.w), _p(self.h), _p(g), _p(out))
+        return out
+
+    def stiffness_coo(self, D):
+        D = _c(D, np.float64)
+        N = 4 * self.nd * self.nd * self.ngauss
+        idx = np.empty(2 * N, np.int64)
+        vv = np.empty(N)
+        lib().orc_gen_stiffness_coo(*self._args(), self.ndof, _p(self.dof), _p(self.w), _p(self.hx), _p(self.hy),
+                                    _p(D), _p(idx), _p(vv))
+        return idx.reshape(-1, 2), vv
+
+    def stiffness_coo_backward(self, grad_vv):
+        g = _c(grad_vv, np.float64)
+        out = np.empty(9 * self.ngauss)
+        lib().orc_gen_stiffness_coo_backward(*self._args(), _p(self.w), _p(self.hx), _p(self.hy), _p(g), _p(out))
+        return out
+
+    def stiffness_csc(self, D):
+        idx, vv = self.stiffness_coo(D)
+        return coo_to_csc(idx, vv, 2 * self.ndof)
+
+    def fem_to_gauss(self, u):
+        u = _c(u, np.float64)
+        out = np.empty(self.ngauss)
+        lib().orc_fem_to_gauss(self.nelem, self.ng, _p(self.p1.elem), _p(self.hs), _p(u), _p(out))
+        return out
+
+    def fem_to_gauss_backward(self, grad_out, nu=None):
+        g = _c(grad_out, np.float64)
+        out = np.zeros(self.nnode if nu is None else nu)
+        lib().orc_fem_to_gauss_backward(self.nelem, self.ng, _p(self.p1.elem), _p(self.hs), _p(g), _p(out))
+        return out
+
+    def dof_to_gauss(self, u):
+        u = _c(u, np.float64)
+        out = np.empty(self.ngauss)
+        lib().orc_dof_to_gauss(*self._args(), _p(self.dof), _p(self.h), _p(u), _p(out))
+        return out
+
+    def dof_to_gauss_backward(self, grad_out):
+        g = _c(grad_out, np.float64)
+        out = np.zeros(self.ndof)
+        lib().orc_dof_to_gauss_backward(*self._args(), _p(self.dof), _p(self.h), _p(g), _p(out))
+        return out
+
+    def bcnode(self):
+        if self.degree == 1:
+            return self.p1.bcnode()
+        n = lib().orc_bcnode_p2(self.nnode, self.nelem, _p(self.p1.elem), _p(self.eedge), self.nedge, None)
+        out = np.empty(n, np.int64)
+        lib().orc_bcnode_p2(self.nnode, self.nelem, _p(self.p1.elem), _p(self.eedge), self.nedge, _p(out))
         return out
 
 

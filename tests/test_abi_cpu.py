@@ -22,7 +22,8 @@ def test_header_declares_reference_symbols():
     for s in ("init_nnfem_mesh", "mfem_get_ngauss", "mfem_get_gauss", "mfem_get_gauss_weights", "mfem_get_area",
               "mfem_get_elem_ndof", "mfem_get_ndof", "mfem_get_connectivity", "mfem_get_element_to_vertices",
               "FemLaplaceScalar_forward_Julia", "FemSourceScalar_forward_Julia",
-              "ComputeFemStiffnessMatrixMfem_forward_Julia"):
+              "ComputeFemStiffnessMatrixMfem_forward_Julia", "FemToGaussPointsMfem_Julia",
+              "DofToGaussPointsMfem_forward_Julia"):
         assert s in syms, s
 
 
@@ -61,6 +62,8 @@ def test_invalid_arguments_rejected_on_host(gpulib):
     st = L.adfem_mesh_create(_lib.ptr(xyz), 3, _lib.ptr(el), 1, 1, ctypes.byref(h))
     assert st == _lib.ERR_INVALID
     st = L.adfem_mesh_create(_lib.ptr(xyz), 3, _lib.ptr(el), 1, 2, ctypes.byref(h))
+    assert st == _lib.ERR_INVALID  # P2 meshes check their vertices the same way
+    st = L.adfem_mesh_create(_lib.ptr(xyz), 3, _lib.ptr(el), 1, 3, ctypes.byref(h))
     assert st == _lib.ERR_UNSUPPORTED
     cnt = ctypes.c_longlong()
     cp = np.array([1, 2, 3], np.int64)

@@ -1,0 +1,263 @@
+"""GPU parity of the degree-generic ops (P2 Laplace/source/stiffness, mass matrix,
+Gauss-point interpolation) through the C ABI against the CPU oracle.
+
+Same bar as the P1 parity tests: patterns and COO indices bit-exact; values within
+1e-12 relative to their row maximum (matrices) or their max norm (vectors).
+"""
+import ctypes
+
+import numpy as np
+import pytest
+
+from adfem_gpu import synth
+
+pytestmark = pytest.mark.gpu
+TOL = 1e-12
+
+
+def row_scaled_err(A, B):
+    import scipy.sparse as sp
+
+    A = sp.csr_matrix(A)
+    B = sp.csr_matrix(B)
+    d = abs(A - B).max(axis=1).toarray().ravel()
+    s = abs(B).max(axis=1).toarray().ravel()
+    s[s == 0] = 1.0
+    return float(np.max(d / s))
+
+
+def rel(a, b):
+    return float(np.max(np.abs(np.asarray(a) - np.asarray(b))) / max(np.max(np.abs(b)), 1e-300))
+
+
+def spaces(oracle, gpulib, m, degree, seed=0, jitter=0.2):
+    coords, elems = synth.jittered_square(m, seed=seed, jitter=jitter)
+    return oracle.OracleSpace(coords, elems, degree), gpulib.Mesh(coords, elems, degree=degree)
+
+
+@pytest.mark.parametrize("degree", [1, 2])
+@pytest.mark.parametrize("m,jitter", [(1, 0.0), (2, 0.0), (9, 0.2), (24, 0.2)])
+def test_space_mesh_runtime(oracle, gpulib, degree, m, jitter):
+    O, G = spaces(oracle, gpulib, m, degree, 0, jitter)
+    assert (G.ndof, G.elem_ndof, gpulib.get_ngauss(G)) == (O.ndof, O.nd, O.ngauss)
+    np.testing.assert_array_equal(G.conn, O.connectivity1())
+    np.testing.assert_allclose(gpulib.gauss_nodes(G), O.gauss_nodes(), rtol=0, atol=1e-15)
+    np.testing.assert_allclose(gpulib.gauss_weights(G), O.w.ravel(), rtol=1e-15)
+    np.testing.assert_array_equal(gpulib.bcnode(G), O.bcnode())
+    np.testing.assert_allclose(gpulib.dof_nodes(G), O.dof_nodes(), rtol=0, atol=1e-15)
+    K = O.laplace_csc(np.ones(O.ngauss))
+    cp, rv = G.pattern()
+    np.testing.assert_array_equal(cp - 1, K.indptr)
+    np.testing.assert_array_equal(rv - 1, K.indices)
+    Ks = O.stiffness_csc(np.tile(np.eye(3), (O.ngauss, 1, 1)))
+    cp2, rv2 = G.pattern_elasticity()
+    np.testing.assert_array_equal(cp2 - 1, Ks.indptr)
+    np.testing.assert_array_equal(rv2 - 1, Ks.indices)
+
+
+@pytest.mark.parametrize("m,seed", [(7, 0), (20, 3)])
+def test_p2_summed_operators(oracle, gpulib, m, seed):
+    O, G = spaces(oracle, gpulib, m, 2, seed)
+    g = O.gauss_nodes()
+    rng = np.random.default_rng(seed)
+    kappa = np.sin(g[:, 0]) * (1 + g[:, 1] ** 2) + 1
+    A = gpulib.compute_fem_laplace_matrix1(kappa, G)
+    B = O.laplace_csc(kappa)
+    np.testing.assert_array_equal(A.indptr, B.indptr)
+    np.testing.assert_array_equal(A.indices, B.indices)
+    assert row_scaled_err(A, B) < TOL
+    f = 1e5 * (g[:, 0] + g[:, 1])
+    assert rel(gpulib.compute_fem_source_term1(f, G), O.source(f)) < TOL
+    D = rng.random((O.ngauss, 3, 3)) + np.eye(3)  # not symmetric: checks the CSC transpose
+    As = gpulib.compute_fem_stiffness_matrix(D, G)
+    Bs = O.stiffness_csc(D)
+    np.testing.assert_array_equal(As.indptr, Bs.indptr)
+    np.testing.assert_array_equal(As.indices, Bs.indices)
+    assert row_scaled_err(As, Bs) < TOL
+
+
+@pytest.mark.parametrize("degree", [1, 2])
+def test_mass_matrix(oracle, gpulib, degree):
+    import torch
+
+    from adfem_gpu import system as S
+
+    O, G = spaces(oracle, gpulib, 13, degree, 2)
+    rho = 1 + np.random.default_rng(5).random(O.ngauss)
+    A = gpulib.compute_fem_mass_matrix1(rho, G)
+    B = O.mass_csc(rho)
+    np.testing.assert_array_equal(A.indptr, B.indptr)
+    np.testing.assert_array_equal(A.indices, B.indices)
+    assert row_scaled_err(A, B) < TOL
+    A1 = gpulib.compute_fem_mass_matrix1(G)
+    assert abs(A1.sum() - 1.0) < 1e-13
+    assert gpulib.compute_fem_mass_matrix(G).shape == (2 * G.ndof, 2 * G.ndof)
+    v = S.mass_csr(G, torch.tensor(rho, device="cuda")).cpu().numpy()
+    np.testing.assert_array_equal(v, A.data)  # symmetric pattern and values: CSR == CSC
+    idx, vv = S.mass_coo(G, torch.tensor(rho, device="cuda"))
+    oi, ov = O.mass_coo(rho)
+    np.testing.assert_array_equal(idx.cpu().numpy(), oi)
+    assert rel(vv.cpu().numpy(), ov) < TOL
+    gvv = np.random.default_rng(6).standard_normal(ov.size)
+    gr = S.mass_coo_backward(G, torch.tensor(gvv, device="cuda")).cpu().numpy()
+    assert rel(gr, O.mass_coo_backward(gvv)) < TOL
+
+
+def test_p2_coo_and_backward(oracle, gpulib):
+    import torch
+
+    from adfem_gpu import system as S
+
+    O, G = spaces(oracle, gpulib, 9, 2, 1)
+    rng = np.random.default_rng(7)
+    kappa = 1 + rng.random(O.ngauss)
+    idx, vv = S.laplace_coo(G, torch.tensor(kappa, device="cuda"))
+    oi, ov = O.laplace_coo(kappa)
+    np.testing.assert_array_equal(idx.cpu().numpy(), oi)
+    assert rel(vv.cpu().numpy(), ov) < TOL
+    gvv = rng.standard_normal(ov.size)
+    gk = S.laplace_coo_backward(G, torch.tensor(gvv, device="cuda")).cpu().numpy()
+    assert rel(gk, O.laplace_coo_backward(gvv)) < TOL
+    gr = rng.standard_normal(O.ndof)
+    gf = S.source_backward(G, torch.tensor(gr, device="cuda")).cpu().numpy()
+    assert rel(gf, O.source_backward(gr)) < TOL
+    D = rng.random(9 * O.ngauss)
+    idx2, vv2 = S.stiffness_coo(G, torch.tensor(D, device="cuda"))
+    oi2, ov2 = O.stiffness_coo(D)
+    np.testing.assert_array_equal(idx2.cpu().numpy(), oi2)
+    assert rel(vv2.cpu().numpy(), ov2) < TOL
+    gvv2 = rng.standard_normal(ov2.size)
+    gD = S.stiffness_coo_backward(G, torch.tensor(gvv2, device="cuda")).cpu().numpy()
+    assert rel(gD, O.stiffness_coo_backward(gvv2)) < TOL
+
+
+@pytest.mark.parametrize("degree", [1, 2])
+def test_interpolation(oracle, gpulib, degree):
+    import torch
+
+    from adfem_gpu import system as S
+
+    O, G = spaces(oracle, gpulib, 11, degree, 4)
+    rng = np.random.default_rng(9)
+    un = rng.standard_normal(O.nnode)
+    ud = rng.standard_normal(O.ndof)
+    assert rel(gpulib.fem_to_gauss_points(un, G), O.fem_to_gauss(un)) < TOL
+    assert rel(gpulib.dof_to_gauss_points(ud, G), O.dof_to_gauss(ud)) < TOL
+    assert rel(S.fem_to_gauss(G, torch.tensor(un, device="cuda")).cpu().numpy(), O.fem_to_gauss(un)) < TOL
+    assert rel(S.dof_to_gauss(G, torch.tensor(ud, device="cuda")).cpu().numpy(), O.dof_to_gauss(ud)) < TOL
+    go = rng.standard_normal(O.ngauss)
+    gt = torch.tensor(go, device="cuda")
+    # transposes: overwrite (entries past the vertices zeroed), then accumulate
+    gu = S.fem_to_gauss_backward(G, gt, nu=O.ndof).cpu().numpy()
+    assert rel(gu, O.fem_to_gauss_backward(go, O.ndof)) < TOL
+    base = torch.tensor(ud, device="cuda")
+    acc = S.fem_to_gauss_backward(G, gt, grad_u=base.clone()).cpu().numpy()
+    want = ud.copy()
+    want[:O.nnode] += O.fem_to_gauss_backward(go)
+    assert rel(acc, want) < TOL
+    gd = S.dof_to_gauss_backward(G, gt).cpu().numpy()
+    assert rel(gd, O.dof_to_gauss_backward(go)) < TOL
+    acc2 = S.dof_to_gauss_backward(G, gt, grad_u=base.clone()).cpu().numpy()
+    assert rel(acc2, ud + O.dof_to_gauss_backward(go)) < TOL
+    # DofToGaussPoints/test.jl: exact for 2x^2 + y on P2 (linear f on P1)
+    f = (lambda x, y: 2 * x ** 2 + y) if degree == 2 else (lambda x, y: 3 * x - y)
+    fg = gpulib.dof_to_gauss_points(gpulib.eval_f_on_dof_pts(f, G), G)
+    assert np.abs(fg - gpulib.eval_f_on_gauss_pts(f, G)).max() < 1e-13
+
+
+def test_legacy_p2_layer(oracle, gpulib):
+    """The libadmfem symbols on a P2 current mesh, driven like src/MFEM/MFEM.jl:92-106."""
+    from adfem_gpu import _lib
+
+    L = _lib.load()
+    coords, elems = synth.jittered_square(5, seed=9)
+    O = oracle.OracleSpace(coords, elems, 2)
+    c = np.concatenate([coords, np.zeros((coords.shape[0], 1))], 1).ravel()
+    e = np.ascontiguousarray((elems - 1).ravel(), np.int32)
+    ned = np.zeros(1, np.int64)
+    p = L.init_nnfem_mesh(_lib.ptr(c), coords.shape[0], _lib.ptr(e), elems.shape[0], -1, -1, 2, _lib.ptr(ned))
+    assert p
+    edges = np.ctypeslib.as_array(p, shape=(2 * ned[0],)).copy()
+    ctypes.CDLL(None).free(ctypes.cast(p, ctypes.c_void_p))
+    np.testing.assert_array_equal(edges.reshape(2, -1).T, O.p1.edges())
+    assert L.mfem_get_ngauss() == O.ngauss and L.mfem_get_ndof() == O.ndof and L.mfem_get_elem_ndof() == 6
+    x, y, w = np.empty(O.ngauss), np.empty(O.ngauss), np.empty(O.ngauss)
+    L.mfem_get_gauss(_lib.ptr(x), _lib.ptr(y))
+    L.mfem_get_gauss_weights(_lib.ptr(w))
+    np.testing.assert_allclose(np.stack([x, y], 1), O.gauss_nodes(), atol=1e-15)
+    np.testing.assert_allclose(w, O.w.ravel(), rtol=1e-15)
+    conn = np.empty(6 * O.nelem, np.int64)
+    L.mfem_get_connectivity(_lib.ptr(conn))
+    np.testing.assert_array_equal(conn.reshape(-1, 6), O.connectivity1())
+    rng = np.random.default_rng(0)
+    kappa = 1 + rng.random(O.ngauss)
+    N = 36 * O.ngauss
+    idx, vv = np.zeros(2 * N, np.int64), np.zeros(N)
+    L.FemLaplaceScalar_forward_Julia(_lib.ptr(idx), _lib.ptr(vv), _lib.ptr(kappa))
+    oi, ov = O.laplace_coo(kappa)
+    np.testing.assert_array_equal(idx.reshape(-1, 2), oi)
+    assert rel(vv, ov) < TOL
+    L.ComputeFemMassMatrix1_forward(_lib.ptr(idx), _lib.ptr(vv), _lib.ptr(kappa))
+    oi, ov = O.mass_coo(kappa)
+    np.testing.assert_array_equal(idx.reshape(-1, 2), oi)
+    assert rel(vv, ov) < TOL
+    gvv = rng.standard_normal(N)
+    gr = np.empty(O.ngauss)
+    L.ComputeFemMassMatrix1_backward(_lib.ptr(gr), _lib.ptr(gvv), None, None)
+    assert rel(gr, O.mass_coo_backward(gvv)) < TOL
+    L.FemLaplaceScalar_backward(_lib.ptr(gr), _lib.ptr(gvv), None, None, None)
+    assert rel(gr, O.laplace_coo_backward(gvv)) < TOL
+    rhs = np.ones(O.ndof)  # accumulates into the caller's array
+    L.FemSourceScalar_forward_Julia(_lib.ptr(rhs), _lib.ptr(kappa))
+    assert rel(rhs, O.source(kappa, np.ones(O.ndof))) < TOL
+    D = rng.random(9 * O.ngauss)
+    N2 = 144 * O.ngauss
+    idx2, vv2 = np.zeros(2 * N2, np.int64), np.zeros(N2)
+    L.ComputeFemStiffnessMatrixMfem_forward_Julia(_lib.ptr(idx2), _lib.ptr(vv2), _lib.ptr(D))
+    oi2, ov2 = O.stiffness_coo(D)
+    np.testing.assert_array_equal(idx2.reshape(-1, 2), oi2)
+    assert rel(vv2, ov2) < TOL
+    un, ud = rng.standard_normal(O.nnode), rng.standard_normal(O.ndof)
+    out = np.empty(O.ngauss)
+    L.FemToGaussPointsMfem_Julia(_lib.ptr(out), _lib.ptr(un))
+    assert rel(out, O.fem_to_gauss(un)) < TOL
+    L.DofToGaussPointsMfem_forward_Julia(_lib.ptr(out), _lib.ptr(ud))
+    assert rel(out, O.dof_to_gauss(ud)) < TOL
+    go = rng.standard_normal(O.ngauss)
+    gu = np.ones(O.ndof)
+    L.DofToGaussPointsMfem_backward(_lib.ptr(gu), _lib.ptr(go), None, None)
+    assert rel(gu, 1 + O.dof_to_gauss_backward(go)) < TOL
+    gn = np.ones(O.nnode)
+    L.FemToGaussPointsMfem_backward(_lib.ptr(gn), _lib.ptr(go), None, None)
+    assert rel(gn, 1 + O.fem_to_gauss_backward(go)) < TOL
+    L.adfem_set_current_mesh(None)
+
+
+def test_p2_poisson_exact_for_quadratics(oracle, gpulib):
+    """-lap u = -6 with u = 1 + x^2 + 2 y^2 on the boundary: the P2 solution equals u at
+    every DOF (quadratics are in the space), through assembly, Dirichlet and K\\F."""
+    coords, elems = synth.jittered_square(16, seed=2)
+    G = gpulib.Mesh(coords, elems, degree=2)
+    O = oracle.OracleSpace(coords, elems, 2)
+    ng = gpulib.get_ngauss(G)
+    K = gpulib.compute_fem_laplace_matrix1(np.ones(ng), G)
+    F = gpulib.compute_fem_source_term1(np.full(ng, -6.0), G)
+    ue = gpulib.eval_f_on_dof_pts(lambda x, y: 1 + x ** 2 + 2 * y ** 2, G)
+    bd = gpulib.bcnode(G)
+    A, r = gpulib.impose_Dirichlet_boundary_conditions(K, F, bd, ue[bd - 1])
+    u = gpulib.solve(A, r, rtol=1e-14)
+    assert np.abs(u - ue).max() < 1e-10
+    Ao, ro = oracle.dirichlet_csc(O.laplace_csc(np.ones(ng)), O.source(np.full(ng, -6.0)), bd, ue[bd - 1])
+    uo = oracle.spsolve(Ao, ro)
+    assert np.abs(u - uo).max() < 1e-10
+
+
+def test_p2_input_checks(gpulib):
+    coords, elems = synth.jittered_square(3, seed=0)
+    G = gpulib.Mesh(coords, elems, degree=2)
+    with pytest.raises(gpulib.AdFemError):
+        gpulib.compute_fem_laplace_matrix1(np.ones(3 * G.nelem), G)  # P1 length on a P2 mesh
+    with pytest.raises(gpulib.AdFemError):
+        gpulib.PoissonSystem(G)  # resident systems are P1
+    with pytest.raises(gpulib.AdFemError):
+        gpulib.Mesh(coords, elems, degree=2, order=2)

@@ -284,7 +284,7 @@ def test_error_paths(gpulib):
     with pytest.raises(AdFemError):
         gpulib.compute_fem_laplace_matrix1(np.ones(5), G)
     with pytest.raises(AdFemError):
-        gpulib.Mesh(coords, elems, degree=2)
+        gpulib.Mesh(coords, elems, degree=3)
     bad = np.array([[1, 2, 2]])
     with pytest.raises(AdFemError):
         gpulib.Mesh(coords, bad)
