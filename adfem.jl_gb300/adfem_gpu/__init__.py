@@ -37,7 +37,8 @@ __all__ = [
     "impose_Dirichlet_boundary_conditions", "impose_Dirichlet_coo", "impose_Dirichlet_coo_backward",
     "solve", "solver_opts", "get_connectivity", "gauss_weights", "dof_nodes", "eval_f_on_gauss_pts",
     "eval_f_on_fem_pts", "eval_f_on_dof_pts", "compute_fem_mass_matrix1", "compute_fem_mass_matrix",
-    "fem_to_gauss_points", "dof_to_gauss_points", "P1", "P2",
+    "fem_to_gauss_points", "dof_to_gauss_points", "P1", "P2", "pcl_compute_fem_laplace_matrix1",
+    "pcl_impose_Dirichlet_boundary_conditions",
 ]
 
 P1 = 1
@@ -298,6 +299,31 @@ def compute_fem_mass_matrix(rho, mesh: Mesh | None = None):
     """[M 0; 0 M] for the two displacement components (MCore.jl:183-193)."""
     M = compute_fem_mass_matrix1(rho, mesh)
     return sp.block_diag([M, M], format="csc")
+
+
+def pcl_compute_fem_laplace_matrix1(mesh: Mesh):
+    """J[i, j] = d v_j / d kappa_i for v the unsummed Laplace COO values (src/pcl.jl:24-39)."""
+    ng = get_ngauss(mesh)
+    J = np.zeros((ng, mesh.elem_ndof ** 2 * ng), order="F")
+    check(_lib_().adfem_pcl_laplace_jacobian(mesh.handle, ptr(J)), "pcl_compute_fem_laplace_matrix1")
+    return J
+
+
+def pcl_impose_Dirichlet_boundary_conditions(indices, bdnode, outdof: int):
+    """J[i, j] = d (v_B)_j / d (v_A)_i of the COO Dirichlet arm; indices 1-based (n_A, 2) (src/pcl.jl:1-21)."""
+    idx = np.asarray(indices, dtype=np.int64)
+    sN = idx.shape[0]
+    i0 = _c(idx - 1, np.int64).reshape(-1)
+    bd = _c(bdnode, np.int64).ravel()
+    N = int(max(idx.max(initial=0), bd.max(initial=0)))
+    pos = np.empty(sN, np.int64)
+    nk = ctypes.c_longlong()
+    check(_lib_().adfem_pcl_dirichlet(ptr(i0), sN, ptr(bd), bd.size, N, ptr(pos), ctypes.byref(nk)),
+          "pcl_impose_Dirichlet_boundary_conditions")
+    J = np.zeros((sN, outdof))
+    k = np.nonzero(pos >= 0)[0]
+    J[k, pos[k]] = 1.0
+    return J
 
 
 def fem_to_gauss_points(u, mesh: Mesh):

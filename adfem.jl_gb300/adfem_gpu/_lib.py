@@ -101,6 +101,8 @@ SIGNATURES = {
     "DofToGaussPointsMfem_forward_Julia": (None, [c_p, c_p]),
     "DofToGaussPointsMfem_forward": (None, [c_p, c_p]),
     "DofToGaussPointsMfem_backward": (None, [c_p, c_p, c_p, c_p]),
+    "pcl_FemLaplaceScalar_Jacobian": (None, [c_p]),
+    "pcl_ImposeDirichlet": (None, [c_p, c_p, c_p, c_i, c_i]),
     "PlaneStrainMatrix_forward": (None, [c_p, c_p, c_p, c_i]),
     "PlaneStrainMatrix_backward": (None, [c_p, c_p, c_p, c_p, c_p, c_i]),
     "PlaneStressMatrix_forward": (None, [c_p, c_p, c_p, c_i]),
@@ -124,6 +126,9 @@ SIGNATURES = {
     "adfem_mass_csr_d": (c_i, [c_p, c_p, c_p, c_p]),
     "adfem_mass_coo_d": (c_i, [c_p, c_p, c_p, c_p, c_p]),
     "adfem_mass_coo_backward_d": (c_i, [c_p, c_p, c_p, c_p]),
+    "adfem_pcl_laplace_jacobian": (c_i, [c_p, c_p]),
+    "adfem_pcl_laplace_jacobian_d": (c_i, [c_p, c_p, c_p]),
+    "adfem_pcl_dirichlet": (c_i, [c_p, c_ll, c_p, c_ll, c_ll, c_p, c_p]),
     "adfem_fem_to_gauss": (c_i, [c_p, c_p, c_ll, c_p]),
     "adfem_dof_to_gauss": (c_i, [c_p, c_p, c_ll, c_p]),
     "adfem_fem_to_gauss_d": (c_i, [c_p, c_p, c_p, c_p]),

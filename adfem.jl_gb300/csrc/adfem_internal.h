@@ -256,6 +256,11 @@ cudaError_t launch_gen_to_gauss(const Mesh& m, const Space& sp, bool vertex_only
 cudaError_t launch_gen_to_gauss_backward(const Mesh& m, const Space& sp, bool vertex_only, const double* grad_out,
                                          double* grad_u, bool accumulate, cudaStream_t st);
 
+cudaError_t launch_fill(int64_t n, double v, double* out, cudaStream_t st);
+// dense column-major Jacobian of the unsummed Laplace COO values with respect to kappa:
+// H[gp + nz * ng] = vv[nz] (vv: COO values at kappa = 1, nd2 per Gauss point)
+cudaError_t launch_pcl_scatter(int64_t N, int nd2, int64_t ng, const double* vv, double* H, cudaStream_t st);
+
 // Device bytes held by a resident system (operator copies, Dirichlet data, solver
 // vectors) -- what the serving loop counts against its HBM budget.
 size_t system_device_bytes(const adfem_system* s);

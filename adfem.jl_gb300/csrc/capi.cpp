@@ -415,6 +415,70 @@ int adfem_dof_to_gauss(adfem_mesh* mesh, const double* u, long long nu, double* 
   return to_gauss_host(mesh, false, u, nu, out);
 }
 
+// ------------------------------------------------------------------ PCL Jacobians
+// Values of the Laplace COO at kappa = 1 (nd^2 per Gauss point) in vv; the dense
+// Jacobian holds them at (gp, nz) (FemLaplaceScalar.h:63-91).
+static int pcl_laplace_values(Mesh& m, Space& sp, DevBuf& vv, int64_t* N, cudaStream_t st) {
+  const int64_t ng = mesh_ngauss(m);
+  *N = (int64_t)sp.nd * sp.nd * ng;
+  DevBuf ones, idx;
+  ADFEM_TRY(ones.alloc(sizeof(double) * (size_t)std::max<int64_t>(ng, 1)));
+  ADFEM_TRY(idx.alloc(sizeof(long long) * 2 * (size_t)std::max<int64_t>(*N, 1)));
+  ADFEM_TRY(vv.alloc(sizeof(double) * (size_t)std::max<int64_t>(*N, 1)));
+  ADFEM_TRY(kerr(launch_fill(ng, 1.0, ones.as<double>(), st), "fill"));
+  ADFEM_TRY(kerr(launch_gen_coo(m, sp, GenOp::LAPLACE, ones.as<double>(), idx.as<long long>(), vv.as<double>(), st),
+                 "laplace coo"));
+  ADFEM_CUDA(cudaStreamSynchronize(st));
+  return ADFEM_OK;
+}
+
+int adfem_pcl_laplace_jacobian_d(adfem_mesh* mesh, double* H_d, void* stream) {
+  if (!mesh || !H_d) return fail(ADFEM_ERR_INVALID, "null argument");
+  Mesh& m = *mesh->m;
+  Space* sp = nullptr;
+  ADFEM_TRY(get_space(m, m.degree, &sp));
+  DevBuf vv;
+  int64_t N = 0;
+  ADFEM_TRY(pcl_laplace_values(m, *sp, vv, &N, S(stream)));
+  ADFEM_TRY(kerr(launch_pcl_scatter(N, sp->nd * sp->nd, mesh_ngauss(m), vv.as<double>(), H_d, S(stream)), "scatter"));
+  ADFEM_CUDA(cudaStreamSynchronize(S(stream)));
+  return ADFEM_OK;
+}
+
+int adfem_pcl_laplace_jacobian(adfem_mesh* mesh, double* H) {
+  if (!mesh || !H) return fail(ADFEM_ERR_INVALID, "null argument");
+  Mesh& m = *mesh->m;
+  Space* sp = nullptr;
+  ADFEM_TRY(get_space(m, m.degree, &sp));
+  DevBuf vv;
+  int64_t N = 0;
+  ADFEM_TRY(pcl_laplace_values(m, *sp, vv, &N, nullptr));
+  std::vector<double> v((size_t)N);
+  ADFEM_TRY(to_host(v.data(), vv, (size_t)N));
+  const int64_t ng = mesh_ngauss(m), nd2 = (int64_t)sp->nd * sp->nd;
+  for (int64_t nz = 0; nz < N; nz++) H[nz / nd2 + nz * ng] = v[nz];  // only the nonzeros are written
+  return ADFEM_OK;
+}
+
+int adfem_pcl_dirichlet(const long long* indices, long long sN, const long long* bd, long long nbd, long long N,
+                        long long* pos, long long* nkeep) {
+  if (sN < 0 || N < 0 || !nkeep || (sN > 0 && (!indices || !pos)) || (nbd > 0 && !bd))
+    return fail(ADFEM_ERR_INVALID, "bad arguments");
+  std::vector<uint8_t> tag(std::max<long long>(N, 1), 0);
+  for (long long q = 0; q < nbd; q++) {
+    if (bd[q] < 1 || bd[q] > N) return fail(ADFEM_ERR_INVALID, "bd index out of range");
+    tag[bd[q] - 1] = 1;
+  }
+  DevBuf di, isbd, dpos;
+  ADFEM_TRY(to_dev(di, indices, 2 * (size_t)sN));
+  ADFEM_TRY(to_dev(isbd, tag.data(), (size_t)std::max<long long>(N, 1)));
+  ADFEM_TRY(dpos.alloc(sizeof(int64_t) * (size_t)std::max<long long>(sN, 1)));
+  int64_t nk = 0;
+  ADFEM_TRY(pcl_dirichlet_device(sN, di.as<long long>(), isbd.as<uint8_t>(), N, dpos.as<int64_t>(), &nk, nullptr));
+  *nkeep = nk;
+  return to_host(pos, dpos, (size_t)sN);
+}
+
 int adfem_mesh_elements(const adfem_mesh* mesh, long long* elems1) {
   if (!mesh || !elems1) return fail(ADFEM_ERR_INVALID, "null argument");
   for (int64_t k = 0; k < 3 * mesh->m->ne; k++) elems1[k] = (long long)mesh->m->elem[k] + 1;
@@ -1321,6 +1385,40 @@ void DofToGaussPointsMfem_backward(double* grad_u, const double* grad_out, const
   (void)u;
   LEGACY_MESH("DofToGaussPointsMfem_backward", );
   legacy_report(legacy_to_gauss_backward(m, false, grad_u, grad_out), "DofToGaussPointsMfem_backward");
+}
+
+// pcl_FemLaplaceScalar_Jacobian (FemLaplaceScalar.h:63-91, caller src/pcl.jl:34-38): H is
+// the caller's zeroed ngauss x elem_ndof^2 ngauss column-major matrix
+void pcl_FemLaplaceScalar_Jacobian(double* H) {
+  LEGACY_MESH("pcl_FemLaplaceScalar_Jacobian", );
+  adfem_mesh h{m};
+  legacy_report(adfem_pcl_laplace_jacobian(&h, H), "pcl_FemLaplaceScalar_Jacobian");
+}
+
+// pcl_ImposeDirichlet (ImposeDirichlet.h:97-111, caller src/pcl.jl:14-21): indices is the
+// 1-based sN x 2 column-major index array of A, J the caller's zeroed sN x outdof
+// column-major matrix; J[k, s] = 1 for the s-th entry the Dirichlet op keeps.
+static int legacy_pcl_dirichlet(double* J, const long long* indices, const long long* bd, int bdN, int sN) {
+  if (sN < 0 || bdN < 0 || (sN > 0 && (!J || !indices)) || (bdN > 0 && !bd))
+    return fail(ADFEM_ERR_INVALID, "bad arguments");
+  std::vector<long long> idx0(2 * (size_t)sN);
+  long long N = 0;
+  for (int k = 0; k < sN; k++) {
+    idx0[2 * (size_t)k] = indices[k] - 1;
+    idx0[2 * (size_t)k + 1] = indices[k + (int64_t)sN] - 1;
+    N = std::max(N, std::max(indices[k], indices[k + (int64_t)sN]));
+  }
+  for (int q = 0; q < bdN; q++) N = std::max(N, bd[q]);
+  std::vector<long long> pos(std::max(sN, 1));
+  long long nkeep = 0;
+  ADFEM_TRY(adfem_pcl_dirichlet(idx0.data(), sN, bd, bdN, N, pos.data(), &nkeep));
+  for (int k = 0; k < sN; k++)
+    if (pos[k] >= 0) J[k + pos[k] * (int64_t)sN] = 1.0;
+  return ADFEM_OK;
+}
+
+void pcl_ImposeDirichlet(double* J, const long long* indices, const long long* bd, int bdN, int sN) {
+  legacy_report(legacy_pcl_dirichlet(J, indices, bd, bdN, sN), "pcl_ImposeDirichlet");
 }
 
 static int host_plane(int mode, const double* E, const double* nu, int N, double* out) {

@@ -239,6 +239,40 @@ int dirichlet_coo_device(int64_t sN, const long long* idx, const double* vv, con
 }
 
 // backward: grad_vv_in[k] = keep ? grad_vv[z_k] : 0, minus bdval_j grad_rhs_i on lift entries
+// pcl_ImposeDirichlet (deps/MFEM/ImposeDirichlet/ImposeDirichlet.h:97-111): output
+// position of every input entry the COO arm keeps (its exclusive keep-scan), -1 for the
+// dropped ones.
+__global__ void k_pcl_positions(int64_t sN, const longlong2* __restrict__ idx, const uint8_t* __restrict__ isbd,
+                                const int64_t* __restrict__ keep_pos, int64_t* __restrict__ pos) {
+  const int64_t k = gtid();
+  if (k >= sN) return;
+  const longlong2 ij = idx[k];
+  pos[k] = (isbd[ij.x] == 0 && isbd[ij.y] == 0) ? keep_pos[k] : -1;
+}
+
+int pcl_dirichlet_device(int64_t sN, const long long* idx, const uint8_t* isbd, int64_t N, int64_t* pos,
+                         int64_t* nkeep, cudaStream_t st) {
+  DevBuf keep, lift, bad;
+  ADFEM_TRY(keep.alloc(sizeof(int64_t) * (size_t)std::max<int64_t>(sN, 1)));
+  ADFEM_TRY(lift.alloc(sizeof(int64_t) * (size_t)std::max<int64_t>(sN, 1)));
+  ADFEM_TRY(bad.alloc(sizeof(int)));
+  ADFEM_CUDA(cudaMemsetAsync(bad.p, 0, sizeof(int), st));
+  const auto* ij = reinterpret_cast<const longlong2*>(idx);
+  k_coo_flags<<<nblk(sN, kT), kT, 0, st>>>(sN, ij, isbd, N, keep.as<int64_t>(), lift.as<int64_t>(), bad.as<int>());
+  ADFEM_CUDA(cudaGetLastError());
+  int hbad = 0;
+  ADFEM_CUDA(cudaMemcpyAsync(&hbad, bad.p, sizeof(int), cudaMemcpyDeviceToHost, st));
+  ADFEM_CUDA(cudaStreamSynchronize(st));
+  if (hbad) return fail(ADFEM_ERR_INVALID, "pcl_ImposeDirichlet: a COO index is outside [0, N)");
+  ADFEM_TRY(scan_counts(sN, keep.as<int64_t>(), nkeep, st));
+  if (sN > 0) {
+    k_pcl_positions<<<nblk(sN, kT), kT, 0, st>>>(sN, ij, isbd, keep.as<int64_t>(), pos);
+    ADFEM_CUDA(cudaGetLastError());
+  }
+  ADFEM_CUDA(cudaStreamSynchronize(st));
+  return ADFEM_OK;
+}
+
 __global__ void k_coo_backward(int64_t sN, const longlong2* __restrict__ idx, const uint8_t* __restrict__ isbd,
                                const int64_t* __restrict__ keep_pos, const double* __restrict__ gvv,
                                const double* __restrict__ bdval_dense, const double* __restrict__ grhs,

@@ -14,6 +14,9 @@ int dirichlet_coo_device(int64_t sN, const long long* idx, const double* vv, con
 int dirichlet_coo_backward_device(int64_t sN, const long long* idx, const uint8_t* isbd, int64_t N,
                                   const double* gvv, const double* bdval_dense, const double* grhs, double* gvv_in,
                                   cudaStream_t st);
+// positions of the kept COO entries in the output of the COO arm (-1: dropped)
+int pcl_dirichlet_device(int64_t sN, const long long* idx, const uint8_t* isbd, int64_t N, int64_t* pos,
+                         int64_t* nkeep, cudaStream_t st);
 cudaError_t launch_to0(int64_t n, const int64_t* a1, int64_t* a0, cudaStream_t st);
 cudaError_t launch_to1(int64_t n, const int64_t* a0, int64_t* a1, int64_t add, cudaStream_t st);
 }  // namespace adfem

@@ -551,7 +551,31 @@ __global__ void __launch_bounds__(kGT) k_gen_to_gauss_backward(int64_t nrow, con
   }
 }
 
+// ---------------------------------------------------------------- PCL
+__global__ void __launch_bounds__(kGT) k_fill(int64_t n, double v, double* __restrict__ out) {
+  for (int64_t i = gtid(); i < n; i += gstride()) out[i] = v;
+}
+
+// H[gp + nz * ng] = vv[nz] for the nd^2 entries nz of Gauss point gp (column-major
+// ngauss x nd^2 ngauss, pcl_FemLaplaceScalar_Jacobian, FemLaplaceScalar.h:63-91)
+__global__ void __launch_bounds__(kGT) k_pcl_scatter(int64_t N, int nd2, int64_t ng, const double* __restrict__ vv,
+                                                     double* __restrict__ H) {
+  for (int64_t nz = gtid(); nz < N; nz += gstride()) H[nz / nd2 + nz * ng] = vv[nz];
+}
+
 }  // namespace
+
+cudaError_t launch_fill(int64_t n, double v, double* out, cudaStream_t st) {
+  if (n <= 0) return cudaSuccess;
+  k_fill<<<grid_for(n), kGT, 0, st>>>(n, v, out);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_pcl_scatter(int64_t N, int nd2, int64_t ng, const double* vv, double* H, cudaStream_t st) {
+  if (N <= 0) return cudaSuccess;
+  k_pcl_scatter<<<grid_for(N), kGT, 0, st>>>(N, nd2, ng, vv, H);
+  return cudaGetLastError();
+}
 
 // ---------------------------------------------------------------- launchers
 #define GEN_DISPATCH(sp, KERNEL_CALL1, KERNEL_CALL2) \

@@ -120,6 +120,12 @@ ADFEM_API void FemToGaussPointsMfem_backward(double *grad_u, const double *grad_
 ADFEM_API void DofToGaussPointsMfem_forward(double *out, const double *u);
 ADFEM_API void DofToGaussPointsMfem_backward(double *grad_u, const double *grad_out, const double *out,
                                              const double *u);
+/* PCL helpers (src/pcl.jl:1-39).  FemLaplaceScalar.h:63-91: H = d vv / d kappa of the
+ * unsummed Laplace COO, column-major ngauss x elem_ndof^2 ngauss, only nonzeros written.
+ * ImposeDirichlet.h:97-111: J = d v_B / d v_A of the COO Dirichlet arm, column-major
+ * sN x outdof; indices 1-based sN x 2 column-major; only the ones are written. */
+ADFEM_API void pcl_FemLaplaceScalar_Jacobian(double *H);
+ADFEM_API void pcl_ImposeDirichlet(double *J, const long long *indices, const long long *bd, int bdN, int sN);
 /* deps/MFEM/PlaneStrainAndStress/PlaneStrainAndStress.h:5-78 (op plane_strain_and_stress,
  * mode 0 = strain with the reference's all-nine-entries formula, mode 1 = stress) */
 ADFEM_API void PlaneStrainMatrix_forward(double *out, const double *E, const double *nu, int N);
@@ -186,6 +192,17 @@ ADFEM_API int adfem_mass_csr_d(adfem_mesh *mesh, const double *rho_d, double *va
 ADFEM_API int adfem_mass_coo_d(adfem_mesh *mesh, const double *rho_d, long long *indices_d, double *vv_d,
                                void *stream);
 ADFEM_API int adfem_mass_coo_backward_d(adfem_mesh *mesh, const double *grad_vv_d, double *grad_rho_d, void *stream);
+
+/* ---- PCL Jacobians (src/pcl.jl:1-39) ----
+ * pcl_compute_fem_laplace_matrix1: H[gp, nz] = d vv_nz / d kappa_gp, dense column-major
+ * ngauss x (elem_ndof^2 ngauss) (host: only nonzeros written; device: the caller zeroes H).
+ * pcl_impose_Dirichlet_boundary_conditions: pos[k] = output position of input COO entry
+ * k (0-based (row, col) pairs, bd 1-based) in the COO Dirichlet arm, -1 if dropped; J is
+ * then J[k, pos[k]] = 1. */
+ADFEM_API int adfem_pcl_laplace_jacobian(adfem_mesh *mesh, double *H);
+ADFEM_API int adfem_pcl_laplace_jacobian_d(adfem_mesh *mesh, double *H_d, void *stream);
+ADFEM_API int adfem_pcl_dirichlet(const long long *indices, long long sN, const long long *bd, long long nbd,
+                                  long long N, long long *pos, long long *nkeep);
 
 /* ---- fem_to_gauss_points / dof_to_gauss_points (src/MFEM/MUtils.jl:231-275) ----
  * fem: u holds nodal values (nu >= nnode; P1 shape of the vertices); dof: u holds DOF

@@ -733,6 +733,45 @@ void orc_dirichlet_coo_backward(const double *grad_vv, const double *grad_rhs, c
   free(t);
 }
 
+/* pcl_FemLaplaceScalar_Jacobian, deps/MFEM/FemLaplace1/FemLaplaceScalar.h:63-91: H is
+ * column-major ngauss x (nd^2 ngauss); H[s + nz*ngauss] = (D D^T w)_pq for entry nz of
+ * Gauss point s.  Only these entries are written (the caller zeroes H). */
+void orc_pcl_laplace_jacobian(int ne, int nd, int ng, const double *w, const double *hx, const double *hy,
+                              double *H) {
+  const i64 ngauss = (i64)ng * ne;
+  i64 nz = 0;
+  for (int e = 0; e < ne; e++)
+    for (int k = 0; k < ng; k++) {
+      const i64 p = (i64)ng * e + k;
+      for (int a = 0; a < nd; a++)
+        for (int b = 0; b < nd; b++) {
+          double dd = hx[nd * p + a] * hx[nd * p + b] + hy[nd * p + a] * hy[nd * p + b];
+          H[p + nz * ngauss] = dd * w[p];
+          nz++;
+        }
+    }
+}
+
+/* pcl_ImposeDirichlet, deps/MFEM/ImposeDirichlet/ImposeDirichlet.h:97-111: indices is the
+ * 1-based sN x 2 column-major index array, J column-major sN x outdof (zeroed by the
+ * caller); J[k + s*sN] = 1 for the s-th entry whose row and column are both off bd. */
+void orc_pcl_dirichlet(double *J, const i64 *indices, const i64 *bd, int bdN, int sN) {
+  i64 *b = (i64 *)malloc(sizeof(i64) * (size_t)(bdN > 0 ? bdN : 1));
+  for (int q = 0; q < bdN; q++) b[q] = bd[q] - 1;
+  qsort(b, (size_t)bdN, sizeof(i64), cmp_i64);
+  i64 s = 0;
+  for (int k = 0; k < sN; k++) {
+    i64 i = indices[k] - 1, j = indices[k + sN] - 1;
+    int ini = bdN > 0 && bsearch(&i, b, (size_t)bdN, sizeof(i64), cmp_i64) != NULL;
+    int inj = bdN > 0 && bsearch(&j, b, (size_t)bdN, sizeof(i64), cmp_i64) != NULL;
+    if (!ini && !inj) {
+      J[k + s * sN] = 1.0;
+      s++;
+    }
+  }
+  free(b);
+}
+
 /*
  * COO -> CSC with Julia SparseArrays `sparse(I, J, V, m, n)` semantics
  * (src/MFEM/MCore.jl:118-119): duplicates summed in input order, row indices

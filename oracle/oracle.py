@@ -78,6 +78,8 @@ def lib():
             "orc_dof_to_gauss": (None, [_I, _I, _I, _P, _P, _P, _P]),
             "orc_dof_to_gauss_backward": (None, [_I, _I, _I, _P, _P, _P, _P]),
             "orc_bcnode_p2": (_L, [_I, _I, _P, _P, _L, _P]),
+            "orc_pcl_laplace_jacobian": (None, [_I, _I, _I, _P, _P, _P, _P]),
+            "orc_pcl_dirichlet": (None, [_P, _P, _P, _I, _I]),
         }
         for name, (res, args) in sig.items():
             f = getattr(L, name)
@@ -346,6 +348,12 @@ class OracleSpace:
         lib().orc_dof_to_gauss_backward(*self._args(), _p(self.dof), _p(self.h), _p(g), _p(out))
         return out
 
+    def pcl_laplace_jacobian(self):
+        """pcl_compute_fem_laplace_matrix1 (src/pcl.jl:24-39): dense ngauss x nd^2 ngauss."""
+        H = np.zeros((self.ngauss, self.nd * self.nd * self.ngauss), order="F")
+        lib().orc_pcl_laplace_jacobian(*self._args(), _p(self.w), _p(self.hx), _p(self.hy), _p(H))
+        return H
+
     def bcnode(self):
         if self.degree == 1:
             return self.p1.bcnode()
@@ -438,6 +446,16 @@ def dirichlet_csc(A, rhs, bd, bdval, keep_zeros: bool = False):
     lib().orc_dirichlet_csc(n, _p(colptr), _p(rowval), _p(nzval), _p(rhs), _p(bd), bd.size, _p(bdval),
                             int(keep_zeros), _p(oc), _p(orr), _p(ov), _p(orhs))
     return sp.csc_matrix((ov, orr, oc), shape=(n, n)), orhs
+
+
+def pcl_dirichlet(indices1, bd, outdof):
+    """pcl_impose_Dirichlet_boundary_conditions (src/pcl.jl:1-21): indices 1-based (sN, 2)."""
+    idx = np.asfortranarray(np.asarray(indices1, dtype=np.int64))
+    sN = idx.shape[0]
+    bd = _c(bd, np.int64).ravel()
+    J = np.zeros((sN, outdof), order="F")
+    lib().orc_pcl_dirichlet(_p(J), idx.ctypes.data_as(ctypes.c_void_p), _p(bd), bd.size, sN)
+    return J
 
 
 def spsolve(A, b):

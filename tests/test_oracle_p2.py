@@ -11,8 +11,8 @@ reads fenics/A.txt, A2.txt).  What they check is restated here as assertions:
     area/180 [6 -1 -1 0 -4 0; ...]) and the total mass = area;
 plus the closed-form P2 Laplace element matrix, the P2 patch test (K x^2 = -2 M 1 on
 interior rows: quadratics are in the space), the rigid-body null space of the P2
-elasticity operator, and the Taylor test of deps/MFEM/*/gradtest.jl (seed 233) for
-every backward.
+elasticity operator, the Taylor test of deps/MFEM/*/gradtest.jl (seed 233) for every
+backward, and the PCL Jacobians (src/pcl.jl) against the forward ops they differentiate.
 """
 import numpy as np
 import pytest
@@ -159,3 +159,28 @@ def test_generic_degree1_equals_p1_oracle(oracle):
     i2, v2 = P.stiffness_coo(D)
     np.testing.assert_array_equal(i1, i2)
     np.testing.assert_allclose(v1, v2, rtol=1e-15, atol=1e-15 * np.abs(v2).max())
+
+
+@pytest.mark.parametrize("degree", [1, 2])
+def test_pcl_laplace_jacobian_kat(oracle, degree):
+    """src/pcl.jl:24-39: J[i, j] = d v_j / d kappa_i, so v(kappa) = J^T kappa exactly."""
+    S = space(oracle, 2, degree)
+    J = S.pcl_laplace_jacobian()
+    assert J.shape == (S.ngauss, S.nd * S.nd * S.ngauss)
+    kappa = 1 + np.random.default_rng(2).random(S.ngauss)
+    _, vv = S.laplace_coo(kappa)
+    np.testing.assert_allclose(J.T @ kappa, vv, rtol=1e-14, atol=0)
+    assert np.count_nonzero(J) <= vv.size
+
+
+def test_pcl_dirichlet_kat(oracle):
+    """src/pcl.jl:1-21: J[i, j] = d (v_B)_j / d (v_A)_i; J^T v_A gives the kept values of the
+    COO Dirichlet op in its output order."""
+    S = space(oracle, 3, 1)
+    idx, vv = S.laplace_coo(1 + np.random.default_rng(4).random(S.ngauss))
+    bd = S.bcnode()
+    oi, ov, _ = oracle.dirichlet_coo(idx, vv, bd, np.zeros(S.ndof), np.zeros(bd.size), S.ndof)
+    nkeep = ov.size - bd.size
+    J = oracle.pcl_dirichlet(idx + 1, bd, ov.size)
+    np.testing.assert_array_equal(J.T @ vv, np.r_[ov[:nkeep], np.zeros(bd.size)])
+    assert J.sum() == nkeep

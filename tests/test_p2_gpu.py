@@ -261,3 +261,44 @@ def test_p2_input_checks(gpulib):
         gpulib.PoissonSystem(G)  # resident systems are P1
     with pytest.raises(gpulib.AdFemError):
         gpulib.Mesh(coords, elems, degree=2, order=2)
+
+
+@pytest.mark.parametrize("degree", [1, 2])
+def test_pcl_jacobians(oracle, gpulib, degree):
+    import torch
+
+    from adfem_gpu import _lib
+
+    O, G = spaces(oracle, gpulib, 3, degree, 1)
+    H = gpulib.pcl_compute_fem_laplace_matrix1(G)
+    Ho = O.pcl_laplace_jacobian()
+    assert H.shape == Ho.shape
+    assert rel(H, Ho) < TOL
+    Hd = torch.zeros(Ho.shape[1], Ho.shape[0], dtype=torch.float64, device="cuda")  # column-major ng x N
+    _lib.check(_lib.load().adfem_pcl_laplace_jacobian_d(G.handle, _lib.ptr(Hd), None))
+    assert rel(Hd.cpu().numpy().T, Ho) < TOL
+    idx, vv = O.laplace_coo(np.ones(O.ngauss))
+    bd = O.bcnode()
+    nout = oracle.dirichlet_coo(idx, vv, bd, np.zeros(O.ndof), np.zeros(bd.size), O.ndof)[1].size
+    J = gpulib.pcl_impose_Dirichlet_boundary_conditions(idx + 1, bd, nout)
+    np.testing.assert_array_equal(J, oracle.pcl_dirichlet(idx + 1, bd, nout))
+
+
+def test_pcl_legacy_symbols(oracle, gpulib):
+    from adfem_gpu import _lib
+
+    L = _lib.load()
+    coords, elems = synth.jittered_square(3, seed=5)
+    O = oracle.OracleSpace(coords, elems, 2)
+    G = gpulib.Mesh(coords, elems, degree=2)
+    L.adfem_set_current_mesh(G.handle)
+    H = np.zeros((O.ngauss, 36 * O.ngauss), order="F")
+    L.pcl_FemLaplaceScalar_Jacobian(_lib.ptr(H))
+    assert rel(H, O.pcl_laplace_jacobian()) < TOL
+    idx, _ = O.laplace_coo(np.ones(O.ngauss))
+    idx1 = np.asfortranarray(idx + 1)
+    bd = O.bcnode()
+    J = np.zeros((idx.shape[0], idx.shape[0]), order="F")
+    L.pcl_ImposeDirichlet(_lib.ptr(J), idx1.ctypes.data_as(ctypes.c_void_p), _lib.ptr(bd), bd.size, idx.shape[0])
+    np.testing.assert_array_equal(J, oracle.pcl_dirichlet(idx + 1, bd, idx.shape[0]))
+    L.adfem_set_current_mesh(None)
