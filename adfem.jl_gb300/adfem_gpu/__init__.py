@@ -7,6 +7,7 @@ Julia's SparseMatrixCSC).  All arithmetic runs in the CUDA library; this layer
 only converts arguments.
 
     Mesh(coords, elems)                          src/MFEM/MFEM.jl:60-119
+    Mesh(filename)                               src/MFEM/MUtils.jl:33-50
     Mesh.rectangle(m, n, h)                      src/MFEM/MFEM.jl:134-170
     get_ngauss / get_area / gauss_nodes          src/MFEM/MFEM.jl:207-232
     compute_fem_laplace_matrix1(kappa, mesh)     src/MFEM/MCore.jl:112-120
@@ -56,13 +57,20 @@ def _c(a, dt):
 class Mesh:
     """Triangle mesh resident on the GPU (mirror of AdFem's ``Mesh``).
 
-    ``coords``: (nnode, 2) float; ``elems``: (nelem, 3) 1-based vertex ids.  Degree 1
+    ``coords``: (nnode, 2) float; ``elems``: (nelem, 3) 1-based vertex ids; or
+    ``Mesh(filename)`` for a .mat/.stl/.msh/.vtk mesh file (adfem_gpu.meshfile).  Degree 1
     (P1, order-2 rule) and degree 2 (P2, order-4 rule) are supported (``order=-1``
     selects these defaults, src/MFEM/MFEM.jl:71-77); BDM1 and other orders raise
     ``AdFemError`` with status ``ERR_UNSUPPORTED``.
     """
 
-    def __init__(self, coords, elems, order: int = -1, degree: int = 1, lorder: int = -1):
+    def __init__(self, coords, elems=None, order: int = -1, degree: int = 1, lorder: int = -1,
+                 file_format: str | None = None):
+        if isinstance(coords, (str, bytes)) or hasattr(coords, "__fspath__"):
+            # Mesh(filename) (src/MFEM/MUtils.jl:33-50)
+            from .meshfile import read_mesh_file
+
+            coords, elems = read_mesh_file(str(coords), file_format)
         if degree not in (1, 2):
             raise AdFemError(_lib.ERR_UNSUPPORTED, "degree 1 (P1) and 2 (P2) elements are implemented")
         if order not in (-1, 2 * degree):

@@ -302,3 +302,26 @@ def test_pcl_legacy_symbols(oracle, gpulib):
     L.pcl_ImposeDirichlet(_lib.ptr(J), idx1.ctypes.data_as(ctypes.c_void_p), _lib.ptr(bd), bd.size, idx.shape[0])
     np.testing.assert_array_equal(J, oracle.pcl_dirichlet(idx + 1, bd, idx.shape[0]))
     L.adfem_set_current_mesh(None)
+
+
+@pytest.mark.parametrize("degree", [1, 2])
+def test_mesh_from_file(oracle, gpulib, tmp_path, degree):
+    """Mesh(filename) (src/MFEM/MUtils.jl:33-50) from an ASCII STL written here."""
+    from adfem_gpu.meshfile import read_mesh_file
+
+    coords, elems = synth.jittered_square(6, seed=8)
+    tri = np.concatenate([coords, np.zeros((coords.shape[0], 1))], 1)[elems - 1]
+    p = tmp_path / "sq.stl"
+    with open(p, "w") as f:
+        f.write("solid sq\n")
+        for t in tri:
+            f.write("facet normal 0 0 1\nouter loop\n" + "".join("vertex %.17g %.17g %.17g\n" % tuple(v) for v in t)
+                    + "endloop\nendfacet\n")
+        f.write("endsolid sq\n")
+    G = gpulib.Mesh(str(p), degree=degree)
+    c, e = read_mesh_file(str(p))
+    O = oracle.OracleSpace(c, e, degree)
+    assert (G.nnode, G.nelem, G.ndof) == (coords.shape[0], elems.shape[0], O.ndof)
+    kappa = 1 + np.random.default_rng(1).random(O.ngauss)
+    assert row_scaled_err(gpulib.compute_fem_laplace_matrix1(kappa, G), O.laplace_csc(kappa)) < TOL
+    np.testing.assert_array_equal(gpulib.bcnode(G), O.bcnode())
