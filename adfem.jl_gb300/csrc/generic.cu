@@ -18,6 +18,8 @@
 // DOF->element incidence in ascending element order, so results are deterministic
 // and no atomics are needed.  The per-point basis tables of the degree are built in
 // shared memory by every block from the rule (a few hundred flops).
+#include <mutex>
+
 #include "adfem_internal.h"
 #include "cg_common.cuh"
 
@@ -315,48 +317,76 @@ __global__ void __launch_bounds__(32 * 2 * Tab<DEG>::ND) k_gen_stiffness_coo_bac
 }
 
 // ---------------------------------------------------------------- summed operators
-// element matrices: thread (e, p) forms row p of sum_k N_k (Laplace / mass)
+// Gradients of every basis function at point k with compile-time indices (the P2
+// vertex functions depend on one barycentric gradient, the edge functions on two).
+template <int DEG>
+__device__ __forceinline__ void grads_all(const Tab<DEG>& T, int k, const double2 (&g)[3],
+                                          double (&hx)[Tab<DEG>::ND], double (&hy)[Tab<DEG>::ND]) {
+#pragma unroll
+  for (int a = 0; a < 3; a++) {
+    const double t = T.t[k][a][a];
+    hx[a] = t * g[a].x;
+    hy[a] = t * g[a].y;
+  }
+  if constexpr (DEG == 2) {
+#pragma unroll
+    for (int j = 0; j < 3; j++) {
+      const int a = j, b = (j + 1) % 3;
+      const double ta = T.t[k][3 + j][a], tb = T.t[k][3 + j][b];
+      hx[3 + j] = ta * g[a].x + tb * g[b].x;
+      hy[3 + j] = ta * g[a].y + tb * g[b].y;
+    }
+  }
+}
+
+// packed index of (a, b), a <= b, in the upper triangle of an nd x nd matrix
+__host__ __device__ constexpr int sym_idx(int nd, int a, int b) { return a * nd - a * (a - 1) / 2 + (b - a); }
+
+// Laplace / mass element matrices, one thread per element: the nd (nd + 1) / 2 distinct
+// entries of sum_k coef_k w_k N_k, stored as the full nd x nd matrix of the element
+// (row-major, ke[(e * nd + a) * nd + b]) so that a row gather reads one contiguous row.
 template <int DEG, int OP>
 __global__ void __launch_bounds__(kGT) k_gen_ke(int64_t ne, const double* __restrict__ area,
                                                 const double2* __restrict__ grad, const double* __restrict__ coef,
                                                 double* __restrict__ ke) {
-  constexpr int ND = Tab<DEG>::ND, NG = Tab<DEG>::NG;
+  constexpr int ND = Tab<DEG>::ND, NG = Tab<DEG>::NG, NS = ND * (ND + 1) / 2;
   __shared__ Tab<DEG> T;
   tab_init(T);
-  const int64_t n = ne * ND;
-  for (int64_t t = gtid(); t < n; t += gstride()) {
-    const int64_t e = t / ND;
-    const int p = (int)(t - e * ND);
+  for (int64_t e = gtid(); e < ne; e += gstride()) {
     const double ar = area[e];
     double2 g[3];
     if (OP == (int)GenOp::LAPLACE) load_grad(grad, e, g);
-    double row[ND];
+    double acc[NS];
 #pragma unroll
-    for (int q = 0; q < ND; q++) row[q] = 0.0;
-#pragma unroll
+    for (int j = 0; j < NS; j++) acc[j] = 0.0;
+#pragma unroll 1
     for (int k = 0; k < NG; k++) {
-      const double cw = coef[NG * e + k];
-      const double w = weight_at(T, k, ar);
+      const double cw = coef[NG * e + k] * weight_at(T, k, ar);
       if (OP == (int)GenOp::LAPLACE) {
-        double px, py;
-        grad_at(T, k, p, g, px, py);
+        double hx[ND], hy[ND];
+        grads_all(T, k, g, hx, hy);
 #pragma unroll
-        for (int q = 0; q < ND; q++) {
-          double qx, qy;
-          grad_at(T, k, q, g, qx, qy);
-          row[q] += (px * qx + py * qy) * cw * w;
-        }
+        for (int a = 0; a < ND; a++)
+#pragma unroll
+          for (int b = a; b < ND; b++) acc[sym_idx(ND, a, b)] += (hx[a] * hx[b] + hy[a] * hy[b]) * cw;
       } else {
 #pragma unroll
-        for (int q = 0; q < ND; q++) row[q] += T.h[k][p] * T.h[k][q] * cw * w;
+        for (int a = 0; a < ND; a++)
+#pragma unroll
+          for (int b = a; b < ND; b++) acc[sym_idx(ND, a, b)] += T.h[k][a] * T.h[k][b] * cw;
       }
     }
+    double* out = ke + e * ND * ND;
 #pragma unroll
-    for (int q = 0; q < ND; q++) ke[t * ND + q] = row[q];
+    for (int a = 0; a < ND; a++)
+#pragma unroll
+      for (int b = 0; b < ND; b++) out[a * ND + b] = acc[a <= b ? sym_idx(ND, a, b) : sym_idx(ND, b, a)];
   }
 }
 
-// elasticity element matrices (2 nd x 2 nd): thread (e, l) forms row l of sum_k w B^T D_k B
+// elasticity element matrices (2 nd x 2 nd, not symmetric for a general D): thread
+// (l, e) forms row l of sum_k w_k B_k^T D_k B_k, elements fastest so that a warp shares
+// l; stored row-major per element, ke[(e * 2nd + l) * 2nd + c]
 template <int DEG>
 __global__ void __launch_bounds__(kGT) k_gen_ke_stiffness(int64_t ne, const double* __restrict__ area,
                                                           const double2* __restrict__ grad,
@@ -366,8 +396,9 @@ __global__ void __launch_bounds__(kGT) k_gen_ke_stiffness(int64_t ne, const doub
   tab_init(T);
   const int64_t n = ne * N2;
   for (int64_t t = gtid(); t < n; t += gstride()) {
-    const int64_t e = t / N2;
-    const int l = (int)(t - e * N2);
+    const int l = (int)(t / ne);
+    const int64_t e = t - (int64_t)l * ne;
+    const int r = l < ND ? l : l - ND;
     const double ar = area[e];
     double2 g[3];
     load_grad(grad, e, g);
@@ -378,79 +409,100 @@ __global__ void __launch_bounds__(kGT) k_gen_ke_stiffness(int64_t ne, const doub
     for (int k = 0; k < NG; k++) {
       const double w = weight_at(T, k, ar);
       double hx[ND], hy[ND];
-#pragma unroll
-      for (int r = 0; r < ND; r++) grad_at(T, k, r, g, hx[r], hy[r]);
+      grads_all(T, k, g, hx, hy);
+      double rx, ry;  // gradient of the row's own basis function
+      grad_at(T, k, r, g, rx, ry);
       const double* K = D + 9 * (NG * e + k);
-      double b0, b1, b2;
-      bcol<ND>(hx, hy, l, b0, b1, b2);
+      // column l of B: (rx, 0, ry) for an x row, (0, ry, rx) for a y row
+      const double b0 = l < ND ? rx : 0.0, b1 = l < ND ? 0.0 : ry, b2 = l < ND ? ry : rx;
       double tq[3];
 #pragma unroll
-      for (int q = 0; q < 3; q++) tq[q] = b0 * K[q] + b1 * K[3 + q] + b2 * K[6 + q];
+      for (int q = 0; q < 3; q++) tq[q] = (b0 * K[q] + b1 * K[3 + q] + b2 * K[6 + q]) * w;
 #pragma unroll
-      for (int c = 0; c < N2; c++) {
-        double c0, c1, c2;
-        bcol<ND>(hx, hy, c, c0, c1, c2);
-        row[c] += (tq[0] * c0 + tq[1] * c1 + tq[2] * c2) * w;
+      for (int c = 0; c < ND; c++) {
+        row[c] += tq[0] * hx[c] + tq[2] * hy[c];       // column (c, x): B[:, c] = (hx, 0, hy)
+        row[ND + c] += tq[1] * hy[c] + tq[2] * hx[c];  // column (c, y): B[:, c + nd] = (0, hy, hx)
       }
     }
+    double* out = ke + (e * N2 + l) * N2;
 #pragma unroll
-    for (int c = 0; c < N2; c++) ke[t * N2 + c] = row[c];
+    for (int c = 0; c < N2; c++) out[c] = row[c];
   }
 }
 
-// scalar rows: vals[row i] = sum over incident elements of ke row (or column) a
-template <int DEG>
-__global__ void __launch_bounds__(kGT) k_gen_rows(int64_t ndof, const int32_t* __restrict__ rowptr,
-                                                  const int32_t* __restrict__ inc_ptr, const uint4* __restrict__ inc,
-                                                  const double* __restrict__ ke, double* __restrict__ vals,
-                                                  bool transpose) {
-  constexpr int ND = Tab<DEG>::ND;
-  for (int64_t i = gtid(); i < ndof; i += gstride()) {
-    const int64_t base = rowptr[i];
-    const int len = rowptr[i + 1] - rowptr[i];
-    for (int j = 0; j < len; j++) vals[base + j] = 0.0;
-    for (int32_t s = inc_ptr[i]; s < inc_ptr[i + 1]; s++) {
-      const uint4 r = inc[s];
-      const double* K = ke + (int64_t)r.x * ND * ND;
+// Summed rows, one thread per scalar DOF row (every FP64 add of a warp does 32 rows'
+// work): the row is accumulated in a per-thread shared-memory buffer of CAP entries in
+// ascending element order, then written out.  The block's rows occupy one contiguous
+// range of vals, written by the whole block in order.  NB = 1: scalar operator (row of
+// len entries).  NB = 2: [x; y] elasticity blocks; the thread owns the x row at
+// 2 rowptr[i] and the y row at 2 nnz + 2 rowptr[i], each with the x columns, then the y
+// columns, of the scalar row; transpose gives the CSC values.  Rows longer than the
+// buffer are summed in place in global memory.
+template <int DEG, int NB, int BT, int CAP>
+__global__ void __launch_bounds__(BT) k_gen_rows(int64_t ndof, int64_t nnz, const int32_t* __restrict__ rowptr,
+                                                 const int32_t* __restrict__ inc_ptr, const uint4* __restrict__ inc,
+                                                 const double* __restrict__ ke, double* __restrict__ vals,
+                                                 bool transpose) {
+  constexpr int ND = Tab<DEG>::ND, KN = NB * ND;  // element matrix is KN x KN
+  extern __shared__ double buf[];                 // [NB][CAP][BT]
+  __shared__ int32_t srp[BT + 1];
+  const int tid = threadIdx.x;
+  for (int64_t i0 = (int64_t)blockIdx.x * BT; i0 < ndof; i0 += (int64_t)gridDim.x * BT) {
+    const int nrow = (int)std::min<int64_t>(BT, ndof - i0);
+    __syncthreads();  // previous tile's write-out done with buf / srp
+    if (tid < nrow) srp[tid] = rowptr[i0 + tid];
+    if (tid == 0) srp[nrow] = rowptr[i0 + nrow];
+    const int64_t i = i0 + tid;
+    int len = 0;
+    if (tid < nrow) {
+      len = rowptr[i + 1] - rowptr[i];
+      const int rl = NB * len;  // entries of each of the thread's NB rows
+      const bool fits = rl <= CAP;
+      const int64_t gb[2] = {NB * (int64_t)rowptr[i], 2 * nnz + 2 * (int64_t)rowptr[i]};
 #pragma unroll
-      for (int b = 0; b < ND; b++) {
-        const double v = transpose ? K[b * ND + r.y] : K[r.y * ND + b];
-        vals[base + space_off(r, b)] += v;
-      }
-    }
-  }
-}
-
-// [x; y] block rows of the elasticity operator: x-row i at 2 rowptr[i], y-row ndof + i
-// at 2 nnz + 2 rowptr[i]; within a row the x columns, then the y columns
-template <int DEG>
-__global__ void __launch_bounds__(kGT) k_gen_rows_block2(int64_t ndof, int64_t nnz, const int32_t* __restrict__ rowptr,
-                                                         const int32_t* __restrict__ inc_ptr,
-                                                         const uint4* __restrict__ inc, const double* __restrict__ ke,
-                                                         double* __restrict__ vals, bool transpose) {
-  constexpr int ND = Tab<DEG>::ND, N2 = 2 * ND;
-  for (int64_t i = gtid(); i < ndof; i += gstride()) {
-    const int len = rowptr[i + 1] - rowptr[i];
-    const int64_t rb[2] = {2 * (int64_t)rowptr[i], 2 * nnz + 2 * (int64_t)rowptr[i]};
-    for (int j = 0; j < 2 * len; j++) {
-      vals[rb[0] + j] = 0.0;
-      vals[rb[1] + j] = 0.0;
-    }
-    for (int32_t s = inc_ptr[i]; s < inc_ptr[i + 1]; s++) {
-      const uint4 r = inc[s];
-      const double* K = ke + (int64_t)r.x * N2 * N2;
-#pragma unroll
-      for (int rc = 0; rc < 2; rc++) {
-        const int li = (int)r.y + rc * ND;
-#pragma unroll
-        for (int b = 0; b < ND; b++) {
-          const int64_t pos = rb[rc] + space_off(r, b);
-#pragma unroll
-          for (int cc = 0; cc < 2; cc++) {
-            const int lj = b + cc * ND;
-            vals[pos + cc * len] += transpose ? K[lj * N2 + li] : K[li * N2 + lj];
-          }
+      for (int rc = 0; rc < NB; rc++)
+        for (int j = 0; j < rl; j++) {
+          if (fits) buf[(rc * CAP + j) * BT + tid] = 0.0;
+          else vals[gb[rc] + j] = 0.0;
         }
+      for (int32_t s = inc_ptr[i]; s < inc_ptr[i + 1]; s++) {
+        const uint4 r = inc[s];
+        const double* K = ke + (int64_t)r.x * KN * KN;
+#pragma unroll
+        for (int rc = 0; rc < NB; rc++) {
+          const int li = (int)r.y + rc * ND;
+#pragma unroll
+          for (int cb = 0; cb < NB; cb++)
+#pragma unroll
+            for (int b = 0; b < ND; b++) {
+              const int lj = b + cb * ND;
+              const double v = transpose ? K[lj * KN + li] : K[li * KN + lj];
+              const int j = (int)space_off(r, b) + cb * len;
+              if (fits) buf[(rc * CAP + j) * BT + tid] += v;
+              else vals[gb[rc] + j] += v;
+            }
+        }
+      }
+      if (!fits) len = -1;  // written in place
+    }
+    __syncthreads();
+    // write-out: the tile's rows of each block are contiguous in vals
+    const int64_t b0 = srp[0], b1 = srp[nrow];
+    for (int rc = 0; rc < NB; rc++) {
+      const int64_t out0 = rc == 0 ? NB * b0 : 2 * nnz + 2 * b0;
+      const int64_t total = NB * (b1 - b0);
+      for (int64_t q = tid; q < total; q += BT) {
+        // row of entry q: the last row whose start (in this block's entries) is <= q
+        int lo = 0, hi = nrow - 1;
+        while (lo < hi) {
+          const int mid = (lo + hi + 1) >> 1;
+          if ((int64_t)NB * (srp[mid] - b0) <= q) lo = mid;
+          else hi = mid - 1;
+        }
+        const int rlen = NB * (srp[lo + 1] - srp[lo]);
+        if (rlen > CAP) continue;  // that row was summed in place
+        const int j = (int)(q - (int64_t)NB * (srp[lo] - b0));
+        vals[out0 + q] = buf[(rc * CAP + j) * BT + lo];
       }
     }
   }
@@ -642,9 +694,14 @@ cudaError_t launch_gen_stiffness_coo_backward(const Mesh& m, const Space& sp, co
   return cudaGetLastError();
 }
 
+constexpr int kRowBT = 128;     // rows per block of the row gathers
+constexpr int kRowCap1 = 32;    // buffered entries per scalar row
+constexpr int kRowCap2 = 48;    // buffered entries per elasticity row (x and y columns)
+
 cudaError_t launch_gen_matrix(const Mesh& m, const Space& sp, GenOp op, const double* coef, double* ke, double* vals,
                               bool transpose, cudaStream_t st) {
-  const int g = grid_for(m.ne * sp.nd);
+  (void)transpose;  // Laplace and mass element matrices are symmetric: CSR and CSC values agree
+  const int g = grid_for(m.ne);
   const double* area = sp.d_area.as<double>();
   const double2* grad = m.d_grad.as<double2>();
   if (op == GenOp::LAPLACE)
@@ -655,12 +712,16 @@ cudaError_t launch_gen_matrix(const Mesh& m, const Space& sp, GenOp op, const do
                  (k_gen_ke<2, 1><<<g, kGT, 0, st>>>(m.ne, area, grad, coef, ke)));
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return e;
-  const int gr = grid_for(sp.ndof);
+  const int gr = grid_for(sp.ndof, kRowBT);
+  const size_t smem = sizeof(double) * kRowCap1 * kRowBT;
   const int32_t* rp = sp.d_rowptr.as<int32_t>();
   const int32_t* ip = sp.d_inc_ptr.as<int32_t>();
   const uint4* inc = sp.d_inc.as<uint4>();
-  GEN_DISPATCH(sp, (k_gen_rows<1><<<gr, kGT, 0, st>>>(sp.ndof, rp, ip, inc, ke, vals, transpose)),
-               (k_gen_rows<2><<<gr, kGT, 0, st>>>(sp.ndof, rp, ip, inc, ke, vals, transpose)));
+  GEN_DISPATCH(sp,
+               (k_gen_rows<1, 1, kRowBT, kRowCap1><<<gr, kRowBT, smem, st>>>(sp.ndof, sp.nnz, rp, ip, inc, ke, vals,
+                                                                              false)),
+               (k_gen_rows<2, 1, kRowBT, kRowCap1><<<gr, kRowBT, smem, st>>>(sp.ndof, sp.nnz, rp, ip, inc, ke, vals,
+                                                                              false)));
   return cudaGetLastError();
 }
 
@@ -673,12 +734,22 @@ cudaError_t launch_gen_stiffness_matrix(const Mesh& m, const Space& sp, const do
                (k_gen_ke_stiffness<2><<<g, kGT, 0, st>>>(m.ne, area, grad, D, ke)));
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return e;
-  const int gr = grid_for(sp.ndof);
+  static std::once_flag once;
+  std::call_once(once, [] {
+    const int bytes = (int)(sizeof(double) * 2 * kRowCap2 * kRowBT);
+    cudaFuncSetAttribute(k_gen_rows<1, 2, kRowBT, kRowCap2>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    cudaFuncSetAttribute(k_gen_rows<2, 2, kRowBT, kRowCap2>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+  });
+  const int gr = grid_for(sp.ndof, kRowBT);
+  const size_t smem = sizeof(double) * 2 * kRowCap2 * kRowBT;
   const int32_t* rp = sp.d_rowptr.as<int32_t>();
   const int32_t* ip = sp.d_inc_ptr.as<int32_t>();
   const uint4* inc = sp.d_inc.as<uint4>();
-  GEN_DISPATCH(sp, (k_gen_rows_block2<1><<<gr, kGT, 0, st>>>(sp.ndof, sp.nnz, rp, ip, inc, ke, vals, transpose)),
-               (k_gen_rows_block2<2><<<gr, kGT, 0, st>>>(sp.ndof, sp.nnz, rp, ip, inc, ke, vals, transpose)));
+  GEN_DISPATCH(sp,
+               (k_gen_rows<1, 2, kRowBT, kRowCap2><<<gr, kRowBT, smem, st>>>(sp.ndof, sp.nnz, rp, ip, inc, ke, vals,
+                                                                              transpose)),
+               (k_gen_rows<2, 2, kRowBT, kRowCap2><<<gr, kRowBT, smem, st>>>(sp.ndof, sp.nnz, rp, ip, inc, ke, vals,
+                                                                              transpose)));
   return cudaGetLastError();
 }
 
