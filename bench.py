@@ -536,6 +536,97 @@ def run_c4(A, args):
     return out
 
 
+def run_p2(A, args):
+    """P2 elements, mass matrix and Gauss-point interpolation on the m x m jittered square
+    (m = 1000: 4,004,001 P2 DOF, 46,016,001 stored entries, 12M Gauss points).
+
+    Device time of each op through the C ABI (CUDA events on the current stream, inputs
+    resident), the roofline of the P2 Laplace assembly (FP64-instruction bound on GB300:
+    738 flops per element for the 6-point element matrix plus 36 adds per element in the
+    row gather, against the nominal 1.25 TFLOP/s FP64 rate; and its algorithmic bytes
+    against the measured copy peak), a bounded serial oracle sample of the same Array-arm
+    op (COO loop + sparse() sum, Julia semantics) scaled by element count, and one
+    end-to-end P2 solve (assembly, load, Dirichlet, K\\F) of -lap u = -6 with
+    u = 1 + x^2 + 2y^2 on the boundary, whose P2 solution is exact."""
+    import torch
+    from adfem_gpu import synth
+    from adfem_gpu import system as S
+
+    m = args.p2_m
+    coords, elems = synth.jittered_square(m, seed=0)
+    mesh = A.Mesh(coords, elems, degree=2)
+    ng = A.get_ngauss(mesh)
+    g = torch.tensor(A.gauss_nodes(mesh), device="cuda")
+    kappa = (1.0 + synth.fourier_field(g[:, 0], g[:, 1], seed=1).exp()).contiguous()
+    D = torch.tensor([[2.0, 1.0, 0.0], [1.0, 2.0, 0.0], [0.0, 0.0, 0.5]], dtype=torch.float64,
+                     device="cuda").repeat(ng, 1).reshape(-1).contiguous()
+    u = torch.rand(mesh.ndof, dtype=torch.float64, device="cuda")
+    nnz = int(mesh.pattern()[1].size)
+
+    def timed(fn, reps=3):
+        fn()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(reps):
+            fn()
+        e1.record()
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / reps
+
+    ops = {
+        "laplace_csr_ms": timed(lambda: S.laplace_csr(mesh, kappa)),
+        "mass_csr_ms": timed(lambda: S.mass_csr(mesh, kappa)),
+        "stiffness_csr_ms": timed(lambda: S.stiffness_csr(mesh, D), 1),
+        "source_ms": timed(lambda: S.source(mesh, kappa)),
+        "source_backward_ms": timed(lambda: S.source_backward(mesh, u)),
+        "dof_to_gauss_ms": timed(lambda: S.dof_to_gauss(mesh, u)),
+        "dof_to_gauss_backward_ms": timed(lambda: S.dof_to_gauss_backward(mesh, kappa)),
+        "fem_to_gauss_ms": timed(lambda: S.fem_to_gauss(mesh, u[:mesh.nnode].contiguous())),
+    }
+    ne = mesh.nelem
+    lap_s = ops["laplace_csr_ms"] * 1e-3
+    flops = (738 + 36) * ne
+    bytes_alg = 8 * ng + 56 * ne + 16 * 6 * ne + 4 * (mesh.ndof + 1) * 2 + 8 * nnz
+    hbm, kind = peaks()
+    out = {"workload": "P2 Lagrange %dx%d jittered square, %d DOF, %d stored entries" % (m, m, mesh.ndof, nnz),
+           "ndof": mesh.ndof, "nnz": nnz, "ngauss": ng, "device_ms": ops,
+           "laplace_roofline": {"bound": "fp64", "achieved_tflops": flops / lap_s / 1e12, "peak_tflops": 1.25,
+                                "peak_kind": "nominal GB300 FP64", "frac": flops / lap_s / 1e12 / 1.25,
+                                "flops_per_element": 774, "bytes": bytes_alg, "achieved_gbs": bytes_alg / lap_s / 1e9,
+                                "hbm_frac": bytes_alg / lap_s / 1e9 / hbm, "hbm_peak_kind": kind}}
+    # serial oracle sample of the same Array-arm op, scaled by element count
+    if not args.no_cpu:
+        import oracle as O
+
+        ms = args.p2_cpu_m
+        c2, e2 = synth.jittered_square(ms, seed=0)
+        Os = O.OracleSpace(c2, e2, 2)
+        kk = 1.0 + np.random.default_rng(0).random(Os.ngauss)
+        t0 = time.perf_counter()
+        Os.laplace_csc(kk)
+        tc = time.perf_counter() - t0
+        out["cpu_baseline"] = {"laplace_csc_s": tc * ne / Os.nelem, "cores": 1, "kind": "port",
+                               "sample": "serial oracle COO loop + sparse() sum on the %dx%d P2 mesh, scaled x%.0f by "
+                                         "element count" % (ms, ms, ne / Os.nelem),
+                               "gpu_speedup": tc * ne / Os.nelem / lap_s}
+    # end-to-end P2 solve with a known exact answer
+    ms = args.p2_solve_m
+    c3, e3 = synth.jittered_square(ms, seed=3)
+    M3 = A.Mesh(c3, e3, degree=2)
+    n3 = A.get_ngauss(M3)
+    t0 = time.perf_counter()
+    K = A.compute_fem_laplace_matrix1(np.ones(n3), M3)
+    F = A.compute_fem_source_term1(np.full(n3, -6.0), M3)
+    ue = A.eval_f_on_dof_pts(lambda x, y: 1 + x ** 2 + 2 * y ** 2, M3)
+    bd = A.bcnode(M3)
+    Kb, Fb = A.impose_Dirichlet_boundary_conditions(K, F, bd, ue[bd - 1])
+    sol, st = A.solve(Kb, Fb, rtol=1e-12, return_stats=True)
+    out["solve_exact_quadratic"] = {"m": ms, "ndof": M3.ndof, "seconds": time.perf_counter() - t0,
+                                    "cg_iterations": st.iterations, "max_abs_err": float(np.abs(sol - ue).max())}
+    return out
+
+
 # ----------------------------------------------------------------------------- our arm
 def run_ours(args, rank, world, dist):
     import torch
@@ -698,6 +789,7 @@ def run_ours(args, rank, world, dist):
     serve = run_serve(A, args, rank, world, dist) if args.serve_requests > 0 else None
     c2 = run_c2(A, args) if args.c2_m > 0 else None
     c4 = run_c4(A, args) if args.c4_m > 0 else None
+    p2 = run_p2(A, args) if args.p2_m > 0 else None
 
     # ------------------------------------------------------------------ CPU baseline (rank 0, N=1)
     cpu = None
@@ -745,6 +837,7 @@ def run_ours(args, rank, world, dist):
             "serve": serve,
             "inverse_poisson_1M": c2,
             "elasticity_2M": c4,
+            "p2_4M": p2,
         }
         print(json.dumps(line), flush=True)
     return 0
@@ -777,6 +870,11 @@ def main():
     ap.add_argument("--c2-dirs", type=int, default=32, help="finite-difference directions of the gradient check")
     ap.add_argument("--c4-m", type=int, default=1000, help="elasticity cells per side (0 skips)")
     ap.add_argument("--c4-steps", type=int, default=1)
+    ap.add_argument("--p2-m", type=int, default=1000, help="P2 / mass / interpolation ops cells per side (0 skips)")
+    ap.add_argument("--p2-cpu-m", type=int, default=120, help="P2 oracle sample cells per side")
+    ap.add_argument("--p2-solve-m", type=int, default=200, help="P2 exact-solution solve cells per side")
+    ap.add_argument("--only-p2", action="store_true",
+                    help="profiling aid: run only the P2 / mass / interpolation leg and print it")
     ap.add_argument("--trace-iters", type=int, default=0,
                     help="profiling aid: run one truncated step (this many CG iterations) and exit")
     args = ap.parse_args()
@@ -787,6 +885,11 @@ def main():
     dist = None
     if args.impl == "reference":
         return run_reference(args, rank, world)
+    if args.only_p2:
+        import adfem_gpu as A
+
+        print(json.dumps({"p2_4M": run_p2(A, args)}), flush=True)
+        return 0
     if world > 1:
         import torch
         import torch.distributed as td
