@@ -7,9 +7,9 @@ Julia bindings of libadfem_gpu.so for AdFem.jl users.
   signatures AdFem already ccalls, so pointing AdFem's `LIBMFEM` at this library
   makes `Mesh`, `compute_fem_laplace_matrix1`, `compute_fem_source_term1` and
   `compute_fem_stiffness_matrix` run on the GPU unchanged.
-* This module adds the direct SparseMatrixCSC outputs (no COO + `sparse` round trip),
-  the Dirichlet imposition and `K\\F` on the GPU, and the resident Poisson system
-  with its adjoint gradient.
+* This module adds the direct SparseMatrixCSC outputs (no COO + `sparse` round trip)
+  for P1 and P2 meshes (Laplace, mass), the Gauss-point interpolation ops, the
+  Dirichlet imposition and `K\\F` on the GPU.
 """
 module AdFemGPU
 
@@ -23,29 +23,35 @@ function check(st::Integer)
     error("libadfem_gpu: $msg (status $st)")
 end
 
-"""GPU-resident P1 mesh; `coords` (n,2), `elems` (m,3) 1-based, as `AdFem.Mesh(coords, elems)`."""
+"""GPU-resident mesh; `coords` (n,2), `elems` (m,3) 1-based, as `AdFem.Mesh(coords, elems; degree)`
+(degree 1: P1 with the order-2 rule; degree 2: P2 with the order-4 rule)."""
 mutable struct GMesh
     h::Ptr{Cvoid}
     nnode::Int
     nelem::Int
+    ndof::Int
+    ngauss::Int
     nnz::Int
-    function GMesh(coords::Matrix{Float64}, elems::Matrix{Int64})
+    function GMesh(coords::Matrix{Float64}, elems::Matrix{Int64}; degree::Integer = 1)
         xyz = vec([coords zeros(size(coords, 1))]')
         e0 = Int32.(vec(elems' .- 1))
         h = Ref{Ptr{Cvoid}}(C_NULL)
         check(ccall((:adfem_mesh_create, LIB), Cint, (Ptr{Cdouble}, Clonglong, Ptr{Cint}, Clonglong, Cint, Ptr{Ptr{Cvoid}}),
-                    xyz, size(coords, 1), e0, size(elems, 1), 1, h))
-        nnz = Ref{Clonglong}(0)
+                    xyz, size(coords, 1), e0, size(elems, 1), degree, h))
+        ng, nnz = Ref{Clonglong}(0), Ref{Clonglong}(0)
         check(ccall((:adfem_mesh_sizes, LIB), Cint, (Ptr{Cvoid}, Ptr{Clonglong}, Ptr{Clonglong}, Ptr{Clonglong}, Ptr{Clonglong}),
-                    h[], C_NULL, C_NULL, C_NULL, nnz))
-        m = new(h[], size(coords, 1), size(elems, 1), nnz[])
+                    h[], C_NULL, C_NULL, ng, nnz))
+        ndof = Ref{Clonglong}(0)
+        check(ccall((:adfem_mesh_space, LIB), Cint, (Ptr{Cvoid}, Ptr{Cint}, Ptr{Cint}, Ptr{Cint}, Ptr{Clonglong}, Ptr{Clonglong}),
+                    h[], C_NULL, C_NULL, C_NULL, ndof, C_NULL))
+        m = new(h[], size(coords, 1), size(elems, 1), ndof[], ng[], nnz[])
         finalizer(x -> ccall((:adfem_mesh_destroy, LIB), Cint, (Ptr{Cvoid},), x.h), m)
         return m
     end
 end
 
 function pattern(m::GMesh)
-    colptr = Vector{Int64}(undef, m.nnode + 1)
+    colptr = Vector{Int64}(undef, m.ndof + 1)
     rowval = Vector{Int64}(undef, m.nnz)
     check(ccall((:adfem_mesh_pattern, LIB), Cint, (Ptr{Cvoid}, Ptr{Clonglong}, Ptr{Clonglong}), m.h, colptr, rowval))
     colptr, rowval
@@ -57,12 +63,37 @@ function compute_fem_laplace_matrix1(kappa::Vector{Float64}, m::GMesh)
     nzval = Vector{Float64}(undef, length(rowval))
     check(ccall((:adfem_laplace_csc, LIB), Cint, (Ptr{Cvoid}, Ptr{Cdouble}, Clonglong, Ptr{Cdouble}),
                 m.h, kappa, length(kappa), nzval))
-    SparseMatrixCSC(m.nnode, m.nnode, colptr, rowval, nzval)
+    SparseMatrixCSC(m.ndof, m.ndof, colptr, rowval, nzval)
+end
+
+"""compute_fem_mass_matrix1(ρ, mesh) (MCore.jl:170-181)."""
+function compute_fem_mass_matrix1(rho::Vector{Float64}, m::GMesh)
+    colptr, rowval = pattern(m)
+    nzval = Vector{Float64}(undef, length(rowval))
+    check(ccall((:adfem_mass_csc, LIB), Cint, (Ptr{Cvoid}, Ptr{Cdouble}, Clonglong, Ptr{Cdouble}),
+                m.h, rho, length(rho), nzval))
+    SparseMatrixCSC(m.ndof, m.ndof, colptr, rowval, nzval)
+end
+
+"""fem_to_gauss_points(u, mesh) (MUtils.jl:241-246): nodal values at the Gauss points."""
+function fem_to_gauss_points(u::Vector{Float64}, m::GMesh)
+    out = Vector{Float64}(undef, m.ngauss)
+    check(ccall((:adfem_fem_to_gauss, LIB), Cint, (Ptr{Cvoid}, Ptr{Cdouble}, Clonglong, Ptr{Cdouble}),
+                m.h, u, length(u), out))
+    out
+end
+
+"""dof_to_gauss_points(u, mesh) (MUtils.jl:264-270): DOF values at the Gauss points."""
+function dof_to_gauss_points(u::Vector{Float64}, m::GMesh)
+    out = Vector{Float64}(undef, m.ngauss)
+    check(ccall((:adfem_dof_to_gauss, LIB), Cint, (Ptr{Cvoid}, Ptr{Cdouble}, Clonglong, Ptr{Cdouble}),
+                m.h, u, length(u), out))
+    out
 end
 
 """compute_fem_source_term1(f, mesh) (MCore.jl:77-82)."""
 function compute_fem_source_term1(f::Vector{Float64}, m::GMesh)
-    out = zeros(m.nnode)
+    out = zeros(m.ndof)
     check(ccall((:adfem_source, LIB), Cint, (Ptr{Cvoid}, Ptr{Cdouble}, Clonglong, Ptr{Cdouble}, Cint),
                 m.h, f, length(f), out, 0))
     out
