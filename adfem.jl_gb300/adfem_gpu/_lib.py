@@ -168,6 +168,10 @@ SIGNATURES = {
     "adfem_system_solve_profiled_d": (c_i, [c_p, c_p, ctypes.POINTER(SolverOpts), ctypes.POINTER(SolverStats), c_p,
                                             c_p, c_p]),
     "adfem_system_solver_info": (c_i, [c_p, ctypes.POINTER(SolverInfo)]),
+    "adfem_system_solve_packed_d": (c_i, [c_p, c_i, c_p, ctypes.POINTER(SolverOpts), ctypes.POINTER(SolverStats),
+                                          c_p]),
+    "adfem_system_adjoint_packed_d": (c_i, [c_p, c_i, c_p, c_p, ctypes.POINTER(SolverOpts),
+                                            ctypes.POINTER(SolverStats), c_p]),
     "adfem_server_config_default": (None, [ctypes.POINTER(ServerConfig)]),
     "adfem_server_create": (c_i, [ctypes.POINTER(ServerConfig), c_pp]),
     "adfem_server_destroy": (c_i, [c_p]),

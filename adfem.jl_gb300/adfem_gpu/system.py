@@ -173,6 +173,41 @@ class ElasticitySystem(_System):
         return g
 
 
+# --------------------------------------------------------------- packed solves
+def _packed(systems, outs, gs, rtol, max_iter, warm_start, adjoint):
+    torch = _torch()
+    n = len(systems)
+    if outs is None:
+        outs = [torch.zeros(s.ndof, dtype=torch.float64, device="cuda") for s in systems]
+    for s, u in zip(systems, outs):
+        _dev(u, s.ndof, "u")
+    o = _lib.SolverOpts()
+    _lib.load().adfem_solver_opts_default(ctypes.byref(o))
+    o.rtol, o.max_iter, o.warm_start = rtol, max_iter, int(warm_start)
+    st = (SolverStats * n)()
+    hs = (ctypes.c_void_p * n)(*[s.handle.value for s in systems])
+    us = (ctypes.c_void_p * n)(*[u.data_ptr() for u in outs])
+    L = _lib.load()
+    if adjoint:
+        for s, g in zip(systems, gs):
+            _dev(g, s.ndof, "g")
+        gp = (ctypes.c_void_p * n)(*[g.data_ptr() for g in gs])
+        check(L.adfem_system_adjoint_packed_d(hs, n, gp, us, ctypes.byref(o), st, _cur_stream()), "adjoint_packed")
+    else:
+        check(L.adfem_system_solve_packed_d(hs, n, us, ctypes.byref(o), st, _cur_stream()), "solve_packed")
+    return outs, list(st)
+
+
+def solve_packed(systems, outs=None, rtol=1e-9, max_iter=200000, warm_start=False):
+    """Solve assembled small systems (<= 16384 DOFs each) in one packed launch; returns (u list, stats list)."""
+    return _packed(systems, outs, None, rtol, max_iter, warm_start, False)
+
+
+def adjoint_packed(systems, gs, outs=None, rtol=1e-9, max_iter=200000):
+    """Adjoint solves K^T lam = g of assembled small systems in one packed launch."""
+    return _packed(systems, outs, gs, rtol, max_iter, False, True)
+
+
 # --------------------------------------------------------------- device operators
 def _ng(mesh):
     return (3 if mesh.degree == 1 else 6) * mesh.nelem

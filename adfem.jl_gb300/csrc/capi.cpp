@@ -1036,6 +1036,80 @@ int adfem_system_solver_info(const adfem_system* sys, adfem_solver_info* info) {
   return ADFEM_OK;
 }
 
+// Packed solves (pack.cu): every system of the list solved by one launch, one thread
+// block per system; forward (rhs of the system, Dirichlet rows fixed to their values) or
+// adjoint (rhs g with Dirichlet rows zeroed, lambda zero there).
+static int packed_solves(adfem_system** sys, int count, double** out, const double* const* g,
+                         const adfem_solver_opts* opts, adfem_solver_stats* stats, void* stream, bool adjoint) {
+  if (!sys || !out || count < 1 || (adjoint && !g)) return fail(ADFEM_ERR_INVALID, "packed solve: bad arguments");
+  std::vector<adfem_system*> order(sys, sys + count);
+  for (int i = 0; i < count; i++)
+    if (!sys[i] || !out[i] || (adjoint && !g[i])) return fail(ADFEM_ERR_INVALID, "packed solve: null system or vector");
+  std::sort(order.begin(), order.end());
+  if (std::adjacent_find(order.begin(), order.end()) != order.end())
+    return fail(ADFEM_ERR_INVALID, "packed solve: a system appears twice");
+  std::vector<std::unique_lock<std::mutex>> locks;
+  for (adfem_system* s : order) locks.emplace_back(s->mu);
+  adfem_solver_opts o;
+  adfem_solver_opts_default(&o);
+  if (opts) o = *opts;
+  cudaStream_t st = S(stream);
+  std::vector<PackItem> items(count);
+  for (int i = 0; i < count; i++) {
+    adfem_system* s = sys[i];
+    if (!s->assembled) return fail(ADFEM_ERR_INVALID, "packed solve: system not assembled");
+    if (s->ndof > kPackMaxRows)
+      return fail(ADFEM_ERR_INVALID, "packed solve: a system has more than " + std::to_string(kPackMaxRows) + " DOFs");
+    PackItem& it = items[i];
+    it.S = &s->solver;
+    it.rtol = o.rtol;
+    it.max_iter = o.max_iter;
+    it.warm = o.warm_start != 0;
+    it.zero_rows = adjoint ? s->isbd.as<uint8_t>() : nullptr;
+    it.fix_rows = s->isbd.as<uint8_t>();
+    it.fix_vals = adjoint ? nullptr : s->bdval.as<double>();
+    if (s->kind == ADFEM_SYS_POISSON) {
+      it.rhs = adjoint ? g[i] : s->rhs.as<double>();
+      it.u = out[i];
+    } else {
+      const int64_t nv = s->mesh->m->nv;
+      if (adjoint) ADFEM_TRY(kerr(launch_to_interleaved(nv, g[i], s->t1.as<double>(), st), "interleave"));
+      if (it.warm) ADFEM_TRY(kerr(launch_to_interleaved(nv, out[i], s->t0.as<double>(), st), "interleave"));
+      it.rhs = adjoint ? s->t1.as<double>() : s->rhs.as<double>();
+      it.u = s->t0.as<double>();
+    }
+  }
+  ADFEM_TRY(solve_packed(items.data(), count, st));
+  int status = ADFEM_OK;
+  for (int i = 0; i < count; i++) {
+    adfem_system* s = sys[i];
+    if (s->kind == ADFEM_SYS_ELASTICITY)
+      ADFEM_TRY(kerr(launch_from_interleaved(s->mesh->m->nv, s->t0.as<double>(), out[i], st), "deinterleave"));
+    if (stats) {
+      stats[i].iterations = items[i].iters;
+      stats[i].updates = items[i].passes;
+      stats[i].relres = items[i].relres;
+      stats[i].ms = 0.0;
+      stats[i].status = items[i].status;
+      stats[i].launches = 1;
+    }
+    if (status == ADFEM_OK && items[i].status != ADFEM_OK) status = items[i].status;
+  }
+  ADFEM_CUDA(cudaStreamSynchronize(st));
+  if (status != ADFEM_OK) return fail(status, "packed solve: a system did not converge (see its stats)");
+  return ADFEM_OK;
+}
+
+int adfem_system_solve_packed_d(adfem_system** sys, int count, double** u_d, const adfem_solver_opts* opts,
+                                adfem_solver_stats* stats, void* stream) {
+  return packed_solves(sys, count, u_d, nullptr, opts, stats, stream, false);
+}
+
+int adfem_system_adjoint_packed_d(adfem_system** sys, int count, const double* const* g_d, double** lam_d,
+                                  const adfem_solver_opts* opts, adfem_solver_stats* stats, void* stream) {
+  return packed_solves(sys, count, lam_d, g_d, opts, stats, stream, true);
+}
+
 int adfem_system_adjoint_d(adfem_system* sys, const double* g_d, double* lam_d, const adfem_solver_opts* opts,
                            adfem_solver_stats* stats, void* stream) {
   if (!sys || !g_d || !lam_d) return fail(ADFEM_ERR_INVALID, "null argument");

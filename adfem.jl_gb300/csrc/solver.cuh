@@ -104,6 +104,49 @@ void zcg_enqueue_fold(Solver& S, cudaStream_t st, int force);
 void zcg_enqueue_unscale(Solver& S, cudaStream_t st, const uint8_t* fix, const double* fixval, double* u);
 
 // Fill sliced-ELL values from CSR values (same pattern).
+// ---- packed solves of small systems (pack.cu)
+constexpr int kPackMaxRows = 16384;    // rows of a system solved by one thread block
+constexpr int kPackMaxSystems = 128;   // systems per packed launch
+// one system of a packed launch (device-side descriptor; outputs filled by the kernel)
+struct PackDesc {
+  const int32_t* sptr;
+  const void* col;
+  const double* valD;     // FP64 difference form (outer residual)
+  const float* val32;     // FP32 difference form (inner CG)
+  const float* s;         // Jacobi scaling
+  const double* rhs;
+  const uint8_t* zero_rows;
+  const uint8_t* fix_rows;
+  const double* fix_vals;
+  const double* u0;       // warm start (may alias u) or NULL
+  double* u;
+  double* y;              // scratch: scaled solution (FP64)
+  float* r;               // scratch: inner residual, correction, A p (FP32)
+  float* d;
+  float* q;
+  double rtol2;
+  int n, d16, max_iter;
+  int iters, passes, status, floor_hit;
+  double rr64, bnorm2;
+};
+struct PackItem {
+  Solver* S = nullptr;
+  const double* rhs = nullptr;
+  double* u = nullptr;
+  const uint8_t* zero_rows = nullptr;
+  const uint8_t* fix_rows = nullptr;
+  const double* fix_vals = nullptr;
+  bool warm = false;
+  double rtol = 1e-12;
+  int max_iter = 200000;
+  // results
+  int iters = 0, passes = 0, status = 0;
+  double relres = 0.0;
+};
+// Solves every item in one launch per kPackMaxSystems items (one block per system;
+// the systems must be prepared and have at most kPackMaxRows rows).  Synchronises st.
+int solve_packed(PackItem* items, int count, cudaStream_t st);
+
 cudaError_t launch_csr_to_sell(const Sell& A, int64_t n, const int32_t* rowptr, const double* csr, double* sell,
                                cudaStream_t st);
 int sell_build_pattern(int64_t n, const int32_t* rowptr, const int32_t* colind, Sell& s, int period);

@@ -371,6 +371,17 @@ typedef struct adfem_solver_info {
   int ring;                   /* shared-memory positions per super-tile: rows + 2 band (0 if not banded) */
 } adfem_solver_info;
 ADFEM_API int adfem_system_solver_info(const adfem_system *sys, adfem_solver_info *info);
+/* Packed solves of small systems: the systems (each assembled, at most 16384 DOFs,
+ * distinct) are solved by one graph-captured launch, one thread block per system, with
+ * FP32 inner CG iterations inside FP64 iterative refinement (the mixed method; opts
+ * precision is ignored).  Forward: u_d[i] as adfem_system_solve_d.  Adjoint: lam_d[i]
+ * for right-hand sides g_d[i], as adfem_system_adjoint_d.  stats[i] (may be NULL):
+ * iterations = inner CG iterations, updates = FP64 refinement passes.  Each system's
+ * result is independent of the others in the pack.  Synchronises the stream. */
+ADFEM_API int adfem_system_solve_packed_d(adfem_system **sys, int count, double **u_d, const adfem_solver_opts *opts,
+                                          adfem_solver_stats *stats, void *stream);
+ADFEM_API int adfem_system_adjoint_packed_d(adfem_system **sys, int count, const double *const *g_d, double **lam_d,
+                                            const adfem_solver_opts *opts, adfem_solver_stats *stats, void *stream);
 
 /* No counterpart in the reference.  Allocation-free FP64 Jacobi-CG on a caller-owned
  * device CSR matrix (0-based rowptr[n+1], colind[nnz], vals[nnz], symmetric positive
