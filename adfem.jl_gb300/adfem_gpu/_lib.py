@@ -36,7 +36,8 @@ class SolverInfo(ctypes.Structure):
 
 
 class ServerConfig(ctypes.Structure):
-    _fields_ = [("hbm_budget_bytes", c_ll), ("workers", c_i), ("max_queue", c_i), ("opts", SolverOpts)]
+    _fields_ = [("hbm_budget_bytes", c_ll), ("workers", c_i), ("max_queue", c_i), ("opts", SolverOpts),
+                ("pack_max_dof", c_i), ("pack_max", c_i)]
 
 
 class Request(ctypes.Structure):
@@ -47,14 +48,15 @@ class Request(ctypes.Structure):
 
 class Response(ctypes.Structure):
     _fields_ = [("status", c_i), ("iterations", c_i), ("adjoint_iterations", c_i), ("relres", c_d), ("loss", c_d),
-                ("queue_ms", c_d), ("run_ms", c_d), ("total_ms", c_d), ("message", ctypes.c_char * 160)]
+                ("queue_ms", c_d), ("run_ms", c_d), ("total_ms", c_d), ("message", ctypes.c_char * 160),
+                ("packed", c_i)]
 
 
 class ServerStats(ctypes.Structure):
     _fields_ = [("submitted", c_ll), ("completed", c_ll), ("rejected", c_ll), ("timeouts", c_ll), ("failed", c_ll),
                 ("cache_hits", c_ll), ("cache_misses", c_ll), ("evictions", c_ll), ("resident_systems", c_ll),
                 ("device_bytes", c_ll), ("p50_ms", c_d), ("p99_ms", c_d), ("mean_ms", c_d), ("max_ms", c_d),
-                ("p50_queue_ms", c_d), ("p99_queue_ms", c_d)]
+                ("p50_queue_ms", c_d), ("p99_queue_ms", c_d), ("packs", c_ll), ("packed_requests", c_ll)]
 
 
 OK = 0

@@ -23,7 +23,10 @@ def _f64(a):
 
 class Server:
     def __init__(self, hbm_budget_bytes: int = 0, workers: int = 8, max_queue: int = 0, precision: str = "mixed",
-                 rtol: float = 1e-10, max_iter: int = 200000, ru_delta: float = 0.1, chunk: int = 32):
+                 rtol: float = 1e-10, max_iter: int = 200000, ru_delta: float = 0.1, chunk: int = 32,
+                 pack_max_dof: int = 0, pack_max: int = 0):
+        """pack_max_dof: mixed-precision requests up to this many DOFs are solved in packed
+        launches (0: the library default, 16384; -1: never); pack_max: systems per pack."""
         from . import solver_opts
 
         L = _lib.load()
@@ -33,6 +36,8 @@ class Server:
         cfg.workers = int(workers)
         cfg.max_queue = int(max_queue)
         cfg.opts = solver_opts(precision, rtol, max_iter, ru_delta, chunk)
+        cfg.pack_max_dof = int(pack_max_dof)
+        cfg.pack_max = int(pack_max)
         h = ctypes.c_void_p()
         check(L.adfem_server_create(ctypes.byref(cfg), ctypes.byref(h)), "server_create")
         self._h = h

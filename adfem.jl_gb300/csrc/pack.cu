@@ -63,7 +63,7 @@ __device__ void pack_body(const PackDesc& D, float* __restrict__ sp, double* shb
     const double si = (double)s[r];
     const double bi = (D.zero_rows && D.zero_rows[r] == 1) ? 0.0 : si * D.rhs[r];
     bb = fma(bi, bi, bb);
-    y[r] = D.u0 ? D.u0[r] * (double)(1.0f / s[r]) : 0.0;
+    y[r] = D.u0 ? D.u0[r] / (double)s[r] : 0.0;  // inverse of u = s y up to one rounding
   }
   bsum2(bb, dummy, shb);
   const double bnorm2 = bb, stop2 = D.rtol2 * bnorm2;

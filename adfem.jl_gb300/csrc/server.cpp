@@ -13,9 +13,13 @@
 //    idle systems are evicted least-recently-used when a new one does not fit; a request
 //    that does not fit even into an empty server is rejected with ADFEM_ERR_BUSY (never
 //    an abort), one that fits later waits in the queue;
+//  * packing: the solves of small mixed-precision requests (at most pack_max_dof DOFs)
+//    are handed to a packer thread that solves all waiting ones in one graph-captured
+//    launch, one thread block per system (pack.cu); packs grow with the load;
 //  * per-request status and timings; p50/p99 of the completed requests.
-// A request runs its own kernels with grids and reduction orders fixed by its own sizes,
-// so its results do not depend on the other requests in flight.
+// A request runs its own kernels with grids and reduction orders fixed by its own sizes
+// (a packed request: its own thread block), so its results do not depend on the other
+// requests in flight.
 #include <algorithm>
 #include <chrono>
 #include <cmath>
@@ -30,6 +34,7 @@
 #include <vector>
 
 #include "adfem_internal.h"
+#include "solver.cuh"
 
 using Clock = std::chrono::steady_clock;
 
@@ -59,6 +64,21 @@ struct Resident {
   std::vector<double> bdval;
   adfem::DevBuf uprev;         // last solution (warm starts)
   bool uprev_valid = false;
+};
+
+// A solve handed to the packer: forward (u from the system's rhs) or adjoint (lam
+// from g); the worker waits for done.
+struct PackTicket {
+  adfem_system* sys = nullptr;
+  double* out = nullptr;
+  const double* g = nullptr;
+  bool adjoint = false;
+  bool warm = false;
+  adfem_solver_opts opts{};
+  adfem_solver_stats stats{};
+  int status = ADFEM_OK;
+  std::string msg;
+  bool done = false;
 };
 
 struct Worker {
@@ -104,10 +124,19 @@ struct adfem_server {
   std::unordered_map<long long, std::shared_ptr<Job>> jobs;
   long long next_ticket = 1;
   bool stopping = false;
+  bool stopping_packer = false;
   int running = 0;
   std::vector<std::thread> threads;
   std::vector<std::unique_ptr<Resident>> residents;
   std::vector<std::unique_ptr<Worker>> workers;
+  // packer
+  int pack_max_dof = 0, pack_max = 0;
+  std::deque<PackTicket*> pack_queue;
+  std::condition_variable cv_pack;       // pack queue non-empty or stopping
+  std::condition_variable cv_pack_done;  // a ticket finished
+  std::thread packer;
+  cudaStream_t pack_stream = nullptr;
+  long long packs = 0, packed_requests = 0;
   size_t used = 0;  // resident systems + worker buffers
   uint64_t tick = 0;
   std::vector<double> lat, qlat;
@@ -158,8 +187,86 @@ struct adfem_server {
     return false;
   }
   void run_worker(int wid);
+  void run_packer();
+  int pack_solve(PackTicket& t);
   int run_job(Worker& W, Resident& R, Job& job);
 };
+
+// Hand a solve to the packer and wait for it (the worker's stream work before it must
+// be complete).
+int adfem_server::pack_solve(PackTicket& t) {
+  {
+    std::lock_guard<std::mutex> lk(mu);
+    pack_queue.push_back(&t);
+  }
+  cv_pack.notify_one();
+  std::unique_lock<std::mutex> lk(mu);
+  cv_pack_done.wait(lk, [&] { return t.done; });
+  if (t.status != ADFEM_OK) return adfem::fail(t.status, t.msg);
+  return ADFEM_OK;
+}
+
+void adfem_server::run_packer() {
+  cudaSetDevice(device);
+  std::vector<PackTicket*> batch;
+  for (;;) {
+    {
+      std::unique_lock<std::mutex> lk(mu);
+      cv_pack.wait(lk, [&] { return stopping_packer || !pack_queue.empty(); });
+      if (pack_queue.empty()) break;
+      batch.clear();
+      while (!pack_queue.empty() && (int)batch.size() < pack_max) {
+        batch.push_back(pack_queue.front());
+        pack_queue.pop_front();
+      }
+    }
+    // one launch for the forward solves, one for the adjoint solves
+    for (int adj = 0; adj < 2; adj++) {
+      std::vector<PackTicket*> grp;
+      for (PackTicket* t : batch)
+        if (t->adjoint == (adj == 1)) grp.push_back(t);
+      if (grp.empty()) continue;
+      std::vector<adfem_system*> sys;
+      std::vector<double*> out;
+      std::vector<const double*> g;
+      std::vector<adfem_solver_stats> st(grp.size());
+      adfem_solver_opts o = grp[0]->opts;
+      for (PackTicket* t : grp) {
+        sys.push_back(t->sys);
+        out.push_back(t->out);
+        g.push_back(t->g);
+      }
+      // warm starts and tolerances are per request: split the group where they differ
+      size_t i0 = 0;
+      while (i0 < grp.size()) {
+        size_t i1 = i0 + 1;
+        while (i1 < grp.size() && grp[i1]->warm == grp[i0]->warm && grp[i1]->opts.rtol == grp[i0]->opts.rtol &&
+               grp[i1]->opts.max_iter == grp[i0]->opts.max_iter)
+          i1++;
+        o = grp[i0]->opts;
+        o.warm_start = grp[i0]->warm ? 1 : 0;
+        const int cnt = (int)(i1 - i0);
+        const int r = adj ? adfem_system_adjoint_packed_d(sys.data() + i0, cnt, g.data() + i0, out.data() + i0, &o,
+                                                          st.data() + i0, pack_stream)
+                          : adfem_system_solve_packed_d(sys.data() + i0, cnt, out.data() + i0, &o, st.data() + i0,
+                                                        pack_stream);
+        const std::string msg = r == ADFEM_OK ? std::string() : std::string(adfem_last_error());
+        std::lock_guard<std::mutex> lk(mu);
+        packs++;
+        packed_requests += adj ? 0 : cnt;
+        for (size_t i = i0; i < i1; i++) {
+          grp[i]->stats = st[i];
+          // a failed pack call reports per-system statuses; a setup failure applies to all
+          grp[i]->status = r == ADFEM_OK ? ADFEM_OK : (st[i].status != ADFEM_OK ? st[i].status : r);
+          grp[i]->msg = msg;
+          grp[i]->done = true;
+        }
+        i0 = i1;
+      }
+    }
+    cv_pack_done.notify_all();
+  }
+}
 
 // ---------------------------------------------------------------------------
 int adfem_server::run_job(Worker& W, Resident& R, Job& job) {
@@ -213,8 +320,21 @@ int adfem_server::run_job(Worker& W, Resident& R, Job& job) {
     ADFEM_CUDA(cudaMemcpyAsync(W.u.p, R.uprev.p, sizeof(double) * nd, cudaMemcpyDeviceToDevice, st));
     o.warm_start = 1;
   }
+  const bool packed = pack_max_dof > 0 && o.precision == ADFEM_PREC_MIXED && (long long)nd <= pack_max_dof;
   adfem_solver_stats fs{};
-  ADFEM_TRY(adfem_system_solve_d(R.sys, W.u.as<double>(), &o, &fs, st));
+  if (packed) {
+    ADFEM_CUDA(cudaStreamSynchronize(st));  // assembly and the warm-start copy are done
+    PackTicket t;
+    t.sys = R.sys;
+    t.out = W.u.as<double>();
+    t.warm = o.warm_start != 0;
+    t.opts = o;
+    ADFEM_TRY(pack_solve(t));
+    fs = t.stats;
+    job.resp.packed = 1;
+  } else {
+    ADFEM_TRY(adfem_system_solve_d(R.sys, W.u.as<double>(), &o, &fs, st));
+  }
   job.resp.iterations = fs.iterations;
   job.resp.relres = fs.relres;
   if (R.uprev.bytes < sizeof(double) * nd) {
@@ -241,7 +361,20 @@ int adfem_server::run_job(Worker& W, Resident& R, Job& job) {
     job.resp.loss = loss;
     ADFEM_CUDA(cudaMemcpyAsync(W.g.p, W.hg.data(), sizeof(double) * nd, cudaMemcpyHostToDevice, st));
     adfem_solver_stats as{};
-    ADFEM_TRY(adfem_system_adjoint_d(R.sys, W.g.as<double>(), W.lam.as<double>(), &o, &as, st));
+    if (packed) {
+      ADFEM_CUDA(cudaStreamSynchronize(st));
+      PackTicket t;
+      t.sys = R.sys;
+      t.out = W.lam.as<double>();
+      t.g = W.g.as<double>();
+      t.adjoint = true;
+      t.opts = o;
+      t.opts.warm_start = 0;
+      ADFEM_TRY(pack_solve(t));
+      as = t.stats;
+    } else {
+      ADFEM_TRY(adfem_system_adjoint_d(R.sys, W.g.as<double>(), W.lam.as<double>(), &o, &as, st));
+    }
     job.resp.adjoint_iterations = as.iterations;
     if (kind == ADFEM_SYS_POISSON)
       ADFEM_TRY(adfem_system_grad_kappa_d(R.sys, W.u.as<double>(), W.lam.as<double>(), W.grad.as<double>(), st));
@@ -344,6 +477,8 @@ void adfem_server_config_default(adfem_server_config* cfg) {
   cfg->workers = 8;
   cfg->max_queue = 65536;
   adfem_solver_opts_default(&cfg->opts);
+  cfg->pack_max_dof = 0;
+  cfg->pack_max = 0;
 }
 
 int adfem_server_create(const adfem_server_config* cfg, adfem_server** out) {
@@ -355,6 +490,9 @@ int adfem_server_create(const adfem_server_config* cfg, adfem_server** out) {
   if (S->cfg.workers <= 0) S->cfg.workers = 8;
   if (S->cfg.workers > 256) return adfem::fail(ADFEM_ERR_INVALID, "server: at most 256 workers");
   if (S->cfg.max_queue <= 0) S->cfg.max_queue = 65536;
+  S->pack_max_dof = S->cfg.pack_max_dof == 0 ? adfem::kPackMaxRows
+                                             : (S->cfg.pack_max_dof < 0 ? 0 : std::min(S->cfg.pack_max_dof, adfem::kPackMaxRows));
+  S->pack_max = S->cfg.pack_max <= 0 ? 64 : std::min(S->cfg.pack_max, adfem::kPackMaxSystems);
   ADFEM_CUDA(cudaGetDevice(&S->device));
   size_t freeb = 0, total = 0;
   ADFEM_CUDA(cudaMemGetInfo(&freeb, &total));
@@ -364,7 +502,9 @@ int adfem_server_create(const adfem_server_config* cfg, adfem_server** out) {
     ADFEM_CUDA(cudaStreamCreateWithFlags(&W->stream, cudaStreamNonBlocking));
     S->workers.push_back(std::move(W));
   }
+  ADFEM_CUDA(cudaStreamCreateWithFlags(&S->pack_stream, cudaStreamNonBlocking));
   adfem_server* s = S.get();
+  s->packer = std::thread([s] { s->run_packer(); });
   for (int i = 0; i < s->cfg.workers; i++) s->threads.emplace_back([s, i] { s->run_worker(i); });
   *out = S.release();
   return ADFEM_OK;
@@ -379,6 +519,13 @@ int adfem_server_destroy(adfem_server* srv) {
   srv->cv_work.notify_all();
   srv->cv_done.notify_all();
   for (auto& t : srv->threads) t.join();
+  {
+    std::lock_guard<std::mutex> lk(srv->mu);
+    srv->stopping_packer = true;
+  }
+  srv->cv_pack.notify_all();
+  if (srv->packer.joinable()) srv->packer.join();
+  if (srv->pack_stream) cudaStreamDestroy(srv->pack_stream);
   for (auto& r : srv->residents)
     if (r->sys) adfem_system_destroy(r->sys);
   srv->residents.clear();
@@ -481,6 +628,8 @@ int adfem_server_get_stats(adfem_server* srv, adfem_server_stats* out) {
   }
   out->mean_ms = srv->lat.empty() ? 0.0 : s / (double)srv->lat.size();
   out->max_ms = mx;
+  out->packs = srv->packs;
+  out->packed_requests = srv->packed_requests;
   return ADFEM_OK;
 }
 
@@ -491,6 +640,7 @@ int adfem_server_reset_stats(adfem_server* srv) {
   srv->qlat.clear();
   srv->submitted = srv->completed = srv->rejected = srv->timeouts = srv->failed = 0;
   srv->hits = srv->misses = srv->evictions = 0;
+  srv->packs = srv->packed_requests = 0;
   return ADFEM_OK;
 }
 

@@ -109,7 +109,7 @@ __global__ void __launch_bounds__(kT) k_init(int64_t n, const double* __restrict
     const double si = (double)s[i];
     const double bi = (zero_rows && zero_rows[i] == 1) ? 0.0 : si * rhs[i];
     b[i] = bi;
-    y[i] = u0 ? u0[i] * (double)(1.0f / s[i]) : 0.0;
+    y[i] = u0 ? u0[i] / (double)s[i] : 0.0;  // inverse of u = s y up to one rounding
     acc = fma(bi, bi, acc);
   }
   double v[1] = {acc}, tot[1];

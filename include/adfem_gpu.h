@@ -419,6 +419,9 @@ typedef struct adfem_server_config {
   int workers;                /* concurrent requests (one CUDA stream each); 0: 8 */
   int max_queue;              /* pending requests accepted; 0: 65536 */
   adfem_solver_opts opts;     /* solver options of every request (precision per request may override) */
+  int pack_max_dof;           /* mixed-precision requests with at most this many DOFs are solved in
+                                 packs (one launch, one thread block each); 0: 16384; < 0: never */
+  int pack_max;               /* systems per packed launch; 0: 64 (at most 128) */
 } adfem_server_config;
 ADFEM_API void adfem_server_config_default(adfem_server_config *cfg);
 
@@ -449,6 +452,7 @@ typedef struct adfem_response {
   double run_ms;             /* start to completion */
   double total_ms;           /* submission to completion */
   char message[160];         /* failure message ("" on success) */
+  int packed;                /* 1: the solves ran in a packed launch */
 } adfem_response;
 
 typedef struct adfem_server_stats {
@@ -457,6 +461,7 @@ typedef struct adfem_server_stats {
   long long resident_systems, device_bytes;
   double p50_ms, p99_ms, mean_ms, max_ms;  /* total latency of completed requests */
   double p50_queue_ms, p99_queue_ms;
+  long long packs, packed_requests;        /* packed launches; requests solved in them */
 } adfem_server_stats;
 
 ADFEM_API int adfem_server_create(const adfem_server_config *cfg, adfem_server **out);
