@@ -261,6 +261,13 @@ cudaError_t launch_fill(int64_t n, double v, double* out, cudaStream_t st);
 // H[gp + nz * ng] = vv[nz] (vv: COO values at kappa = 1, nd2 per Gauss point)
 cudaError_t launch_pcl_scatter(int64_t N, int nd2, int64_t ng, const double* vv, double* H, cudaStream_t st);
 
+// Packed forward (g == NULL) or adjoint solves of resident systems on a pack slot
+// (adfem_system_solve_packed_d / adfem_system_adjoint_packed_d with an explicit slot).
+struct PackSlot;
+int system_solve_packed(adfem_system** sys, int count, double** out, const double* const* g,
+                        const adfem_solver_opts* opts, adfem_solver_stats* stats, void* stream, bool adjoint,
+                        PackSlot* slot);
+
 // Device bytes held by a resident system (operator copies, Dirichlet data, solver
 // vectors) -- what the serving loop counts against its HBM budget.
 size_t system_device_bytes(const adfem_system* s);

@@ -1039,8 +1039,12 @@ int adfem_system_solver_info(const adfem_system* sys, adfem_solver_info* info) {
 // Packed solves (pack.cu): every system of the list solved by one launch, one thread
 // block per system; forward (rhs of the system, Dirichlet rows fixed to their values) or
 // adjoint (rhs g with Dirichlet rows zeroed, lambda zero there).
-static int packed_solves(adfem_system** sys, int count, double** out, const double* const* g,
-                         const adfem_solver_opts* opts, adfem_solver_stats* stats, void* stream, bool adjoint) {
+}  // extern "C"
+
+namespace adfem {
+int system_solve_packed(adfem_system** sys, int count, double** out, const double* const* g,
+                        const adfem_solver_opts* opts, adfem_solver_stats* stats, void* stream, bool adjoint,
+                        PackSlot* slot) {
   if (!sys || !out || count < 1 || (adjoint && !g)) return fail(ADFEM_ERR_INVALID, "packed solve: bad arguments");
   std::vector<adfem_system*> order(sys, sys + count);
   for (int i = 0; i < count; i++)
@@ -1079,7 +1083,7 @@ static int packed_solves(adfem_system** sys, int count, double** out, const doub
       it.u = s->t0.as<double>();
     }
   }
-  ADFEM_TRY(solve_packed(items.data(), count, st));
+  ADFEM_TRY(solve_packed(items.data(), count, st, slot));
   int status = ADFEM_OK;
   for (int i = 0; i < count; i++) {
     adfem_system* s = sys[i];
@@ -1099,15 +1103,18 @@ static int packed_solves(adfem_system** sys, int count, double** out, const doub
   if (status != ADFEM_OK) return fail(status, "packed solve: a system did not converge (see its stats)");
   return ADFEM_OK;
 }
+}  // namespace adfem
+
+extern "C" {
 
 int adfem_system_solve_packed_d(adfem_system** sys, int count, double** u_d, const adfem_solver_opts* opts,
                                 adfem_solver_stats* stats, void* stream) {
-  return packed_solves(sys, count, u_d, nullptr, opts, stats, stream, false);
+  return system_solve_packed(sys, count, u_d, nullptr, opts, stats, stream, false, nullptr);
 }
 
 int adfem_system_adjoint_packed_d(adfem_system** sys, int count, const double* const* g_d, double** lam_d,
                                   const adfem_solver_opts* opts, adfem_solver_stats* stats, void* stream) {
-  return packed_solves(sys, count, lam_d, g_d, opts, stats, stream, true);
+  return system_solve_packed(sys, count, lam_d, g_d, opts, stats, stream, true, nullptr);
 }
 
 int adfem_system_adjoint_d(adfem_system* sys, const double* g_d, double* lam_d, const adfem_solver_opts* opts,

@@ -34,6 +34,7 @@ namespace {
 constexpr int kPBT = 512;                // threads per system
 constexpr int kMaxPasses = 64;           // outer refinement passes
 constexpr double kInner2 = 1e-8;         // inner CG stops at |r_inner|^2 <= 1e-8 |r|^2
+constexpr int kU = 8;                    // row entries loaded together in the inner SpMV
 
 __device__ __forceinline__ void bsum2(double& a, double& b, double* shb) {
   double v[2] = {a, b};
@@ -118,7 +119,8 @@ __device__ void pack_body(const PackDesc& D, float* __restrict__ sp, double* shb
     double rho = a1;
     const double target = kInner2 * rho;
     while (it < D.max_iter) {
-      // q = K~ p (FP32 difference form) and p.q
+      // q = K~ p (FP32 difference form) and p.q; a row's entries are loaded kU at a
+      // time before they are used, so their gathers overlap
       float acc = 0.0f;
       for (int r = tid; r < n; r += kPBT) {
         int64_t base;
@@ -127,11 +129,23 @@ __device__ void pack_body(const PackDesc& D, float* __restrict__ sp, double* shb
         const float pr = sp[r];
         const float zr = __ldg(s + r) * pr;
         float q = 0.0f;
-        for (int k = 0; k < w; k++) {
-          const int64_t idx = base + 32 * (int64_t)k;
-          const int j = colof<D16>(D.col, idx, r);
-          const float t = (j == r) ? pr : fmaf(__ldg(s + j), sp[j], -zr);
-          q = fmaf(__ldg(D.val32 + idx), t, q);
+        for (int k0 = 0; k0 < w; k0 += kU) {
+          float v[kU];
+          int j[kU];
+#pragma unroll
+          for (int u = 0; u < kU; u++) {
+            const int64_t idx = base + 32 * (int64_t)(k0 + u);
+            v[u] = k0 + u < w ? __ldg(D.val32 + idx) : 0.0f;
+            j[u] = k0 + u < w ? colof<D16>(D.col, idx, r) : r;
+          }
+          float sj[kU];
+#pragma unroll
+          for (int u = 0; u < kU; u++) sj[u] = __ldg(s + j[u]);
+#pragma unroll
+          for (int u = 0; u < kU; u++) {
+            const float t = (j[u] == r) ? pr : fmaf(sj[u], sp[j[u]], -zr);
+            q = fmaf(v[u], t, q);
+          }
         }
         qv[r] = q;
         acc = fmaf(pr, q, acc);
@@ -184,23 +198,39 @@ __global__ void __launch_bounds__(kPBT, 1) k_pack_solve(PackDesc* desc) {
   else pack_body<false>(D, sp, shb, desc + blockIdx.x);
 }
 
-struct PackContext {
+}  // namespace
+
+struct PackSlot {
   std::mutex mu;
   PackDesc* h = nullptr;  // pinned descriptors of one pack
   DevBuf d;
   cudaGraphExec_t g = nullptr;
 };
 
+PackSlot* pack_slot_create() { return new PackSlot(); }
+
+void pack_slot_destroy(PackSlot* s) {
+  if (!s) return;
+  if (s->g) cudaGraphExecDestroy(s->g);
+  if (s->h) {
+    std::lock_guard<std::mutex> lk(device_alloc_mutex());
+    cudaFreeHost(s->h);
+  }
+  delete s;
+}
+
+namespace {
+
 // process lifetime (never destroyed: its buffers would otherwise be released after the
 // allocation mutex and the CUDA runtime have shut down)
-PackContext& pack_ctx() {
-  static PackContext* c = new PackContext();
+PackSlot& default_slot() {
+  static PackSlot* c = new PackSlot();
   return *c;
 }
 
 // graph: descriptors up, one block per descriptor slot (unused slots have n = 0 and
 // return at entry), results down
-int pack_graph(PackContext& c) {
+int pack_graph(PackSlot& c) {
   if (c.g) return ADFEM_OK;
   const size_t bytes = sizeof(PackDesc) * kPackMaxSystems;
   std::lock_guard<std::mutex> lk(device_alloc_mutex());
@@ -238,14 +268,14 @@ int pack_graph(PackContext& c) {
 
 }  // namespace
 
-int solve_packed(PackItem* items, int count, cudaStream_t st) {
+int solve_packed(PackItem* items, int count, cudaStream_t st, PackSlot* slot) {
   for (int i = 0; i < count; i++) {
     const Solver& S = *items[i].S;
     if (!S.prepared) return fail(ADFEM_ERR_INVALID, "packed solve: operator not prepared");
     if (S.n > kPackMaxRows) return fail(ADFEM_ERR_INVALID, "packed solve: system larger than the packed limit");
     if (!(items[i].rtol > 0.0) || items[i].max_iter < 1) return fail(ADFEM_ERR_INVALID, "packed solve: bad options");
   }
-  PackContext& c = pack_ctx();
+  PackSlot& c = slot ? *slot : default_slot();
   std::lock_guard<std::mutex> lk(c.mu);
   ADFEM_TRY(pack_graph(c));
   for (int i0 = 0; i0 < count; i0 += kPackMaxSystems) {

@@ -92,6 +92,12 @@ struct Worker {
   }
 };
 
+constexpr int kPackers = 4;  // packer threads (concurrent packed launches)
+// Default packing threshold: up to ~4k DOFs a system solved by one thread block is about
+// as fast as the whole-GPU solver even alone, and packs of many run at a fraction of the
+// per-solve cost; larger systems are faster on the whole GPU unless many are packed.
+constexpr int kPackDefaultDof = 4096;
+
 int ndof_of(const adfem::Mesh* m, int kind) { return (int)(kind == ADFEM_SYS_ELASTICITY ? 2 * m->nv : m->nv); }
 
 // Device bytes of a resident system before it exists (admission): per stored operator
@@ -134,8 +140,12 @@ struct adfem_server {
   std::deque<PackTicket*> pack_queue;
   std::condition_variable cv_pack;       // pack queue non-empty or stopping
   std::condition_variable cv_pack_done;  // a ticket finished
-  std::thread packer;
-  cudaStream_t pack_stream = nullptr;
+  struct Packer {
+    std::thread th;
+    cudaStream_t stream = nullptr;
+    adfem::PackSlot* slot = nullptr;
+  };
+  std::vector<Packer> packers;
   long long packs = 0, packed_requests = 0;
   size_t used = 0;  // resident systems + worker buffers
   uint64_t tick = 0;
@@ -187,7 +197,7 @@ struct adfem_server {
     return false;
   }
   void run_worker(int wid);
-  void run_packer();
+  void run_packer(int pid);
   int pack_solve(PackTicket& t);
   int run_job(Worker& W, Resident& R, Job& job);
 };
@@ -206,8 +216,9 @@ int adfem_server::pack_solve(PackTicket& t) {
   return ADFEM_OK;
 }
 
-void adfem_server::run_packer() {
+void adfem_server::run_packer(int pid) {
   cudaSetDevice(device);
+  Packer& P = packers[pid];
   std::vector<PackTicket*> batch;
   for (;;) {
     {
@@ -246,10 +257,8 @@ void adfem_server::run_packer() {
         o = grp[i0]->opts;
         o.warm_start = grp[i0]->warm ? 1 : 0;
         const int cnt = (int)(i1 - i0);
-        const int r = adj ? adfem_system_adjoint_packed_d(sys.data() + i0, cnt, g.data() + i0, out.data() + i0, &o,
-                                                          st.data() + i0, pack_stream)
-                          : adfem_system_solve_packed_d(sys.data() + i0, cnt, out.data() + i0, &o, st.data() + i0,
-                                                        pack_stream);
+        const int r = adfem::system_solve_packed(sys.data() + i0, cnt, out.data() + i0, g.data() + i0, &o,
+                                                 st.data() + i0, P.stream, adj == 1, P.slot);
         const std::string msg = r == ADFEM_OK ? std::string() : std::string(adfem_last_error());
         std::lock_guard<std::mutex> lk(mu);
         packs++;
@@ -490,7 +499,7 @@ int adfem_server_create(const adfem_server_config* cfg, adfem_server** out) {
   if (S->cfg.workers <= 0) S->cfg.workers = 8;
   if (S->cfg.workers > 256) return adfem::fail(ADFEM_ERR_INVALID, "server: at most 256 workers");
   if (S->cfg.max_queue <= 0) S->cfg.max_queue = 65536;
-  S->pack_max_dof = S->cfg.pack_max_dof == 0 ? adfem::kPackMaxRows
+  S->pack_max_dof = S->cfg.pack_max_dof == 0 ? kPackDefaultDof
                                              : (S->cfg.pack_max_dof < 0 ? 0 : std::min(S->cfg.pack_max_dof, adfem::kPackMaxRows));
   S->pack_max = S->cfg.pack_max <= 0 ? 64 : std::min(S->cfg.pack_max, adfem::kPackMaxSystems);
   ADFEM_CUDA(cudaGetDevice(&S->device));
@@ -502,9 +511,15 @@ int adfem_server_create(const adfem_server_config* cfg, adfem_server** out) {
     ADFEM_CUDA(cudaStreamCreateWithFlags(&W->stream, cudaStreamNonBlocking));
     S->workers.push_back(std::move(W));
   }
-  ADFEM_CUDA(cudaStreamCreateWithFlags(&S->pack_stream, cudaStreamNonBlocking));
+  // packers: several packs run at once (a pack lasts as long as its largest system)
+  const int npack = S->pack_max_dof > 0 ? kPackers : 0;
+  S->packers.resize(npack);
+  for (auto& P : S->packers) {
+    ADFEM_CUDA(cudaStreamCreateWithFlags(&P.stream, cudaStreamNonBlocking));
+    P.slot = adfem::pack_slot_create();
+  }
   adfem_server* s = S.get();
-  s->packer = std::thread([s] { s->run_packer(); });
+  for (int i = 0; i < npack; i++) s->packers[i].th = std::thread([s, i] { s->run_packer(i); });
   for (int i = 0; i < s->cfg.workers; i++) s->threads.emplace_back([s, i] { s->run_worker(i); });
   *out = S.release();
   return ADFEM_OK;
@@ -524,8 +539,11 @@ int adfem_server_destroy(adfem_server* srv) {
     srv->stopping_packer = true;
   }
   srv->cv_pack.notify_all();
-  if (srv->packer.joinable()) srv->packer.join();
-  if (srv->pack_stream) cudaStreamDestroy(srv->pack_stream);
+  for (auto& P : srv->packers) {
+    if (P.th.joinable()) P.th.join();
+    if (P.stream) cudaStreamDestroy(P.stream);
+    adfem::pack_slot_destroy(P.slot);
+  }
   for (auto& r : srv->residents)
     if (r->sys) adfem_system_destroy(r->sys);
   srv->residents.clear();

@@ -143,9 +143,15 @@ struct PackItem {
   int iters = 0, passes = 0, status = 0;
   double relres = 0.0;
 };
+// Descriptor buffers and the captured graph of packed launches; one pack at a time runs
+// on a slot (packs on different slots run concurrently).
+struct PackSlot;
+PackSlot* pack_slot_create();
+void pack_slot_destroy(PackSlot* s);
 // Solves every item in one launch per kPackMaxSystems items (one block per system;
-// the systems must be prepared and have at most kPackMaxRows rows).  Synchronises st.
-int solve_packed(PackItem* items, int count, cudaStream_t st);
+// the systems must be prepared and have at most kPackMaxRows rows) on the given slot
+// (NULL: a process-wide slot).  Synchronises st.
+int solve_packed(PackItem* items, int count, cudaStream_t st, PackSlot* slot = nullptr);
 
 cudaError_t launch_csr_to_sell(const Sell& A, int64_t n, const int32_t* rowptr, const double* csr, double* sell,
                                cudaStream_t st);

@@ -358,7 +358,8 @@ def run_serve(A, args, rank=0, world=1, dist=None):
     t0 = time.perf_counter()
     cat = ServeCatalog(A, SERVE_SIZES)
     setup_s = time.perf_counter() - t0
-    with A.Server(workers=args.serve_workers, precision="mixed", rtol=args.serve_rtol) as srv:
+    with A.Server(workers=args.serve_workers, precision="mixed", rtol=args.serve_rtol,
+                  pack_max_dof=args.serve_pack_max_dof) as srv:
         warm = [(m, k, 0, True) for m in SERVE_SIZES for k in (0, 1)]
         for t in [cat.submit(srv, r) for r in warm]:
             srv.wait(t)
@@ -374,7 +375,8 @@ def run_serve(A, args, rank=0, world=1, dist=None):
         sat = {"requests": args.serve_requests, "wall_s": wall,
                "throughput_req_s": replica_rate(world, len(reqs), wall),
                "dof_per_s": replica_rate(world, sum(cat.dof(r) for r in reqs), wall), "p50_ms": st["p50_ms"], "p99_ms": st["p99_ms"],
-               "failed": bad, "gradients": sum(1 for r in reqs if r[3])}
+               "failed": bad, "gradients": sum(1 for r in reqs if r[3]), "packs": st["packs"],
+               "packed_requests": st["packed_requests"]}
         # open loop: exponential inter-arrival gaps at a fraction of the saturation rate
         sweep = []
         for frac in args.serve_loads:
@@ -396,13 +398,15 @@ def run_serve(A, args, rank=0, world=1, dist=None):
             s = srv.stats()
             sweep.append({"offered_req_s": rate, "load": frac, "achieved_req_s": replica_rate(world, len(sub), wall),
                           "p50_ms": s["p50_ms"], "p99_ms": s["p99_ms"], "p50_queue_ms": s["p50_queue_ms"],
-                          "failed": sum(1 for r in rs if r["status"] != 0)})
+                          "failed": sum(1 for r in rs if r["status"] != 0), "packs": s["packs"],
+                          "packed_requests": s["packed_requests"]})
         cache = srv.stats()
     ref = min(sweep, key=lambda x: abs(x["load"] - 0.5)) if sweep else None
     return {"workload": "C5 mix: 80/20 Poisson/elasticity, m log-uniform in [16,1024] rounded to %d sizes "
                         "(ratio 2^(1/4)), 50%% with a misfit gradient (1%% observations), seeded fields"
                         % len(SERVE_SIZES),
             "workers": args.serve_workers, "rtol": args.serve_rtol, "precision": "mixed",
+            "pack_max_dof": args.serve_pack_max_dof if args.serve_pack_max_dof != 0 else 4096,
             "p50_ms": ref["p50_ms"] if ref else sat["p50_ms"], "p99_ms": ref["p99_ms"] if ref else sat["p99_ms"],
             "latency_at_load": ref["load"] if ref else 1.0,
             "saturation": sat, "sweep": sweep, "setup_s": setup_s,
@@ -865,6 +869,9 @@ def main():
     ap.add_argument("--serve-loads", type=float, nargs="*", default=[0.5, 0.8])
     ap.add_argument("--serve-workers", type=int, default=8)
     ap.add_argument("--serve-rtol", type=float, default=1e-9)
+    ap.add_argument("--serve-pack-max-dof", type=int, default=0,
+                    help="requests up to this many DOFs are solved in packed launches (0: library default; -1: off)")
+    ap.add_argument("--only-serve", action="store_true", help="run only the serving leg and print it")
     ap.add_argument("--c2-m", type=int, default=1000, help="inverse Poisson cells per side (0 skips)")
     ap.add_argument("--c2-steps", type=int, default=2)
     ap.add_argument("--c2-dirs", type=int, default=32, help="finite-difference directions of the gradient check")
@@ -885,10 +892,11 @@ def main():
     dist = None
     if args.impl == "reference":
         return run_reference(args, rank, world)
-    if args.only_p2:
+    if args.only_p2 or args.only_serve:
         import adfem_gpu as A
 
-        print(json.dumps({"p2_4M": run_p2(A, args)}), flush=True)
+        out = {"p2_4M": run_p2(A, args)} if args.only_p2 else {"serve": run_serve(A, args)}
+        print(json.dumps(out), flush=True)
         return 0
     if world > 1:
         import torch

@@ -420,7 +420,8 @@ typedef struct adfem_server_config {
   int max_queue;              /* pending requests accepted; 0: 65536 */
   adfem_solver_opts opts;     /* solver options of every request (precision per request may override) */
   int pack_max_dof;           /* mixed-precision requests with at most this many DOFs are solved in
-                                 packs (one launch, one thread block each); 0: 16384; < 0: never */
+                                 packs (one launch, one thread block each); 0: 4096; < 0: never;
+                                 at most 16384 */
   int pack_max;               /* systems per packed launch; 0: 64 (at most 128) */
 } adfem_server_config;
 ADFEM_API void adfem_server_config_default(adfem_server_config *cfg);

@@ -146,7 +146,7 @@ def test_server_packs_small_requests(oracle, gpulib):
     P, E = gpulib._lib.SYS_POISSON, gpulib._lib.SYS_ELASTICITY
     cases = [Case(gpulib, m, P, 30 + i, obs_frac=0.03 if i % 2 else 0.0) for i, m in enumerate([12, 30, 50, 70])]
     cases += [Case(gpulib, 20, E, 40, obs_frac=0.03), Case(gpulib, 140, P, 41)]  # 19,881 DOFs: not packed
-    with gpulib.Server(workers=6, rtol=RTOL) as srv:
+    with gpulib.Server(workers=6, rtol=RTOL, pack_max_dof=16384) as srv:
         tk = [c.submit(srv) for c in cases]
         res = [srv.wait(t) for t in tk]
         fp64 = srv.wait(cases[0].submit(srv, precision="fp64"))[0]
