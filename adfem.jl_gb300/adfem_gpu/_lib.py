@@ -160,6 +160,7 @@ SIGNATURES = {
     "adfem_system_destroy": (c_i, [c_p]),
     "adfem_system_set_dirichlet": (c_i, [c_p, c_p, c_ll, c_p]),
     "adfem_system_assemble_poisson_d": (c_i, [c_p, c_p, c_p, c_p]),
+    "adfem_system_assemble_poisson_profiled_d": (c_i, [c_p, c_p, c_p, c_p, c_p]),
     "adfem_system_assemble_elasticity_d": (c_i, [c_p, c_p, c_p, c_p, c_p, c_p]),
     "adfem_system_solve_d": (c_i, [c_p, c_p, ctypes.POINTER(SolverOpts), ctypes.POINTER(SolverStats), c_p]),
     "adfem_system_adjoint_d": (c_i, [c_p, c_p, c_p, ctypes.POINTER(SolverOpts), ctypes.POINTER(SolverStats), c_p]),

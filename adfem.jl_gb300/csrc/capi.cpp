@@ -938,23 +938,54 @@ int adfem_system_set_dirichlet(adfem_system* sys, const long long* bd, long long
   return system_set_bd(sys, bd, nbd, bdval);
 }
 
+// Poisson assembly: element pass (sigma, element loads), fused Laplace + load + Dirichlet
+// rows into the sliced-ELL operator, operator conversion for the solver.  ev: optional
+// four events recorded around the three phases.
+static int assemble_poisson(adfem_system* sys, const double* kappa_d, const double* f_d, cudaStream_t st,
+                            cudaEvent_t* ev) {
+  Mesh& m = *sys->mesh->m;
+  sys->assembled = false;
+  ADFEM_TRY(sys->sigma.alloc(sizeof(double) * m.ne));
+  ADFEM_TRY(sys->src3.alloc(sizeof(double) * 3 * m.ne));
+  if (ev) ADFEM_CUDA(cudaEventRecord(ev[0], st));
+  ADFEM_TRY(kerr(launch_element_prepass(m, kappa_d, f_d, sys->sigma.as<double>(), sys->src3.as<double>(), st),
+                 "element prepass"));
+  if (ev) ADFEM_CUDA(cudaEventRecord(ev[1], st));
+  ADFEM_TRY(kerr(launch_poisson_system(m, sys->sigma.as<double>(), sys->src3.as<double>(), sys->isbd.as<uint8_t>(),
+                                       sys->bdval.as<double>(), sys->A.val64.as<double>(), sys->rhs.as<double>(), st),
+                 "poisson system"));
+  if (ev) ADFEM_CUDA(cudaEventRecord(ev[2], st));
+  ADFEM_TRY(solver_prepare(sys->solver, sys->diagpos.as<int32_t>(), st));
+  if (ev) ADFEM_CUDA(cudaEventRecord(ev[3], st));
+  sys->assembled = true;
+  return ADFEM_OK;
+}
+
 int adfem_system_assemble_poisson_d(adfem_system* sys, const double* kappa_d, const double* f_d, void* stream) {
   if (!sys || !kappa_d || !f_d) return fail(ADFEM_ERR_INVALID, "null argument");
   if (sys->kind != ADFEM_SYS_POISSON) return fail(ADFEM_ERR_INVALID, "not a Poisson system");
   std::lock_guard<std::mutex> lk(sys->mu);
-  Mesh& m = *sys->mesh->m;
-  cudaStream_t st = S(stream);
-  sys->assembled = false;
-  ADFEM_TRY(sys->sigma.alloc(sizeof(double) * m.ne));
-  ADFEM_TRY(sys->src3.alloc(sizeof(double) * 3 * m.ne));
-  ADFEM_TRY(kerr(launch_element_prepass(m, kappa_d, f_d, sys->sigma.as<double>(), sys->src3.as<double>(), st),
-                 "element prepass"));
-  ADFEM_TRY(kerr(launch_poisson_system(m, sys->sigma.as<double>(), sys->src3.as<double>(), sys->isbd.as<uint8_t>(),
-                                       sys->bdval.as<double>(), sys->A.val64.as<double>(), sys->rhs.as<double>(), st),
-                 "poisson system"));
-  ADFEM_TRY(solver_prepare(sys->solver, sys->diagpos.as<int32_t>(), st));
-  sys->assembled = true;
-  return ADFEM_OK;
+  return assemble_poisson(sys, kappa_d, f_d, S(stream), nullptr);
+}
+
+int adfem_system_assemble_poisson_profiled_d(adfem_system* sys, const double* kappa_d, const double* f_d, double* ms,
+                                             void* stream) {
+  if (!sys || !kappa_d || !f_d || !ms) return fail(ADFEM_ERR_INVALID, "null argument");
+  if (sys->kind != ADFEM_SYS_POISSON) return fail(ADFEM_ERR_INVALID, "not a Poisson system");
+  std::lock_guard<std::mutex> lk(sys->mu);
+  cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+  for (auto& e : ev) ADFEM_CUDA(cudaEventCreate(&e));
+  const int r = assemble_poisson(sys, kappa_d, f_d, S(stream), ev);
+  if (r == ADFEM_OK) {
+    cudaEventSynchronize(ev[3]);
+    for (int k = 0; k < 3; k++) {
+      float t = 0.0f;
+      cudaEventElapsedTime(&t, ev[k], ev[k + 1]);
+      ms[k] = t;
+    }
+  }
+  for (auto& e : ev) cudaEventDestroy(e);
+  return r;
 }
 
 int adfem_system_assemble_elasticity_d(adfem_system* sys, const double* E_d, const double* nu_d, const double* fx_d,

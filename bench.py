@@ -759,14 +759,28 @@ def run_ours(args, rank, world, dist):
         kname, b32 = "k_cg32_spmv", spmv32_bytes(nent, nrow, nsl)
         others = {"k_cg32_update": upd_ms, "k_fold": kms[2] / max(kn[2], 1), "k_residual64": kms[3] / max(kn[3], 1)}
     achieved = b32 / (spmv_ms * 1e-3) / 1e9
-    # assembly pass timing (prepass + fused system kernel + scaling), for the record
-    a0, a1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    a0.record()
+    # assembly phases (CUDA events inside the library): element pass, fused Laplace + load +
+    # Dirichlet rows, operator conversion for the solver; median of 3
+    phases = []
     for _ in range(3):
-        S.assemble(kappa, f)
-    a1.record()
-    torch.cuda.synchronize()
-    asm_ms = a0.elapsed_time(a1) / 3
+        ms3 = (ctypes.c_double * 3)()
+        _lib.check(_lib.load().adfem_system_assemble_poisson_profiled_d(
+            S.handle, _lib.ptr(kappa), _lib.ptr(f), ms3, _lib.stream_ptr(torch.cuda.current_stream())))
+        phases.append(list(ms3))
+    ph = [statistics.median(p[k] for p in phases) for k in range(3)]
+    asm_ms = sum(ph)
+    ne_ = mesh.nelem
+    ng_ = 3 * ne_
+    # algorithmic bytes of the assembly proper (element pass + rows): kappa and f at the
+    # Gauss points, per-element geometry (32 B) and the three incidence records (24 B), the
+    # operator values (8 B per stored entry) and the load vector
+    asm_bytes = 16 * ng_ + 56 * ne_ + 8 * nent + 8 * n
+    asm_s = (ph[0] + ph[1]) * 1e-3
+    assembly = {"element_pass_ms": ph[0], "rows_ms": ph[1], "solver_conversion_ms": ph[2], "total_ms": asm_ms,
+                "bytes": asm_bytes, "achieved_gbs": asm_bytes / asm_s / 1e9, "hbm_frac": asm_bytes / asm_s / 1e9 / hbm,
+                "dof_per_s": n / asm_s, "elements_per_s": ne_ / asm_s,
+                "bound": "fp64 (GB300 FP64 pipe: 82% busy in the element pass, 64% in the row pass; "
+                         "profiles/assembly_poisson_1M.md)"}
 
     # ------------------------------------------------------------------ e2e through host buffers
     kh = kappa.cpu().pin_memory()
@@ -827,6 +841,8 @@ def run_ours(args, rank, world, dist):
             "fp64": {"solves_per_s": fp64_value, "iters": [s[0] for s in fp64_stats], "rel_err_vs_fp64_ref": err_fp64,
                      "speedup_mixed_over_fp64": value / fp64_value},
             "grads_per_s": grads_value,
+            "dof_per_s": value * n,
+            "assembly": assembly,
             "fp64_reference": {"rtol": args.ref_rtol, "iters": ref_stats.iterations, "relres": ref_stats.relres},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
                          "traffic": traffic, "kernel": kname, "bytes_per_launch": b32,

@@ -327,6 +327,12 @@ ADFEM_API int adfem_system_assemble_poisson_d(adfem_system *sys, const double *k
                                               void *stream);
 /* Elasticity with plane-strain D(E, nu) (reference formula) at each Gauss point and
  * body force (fx, fy) at the Gauss points. */
+/* Same as adfem_system_assemble_poisson_d, and ms[0..2] receive the device time of its
+ * three phases (CUDA events): element pass (sigma, element loads), fused Laplace + load +
+ * Dirichlet rows, operator conversion for the solver (Jacobi scaling, FP32 and banded copies).
+ * Synchronises the stream. */
+ADFEM_API int adfem_system_assemble_poisson_profiled_d(adfem_system *sys, const double *kappa_d, const double *f_d,
+                                                       double *ms, void *stream);
 ADFEM_API int adfem_system_assemble_elasticity_d(adfem_system *sys, const double *E_d, const double *nu_d,
                                                  const double *fx_d, const double *fy_d, void *stream);
 /* Solve the assembled system; u_d: ndof (nv or 2nv, reference DOF ordering). */
