@@ -171,6 +171,9 @@ int mesh_edges(Mesh* m);  // fills m->edges / eedge / nedges (first-appearance n
 // Boundary DOFs, 1-based: ascending boundary vertices; for degree-2 meshes followed by
 // the ascending DOFs of boundary edges
 int64_t mesh_bcnode(Mesh* m, int64_t* out1);
+// Reverse Cuthill-McKee renumbering of the mesh nodes (pi[node] = new index); returns
+// the bandwidth of the renumbered pattern.
+int64_t mesh_rcm(const Mesh& m, std::vector<int32_t>& pi);
 // Gauss points per element (3 for the order-2 rule of P1, 6 for the order-4 rule of P2)
 inline int mesh_ng(const Mesh& m) { return m.degree == 2 ? 6 : 3; }
 inline int64_t mesh_ngauss(const Mesh& m) { return (int64_t)mesh_ng(m) * m.ne; }
@@ -201,9 +204,14 @@ cudaError_t launch_laplace_coo(const Mesh& m, const double* kappa, long long* in
 cudaError_t launch_laplace_coo_backward(const Mesh& m, const double* grad_vv, double* grad_kappa, cudaStream_t st);
 cudaError_t launch_source_backward(const Mesh& m, const double* grad_rhs, double* grad_f, cudaStream_t st);
 // fused Poisson system: Laplace + load + Dirichlet (bd rows -> identity, bd columns
-// dropped into the rhs lift), values into sliced-ELL (full pattern, dropped entries 0)
+// dropped into the rhs lift), values into the system's sliced-ELL (sptr; full pattern,
+// dropped entries 0).  diagpos_mesh: diagonal slot of each mesh pattern row.  nperm /
+// kperm (NULL: no renumbering): solver row of each node and rank of each pattern slot in
+// its renumbered row; isbd, bdval and rhs are in solver order.
 cudaError_t launch_poisson_system(const Mesh& m, const double* sigma, const double* src3, const uint8_t* isbd,
-                                  const double* bdval_dense, double* sell_vals, double* rhs, cudaStream_t st);
+                                  const double* bdval_dense, double* sell_vals, double* rhs, const int32_t* sptr,
+                                  const int32_t* diagpos_mesh, const int32_t* nperm, const uint8_t* kperm,
+                                  cudaStream_t st);
 // adjoint element kernel: grad_kappa[3e+k] = -w_e (grad lam_e).(grad u_e), lam zero on bd
 cudaError_t launch_poisson_kappa_grad(const Mesh& m, const double* u, const double* lam, const uint8_t* isbd,
                                       double* grad_kappa, cudaStream_t st);

@@ -197,24 +197,30 @@ cudaError_t launch_source_rows(const Mesh& m, const double* src3, double* rhs, b
 // ---------------------------------------------------------------------------
 // Fused Poisson system: Laplace row + load + Dirichlet in one pass, into sliced-ELL.
 // isbd[i]: 0 interior, 1 Dirichlet node, 2 interior with a Dirichlet neighbour.
-template <int MAXW>
+// PERM: the system's DOFs are renumbered (nperm[node] = solver row); the row of mesh
+// node i goes to solver row nperm[i], its slot k to the rank kperm[rowptr[i] + k] of the
+// renumbered column in that row; isbd, bdval and rhs are in solver order.
+template <int MAXW, bool PERM>
 __global__ void __launch_bounds__(kBlock) k_poisson_system(
     int64_t n, const int32_t* __restrict__ inc_ptr, const uint2* __restrict__ inc, const double4* __restrict__ geo,
     const double* __restrict__ sigma, const double* __restrict__ src3, const int32_t* __restrict__ rowptr,
     const int32_t* __restrict__ colind, const int32_t* __restrict__ diagpos, const int32_t* __restrict__ sptr,
     const uint8_t* __restrict__ isbd, const double* __restrict__ bdval, double* __restrict__ vals,
-    double* __restrict__ rhs) {
+    double* __restrict__ rhs, const int32_t* __restrict__ nperm, const uint8_t* __restrict__ kperm) {
   __shared__ double acc[MAXW][kBlock];
   const int t = threadIdx.x;
   const int64_t i = gtid();
   if (i >= n) return;
   const int w = rowptr[i + 1] - rowptr[i];
+  const int32_t r0 = rowptr[i];
+  const int64_t ri = PERM ? (int64_t)nperm[i] : i;
   const int dp = diagpos[i];
-  const int64_t base = (int64_t)sptr[i >> 5] + (i & 31);
-  const uint8_t tag = isbd[i];
+  const int64_t base = (int64_t)sptr[ri >> 5] + (ri & 31);
+  const uint8_t tag = isbd[ri];
   if (tag == 1) {
-    for (int k = 0; k < w; k++) vals[base + 32 * k] = (k == dp) ? 1.0 : 0.0;
-    rhs[i] = bdval[i];
+    const int dps = PERM ? (int)kperm[r0 + dp] : dp;
+    for (int k = 0; k < w; k++) vals[base + 32 * k] = (k == dps) ? 1.0 : 0.0;
+    rhs[ri] = bdval[ri];
     return;
   }
   laplace_row_acc<MAXW>(i, inc_ptr, inc, geo, sigma, w, dp, acc, t);
@@ -224,39 +230,43 @@ __global__ void __launch_bounds__(kBlock) k_poisson_system(
     r += src3[3 * (int64_t)rec.x + inc_a(rec.y)];
   }
   if (tag == 2) {
-    const int32_t r0 = rowptr[i];
     for (int k = 0; k < w; k++) {
-      const int32_t j = colind[r0 + k];
+      const int64_t j = PERM ? (int64_t)nperm[colind[r0 + k]] : (int64_t)colind[r0 + k];
       if (isbd[j] == 1) {
         r = fma(-acc[k][t], bdval[j], r);
         acc[k][t] = 0.0;
       }
     }
   }
-  rhs[i] = r;
-  for (int k = 0; k < w; k++) vals[base + 32 * k] = acc[k][t];
+  rhs[ri] = r;
+  for (int k = 0; k < w; k++) vals[base + 32 * (PERM ? (int)kperm[r0 + k] : k)] = acc[k][t];
 }
 
 cudaError_t launch_poisson_system(const Mesh& m, const double* sigma, const double* src3, const uint8_t* isbd,
-                                  const double* bdval_dense, double* sell_vals, double* rhs, cudaStream_t st) {
+                                  const double* bdval_dense, double* sell_vals, double* rhs, const int32_t* sptr,
+                                  const int32_t* diagpos_mesh, const int32_t* nperm, const uint8_t* kperm,
+                                  cudaStream_t st) {
   const auto* ip = m.d_inc_ptr.as<int32_t>();
   const auto* inc = m.d_inc.as<uint2>();
   const auto* geo = m.d_geo.as<double4>();
   const auto* rp = m.d_rowptr.as<int32_t>();
   const auto* ci = m.d_colind.as<int32_t>();
-  const auto* dp = m.d_diagpos.as<int32_t>();
-  const auto* sp = m.sell.sptr.as<int32_t>();
-  if (m.maxrow <= 8)
-    k_poisson_system<8><<<nblocks(m.nv), kBlock, 0, st>>>(m.nv, ip, inc, geo, sigma, src3, rp, ci, dp, sp, isbd,
-                                                          bdval_dense, sell_vals, rhs);
-  else if (m.maxrow <= 16)
-    k_poisson_system<16><<<nblocks(m.nv), kBlock, 0, st>>>(m.nv, ip, inc, geo, sigma, src3, rp, ci, dp, sp, isbd,
-                                                           bdval_dense, sell_vals, rhs);
-  else if (m.maxrow <= 24)
-    k_poisson_system<24><<<nblocks(m.nv), kBlock, 0, st>>>(m.nv, ip, inc, geo, sigma, src3, rp, ci, dp, sp, isbd,
-                                                           bdval_dense, sell_vals, rhs);
-  else
-    return cudaErrorNotSupported;
+  const auto* dp = diagpos_mesh;
+  const unsigned nb = nblocks(m.nv);
+#define ADFEM_PS(W)                                                                                            \
+  do {                                                                                                         \
+    if (nperm)                                                                                                 \
+      k_poisson_system<W, true><<<nb, kBlock, 0, st>>>(m.nv, ip, inc, geo, sigma, src3, rp, ci, dp, sptr, isbd, \
+                                                       bdval_dense, sell_vals, rhs, nperm, kperm);              \
+    else                                                                                                       \
+      k_poisson_system<W, false><<<nb, kBlock, 0, st>>>(m.nv, ip, inc, geo, sigma, src3, rp, ci, dp, sptr,      \
+                                                        isbd, bdval_dense, sell_vals, rhs, nullptr, nullptr);  \
+  } while (0)
+  if (m.maxrow <= 8) ADFEM_PS(8);
+  else if (m.maxrow <= 16) ADFEM_PS(16);
+  else if (m.maxrow <= 24) ADFEM_PS(24);
+  else return cudaErrorNotSupported;
+#undef ADFEM_PS
   return cudaGetLastError();
 }
 

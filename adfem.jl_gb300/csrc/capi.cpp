@@ -29,8 +29,17 @@ struct adfem_system {
   int64_t ndof = 0;  // nv (Poisson) or 2 nv (elasticity)
   Sell A;            // operator in solver DOF order (interleaved for elasticity)
   DevBuf diagpos;    // int32 [ndof]
-  DevBuf isbd;       // uint8 [ndof] 0 free, 1 Dirichlet, 2 free next to a Dirichlet DOF
-  DevBuf bdval;      // double [ndof] dense Dirichlet values
+  DevBuf isbd;       // uint8 [ndof] 0 free, 1 Dirichlet, 2 free next to a Dirichlet DOF (solver order)
+  DevBuf bdval;      // double [ndof] dense Dirichlet values (solver order)
+  DevBuf isbd_ref;   // uint8 [ndof] the same tags in node order (interleaved for elasticity)
+  // Solver DOF order: elasticity interleaves the [x; y] blocks (2i + c); either kind may
+  // renumber its nodes (reverse Cuthill-McKee) when that at least halves the bandwidth,
+  // so that the banded mixed iteration applies to arbitrarily numbered meshes.
+  bool renumbered = false;
+  std::vector<int32_t> hperm;  // node -> solver node (identity unless renumbered)
+  DevBuf nperm;      // int32 [nv] (renumbered only)
+  DevBuf kperm;      // uint8 [nnz] rank of each mesh pattern slot in its renumbered row
+  DevBuf dofmap;     // int32 [ndof] reference DOF -> solver DOF (elasticity or renumbered)
   DevBuf rhs;        // double [ndof]
   DevBuf sigma, src3, srcy3, Dbar;  // per-element scratch
   DevBuf t0, t1, t2;                // ndof scratch (interleaving, host staging)
@@ -83,39 +92,49 @@ void legacy_report(int st, const char* fn) {
 int system_set_bd(adfem_system* s, const long long* bd, long long nbd, const double* bdval) {
   Mesh& m = *s->mesh->m;
   const int64_t nd = s->ndof;
-  std::vector<uint8_t> tag(nd, 0);
+  const bool el = s->kind == ADFEM_SYS_ELASTICITY;
+  std::vector<uint8_t> tag(nd, 0), tref(nd, 0);
   std::vector<double> val(nd, 0.0);
-  auto map = [&](int64_t d0) -> int64_t {  // reference DOF -> solver DOF
-    if (s->kind == ADFEM_SYS_POISSON) return d0;
-    return d0 < m.nv ? 2 * d0 : 2 * (d0 - m.nv) + 1;
-  };
+  // node (and component) -> solver DOF; -> node-order DOF of the reference tags
+  auto sdof = [&](int64_t i, int c) -> int64_t { return el ? 2 * (int64_t)s->hperm[i] + c : s->hperm[i]; };
+  auto rdof = [&](int64_t i, int c) -> int64_t { return el ? 2 * i + c : i; };
   for (long long k = 0; k < nbd; k++) {
     const long long d = bd[k] - 1;
     if (d < 0 || d >= nd) return fail(ADFEM_ERR_INVALID, "Dirichlet DOF " + std::to_string(bd[k]) + " out of range");
-    const int64_t q = map(d);
+    const int64_t i = el ? (d < m.nv ? d : d - m.nv) : d;
+    const int c = el && d >= m.nv ? 1 : 0;
+    const int64_t q = sdof(i, c);
     if (tag[q]) return fail(ADFEM_ERR_INVALID, "duplicate Dirichlet DOF " + std::to_string(bd[k]));
     tag[q] = 1;
+    tref[rdof(i, c)] = 1;
     val[q] = bdval ? bdval[k] : 0.0;
   }
+  const int nc = el ? 2 : 1;
   for (int64_t i = 0; i < m.nv; i++) {
     bool near = false;
-    for (int32_t k = m.rowptr[i]; k < m.rowptr[i + 1]; k++) {
-      const int64_t j = m.colind[k];
-      if (s->kind == ADFEM_SYS_POISSON) near |= tag[j] == 1;
-      else near |= (tag[2 * j] == 1) || (tag[2 * j + 1] == 1);
-    }
+    for (int32_t k = m.rowptr[i]; k < m.rowptr[i + 1]; k++)
+      for (int c = 0; c < nc; c++) near |= tag[sdof(m.colind[k], c)] == 1;
     if (!near) continue;
-    if (s->kind == ADFEM_SYS_POISSON) {
-      if (tag[i] == 0) tag[i] = 2;
-    } else {
-      if (tag[2 * i] == 0) tag[2 * i] = 2;
-      if (tag[2 * i + 1] == 0) tag[2 * i + 1] = 2;
-    }
+    for (int c = 0; c < nc; c++)
+      if (tag[sdof(i, c)] == 0) {
+        tag[sdof(i, c)] = 2;
+        tref[rdof(i, c)] = 2;
+      }
   }
   ADFEM_TRY(to_dev(s->isbd, tag.data(), tag.size()));
+  ADFEM_TRY(to_dev(s->isbd_ref, tref.data(), tref.size()));
   ADFEM_TRY(to_dev(s->bdval, val.data(), val.size()));
   s->assembled = false;
   return ADFEM_OK;
+}
+
+// vectors between the reference DOF order and the solver's
+bool mapped(const adfem_system* s) { return s->kind == ADFEM_SYS_ELASTICITY || s->renumbered; }
+int to_solver(adfem_system* s, const double* ref, double* sol, cudaStream_t st) {
+  return kerr(launch_to_solver(s->ndof, s->dofmap.as<int32_t>(), ref, sol, st), "to solver order");
+}
+int from_solver(adfem_system* s, const double* sol, double* ref, cudaStream_t st) {
+  return kerr(launch_from_solver(s->ndof, s->dofmap.as<int32_t>(), sol, ref, st), "from solver order");
 }
 
 }  // namespace
@@ -127,7 +146,7 @@ size_t system_device_bytes(const adfem_system* s) {
   const Sell& A = s->A;
   for (const DevBuf* d : {&A.sptr, &A.col, &A.spat, &A.pat, &A.val64, &A.valD64, &A.val32, &s->diagpos, &s->isbd,
                           &s->bdval, &s->rhs, &s->sigma, &s->src3, &s->srcy3, &s->Dbar, &s->t0, &s->t1, &s->t2,
-                          &s->in0, &s->in1})
+                          &s->in0, &s->in1, &s->isbd_ref, &s->nperm, &s->kperm, &s->dofmap})
     b += d->bytes;
   const Solver& v = s->solver;
   for (const DevBuf* d : {&v.s32, &v.state, &v.partials, &v.b, &v.y64, &v.r64, &v.p64, &v.q64, &v.r32, &v.pa32,
@@ -882,34 +901,78 @@ int adfem_system_create(adfem_mesh* mesh, int kind, adfem_system** out) {
   s->mesh = mesh;
   s->kind = kind;
   Mesh& m = *mesh->m;
+  if (kind == ADFEM_SYS_ELASTICITY && m.maxrow > 16)
+    return fail(ADFEM_ERR_UNSUPPORTED, "elasticity systems support at most 15 neighbours per node");
+  // node numbering of the solver: reverse Cuthill-McKee when it at least halves the band
+  // (not tried when the band is already within 4 sqrt(n), about what RCM reaches on a
+  // planar mesh)
+  {
+    std::vector<int32_t> pi;
+    const bool try_rcm = (double)m.sell.band > 4.0 * std::sqrt((double)m.nv);
+    const int64_t rb = try_rcm ? mesh_rcm(m, pi) : m.sell.band;
+    s->renumbered = try_rcm && 2 * rb < m.sell.band;
+    if (s->renumbered) s->hperm = std::move(pi);
+    else {
+      s->hperm.resize(m.nv);
+      for (int64_t i = 0; i < m.nv; i++) s->hperm[i] = (int32_t)i;
+    }
+  }
+  const std::vector<int32_t>& pi = s->hperm;
+  // scalar pattern in solver order: row pi(i) holds the sorted pi(j); kp = rank of each
+  // mesh slot in its renumbered row
+  std::vector<int32_t> rpS(m.nv + 1, 0), ciS(m.nnz), dpS(m.nv);
+  std::vector<uint8_t> kp(m.nnz);
+  {
+    std::vector<int32_t> inv(m.nv);
+    for (int64_t i = 0; i < m.nv; i++) inv[pi[i]] = (int32_t)i;
+    for (int64_t r = 0; r < m.nv; r++) rpS[r + 1] = rpS[r] + (m.rowptr[inv[r] + 1] - m.rowptr[inv[r]]);
+    std::vector<std::pair<int32_t, int32_t>> tmp;
+    for (int64_t i = 0; i < m.nv; i++) {
+      tmp.clear();
+      for (int32_t k = m.rowptr[i]; k < m.rowptr[i + 1]; k++) tmp.emplace_back(pi[m.colind[k]], k - m.rowptr[i]);
+      std::sort(tmp.begin(), tmp.end());
+      const int64_t r = pi[i];
+      for (size_t q = 0; q < tmp.size(); q++) {
+        ciS[rpS[r] + q] = tmp[q].first;
+        kp[m.rowptr[i] + tmp[q].second] = (uint8_t)q;
+        if (tmp[q].first == r) dpS[r] = (int32_t)q;
+      }
+    }
+  }
   if (kind == ADFEM_SYS_POISSON) {
     s->ndof = m.nv;
-    ADFEM_TRY(sell_build_pattern(m.nv, m.rowptr.data(), m.colind.data(), s->A, 1));
-    std::vector<int32_t> dp(m.nv);
-    for (int64_t i = 0; i < m.nv; i++)
-      for (int32_t k = m.rowptr[i]; k < m.rowptr[i + 1]; k++)
-        if (m.colind[k] == i) dp[i] = k - m.rowptr[i];
-    ADFEM_TRY(to_dev(s->diagpos, dp.data(), dp.size()));
+    ADFEM_TRY(sell_build_pattern(m.nv, rpS.data(), ciS.data(), s->A, 1));
+    ADFEM_TRY(to_dev(s->diagpos, dpS.data(), dpS.size()));
+    if (s->renumbered) ADFEM_TRY(to_dev(s->dofmap, pi.data(), pi.size()));
   } else {
-    if (m.maxrow > 16) return fail(ADFEM_ERR_UNSUPPORTED, "elasticity systems support at most 15 neighbours per node");
     s->ndof = 2 * m.nv;
     std::vector<int32_t> rp2(2 * m.nv + 1, 0), dp2(2 * m.nv);
     for (int64_t r = 0; r < 2 * m.nv; r++) {
       const int64_t i = r >> 1;
-      rp2[r + 1] = rp2[r] + 2 * (m.rowptr[i + 1] - m.rowptr[i]);
+      rp2[r + 1] = rp2[r] + 2 * (rpS[i + 1] - rpS[i]);
+      dp2[r] = 2 * dpS[i] + (int32_t)(r & 1);
     }
     std::vector<int32_t> ci2(rp2[2 * m.nv]);
     for (int64_t r = 0; r < 2 * m.nv; r++) {
       const int64_t i = r >> 1;
       int32_t z = rp2[r];
-      for (int32_t k = m.rowptr[i]; k < m.rowptr[i + 1]; k++) {
-        if (m.colind[k] == i) dp2[r] = 2 * (k - m.rowptr[i]) + (int32_t)(r & 1);
-        ci2[z++] = 2 * m.colind[k];
-        ci2[z++] = 2 * m.colind[k] + 1;
+      for (int32_t k = rpS[i]; k < rpS[i + 1]; k++) {
+        ci2[z++] = 2 * ciS[k];
+        ci2[z++] = 2 * ciS[k] + 1;
       }
     }
     ADFEM_TRY(sell_build_pattern(2 * m.nv, rp2.data(), ci2.data(), s->A, 2));
     ADFEM_TRY(to_dev(s->diagpos, dp2.data(), dp2.size()));
+    std::vector<int32_t> map(2 * m.nv);
+    for (int64_t i = 0; i < m.nv; i++) {
+      map[i] = 2 * pi[i];
+      map[m.nv + i] = 2 * pi[i] + 1;
+    }
+    ADFEM_TRY(to_dev(s->dofmap, map.data(), map.size()));
+  }
+  if (s->renumbered) {
+    ADFEM_TRY(to_dev(s->nperm, pi.data(), pi.size()));
+    ADFEM_TRY(to_dev(s->kperm, kp.data(), kp.size()));
   }
   const size_t ne = std::max<int64_t>(s->A.nent, 1);
   ADFEM_TRY(s->A.val64.alloc(sizeof(double) * ne));
@@ -952,7 +1015,10 @@ static int assemble_poisson(adfem_system* sys, const double* kappa_d, const doub
                  "element prepass"));
   if (ev) ADFEM_CUDA(cudaEventRecord(ev[1], st));
   ADFEM_TRY(kerr(launch_poisson_system(m, sys->sigma.as<double>(), sys->src3.as<double>(), sys->isbd.as<uint8_t>(),
-                                       sys->bdval.as<double>(), sys->A.val64.as<double>(), sys->rhs.as<double>(), st),
+                                       sys->bdval.as<double>(), sys->A.val64.as<double>(), sys->rhs.as<double>(),
+                                       sys->A.sptr.as<int32_t>(), m.d_diagpos.as<int32_t>(),
+                                       sys->renumbered ? sys->nperm.as<int32_t>() : nullptr,
+                                       sys->renumbered ? sys->kperm.as<uint8_t>() : nullptr, st),
                  "poisson system"));
   if (ev) ADFEM_CUDA(cudaEventRecord(ev[2], st));
   ADFEM_TRY(solver_prepare(sys->solver, sys->diagpos.as<int32_t>(), st));
@@ -1004,7 +1070,9 @@ int adfem_system_assemble_elasticity_d(adfem_system* sys, const double* E_d, con
   ADFEM_TRY(kerr(launch_element_prepass(m, nullptr, fy_d, nullptr, sys->srcy3.as<double>(), st), "prepass fy"));
   ADFEM_TRY(kerr(launch_elastic_system(m, sys->Dbar.as<double>(), sys->src3.as<double>(), sys->srcy3.as<double>(),
                                        sys->A.sptr.as<int32_t>(), sys->isbd.as<uint8_t>(), sys->bdval.as<double>(),
-                                       sys->A.val64.as<double>(), sys->rhs.as<double>(), st),
+                                       sys->A.val64.as<double>(), sys->rhs.as<double>(),
+                                       sys->renumbered ? sys->nperm.as<int32_t>() : nullptr,
+                                       sys->renumbered ? sys->kperm.as<uint8_t>() : nullptr, st),
                  "elastic system"));
   ADFEM_TRY(solver_prepare(sys->solver, sys->diagpos.as<int32_t>(), st));
   sys->assembled = true;
@@ -1020,15 +1088,14 @@ int adfem_system_solve_d(adfem_system* sys, double* u_d, const adfem_solver_opts
   adfem_solver_opts_default(&o);
   if (opts) o = *opts;
   cudaStream_t st = S(stream);
-  if (sys->kind == ADFEM_SYS_POISSON)
+  if (!mapped(sys))
     return solver_solve(sys->solver, sys->rhs.as<double>(), u_d, nullptr, sys->isbd.as<uint8_t>(),
                         sys->bdval.as<double>(), o, stats, st);
-  const int64_t nv = sys->mesh->m->nv;
-  if (o.warm_start) ADFEM_TRY(kerr(launch_to_interleaved(nv, u_d, sys->t0.as<double>(), st), "interleave"));
+  if (o.warm_start) ADFEM_TRY(to_solver(sys, u_d, sys->t0.as<double>(), st));
   const int r = solver_solve(sys->solver, sys->rhs.as<double>(), sys->t0.as<double>(), nullptr,
                              sys->isbd.as<uint8_t>(), sys->bdval.as<double>(), o, stats, st);
   if (r != ADFEM_OK && r != ADFEM_ERR_NOT_CONVERGED) return r;
-  ADFEM_TRY(kerr(launch_from_interleaved(nv, sys->t0.as<double>(), u_d, st), "deinterleave"));
+  ADFEM_TRY(from_solver(sys, sys->t0.as<double>(), u_d, st));
   return r;
 }
 
@@ -1064,6 +1131,7 @@ int adfem_system_solver_info(const adfem_system* sys, adfem_solver_info* info) {
   info->blocks = sv.zcg ? sv.zgrid : 0;
   info->rows_per_block = sv.zcg ? sv.zL : 0;
   info->ring = sv.zcg ? sv.zW : 0;
+  info->renumbered = sys->renumbered ? 1 : 0;
   return ADFEM_OK;
 }
 
@@ -1103,13 +1171,12 @@ int system_solve_packed(adfem_system** sys, int count, double** out, const doubl
     it.zero_rows = adjoint ? s->isbd.as<uint8_t>() : nullptr;
     it.fix_rows = s->isbd.as<uint8_t>();
     it.fix_vals = adjoint ? nullptr : s->bdval.as<double>();
-    if (s->kind == ADFEM_SYS_POISSON) {
+    if (!mapped(s)) {
       it.rhs = adjoint ? g[i] : s->rhs.as<double>();
       it.u = out[i];
     } else {
-      const int64_t nv = s->mesh->m->nv;
-      if (adjoint) ADFEM_TRY(kerr(launch_to_interleaved(nv, g[i], s->t1.as<double>(), st), "interleave"));
-      if (it.warm) ADFEM_TRY(kerr(launch_to_interleaved(nv, out[i], s->t0.as<double>(), st), "interleave"));
+      if (adjoint) ADFEM_TRY(to_solver(s, g[i], s->t1.as<double>(), st));
+      if (it.warm) ADFEM_TRY(to_solver(s, out[i], s->t0.as<double>(), st));
       it.rhs = adjoint ? s->t1.as<double>() : s->rhs.as<double>();
       it.u = s->t0.as<double>();
     }
@@ -1118,8 +1185,7 @@ int system_solve_packed(adfem_system** sys, int count, double** out, const doubl
   int status = ADFEM_OK;
   for (int i = 0; i < count; i++) {
     adfem_system* s = sys[i];
-    if (s->kind == ADFEM_SYS_ELASTICITY)
-      ADFEM_TRY(kerr(launch_from_interleaved(s->mesh->m->nv, s->t0.as<double>(), out[i], st), "deinterleave"));
+    if (mapped(s)) ADFEM_TRY(from_solver(s, s->t0.as<double>(), out[i], st));
     if (stats) {
       stats[i].iterations = items[i].iters;
       stats[i].updates = items[i].passes;
@@ -1157,16 +1223,15 @@ int adfem_system_adjoint_d(adfem_system* sys, const double* g_d, double* lam_d, 
   adfem_solver_opts_default(&o);
   if (opts) o = *opts;
   cudaStream_t st = S(stream);
-  if (sys->kind == ADFEM_SYS_POISSON)
+  if (!mapped(sys))
     return solver_solve(sys->solver, g_d, lam_d, sys->isbd.as<uint8_t>(), sys->isbd.as<uint8_t>(), nullptr, o, stats,
                         st);
-  const int64_t nv = sys->mesh->m->nv;
-  ADFEM_TRY(kerr(launch_to_interleaved(nv, g_d, sys->t1.as<double>(), st), "interleave"));
-  if (o.warm_start) ADFEM_TRY(kerr(launch_to_interleaved(nv, lam_d, sys->t0.as<double>(), st), "interleave"));
+  ADFEM_TRY(to_solver(sys, g_d, sys->t1.as<double>(), st));
+  if (o.warm_start) ADFEM_TRY(to_solver(sys, lam_d, sys->t0.as<double>(), st));
   const int r = solver_solve(sys->solver, sys->t1.as<double>(), sys->t0.as<double>(), sys->isbd.as<uint8_t>(),
                              sys->isbd.as<uint8_t>(), nullptr, o, stats, st);
   if (r != ADFEM_OK && r != ADFEM_ERR_NOT_CONVERGED) return r;
-  ADFEM_TRY(kerr(launch_from_interleaved(nv, sys->t0.as<double>(), lam_d, st), "deinterleave"));
+  ADFEM_TRY(from_solver(sys, sys->t0.as<double>(), lam_d, st));
   return r;
 }
 
@@ -1174,7 +1239,7 @@ int adfem_system_grad_kappa_d(adfem_system* sys, const double* u_d, const double
                               void* stream) {
   if (!sys || !u_d || !lam_d || !grad_kappa_d) return fail(ADFEM_ERR_INVALID, "null argument");
   if (sys->kind != ADFEM_SYS_POISSON) return fail(ADFEM_ERR_INVALID, "not a Poisson system");
-  ADFEM_TRY(kerr(launch_poisson_kappa_grad(*sys->mesh->m, u_d, lam_d, sys->isbd.as<uint8_t>(), grad_kappa_d,
+  ADFEM_TRY(kerr(launch_poisson_kappa_grad(*sys->mesh->m, u_d, lam_d, sys->isbd_ref.as<uint8_t>(), grad_kappa_d,
                                            S(stream)),
                  "kappa grad"));
   return ADFEM_OK;
@@ -1191,7 +1256,7 @@ int adfem_system_grad_E_d(adfem_system* sys, const double* u_d, const double* la
   ADFEM_TRY(kerr(launch_to_interleaved(nv, u_d, sys->t1.as<double>(), st), "interleave"));
   ADFEM_TRY(kerr(launch_to_interleaved(nv, lam_d, sys->t2.as<double>(), st), "interleave"));
   ADFEM_TRY(kerr(launch_elastic_grad_E(*sys->mesh->m, sys->t1.as<double>(), sys->t2.as<double>(),
-                                       sys->isbd.as<uint8_t>(), nu_d, grad_E_d, st),
+                                       sys->isbd_ref.as<uint8_t>(), nu_d, grad_E_d, st),
                  "grad E"));
   return ADFEM_OK;
 }
@@ -1201,11 +1266,10 @@ int adfem_system_apply_d(adfem_system* sys, const double* x_d, double* y_d, void
   std::lock_guard<std::mutex> lk(sys->mu);
   if (!sys->assembled) return fail(ADFEM_ERR_INVALID, "system not assembled");
   cudaStream_t st = S(stream);
-  if (sys->kind == ADFEM_SYS_POISSON) return solver_apply(sys->solver, x_d, y_d, st);
-  const int64_t nv = sys->mesh->m->nv;
-  ADFEM_TRY(kerr(launch_to_interleaved(nv, x_d, sys->t1.as<double>(), st), "interleave"));
+  if (!mapped(sys)) return solver_apply(sys->solver, x_d, y_d, st);
+  ADFEM_TRY(to_solver(sys, x_d, sys->t1.as<double>(), st));
   ADFEM_TRY(solver_apply(sys->solver, sys->t1.as<double>(), sys->t2.as<double>(), st));
-  ADFEM_TRY(kerr(launch_from_interleaved(nv, sys->t2.as<double>(), y_d, st), "deinterleave"));
+  ADFEM_TRY(from_solver(sys, sys->t2.as<double>(), y_d, st));
   return ADFEM_OK;
 }
 
@@ -1214,12 +1278,11 @@ int adfem_system_rhs_d(adfem_system* sys, double* rhs_d, void* stream) {
   std::lock_guard<std::mutex> lk(sys->mu);
   if (!sys->assembled) return fail(ADFEM_ERR_INVALID, "system not assembled");
   cudaStream_t st = S(stream);
-  if (sys->kind == ADFEM_SYS_POISSON) {
+  if (!mapped(sys)) {
     ADFEM_CUDA(cudaMemcpyAsync(rhs_d, sys->rhs.p, sizeof(double) * sys->ndof, cudaMemcpyDeviceToDevice, st));
     return ADFEM_OK;
   }
-  ADFEM_TRY(kerr(launch_from_interleaved(sys->mesh->m->nv, sys->rhs.as<double>(), rhs_d, st), "deinterleave"));
-  return ADFEM_OK;
+  return from_solver(sys, sys->rhs.as<double>(), rhs_d, st);
 }
 
 int adfem_poisson_solve(adfem_system* sys, const double* kappa, const double* f, double* u,

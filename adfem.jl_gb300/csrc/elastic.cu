@@ -202,7 +202,9 @@ cudaError_t launch_stiffness_rows(const Mesh& m, const double* Dbar, double* val
 // slot 2k is the x-column of the k-th neighbour, slot 2k+1 its y-column.
 // isbd: 0 free, 1 Dirichlet DOF, 2 free with a Dirichlet neighbour (interleaved ids).
 // rhs: body force [src(fx); src(fy)] interleaved, minus the Dirichlet lift.
-template <int MAXW>
+// PERM: nodes renumbered (nperm[node]); row 2i+c goes to solver row 2 nperm[i] + c and
+// slot 2k+cc to 2 kperm[rowptr[i] + k] + cc; isbd, bdval and rhs in solver order.
+template <int MAXW, bool PERM>
 __global__ void __launch_bounds__(kB) k_elastic_system(int64_t nv, const int32_t* __restrict__ inc_ptr,
                                                        const uint2* __restrict__ inc,
                                                        const double2* __restrict__ grad,
@@ -214,7 +216,9 @@ __global__ void __launch_bounds__(kB) k_elastic_system(int64_t nv, const int32_t
                                                        const int32_t* __restrict__ sptr,
                                                        const uint8_t* __restrict__ isbd,
                                                        const double* __restrict__ bdval,
-                                                       double* __restrict__ vals, double* __restrict__ rhs) {
+                                                       double* __restrict__ vals, double* __restrict__ rhs,
+                                                       const int32_t* __restrict__ nperm,
+                                                       const uint8_t* __restrict__ kperm) {
   __shared__ double acc[2 * MAXW][kB];
   const int t = threadIdx.x;
   const int64_t r = gtid();
@@ -222,16 +226,20 @@ __global__ void __launch_bounds__(kB) k_elastic_system(int64_t nv, const int32_t
   const int64_t i = r >> 1;
   const int c = (int)(r & 1);
   const int w = rowptr[i + 1] - rowptr[i];
-  const int64_t base = (int64_t)sptr[r >> 5] + (r & 31);
-  const uint8_t tag = isbd[r];
+  const int32_t r0 = rowptr[i];
+  const int64_t rs = PERM ? 2 * (int64_t)nperm[i] + c : r;
+  const int64_t base = (int64_t)sptr[rs >> 5] + (rs & 31);
+  auto slot = [&](int k) { return PERM ? (int)kperm[r0 + k] : k; };
+  const uint8_t tag = isbd[rs];
   if (tag == 1) {
     // diagonal: slot 2*diagpos + c
-    const int32_t* row = colind + rowptr[i];
+    const int32_t* row = colind + r0;
     int dk = 0;
     for (int k = 0; k < w; k++)
       if (row[k] == i) dk = k;
-    for (int k = 0; k < 2 * w; k++) vals[base + 32 * k] = (k == 2 * dk + c) ? 1.0 : 0.0;
-    rhs[r] = bdval[r];
+    const int ds = 2 * slot(dk) + c;
+    for (int k = 0; k < 2 * w; k++) vals[base + 32 * k] = (k == ds) ? 1.0 : 0.0;
+    rhs[rs] = bdval[rs];
     return;
   }
   for (int k = 0; k < 2 * w; k++) acc[k][t] = 0.0;
@@ -250,9 +258,9 @@ __global__ void __launch_bounds__(kB) k_elastic_system(int64_t nv, const int32_t
     rr += src[3 * (int64_t)e + a];
   }
   if (tag == 2) {
-    const int32_t* row = colind + rowptr[i];
+    const int32_t* row = colind + r0;
     for (int k = 0; k < w; k++) {
-      const int64_t j = row[k];
+      const int64_t j = PERM ? (int64_t)nperm[row[k]] : (int64_t)row[k];
 #pragma unroll
       for (int cc = 0; cc < 2; cc++) {
         const int64_t dj = 2 * j + cc;
@@ -263,27 +271,36 @@ __global__ void __launch_bounds__(kB) k_elastic_system(int64_t nv, const int32_t
       }
     }
   }
-  rhs[r] = rr;
-  for (int k = 0; k < 2 * w; k++) vals[base + 32 * k] = acc[k][t];
+  rhs[rs] = rr;
+  for (int k = 0; k < w; k++) {
+    const int sk = 2 * slot(k);
+    vals[base + 32 * sk] = acc[2 * k][t];
+    vals[base + 32 * (sk + 1)] = acc[2 * k + 1][t];
+  }
 }
 
 cudaError_t launch_elastic_system(const Mesh& m, const double* Dbar, const double* srcx, const double* srcy,
                                   const int32_t* sptr2, const uint8_t* isbd2, const double* bdval2, double* vals,
-                                  double* rhs, cudaStream_t st) {
+                                  double* rhs, const int32_t* nperm, const uint8_t* kperm, cudaStream_t st) {
   const auto* ip = m.d_inc_ptr.as<int32_t>();
   const auto* inc = m.d_inc.as<uint2>();
   const auto* gr = m.d_grad.as<double2>();
   const auto* rp = m.d_rowptr.as<int32_t>();
   const auto* ci = m.d_colind.as<int32_t>();
   const unsigned nb = nblk(2 * m.nv, kB);
-  if (m.maxrow <= 8)
-    k_elastic_system<8><<<nb, kB, 0, st>>>(m.nv, ip, inc, gr, Dbar, srcx, srcy, rp, ci, sptr2, isbd2, bdval2, vals,
-                                           rhs);
-  else if (m.maxrow <= 16)
-    k_elastic_system<16><<<nb, kB, 0, st>>>(m.nv, ip, inc, gr, Dbar, srcx, srcy, rp, ci, sptr2, isbd2, bdval2, vals,
-                                            rhs);
-  else
-    return cudaErrorNotSupported;
+#define ADFEM_ES(W)                                                                                              \
+  do {                                                                                                           \
+    if (nperm)                                                                                                   \
+      k_elastic_system<W, true><<<nb, kB, 0, st>>>(m.nv, ip, inc, gr, Dbar, srcx, srcy, rp, ci, sptr2, isbd2,    \
+                                                   bdval2, vals, rhs, nperm, kperm);                            \
+    else                                                                                                         \
+      k_elastic_system<W, false><<<nb, kB, 0, st>>>(m.nv, ip, inc, gr, Dbar, srcx, srcy, rp, ci, sptr2, isbd2,   \
+                                                    bdval2, vals, rhs, nullptr, nullptr);                       \
+  } while (0)
+  if (m.maxrow <= 8) ADFEM_ES(8);
+  else if (m.maxrow <= 16) ADFEM_ES(16);
+  else return cudaErrorNotSupported;
+#undef ADFEM_ES
   return cudaGetLastError();
 }
 
@@ -422,6 +439,30 @@ cudaError_t launch_elastic_grad_E(const Mesh& m, const double* u2, const double*
                                   const double* nu, double* gE, cudaStream_t st) {
   k_elastic_grad_E<<<nblk(m.ne, 256), 256, 0, st>>>(m.ne, m.d_conn.as<int4>(), m.d_grad.as<double2>(),
                                                     m.d_geo.as<double4>(), u2, lam2, isbd2, nu, gE);
+  return cudaGetLastError();
+}
+
+// reference order <-> solver order through a DOF map: sol[map[d]] = ref[d]
+__global__ void k_to_solver(int64_t n, const int32_t* __restrict__ map, const double* __restrict__ ref,
+                            double* __restrict__ sol) {
+  const int64_t d = gtid();
+  if (d >= n) return;
+  sol[map[d]] = ref[d];
+}
+__global__ void k_from_solver(int64_t n, const int32_t* __restrict__ map, const double* __restrict__ sol,
+                              double* __restrict__ ref) {
+  const int64_t d = gtid();
+  if (d >= n) return;
+  ref[d] = sol[map[d]];
+}
+cudaError_t launch_to_solver(int64_t n, const int32_t* map, const double* ref, double* sol, cudaStream_t st) {
+  if (n <= 0) return cudaSuccess;
+  k_to_solver<<<nblk(n, 256), 256, 0, st>>>(n, map, ref, sol);
+  return cudaGetLastError();
+}
+cudaError_t launch_from_solver(int64_t n, const int32_t* map, const double* sol, double* ref, cudaStream_t st) {
+  if (n <= 0) return cudaSuccess;
+  k_from_solver<<<nblk(n, 256), 256, 0, st>>>(n, map, sol, ref);
   return cudaGetLastError();
 }
 

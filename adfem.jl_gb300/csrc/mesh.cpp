@@ -462,6 +462,73 @@ int64_t mesh_bcnode(Mesh* m, int64_t* out1) {
   return c;
 }
 
+// Reverse Cuthill-McKee order of the node graph: per connected component a BFS from a
+// pseudo-peripheral node (two BFS sweeps from a minimum-degree node, each restarting at
+// the last node reached), neighbours visited in ascending degree, the whole order then
+// reversed.  pi[node] = new index.  Returns the bandwidth max |pi(i) - pi(j)| over the
+// pattern.
+int64_t mesh_rcm(const Mesh& m, std::vector<int32_t>& pi) {
+  const int64_t n = m.nv;
+  auto deg = [&](int64_t i) { return m.rowptr[i + 1] - m.rowptr[i]; };
+  std::vector<int32_t> order;
+  order.reserve(n);
+  std::vector<uint8_t> seen(n, 0), mark(n, 0);
+  std::vector<int32_t> q, nb;
+  q.reserve(n);
+  // BFS from s over the unseen part of the graph (marks in `mark` reset afterwards);
+  // returns the last node reached
+  auto sweep = [&](int32_t s) {
+    q.clear();
+    q.push_back(s);
+    mark[s] = 1;
+    for (size_t h = 0; h < q.size(); h++) {
+      const int32_t v = q[h];
+      for (int32_t k = m.rowptr[v]; k < m.rowptr[v + 1]; k++) {
+        const int32_t j = m.colind[k];
+        if (!seen[j] && !mark[j]) {
+          mark[j] = 1;
+          q.push_back(j);
+        }
+      }
+    }
+    for (int32_t v : q) mark[v] = 0;
+    return q.back();
+  };
+  for (int64_t start = 0; start < n; start++) {
+    if (seen[start]) continue;
+    // minimum-degree node of this component
+    sweep((int32_t)start);
+    int32_t s = (int32_t)start;
+    for (int32_t v : q)
+      if (deg(v) < deg(s)) s = v;
+    for (int r = 0; r < 2; r++) s = sweep(s);
+    // Cuthill-McKee BFS from s
+    const size_t c0 = order.size();
+    order.push_back(s);
+    seen[s] = 1;
+    for (size_t h = c0; h < order.size(); h++) {
+      const int32_t v = order[h];
+      nb.clear();
+      for (int32_t k = m.rowptr[v]; k < m.rowptr[v + 1]; k++) {
+        const int32_t j = m.colind[k];
+        if (!seen[j]) {
+          seen[j] = 1;
+          nb.push_back(j);
+        }
+      }
+      std::stable_sort(nb.begin(), nb.end(), [&](int32_t a, int32_t b) { return deg(a) < deg(b); });
+      order.insert(order.end(), nb.begin(), nb.end());
+    }
+  }
+  pi.assign(n, 0);
+  for (int64_t k = 0; k < n; k++) pi[order[k]] = (int32_t)(n - 1 - k);
+  int64_t band = 0;
+  for (int64_t i = 0; i < n; i++)
+    for (int32_t k = m.rowptr[i]; k < m.rowptr[i + 1]; k++)
+      band = std::max<int64_t>(band, std::llabs((int64_t)pi[i] - pi[m.colind[k]]));
+  return band;
+}
+
 int64_t mesh_ndof(Mesh* m) {
   if (m->degree != 2) return m->nv;
   mesh_edges(m);

@@ -375,6 +375,8 @@ typedef struct adfem_solver_info {
   int blocks;                 /* blocks of the banded iteration kernel (0 if not banded) */
   long long rows_per_block;   /* contiguous rows per block (0 if not banded) */
   int ring;                   /* shared-memory positions per super-tile: rows + 2 band (0 if not banded) */
+  int renumbered;             /* 1: nodes renumbered for the solver (reverse Cuthill-McKee; inputs and
+                                 outputs stay in the reference order) */
 } adfem_solver_info;
 ADFEM_API int adfem_system_solver_info(const adfem_system *sys, adfem_solver_info *info);
 /* Packed solves of small systems: the systems (each assembled, at most 16384 DOFs,

@@ -73,30 +73,90 @@ def test_banded_path_super_tiles_and_deterministic(oracle, gpulib, monkeypatch):
     assert rel(u3, u64) < 1e-9
 
 
-@pytest.mark.parametrize("m,banded", [(40, 1), (80, 0)])
-def test_randomly_renumbered_mesh(oracle, gpulib, monkeypatch, m, banded):
-    # a random node numbering spreads the band over the whole matrix: at 1681 DOF a
-    # super-tile still holds every column its rows need; at 6561 DOF the band exceeds
-    # what shared memory can hold and the scaled two-kernel path takes over
-    import torch
-
-    monkeypatch.delenv("ADFEM_ZCG", raising=False)
-    coords, elems = synth.jittered_square(m, seed=3)
-    perm = np.random.default_rng(5).permutation(coords.shape[0])  # new id of old node i: inv[i]
+def renumbered(m, seed=3):
+    """Jittered square with a random node numbering: (coords, elems) in the original and the
+    permuted numbering, and inv (new id of old node i)."""
+    coords, elems = synth.jittered_square(m, seed=seed)
+    perm = np.random.default_rng(5).permutation(coords.shape[0])
     inv = np.empty_like(perm)
     inv[perm] = np.arange(perm.size)
-    coords_p = coords[perm]
-    elems_p = inv[elems - 1] + 1
+    return coords, elems, coords[perm], inv[elems - 1] + 1, inv
+
+
+@pytest.mark.parametrize("m", [40, 80])
+def test_randomly_renumbered_mesh(oracle, gpulib, monkeypatch, m):
+    # A random node numbering spreads the band over the whole matrix.  The resident system
+    # renumbers its nodes (reverse Cuthill-McKee) so the banded mixed iteration applies;
+    # every input and output stays in the caller's numbering.
+    import torch
+
+    from adfem_gpu import system as SY
+
+    monkeypatch.delenv("ADFEM_ZCG", raising=False)
+    coords, elems, coords_p, elems_p, inv = renumbered(m)
     O = oracle.OracleMesh(coords_p, elems_p)
     g = O.gauss_nodes()
     kappa, f = synth.poisson_c1_fields(g[:, 0], g[:, 1])
     bd = O.bcnode()
-    B, r = oracle.dirichlet_csc(O.laplace_csc(kappa), O.source(f), bd, np.zeros(bd.size))
+    bv = np.cos(2 * O.coords[bd - 1, 0])
+    B, r = oracle.dirichlet_csc(O.laplace_csc(kappa), O.source(f), bd, bv)
+    t = lambda a: torch.tensor(a, device="cuda")  # noqa: E731
     S = gpulib.PoissonSystem(gpulib.Mesh(coords_p, elems_p))
-    S.set_dirichlet(bd)
-    S.assemble(torch.tensor(kappa, device="cuda"), torch.tensor(f, device="cuda"))
+    S.set_dirichlet(bd, bv)
+    S.assemble(t(kappa), t(f))
     info = S.solver_info()
-    assert info["banded"] == banded, info
+    assert info["renumbered"] == 1 and info["banded"] == 1, info
+    assert info["band"] < 4 * m
+    u0 = oracle.spsolve(B, r)
+    for prec, rtol in (("mixed", RTOL_MIXED), ("fp64", 1e-12)):
+        u = S.solve(precision=prec, rtol=rtol)
+        assert S.last_stats.status == 0
+        assert rel(u.cpu().numpy(), u0) < 1e-9
+    assert rel(S.rhs().cpu().numpy(), r) < 1e-12
+    x = np.random.default_rng(1).standard_normal(O.ndof)
+    assert rel(S.apply(t(x)).cpu().numpy(), B @ x) < 1e-12
+    (up,), _ = SY.solve_packed([S], rtol=1e-11)
+    assert rel(up.cpu().numpy(), u0) < 1e-9
+    # adjoint gradient against the same problem in the natural numbering (same elements,
+    # same Gauss points): the gradients agree
+    S2 = gpulib.PoissonSystem(gpulib.Mesh(coords, elems))
+    S2.set_dirichlet(np.sort(np.argsort(inv)[bd - 1] + 1), bv[np.argsort(np.argsort(inv)[bd - 1])])
+    S2.assemble(t(kappa), t(f))
+    assert S2.solver_info()["renumbered"] == 0
+    obs = np.arange(1, O.ndof + 1, 7)
+    grads = []
+    for SS, ob in ((S, obs), (S2, np.argsort(inv)[obs - 1] + 1)):
+        uu = SS.solve(precision="fp64", rtol=1e-13)
+        gu = torch.zeros_like(uu)
+        gu[torch.tensor(ob - 1, device="cuda")] = 2 * uu[torch.tensor(ob - 1, device="cuda")]
+        lam = SS.adjoint(gu, precision="fp64", rtol=1e-13)
+        grads.append(SS.grad_kappa(uu, lam).cpu().numpy())
+    assert rel(grads[0], grads[1]) < 1e-8
+
+
+def test_renumbered_elasticity(oracle, gpulib, monkeypatch):
+    import torch
+
+    monkeypatch.delenv("ADFEM_ZCG", raising=False)
+    coords, elems, coords_p, elems_p, inv = renumbered(30, seed=6)
+    O = oracle.OracleMesh(coords_p, elems_p)
+    g = O.gauss_nodes()
+    E = 1e9 * np.exp(0.3 * synth.fourier_field(g[:, 0], g[:, 1], seed=2))
+    nu = np.full(O.ngauss, 0.3)
+    K = O.stiffness_csc(oracle.plane_strain(E, nu, 0))
+    fx, fy = np.zeros(O.ngauss), np.full(O.ngauss, -1e6)
+    left = synth.left_edge_nodes(coords_p)
+    bd = np.concatenate([left + 1, left + 1 + O.ndof])
+    B, r = oracle.dirichlet_csc(K, np.concatenate([O.source(fx), O.source(fy)]), bd, np.zeros(bd.size))
+    S = gpulib.ElasticitySystem(gpulib.Mesh(coords_p, elems_p))
+    S.set_dirichlet(bd)
+    t = lambda a: torch.tensor(a, device="cuda")  # noqa: E731
+    S.assemble(t(E), t(nu), t(fx), t(fy))
+    info = S.solver_info()
+    assert info["renumbered"] == 1 and info["banded"] == 1, info
+    assert rel(S.rhs().cpu().numpy(), r) < 1e-12
+    x = np.random.default_rng(2).standard_normal(2 * O.ndof)
+    assert rel(S.apply(t(x)).cpu().numpy(), B @ x) < 1e-12
     u = S.solve(precision="mixed", rtol=RTOL_MIXED)
     assert S.last_stats.status == 0
     assert rel(u.cpu().numpy(), oracle.spsolve(B, r)) < 1e-9
