@@ -526,6 +526,12 @@ static constexpr int kZPerSM = 1024 / kZBT;          // resident blocks per SM (
 #endif
 static constexpr int kZU1 = ADFEM_ZCG_U1;            // phase-1 positions per thread and trip
 static constexpr int kZU2 = ADFEM_ZCG_U2;            // phase-2 matrix rows per thread and trip
+#ifndef ADFEM_ZCG_U2_WIDE
+#define ADFEM_ZCG_U2_WIDE 1
+#endif
+// rows per trip of the 16-wide variants: two rows of 16 entries do not fit the 64 registers
+// of a two-blocks-per-SM launch (they spill)
+static constexpr int kZU2W = ADFEM_ZCG_U2_WIDE;
 static constexpr size_t kZSmemBlock = (kZPerSM >= 2 ? 100 : 200) * 1024;  // shared memory per block
 
 // Distinct slice column patterns (at most kZMaxPatterns; further slices use their
@@ -576,7 +582,7 @@ static int zcg_build_pool(Solver& S) {
 
 template <int MAXW, bool B2>
 static int zcg_configure(Solver& S, int sms) {
-  auto kern = k_zcg_iter<MAXW, kZBT, kZU1, kZU2, B2>;
+  auto kern = k_zcg_iter<MAXW, kZBT, kZU1, (MAXW > 8 ? kZU2W : kZU2), B2>;
   // The shared-memory limit is raised once per process to the most any plan uses:
   // changing a kernel's attributes while another thread captures a graph with that
   // kernel invalidates the capture.
@@ -708,8 +714,8 @@ static ZcgArgs zcg_args(Solver& S) {
 void zcg_enqueue_iter(Solver& S, cudaStream_t st) {
   const ZcgArgs z = zcg_args(S);
   if (S.A->maxw <= 8) k_zcg_iter<8, kZBT, kZU1, kZU2, false><<<S.zgrid, kZBT, S.zsmem, st>>>(z);
-  else if (S.zblock2) k_zcg_iter<16, kZBT, kZU1, kZU2, true><<<S.zgrid, kZBT, S.zsmem, st>>>(z);
-  else k_zcg_iter<16, kZBT, kZU1, kZU2, false><<<S.zgrid, kZBT, S.zsmem, st>>>(z);
+  else if (S.zblock2) k_zcg_iter<16, kZBT, kZU1, kZU2W, true><<<S.zgrid, kZBT, S.zsmem, st>>>(z);
+  else k_zcg_iter<16, kZBT, kZU1, kZU2W, false><<<S.zgrid, kZBT, S.zsmem, st>>>(z);
 }
 
 void zcg_enqueue_init(Solver& S, cudaStream_t st, const double* rhs, const uint8_t* zero_rows, const double* u0,
