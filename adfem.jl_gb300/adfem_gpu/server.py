@@ -26,7 +26,7 @@ class Server:
                  rtol: float = 1e-10, max_iter: int = 200000, ru_delta: float = 0.1, chunk: int = 32,
                  pack_max_dof: int = 0, pack_max: int = 0):
         """pack_max_dof: mixed-precision requests up to this many DOFs are solved in packed
-        launches (0: the library default, 4096; -1: never); pack_max: systems per pack."""
+        launches (0: the library default, 16384; -1: never); pack_max: systems per pack."""
         from . import solver_opts
 
         L = _lib.load()

@@ -199,7 +199,7 @@ def _packed(systems, outs, gs, rtol, max_iter, warm_start, adjoint):
 
 
 def solve_packed(systems, outs=None, rtol=1e-9, max_iter=200000, warm_start=False):
-    """Solve assembled small systems (<= 16384 DOFs each) in one packed launch; returns (u list, stats list)."""
+    """Solve assembled small systems (<= 65536 DOFs each) in one packed launch; returns (u list, stats list)."""
     return _packed(systems, outs, None, rtol, max_iter, warm_start, False)
 
 

@@ -96,7 +96,7 @@ constexpr int kPackers = 4;  // packer threads (concurrent packed launches)
 // Default packing threshold: up to ~4k DOFs a system solved by one thread block is about
 // as fast as the whole-GPU solver even alone, and packs of many run at a fraction of the
 // per-solve cost; larger systems are faster on the whole GPU unless many are packed.
-constexpr int kPackDefaultDof = 4096;
+constexpr int kPackDefaultDof = 16384;
 
 int ndof_of(const adfem::Mesh* m, int kind) { return (int)(kind == ADFEM_SYS_ELASTICITY ? 2 * m->nv : m->nv); }
 

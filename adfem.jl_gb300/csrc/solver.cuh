@@ -105,8 +105,12 @@ void zcg_enqueue_unscale(Solver& S, cudaStream_t st, const uint8_t* fix, const d
 
 // Fill sliced-ELL values from CSR values (same pattern).
 // ---- packed solves of small systems (pack.cu)
-constexpr int kPackMaxRows = 16384;    // rows of a system solved by one thread block
-constexpr int kPackMaxSystems = 128;   // systems per packed launch
+#ifndef ADFEM_PACK_BLOCK_ROWS
+#define ADFEM_PACK_BLOCK_ROWS 3072
+#endif
+constexpr int kPackBlockRows = ADFEM_PACK_BLOCK_ROWS;  // rows of a system solved by one thread block
+constexpr int kPackMaxRows = 65536;    // rows of a packed system (larger ones: a cluster of 8 blocks)
+constexpr int kPackMaxSystems = 128;   // systems of each kind per packed launch
 // one system of a packed launch (device-side descriptor; outputs filled by the kernel)
 struct PackDesc {
   const int32_t* sptr;

@@ -406,7 +406,7 @@ def run_serve(A, args, rank=0, world=1, dist=None):
                         "(ratio 2^(1/4)), 50%% with a misfit gradient (1%% observations), seeded fields"
                         % len(SERVE_SIZES),
             "workers": args.serve_workers, "rtol": args.serve_rtol, "precision": "mixed",
-            "pack_max_dof": args.serve_pack_max_dof if args.serve_pack_max_dof != 0 else 4096,
+            "pack_max_dof": args.serve_pack_max_dof if args.serve_pack_max_dof != 0 else 16384,
             "p50_ms": ref["p50_ms"] if ref else sat["p50_ms"], "p99_ms": ref["p99_ms"] if ref else sat["p99_ms"],
             "latency_at_load": ref["load"] if ref else 1.0,
             "saturation": sat, "sweep": sweep, "setup_s": setup_s,

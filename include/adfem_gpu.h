@@ -379,8 +379,9 @@ typedef struct adfem_solver_info {
                                  outputs stay in the reference order) */
 } adfem_solver_info;
 ADFEM_API int adfem_system_solver_info(const adfem_system *sys, adfem_solver_info *info);
-/* Packed solves of small systems: the systems (each assembled, at most 16384 DOFs,
- * distinct) are solved by one graph-captured launch, one thread block per system, with
+/* Packed solves of small systems: the systems (each assembled, at most 65536 DOFs,
+ * distinct) are solved by one graph-captured launch, one thread block per system up to
+ * 16384 DOFs and one cluster of eight thread blocks per larger system, with
  * FP32 inner CG iterations inside FP64 iterative refinement (the mixed method; opts
  * precision is ignored).  Forward: u_d[i] as adfem_system_solve_d.  Adjoint: lam_d[i]
  * for right-hand sides g_d[i], as adfem_system_adjoint_d.  stats[i] (may be NULL):
@@ -428,8 +429,8 @@ typedef struct adfem_server_config {
   int max_queue;              /* pending requests accepted; 0: 65536 */
   adfem_solver_opts opts;     /* solver options of every request (precision per request may override) */
   int pack_max_dof;           /* mixed-precision requests with at most this many DOFs are solved in
-                                 packs (one launch, one thread block each); 0: 4096; < 0: never;
-                                 at most 16384 */
+                                 packs (one launch, one thread block or cluster each); 0: 16384;
+                                 < 0: never; at most 65536 */
   int pack_max;               /* systems per packed launch; 0: 64 (at most 128) */
 } adfem_server_config;
 ADFEM_API void adfem_server_config_default(adfem_server_config *cfg);

@@ -1,5 +1,6 @@
-"""Packed small-system solves (one launch, one thread block per system) against the
-oracle's direct solve, and their independence from what they are packed with.
+"""Packed small-system solves (one launch; one thread block per system up to 16,384
+DOFs, one cluster of eight blocks per system up to 65,536) against the oracle's direct
+solve, and their independence from what they are packed with.
 
 Bars: solutions and adjoints within 1e-9 relative of the direct solve at rtol 1e-11;
 a system's packed result bit-identical alone and inside any pack.
@@ -108,8 +109,48 @@ def test_packed_warm_start_and_limits(oracle, gpulib):
     (u2,), (st2,) = SY.solve_packed([S], outs=[uc], rtol=1e-11, warm_start=True)
     assert st2.iterations < st.iterations
     assert rel(u2.cpu().numpy(), oracle.spsolve(B, r)) < 1e-9
-    big = poisson(oracle, gpulib, 130, 9)[1]  # 17,161 DOFs > 16,384
+    big = poisson(oracle, gpulib, 256, 9)[1]  # 66,049 DOFs > 65,536
     with pytest.raises(AdFemError):
         SY.solve_packed([big])
     with pytest.raises(AdFemError):
         SY.solve_packed([S, S])  # the same system twice
+
+
+def test_cluster_packed_solves_match_direct(oracle, gpulib):
+    """Systems above 16,384 DOFs run on a cluster of eight blocks, mixed with one-block
+    systems in the same launch; 255 x 255 (65,536 DOFs) is the largest packed size."""
+    from adfem_gpu import system as SY
+
+    cases = [poisson(oracle, gpulib, m, s) for m, s in ((130, 10), (200, 11), (255, 12), (50, 13))]
+    cases += [elasticity(oracle, gpulib, 100, 14)]  # 20,402 DOFs
+    systems = [c[1] for c in cases]
+    us, stats = SY.solve_packed(systems, rtol=1e-11)
+    for (G, S, B, r, bd), u, st in zip(cases, us, stats):
+        assert st.status == 0 and st.relres <= 1e-10
+        assert rel(u.cpu().numpy(), oracle.spsolve(B, r)) < 1e-9
+    import torch
+
+    rng = np.random.default_rng(1)
+    gs, want = [], []
+    for G, S, B, r, bd in cases[:2]:
+        g = rng.standard_normal(S.ndof)
+        gz = g.copy()
+        gz[bd - 1] = 0.0
+        want.append(oracle.spsolve(B, gz))
+        gs.append(torch.tensor(g, device="cuda"))
+    lams, _ = SY.adjoint_packed(systems[:2], gs, rtol=1e-11)
+    for lam, w, (G, S, B, r, bd) in zip(lams, want, cases):
+        lam = lam.cpu().numpy()
+        assert np.all(lam[bd - 1] == 0.0)
+        assert rel(lam, w) < 1e-9
+
+
+def test_cluster_packed_result_independent_of_pack(oracle, gpulib):
+    from adfem_gpu import system as SY
+
+    cases = [poisson(oracle, gpulib, m, s) for m, s in ((30, 15), (150, 16), (180, 17))]
+    alone = SY.solve_packed([cases[1][1]], rtol=1e-10)[0][0].cpu().numpy()
+    packed = SY.solve_packed([c[1] for c in cases], rtol=1e-10)[0][1].cpu().numpy()
+    reordered = SY.solve_packed([cases[2][1], cases[1][1]], rtol=1e-10)[0][1].cpu().numpy()
+    np.testing.assert_array_equal(alone, packed)
+    np.testing.assert_array_equal(alone, reordered)
