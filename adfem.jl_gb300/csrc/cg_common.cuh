@@ -47,6 +47,75 @@ __device__ __forceinline__ void block_sum(T (&v)[NV]) {
   __syncthreads();
 }
 
+// Grid sum of FP32 per-thread partials with the FP64 work confined to one warp per
+// block: FP32 within each warp, FP64 across the block's warps (warp 0) and across the
+// blocks (warp 0 of the last block to arrive, in block order).  On GB300 an FP64 warp
+// instruction holds the FP64 pipe ~16 cycles, so FP64 shuffle-adds by every warp of two
+// 512-thread blocks per SM would cost microseconds at the end of every launch.  Returns
+// true in the last block (block-uniform); tot is valid in thread 0.
+// Warp sum of FP32 values as an unevaluated FP32 pair (h + l): each butterfly step adds
+// the partner's pair with an error-free two-sum, so the result carries ~48 bits.
+__device__ __forceinline__ float2 warp_sum_pair(float v) {
+  float h = v, l = 0.0f;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    const float h2 = __shfl_xor_sync(0xffffffffu, h, o), l2 = __shfl_xor_sync(0xffffffffu, l, o);
+    const float s = __fadd_rn(h, h2);
+    const float bb = __fsub_rn(s, h);
+    const float e = __fadd_rn(__fsub_rn(h, __fsub_rn(s, bb)), __fsub_rn(h2, bb));
+    l = __fadd_rn(__fadd_rn(l, l2), e);
+    h = s;
+  }
+  return make_float2(h, l);
+}
+
+template <int NV, int BT, bool PAIR = false>
+__device__ __forceinline__ bool reduce_grid_w(float (&v)[NV], double* partials, unsigned* counter, double (&tot)[NV]) {
+  static_assert(BT % 32 == 0 && BT <= 1024, "block size");
+  __shared__ double sh[NV][BT / 32];
+  __shared__ bool last;
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  float2 w[NV];
+#pragma unroll
+  for (int j = 0; j < NV; j++) w[j] = PAIR ? warp_sum_pair(v[j]) : make_float2(warp_sum(v[j]), 0.0f);
+  if (lane == 0)  // (FP64 conversions by one lane only)
+#pragma unroll
+    for (int j = 0; j < NV; j++) sh[j][wid] = PAIR ? (double)w[j].x + (double)w[j].y : (double)w[j].x;
+  __syncthreads();
+  if (wid == 0) {
+    double x[NV];
+#pragma unroll
+    for (int j = 0; j < NV; j++) x[j] = warp_sum(lane < BT / 32 ? sh[j][lane] : 0.0);
+    if (lane == 0) {
+#pragma unroll
+      for (int j = 0; j < NV; j++) partials[j * gridDim.x + blockIdx.x] = x[j];
+      __threadfence();
+      const unsigned prev = atomicAdd(counter, 1u);
+      last = (prev == gridDim.x - 1);
+    }
+  }
+  __syncthreads();
+  if (!last) return false;
+  if (wid == 0) {
+    __threadfence();
+    double s[NV];
+#pragma unroll
+    for (int j = 0; j < NV; j++) s[j] = 0.0;
+#pragma unroll 4
+    for (int b = lane; b < (int)gridDim.x; b += 32)
+#pragma unroll
+      for (int j = 0; j < NV; j++) s[j] += __ldcg(partials + j * gridDim.x + b);
+#pragma unroll
+    for (int j = 0; j < NV; j++) s[j] = warp_sum(s[j]);
+    if (lane == 0) {
+#pragma unroll
+      for (int j = 0; j < NV; j++) tot[j] = s[j];
+      *counter = 0u;
+    }
+  }
+  return true;
+}
+
 // Publish this block's partial sums; the last block to arrive sums all partials in
 // block order into tot (valid in thread 0) and returns true (block-uniform).
 template <class T, int NV, int BT = kT>
