@@ -643,18 +643,19 @@ int solver_prepare(Solver& S, const int32_t* diagpos_dev, cudaStream_t user) {
   return ADFEM_OK;
 }
 
-// Optional per-launch timing: a pair of events around each launch (profiled solves only).
+// Optional per-launch timing (profiled solves only): a pair of events around each launch,
+// or around a run of launches of one kernel (open, the launches, open_n = their number,
+// close), whose time is shared by its launches.
 struct Timer {
+  struct Pending {
+    int kind, ev, count;
+  };
   Solver* S = nullptr;
   SolveProfile* prof = nullptr;
-  std::vector<std::pair<int, int>> pending;  // (kind, first event index)
+  std::vector<Pending> pending;
   int next = 0;
-  template <class F>
-  void run(int kind, cudaStream_t st, F&& launch) {
-    if (!prof) {
-      launch();
-      return;
-    }
+  int open_kind = -1, open_ev = 0, open_n = 0;
+  void reserve() {
     if (next + 2 > (int)S->pev.size()) {
       for (int i = 0; i < 64; i++) {
         cudaEvent_t e;
@@ -662,19 +663,43 @@ struct Timer {
         S->pev.push_back(e);
       }
     }
+  }
+  template <class F>
+  void run(int kind, cudaStream_t st, F&& launch) {
+    if (!prof) {
+      launch();
+      return;
+    }
+    reserve();
     cudaEventRecord(S->pev[next], st);
     launch();
     cudaEventRecord(S->pev[next + 1], st);
-    pending.push_back({kind, next});
+    pending.push_back({kind, next, 1});
     next += 2;
+  }
+  // a run of launches of one kind: open, run_in per launch, close
+  void open(int kind, cudaStream_t st) {
+    if (!prof) return;
+    reserve();
+    open_kind = kind;
+    open_ev = next;
+    open_n = 0;
+    cudaEventRecord(S->pev[next], st);
+    next += 2;
+  }
+  void close(cudaStream_t st) {
+    if (!prof || open_kind < 0) return;
+    cudaEventRecord(S->pev[open_ev + 1], st);
+    pending.push_back({open_kind, open_ev, open_n});
+    open_kind = -1;
   }
   // after a stream sync: add the measured durations, recycle the events
   void collect() {
     for (auto& pk : pending) {
       float ms = 0.0f;
-      cudaEventElapsedTime(&ms, S->pev[pk.second], S->pev[pk.second + 1]);
-      prof->ms[pk.first] += ms;
-      prof->n[pk.first] += 1;
+      cudaEventElapsedTime(&ms, S->pev[pk.ev], S->pev[pk.ev + 1]);
+      prof->ms[pk.kind] += ms;
+      prof->n[pk.kind] += pk.count;
     }
     pending.clear();
     next = 0;
@@ -789,14 +814,15 @@ static int chunk_launches(Path path, int chunk) {
 // A capture can be invalidated by work another host thread does at the same time that
 // has to synchronise the device (allocations take device_alloc_mutex for that reason;
 // first-use loading of kernel code is another such event); such a capture is retried.
-static int capture_chunk(Solver& S, Path path, int chunk, cudaGraphExec_t* out) {
+template <class F>
+static int capture_graph(Solver& S, cudaGraphExec_t* out, F&& body) {
   cudaError_t e = cudaSuccess;
   for (int attempt = 0; attempt < 8; attempt++) {
     cudaGraph_t g = nullptr;
     {
       std::lock_guard<std::mutex> lk(device_alloc_mutex());
       ADFEM_CUDA(cudaStreamBeginCapture(S.stream, cudaStreamCaptureModeThreadLocal));
-      for (int i = 0; i < chunk; i++) enqueue_iteration(S, path, i, chunk, S.stream);
+      body();
       e = cudaStreamEndCapture(S.stream, &g);
     }
     if (e == cudaErrorStreamCaptureInvalidated || e == cudaErrorStreamCaptureUnjoined) {
@@ -813,6 +839,19 @@ static int capture_chunk(Solver& S, Path path, int chunk, cudaGraphExec_t* out) 
   }
   return cuda_fail(e, "cudaStreamEndCapture (retried)");
 }
+
+static int capture_chunk(Solver& S, Path path, int chunk, cudaGraphExec_t* out) {
+  return capture_graph(S, out, [&] {
+    for (int i = 0; i < chunk; i++) enqueue_iteration(S, path, i, chunk, S.stream);
+  });
+}
+
+struct GraphExecGuard {
+  cudaGraphExec_t g = nullptr;
+  ~GraphExecGuard() {
+    if (g) cudaGraphExecDestroy(g);
+  }
+};
 
 int solver_solve(Solver& S, const double* rhs, double* u, const uint8_t* zero_rows, const uint8_t* fix_rows,
                  const double* fix_vals, const adfem_solver_opts& o, adfem_solver_stats* stats, cudaStream_t user,
@@ -871,7 +910,33 @@ int solver_solve(Solver& S, const double* rhs, double* u, const uint8_t* zero_ro
   launches += 2;
 
   CgState cur;
-  if (prof) {
+  if (prof && path == Path::BANDED) {
+    // runs of eight iterations as a captured graph (as in the solve) with an event pair
+    // around each run, the fold and residual checks with an event pair around each launch
+    Timer tm;
+    tm.S = &S;
+    tm.prof = prof;
+    GraphExecGuard run8;
+    ADFEM_TRY(capture_graph(S, &run8.g, [&] {
+      for (int i = 0; i < 8; i++) zcg_enqueue_iter(S, S.stream);
+    }));
+    for (;;) {
+      for (int r = 0; r < 4; r++) {
+        tm.open(0, st);
+        tm.open_n = 8;
+        ADFEM_CUDA(cudaGraphLaunch(run8.g, st));
+        tm.close(st);
+        enqueue_zreliable_update(S, st, 0, &tm);
+      }
+      launches += 4 * (8 + 2);
+      ADFEM_CUDA(cudaGetLastError());
+      ADFEM_CUDA(cudaMemcpyAsync(&S.h_state[0], S.state.p, sizeof(CgState), cudaMemcpyDeviceToHost, st));
+      ADFEM_CUDA(cudaStreamSynchronize(st));
+      tm.collect();
+      cur = S.h_state[0];
+      if (cur.done == 1 || cur.done == 2 || cur.done == 4) break;
+    }
+  } else if (prof) {
     // kernel-by-kernel loop with an event pair around every launch
     Timer tm;
     tm.S = &S;

@@ -354,8 +354,11 @@ ADFEM_API int adfem_system_grad_E_d(adfem_system *sys, const double *u_d, const 
 ADFEM_API int adfem_system_apply_d(adfem_system *sys, const double *x_d, double *y_d, void *stream);
 /* copy out the assembled right-hand side (reference DOF ordering) */
 ADFEM_API int adfem_system_rhs_d(adfem_system *sys, double *rhs_d, void *stream);
-/* Same solve as adfem_system_solve_d, launched kernel by kernel (no graph) with a CUDA
- * event pair around every launch on the solver's stream, for measurement.  kernel_ms[j]
+/* Same solve as adfem_system_solve_d with CUDA event pairs on the solver's stream, for
+ * measurement: launched kernel by kernel with an event pair around every launch, except
+ * that on the banded mixed path each run of eight iterations between two replacement
+ * checks is one captured graph (as in the solve) with an event pair around the run, whose
+ * time is shared by its eight launches.  kernel_ms[j]
  * and launches[j] receive the summed duration and launch count of: 0 SpMV+dot (the whole
  * iteration on the banded mixed path), 1 vector update+dot, 2 p update (FP64) / fold
  * (mixed), 3 FP64 residual. */
