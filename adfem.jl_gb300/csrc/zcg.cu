@@ -529,8 +529,13 @@ __global__ void k_zunscale(int64_t n, const double* __restrict__ y, const uint8_
 }
 
 // ---------------------------------------------------------------------------
+// One 1024-thread block per SM: half the blocks of a 2 x 512 launch, so half the halo
+// positions each block recomputes in phase 1.  Measured on GB300 (with the one-warp FP64
+// reductions; per launch, graph-launched runs): 4M-DOF Poisson 52.9 vs 54.6 us, 1M-DOF
+// Poisson 19.8 vs 20.8 us, 2M-DOF elasticity +7.7% solves/s.  (With FP64 shuffle-adds by
+// every warp at the end of a launch the 1024-thread block had been the slower one.)
 #ifndef ADFEM_ZCG_BT
-#define ADFEM_ZCG_BT 512
+#define ADFEM_ZCG_BT 1024
 #endif
 static constexpr int kZBT = ADFEM_ZCG_BT;            // threads per block
 static constexpr int kZPerSM = 1024 / kZBT;          // resident blocks per SM (1024 threads)
@@ -545,8 +550,8 @@ static constexpr int kZU2 = ADFEM_ZCG_U2;            // phase-2 matrix rows per 
 #ifndef ADFEM_ZCG_U2_WIDE
 #define ADFEM_ZCG_U2_WIDE 1
 #endif
-// rows per trip of the 16-wide variants: two rows of 16 entries do not fit the 64 registers
-// of a two-blocks-per-SM launch (they spill)
+// rows per trip of the 16-wide variants: two rows of 16 entries do not fit in 64 registers
+// per thread (they spill)
 static constexpr int kZU2W = ADFEM_ZCG_U2_WIDE;
 static constexpr size_t kZSmemBlock = (kZPerSM >= 2 ? 100 : 200) * 1024;  // shared memory per block
 

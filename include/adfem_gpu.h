@@ -356,9 +356,9 @@ ADFEM_API int adfem_system_apply_d(adfem_system *sys, const double *x_d, double 
 ADFEM_API int adfem_system_rhs_d(adfem_system *sys, double *rhs_d, void *stream);
 /* Same solve as adfem_system_solve_d with CUDA event pairs on the solver's stream, for
  * measurement: launched kernel by kernel with an event pair around every launch, except
- * that on the banded mixed path each run of eight iterations between two replacement
- * checks is one captured graph (as in the solve) with an event pair around the run, whose
- * time is shared by its eight launches.  kernel_ms[j]
+ * that on the banded mixed path each run of iterations between two replacement checks
+ * (16) is one captured graph (as in the solve) with an event pair around the run, whose
+ * time is shared by its launches.  kernel_ms[j]
  * and launches[j] receive the summed duration and launch count of: 0 SpMV+dot (the whole
  * iteration on the banded mixed path), 1 vector update+dot, 2 p update (FP64) / fold
  * (mixed), 3 FP64 residual. */
