@@ -1161,8 +1161,9 @@ int system_solve_packed(adfem_system** sys, int count, double** out, const doubl
   for (int i = 0; i < count; i++) {
     adfem_system* s = sys[i];
     if (!s->assembled) return fail(ADFEM_ERR_INVALID, "packed solve: system not assembled");
-    if (s->ndof > kPackMaxRows)
-      return fail(ADFEM_ERR_INVALID, "packed solve: a system has more than " + std::to_string(kPackMaxRows) + " DOFs");
+    if (s->ndof > pack_rows_limit())
+      return fail(ADFEM_ERR_INVALID,
+                  "packed solve: a system has more than " + std::to_string(pack_rows_limit()) + " DOFs");
     PackItem& it = items[i];
     it.S = &s->solver;
     it.rtol = o.rtol;

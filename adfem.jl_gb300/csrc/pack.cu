@@ -614,11 +614,37 @@ int pack_graph(PackSlot& c) {
 
 }  // namespace
 
+int pack_rows_limit() {
+  // a cluster of kCC blocks of kCBT threads with kCSmem shared memory each must fit one
+  // GPC of this device (not so on small partitions of a GPU); if the query itself fails,
+  // the launch reports any problem
+  static const int limit = [] {
+    std::lock_guard<std::mutex> lk(device_alloc_mutex());  // (no graph capture meanwhile)
+    if (cudaFuncSetAttribute(k_pack_cluster, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kCSmem) !=
+        cudaSuccess) {
+      cudaGetLastError();
+      return kPackBlockRows;
+    }
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(kCC);
+    cfg.blockDim = dim3(kCBT);
+    cfg.dynamicSmemBytes = kCSmem;
+    int nc = 0;
+    if (cudaOccupancyMaxActiveClusters(&nc, k_pack_cluster, &cfg) != cudaSuccess) {
+      cudaGetLastError();
+      return kPackMaxRows;
+    }
+    return nc >= 1 ? kPackMaxRows : kPackBlockRows;
+  }();
+  return limit;
+}
+
 int solve_packed(PackItem* items, int count, cudaStream_t st, PackSlot* slot) {
+  const int limit = pack_rows_limit();
   for (int i = 0; i < count; i++) {
     const Solver& S = *items[i].S;
     if (!S.prepared) return fail(ADFEM_ERR_INVALID, "packed solve: operator not prepared");
-    if (S.n > kPackMaxRows) return fail(ADFEM_ERR_INVALID, "packed solve: system larger than the packed limit");
+    if (S.n > limit) return fail(ADFEM_ERR_INVALID, "packed solve: system larger than the packed limit");
     if (!(items[i].rtol > 0.0) || items[i].max_iter < 1) return fail(ADFEM_ERR_INVALID, "packed solve: bad options");
   }
   PackSlot& c = slot ? *slot : default_slot();

@@ -499,8 +499,8 @@ int adfem_server_create(const adfem_server_config* cfg, adfem_server** out) {
   if (S->cfg.workers <= 0) S->cfg.workers = 8;
   if (S->cfg.workers > 256) return adfem::fail(ADFEM_ERR_INVALID, "server: at most 256 workers");
   if (S->cfg.max_queue <= 0) S->cfg.max_queue = 65536;
-  S->pack_max_dof = S->cfg.pack_max_dof == 0 ? kPackDefaultDof
-                                             : (S->cfg.pack_max_dof < 0 ? 0 : std::min(S->cfg.pack_max_dof, adfem::kPackMaxRows));
+  S->pack_max_dof = std::min(S->cfg.pack_max_dof == 0 ? kPackDefaultDof : std::max(S->cfg.pack_max_dof, 0),
+                             adfem::pack_rows_limit());
   S->pack_max = S->cfg.pack_max <= 0 ? 64 : std::min(S->cfg.pack_max, adfem::kPackMaxSystems);
   ADFEM_CUDA(cudaGetDevice(&S->device));
   size_t freeb = 0, total = 0;

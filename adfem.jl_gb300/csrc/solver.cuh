@@ -156,6 +156,9 @@ void pack_slot_destroy(PackSlot* s);
 // the systems must be prepared and have at most kPackMaxRows rows) on the given slot
 // (NULL: a process-wide slot).  Synchronises st.
 int solve_packed(PackItem* items, int count, cudaStream_t st, PackSlot* slot = nullptr);
+// largest packed system on this device: kPackMaxRows, or kPackBlockRows where a cluster
+// of the packed solver cannot be scheduled
+int pack_rows_limit();
 
 cudaError_t launch_csr_to_sell(const Sell& A, int64_t n, const int32_t* rowptr, const double* csr, double* sell,
                                cudaStream_t st);
