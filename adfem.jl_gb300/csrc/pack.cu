@@ -47,6 +47,8 @@ constexpr int kPBT = 512;                // threads per system
 constexpr int kMaxPasses = 64;           // outer refinement passes
 constexpr double kInner2 = 1e-8;         // inner CG stops at |r_inner|^2 <= 1e-8 |r|^2
 constexpr int kU = 8;                    // row entries loaded together in the inner SpMV
+// dynamic shared memory of the one-block kernel: p, r, d, q of every row (FP32)
+constexpr size_t kPSmem = 4 * sizeof(float) * kPackBlockRows;
 
 // Scalars of the inner CG, kept by thread 0 and read by every thread after a barrier.
 // Only thread 0 does FP64 work per inner iteration: on GB300 an FP64 instruction of a
@@ -106,9 +108,10 @@ __device__ void pack_body(const PackDesc& D, float* __restrict__ sp, double* shb
   const int tid = threadIdx.x;
   const float* __restrict__ s = D.s;
   double* __restrict__ y = D.y;
-  float* __restrict__ rv = D.r;
-  float* __restrict__ dv = D.d;
-  float* __restrict__ qv = D.q;
+  // r, d, q of the inner CG next to p in shared memory
+  float* __restrict__ rv = sp + kPackBlockRows;
+  float* __restrict__ dv = sp + 2 * kPackBlockRows;
+  float* __restrict__ qv = sp + 3 * kPackBlockRows;
   // b~ and the start
   double bb = 0.0, dummy = 0.0;
   for (int r = tid; r < n; r += kPBT) {
@@ -544,7 +547,7 @@ int pack_graph(PackSlot& c) {
     c.d.bytes = bytes;
   }
   ADFEM_CUDA(cudaFuncSetAttribute(k_pack_solve, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                  (int)(sizeof(float) * kPackBlockRows)));
+                                  (int)kPSmem));
   ADFEM_CUDA(cudaFuncSetAttribute(k_pack_cluster, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kCSmem));
   std::memset(c.h, 0, bytes);
   cudaStream_t cs, cs2;
@@ -560,7 +563,7 @@ int pack_graph(PackSlot& c) {
     cudaMemcpyAsync(c.d.p, c.h, bytes, cudaMemcpyHostToDevice, cs);
     cudaEventRecord(e0, cs);
     cudaStreamWaitEvent(cs2, e0, 0);
-    k_pack_solve<<<kPackMaxSystems, kPBT, sizeof(float) * kPackBlockRows, cs>>>(c.d.as<PackDesc>());
+    k_pack_solve<<<kPackMaxSystems, kPBT, kPSmem, cs>>>(c.d.as<PackDesc>());
     k_pack_cluster<<<kPackMaxSystems * kCC, kCBT, kCSmem, cs2>>>(c.d.as<PackDesc>() +
                                                                                 kPackMaxSystems);
     cudaEventRecord(e1, cs2);
@@ -677,9 +680,6 @@ int solve_packed(PackItem* items, int count, cudaStream_t st, PackSlot* slot) {
       D.u0 = it.warm ? it.u : nullptr;
       D.u = it.u;
       D.y = S.y64.as<double>();
-      D.r = S.r32.as<float>();
-      D.d = S.pa32.as<float>();
-      D.q = S.q32.as<float>();
       D.rtol2 = it.rtol * it.rtol;
       D.n = (int)S.n;
       D.d16 = A.delta16 ? 1 : 0;

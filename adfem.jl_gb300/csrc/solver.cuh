@@ -124,10 +124,8 @@ struct PackDesc {
   const double* fix_vals;
   const double* u0;       // warm start (may alias u) or NULL
   double* u;
-  double* y;              // scratch: scaled solution (FP64)
-  float* r;               // scratch: inner residual, correction, A p (FP32)
-  float* d;
-  float* q;
+  double* y;              // scratch: scaled solution (FP64); the FP32 inner-CG vectors live in
+                          // shared memory
   double rtol2;
   int n, d16, max_iter;
   int iters, passes, status, floor_hit;
