@@ -1,8 +1,10 @@
 // Packed solves of small systems: many independent Jacobi-scaled systems solved by one
-// kernel launch, one thread block per system, the whole mixed-precision solve inside
-// the block.  The launch (descriptor upload, solve kernel, result download) is a CUDA
-// graph captured once and relaunched for every pack, so a pack of small requests costs
-// one graph launch instead of a chain of per-iteration launches per request.
+// graph launch, one thread block per system of at most kPackBlockRows rows and one
+// thread-block cluster per larger system, the whole mixed-precision solve inside the
+// block or cluster.  The launch (descriptor upload, the two solve kernels, result
+// download) is a CUDA graph captured once and relaunched for every pack (its kernel
+// grids set to the pack's systems), so a pack of small requests costs one graph launch
+// instead of a chain of per-iteration launches per request.
 //
 // Method per system (the block owns every row; no grid-wide synchronisation):
 //   b~ = s * rhs, y = u0 / s or 0                                    (FP64)
@@ -17,7 +19,7 @@
 // the outer residual, the solution update and the stopping test.  On GB300 an FP64
 // instruction costs the FP64 pipe ~60x an FP32 one, so a block running its CG in FP64
 // would spend ~30 us per iteration on a 16k-row system; in FP32 the inner iterations
-// are limited by the block's shared-memory and L1 traffic instead.
+// are limited by the latency of the matrix loads and of the block's barriers instead.
 //
 // Larger systems (above kPackBlockRows rows) are solved by a thread-block cluster of
 // kCC blocks instead (k_pack_cluster): each block owns a contiguous slice of rows and
