@@ -383,9 +383,11 @@ __global__ void __launch_bounds__(kT, PF ? 4 : 1) k_cg32_spmv(int64_t n, const i
       acc = fmaf(pr, s, acc);
     }
   }
-  // per-thread partials in FP32, combined across threads and blocks in FP64
-  double v1[1] = {(double)acc}, tot[1];
-  if (reduce_grid<double, 1>(v1, partials, &st->counter[0], tot) && threadIdx.x == 0) {
+  // per-thread partials in FP32, summed as FP32 pairs within warps and in FP64 by one warp
+  // per block and across blocks
+  float v1[1] = {acc};
+  double tot[1];
+  if (reduce_grid_w<1, kT, true>(v1, partials, &st->counter[0], tot) && threadIdx.x == 0) {
     const double pq = tot[0];
     if (!(pq > 0.0) || !isfinite(pq)) st->done = 2;
     else st->alpha = st->rho / pq;
@@ -438,8 +440,9 @@ __global__ void __launch_bounds__(kT) k_cg32_update(int64_t n, float* __restrict
     r[i] = ri;
     acc = fmaf(ri, ri, acc);
   }
-  double v[1] = {(double)acc}, tot[1];
-  if (reduce_grid<double, 1>(v, partials + gridDim.x, &st->counter[2], tot) && threadIdx.x == 0) {
+  float v[1] = {acc};
+  double tot[1];
+  if (reduce_grid_w<1, kT, true>(v, partials + gridDim.x, &st->counter[2], tot) && threadIdx.x == 0) {
     const double rn = tot[0];
     st->iters = it + 1;
     st->rho_new = rn;
