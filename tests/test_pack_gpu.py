@@ -154,3 +154,25 @@ def test_cluster_packed_result_independent_of_pack(oracle, gpulib):
     reordered = SY.solve_packed([cases[2][1], cases[1][1]], rtol=1e-10)[0][1].cpu().numpy()
     np.testing.assert_array_equal(alone, packed)
     np.testing.assert_array_equal(alone, reordered)
+
+
+def test_pack_kernel_boundary_warm_start_and_zero_rhs(oracle, gpulib):
+    """3025 DOFs (largest one-block size below 3072) and 3136 DOFs (smallest cluster size
+    here) both match the direct solve; on the cluster a converged warm start takes no
+    iteration and a zero right-hand side gives u = 0 exactly."""
+    import torch
+
+    from adfem_gpu import system as SY
+
+    block = poisson(oracle, gpulib, 54, 20)
+    clus = poisson(oracle, gpulib, 55, 21)
+    us, stats = SY.solve_packed([block[1], clus[1]], rtol=1e-11)
+    for (G, S, B, r, bd), u, st in zip((block, clus), us, stats):
+        assert st.status == 0
+        assert rel(u.cpu().numpy(), oracle.spsolve(B, r)) < 1e-9
+    (u1,), (st1,) = SY.solve_packed([clus[1]], outs=[us[1].clone()], rtol=1e-9, warm_start=True)
+    assert st1.iterations == 0 and st1.status == 0
+    S = clus[1]
+    (lam,), (st2,) = SY.adjoint_packed([S], [torch.zeros(S.ndof, dtype=torch.float64, device="cuda")], rtol=1e-11)
+    assert st2.status == 0 and st2.iterations == 0
+    assert torch.count_nonzero(lam).item() == 0
