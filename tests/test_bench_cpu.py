@@ -1,0 +1,35 @@
+"""The reference arm of bench.py on CPU: one JSON line with the contract's keys, the
+oracle port timed on the host cores, and silence on ranks other than 0."""
+import json
+import os
+import subprocess
+import sys
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def run_bench(env_extra, *args):
+    env = dict(os.environ, **env_extra)
+    r = subprocess.run([sys.executable, "bench.py", *args], cwd=ROOT, env=env, capture_output=True, text=True,
+                       timeout=600)
+    assert r.returncode == 0, r.stderr[-2000:]
+    return [json.loads(line) for line in r.stdout.splitlines() if line.startswith("{")]
+
+
+def test_reference_arm_line():
+    import bench
+
+    lines = run_bench({}, "--impl", "reference", "--m", "100", "--steps", "1", "--warmup", "3", "--ref-iters", "2")
+    assert len(lines) == 1
+    d = lines[0]
+    assert d["impl"] == "reference"
+    assert d["metric"] == bench.METRIC and d["unit"] == bench.UNIT and d["higher_is_better"] is True
+    assert d["value"] > 0 and d["steps"] == 1 and d["warmup"] == 3 and d["n_gpus"] == 1
+    assert d["e2e"] == {"value": d["value"], "unit": d["unit"], "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}
+    cb = d["cpu_baseline"]
+    assert cb["kind"] == "port" and cb["cores"] >= 1 and cb["value"] == d["value"] and cb["sample"]
+    assert d["config"]["workload"]
+
+
+def test_reference_arm_other_ranks_print_nothing():
+    assert run_bench({"RANK": "1", "WORLD_SIZE": "2"}, "--impl", "reference", "--m", "100", "--steps", "1") == []
