@@ -33,3 +33,17 @@ def test_reference_arm_line():
 
 def test_reference_arm_other_ranks_print_nothing():
     assert run_bench({"RANK": "1", "WORLD_SIZE": "2"}, "--impl", "reference", "--m", "100", "--steps", "1") == []
+
+
+def test_clock_sampler_summary():
+    """The clocks object from nvidia-smi rows: median SM clock, max clock, active reasons."""
+    import bench
+
+    cs = bench.ClockSampler(0)
+    cs.rows = [["0", "2070", "2070", "900.1", "0x0", "Not Active", "Not Active", "Not Active", "Not Active"],
+               ["0", "1980", "2070", "1390.5", "0x4", "Not Active", "Not Active", "Not Active", "Active"],
+               ["0", "2070", "2070", "1100.0", "0x0", "Not Active", "Not Active", "Not Active", "Not Active"],
+               ["garbage"]]
+    c = cs.stop()
+    assert c == {"sm_mhz": 2070.0, "sm_max_mhz": 2070.0, "reasons": ["sw_power_cap"], "samples": 3}
+    assert bench.ClockSampler(0).stop() == {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
