@@ -47,3 +47,15 @@ def test_clock_sampler_summary():
     c = cs.stop()
     assert c == {"sm_mhz": 2070.0, "sm_max_mhz": 2070.0, "reasons": ["sw_power_cap"], "samples": 3}
     assert bench.ClockSampler(0).stop() == {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+
+
+def test_roofline_inputs():
+    """The banded iteration's algorithmic byte model at the 4M-DOF layout the bench reports,
+    and the DRAM traffic read back from the committed ncu summary."""
+    import bench
+
+    layout = {"rows": 4004001, "stored": 28020160, "uniform_entries": 27558016, "slices": 125126}
+    assert bench.zcg_bytes(layout) == 38 * 4004001 + 4 * 28020160 + 2 * 462144 + 8 * 125126 == 266157974
+    t = bench.profiled_traffic("k_zcg_iter_poisson_4M.md")
+    assert t is not None and 0.5 * 266157974 < t < 1.2 * 266157974
+    assert bench.profiled_traffic("no_such_summary.md") is None
