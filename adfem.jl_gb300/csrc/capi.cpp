@@ -840,6 +840,67 @@ void adfem_solver_opts_default(adfem_solver_opts* o) {
   o->warm_start = 0;
 }
 
+// K\F by CG is only right for a symmetric K: the CSC arrays are read as CSR (which is
+// the transpose), and CG on a non-symmetric operator has no meaning.  The reference's
+// direct solve accepts any nonsingular K, so a non-symmetric one is refused here rather
+// than solved wrongly.  Entries present on one side only must be (numerically) zero;
+// matched pairs must agree to 1e-12 relative (or 1e-15 of the larger diagonal).
+// rp/ci: 0-based CSR of K^T (the CSC arrays of K); returns ADFEM_OK or a refusal.
+static int check_symmetric(int64_t n, const std::vector<int32_t>& rp, const std::vector<int32_t>& ci,
+                           const double* val) {
+  const int64_t nnz = rp[n];
+  // transpose by counting sort: rows of K (sorted columns, since rows are visited in order)
+  std::vector<int32_t> tp(n + 2, 0), tc(std::max<int64_t>(nnz, 1));
+  std::vector<double> tv(std::max<int64_t>(nnz, 1));
+  for (int64_t k = 0; k < nnz; k++) tp[ci[k] + 2]++;
+  for (int64_t i = 0; i < n; i++) tp[i + 2] += tp[i + 1];
+  for (int64_t r = 0; r < n; r++)
+    for (int32_t k = rp[r]; k < rp[r + 1]; k++) {
+      const int32_t t = tp[ci[k] + 1]++;
+      tc[t] = (int32_t)r;
+      tv[t] = val[k];
+    }
+  std::vector<double> diag(n, 0.0);
+  for (int64_t r = 0; r < n; r++)
+    for (int32_t k = rp[r]; k < rp[r + 1]; k++)
+      if (ci[k] == r) diag[r] += std::fabs(val[k]);
+  std::vector<std::pair<int32_t, double>> row;
+  for (int64_t r = 0; r < n; r++) {
+    row.clear();
+    for (int32_t k = rp[r]; k < rp[r + 1]; k++) row.emplace_back(ci[k], val[k]);
+    std::stable_sort(row.begin(), row.end(),
+                     [](const std::pair<int32_t, double>& a, const std::pair<int32_t, double>& b) {
+                       return a.first < b.first;
+                     });
+    // duplicates within a row (unsorted, repeated row indices in a column) are summed
+    size_t m = 0;
+    for (size_t q = 0; q < row.size(); q++) {
+      if (m > 0 && row[m - 1].first == row[q].first) row[m - 1].second += row[q].second;
+      else row[m++] = row[q];
+    }
+    row.resize(m);
+    size_t a = 0;
+    int32_t b = tp[r];
+    const int32_t be = tp[r + 1];
+    while (a < row.size() || b < be) {
+      const int32_t ca = a < row.size() ? row[a].first : INT32_MAX;
+      const int32_t cb = b < be ? tc[b] : INT32_MAX;
+      const int32_t c = std::min(ca, cb);
+      double x = 0.0, y = 0.0;
+      if (ca == c) x = row[a++].second;
+      while (b < be && tc[b] == c) y += tv[b++];
+      const double d = std::fabs(x - y);
+      const double scale = std::max(std::fabs(x), std::fabs(y));
+      if (d > 1e-12 * scale && d > 1e-15 * std::max(diag[r], diag[c]))
+        return fail(ADFEM_ERR_UNSUPPORTED,
+                    "K\\F by CG needs a symmetric K: entries (" + std::to_string(r + 1) + ", " +
+                        std::to_string(c + 1) + ") and (" + std::to_string(c + 1) + ", " + std::to_string(r + 1) +
+                        ") differ");
+    }
+  }
+  return ADFEM_OK;
+}
+
 int adfem_csc_solve(long long n, const long long* colptr1, const long long* rowval1, const double* nzval,
                     const double* rhs, double* u, const adfem_solver_opts* opts, adfem_solver_stats* stats) {
   if (n <= 0 || !colptr1 || !rowval1 || !nzval || !rhs || !u) return fail(ADFEM_ERR_INVALID, "bad arguments");
@@ -858,6 +919,7 @@ int adfem_csc_solve(long long n, const long long* colptr1, const long long* rowv
     if (c < 0 || c >= n) return fail(ADFEM_ERR_INVALID, "row index out of range");
     ci[k] = (int32_t)c;
   }
+  ADFEM_TRY(check_symmetric(n, rp, ci, nzval));
   for (long long i = 0; i < n; i++) {
     int found = -1;
     for (int32_t k = rp[i]; k < rp[i + 1]; k++)

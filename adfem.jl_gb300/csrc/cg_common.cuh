@@ -219,4 +219,37 @@ __device__ __forceinline__ void replacement_step(CgState* st, double rr, double 
   st->done = 0;
 }
 
+// Bookkeeping after the true FP64 residual of an FP64 CG solve (thread 0 of the last
+// block; mode 3 of k_residual64, which has already replaced r and updated p).  rr: true
+// residual norm^2 (scaled).  The FP64 iterate has an attainable accuracy too: its
+// residual cannot fall below the rounding of y itself (~2^-53 |K| |y|, relative to b
+// about 1e-11 at 4M DOF); when the recurrence has met rtol twice in a row and the true
+// residual improved less than 4x in between, the solve stops there.
+__device__ __forceinline__ void replacement_step64(CgState* st, double rr) {
+  st->rr64 = rr;
+  if (!isfinite(rr)) {
+    st->done = 2;
+    return;
+  }
+  if (rr <= st->stop2) {
+    st->done = 1;
+    return;
+  }
+  if (st->final_req && st->last_rr64 > 0.0 && rr > 0.0625 * st->last_rr64) {
+    st->floor_hit = 1;
+    st->done = 1;
+    return;
+  }
+  if (st->iters >= st->max_iter) {
+    st->done = 4;
+    return;
+  }
+  if (st->final_req) st->last_rr64 = rr;
+  st->final_req = 0;
+  st->updates += 1;
+  st->rho = rr;
+  st->ru2 = st->delta2 * rr;
+  st->done = 0;
+}
+
 }  // namespace adfem

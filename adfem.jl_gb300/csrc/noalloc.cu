@@ -20,6 +20,11 @@
 // host-side stand-in).  The device address is obtained once per device with
 // cudaGetSymbolAddress, with that device current, the first time the entry point is
 // called on it -- so that first call should happen before any stream capture.
+//
+// The call is synchronous: every 16 iterations it reads the CG scalars back to the host
+// and waits for its stream, so it returns only when the solve has ended.  Called on a
+// stream that is being captured it returns ADFEM_ERR_UNSUPPORTED before enqueueing
+// anything, so the caller's capture is left intact.
 #include <algorithm>
 #include <cmath>
 #include <mutex>
@@ -228,9 +233,14 @@ extern "C" int adfem_csr_pcg_noalloc_d(int n, const int* rowptr_d, const int* co
     return fail(ADFEM_ERR_INVALID, "csr_pcg_noalloc: n = " + std::to_string(n) + " exceeds the fixed scratch of " +
                                        std::to_string(kNoAllocMaxRows) + " rows");
   if (!(rtol > 0.0) || max_iter < 1) return fail(ADFEM_ERR_INVALID, "csr_pcg_noalloc: rtol > 0 and max_iter >= 1");
+  cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+  cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+  ADFEM_CUDA(cudaStreamIsCapturing(st, &cap));
+  if (cap != cudaStreamCaptureStatusNone)
+    return fail(ADFEM_ERR_UNSUPPORTED, "csr_pcg_noalloc: the call waits for its stream (it reads the CG state back "
+                                       "every 16 iterations); it cannot run on a stream that is being captured");
   double* scratch = nullptr;
   ADFEM_TRY(na_scratch(&scratch));
-  cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
   NaPtrs P = na_ptrs(scratch);
   // the previous call's state stays in the array: clear the scalars and counters
   ADFEM_CUDA(cudaMemsetAsync(P.st, 0, sizeof(NaState), st));

@@ -123,7 +123,10 @@ __global__ void __launch_bounds__(kT) k_init(int64_t n, const double* __restrict
 // that its rounding follows the differences of the solution rather than its size.
 // mode 0: FP64 CG start (r64 = p64 = r, rho = r.r);
 // mode 1: mixed residual replacement (r32 = (float) r, re-orthogonalise p, new coefficients);
-// mode 2: final check only (rr64).
+// mode 2: final check only (rr64);
+// mode 3: FP64 CG residual replacement (r64 = r, p64 = r + beta p64 with the beta of the
+//         recurrence, then replacement_step64 decides: converged, at the attainable floor,
+//         out of iterations, or continue from the true residual).
 template <bool D16>
 __global__ void __launch_bounds__(kT) k_residual64(int64_t n, const int32_t* __restrict__ sptr,
                                                    const void* __restrict__ col, const double* __restrict__ valD,
@@ -154,6 +157,9 @@ __global__ void __launch_bounds__(kT) k_residual64(int64_t n, const int32_t* __r
     if (mode == 0) {
       r64[r] = ri;
       p64[r] = ri;
+    } else if (mode == 3) {
+      r64[r] = ri;
+      p64[r] = fma(st->beta, p64[r], ri);
     } else if (mode == 1) {
       const float rf = (float)ri;
       r32[r] = rf;
@@ -164,6 +170,10 @@ __global__ void __launch_bounds__(kT) k_residual64(int64_t n, const int32_t* __r
   double v[3] = {a0, a1, a2}, tot[3];
   if (reduce_grid<double, 3>(v, partials, &st->counter[1], tot) && threadIdx.x == 0) {
     const double rr = tot[0];
+    if (mode == 3) {
+      replacement_step64(st, rr);
+      return;
+    }
     if (mode != 0) {
       replacement_step(st, rr, tot[1], tot[2], mode);
       return;
@@ -174,6 +184,7 @@ __global__ void __launch_bounds__(kT) k_residual64(int64_t n, const int32_t* __r
     else if (st->iters >= st->max_iter) st->done = 4;
     else {
       st->rho = rr;
+      st->ru2 = st->delta2 * rr;
       st->done = 0;
     }
   }
@@ -295,12 +306,22 @@ __global__ void __launch_bounds__(kT) k_cg64_update(int64_t n, double* __restric
     const double rn = tot[0];
     st->iters += 1;
     st->rho_new = rn;
-    if (!isfinite(rn)) st->done = 2;
-    else if (rn <= st->stop2) st->done = 1;
-    else if (st->iters >= st->max_iter) st->done = 4;
-    else {
-      st->beta = rn / st->rho;
-      st->rho = rn;
+    if (!isfinite(rn)) {
+      st->done = 2;
+    } else {
+      st->beta = rn / st->rho;  // the direction update also uses it after a replacement
+      // The recurrence residual drifts from the true one (at 4M DOF by ~6e-9 relative
+      // over a solve): a recurrence that meets rtol, has dropped by delta since the last
+      // replacement, or runs out of iterations hands over to the true FP64 residual
+      // (k_residual64 mode 3), which replaces r and decides.
+      if (rn <= st->stop2) {
+        st->final_req = 1;
+        st->done = 3;
+      } else if (rn <= st->ru2 || st->iters >= st->max_iter) {
+        st->done = 3;
+      } else {
+        st->rho = rn;
+      }
     }
   }
 }
@@ -803,6 +824,7 @@ static void enqueue_iteration(Solver& S, Path path, int i, int chunk, cudaStream
   const bool check = (i + 1) % kCheck == 0 || i + 1 == chunk;
   if (path == Path::FP64) {
     enqueue_cg64(S, st, tm);
+    if (check) enqueue_residual(S, st, 3, 0, tm);
   } else if (path == Path::MIXED) {
     enqueue_cg32(S, st, tm);
     if (check) enqueue_reliable_update(S, st, 0, tm);
@@ -814,10 +836,10 @@ static void enqueue_iteration(Solver& S, Path path, int i, int chunk, cudaStream
 }
 
 static int chunk_launches(Path path, int chunk) {
-  if (path == Path::FP64) return 3 * chunk;
   int ru = 0;
   for (int i = 0; i < chunk; i++)
     if ((i + 1) % kCheck == 0 || i + 1 == chunk) ru++;
+  if (path == Path::FP64) return 3 * chunk + ru;
   return (path == Path::MIXED ? 2 : 1) * chunk + 2 * ru;
 }
 

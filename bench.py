@@ -144,17 +144,29 @@ def zcg_bytes(info):
             + 8 * info["slices"])
 
 
-def profiled_traffic(summary):
-    """DRAM bytes per launch (dram__bytes_read.sum + dram__bytes_write.sum of one ncu
-    capture of the same workload), from the committed profile summary."""
-    path = os.path.join(os.path.dirname(os.path.abspath(__file__)), "profiles", summary)
+def profiled_traffic(kernel, m):
+    """DRAM bytes per launch of `kernel` on the m x m workload (dram__bytes_read.sum +
+    dram__bytes_write.sum of one ncu capture, averaged over the launches captured), from
+    profiles/traffic.json, which records each figure with the command that measured it;
+    None when no capture of that kernel and size is recorded."""
+    path = os.path.join(ROOT, "profiles", "traffic.json")
     try:
-        for line in open(path):
-            if line.startswith("traffic_bytes_per_launch"):
-                return int(line.split("=")[1])
-    except OSError:
-        pass
-    return None
+        with open(path) as fh:
+            d = json.load(fh)
+    except (OSError, ValueError):
+        return None
+    e = d.get(kernel)
+    if not e or int(e.get("m", -1)) != int(m):
+        return None
+    return int(e["bytes_per_launch"])
+
+
+def bench_config(m, world):
+    """The workload description both arms print (same dict, so the lines compare)."""
+    n = (m + 1) ** 2
+    return {"workload": "poisson-%dx%d-jittered-%s-dof-contrast1e3" % (m, m, "4M" if m == 2000 else str(n)),
+            "m": m, "dof": n, "nnz": n + 2 * (3 * m * m + 2 * m), "kappa_contrast": 1e3,
+            "l2": "working set > L2 (no flush needed)", "parallelism": "single" if world == 1 else "replicas"}
 
 
 def spmv64_bytes(mesh_nent, n, nslices):
@@ -174,89 +186,176 @@ def sell_entries(mesh):
 
 
 # ----------------------------------------------------------------------------- CPU leg
-def cpu_sample(mesh_m, threads, pcg_iters, Bcsr=None, fp64_iters=FP64_ITERS_DEFAULT, asm_m=500):
-    """Bounded CPU sample of the oracle restatement of the reference path.
-
-    (a) serial oracle assembly (unsummed COO -> Julia-sparse CSC -> load -> Dirichlet) on an
-        asm_m x asm_m sub-mesh, scaled to the full mesh by element count;
-    (b) pcg_iters Jacobi-PCG iterations (oracle, `threads` pthreads) on the full-size
-        Dirichlet-imposed operator Bcsr, scaled to fp64_iters iterations.
-    Returns (solves/s, details)."""
+def oracle_system(coords, elems, kappa, f):
+    """The oracle's Array-arm pipeline on the full mesh (serial C restatement of the reference):
+    unsummed COO of FemLaplaceScalar -> Julia sparse() CSC -> FemSourceScalar load -> CSC
+    Dirichlet arm with u = 0 on bcnode.  The mesh geometry is set up first and not timed (the
+    reference builds its mesh once); t_assembly_s times the per-solve part, on one core."""
     import oracle as O
-
-    from adfem_gpu import synth
 
     O.build()
-    coords, elems = synth.jittered_square(asm_m, seed=0)
-    t0 = time.perf_counter()
     M = O.OracleMesh(coords, elems)
-    g = M.gauss_nodes()
-    kap = 1 + np.exp(0.5 * synth.fourier_field(g[:, 0], g[:, 1], seed=1))
-    K = M.laplace_csc(kap)
-    F = M.source(1e5 * (g[:, 0] + g[:, 1]))
     bd = M.bcnode()
-    O.dirichlet_csc(K, F, bd, np.zeros(bd.size))
-    t_asm = (time.perf_counter() - t0) * (mesh_m / asm_m) ** 2
-    n = Bcsr.shape[0]
-    b = np.ones(n)
     t0 = time.perf_counter()
-    O.pcg(Bcsr, b, rtol=0.0, max_iter=pcg_iters, threads=threads)
-    t_it = (time.perf_counter() - t0) / pcg_iters
-    t_solve = t_asm + fp64_iters * t_it
-    return 1.0 / t_solve, {"t_assembly_s": t_asm, "t_iter_s": t_it, "iters": fp64_iters}
+    K = M.laplace_csc(kappa)
+    F = M.source(f)
+    B, Fb = O.dirichlet_csc(K, F, bd, np.zeros(bd.size))
+    t_asm = time.perf_counter() - t0
+    return {"mesh": M, "K": K, "F": F, "B": B, "Fb": Fb, "bd": bd, "t_assembly_s": t_asm}
 
 
-def cpu_operator_from_oracle(m, chunks=8):
-    """Full-size Dirichlet-imposed operator built by the oracle (chunked COO -> CSR)."""
-    import scipy.sparse as sp
+def cpu_pcg_iter_s(B, b, iters, threads):
+    """Seconds per Jacobi-PCG iteration of the oracle (FP64, `threads` pthreads) on B, timed
+    over `iters` iterations from zero."""
+    import oracle as O
+
+    t0 = time.perf_counter()
+    O.pcg(B, b, rtol=0.0, max_iter=iters, threads=threads)
+    return (time.perf_counter() - t0) / iters
+
+
+def matrix_parity(Kg, Ko):
+    """Entry-by-entry comparison of two CSC matrices of one pattern: pattern equality, the
+    largest difference over the largest entry of its column (row-scaled; the matrices are
+    symmetric), and the largest elementwise relative difference over entries at least 1e-10
+    of their column's largest entry."""
+    Kg, Ko = Kg.tocsc(), Ko.tocsc()
+    Kg.sort_indices()
+    Ko.sort_indices()
+    same = Kg.shape == Ko.shape and np.array_equal(Kg.indptr, Ko.indptr) and np.array_equal(Kg.indices, Ko.indices)
+    if not same:
+        return {"pattern_equal": False}
+    d = np.abs(Kg.data - Ko.data)
+    a = np.abs(Ko.data)
+    lens = np.diff(Ko.indptr)
+    nzc = np.flatnonzero(lens)
+    cmax = np.zeros(Ko.shape[1])
+    cmax[nzc] = np.maximum.reduceat(a, Ko.indptr[nzc])
+    colmax = np.repeat(cmax, lens)
+    big = a >= 1e-10 * colmax
+    return {"pattern_equal": True, "nnz": int(Ko.nnz),
+            "max_err_row_scaled": float(np.max(d / np.maximum(colmax, 1e-300))) if d.size else 0.0,
+            "max_err_elementwise": float(np.max(d[big] / a[big])) if big.any() else 0.0,
+            "entries_compared_elementwise": int(big.sum())}
+
+
+def vector_parity(g, o):
+    d = np.abs(np.asarray(g) - np.asarray(o))
+    a = np.abs(np.asarray(o))
+    big = a >= 1e-10 * a.max()
+    return {"max_err_scaled": float(d.max() / max(a.max(), 1e-300)),
+            "max_err_elementwise": float(np.max(d[big] / a[big])) if big.any() else 0.0}
+
+
+def residual_report(B, x, b, oracle_mod):
+    """Residual of a solution against the oracle's operator, in doubled precision: relres in
+    the solver's own measure (Jacobi-scaled 2-norm), plain relres, and the normwise backward
+    error ||r||_inf / (|| |B| |x| ||_inf + ||b||_inf)."""
+    r = oracle_mod.residual_dd(B, x, b)
+    s = 1.0 / np.sqrt(B.diagonal())
+    absbx = abs(B) @ np.abs(x)
+    return r, {"relres_scaled": float(np.linalg.norm(s * r) / np.linalg.norm(s * b)),
+               "relres": float(np.linalg.norm(r) / np.linalg.norm(b)),
+               "backward_error": float(np.abs(r).max() / (absbx.max() + np.abs(b).max()))}
+
+
+def accuracy_c3(A, S, mesh, coords, elems, kappa, f, u_ref, sols):
+    """Independent CPU checks of the 4M-DOF workload against the oracle (run once, after the
+    timed legs):
+    (a) the oracle's full-size assembly (oracle_system), timed on one core;
+    (b) entry-by-entry parity of the GPU's Array-arm outputs (compute_fem_laplace_matrix1,
+        compute_fem_source_term1) with (a);
+    (c) the residual of each GPU solution against (a) in doubled precision;
+    (d) a forward-error estimate of the FP64 reference by one refinement step: the correction
+        delta = B^-1 r_ref (r_ref from (c), solved on the GPU in FP64) estimates u* - u_ref,
+        and every solution's error is measured against u_ref + delta.
+    sols: {name: device solution}.  Returns (report, oracle system)."""
+    import torch
 
     import oracle as O
 
-    from adfem_gpu import synth
-
-    coords, elems = synth.jittered_square(m, seed=0)
-    n = coords.shape[0]
-    K = None
-    ne = elems.shape[0]
-    for c in range(chunks):
-        sub = elems[ne * c // chunks: ne * (c + 1) // chunks]
-        M = O.OracleMesh(coords, sub)
-        idx, vv = M.laplace_coo(np.ones(M.ngauss))
-        Kc = sp.coo_matrix((vv, (idx[:, 0], idx[:, 1])), shape=(n, n)).tocsr()
-        K = Kc if K is None else K + Kc
-    bmask = np.zeros(n, bool)
-    x, y = coords[:, 0], coords[:, 1]
-    bmask[(x == 0) | (x == 1) | (y == 0) | (y == 1)] = True
-    keep = ~bmask
-    D = sp.diags(keep.astype(float))
-    B = (D @ K @ D + sp.diags(bmask.astype(float))).tocsr()
-    B.sort_indices()
-    return B
+    kap = kappa.cpu().numpy()
+    fh = f.cpu().numpy()
+    osys = oracle_system(coords, elems, kap, fh)
+    B, Fb = osys["B"], osys["Fb"]
+    Kg = A.compute_fem_laplace_matrix1(kap, mesh)
+    Fg = A.compute_fem_source_term1(fh, mesh)
+    rep = {"oracle": "serial C restatement: unsummed COO -> Julia sparse() CSC -> load -> CSC Dirichlet arm, "
+                     "%d DOF, %d stored entries; residuals in doubled precision" % (B.shape[0], osys["K"].nnz),
+           "matrix_parity": matrix_parity(Kg, osys["K"]), "load_parity": vector_parity(Fg, osys["F"])}
+    del Kg
+    ur = u_ref.cpu().numpy()
+    r_ref, rr = residual_report(B, ur, Fb, O)
+    delta = S.adjoint(torch.tensor(r_ref, device="cuda"), precision="fp64", rtol=1e-10).cpu().numpy()
+    scale = float(np.abs(ur).max())
+    rr["forward_error_estimate"] = float(np.abs(delta).max() / scale)
+    rep["fp64_reference"] = rr
+    for name, u in sols.items():
+        uh = u.cpu().numpy()
+        _, rs = residual_report(B, uh, Fb, O)
+        rs["rel_err_vs_refined_reference"] = float(np.abs((uh - ur) - delta).max() / scale)
+        rep[name] = rs
+    return rep, osys
 
 
 # ----------------------------------------------------------------------------- reference arm
+def c3_fields_cpu(m, threads):
+    """The C3 fields on the host (torch on the CPU threads, no GPU): mesh, Gauss points,
+    kappa = 1 + exp(sigma G) with max/min = 1e3, f = 1e5 (x + y)."""
+    import torch
+
+    from adfem_gpu import synth
+
+    import oracle as O
+
+    torch.set_num_threads(threads)
+    coords, elems = synth.jittered_square(m, seed=0)
+    M = O.OracleMesh(coords, elems)
+    g = M.gauss_nodes()
+    G = synth.fourier_field(torch.from_numpy(g[:, 0].copy()), torch.from_numpy(g[:, 1].copy()), seed=1).numpy()
+    sigma = synth.contrast_sigma(G, 1e3)
+    return coords, elems, synth.lognormal_kappa(G, sigma), 1e5 * (g[:, 0] + g[:, 1])
+
+
 def run_reference(args, rank, world):
+    """The reference's CPU path (the oracle port; the reference itself cannot be built here):
+    the full-size Array-arm assembly timed once, serially as in the reference, then each step
+    = `ref_iters` Jacobi-PCG iterations on the full Dirichlet-imposed operator with every host
+    thread, timed.  solves/s = 1 / (assembly + fp64_iters x per-iteration time): the assembly is
+    measured whole, only the iteration count is extrapolated (factor printed)."""
     if rank != 0:
         return 0
+    import scipy.sparse as sp
+
     threads = os.cpu_count() or 1
-    B = cpu_operator_from_oracle(args.m)
-    vals = []
+    coords, elems, kappa, f = c3_fields_cpu(args.m, threads)
+    osys = oracle_system(coords, elems, kappa, f)
+    B = sp.csr_matrix(osys["B"])
+    b = osys["Fb"]
+    steps = []
     for i in range(args.warmup + args.steps):
-        v, det = cpu_sample(args.m, threads, args.ref_iters, B, args.fp64_iters)
+        t = cpu_pcg_iter_s(B, b, args.ref_iters, threads)
         if i >= args.warmup:
-            vals.append(v)
-    v = statistics.median(vals)
-    sample = ("serial oracle assembly (COO -> Julia-sparse CSC -> load -> Dirichlet) timed on the 500x500 "
-              "sub-mesh and scaled x%d by element count, plus %d Jacobi-PCG iterations on the full %d-DOF "
-              "operator with %d threads scaled to %d iterations" %
-              ((args.m // 500) ** 2, args.ref_iters, B.shape[0], threads, args.fp64_iters))
+            steps.append(t * args.ref_iters)
+    t_step = statistics.median(steps)
+    t_iter = t_step / args.ref_iters
+    t_solve = osys["t_assembly_s"] + args.fp64_iters * t_iter
+    v = 1.0 / t_solve
+    sample = ("oracle port of the reference path: full %dx%d assembly (COO -> Julia sparse() CSC -> load -> "
+              "Dirichlet) timed once on 1 core (%.2f s), plus Jacobi-PCG on the full %d-DOF operator with %d threads, "
+              "%d iterations per step (%.1f ms per iteration), extrapolated to the %d FP64 iterations the solve needs"
+              % (args.m, args.m, osys["t_assembly_s"], B.shape[0], threads, args.ref_iters, 1e3 * t_iter,
+                 args.fp64_iters))
     line = {"metric": METRIC, "value": v, "unit": UNIT, "n_gpus": world, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": 1000.0 / v, "higher_is_better": True, "scaling": "weak",
+            "warmup": args.warmup, "ms_per_step": 1e3 * t_step, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": "poisson-2000x2000-jittered-4M-dof-contrast1e3", "m": args.m,
-                       "parallelism": "replicas"},
+            "config": bench_config(args.m, world),
             "impl": "reference",
-            "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},
+            "step": "%d Jacobi-PCG iterations (ms_per_step); one solve = assembly + %d iterations"
+                    % (args.ref_iters, args.fp64_iters),
+            "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample,
+                             "t_assembly_s": osys["t_assembly_s"], "t_iter_s": t_iter,
+                             "extrapolated": {"assembly_x": 1, "iters_x": args.fp64_iters / args.ref_iters}},
             "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
     return 0
@@ -421,9 +520,14 @@ def run_c2(A, args):
     plus N(0, 1e-3^2) noise (seed 4); L = sum (u[obs] - uobs)^2.  The gradient dL/dkappa at
     all Gauss points is taken at the iterate kappa0 = kappa_true (1 + 0.1 G2) (G2 seed 5)
     by one mixed forward and one mixed adjoint solve; grads/s is timed over `c2_steps`
-    such gradients.  Check: central differences of L (FP64 solves, rtol 1e-13) along
-    `c2_dirs` random unit directions d with step eps = 1e-4 ||kappa0||, against d.grad
-    from an FP64 adjoint."""
+    such gradients.  Checks:
+    * the FP64 adjoint gradient against the reference's backward chain at full size, with
+      the oracle (sparse-solve gradient -lam_i u_j per stored entry of the Dirichlet-imposed
+      COO, ImposeDirichlet backward, FemLaplaceScalar backward) fed the GPU's FP64 u and lam,
+      whose residuals against the oracle's operator are reported beside it;
+    * central differences of L (FP64 solves at rtol 1e-13) along `c2_dirs` random unit
+      directions d, steps eps = 1e-4 ||kappa0|| and eps/2, and their Richardson combination
+      (4 D(eps/2) - D(eps)) / 3, against d.grad; errors relative to |d.grad| and to ||grad||."""
     import torch
     from adfem_gpu import synth
 
@@ -437,7 +541,8 @@ def run_c2(A, args):
     kap0 = (kap_true * (1.0 + 0.1 * G2)).contiguous()
     f = (1e5 * (g[:, 0] + g[:, 1])).contiguous()
     S = A.PoissonSystem(mesh)
-    S.set_dirichlet(A.bcnode(mesh))
+    bd = A.bcnode(mesh)
+    S.set_dirichlet(bd)
     S.assemble(kap_true, f)
     u_true = S.solve(precision="fp64", rtol=1e-13)
     obs = torch.tensor(synth.observation_nodes(mesh.nnode, seed=3), device="cuda")
@@ -451,37 +556,84 @@ def run_c2(A, args):
         r = u[obs] - uobs
         L = float((r * r).sum())
         if not grad:
-            return L, None
+            return L, None, u, None
         gu = torch.zeros_like(u)
         gu[obs] = 2 * r
         lam = S.adjoint(gu, precision=precision, rtol=rtol)
-        return L, S.grad_kappa(u, lam)
+        return L, S.grad_kappa(u, lam), u, lam
 
     loss_grad(kap0, "mixed", args.rtol)  # warm-up (graph capture)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     for _ in range(args.c2_steps):
-        L, gk = loss_grad(kap0, "mixed", args.rtol)
+        L, gk, _, _ = loss_grad(kap0, "mixed", args.rtol)
     torch.cuda.synchronize()
     grads_s = args.c2_steps / (time.perf_counter() - t0)
-    # finite-difference check of the adjoint gradient (FP64 solves)
-    L0, g64 = loss_grad(kap0, "fp64", 1e-13)
+    L0, g64, u64, lam64 = loss_grad(kap0, "fp64", 1e-13)
+    out = {"workload": "inverse Poisson %dx%d jittered, %d DOF, %d Gauss-point parameters, 1%% observations"
+                       % (m, m, mesh.nnode, kap0.numel()),
+           "grads_per_s": grads_s, "loss": L, "grad_mixed_vs_fp64_rel": float((gk - g64).norm() / g64.norm())}
+    # finite differences (FP64 solves) at eps and eps/2, Richardson-combined
     eps = 1e-4 * float(kap0.norm())
     gen = torch.Generator(device="cuda").manual_seed(6)
-    errs = []
+    gnorm = float(g64.norm())
+    e1, e2, er, en = [], [], [], []
     for _ in range(args.c2_dirs):
         d = torch.randn(kap0.numel(), dtype=torch.float64, device="cuda", generator=gen)
         d /= d.norm()
-        lp, _ = loss_grad(kap0 + eps * d, "fp64", 1e-13, grad=False)
-        lm, _ = loss_grad(kap0 - eps * d, "fp64", 1e-13, grad=False)
-        fd = (lp - lm) / (2 * eps)
         an = float((g64 * d).sum())
-        errs.append(abs(fd - an) / max(abs(an), 1e-300))
-    return {"workload": "inverse Poisson %dx%d jittered, %d DOF, %d Gauss-point parameters, 1%% observations"
-                        % (m, m, mesh.nnode, kap0.numel()),
-            "grads_per_s": grads_s, "loss": L, "grad_mixed_vs_fp64_rel": float((gk - g64).norm() / g64.norm()),
-            "fd_check": {"directions": args.c2_dirs, "eps": eps, "max_rel_err": max(errs) if errs else None,
-                         "median_rel_err": statistics.median(errs) if errs else None}}
+        D = []
+        for h in (eps, eps / 2):
+            lp = loss_grad(kap0 + h * d, "fp64", 1e-13, grad=False)[0]
+            lm = loss_grad(kap0 - h * d, "fp64", 1e-13, grad=False)[0]
+            D.append((lp - lm) / (2 * h))
+        rich = (4 * D[1] - D[0]) / 3
+        e1.append(abs(D[0] - an) / max(abs(an), 1e-300))
+        e2.append(abs(D[1] - an) / max(abs(an), 1e-300))
+        er.append(abs(rich - an) / max(abs(an), 1e-300))
+        en.append(abs(rich - an) / gnorm)
+    out["fd_check"] = {"directions": args.c2_dirs, "eps": eps,
+                       "max_rel_err": max(e1) if e1 else None,
+                       "median_rel_err": statistics.median(e1) if e1 else None,
+                       "max_rel_err_half_eps": max(e2) if e2 else None,
+                       "max_rel_err_richardson": max(er) if er else None,
+                       "median_rel_err_richardson": statistics.median(er) if er else None,
+                       "max_err_richardson_over_grad_norm": max(en) if en else None}
+    # the reference's backward chain at full size (oracle), fed the GPU's FP64 u and lam
+    if not args.no_cpu:
+        import scipy.sparse as sp
+
+        import oracle as O
+
+        t0 = time.perf_counter()
+        kh = kap0.cpu().numpy()
+        osys = oracle_system(coords, elems, kh, f.cpu().numpy())
+        M, Bo, Fb = osys["mesh"], osys["B"], osys["Fb"]
+        uh, lh = u64.cpu().numpy(), lam64.cpu().numpy()
+        gu = np.zeros(M.ndof)
+        oi = obs.cpu().numpy()
+        gu[oi] = 2 * (uh[oi] - uobs.cpu().numpy())
+        _, ru = residual_report(Bo, uh, Fb, O)
+        gz = gu.copy()
+        gz[bd - 1] = 0.0  # the adjoint solve takes lambda = 0 on Dirichlet rows
+        _, rl = residual_report(Bo, lh, gz, O)
+        idx, vv = M.laplace_coo(kh)
+        bv = np.zeros(bd.size)
+        oi2, ov, _ = O.dirichlet_coo(idx, vv, bd, osys["F"], bv, M.ndof)
+        grad_ov = -lh[oi2[:, 0]] * uh[oi2[:, 1]]
+        del oi2, ov
+        gvv, _, _ = O.dirichlet_coo_backward(grad_ov, lh, idx, vv, bd, bv, M.ndof)
+        del idx, vv, grad_ov
+        gref = M.laplace_coo_backward(gvv)
+        gg = g64.cpu().numpy()
+        out["grad_vs_oracle_chain"] = {
+            "chain": "sparse-solve gradient -> ImposeDirichlet backward -> FemLaplaceScalar backward (oracle, "
+                     "%d Gauss points), fed the GPU's FP64 u and lambda" % gg.size,
+            "max_rel_err": float(np.abs(gg - gref).max() / np.abs(gref).max()),
+            "rel_err_2norm": float(np.linalg.norm(gg - gref) / np.linalg.norm(gref)),
+            "u_residual": ru, "lambda_residual": rl, "cpu_s": time.perf_counter() - t0}
+        del osys, Bo
+    return out
 
 
 def run_c4(A, args):
@@ -753,7 +905,7 @@ def run_ours(args, rank, world, dist):
     traffic = None
     if info["banded"]:
         kname, b32 = "k_zcg_iter", zcg_bytes(info)
-        traffic = profiled_traffic("k_zcg_iter_poisson_4M.md") if args.m == 2000 else None
+        traffic = profiled_traffic("k_zcg_iter", args.m)
         others = {"k_fold": kms[2] / max(kn[2], 1), "k_zres64": kms[3] / max(kn[3], 1)}
     else:
         kname, b32 = "k_cg32_spmv", spmv32_bytes(nent, nrow, nsl)
@@ -778,9 +930,7 @@ def run_ours(args, rank, world, dist):
     asm_s = (ph[0] + ph[1]) * 1e-3
     assembly = {"element_pass_ms": ph[0], "rows_ms": ph[1], "solver_conversion_ms": ph[2], "total_ms": asm_ms,
                 "bytes": asm_bytes, "achieved_gbs": asm_bytes / asm_s / 1e9, "hbm_frac": asm_bytes / asm_s / 1e9 / hbm,
-                "dof_per_s": n / asm_s, "elements_per_s": ne_ / asm_s,
-                "bound": "fp64 (GB300 FP64 pipe: 82% busy in the element pass, 64% in the row pass; "
-                         "profiles/assembly_poisson_1M.md)"}
+                "dof_per_s": n / asm_s, "elements_per_s": ne_ / asm_s}
 
     # ------------------------------------------------------------------ e2e through host buffers
     kh = kappa.cpu().pin_memory()
@@ -809,41 +959,47 @@ def run_ours(args, rank, world, dist):
     c4 = run_c4(A, args) if args.c4_m > 0 else None
     p2 = run_p2(A, args) if args.p2_m > 0 else None
 
-    # ------------------------------------------------------------------ CPU baseline (rank 0, N=1)
+    # ------------------------------------------------------------------ CPU checks and baseline (rank 0, N=1)
     cpu = None
+    accuracy = None
     if rank == 0 and world == 1 and not args.no_cpu:
         import scipy.sparse as sp
 
-        K = A.compute_fem_laplace_matrix1(kappa.cpu().numpy(), mesh)
-        B, _ = A.impose_Dirichlet_boundary_conditions(K, _np.zeros(n), bd, _np.zeros(bd.size))
-        Bcsr = sp.csr_matrix(B)
-        fp64_iters = int(round(statistics.median([s[0] for s in fp64_stats])))
-        cv, det = cpu_sample(args.m, 1, args.cpu_iters, Bcsr, fp64_iters)
+        accuracy, osys = accuracy_c3(A, S, mesh, coords, elems, kappa, f, u_ref, {"mixed": u, "fp64": u64})
+        fp64_iters = int(round(statistics.median([s_[0] for s_ in fp64_stats])))
+        t_it = cpu_pcg_iter_s(sp.csr_matrix(osys["B"]), osys["Fb"], args.cpu_iters, 1)
+        t_asm = osys["t_assembly_s"]
+        cv = 1.0 / (t_asm + fp64_iters * t_it)
         cpu = {"value": cv, "unit": UNIT, "cores": 1, "kind": "port",
-               "sample": "serial oracle assembly on the 500x500 sub-mesh scaled x%d by element count + %d "
-                         "single-thread oracle Jacobi-PCG iterations on the full %d-DOF operator scaled to the "
-                         "%d FP64 iterations of this run" % ((args.m // 500) ** 2, args.cpu_iters, n, fp64_iters),
-               "detail": det}
+               "sample": "oracle port, 1 core: full %dx%d assembly (COO -> Julia sparse() CSC -> load -> Dirichlet) "
+                         "timed once (%.2f s) + %d Jacobi-PCG iterations on the full %d-DOF operator (%.1f ms each), "
+                         "extrapolated to the %d FP64 iterations of this run"
+                         % (args.m, args.m, t_asm, args.cpu_iters, n, 1e3 * t_it, fp64_iters),
+               "t_assembly_s": t_asm, "t_iter_s": t_it,
+               "extrapolated": {"assembly_x": 1, "iters_x": fp64_iters / args.cpu_iters}}
+        del osys
 
     if rank == 0:
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic",
-            "config": {"workload": "poisson-2000x2000-jittered-4M-dof-contrast1e3", "m": args.m, "dof": n,
-                       "nnz": int(mesh.pattern()[1].size), "rtol_mixed": args.rtol, "rtol_fp64": args.rtol_fp64,
-                       "precision": "mixed",
-                       "parallelism": "replicas" if world > 1 else "single",
-                       "l2": "working set > L2 (no flush needed)", "kappa_sigma": sigma},
-            "mixed": {"solves_per_s": value, "iters": [s[0] for s in mixed_stats],
+            "config": bench_config(args.m, world),
+            "kappa_sigma": sigma,
+            "mixed": {"solves_per_s": value, "rtol": args.rtol, "iters": [s[0] for s in mixed_stats],
                       "fp64_residual_evals": [s[1] for s in mixed_stats], "relres": mixed_stats[-1][2],
-                      "rel_err_vs_fp64_ref": err_mixed},
-            "fp64": {"solves_per_s": fp64_value, "iters": [s[0] for s in fp64_stats], "rel_err_vs_fp64_ref": err_fp64,
+                      "rel_err_vs_fp64_ref": err_mixed,
+                      "rel_err_vs_oracle": accuracy["mixed"]["rel_err_vs_refined_reference"] if accuracy else None},
+            "fp64": {"solves_per_s": fp64_value, "rtol": args.rtol_fp64, "iters": [s[0] for s in fp64_stats],
+                     "relres": fp64_stats[-1][1], "rel_err_vs_fp64_ref": err_fp64,
+                     "rel_err_vs_oracle": accuracy["fp64"]["rel_err_vs_refined_reference"] if accuracy else None,
                      "speedup_mixed_over_fp64": value / fp64_value},
+            "accuracy_vs_oracle": accuracy,
             "grads_per_s": grads_value,
             "dof_per_s": value * n,
             "assembly": assembly,
-            "fp64_reference": {"rtol": args.ref_rtol, "iters": ref_stats.iterations, "relres": ref_stats.relres},
+            "fp64_reference": {"rtol": args.ref_rtol, "iters": ref_stats.iterations, "relres": ref_stats.relres,
+                               "true_residual_replacements": ref_stats.updates},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
                          "traffic": traffic, "kernel": kname, "bytes_per_launch": b32,
                          "avg_launch_ms": spmv_ms, "launches": int(kn[0]), "peak_kind": peak_kind,
@@ -875,8 +1031,8 @@ def main():
     ap.add_argument("--ref-rtol", type=float, default=1e-14)
     ap.add_argument("--fp64-steps", type=int, default=2)
     ap.add_argument("--grad-steps", type=int, default=2)
-    ap.add_argument("--cpu-iters", type=int, default=5)
-    ap.add_argument("--ref-iters", type=int, default=10)
+    ap.add_argument("--cpu-iters", type=int, default=200, help="CPU baseline: single-thread PCG iterations timed")
+    ap.add_argument("--ref-iters", type=int, default=200, help="reference arm: PCG iterations per step")
     ap.add_argument("--fp64-iters", type=int, default=FP64_ITERS_DEFAULT)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--serve-requests", type=int, default=300,

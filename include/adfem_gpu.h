@@ -404,9 +404,11 @@ ADFEM_API int adfem_system_adjoint_packed_d(adfem_system **sys, int count, const
  * returns ADFEM_ERR_INVALID).  No cudaMalloc/cudaFree or allocating library call is
  * made.  The first call on a device looks up the array's device address, so it should
  * come before any stream capture.  Calls share the array: calls that overlap on the
- * GPU race and must be serialised by the caller.  u_d receives the solution (the
- * iteration starts from zero); iterations/relres (optional) receive the CG count and
- * the final recursive ||r||/||b||. */
+ * GPU race and must be serialised by the caller.  The call is synchronous: it reads
+ * the CG state back every 16 iterations and returns when the solve has ended; on a
+ * stream that is being captured it returns ADFEM_ERR_UNSUPPORTED without enqueueing
+ * work.  u_d receives the solution (the iteration starts from zero); iterations/relres
+ * (optional) receive the CG count and the final recursive ||r||/||b||. */
 ADFEM_API int adfem_csr_pcg_noalloc_d(int n, const int *rowptr_d, const int *colind_d, const double *vals_d,
                                       const double *rhs_d, double *u_d, double rtol, int max_iter, int *iterations,
                                       double *relres, void *stream);

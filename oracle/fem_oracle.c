@@ -786,7 +786,7 @@ static int cmp_cooent(const void *a, const void *b) {
   if (x->row != y->row) return x->row < y->row ? -1 : 1;
   return x->pos < y->pos ? -1 : (x->pos > y->pos ? 1 : 0);
 }
-i64 orc_coo_to_csc(const i64 *indices, const double *v, i64 N, i64 n, i64 *colptr, i64 *rowval, double *nzval) {
+i64 orc_coo_to_csc_sorted(const i64 *indices, const double *v, i64 N, i64 n, i64 *colptr, i64 *rowval, double *nzval) {
   cooent *t = (cooent *)malloc(sizeof(cooent) * (size_t)(N > 0 ? N : 1));
   for (i64 k = 0; k < N; k++) { t[k].row = indices[2 * k]; t[k].col = indices[2 * k + 1]; t[k].pos = k; }
   qsort(t, (size_t)N, sizeof(cooent), cmp_cooent);
@@ -805,6 +805,95 @@ i64 orc_coo_to_csc(const i64 *indices, const double *v, i64 N, i64 n, i64 *colpt
   free(t);
   return nnz;
 }
+
+
+/*
+ * The same COO -> CSC in linear time, by counting sorts, the way Julia's SparseArrays
+ * builds a CSC from triplets: the entries are bucketed by row in input order, the
+ * duplicates of each row are combined in input order, and a counting transpose moves
+ * the combined entries into their columns (rows ascending).  Every stored value is the
+ * same sum, taken in the same (input) order, as in orc_coo_to_csc_sorted, so the two are
+ * bit-identical.  Out-of-range indices are skipped.  Returns nnz, or -1 when out of memory;
+ * the three arrays are malloc'ed (release with orc_free).
+ */
+i64 orc_coo_to_csc_alloc(const i64 *indices, const double *v, i64 N, i64 n, i64 **colptr_out, i64 **rowval_out,
+                         double **nzval_out) {
+  i64 *rcnt = (i64 *)calloc((size_t)n + 2, sizeof(i64));
+  i64 *bcol = (i64 *)malloc(sizeof(i64) * (size_t)(N > 0 ? N : 1));
+  i64 *bpos = (i64 *)malloc(sizeof(i64) * (size_t)(N > 0 ? N : 1));
+  i64 *stamp = (i64 *)malloc(sizeof(i64) * (size_t)(n > 0 ? n : 1));
+  i64 *slot = (i64 *)malloc(sizeof(i64) * (size_t)(n > 0 ? n : 1));
+  if (!rcnt || !bcol || !bpos || !stamp || !slot) {
+    free(rcnt); free(bcol); free(bpos); free(stamp); free(slot);
+    return -1;
+  }
+  for (i64 k = 0; k < N; k++) {
+    const i64 r = indices[2 * k], c = indices[2 * k + 1];
+    if (r >= 0 && r < n && c >= 0 && c < n) rcnt[r + 2]++;
+  }
+  for (i64 r = 0; r < n; r++) rcnt[r + 2] += rcnt[r + 1];
+  /* rcnt[r + 1] is the next free bucket slot of row r */
+  for (i64 k = 0; k < N; k++) {
+    const i64 r = indices[2 * k], c = indices[2 * k + 1];
+    if (r < 0 || r >= n || c < 0 || c >= n) continue;
+    const i64 q = rcnt[r + 1]++;
+    bcol[q] = c;
+    bpos[q] = k;
+  }
+  /* combine duplicates row by row (in place: the combined row is a prefix of its bucket) */
+  for (i64 c = 0; c < n; c++) stamp[c] = -1;
+  double *bval = (double *)malloc(sizeof(double) * (size_t)(N > 0 ? N : 1));
+  i64 *rlen = (i64 *)calloc((size_t)n + 1, sizeof(i64));
+  if (!bval || !rlen) {
+    free(rcnt); free(bcol); free(bpos); free(stamp); free(slot); free(bval); free(rlen);
+    return -1;
+  }
+  i64 nnz = 0;
+  for (i64 r = 0; r < n; r++) {
+    const i64 b0 = rcnt[r], b1 = rcnt[r + 1];
+    i64 z = b0;
+    for (i64 q = b0; q < b1; q++) {
+      const i64 c = bcol[q];
+      const double x = v[bpos[q]];
+      if (stamp[c] == r) {
+        bval[slot[c]] = bval[slot[c]] + x;
+      } else {
+        stamp[c] = r;
+        slot[c] = z;
+        bcol[z] = c;
+        bval[z] = x;
+        z++;
+      }
+    }
+    rlen[r] = z - b0;
+    nnz += z - b0;
+  }
+  free(bpos); free(stamp); free(slot);
+  i64 *colptr = (i64 *)calloc((size_t)n + 2, sizeof(i64));
+  i64 *rowval = (i64 *)malloc(sizeof(i64) * (size_t)(nnz > 0 ? nnz : 1));
+  double *nzval = (double *)malloc(sizeof(double) * (size_t)(nnz > 0 ? nnz : 1));
+  if (!colptr || !rowval || !nzval) {
+    free(rcnt); free(bcol); free(bval); free(rlen); free(colptr); free(rowval); free(nzval);
+    return -1;
+  }
+  for (i64 r = 0; r < n; r++)
+    for (i64 q = rcnt[r]; q < rcnt[r] + rlen[r]; q++) colptr[bcol[q] + 2]++;
+  for (i64 c = 0; c < n; c++) colptr[c + 2] += colptr[c + 1];
+  /* colptr[c + 1] is the next free slot of column c; rows visited in ascending order */
+  for (i64 r = 0; r < n; r++)
+    for (i64 q = rcnt[r]; q < rcnt[r] + rlen[r]; q++) {
+      const i64 t = colptr[bcol[q] + 1]++;
+      rowval[t] = r;
+      nzval[t] = bval[q];
+    }
+  free(rcnt); free(bcol); free(bval); free(rlen);
+  *colptr_out = colptr;
+  *rowval_out = rowval;
+  *nzval_out = nzval;
+  return nnz;
+}
+
+void orc_free(void *p) { free(p); }
 
 /*
  * impose_Dirichlet_boundary_conditions, Array/SparseMatrixCSC arm, src/MFEM/MUtils.jl:184-199.
@@ -895,6 +984,35 @@ i64 orc_bcnode(int nv, int ne, const int *elem, i64 *out) {
     if (mark[i]) { if (out) out[c] = i + 1; c++; }
   free(keys); free(mark);
   return c;
+}
+
+/*
+ * Residual r = b - A x of a 0-based CSC matrix in doubled precision (error-free
+ * transformations: the product a*x split exactly with fma, each row's running sum kept
+ * as an unevaluated pair hi + lo updated by a two-sum), rounded to double at the end.
+ * The result is the residual of the stored FP64 vector x to about 2^-100 relative, so
+ * residuals at the FP64 rounding floor of x are measured, not swamped by the rounding of
+ * their own evaluation.  Used to check GPU solutions against the oracle's operator.
+ */
+void orc_residual_csc_dd(i64 n, const i64 *colptr, const i64 *rowval, const double *nzval, const double *x,
+                         const double *b, double *r) {
+  double *lo = (double *)calloc((size_t)(n > 0 ? n : 1), sizeof(double));
+  for (i64 i = 0; i < n; i++) r[i] = b[i];
+  for (i64 j = 0; j < n; j++) {
+    const double xj = x[j];
+    for (i64 p = colptr[j]; p < colptr[j + 1]; p++) {
+      const i64 i = rowval[p];
+      const double ph = -nzval[p] * xj;
+      const double pl = fma(-nzval[p], xj, -ph); /* exact: -a*x = ph + pl */
+      const double s = r[i] + ph;
+      const double bb = s - r[i];
+      const double e = (r[i] - (s - bb)) + (ph - bb); /* exact: r + ph = s + e */
+      r[i] = s;
+      lo[i] += e + pl;
+    }
+  }
+  for (i64 i = 0; i < n; i++) r[i] = r[i] + lo[i];
+  free(lo);
 }
 
 /* ---- CPU Jacobi-PCG on a 0-based CSR matrix (FP64), multithreaded with pthreads ----

@@ -59,7 +59,10 @@ def lib():
             "orc_plane_strain_stress_backward": (None, [_I, _L, _P, _P, _P, _P, _P]),
             "orc_dirichlet_coo": (_L, [_P, _P, _L, _P, _I, _P, _P, _L, _P, _P, _P]),
             "orc_dirichlet_coo_backward": (None, [_P, _P, _P, _P, _L, _P, _I, _P, _L, _P, _P, _P]),
-            "orc_coo_to_csc": (_L, [_P, _P, _L, _L, _P, _P, _P]),
+            "orc_coo_to_csc_sorted": (_L, [_P, _P, _L, _L, _P, _P, _P]),
+            "orc_coo_to_csc_alloc": (_L, [_P, _P, _L, _L, _P, _P, _P]),
+            "orc_free": (None, [_P]),
+            "orc_residual_csc_dd": (None, [_L, _P, _P, _P, _P, _P, _P]),
             "orc_dirichlet_csc": (_L, [_L, _P, _P, _P, _P, _P, _I, _P, _I, _P, _P, _P, _P]),
             "orc_bcnode": (_L, [_I, _I, _P, _P]),
             "orc_pcg": (_I, [_L, _P, _P, _P, _P, _P, _D, _I, _I, _P]),
@@ -382,16 +385,54 @@ def plane_strain_backward(grad_out, E, nu, mode: int = 0):
 
 
 def coo_to_csc(indices, vv, n):
-    """Julia ``sparse(I+1, J+1, V, n, n)`` (src/MFEM/MCore.jl:118-119) as a scipy CSC matrix."""
+    """Julia ``sparse(I+1, J+1, V, n, n)`` (src/MFEM/MCore.jl:118-119) as a scipy CSC matrix
+    (linear-time counting sorts; duplicates summed in input order)."""
     idx = _c(indices, np.int64).reshape(-1)
     vv = _c(vv, np.float64)
     N = vv.size
-    nnz = lib().orc_coo_to_csc(_p(idx), _p(vv), N, n, None, None, None)
+    cp, rv, nz = ctypes.c_void_p(), ctypes.c_void_p(), ctypes.c_void_p()
+    nnz = lib().orc_coo_to_csc_alloc(_p(idx), _p(vv), N, n, ctypes.byref(cp), ctypes.byref(rv), ctypes.byref(nz))
+    if nnz < 0:
+        raise MemoryError("orc_coo_to_csc_alloc: out of memory")
+
+    def take(ptr, count, ctype, dtype):
+        a = np.ctypeslib.as_array(ctypes.cast(ptr, ctypes.POINTER(ctype)), shape=(max(count, 1),))[:count].copy()
+        lib().orc_free(ptr)
+        return a.astype(dtype, copy=False)
+
+    colptr = take(cp, n + 1, ctypes.c_longlong, np.int64)
+    rowval = take(rv, nnz, ctypes.c_longlong, np.int64)
+    nzval = take(nz, nnz, ctypes.c_double, np.float64)
+    return sp.csc_matrix((nzval, rowval, colptr), shape=(n, n))
+
+
+def coo_to_csc_sorted(indices, vv, n):
+    """The same conversion by a comparison sort of (col, row, position): the plain
+    statement of the semantics, kept to check coo_to_csc bit for bit."""
+    idx = _c(indices, np.int64).reshape(-1)
+    vv = _c(vv, np.float64)
+    N = vv.size
+    nnz = lib().orc_coo_to_csc_sorted(_p(idx), _p(vv), N, n, None, None, None)
     colptr = np.empty(n + 1, np.int64)
     rowval = np.empty(nnz, np.int64)
     nzval = np.empty(nnz)
-    lib().orc_coo_to_csc(_p(idx), _p(vv), N, n, _p(colptr), _p(rowval), _p(nzval))
+    lib().orc_coo_to_csc_sorted(_p(idx), _p(vv), N, n, _p(colptr), _p(rowval), _p(nzval))
     return sp.csc_matrix((nzval, rowval, colptr), shape=(n, n))
+
+
+def residual_dd(A, x, b):
+    """r = b - A x for the stored FP64 vector x, evaluated in doubled precision and rounded
+    once (so that residuals at the FP64 rounding floor of x are resolved)."""
+    A = sp.csc_matrix(A)
+    n = A.shape[0]
+    cp = _c(A.indptr, np.int64)
+    rv = _c(A.indices, np.int64)
+    nz = _c(A.data, np.float64)
+    x = _c(x, np.float64)
+    b = _c(b, np.float64)
+    r = np.empty(n)
+    lib().orc_residual_csc_dd(n, _p(cp), _p(rv), _p(nz), _p(x), _p(b), _p(r))
+    return r
 
 
 def dirichlet_coo(indices, vv, bd, rhs, bdval, n):

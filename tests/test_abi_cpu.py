@@ -6,6 +6,7 @@ import os
 import re
 
 import numpy as np
+import pytest
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 HEADER = os.path.join(ROOT, "include", "adfem_gpu.h")
@@ -77,6 +78,29 @@ def test_invalid_arguments_rejected_on_host(gpulib):
     st = L.adfem_dirichlet_csc(2, _lib.ptr(cp), _lib.ptr(rv), _lib.ptr(nz), _lib.ptr(nz), _lib.ptr(bd), 2,
                                _lib.ptr(nz), 0, None, None, None, ctypes.byref(cnt), None)
     assert st == _lib.ERR_INVALID
+
+
+def test_csc_solve_refuses_non_symmetric_matrix_on_host(gpulib):
+    """K\\F runs CG, which is only right for a symmetric K: a non-symmetric matrix (values,
+    or a structural entry without its mirror) is refused before any device work, with
+    ADFEM_ERR_UNSUPPORTED and a message, instead of being solved as its transpose."""
+    import scipy.sparse as sp
+
+    import adfem_gpu as A
+
+    dense = np.array([[4.0, -1.0, 0.0], [-1.0, 4.0, -1.0], [0.0, -1.0, 4.0]])
+    for bad in (dense + np.array([[0, 0.5, 0], [0, 0, 0], [0, 0, 0]]),   # values differ
+                dense + np.array([[0, 0, 0.25], [0, 0, 0], [0, 0, 0]])):  # (1,3) without (3,1)
+        with pytest.raises(A.AdFemError) as ei:
+            A.solve(sp.csc_matrix(bad), np.ones(3))
+        assert ei.value.status == _unsupported()
+        assert "symmetric" in str(ei.value)
+
+
+def _unsupported():
+    from adfem_gpu import _lib
+
+    return _lib.ERR_UNSUPPORTED
 
 
 def test_synthetic_generator_properties():

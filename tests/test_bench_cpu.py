@@ -19,7 +19,8 @@ def run_bench(env_extra, *args):
 def test_reference_arm_line():
     import bench
 
-    lines = run_bench({}, "--impl", "reference", "--m", "100", "--steps", "1", "--warmup", "3", "--ref-iters", "2")
+    lines = run_bench({}, "--impl", "reference", "--m", "100", "--steps", "1", "--warmup", "3", "--ref-iters", "5",
+                      "--fp64-iters", "50")
     assert len(lines) == 1
     d = lines[0]
     assert d["impl"] == "reference"
@@ -28,7 +29,11 @@ def test_reference_arm_line():
     assert d["e2e"] == {"value": d["value"], "unit": d["unit"], "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}
     cb = d["cpu_baseline"]
     assert cb["kind"] == "port" and cb["cores"] >= 1 and cb["value"] == d["value"] and cb["sample"]
-    assert d["config"]["workload"]
+    assert d["config"] == bench.bench_config(100, 1)  # the same dict as the GPU arm's
+    # what was measured and what was extrapolated: the assembly whole, the iteration count x10
+    assert cb["extrapolated"] == {"assembly_x": 1, "iters_x": 10.0}
+    assert abs(d["value"] - 1.0 / (cb["t_assembly_s"] + 50 * cb["t_iter_s"])) < 1e-9 * d["value"]
+    assert abs(d["ms_per_step"] - 5e3 * cb["t_iter_s"]) < 1e-6 * d["ms_per_step"]
 
 
 def test_reference_arm_other_ranks_print_nothing():
@@ -51,11 +56,34 @@ def test_clock_sampler_summary():
 
 def test_roofline_inputs():
     """The banded iteration's algorithmic byte model at the 4M-DOF layout the bench reports,
-    and the DRAM traffic read back from the committed ncu summary."""
+    and the DRAM traffic read back from the committed data file of the ncu capture."""
     import bench
 
     layout = {"rows": 4004001, "stored": 28020160, "uniform_entries": 27558016, "slices": 125126}
     assert bench.zcg_bytes(layout) == 38 * 4004001 + 4 * 28020160 + 2 * 462144 + 8 * 125126 == 266157974
-    t = bench.profiled_traffic("k_zcg_iter_poisson_4M.md")
+    t = bench.profiled_traffic("k_zcg_iter", 2000)
     assert t is not None and 0.5 * 266157974 < t < 1.2 * 266157974
-    assert bench.profiled_traffic("no_such_summary.md") is None
+    assert bench.profiled_traffic("k_zcg_iter", 1000) is None  # recorded for the 2000x2000 workload only
+    assert bench.profiled_traffic("no_such_kernel", 2000) is None
+
+
+def test_shared_config_and_parity_helpers(oracle):
+    """Both arms print bench_config's dict; the parity helpers measure what they say."""
+    import numpy as np
+    import scipy.sparse as sp
+
+    import bench
+
+    c = bench.bench_config(2000, 1)
+    assert c["dof"] == 4004001 and c["nnz"] == 28012001 and c["workload"].startswith("poisson-2000x2000")
+    K = sp.csc_matrix(np.array([[4.0, -1.0, -1e-14], [-1.0, 4.0, -1.0], [-1e-14, -1.0, 4.0]]))
+    K2 = K.copy()
+    K2.data = K2.data * (1 + 1e-13)
+    p = bench.matrix_parity(K2, K)
+    assert p["pattern_equal"] and abs(p["max_err_row_scaled"] - 1e-13) < 1e-15
+    assert p["entries_compared_elementwise"] == 7 and abs(p["max_err_elementwise"] - 1e-13) < 1e-15
+    K3 = sp.csc_matrix(np.diag([1.0, 2.0, 3.0]))
+    assert bench.matrix_parity(K3, K) == {"pattern_equal": False}
+    x = np.array([1.0, 2.0, 3.0])
+    r, rep = bench.residual_report(K, x, K @ x + np.array([0.0, 1e-12, 0.0]), oracle)
+    assert abs(rep["relres"] - 1e-12 / np.linalg.norm(K @ x)) < 1e-15

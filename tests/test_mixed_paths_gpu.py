@@ -6,7 +6,9 @@
 
 The path that ran is identified by the launch count per iteration (banded: one launch
 per iteration plus the replacement checks; scaled: two plus the checks).  Bars as in
-test_solver_gpu.py: 1e-9 relative (max norm) to SuperLU on the oracle's matrices.
+the mixed-precision target: 1e-10 relative error (max norm) against the FP64 direct solve
+(SuperLU) on the oracle's matrices, or against an FP64 CG solve that stopped on its true
+residual where the system is too large for the direct solve.
 """
 import numpy as np
 import pytest
@@ -16,6 +18,7 @@ from adfem_gpu import synth
 
 pytestmark = pytest.mark.gpu
 RTOL_MIXED = 1e-11
+ERR_BAR = 1e-10  # mixed solves: relative error against the FP64 solution
 
 
 def rel(a, b):
@@ -47,7 +50,7 @@ def test_mixed_paths_match_direct(oracle, gpulib, monkeypatch, zcg):
     u0 = oracle.spsolve(B, r)
     u, st = gpulib.solve(B, r, precision="mixed", rtol=RTOL_MIXED, return_stats=True)
     assert st.status == 0 and st.relres <= 1e-10
-    assert rel(u, u0) < 1e-9
+    assert rel(u, u0) < ERR_BAR
     lpi = launches_per_iter(st)
     assert (lpi < 1.9) if zcg == "1" else (lpi > 2.0), lpi
 
@@ -62,7 +65,7 @@ def test_banded_path_super_tiles_and_deterministic(oracle, gpulib, monkeypatch):
     u2, s2 = gpulib.solve(B, r, precision="mixed", rtol=RTOL_MIXED, return_stats=True)
     assert s64.status == 0 and s1.status == 0
     assert launches_per_iter(s1) < 1.9
-    assert rel(u1, u64) < 1e-9
+    assert rel(u1, u64) < ERR_BAR
     # fixed grid, fixed reduction order, halos recomputed bit-identically
     assert s1.iterations == s2.iterations
     assert np.array_equal(u1, u2)
@@ -70,7 +73,7 @@ def test_banded_path_super_tiles_and_deterministic(oracle, gpulib, monkeypatch):
     monkeypatch.setenv("ADFEM_ZCG_SMAX", "512")
     u3, s3 = gpulib.solve(B, r, precision="mixed", rtol=RTOL_MIXED, return_stats=True)
     assert s3.status == 0 and launches_per_iter(s3) < 1.9
-    assert rel(u3, u64) < 1e-9
+    assert rel(u3, u64) < ERR_BAR
 
 
 def renumbered(m, seed=3):
@@ -111,12 +114,12 @@ def test_randomly_renumbered_mesh(oracle, gpulib, monkeypatch, m):
     for prec, rtol in (("mixed", RTOL_MIXED), ("fp64", 1e-12)):
         u = S.solve(precision=prec, rtol=rtol)
         assert S.last_stats.status == 0
-        assert rel(u.cpu().numpy(), u0) < 1e-9
+        assert rel(u.cpu().numpy(), u0) < ERR_BAR
     assert rel(S.rhs().cpu().numpy(), r) < 1e-12
     x = np.random.default_rng(1).standard_normal(O.ndof)
     assert rel(S.apply(t(x)).cpu().numpy(), B @ x) < 1e-12
     (up,), _ = SY.solve_packed([S], rtol=1e-11)
-    assert rel(up.cpu().numpy(), u0) < 1e-9
+    assert rel(up.cpu().numpy(), u0) < ERR_BAR
     # adjoint gradient against the same problem in the natural numbering (same elements,
     # same Gauss points): the gradients agree
     S2 = gpulib.PoissonSystem(gpulib.Mesh(coords, elems))
@@ -159,7 +162,7 @@ def test_renumbered_elasticity(oracle, gpulib, monkeypatch):
     assert rel(S.apply(t(x)).cpu().numpy(), B @ x) < 1e-12
     u = S.solve(precision="mixed", rtol=RTOL_MIXED)
     assert S.last_stats.status == 0
-    assert rel(u.cpu().numpy(), oracle.spsolve(B, r)) < 1e-9
+    assert rel(u.cpu().numpy(), oracle.spsolve(B, r)) < ERR_BAR
 
 
 def test_banded_path_warm_start_and_zero_rhs(oracle, gpulib, monkeypatch):
@@ -194,4 +197,4 @@ def test_system_reports_banded_layout(oracle, gpulib, monkeypatch):
     assert info["blocks"] * info["rows_per_block"] >= info["rows"]
     assert info["ring"] >= 2 * info["band"] + 32
     u = S.solve(precision="mixed", rtol=RTOL_MIXED)
-    assert rel(u.cpu().numpy(), oracle.spsolve(B, r)) < 1e-9
+    assert rel(u.cpu().numpy(), oracle.spsolve(B, r)) < ERR_BAR

@@ -119,6 +119,53 @@ def test_coo_to_csc_matches_scipy_sum(oracle):
     np.testing.assert_allclose(K1.toarray(), K2.toarray(), rtol=1e-14, atol=1e-14)
 
 
+def test_linear_coo_to_csc_bit_identical_to_sorted(oracle):
+    """The counting-sort conversion equals the comparison-sort statement bit for bit,
+    including repeated (row, col) pairs in shuffled order, unsorted input and empty rows."""
+    coords, elems = synth.jittered_square(9, seed=4)
+    M = oracle.OracleMesh(coords, elems)
+    rng = np.random.default_rng(1)
+    idx, vv = M.laplace_coo(rng.random(M.ngauss))
+    perm = rng.permutation(vv.size)
+    n = M.ndof + 3  # three rows/columns without entries
+    for i, v in ((idx, vv), (idx[perm], vv[perm] * 1e3)):
+        a = oracle.coo_to_csc(i, v, n)
+        b = oracle.coo_to_csc_sorted(i, v, n)
+        assert np.array_equal(a.indptr, b.indptr) and np.array_equal(a.indices, b.indices)
+        assert np.array_equal(a.data.view(np.int64), b.data.view(np.int64))
+    e = oracle.coo_to_csc(np.zeros((0, 2), np.int64), np.zeros(0), 4)
+    assert e.nnz == 0 and e.shape == (4, 4)
+
+
+def test_doubled_precision_residual(oracle):
+    """residual_dd is the exact residual of the stored vector within the doubled-precision
+    bound (one rounding of the result plus ~(k eps)^2 of the row's |a||x| for k terms):
+    checked with exact rational arithmetic on a small system whose residual is all rounding
+    noise of the FP64 product (terms ~1e7 times larger than the residual)."""
+    from fractions import Fraction
+
+    rng = np.random.default_rng(2)
+    n = 40
+    A = sp.random(n, n, density=0.3, random_state=3, format="csc") + sp.eye(n, format="csc") * 4.0
+    A = sp.csc_matrix(A)
+    x = rng.standard_normal(n) * 1e6
+    b = A @ x  # the FP64 product: its residual against x is pure rounding noise
+    r = oracle.residual_dd(A, x, b)
+    Ad = A.toarray()
+    exact = [Fraction(float(b[i])) - sum(Fraction(float(Ad[i, j])) * Fraction(float(x[j])) for j in range(n))
+             for i in range(n)]
+    ax = np.abs(Ad) @ np.abs(x)
+    eps = np.finfo(float).eps
+    for i in range(n):
+        ex = float(exact[i])
+        k = np.count_nonzero(Ad[i]) + 1
+        assert abs(r[i] - ex) <= 2 * np.spacing(abs(ex)) + (k * eps) ** 2 * ax[i], (i, r[i], ex)
+        assert abs(r[i] - ex) <= 1e-12 * abs(ex)
+    assert np.any(r != 0.0)
+    plain = b - A @ x  # the FP64 evaluation sees nothing but its own rounding
+    assert np.max(np.abs(plain - r)) > 10 * np.max(np.abs(r)) or np.max(np.abs(plain)) == 0.0
+
+
 def test_orientation_and_edges(oracle):
     coords, elems = synth.jittered_square(4, seed=0)
     M = oracle.OracleMesh(coords, elems)

@@ -41,6 +41,37 @@ def test_csc_solve_matches_direct(oracle, gpulib, precision):
     assert rel(u, u0) < 1e-9
 
 
+def scaled_relres(B, x, b, oracle):
+    """||S (b - B x)|| / ||S b||, S = diag(B_ii)^-1/2: the solver's stopping quantity,
+    recomputed on the CPU with the oracle's matrix in doubled precision."""
+    s = 1.0 / np.sqrt(B.diagonal())
+    r = oracle.residual_dd(B, x, b)
+    return float(np.linalg.norm(s * r) / np.linalg.norm(s * b))
+
+
+def test_fp64_cg_stops_on_true_residual(oracle, gpulib):
+    """FP64 CG hands over to the true FP64 residual whenever its recurrence meets rtol (or
+    has dropped 10x): the reported relres, and the same quantity recomputed on the CPU from
+    the oracle's matrix, meet rtol; an unattainable rtol stops at the attainable floor."""
+    coords, elems = synth.jittered_square(160, seed=0)
+    O = oracle.OracleMesh(coords, elems)
+    g = O.gauss_nodes()
+    G = synth.fourier_field(g[:, 0], g[:, 1], seed=1)
+    kappa = 1 + np.exp(synth.contrast_sigma(G, 1e3) * G)
+    bd = O.bcnode()
+    B, r = oracle.dirichlet_csc(O.laplace_csc(kappa), O.source(1e5 * (g[:, 0] + g[:, 1])), bd, np.zeros(bd.size))
+    u0 = oracle.spsolve(B, r)
+    for rtol in (1e-10, 1e-12):
+        u, st = gpulib.solve(B, r, precision="fp64", rtol=rtol, return_stats=True)
+        assert st.status == 0 and st.relres <= rtol and st.updates >= 1
+        assert scaled_relres(B, u, r, oracle) <= 1.01 * rtol
+        assert rel(u, u0) < 1e-9
+    # rtol below what FP64 can represent: ends at the floor with status OK, well before max_iter
+    u, st = gpulib.solve(B, r, precision="fp64", rtol=1e-18, max_iter=200000, return_stats=True)
+    assert st.status == 0 and 1e-18 < st.relres < 1e-12 and st.iterations < 100000
+    assert rel(u, u0) < 1e-11
+
+
 @pytest.mark.parametrize("precision", ["fp64", "mixed"])
 def test_poisson_system_matches_oracle_pipeline(oracle, gpulib, precision):
     import torch
