@@ -188,10 +188,12 @@ __device__ __forceinline__ void replacement_step(CgState* st, double rr, double 
     return;
   }
   // The FP64 residual of an FP64 iterate cannot fall below about 2^-53 |K| |y|
-  // (rounding of y itself, amplified by the largest eigenvalues).  When the FP32
-  // residual has met rtol twice in a row and the FP64 residual improved less than
-  // 4x in between, the iterate is at that attainable accuracy: stop there.
-  if (st->final_req && st->last_rr64 > 0.0 && rr > 0.0625 * st->last_rr64) {
+  // (rounding of y itself, amplified by the largest eigenvalues).  Once the FP32
+  // residual has met rtol and the FP64 residual did not, a replacement whose FP64
+  // residual improved less than 4x on the previous one means the iterate is at that
+  // attainable accuracy: stop there.  (Before that, a small improvement can also come
+  // from the FP32 inner iteration's own limits, so it is not taken as the floor.)
+  if (st->final_seen && st->last_rr64 > 0.0 && rr > 0.0625 * st->last_rr64) {
     st->floor_hit = 1;
     st->done = 1;
     return;
@@ -200,7 +202,8 @@ __device__ __forceinline__ void replacement_step(CgState* st, double rr, double 
     st->done = 4;
     return;
   }
-  if (st->final_req) st->last_rr64 = rr;
+  if (st->final_req) st->final_seen = 1;
+  if (st->final_seen) st->last_rr64 = rr;
   st->final_req = 0;
   if (st->updates == 0) {
     st->ar = 1.0;
@@ -221,12 +224,16 @@ __device__ __forceinline__ void replacement_step(CgState* st, double rr, double 
 
 // Bookkeeping after the true FP64 residual of an FP64 CG solve (thread 0 of the last
 // block; mode 3 of k_residual64, which has already replaced r and updated p).  rr: true
-// residual norm^2 (scaled).  The FP64 iterate has an attainable accuracy too: its
-// residual cannot fall below the rounding of y itself (~2^-53 |K| |y|, relative to b
-// about 1e-11 at 4M DOF); when the recurrence has met rtol twice in a row and the true
-// residual improved less than 4x in between, the solve stops there.
+// residual norm^2 (scaled); st->rho_new: the recurrence's value that requested it.  The
+// FP64 iterate has an attainable accuracy: its residual cannot fall below the rounding
+// of y itself (~2^-53 |K| |y|).  The FP64 recurrence tracks the true residual closely
+// until then, so a replacement requested by rtol or by a 10x drop of the recurrence
+// whose true residual improved less than 4x on the previous replacement's means the
+// iterate is at that floor: the solve stops there.
 __device__ __forceinline__ void replacement_step64(CgState* st, double rr) {
+  const double prev = st->last_rr64;
   st->rr64 = rr;
+  st->last_rr64 = rr;
   if (!isfinite(rr)) {
     st->done = 2;
     return;
@@ -235,7 +242,8 @@ __device__ __forceinline__ void replacement_step64(CgState* st, double rr) {
     st->done = 1;
     return;
   }
-  if (st->final_req && st->last_rr64 > 0.0 && rr > 0.0625 * st->last_rr64) {
+  const bool dropped = st->final_req || st->rho_new <= st->delta2 * prev;
+  if (prev > 0.0 && dropped && rr > 0.0625 * prev) {
     st->floor_hit = 1;
     st->done = 1;
     return;
@@ -244,7 +252,6 @@ __device__ __forceinline__ void replacement_step64(CgState* st, double rr) {
     st->done = 4;
     return;
   }
-  if (st->final_req) st->last_rr64 = rr;
   st->final_req = 0;
   st->updates += 1;
   st->rho = rr;

@@ -185,6 +185,7 @@ __global__ void __launch_bounds__(kT) k_residual64(int64_t n, const int32_t* __r
     else {
       st->rho = rr;
       st->ru2 = st->delta2 * rr;
+      st->last_rr64 = rr;
       st->done = 0;
     }
   }

@@ -21,9 +21,10 @@ struct CgState {
   int max_iter;
   int done;            // 0 running, 1 converged, 2 breakdown, 3 residual replacement due, 4 max_iter
   int updates;         // residual replacements done (mixed)
-  int final_req;       // mixed: the last replacement was requested because the FP32 residual met rtol
-  int floor_hit;       // mixed: stopped at the attainable accuracy of the FP64 residual
-  double last_rr64;    // mixed: FP64 residual norm^2 at the previous replacement
+  int final_req;       // the last replacement was requested because the recurrence residual met rtol
+  int floor_hit;       // stopped at the attainable accuracy of the FP64 residual
+  int final_seen;      // mixed: a replacement requested by rtol has already failed the true-residual test
+  double last_rr64;    // FP64 residual norm^2 at the previous replacement (mixed: once final_seen)
   unsigned counter[4]; // last-block arrival counters (returned to 0 by the last block)
 };
 
