@@ -149,7 +149,7 @@ size_t system_device_bytes(const adfem_system* s) {
                           &s->in0, &s->in1, &s->isbd_ref, &s->nperm, &s->kperm, &s->dofmap})
     b += d->bytes;
   const Solver& v = s->solver;
-  for (const DevBuf* d : {&v.s32, &v.state, &v.partials, &v.b, &v.y64, &v.r64, &v.p64, &v.q64, &v.r32, &v.pa32,
+  for (const DevBuf* d : {&v.s32, &v.state, &v.partials, &v.b, &v.y64, &v.r64, &v.p64, &v.q64, &v.z64, &v.r32, &v.pa32,
                           &v.pb32, &v.q32, &v.yh32, &v.yl32, &v.z1, &v.zq1, &v.dz32, &v.valz64, &v.valz32,
                           &v.colz16, &v.zpid32, &v.zpool32, &v.bz32})
     b += d->bytes;

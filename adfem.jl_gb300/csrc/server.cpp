@@ -102,12 +102,12 @@ int ndof_of(const adfem::Mesh* m, int kind) { return (int)(kind == ADFEM_SYS_ELA
 
 // Device bytes of a resident system before it exists (admission): per stored operator
 // entry 8+8+4 (scaled FP64 standard and difference forms, FP32) + 8+4 (banded path
-// copies) + 2+2 (column deltas) = 36 B with 15% padding; per DOF ~200 B of solver and
+// copies) + 2+2 (column deltas) = 36 B with 15% padding; per DOF ~210 B of solver and
 // Dirichlet vectors; per element ~96 B of element scratch and Gauss-point staging.
 size_t estimate_system_bytes(const adfem::Mesh* m, int kind) {
   const double ndof = (double)ndof_of(m, kind);
   const double nnz = (double)m->nnz * (kind == ADFEM_SYS_ELASTICITY ? 4.0 : 1.0);
-  const double b = 36.0 * 1.15 * nnz + 200.0 * ndof + 96.0 * (double)m->ne + 64.0 * 1024;
+  const double b = 36.0 * 1.15 * nnz + 210.0 * ndof + 96.0 * (double)m->ne + 64.0 * 1024;
   return (size_t)b;
 }
 

@@ -39,6 +39,7 @@ struct Solver {
   DevBuf partials;         // 4 * grid doubles
   DevBuf b;                // scaled rhs (FP64)
   DevBuf y64, r64, p64, q64;
+  DevBuf z64;              // FP64 CG: solution correction since the last residual replacement
   DevBuf r32, pa32, pb32, q32;
   DevBuf yh32, yl32;       // mixed: solution correction since the last fold, as an FP32 hi+lo pair
   CgState* h_state = nullptr;  // pinned, 2 slots

