@@ -1194,6 +1194,8 @@ int adfem_system_solver_info(const adfem_system* sys, adfem_solver_info* info) {
   info->rows_per_block = sv.zcg ? sv.zL : 0;
   info->ring = sv.zcg ? sv.zW : 0;
   info->renumbered = sys->renumbered ? 1 : 0;
+  info->banded_fp64 = sv.dcg ? 1 : 0;
+  info->fp64_tile_rows = sv.dcg ? sv.dS : 0;
   return ADFEM_OK;
 }
 

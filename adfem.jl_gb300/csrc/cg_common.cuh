@@ -169,11 +169,14 @@ __device__ __forceinline__ void df_axpy(float& h, float& l, float a, float p) {
   h = hi;
 }
 
-// Bookkeeping after an FP64 residual evaluation of a mixed solve (thread 0 of the
-// last block).  rr: FP64 residual norm^2 (scaled), rn: norm^2 of its FP32 copy, rp:
-// (FP32 residual, current direction) in the same inner product.  mode 1 replaces the
-// recurrence residual; mode 2 only records rr.
-__device__ __forceinline__ void replacement_step(CgState* st, double rr, double rn, double rp, int mode) {
+// Bookkeeping after an FP64 residual evaluation of a mixed solve, or of the banded FP64
+// solve (thread 0 of the last block).  rr: FP64 residual norm^2 (scaled), rn: norm^2 of
+// its copy in the iteration's precision, rp: (that copy, current direction) in the same
+// inner product.  mode 1 replaces the recurrence residual; mode 2 only records rr.
+// st->rho_new: the recurrence's value that requested the replacement.
+__device__ __forceinline__ void replacement_step(CgState* st, double rr, double rn, double rp, int mode,
+                                                 bool fp64_recurrence = false) {
+  const double prev = st->last_rr64;
   st->rr64 = rr;
   if (mode == 2) return;
   // the solution correction has just been folded: no update term is pending any more
@@ -188,12 +191,16 @@ __device__ __forceinline__ void replacement_step(CgState* st, double rr, double 
     return;
   }
   // The FP64 residual of an FP64 iterate cannot fall below about 2^-53 |K| |y|
-  // (rounding of y itself, amplified by the largest eigenvalues).  Once the FP32
-  // residual has met rtol and the FP64 residual did not, a replacement whose FP64
-  // residual improved less than 4x on the previous one means the iterate is at that
-  // attainable accuracy: stop there.  (Before that, a small improvement can also come
-  // from the FP32 inner iteration's own limits, so it is not taken as the floor.)
-  if (st->final_seen && st->last_rr64 > 0.0 && rr > 0.0625 * st->last_rr64) {
+  // (rounding of y itself, amplified by the largest eigenvalues).  A replacement whose
+  // FP64 residual improved less than 4x on the previous one, although the recurrence
+  // dropped 10x in between, means the iterate is at that attainable accuracy: stop there.
+  // An FP32 recurrence can also stall for its own reasons (the inner iteration's
+  // attainable accuracy), so for the mixed solves the test applies only after a
+  // replacement requested by rtol has failed; an FP64 recurrence tracks the true residual
+  // until the floor, so for the banded FP64 solve it applies at once.
+  const bool stalled = prev > 0.0 && rr > 0.0625 * prev;
+  const bool floor = fp64_recurrence ? (stalled && st->rho_new <= st->delta2 * prev) : (st->final_seen && stalled);
+  if (floor) {
     st->floor_hit = 1;
     st->done = 1;
     return;
@@ -203,7 +210,7 @@ __device__ __forceinline__ void replacement_step(CgState* st, double rr, double 
     return;
   }
   if (st->final_req) st->final_seen = 1;
-  if (st->final_seen) st->last_rr64 = rr;
+  if (fp64_recurrence || st->final_seen) st->last_rr64 = rr;
   st->final_req = 0;
   if (st->updates == 0) {
     st->ar = 1.0;
@@ -227,9 +234,9 @@ __device__ __forceinline__ void replacement_step(CgState* st, double rr, double 
 // residual norm^2 (scaled); st->rho_new: the recurrence's value that requested it.  The
 // FP64 iterate has an attainable accuracy: its residual cannot fall below the rounding
 // of y itself (~2^-53 |K| |y|).  The FP64 recurrence tracks the true residual closely
-// until then, so a replacement requested by rtol or by a 10x drop of the recurrence
-// whose true residual improved less than 4x on the previous replacement's means the
-// iterate is at that floor: the solve stops there.
+// until then, so a replacement after a 10x drop of the recurrence whose true residual
+// improved less than 4x on the previous replacement's means the iterate is at that
+// floor: the solve stops there.
 __device__ __forceinline__ void replacement_step64(CgState* st, double rr) {
   const double prev = st->last_rr64;
   st->rr64 = rr;
@@ -242,7 +249,7 @@ __device__ __forceinline__ void replacement_step64(CgState* st, double rr) {
     st->done = 1;
     return;
   }
-  const bool dropped = st->final_req || st->rho_new <= st->delta2 * prev;
+  const bool dropped = st->rho_new <= st->delta2 * prev;
   if (prev > 0.0 && dropped && rr > 0.0625 * prev) {
     st->floor_hit = 1;
     st->done = 1;

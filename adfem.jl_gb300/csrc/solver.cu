@@ -126,7 +126,9 @@ __global__ void __launch_bounds__(kT) k_init(int64_t n, const double* __restrict
 // mode 2: final check only (rr64);
 // mode 3: FP64 CG residual replacement (r64 = r, p64 = r + beta p64 with the beta of the
 //         recurrence, then replacement_step64 decides: converged, at the attainable floor,
-//         out of iterations, or continue from the true residual).
+//         out of iterations, or continue from the true residual);
+// mode 4: banded FP64 CG replacement (r into the current buffer of its pair, the norm and
+//         the product with the current direction for re-orthogonalisation, as mode 1).
 template <bool D16>
 __global__ void __launch_bounds__(kT) k_residual64(int64_t n, const int32_t* __restrict__ sptr,
                                                    const void* __restrict__ col, const double* __restrict__ valD,
@@ -134,10 +136,13 @@ __global__ void __launch_bounds__(kT) k_residual64(int64_t n, const int32_t* __r
                                                    const double* __restrict__ y, double* __restrict__ r64,
                                                    double* __restrict__ p64, float* __restrict__ r32,
                                                    const float* __restrict__ pa, const float* __restrict__ pb,
+                                                   double* __restrict__ r64b, const double* __restrict__ p64b,
                                                    CgState* st, double* partials, int mode, int force) {
   if (!force && st->done != 3) return;
   const int it = st->iters;
   const float* plat = (it & 1) ? pb : pa;
+  double* rcur = (it & 1) ? r64b : r64;           // mode 4: the r / p pair the next launch reads
+  const double* pcur = (it & 1) ? p64b : p64;
   double a0 = 0.0, a1 = 0.0, a2 = 0.0;
   for (int64_t r = gtid(); r < n; r += gstride()) {
     int64_t base;
@@ -160,6 +165,10 @@ __global__ void __launch_bounds__(kT) k_residual64(int64_t n, const int32_t* __r
     } else if (mode == 3) {
       r64[r] = ri;
       p64[r] = fma(st->beta, p64[r], ri);
+    } else if (mode == 4) {
+      rcur[r] = ri;
+      a1 = fma(ri, ri, a1);
+      a2 = fma(ri, pcur[r], a2);
     } else if (mode == 1) {
       const float rf = (float)ri;
       r32[r] = rf;
@@ -175,7 +184,8 @@ __global__ void __launch_bounds__(kT) k_residual64(int64_t n, const int32_t* __r
       return;
     }
     if (mode != 0) {
-      replacement_step(st, rr, tot[1], tot[2], mode);
+      if (mode == 4) replacement_step(st, rr, tot[1], tot[2], 1, true);
+      else replacement_step(st, rr, tot[1], tot[2], mode);
       return;
     }
     st->rr64 = rr;
@@ -565,6 +575,7 @@ static SellPat sell_pat(const Sell& A) {
 
 Solver::~Solver() {
   if (g64) cudaGraphExecDestroy(g64);
+  if (gd) cudaGraphExecDestroy(gd);
   if (g32) cudaGraphExecDestroy(g32);
   if (gz) cudaGraphExecDestroy(gz);
   for (auto& e : ev)
@@ -640,6 +651,7 @@ int Solver::init(const Sell* A_, int64_t n_) {
   ADFEM_TRY(q32.alloc(n4));
   ADFEM_TRY(yh32.alloc(n4));
   ADFEM_TRY(yl32.alloc(n4));
+  ADFEM_TRY(dcg_plan(*this));
   if (!h_state) {
     std::lock_guard<std::mutex> lk(device_alloc_mutex());
     ADFEM_CUDA(cudaMallocHost(&h_state, 2 * sizeof(CgState)));
@@ -779,14 +791,14 @@ static void enqueue_residual(Solver& S, cudaStream_t st, int mode, int force, Ti
       k_residual64<true><<<S.grid, kT, 0, st>>>(S.n, sp, A.col.p, A.valD64.as<double>(), S.s32.as<float>(),
                                                 S.b.as<double>(), S.y64.as<double>(), S.r64.as<double>(),
                                                 S.p64.as<double>(), S.r32.as<float>(), S.pa32.as<float>(),
-                                                S.pb32.as<float>(), S.state.as<CgState>(), S.partials.as<double>(),
-                                                mode, force);
+                                                S.pb32.as<float>(), S.dr1.as<double>(), S.dp1.as<double>(),
+                                                S.state.as<CgState>(), S.partials.as<double>(), mode, force);
     else
       k_residual64<false><<<S.grid, kT, 0, st>>>(S.n, sp, A.col.p, A.valD64.as<double>(), S.s32.as<float>(),
                                                  S.b.as<double>(), S.y64.as<double>(), S.r64.as<double>(),
                                                  S.p64.as<double>(), S.r32.as<float>(), S.pa32.as<float>(),
-                                                 S.pb32.as<float>(), S.state.as<CgState>(), S.partials.as<double>(),
-                                                 mode, force);
+                                                 S.pb32.as<float>(), S.dr1.as<double>(), S.dp1.as<double>(),
+                                                 S.state.as<CgState>(), S.partials.as<double>(), mode, force);
   });
 }
 
@@ -829,9 +841,17 @@ static void enqueue_fp64_replacement(Solver& S, cudaStream_t st, int force, Time
   enqueue_residual(S, st, 3, force, tm);
 }
 
-// The three iteration schemes: FP64 CG, the scaled two-kernel mixed iteration, and the
-// banded one-kernel mixed iteration (zcg.cu).
-enum class Path { FP64, MIXED, BANDED };
+// The four iteration schemes: FP64 CG (three kernels), the scaled two-kernel mixed
+// iteration, and the banded one-kernel iterations (zcg.cu), mixed and FP64.
+enum class Path { FP64, MIXED, BANDED, DBANDED };
+
+// fold + true-residual replacement of the banded FP64 path (both return at entry unless due)
+static void enqueue_dreliable_update(Solver& S, cudaStream_t st, int force, Timer* tm = nullptr) {
+  Timer none;
+  if (!tm) tm = &none;
+  tm->run(2, st, [&] { dcg_enqueue_fold(S, st, force); });
+  enqueue_residual(S, st, 4, force, tm);
+}
 
 // fold + FP64 residual replacement of the banded path (both return at entry unless due)
 static void enqueue_zreliable_update(Solver& S, cudaStream_t st, int force, Timer* tm = nullptr) {
@@ -858,10 +878,14 @@ static void enqueue_iteration(Solver& S, Path path, int i, int chunk, cudaStream
   } else if (path == Path::MIXED) {
     enqueue_cg32(S, st, tm);
     if (check) enqueue_reliable_update(S, st, 0, tm);
-  } else {
+  } else if (path == Path::BANDED) {
     if (tm) tm->run(0, st, [&] { zcg_enqueue_iter(S, st); });
     else zcg_enqueue_iter(S, st);
     if (check) enqueue_zreliable_update(S, st, 0, tm);
+  } else {
+    if (tm) tm->run(0, st, [&] { dcg_enqueue_iter(S, st); });
+    else dcg_enqueue_iter(S, st);
+    if (check) enqueue_dreliable_update(S, st, 0, tm);
   }
 }
 
@@ -870,7 +894,7 @@ static int chunk_launches(Path path, int chunk) {
   for (int i = 0; i < chunk; i++)
     if ((i + 1) % kCheck == 0 || i + 1 == chunk) ru++;
   if (path == Path::FP64) return 3 * chunk + 2 * ru;
-  return (path == Path::MIXED ? 2 : 1) * chunk + 2 * ru;
+  return (path == Path::MIXED ? 2 : 1) * chunk + 2 * ru;  // (both banded paths: one launch)
 }
 
 // capture `chunk` iterations into a graph (kernels read all scalars from device state)
@@ -924,10 +948,12 @@ int solver_solve(Solver& S, const double* rhs, double* u, const uint8_t* zero_ro
   if (o.precision != ADFEM_PREC_FP64 && !mixed) return fail(ADFEM_ERR_INVALID, "solver: unknown precision");
   if (!(o.rtol > 0.0) || o.max_iter < 1) return fail(ADFEM_ERR_INVALID, "solver: rtol must be > 0, max_iter >= 1");
   const int chunk = std::max(1, std::min(o.chunk > 0 ? o.chunk : 32, 512));
-  const Path path = !mixed ? Path::FP64 : (S.zcg ? Path::BANDED : Path::MIXED);
+  const Path path = !mixed ? (S.dcg ? Path::DBANDED : Path::FP64) : (S.zcg ? Path::BANDED : Path::MIXED);
   cudaStream_t st = S.stream;
-  cudaGraphExec_t* gx = path == Path::FP64 ? &S.g64 : (path == Path::MIXED ? &S.g32 : &S.gz);
-  int* gc = path == Path::FP64 ? &S.g64_chunk : (path == Path::MIXED ? &S.g32_chunk : &S.gz_chunk);
+  cudaGraphExec_t* gx = path == Path::FP64 ? &S.g64
+                        : (path == Path::MIXED ? &S.g32 : (path == Path::BANDED ? &S.gz : &S.gd));
+  int* gc = path == Path::FP64 ? &S.g64_chunk
+            : (path == Path::MIXED ? &S.g32_chunk : (path == Path::BANDED ? &S.gz_chunk : &S.gd_chunk));
   if (!prof) {
     if (*gx && *gc != chunk) {
       cudaGraphExecDestroy(*gx);
@@ -965,6 +991,9 @@ int solver_solve(Solver& S, const double* rhs, double* u, const uint8_t* zero_ro
       ADFEM_CUDA(cudaMemsetAsync(S.yh32.p, 0, sizeof(float) * S.n, st));
       ADFEM_CUDA(cudaMemsetAsync(S.yl32.p, 0, sizeof(float) * S.n, st));
       enqueue_residual(S, st, 1, 1);
+    } else if (path == Path::DBANDED) {
+      ADFEM_TRY(dcg_clear(S, st));
+      enqueue_residual(S, st, 4, 1);
     } else {
       ADFEM_CUDA(cudaMemsetAsync(S.z64.p, 0, sizeof(double) * S.n, st));
       enqueue_residual(S, st, 0, 1);
@@ -974,7 +1003,7 @@ int solver_solve(Solver& S, const double* rhs, double* u, const uint8_t* zero_ro
   launches += 2;
 
   CgState cur;
-  if (prof && path == Path::BANDED) {
+  if (prof && (path == Path::BANDED || path == Path::DBANDED)) {
     // runs of kCheck iterations as a captured graph (as in the solve) with an event pair
     // around each run, the fold and residual checks with an event pair around each launch
     Timer tm;
@@ -982,7 +1011,10 @@ int solver_solve(Solver& S, const double* rhs, double* u, const uint8_t* zero_ro
     tm.prof = prof;
     GraphExecGuard runk;
     ADFEM_TRY(capture_graph(S, &runk.g, [&] {
-      for (int i = 0; i < kCheck; i++) zcg_enqueue_iter(S, S.stream);
+      for (int i = 0; i < kCheck; i++) {
+        if (path == Path::BANDED) zcg_enqueue_iter(S, S.stream);
+        else dcg_enqueue_iter(S, S.stream);
+      }
     }));
     for (;;) {
       for (int r = 0; r < 4; r++) {
@@ -990,7 +1022,8 @@ int solver_solve(Solver& S, const double* rhs, double* u, const uint8_t* zero_ro
         tm.open_n = kCheck;
         ADFEM_CUDA(cudaGraphLaunch(runk.g, st));
         tm.close(st);
-        enqueue_zreliable_update(S, st, 0, &tm);
+        if (path == Path::BANDED) enqueue_zreliable_update(S, st, 0, &tm);
+        else enqueue_dreliable_update(S, st, 0, &tm);
       }
       launches += 4 * (kCheck + 2);
       ADFEM_CUDA(cudaGetLastError());
@@ -1037,6 +1070,9 @@ int solver_solve(Solver& S, const double* rhs, double* u, const uint8_t* zero_ro
   // with the Dirichlet rows set exactly
   if (path == Path::BANDED) {
     zcg_enqueue_fold(S, st, 1);
+    launches += 1;
+  } else if (path == Path::DBANDED) {
+    dcg_enqueue_fold(S, st, 1);
     launches += 1;
   } else if (mixed) {
     k_fold<<<S.grid, kT, 0, st>>>(S.n, S.y64.as<double>(), S.yh32.as<float>(), S.yl32.as<float>(),

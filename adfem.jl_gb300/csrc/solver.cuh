@@ -69,6 +69,13 @@ struct Solver {
   DevBuf bz32;             // zblock2: per row {K_ii, K_(i,i^1)} (FP32)
   cudaGraphExec_t gz = nullptr;
   int gz_chunk = 0;
+  // banded FP64 path (zcg.cu, k_dcg_iter): FP64 solves when the band fits
+  bool dcg = false;
+  int dS = 0;              // rows per FP64 super-tile
+  size_t dsmem = 0;
+  DevBuf dr1, dp1, dq1;    // second buffers of the r, p, q pairs (first: r64, p64, q64)
+  cudaGraphExec_t gd = nullptr;
+  int gd_chunk = 0;
   ~Solver();
   int init(const Sell* A, int64_t n);
 };
@@ -104,6 +111,11 @@ void zcg_enqueue_iter(Solver& S, cudaStream_t st);
 void zcg_enqueue_residual(Solver& S, cudaStream_t st, int mode, int force);
 void zcg_enqueue_fold(Solver& S, cudaStream_t st, int force);
 void zcg_enqueue_unscale(Solver& S, cudaStream_t st, const uint8_t* fix, const double* fixval, double* u);
+// Banded FP64 path (zcg.cu): planned after zcg_plan; iteration, fold, clear.
+int dcg_plan(Solver& S);
+void dcg_enqueue_iter(Solver& S, cudaStream_t st);
+void dcg_enqueue_fold(Solver& S, cudaStream_t st, int force);
+int dcg_clear(Solver& S, cudaStream_t st);
 
 // Fill sliced-ELL values from CSR values (same pattern).
 // ---- packed solves of small systems (pack.cu)

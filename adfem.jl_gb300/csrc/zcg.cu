@@ -763,6 +763,305 @@ void zcg_enqueue_unscale(Solver& S, cudaStream_t st, const uint8_t* fix, const d
   k_zunscale<<<(unsigned)((S.n + kT - 1) / kT), kT, 0, st>>>(S.n, S.y64.as<double>(), fix, fixval, u);
 }
 
+// ---------------------------------------------------------------------------
+// Banded FP64 CG: the same one-kernel iteration in FP64 -- same banded row ranges,
+// shared-memory window, column patterns and lagged vector updates -- for the Jacobi-
+// scaled operator K~ = S K S (unit diagonal) in standard form, so it is Jacobi-PCG on K
+// with every value, vector and dot product in FP64.  It is the like-for-like FP64
+// counterpart of k_zcg_iter (and the FP64 path wherever the band fits).  Per launch k:
+//   r_k = r_{k-1} - a_{k-1} q_{k-1},  p_k = ar r_k + ap p_{k-1},  q_k = K~ p_k,
+//   z += a_{k-2} p_{k-2} + a_{k-1} p_{k-1} on even k (the solution correction since the
+//   last fold, as in the mixed kernel), and the dot products r_k.r_k, p_k.q_k, q_k.q_k
+//   (p_{k-1}.q_k after a residual replacement) in one grid reduction; the last block sets
+//   a_k = rho_k / p.q and beta_k from rho_{k+1} ~ rho_k - 2 a_k r.q + a_k^2 q.q.
+// The window holds p_k in FP64 (twice the bytes of the mixed window), so at 4M DOF a
+// block's rows are split into two super-tiles, each with its own halo.  The values are
+// read from the scaled sliced-ELL operator (entry k of row i at sptr[i/32] + 32k + i%32).
+struct DcgArgs {
+  int64_t n;
+  int64_t L;
+  int S, H, period, zw;
+  const int32_t* zpid;
+  const int32_t* pool;
+  int npool;
+  const int16_t* colz;
+  const int32_t* sptr;
+  const double* val;
+  double* r[2];
+  double* p[2];
+  double* q[2];
+  double* z;
+  CgState* st;
+  double* partials;
+};
+
+template <int MAXW, int BT, int U1, int U2>
+__global__ void __launch_bounds__(BT, 1) k_dcg_iter(DcgArgs A) {
+  static_assert(MAXW % 4 == 0, "pattern rows are loaded as int4");
+  CgState* st = A.st;
+  if (st->done) return;
+  extern __shared__ double dsm[];
+  int* spool = reinterpret_cast<int*>(dsm);
+  double* sP = dsm + ((A.npool + 3) & ~3) / 2;  // (pool padded to 16 bytes)
+  for (int j = threadIdx.x; j < A.npool; j += BT) spool[j] = __ldg(A.pool + j);
+  const int it = st->iters;
+  const int cur = it & 1, nxt = cur ^ 1;
+  const double* __restrict__ rprev = A.r[cur];
+  const double* __restrict__ pprev = A.p[cur];
+  const double* __restrict__ qprev = A.q[cur];
+  double* __restrict__ rnew = A.r[nxt];
+  double* __restrict__ pnew = A.p[nxt];
+  double* __restrict__ qnew = A.q[nxt];
+  double* __restrict__ z = A.z;
+  const double a = st->alpha, ar = st->ar, ap = st->ap, a2 = st->alpha_prev;
+  const bool ydo = (it & 1) == 0;
+  const bool plain = ar == 1.0;   // uniform
+  const bool full_zq = !plain;
+  const int tid = threadIdx.x;
+  const int zw = A.zw;
+  const int n = (int)A.n;
+  const int blo = (int)blockIdx.x * (int)A.L;
+  const int bhi = min(blo + (int)A.L, n);
+  double pq = 0.0, pkq = 0.0, qq = 0.0, rr = 0.0;
+
+  for (int lo = blo; lo < bhi; lo += A.S) {
+    const int hi = min(lo + A.S, bhi);
+    const int wlo = max(lo - A.H, 0);
+    const int whi = min(hi + A.H, n);
+    if (lo != blo) __syncthreads();
+    struct In {
+      double rp, qp, pp, p2, y;
+      bool own;
+    };
+    auto fetch1 = [&](int pos, In& x) {
+      x.own = pos >= lo && pos < hi;
+      x.rp = __ldg(rprev + pos);
+      x.qp = __ldg(qprev + pos);
+      x.pp = __ldg(pprev + pos);
+      const bool yupd = x.own && ydo;
+      x.p2 = yupd ? pnew[pos] : 0.0;  // p_{k-2}, read before this thread overwrites it with p_k
+      x.y = yupd ? z[pos] : 0.0;
+    };
+    auto commit = [&](int pos, In& x) {
+      const double rk = fma(-a, x.qp, x.rp);
+      const double pk = plain ? fma(ap, x.pp, rk) : fma(ap, x.pp, ar * rk);
+      sP[pos - wlo] = pk;
+      if (x.own) {
+        rnew[pos] = rk;
+        pnew[pos] = pk;
+        if (ydo) z[pos] = fma(a, x.pp, fma(a2, x.p2, x.y));
+        rr = fma(rk, rk, rr);
+      }
+    };
+    int pos = wlo + tid;
+    for (; pos + (U1 - 1) * BT < whi; pos += U1 * BT) {
+      In x[U1];
+#pragma unroll
+      for (int u = 0; u < U1; u++) fetch1(pos + u * BT, x[u]);
+#pragma unroll
+      for (int u = 0; u < U1; u++) commit(pos + u * BT, x[u]);
+    }
+    for (; pos < whi; pos += BT) {
+      In x0;
+      fetch1(pos, x0);
+      commit(pos, x0);
+    }
+    __syncthreads();
+    // ---- phase 2: q = K~ p_k for the rows [lo, hi)
+    auto fetch = [&](int i, double (&v)[MAXW], int& pid) {
+      const int s0 = __ldg(A.sptr + (i >> 5)), s1 = __ldg(A.sptr + (i >> 5) + 1);
+      const int w = (s1 - s0) >> 5;
+      const int base = s0 + (i & 31);
+#pragma unroll
+      for (int k = 0; k < MAXW; k++) v[k] = k < w ? __ldg(A.val + base + 32 * k) : 0.0;
+      pid = __ldg(A.zpid + (i >> 5));
+    };
+    auto row = [&](int i, const double (&v)[MAXW], int pid) {
+      // column deltas are read as they are used (no register copy of the row's pattern:
+      // the 16-wide variant would spill)
+      double s = 0.0;
+      if (pid >= 0) {
+        const int4* pv = reinterpret_cast<const int4*>(spool) + (pid * A.period + (A.period == 2 ? (i & 1) : 0)) *
+                                                                     (MAXW / 4);
+        const double* sPi = sP + (i - wlo);
+#pragma unroll
+        for (int h = 0; h < MAXW / 4; h++) {
+          const int4 x = pv[h];
+          s = fma(v[4 * h], sPi[x.x], s);
+          s = fma(v[4 * h + 1], sPi[x.y], s);
+          s = fma(v[4 * h + 2], sPi[x.z], s);
+          s = fma(v[4 * h + 3], sPi[x.w], s);
+        }
+      } else {
+        const int base = (i >> 5) * (32 * zw) + (i & 31);
+#pragma unroll
+        for (int k = 0; k < MAXW; k++) {
+          const int dk = k < zw ? (int)__ldg(A.colz + base + 32 * k) : 0;
+          s = fma(v[k], sP[i + dk - wlo], s);
+        }
+      }
+      qnew[i] = s;
+      const double Pi = sP[i - wlo];
+      pq = fma(Pi, s, pq);
+      qq = fma(s, s, qq);
+      if (full_zq) pkq = fma(__ldg(pprev + i), s, pkq);
+    };
+    int i = lo + tid;
+    for (; i + (U2 - 1) * BT < hi; i += U2 * BT) {
+      double v[U2][MAXW];
+      int pid[U2];
+#pragma unroll
+      for (int u = 0; u < U2; u++) fetch(i + u * BT, v[u], pid[u]);
+#pragma unroll
+      for (int u = 0; u < U2; u++) row(i + u * BT, v[u], pid[u]);
+    }
+    for (; i < hi; i += BT) {
+      double v0[MAXW];
+      int g0;
+      fetch(i, v0, g0);
+      row(i, v0, g0);
+    }
+  }
+
+  double v[4] = {pq, pkq, qq, rr}, tot[4];
+  if (reduce_grid<double, 4, BT>(v, A.partials, &st->counter[0], tot) && threadIdx.x == 0) {
+    const double pqd = tot[0], qqd = tot[2], rho = tot[3];
+    const double zqd = (full_zq && st->ar != 0.0) ? (pqd - st->ap * tot[1]) / st->ar : pqd;
+    if (!isfinite(rho) || !isfinite(pqd)) {
+      st->done = 2;
+    } else if (rho <= st->stop2) {
+      st->rho_new = rho;
+      st->final_req = 1;
+      st->done = 3;
+    } else if (rho <= st->ru2 || it >= st->max_iter) {
+      st->rho_new = rho;
+      st->done = 3;
+    } else if (!(pqd > 0.0)) {
+      st->done = 2;
+    } else {
+      const double al = rho / pqd;
+      const double est = rho - 2.0 * al * zqd + al * al * qqd;
+      st->alpha_prev = st->alpha;
+      st->alpha = al;
+      st->ar = 1.0;
+      st->ap = fmax(est, 0.0) / rho;
+      st->rho = rho;
+      st->iters = it + 1;
+    }
+  }
+}
+
+// Fold of the banded FP64 path: y += z plus the update a_{k-1} p_{k-1} still pending
+// after an odd iteration counter; z = 0.  Runs when a replacement is due or when forced.
+__global__ void __launch_bounds__(kT) k_dfold(int64_t n, double* __restrict__ y64, double* __restrict__ z,
+                                              const double* __restrict__ p0, const double* __restrict__ p1,
+                                              const CgState* st, int force) {
+  if (!force && st->done != 3) return;
+  const int it = st->iters;
+  const double a = (it & 1) ? st->alpha : 0.0;
+  const double* __restrict__ pp = (it & 1) ? p1 : p0;
+  for (int64_t i = gtid(); i < n; i += gstride()) {
+    y64[i] += z[i] + a * pp[i];
+    z[i] = 0.0;
+  }
+}
+
+#ifndef ADFEM_DCG_U1
+#define ADFEM_DCG_U1 2
+#endif
+static constexpr int kDU1 = ADFEM_DCG_U1;  // phase-1 positions per thread and trip
+static constexpr int kDU2W8 = 1;           // phase-2 rows per thread and trip
+
+// Plan of the banded FP64 path (after zcg_plan succeeded): FP64 window super-tiles of
+// equal size within each block's rows, and the second buffers of the r, p, q pairs.
+int dcg_plan(Solver& S) {
+  S.dcg = false;
+  const char* env = std::getenv("ADFEM_ZCG64");
+  if (env && env[0] == '0') return ADFEM_OK;
+  if (!S.zcg || S.A->maxw > 16) return ADFEM_OK;
+  const size_t pool_bytes = sizeof(int32_t) * (size_t)((S.znpool + 3) & ~3);
+  const int64_t room = (int64_t)((kZSmemBlock - pool_bytes) / sizeof(double)) - 2 * (int64_t)S.zH - 2;
+  const int64_t smax = room / 32 * 32;
+  if (smax < std::max<int64_t>(512, (int64_t)S.zH)) return ADFEM_OK;
+  const int64_t L = S.zL;
+  const int64_t tiles = (L + smax - 1) / smax;
+  int64_t St = (L + tiles - 1) / tiles;
+  St = (St + 31) / 32 * 32;
+  if (const char* cap = std::getenv("ADFEM_ZCG_SMAX")) {
+    const int64_t c = std::atoll(cap) / 32 * 32;
+    if (c >= 32) St = std::min(St, c);
+  }
+  S.dS = (int)St;
+  S.dsmem = pool_bytes + sizeof(double) * (size_t)(St + 2 * S.zH + 2);
+  if (S.dsmem > kZSmemBlock) return ADFEM_OK;
+  auto kern8 = k_dcg_iter<8, kZBT, kDU1, kDU2W8>;
+  auto kern16 = k_dcg_iter<16, kZBT, 1, 1>;
+  static std::once_flag once;
+  static cudaError_t set_err = cudaSuccess;
+  std::call_once(once, [&] {
+    std::lock_guard<std::mutex> lk(device_alloc_mutex());
+    set_err = cudaFuncSetAttribute(kern8, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kZSmemBlock);
+    if (set_err == cudaSuccess)
+      set_err = cudaFuncSetAttribute(kern16, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kZSmemBlock);
+  });
+  if (set_err != cudaSuccess) return cuda_fail(set_err, "cudaFuncSetAttribute");
+  int per = 0;
+  ADFEM_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, S.A->maxw <= 8 ? kern8 : kern16, kZBT, S.dsmem));
+  if (per < 1) return ADFEM_OK;
+  const size_t n8 = sizeof(double) * (size_t)S.n;
+  ADFEM_TRY(S.dr1.alloc(n8));
+  ADFEM_TRY(S.dp1.alloc(n8));
+  ADFEM_TRY(S.dq1.alloc(n8));
+  S.dcg = true;
+  return ADFEM_OK;
+}
+
+static DcgArgs dcg_args(Solver& S) {
+  const Sell& A = *S.A;
+  DcgArgs d;
+  d.n = S.n;
+  d.L = S.zL;
+  d.S = S.dS;
+  d.H = S.zH;
+  d.period = A.pat_period;
+  d.zw = S.zw;
+  d.zpid = S.zpid32.as<int32_t>();
+  d.pool = S.zpool32.as<int32_t>();
+  d.npool = S.znpool;
+  d.colz = S.colz16.as<int16_t>();
+  d.sptr = A.sptr.as<int32_t>();
+  d.val = A.val64.as<double>();
+  d.r[0] = S.r64.as<double>();
+  d.r[1] = S.dr1.as<double>();
+  d.p[0] = S.p64.as<double>();
+  d.p[1] = S.dp1.as<double>();
+  d.q[0] = S.q64.as<double>();
+  d.q[1] = S.dq1.as<double>();
+  d.z = S.z64.as<double>();
+  d.st = S.state.as<CgState>();
+  d.partials = S.partials.as<double>();
+  return d;
+}
+
+void dcg_enqueue_iter(Solver& S, cudaStream_t st) {
+  const DcgArgs d = dcg_args(S);
+  if (S.A->maxw <= 8) k_dcg_iter<8, kZBT, kDU1, kDU2W8><<<S.zgrid, kZBT, S.dsmem, st>>>(d);
+  else k_dcg_iter<16, kZBT, 1, 1><<<S.zgrid, kZBT, S.dsmem, st>>>(d);
+}
+
+void dcg_enqueue_fold(Solver& S, cudaStream_t st, int force) {
+  k_dfold<<<S.grid, kT, 0, st>>>(S.n, S.y64.as<double>(), S.z64.as<double>(), S.p64.as<double>(),
+                                 S.dp1.as<double>(), S.state.as<CgState>(), force);
+}
+
+// buffers the banded FP64 path zeroes before a solve (r, p, q pairs and the correction)
+int dcg_clear(Solver& S, cudaStream_t st) {
+  const size_t n8 = sizeof(double) * (size_t)S.n;
+  for (DevBuf* b : {&S.r64, &S.dr1, &S.p64, &S.dp1, &S.q64, &S.dq1, &S.z64})
+    ADFEM_CUDA(cudaMemsetAsync(b->p, 0, n8, st));
+  return ADFEM_OK;
+}
+
 // buffers the banded path zeroes before a solve
 int zcg_clear(Solver& S, cudaStream_t st) {
   const size_t n4 = sizeof(float) * (size_t)S.n;

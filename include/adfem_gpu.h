@@ -380,6 +380,9 @@ typedef struct adfem_solver_info {
   int ring;                   /* shared-memory positions per super-tile: rows + 2 band (0 if not banded) */
   int renumbered;             /* 1: nodes renumbered for the solver (reverse Cuthill-McKee; inputs and
                                  outputs stay in the reference order) */
+  int banded_fp64;            /* 1: FP64 solves use the one-kernel banded FP64 iteration (same layout and
+                                 fusion as the mixed one), 0: the three-kernel FP64 iteration */
+  int fp64_tile_rows;         /* rows per super-tile of the banded FP64 iteration (0 if not used) */
 } adfem_solver_info;
 ADFEM_API int adfem_system_solver_info(const adfem_system *sys, adfem_solver_info *info);
 /* Packed solves of small systems: the systems (each assembled, at most 65536 DOFs,
