@@ -80,9 +80,9 @@ class _System:
         _dev(u, self.ndof, "u")
         o = solver_opts(precision, rtol, max_iter, ru_delta, chunk, warm)
         st = SolverStats()
+        self.last_stats = st  # (filled in also when the solve reports an error status)
         check(_lib.load().adfem_system_solve_d(self._h, ptr(u), ctypes.byref(o), ctypes.byref(st), _cur_stream()),
               "system_solve")
-        self.last_stats = st
         return u
 
     def adjoint(self, g, lam=None, precision="fp64", rtol=1e-12, max_iter=200000, ru_delta=0.1, chunk=32):

@@ -36,6 +36,10 @@ __device__ __forceinline__ double gpair(const double4& g, int a, int b) {
 }
 
 // ---------------------------------------------------------------------------
+// src_e[r] = w sum_k f_k phi_r(x_k).  With the degree-2 rule above, phi_r is 2/3 at one
+// point k*(r) and 1/6 at the other two (k* = 0, 2, 1 for r = 0, 1, 2), so the sum is
+// w (S/6 + f_{k*}/2) with S = f0 + f1 + f2: 11 FP64 operations per element instead of 14
+// (the element pass is FP64-instruction bound on GB300).
 __global__ void k_element_prepass(int64_t ne, const double* __restrict__ kappa, const double* __restrict__ f,
                                   const double4* __restrict__ geo, double* __restrict__ sigma,
                                   double* __restrict__ src3) {
@@ -43,10 +47,12 @@ __global__ void k_element_prepass(int64_t ne, const double* __restrict__ kappa, 
   if (e >= ne) return;
   if (kappa) sigma[e] = kappa[3 * e] + kappa[3 * e + 1] + kappa[3 * e + 2];
   if (f) {
-    double w = geo[e].w;
-    double f0 = f[3 * e], f1 = f[3 * e + 1], f2 = f[3 * e + 2];
-#pragma unroll
-    for (int r = 0; r < 3; r++) src3[3 * e + r] = w * (f0 * lam(0, r) + f1 * lam(1, r) + f2 * lam(2, r));
+    const double w = geo[e].w;
+    const double f0 = f[3 * e], f1 = f[3 * e + 1], f2 = f[3 * e + 2];
+    const double s6 = (f0 + f1 + f2) * (1.0 / 6.0);
+    src3[3 * e] = w * fma(f0, 0.5, s6);
+    src3[3 * e + 1] = w * fma(f2, 0.5, s6);
+    src3[3 * e + 2] = w * fma(f1, 0.5, s6);
   }
 }
 

@@ -197,9 +197,12 @@ __device__ __forceinline__ void replacement_step(CgState* st, double rr, double 
   // An FP32 recurrence can also stall for its own reasons (the inner iteration's
   // attainable accuracy), so for the mixed solves the test applies only after a
   // replacement requested by rtol has failed; an FP64 recurrence tracks the true residual
-  // until the floor, so for the banded FP64 solve it applies at once.
+  // until the floor, so for the banded FP64 solve it also applies after a 10x drop.  (A
+  // floor less than 10x above rtol is only seen through a failed rtol replacement: the
+  // recurrence reaches rtol again without dropping 10x.)
   const bool stalled = prev > 0.0 && rr > 0.0625 * prev;
-  const bool floor = fp64_recurrence ? (stalled && st->rho_new <= st->delta2 * prev) : (st->final_seen && stalled);
+  const bool floor =
+      stalled && (st->final_seen || (fp64_recurrence && st->rho_new <= st->delta2 * prev));
   if (floor) {
     st->floor_hit = 1;
     st->done = 1;
@@ -249,8 +252,10 @@ __device__ __forceinline__ void replacement_step64(CgState* st, double rr) {
     st->done = 1;
     return;
   }
+  // (after a failed rtol replacement the recurrence may reach rtol again without a 10x
+  // drop, when the floor is less than 10x above rtol: then the second stall decides)
   const bool dropped = st->rho_new <= st->delta2 * prev;
-  if (prev > 0.0 && dropped && rr > 0.0625 * prev) {
+  if (prev > 0.0 && rr > 0.0625 * prev && (dropped || st->final_seen)) {
     st->floor_hit = 1;
     st->done = 1;
     return;
@@ -259,6 +264,7 @@ __device__ __forceinline__ void replacement_step64(CgState* st, double rr) {
     st->done = 4;
     return;
   }
+  if (st->final_req) st->final_seen = 1;
   st->final_req = 0;
   st->updates += 1;
   st->rho = rr;

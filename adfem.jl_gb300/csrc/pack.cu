@@ -647,8 +647,9 @@ int pack_rows_limit() {
 int solve_packed(PackItem* items, int count, cudaStream_t st, PackSlot* slot) {
   const int limit = pack_rows_limit();
   for (int i = 0; i < count; i++) {
-    const Solver& S = *items[i].S;
+    Solver& S = *items[i].S;
     if (!S.prepared) return fail(ADFEM_ERR_INVALID, "packed solve: operator not prepared");
+    ADFEM_TRY(solver_ensure_scaled(S, st));  // the packed kernels read the Jacobi-scaled copies
     if (S.n > limit) return fail(ADFEM_ERR_INVALID, "packed solve: system larger than the packed limit");
     if (!(items[i].rtol > 0.0) || items[i].max_iter < 1) return fail(ADFEM_ERR_INVALID, "packed solve: bad options");
   }

@@ -671,31 +671,59 @@ int Solver::init(const Sell* A_, int64_t n_) {
   return ADFEM_OK;
 }
 
+// After an assembly: the copies the system's default solve needs are made at once (the
+// banded mixed copies when the band fits, else the Jacobi-scaled copies), which also
+// checks the diagonal; the Jacobi-scaled copies of a banded system (FP64 solves, the
+// scaled mixed path, packed solves, apply) are made on first use (solver_ensure_scaled),
+// so an assembly followed by mixed solves does not pay for them.
 int solver_prepare(Solver& S, const int32_t* diagpos_dev, cudaStream_t user) {
-  const Sell& A = *S.A;
   S.prepared = false;
+  S.prep_scaled = false;
   if (!diagpos_dev) return fail(ADFEM_ERR_INVALID, "solver_prepare: diagonal positions required");
+  S.diagpos = diagpos_dev;
+  if (!S.zcg) {
+    ADFEM_TRY(solver_ensure_scaled(S, user));
+    S.prepared = true;
+    return ADFEM_OK;
+  }
   DevBuf bad;
   ADFEM_TRY(bad.alloc(sizeof(int)));
   ADFEM_CUDA(cudaMemsetAsync(bad.p, 0, sizeof(int), user));
-  const unsigned nb = (unsigned)((S.n + kT - 1) / kT);
-  if (S.zcg) ADFEM_TRY(zcg_prepare(S, diagpos_dev, bad.as<int>(), user));  // reads the unscaled values
-  k_scale_diag<<<nb, kT, 0, user>>>(S.n, A.sptr.as<int32_t>(), A.val64.as<double>(), diagpos_dev, S.s32.as<float>(),
-                                    bad.as<int>());
-  if (A.delta16)
-    k_scale_values<true><<<nb, kT, 0, user>>>(S.n, A.sptr.as<int32_t>(), A.col.p, A.val64.as<double>(),
-                                              A.valD64.as<double>(), A.val32.as<float>(), S.s32.as<float>(),
-                                              diagpos_dev);
-  else
-    k_scale_values<false><<<nb, kT, 0, user>>>(S.n, A.sptr.as<int32_t>(), A.col.p, A.val64.as<double>(),
-                                               A.valD64.as<double>(), A.val32.as<float>(), S.s32.as<float>(),
-                                               diagpos_dev);
-  ADFEM_CUDA(cudaGetLastError());
+  ADFEM_TRY(zcg_prepare(S, diagpos_dev, bad.as<int>(), user));  // reads the unscaled values
   int hbad = 0;
   ADFEM_CUDA(cudaMemcpyAsync(&hbad, bad.p, sizeof(int), cudaMemcpyDeviceToHost, user));
   ADFEM_CUDA(cudaStreamSynchronize(user));
   if (hbad) return fail(ADFEM_ERR_BREAKDOWN, "operator has a non-positive or non-finite diagonal entry");
   S.prepared = true;
+  return ADFEM_OK;
+}
+
+// Jacobi-scaled copies: s_i = rsqrt(K_ii), val64 <- s_i K_ij s_j in place (standard form),
+// valD64 / val32 the FP64 / FP32 difference forms (k_scale_values).  Once per assembly.
+int solver_ensure_scaled(Solver& S, cudaStream_t user) {
+  if (S.prep_scaled) return ADFEM_OK;
+  if (!S.diagpos) return fail(ADFEM_ERR_INVALID, "solver: operator not prepared");
+  const Sell& A = *S.A;
+  DevBuf bad;
+  ADFEM_TRY(bad.alloc(sizeof(int)));
+  ADFEM_CUDA(cudaMemsetAsync(bad.p, 0, sizeof(int), user));
+  const unsigned nb = (unsigned)((S.n + kT - 1) / kT);
+  k_scale_diag<<<nb, kT, 0, user>>>(S.n, A.sptr.as<int32_t>(), A.val64.as<double>(), S.diagpos, S.s32.as<float>(),
+                                    bad.as<int>());
+  if (A.delta16)
+    k_scale_values<true><<<nb, kT, 0, user>>>(S.n, A.sptr.as<int32_t>(), A.col.p, A.val64.as<double>(),
+                                              A.valD64.as<double>(), A.val32.as<float>(), S.s32.as<float>(),
+                                              S.diagpos);
+  else
+    k_scale_values<false><<<nb, kT, 0, user>>>(S.n, A.sptr.as<int32_t>(), A.col.p, A.val64.as<double>(),
+                                               A.valD64.as<double>(), A.val32.as<float>(), S.s32.as<float>(),
+                                               S.diagpos);
+  ADFEM_CUDA(cudaGetLastError());
+  int hbad = 0;
+  ADFEM_CUDA(cudaMemcpyAsync(&hbad, bad.p, sizeof(int), cudaMemcpyDeviceToHost, user));
+  ADFEM_CUDA(cudaStreamSynchronize(user));
+  if (hbad) return fail(ADFEM_ERR_BREAKDOWN, "operator has a non-positive or non-finite diagonal entry");
+  S.prep_scaled = true;
   return ADFEM_OK;
 }
 
@@ -949,6 +977,7 @@ int solver_solve(Solver& S, const double* rhs, double* u, const uint8_t* zero_ro
   if (!(o.rtol > 0.0) || o.max_iter < 1) return fail(ADFEM_ERR_INVALID, "solver: rtol must be > 0, max_iter >= 1");
   const int chunk = std::max(1, std::min(o.chunk > 0 ? o.chunk : 32, 512));
   const Path path = !mixed ? (S.dcg ? Path::DBANDED : Path::FP64) : (S.zcg ? Path::BANDED : Path::MIXED);
+  if (path != Path::BANDED) ADFEM_TRY(solver_ensure_scaled(S, user));
   cudaStream_t st = S.stream;
   cudaGraphExec_t* gx = path == Path::FP64 ? &S.g64
                         : (path == Path::MIXED ? &S.g32 : (path == Path::BANDED ? &S.gz : &S.gd));
@@ -1118,6 +1147,7 @@ int solver_solve(Solver& S, const double* rhs, double* u, const uint8_t* zero_ro
 }
 
 int solver_apply(Solver& S, const double* x, double* y, cudaStream_t user) {
+  ADFEM_TRY(solver_ensure_scaled(S, user));
   const Sell& A = *S.A;
   const unsigned nb = (unsigned)((S.n + kT - 1) / kT);
   if (A.delta16)

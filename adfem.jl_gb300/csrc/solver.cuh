@@ -49,6 +49,8 @@ struct Solver {
   std::vector<cudaEvent_t> pev;  // event pool of profiled solves
   int g64_chunk = 0, g32_chunk = 0;
   bool prepared = false;
+  bool prep_scaled = false;        // the Jacobi-scaled copies are current (see solver_ensure_scaled)
+  const int32_t* diagpos = nullptr; // device: entry index of the diagonal in each row
   // banded mixed path (zcg.cu): used by mixed solves when the band fits the ring
   bool zcg = false;
   int zH = 0, zgrid = 0;
@@ -80,9 +82,12 @@ struct Solver {
   int init(const Sell* A, int64_t n);
 };
 
-// scale the operator: s_i = rsqrt(K_ii) (FP32), val64 <- s_i K_ij s_j, val32 <- the FP32
-// difference-form copy (see k_scale_values).  diagpos: entry index k of the diagonal in row i.
+// After an assembly (diagpos: entry index k of the diagonal in row i): makes the copies
+// the default solve needs now and marks the others for first use.
 int solver_prepare(Solver& S, const int32_t* diagpos_dev, cudaStream_t user);
+// The Jacobi-scaled copies: s_i = rsqrt(K_ii) (FP32), val64 <- s_i K_ij s_j, valD64 / val32
+// the FP64 / FP32 difference-form copies (see k_scale_values); no-op when current.
+int solver_ensure_scaled(Solver& S, cudaStream_t user);
 // Per-kernel timing of a profiled solve: 0 SpMV+dot, 1 update+dot, 2 p update / fold,
 // 3 FP64 residual.
 struct SolveProfile {
