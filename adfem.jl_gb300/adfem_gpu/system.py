@@ -94,9 +94,9 @@ class _System:
             lam = torch.zeros(self.ndof, dtype=torch.float64, device="cuda")
         o = solver_opts(precision, rtol, max_iter, ru_delta, chunk, False)
         st = SolverStats()
+        self.last_stats = st
         check(_lib.load().adfem_system_adjoint_d(self._h, ptr(g), ptr(lam), ctypes.byref(o), ctypes.byref(st),
                                                  _cur_stream()), "system_adjoint")
-        self.last_stats = st
         return lam
 
     def apply(self, x):

@@ -768,7 +768,7 @@ void zcg_enqueue_unscale(Solver& S, cudaStream_t st, const uint8_t* fix, const d
 // shared-memory window, column patterns and lagged vector updates -- for the Jacobi-
 // scaled operator K~ = S K S (unit diagonal) in standard form, so it is Jacobi-PCG on K
 // with every value, vector and dot product in FP64.  It is the like-for-like FP64
-// counterpart of k_zcg_iter (and the FP64 path wherever the band fits).  Per launch k:
+// counterpart of k_zcg_iter (selected with ADFEM_ZCG64=1, see dcg_plan).  Per launch k:
 //   r_k = r_{k-1} - a_{k-1} q_{k-1},  p_k = ar r_k + ap p_{k-1},  q_k = K~ p_k,
 //   z += a_{k-2} p_{k-2} + a_{k-1} p_{k-1} on even k (the solution correction since the
 //   last fold, as in the mixed kernel), and the dot products r_k.r_k, p_k.q_k, q_k.q_k
@@ -884,13 +884,14 @@ __global__ void __launch_bounds__(BT, 1) k_dcg_iter(DcgArgs A) {
         const int4* pv = reinterpret_cast<const int4*>(spool) + (pid * A.period + (A.period == 2 ? (i & 1) : 0)) *
                                                                      (MAXW / 4);
         const double* sPi = sP + (i - wlo);
+        // (slots at and beyond the fixed width zw are padding: no FP64 FMA is spent on them)
 #pragma unroll
         for (int h = 0; h < MAXW / 4; h++) {
           const int4 x = pv[h];
-          s = fma(v[4 * h], sPi[x.x], s);
-          s = fma(v[4 * h + 1], sPi[x.y], s);
-          s = fma(v[4 * h + 2], sPi[x.z], s);
-          s = fma(v[4 * h + 3], sPi[x.w], s);
+          if (4 * h < zw) s = fma(v[4 * h], sPi[x.x], s);
+          if (4 * h + 1 < zw) s = fma(v[4 * h + 1], sPi[x.y], s);
+          if (4 * h + 2 < zw) s = fma(v[4 * h + 2], sPi[x.z], s);
+          if (4 * h + 3 < zw) s = fma(v[4 * h + 3], sPi[x.w], s);
         }
       } else {
         const int base = (i >> 5) * (32 * zw) + (i & 31);
@@ -974,10 +975,18 @@ static constexpr int kDU2W8 = 1;           // phase-2 rows per thread and trip
 
 // Plan of the banded FP64 path (after zcg_plan succeeded): FP64 window super-tiles of
 // equal size within each block's rows, and the second buffers of the r, p, q pairs.
+//
+// Measured on GB300 (Poisson, 4M DOF): 148 us per iteration against 69 + 28 + 13 us for
+// the three FP64 kernels -- the FP64 pipe, not memory, bounds both (0.70 TFLOP/s here),
+// and the fused form does more FP64 work per row (the halo rows of the two super-tiles the
+// FP64 window needs, the extra dot product of the one-step beta estimate).  So FP64
+// solves keep the three-kernel iteration, and this path is selected only with
+// ADFEM_ZCG64=1 at system creation, as the like-for-like FP64 counterpart of the mixed
+// kernel.
 int dcg_plan(Solver& S) {
   S.dcg = false;
   const char* env = std::getenv("ADFEM_ZCG64");
-  if (env && env[0] == '0') return ADFEM_OK;
+  if (!env || env[0] != '1') return ADFEM_OK;
   if (!S.zcg || S.A->maxw > 16) return ADFEM_OK;
   const size_t pool_bytes = sizeof(int32_t) * (size_t)((S.znpool + 3) & ~3);
   const int64_t room = (int64_t)((kZSmemBlock - pool_bytes) / sizeof(double)) - 2 * (int64_t)S.zH - 2;

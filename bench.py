@@ -910,33 +910,32 @@ def run_ours(args, rank, world, dist):
     ms64 = max_over_ranks(dist, ms64)
     fp64_value = replica_rate(world, args.fp64_steps, ms64 / 1000.0)
 
-    # the three-kernel FP64 iteration on the same operator (a system created with the
-    # banded FP64 path switched off)
-    os.environ["ADFEM_ZCG64"] = "0"
+    # the banded one-kernel FP64 iteration on the same operator (the like-for-like FP64
+    # counterpart of the mixed kernel; a system created with ADFEM_ZCG64=1)
+    os.environ["ADFEM_ZCG64"] = "1"
     try:
         S0 = A.PoissonSystem(mesh)
     finally:
         del os.environ["ADFEM_ZCG64"]
     S0.set_dirichlet(bd)
-    u64u = torch.zeros_like(u)
+    u64b = torch.zeros_like(u)
 
-    def step0(uu):
+    def step_banded(uu):
         S0.assemble(kappa, f)
         S0.solve(uu, precision="fp64", rtol=args.rtol_fp64)
         return S0.last_stats
 
-    step0(u64u)
+    step_banded(u64b)
     barrier()
     h0, h1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     h0.record()
-    fp64u_stats = []
+    fp64b_stats = []
     for _ in range(args.fp64_steps):
-        st = step0(u64u)
-        fp64u_stats.append((st.iterations, st.relres))
+        st = step_banded(u64b)
+        fp64b_stats.append((st.iterations, st.relres))
     h1.record()
     barrier()
-    fp64u_value = replica_rate(world, args.fp64_steps, max_over_ranks(dist, h0.elapsed_time(h1)) / 1000.0)
-    del S0
+    fp64b_value = replica_rate(world, args.fp64_steps, max_over_ranks(dist, h0.elapsed_time(h1)) / 1000.0)
 
     # ------------------------------------------------------------------ grads/s (mixed)
     from adfem_gpu import synth
@@ -987,22 +986,25 @@ def run_ours(args, rank, world, dist):
     achieved = b32 / (spmv_ms * 1e-3) / 1e9
     # the banded FP64 iteration's kernel, timed the same way (profiled FP64 solve)
     fp64_kernel = None
-    if info.get("banded_fp64"):
+    info0 = S0.solver_info()
+    if info0.get("banded_fp64"):
+        S0.assemble(kappa, f)
         kms64 = (ctypes.c_double * 4)()
         kn64 = (ctypes.c_longlong * 4)()
         o64 = A.solver_opts("fp64", args.rtol_fp64)
-        _lib.check(_lib.load().adfem_system_solve_profiled_d(S.handle, _lib.ptr(up), ctypes.byref(o64),
+        _lib.check(_lib.load().adfem_system_solve_profiled_d(S0.handle, _lib.ptr(up), ctypes.byref(o64),
                                                              ctypes.byref(pst), kms64, kn64,
                                                              _lib.stream_ptr(torch.cuda.current_stream())))
         d_ms = kms64[0] / max(kn64[0], 1)
-        b64 = dcg_bytes(info)
-        fl64 = dcg_flops(info)
+        b64 = dcg_bytes(info0)
+        fl64 = dcg_flops(info0)
         fp64_kernel = {"kernel": "k_dcg_iter", "avg_launch_ms": d_ms, "launches": int(kn64[0]),
                        "bytes_per_launch": b64, "achieved_gbs": b64 / (d_ms * 1e-3) / 1e9,
                        "hbm_frac": b64 / (d_ms * 1e-3) / 1e9 / peaks()[0],
                        "fp64_flops_per_launch": fl64, "achieved_fp64_tflops": fl64 / (d_ms * 1e-3) / 1e12,
                        "fp64_frac_of_nominal": fl64 / (d_ms * 1e-3) / 1e12 / 1.25,
-                       "tile_rows": info.get("fp64_tile_rows")}
+                       "tile_rows": info0.get("fp64_tile_rows")}
+    del S0
     # assembly phases (CUDA events inside the library): element pass, fused Laplace + load +
     # Dirichlet rows, operator conversion for the solver; median of 3
     phases = []
@@ -1067,7 +1069,7 @@ def run_ours(args, rank, world, dist):
         import scipy.sparse as sp
 
         accuracy, osys = accuracy_c3(A, S, mesh, coords, elems, kappa, f, u_ref,
-                                     {"mixed": u, "fp64": u64, "fp64_unfused": u64u})
+                                     {"mixed": u, "fp64": u64, "fp64_banded": u64b})
         fp64_iters = int(round(statistics.median([s_[0] for s_ in fp64_stats])))
         t_it = cpu_pcg_iter_s(sp.csr_matrix(osys["B"]), osys["Fb"], args.cpu_iters, 1)
         t_asm = osys["t_assembly_s"]
@@ -1095,17 +1097,17 @@ def run_ours(args, rank, world, dist):
             "fp64": {"solves_per_s": fp64_value, "rtol": args.rtol_fp64, "iters": [s[0] for s in fp64_stats],
                      "relres": fp64_stats[-1][1], "rel_err_vs_fp64_ref": err_fp64,
                      "rel_err_vs_oracle": accuracy["fp64"]["rel_err_vs_refined_reference"] if accuracy else None,
-                     "iteration": "banded one-kernel FP64 CG (k_dcg_iter): the mixed iteration's layout and "
-                                  "fusion with FP64 values, vectors and dot products" if info.get("banded_fp64")
-                                  else "three-kernel FP64 CG",
-                     "kernel": fp64_kernel,
+                     "iteration": "three-kernel FP64 CG (SpMV + p.q, update + r.r, direction): the library's "
+                                  "FP64 path and the fastest FP64 iteration here",
                      "speedup_mixed_over_fp64": value / fp64_value},
-            "fp64_unfused": {"solves_per_s": fp64u_value, "rtol": args.rtol_fp64,
-                             "iters": [s[0] for s in fp64u_stats], "relres": fp64u_stats[-1][1],
-                             "rel_err_vs_oracle": accuracy["fp64_unfused"]["rel_err_vs_refined_reference"]
-                             if accuracy else None,
-                             "iteration": "three-kernel FP64 CG (SpMV + p.q, update + r.r, direction)",
-                             "speedup_mixed_over_fp64_unfused": value / fp64u_value},
+            "fp64_banded": {"solves_per_s": fp64b_value, "rtol": args.rtol_fp64,
+                            "iters": [s[0] for s in fp64b_stats], "relres": fp64b_stats[-1][1],
+                            "rel_err_vs_oracle": accuracy["fp64_banded"]["rel_err_vs_refined_reference"]
+                            if accuracy else None,
+                            "iteration": "banded one-kernel FP64 CG (k_dcg_iter): the mixed iteration's layout "
+                                         "and fusion with FP64 values, vectors and dot products",
+                            "kernel": fp64_kernel,
+                            "speedup_mixed_over_fp64_banded": value / fp64b_value},
             "accuracy_vs_oracle": accuracy,
             "grads_per_s": grads_value,
             "dof_per_s": value * n,

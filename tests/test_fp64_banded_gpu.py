@@ -1,10 +1,10 @@
 """The two FP64 iterations of the CG solver against the direct solve and each other.
 
 * banded FP64 path (one kernel per iteration: the mixed iteration's layout and fusion with
-  FP64 values, vectors and dot products on the Jacobi-scaled operator), chosen whenever
-  the band fits;
-* three-kernel FP64 path (SpMV, update, direction), the fallback for wide bands (forced
-  with ADFEM_ZCG64=0 when the system is created).
+  FP64 values, vectors and dot products on the Jacobi-scaled operator), selected with
+  ADFEM_ZCG64=1 when the system is created (the like-for-like FP64 counterpart of the
+  mixed kernel; slower on GB300, where FP64 instructions bound both FP64 iterations);
+* three-kernel FP64 path (SpMV, update, direction), the default.
 
 The path that ran is identified by solver_info and by the launches per iteration.  Bars:
 1e-10 relative (max norm) to SuperLU on the oracle's matrices where that fits, else to the
@@ -40,9 +40,16 @@ def poisson_system(gpulib, oracle, m, contrast=1e3, seed=0):
     return S, O, kappa, f, bd
 
 
+def test_default_fp64_path_is_three_kernel(oracle, gpulib, monkeypatch):
+    monkeypatch.delenv("ADFEM_ZCG64", raising=False)
+    S, *_ = poisson_system(gpulib, oracle, 32)
+    assert S.solver_info()["banded_fp64"] == 0
+
+
 @pytest.mark.parametrize("banded", ["1", "0"])
 def test_fp64_paths_match_direct(oracle, gpulib, monkeypatch, banded):
     monkeypatch.setenv("ADFEM_ZCG64", banded)
+    monkeypatch.delenv("ADFEM_ZCG_SMAX", raising=False)
     S, O, kappa, f, bd = poisson_system(gpulib, oracle, 64)
     assert S.solver_info()["banded_fp64"] == int(banded)
     B, r = oracle.dirichlet_csc(O.laplace_csc(kappa), O.source(f), bd, np.zeros(bd.size))
@@ -59,7 +66,7 @@ def test_fp64_banded_super_tiles_deterministic(oracle, gpulib, monkeypatch):
     """361k DOF: halos across blocks, the FP64 window split into super-tiles (and forced
     into many more with ADFEM_ZCG_SMAX), bit-identical repeats, the same answer as the
     three-kernel FP64 path."""
-    monkeypatch.delenv("ADFEM_ZCG64", raising=False)
+    monkeypatch.setenv("ADFEM_ZCG64", "1")
     monkeypatch.delenv("ADFEM_ZCG_SMAX", raising=False)
     S, O, kappa, f, bd = poisson_system(gpulib, oracle, 600)
     info = S.solver_info()
@@ -88,7 +95,7 @@ def test_fp64_banded_super_tiles_deterministic(oracle, gpulib, monkeypatch):
 def test_fp64_banded_floor_and_adjoint(oracle, gpulib, monkeypatch):
     """An unattainable rtol ends at the FP64 floor with status OK; the adjoint through the
     banded FP64 path gives the gradient of the three-kernel path."""
-    monkeypatch.delenv("ADFEM_ZCG64", raising=False)
+    monkeypatch.setenv("ADFEM_ZCG64", "1")
     monkeypatch.delenv("ADFEM_ZCG_SMAX", raising=False)
     S, O, kappa, f, bd = poisson_system(gpulib, oracle, 96)
     u = S.solve(precision="fp64", rtol=1e-18, max_iter=200000)
