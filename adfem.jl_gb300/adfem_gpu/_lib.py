@@ -81,6 +81,7 @@ SIGNATURES = {
     "adfem_status_string": (ctypes.c_char_p, [c_i]),
     "adfem_last_error": (ctypes.c_char_p, []),
     "adfem_version": (ctypes.c_char_p, []),
+    "adfem_debug_fail_alloc": (c_i, [c_ll]),
     "init_nnfem_mesh": (ctypes.POINTER(c_ll), [c_p, c_i, c_p, c_i, c_i, c_i, c_i, c_p]),
     "mfem_get_ngauss": (c_i, []),
     "mfem_get_gauss": (None, [c_p, c_p]),

@@ -65,7 +65,7 @@ def build(verbose: bool = False, ptxas_info: bool = False) -> str:
         objs = list(ex.map(lambda s: _compile(s, extra), srcs))
     if (not os.path.exists(LIB)) or any(os.path.getmtime(o) > os.path.getmtime(LIB) for o in objs) or extra:
         tmp = LIB + ".tmp%d" % os.getpid()
-        cmd = [nvcc()] + ARCH + ["-shared", "-o", tmp] + objs + ["-lpthread"]
+        cmd = [nvcc()] + ARCH + ["-shared", "-o", tmp] + objs + ["-lpthread", "-ldl"]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError("link failed:\n%s\n%s" % (" ".join(cmd), r.stdout + r.stderr))

@@ -33,6 +33,21 @@ int cuda_fail(cudaError_t e, const char* what);
     if (_s != ADFEM_OK) return _s;       \
   } while (0)
 
+// NVTX range around a C-ABI call: the library's calls appear by name on an Nsight
+// timeline beside their kernels (a push/pop pair costs nanoseconds when no tool is
+// attached; nvtx3 is header-only).
+struct NvtxRange {
+  explicit NvtxRange(const char* name);
+  ~NvtxRange();
+  NvtxRange(const NvtxRange&) = delete;
+  NvtxRange& operator=(const NvtxRange&) = delete;
+};
+#define ADFEM_RANGE(name) ::adfem::NvtxRange _adfem_range_(name)
+
+// Armed by adfem_debug_fail_alloc: true when this device allocation is to fail (once).
+bool injected_alloc_failure();
+void arm_alloc_failure(long long k);
+
 // ---------------------------------------------------------------------------
 // device buffer with RAII ownership (cudaMalloc / cudaFree)
 struct DevBuf {

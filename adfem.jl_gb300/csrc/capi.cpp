@@ -10,12 +10,16 @@
 
 #include "adfem_internal.h"
 #include "dirichlet.cuh"
+#include <nvtx3/nvToolsExt.h>
 #include "elastic.cuh"
 #include "solver.cuh"
 
 using namespace adfem;
 
 namespace adfem {
+
+NvtxRange::NvtxRange(const char* name) { nvtxRangePushA(name); }
+NvtxRange::~NvtxRange() { nvtxRangePop(); }
 const char* last_error_cstr();
 }
 
@@ -184,6 +188,7 @@ const char* adfem_version(void) { return "adfem_gpu 0.1 (sm_103a)"; }
 // ------------------------------------------------------------------ meshes
 int adfem_mesh_create(const double* xyz, long long nv, const int* elems0, long long ne, int degree,
                       adfem_mesh** out) {
+  ADFEM_RANGE("adfem_mesh_create");
   if (!out) return fail(ADFEM_ERR_INVALID, "null output handle");
   *out = nullptr;
   if (degree != 1 && degree != 2) return fail(ADFEM_ERR_UNSUPPORTED, "element degree must be 1 (P1) or 2 (P2)");
@@ -200,6 +205,7 @@ int adfem_mesh_create(const double* xyz, long long nv, const int* elems0, long l
 }
 
 int adfem_mesh_destroy(adfem_mesh* mesh) {
+  ADFEM_RANGE("adfem_mesh_destroy");
   if (!mesh) return ADFEM_OK;
   {
     std::lock_guard<std::mutex> lk(g_cur_mu);
@@ -214,6 +220,7 @@ int adfem_mesh_destroy(adfem_mesh* mesh) {
 }
 
 int adfem_mesh_sizes(const adfem_mesh* mesh, long long* nv, long long* ne, long long* ngauss, long long* nnz) {
+  ADFEM_RANGE("adfem_mesh_sizes");
   if (!mesh) return fail(ADFEM_ERR_INVALID, "null mesh");
   if (nv) *nv = mesh->m->nv;
   if (ne) *ne = mesh->m->ne;
@@ -224,6 +231,7 @@ int adfem_mesh_sizes(const adfem_mesh* mesh, long long* nv, long long* ne, long 
 
 int adfem_mesh_space(const adfem_mesh* mesh, int* degree, int* elem_ndof, int* ngauss_elem, long long* ndof,
                      long long* nnz) {
+  ADFEM_RANGE("adfem_mesh_space");
   if (!mesh) return fail(ADFEM_ERR_INVALID, "null mesh");
   Mesh& m = *mesh->m;
   Space* sp = nullptr;
@@ -237,6 +245,7 @@ int adfem_mesh_space(const adfem_mesh* mesh, int* degree, int* elem_ndof, int* n
 }
 
 int adfem_mesh_connectivity(const adfem_mesh* mesh, long long* conn1) {
+  ADFEM_RANGE("adfem_mesh_connectivity");
   if (!mesh || !conn1) return fail(ADFEM_ERR_INVALID, "null argument");
   Mesh& m = *mesh->m;
   Space* sp = nullptr;
@@ -246,12 +255,14 @@ int adfem_mesh_connectivity(const adfem_mesh* mesh, long long* conn1) {
 }
 
 int adfem_mesh_gauss_weights(const adfem_mesh* mesh, double* w) {
+  ADFEM_RANGE("adfem_mesh_gauss_weights");
   if (!mesh || !w) return fail(ADFEM_ERR_INVALID, "null argument");
   mesh_gauss_weights(mesh->m, w);
   return ADFEM_OK;
 }
 
 int adfem_set_current_mesh(adfem_mesh* mesh) {
+  ADFEM_RANGE("adfem_set_current_mesh");
   std::lock_guard<std::mutex> lk(g_cur_mu);
   if (g_current && g_current_owned && g_current != mesh) {
     delete g_current->m;
@@ -267,6 +278,7 @@ adfem_mesh* adfem_current_mesh(void) {
 }
 
 int adfem_mesh_pattern(const adfem_mesh* mesh, long long* colptr1, long long* rowval1) {
+  ADFEM_RANGE("adfem_mesh_pattern");
   if (!mesh || !colptr1 || !rowval1) return fail(ADFEM_ERR_INVALID, "null argument");
   Mesh& m = *mesh->m;
   Space* sp = nullptr;
@@ -277,6 +289,7 @@ int adfem_mesh_pattern(const adfem_mesh* mesh, long long* colptr1, long long* ro
 }
 
 int adfem_mesh_pattern_elasticity(const adfem_mesh* mesh, long long* colptr1, long long* rowval1) {
+  ADFEM_RANGE("adfem_mesh_pattern_elasticity");
   if (!mesh || !colptr1 || !rowval1) return fail(ADFEM_ERR_INVALID, "null argument");
   Mesh& m = *mesh->m;
   Space* sp = nullptr;
@@ -294,12 +307,14 @@ int adfem_mesh_pattern_elasticity(const adfem_mesh* mesh, long long* colptr1, lo
 }
 
 int adfem_mesh_bcnode(const adfem_mesh* mesh, long long* out, long long* count) {
+  ADFEM_RANGE("adfem_mesh_bcnode");
   if (!mesh || !count) return fail(ADFEM_ERR_INVALID, "null argument");
   *count = mesh_bcnode(mesh->m, reinterpret_cast<int64_t*>(out));
   return ADFEM_OK;
 }
 
 int adfem_mesh_gauss_nodes(const adfem_mesh* mesh, double* x, double* y) {
+  ADFEM_RANGE("adfem_mesh_gauss_nodes");
   if (!mesh || !x || !y) return fail(ADFEM_ERR_INVALID, "null argument");
   mesh_gauss(mesh->m, x, y);
   return ADFEM_OK;
@@ -348,6 +363,7 @@ int gen_matrix_host(adfem_mesh* mesh, int which, const double* in, long long nin
 }  // namespace
 
 int adfem_mass_csr_d(adfem_mesh* mesh, const double* rho_d, double* vals_d, void* stream) {
+  ADFEM_RANGE("adfem_mass_csr_d");
   if (!mesh || !rho_d || !vals_d) return fail(ADFEM_ERR_INVALID, "null argument");
   Mesh& m = *mesh->m;
   Space* sp = nullptr;
@@ -356,11 +372,13 @@ int adfem_mass_csr_d(adfem_mesh* mesh, const double* rho_d, double* vals_d, void
 }
 
 int adfem_mass_csc(adfem_mesh* mesh, const double* rho, long long nrho, double* nzval) {
+  ADFEM_RANGE("adfem_mass_csc");
   if (!mesh || !rho || !nzval) return fail(ADFEM_ERR_INVALID, "null argument");
   return gen_matrix_host(mesh, 1, rho, nrho, nzval);
 }
 
 int adfem_mass_coo_d(adfem_mesh* mesh, const double* rho_d, long long* indices_d, double* vv_d, void* stream) {
+  ADFEM_RANGE("adfem_mass_coo_d");
   if (!mesh || !rho_d || !indices_d || !vv_d) return fail(ADFEM_ERR_INVALID, "null argument");
   Mesh& m = *mesh->m;
   Space* sp = nullptr;
@@ -369,6 +387,7 @@ int adfem_mass_coo_d(adfem_mesh* mesh, const double* rho_d, long long* indices_d
 }
 
 int adfem_mass_coo_backward_d(adfem_mesh* mesh, const double* grad_vv_d, double* grad_rho_d, void* stream) {
+  ADFEM_RANGE("adfem_mass_coo_backward_d");
   if (!mesh || !grad_vv_d || !grad_rho_d) return fail(ADFEM_ERR_INVALID, "null argument");
   Mesh& m = *mesh->m;
   Space* sp = nullptr;
@@ -400,17 +419,21 @@ static int to_gauss_backward_d(adfem_mesh* mesh, bool vertex_only, const double*
 }
 
 int adfem_fem_to_gauss_d(adfem_mesh* mesh, const double* u_d, double* out_d, void* stream) {
+  ADFEM_RANGE("adfem_fem_to_gauss_d");
   return to_gauss_d(mesh, true, u_d, out_d, stream);
 }
 int adfem_fem_to_gauss_backward_d(adfem_mesh* mesh, const double* grad_out_d, double* grad_u_d, long long nu,
                                   int accumulate, void* stream) {
+  ADFEM_RANGE("adfem_fem_to_gauss_backward_d");
   return to_gauss_backward_d(mesh, true, grad_out_d, grad_u_d, nu, accumulate, stream);
 }
 int adfem_dof_to_gauss_d(adfem_mesh* mesh, const double* u_d, double* out_d, void* stream) {
+  ADFEM_RANGE("adfem_dof_to_gauss_d");
   return to_gauss_d(mesh, false, u_d, out_d, stream);
 }
 int adfem_dof_to_gauss_backward_d(adfem_mesh* mesh, const double* grad_out_d, double* grad_u_d, long long nu,
                                   int accumulate, void* stream) {
+  ADFEM_RANGE("adfem_dof_to_gauss_backward_d");
   return to_gauss_backward_d(mesh, false, grad_out_d, grad_u_d, nu, accumulate, stream);
 }
 
@@ -428,9 +451,11 @@ static int to_gauss_host(adfem_mesh* mesh, bool vertex_only, const double* u, lo
 }
 
 int adfem_fem_to_gauss(adfem_mesh* mesh, const double* u, long long nu, double* out) {
+  ADFEM_RANGE("adfem_fem_to_gauss");
   return to_gauss_host(mesh, true, u, nu, out);
 }
 int adfem_dof_to_gauss(adfem_mesh* mesh, const double* u, long long nu, double* out) {
+  ADFEM_RANGE("adfem_dof_to_gauss");
   return to_gauss_host(mesh, false, u, nu, out);
 }
 
@@ -452,6 +477,7 @@ static int pcl_laplace_values(Mesh& m, Space& sp, DevBuf& vv, int64_t* N, cudaSt
 }
 
 int adfem_pcl_laplace_jacobian_d(adfem_mesh* mesh, double* H_d, void* stream) {
+  ADFEM_RANGE("adfem_pcl_laplace_jacobian_d");
   if (!mesh || !H_d) return fail(ADFEM_ERR_INVALID, "null argument");
   Mesh& m = *mesh->m;
   Space* sp = nullptr;
@@ -465,6 +491,7 @@ int adfem_pcl_laplace_jacobian_d(adfem_mesh* mesh, double* H_d, void* stream) {
 }
 
 int adfem_pcl_laplace_jacobian(adfem_mesh* mesh, double* H) {
+  ADFEM_RANGE("adfem_pcl_laplace_jacobian");
   if (!mesh || !H) return fail(ADFEM_ERR_INVALID, "null argument");
   Mesh& m = *mesh->m;
   Space* sp = nullptr;
@@ -481,6 +508,7 @@ int adfem_pcl_laplace_jacobian(adfem_mesh* mesh, double* H) {
 
 int adfem_pcl_dirichlet(const long long* indices, long long sN, const long long* bd, long long nbd, long long N,
                         long long* pos, long long* nkeep) {
+  ADFEM_RANGE("adfem_pcl_dirichlet");
   if (sN < 0 || N < 0 || !nkeep || (sN > 0 && (!indices || !pos)) || (nbd > 0 && !bd))
     return fail(ADFEM_ERR_INVALID, "bad arguments");
   std::vector<uint8_t> tag(std::max<long long>(N, 1), 0);
@@ -499,18 +527,21 @@ int adfem_pcl_dirichlet(const long long* indices, long long sN, const long long*
 }
 
 int adfem_mesh_elements(const adfem_mesh* mesh, long long* elems1) {
+  ADFEM_RANGE("adfem_mesh_elements");
   if (!mesh || !elems1) return fail(ADFEM_ERR_INVALID, "null argument");
   for (int64_t k = 0; k < 3 * mesh->m->ne; k++) elems1[k] = (long long)mesh->m->elem[k] + 1;
   return ADFEM_OK;
 }
 
 int adfem_mesh_area(const adfem_mesh* mesh, double* area) {
+  ADFEM_RANGE("adfem_mesh_area");
   if (!mesh || !area) return fail(ADFEM_ERR_INVALID, "null argument");
   std::memcpy(area, mesh->m->area.data(), sizeof(double) * mesh->m->ne);
   return ADFEM_OK;
 }
 
 int adfem_mesh_edges(const adfem_mesh* mesh, long long* out, long long* nedges) {
+  ADFEM_RANGE("adfem_mesh_edges");
   if (!mesh || !nedges) return fail(ADFEM_ERR_INVALID, "null argument");
   ADFEM_TRY(mesh_edges(mesh->m));
   *nedges = mesh->m->nedges;
@@ -520,6 +551,7 @@ int adfem_mesh_edges(const adfem_mesh* mesh, long long* out, long long* nedges) 
 
 // ------------------------------------------------------------------ Laplace
 int adfem_laplace_csr_d(adfem_mesh* mesh, const double* kappa_d, double* vals_d, void* stream) {
+  ADFEM_RANGE("adfem_laplace_csr_d");
   if (!mesh || !kappa_d || !vals_d) return fail(ADFEM_ERR_INVALID, "null argument");
   Mesh& m = *mesh->m;
   if (Space* sp = p2_space(m)) return gen_matrix_d(m, *sp, GenOp::LAPLACE, kappa_d, vals_d, false, S(stream));
@@ -532,6 +564,7 @@ int adfem_laplace_csr_d(adfem_mesh* mesh, const double* kappa_d, double* vals_d,
 }
 
 int adfem_laplace_csc(adfem_mesh* mesh, const double* kappa, long long nkappa, double* nzval) {
+  ADFEM_RANGE("adfem_laplace_csc");
   if (!mesh || !kappa || !nzval) return fail(ADFEM_ERR_INVALID, "null argument");
   Mesh& m = *mesh->m;
   if (m.degree == 2) return gen_matrix_host(mesh, 0, kappa, nkappa, nzval);
@@ -544,6 +577,7 @@ int adfem_laplace_csc(adfem_mesh* mesh, const double* kappa, long long nkappa, d
 }
 
 int adfem_laplace_coo_d(adfem_mesh* mesh, const double* kappa_d, long long* indices_d, double* vv_d, void* stream) {
+  ADFEM_RANGE("adfem_laplace_coo_d");
   if (!mesh || !kappa_d || !indices_d || !vv_d) return fail(ADFEM_ERR_INVALID, "null argument");
   if (Space* sp = p2_space(*mesh->m))
     return kerr(launch_gen_coo(*mesh->m, *sp, GenOp::LAPLACE, kappa_d, indices_d, vv_d, S(stream)), "laplace coo");
@@ -552,6 +586,7 @@ int adfem_laplace_coo_d(adfem_mesh* mesh, const double* kappa_d, long long* indi
 }
 
 int adfem_laplace_coo_backward_d(adfem_mesh* mesh, const double* grad_vv_d, double* grad_kappa_d, void* stream) {
+  ADFEM_RANGE("adfem_laplace_coo_backward_d");
   if (!mesh || !grad_vv_d || !grad_kappa_d) return fail(ADFEM_ERR_INVALID, "null argument");
   if (Space* sp = p2_space(*mesh->m))
     return kerr(launch_gen_coo_backward(*mesh->m, *sp, GenOp::LAPLACE, grad_vv_d, grad_kappa_d, S(stream)),
@@ -562,6 +597,7 @@ int adfem_laplace_coo_backward_d(adfem_mesh* mesh, const double* grad_vv_d, doub
 
 // ------------------------------------------------------------------ source
 int adfem_source_d(adfem_mesh* mesh, const double* f_d, double* rhs_d, int accumulate, void* stream) {
+  ADFEM_RANGE("adfem_source_d");
   if (!mesh || !f_d || !rhs_d) return fail(ADFEM_ERR_INVALID, "null argument");
   Mesh& m = *mesh->m;
   if (Space* sp = p2_space(m)) {
@@ -578,6 +614,7 @@ int adfem_source_d(adfem_mesh* mesh, const double* f_d, double* rhs_d, int accum
 }
 
 int adfem_source(adfem_mesh* mesh, const double* f, long long nf, double* rhs, int accumulate) {
+  ADFEM_RANGE("adfem_source");
   if (!mesh || !f || !rhs) return fail(ADFEM_ERR_INVALID, "null argument");
   Mesh& m = *mesh->m;
   if (nf != mesh_ngauss(m)) return fail(ADFEM_ERR_INVALID, "f must have one value per Gauss point");
@@ -591,6 +628,7 @@ int adfem_source(adfem_mesh* mesh, const double* f, long long nf, double* rhs, i
 }
 
 int adfem_source_backward_d(adfem_mesh* mesh, const double* grad_rhs_d, double* grad_f_d, void* stream) {
+  ADFEM_RANGE("adfem_source_backward_d");
   if (!mesh || !grad_rhs_d || !grad_f_d) return fail(ADFEM_ERR_INVALID, "null argument");
   if (Space* sp = p2_space(*mesh->m))
     return kerr(launch_gen_source_backward(*mesh->m, *sp, grad_rhs_d, grad_f_d, S(stream)), "source backward");
@@ -600,6 +638,7 @@ int adfem_source_backward_d(adfem_mesh* mesh, const double* grad_rhs_d, double* 
 
 // ------------------------------------------------------------------ stiffness
 int adfem_stiffness_csr_d(adfem_mesh* mesh, const double* D_d, double* vals_d, void* stream) {
+  ADFEM_RANGE("adfem_stiffness_csr_d");
   if (!mesh || !D_d || !vals_d) return fail(ADFEM_ERR_INVALID, "null argument");
   Mesh& m = *mesh->m;
   if (Space* sp = p2_space(m)) return gen_stiffness_d(m, *sp, D_d, vals_d, false, S(stream));
@@ -612,6 +651,7 @@ int adfem_stiffness_csr_d(adfem_mesh* mesh, const double* D_d, double* vals_d, v
 }
 
 int adfem_stiffness_csc(adfem_mesh* mesh, const double* D, long long nD, double* nzval) {
+  ADFEM_RANGE("adfem_stiffness_csc");
   if (!mesh || !D || !nzval) return fail(ADFEM_ERR_INVALID, "null argument");
   Mesh& m = *mesh->m;
   if (m.degree == 2) return gen_matrix_host(mesh, 2, D, nD, nzval);
@@ -629,6 +669,7 @@ int adfem_stiffness_csc(adfem_mesh* mesh, const double* D, long long nD, double*
 }
 
 int adfem_stiffness_coo_d(adfem_mesh* mesh, const double* D_d, long long* indices_d, double* vv_d, void* stream) {
+  ADFEM_RANGE("adfem_stiffness_coo_d");
   if (!mesh || !D_d || !indices_d || !vv_d) return fail(ADFEM_ERR_INVALID, "null argument");
   if (Space* sp = p2_space(*mesh->m))
     return kerr(launch_gen_stiffness_coo(*mesh->m, *sp, D_d, indices_d, vv_d, S(stream)), "stiffness coo");
@@ -637,6 +678,7 @@ int adfem_stiffness_coo_d(adfem_mesh* mesh, const double* D_d, long long* indice
 }
 
 int adfem_stiffness_coo_backward_d(adfem_mesh* mesh, const double* grad_vv_d, double* grad_D_d, void* stream) {
+  ADFEM_RANGE("adfem_stiffness_coo_backward_d");
   if (!mesh || !grad_vv_d || !grad_D_d) return fail(ADFEM_ERR_INVALID, "null argument");
   if (Space* sp = p2_space(*mesh->m))
     return kerr(launch_gen_stiffness_coo_backward(*mesh->m, *sp, grad_vv_d, grad_D_d, S(stream)),
@@ -646,6 +688,7 @@ int adfem_stiffness_coo_backward_d(adfem_mesh* mesh, const double* grad_vv_d, do
 }
 
 int adfem_plane_strain_d(int mode, long long n, const double* E_d, const double* nu_d, double* D_d, void* stream) {
+  ADFEM_RANGE("adfem_plane_strain_d");
   if (mode != 0 && mode != 1) return fail(ADFEM_ERR_INVALID, "mode must be 0 (plane strain) or 1 (plane stress)");
   if (n < 0 || (n > 0 && (!E_d || !nu_d || !D_d))) return fail(ADFEM_ERR_INVALID, "bad arguments");
   if (n == 0) return ADFEM_OK;
@@ -655,6 +698,7 @@ int adfem_plane_strain_d(int mode, long long n, const double* E_d, const double*
 
 int adfem_plane_strain_backward_d(int mode, long long n, const double* g_d, const double* E_d, const double* nu_d,
                                   double* gE_d, double* gnu_d, void* stream) {
+  ADFEM_RANGE("adfem_plane_strain_backward_d");
   if (mode != 0 && mode != 1) return fail(ADFEM_ERR_INVALID, "mode must be 0 (plane strain) or 1 (plane stress)");
   if (n < 0 || (n > 0 && (!g_d || !E_d || !nu_d || !gE_d || !gnu_d))) return fail(ADFEM_ERR_INVALID, "bad arguments");
   if (n == 0) return ADFEM_OK;
@@ -679,6 +723,7 @@ int adfem_dirichlet_csc(long long n, const long long* colptr1, const long long* 
                         const double* rhs, const long long* bd, long long nbd, const double* bdval, int keep_zeros,
                         long long* out_colptr1, long long* out_rowval1, double* out_nzval, long long* out_nnz,
                         double* out_rhs) {
+  ADFEM_RANGE("adfem_dirichlet_csc");
   if (n < 0 || !colptr1 || !out_nnz || (nbd > 0 && (!bd || !bdval))) return fail(ADFEM_ERR_INVALID, "bad arguments");
   const int64_t nnz = colptr1[n] - 1;
   if (nnz < 0 || (nnz > 0 && (!rowval1 || !nzval))) return fail(ADFEM_ERR_INVALID, "bad CSC arrays");
@@ -742,6 +787,7 @@ static void bd_unique(const long long* bd, long long nbd, std::vector<std::pair<
 int adfem_dirichlet_coo(const long long* indices, const double* vv, long long sN, const long long* bd, long long nbd,
                         const double* rhs, const double* bdval, long long N, long long* oindices, double* ov,
                         double* orhs, long long* out_n) {
+  ADFEM_RANGE("adfem_dirichlet_coo");
   if (sN < 0 || N < 0 || !out_n || (sN > 0 && (!indices || !vv)) || (nbd > 0 && (!bd || !bdval)))
     return fail(ADFEM_ERR_INVALID, "bad arguments");
   std::vector<std::pair<int64_t, int64_t>> u;
@@ -788,6 +834,7 @@ int adfem_dirichlet_coo_backward(const double* grad_vv, const double* grad_rhs, 
                                  const double* vv, long long sN, const long long* bd, long long nbd,
                                  const double* bdval, long long N, double* grad_vv_in, double* grad_rhs_in,
                                  double* grad_bdval) {
+  ADFEM_RANGE("adfem_dirichlet_coo_backward");
   if (sN < 0 || N < 0 || (sN > 0 && (!indices || !vv || !grad_vv_in)) || !grad_rhs || !grad_rhs_in ||
       (nbd > 0 && (!bd || !bdval || !grad_bdval)))
     return fail(ADFEM_ERR_INVALID, "bad arguments");
@@ -903,6 +950,7 @@ static int check_symmetric(int64_t n, const std::vector<int32_t>& rp, const std:
 
 int adfem_csc_solve(long long n, const long long* colptr1, const long long* rowval1, const double* nzval,
                     const double* rhs, double* u, const adfem_solver_opts* opts, adfem_solver_stats* stats) {
+  ADFEM_RANGE("adfem_csc_solve");
   if (n <= 0 || !colptr1 || !rowval1 || !nzval || !rhs || !u) return fail(ADFEM_ERR_INVALID, "bad arguments");
   if (n > INT32_MAX) return fail(ADFEM_ERR_UNSUPPORTED, "n > 2^31");
   adfem_solver_opts o;
@@ -953,6 +1001,7 @@ int adfem_csc_solve(long long n, const long long* colptr1, const long long* rowv
 
 // ------------------------------------------------------------------ systems
 int adfem_system_create(adfem_mesh* mesh, int kind, adfem_system** out) {
+  ADFEM_RANGE("adfem_system_create");
   if (!mesh || !out) return fail(ADFEM_ERR_INVALID, "null argument");
   if (kind != ADFEM_SYS_POISSON && kind != ADFEM_SYS_ELASTICITY) return fail(ADFEM_ERR_INVALID, "unknown kind");
   *out = nullptr;
@@ -1053,11 +1102,13 @@ int adfem_system_create(adfem_mesh* mesh, int kind, adfem_system** out) {
 }
 
 int adfem_system_destroy(adfem_system* sys) {
+  ADFEM_RANGE("adfem_system_destroy");
   delete sys;
   return ADFEM_OK;
 }
 
 int adfem_system_set_dirichlet(adfem_system* sys, const long long* bd, long long nbd, const double* bdval) {
+  ADFEM_RANGE("adfem_system_set_dirichlet");
   if (!sys || nbd < 0 || (nbd > 0 && !bd)) return fail(ADFEM_ERR_INVALID, "bad arguments");
   std::lock_guard<std::mutex> lk(sys->mu);
   return system_set_bd(sys, bd, nbd, bdval);
@@ -1090,6 +1141,7 @@ static int assemble_poisson(adfem_system* sys, const double* kappa_d, const doub
 }
 
 int adfem_system_assemble_poisson_d(adfem_system* sys, const double* kappa_d, const double* f_d, void* stream) {
+  ADFEM_RANGE("adfem_system_assemble_poisson_d");
   if (!sys || !kappa_d || !f_d) return fail(ADFEM_ERR_INVALID, "null argument");
   if (sys->kind != ADFEM_SYS_POISSON) return fail(ADFEM_ERR_INVALID, "not a Poisson system");
   std::lock_guard<std::mutex> lk(sys->mu);
@@ -1098,6 +1150,7 @@ int adfem_system_assemble_poisson_d(adfem_system* sys, const double* kappa_d, co
 
 int adfem_system_assemble_poisson_profiled_d(adfem_system* sys, const double* kappa_d, const double* f_d, double* ms,
                                              void* stream) {
+  ADFEM_RANGE("adfem_system_assemble_poisson_profiled_d");
   if (!sys || !kappa_d || !f_d || !ms) return fail(ADFEM_ERR_INVALID, "null argument");
   if (sys->kind != ADFEM_SYS_POISSON) return fail(ADFEM_ERR_INVALID, "not a Poisson system");
   std::lock_guard<std::mutex> lk(sys->mu);
@@ -1118,6 +1171,7 @@ int adfem_system_assemble_poisson_profiled_d(adfem_system* sys, const double* ka
 
 int adfem_system_assemble_elasticity_d(adfem_system* sys, const double* E_d, const double* nu_d, const double* fx_d,
                                        const double* fy_d, void* stream) {
+  ADFEM_RANGE("adfem_system_assemble_elasticity_d");
   if (!sys || !E_d || !nu_d || !fx_d || !fy_d) return fail(ADFEM_ERR_INVALID, "null argument");
   if (sys->kind != ADFEM_SYS_ELASTICITY) return fail(ADFEM_ERR_INVALID, "not an elasticity system");
   std::lock_guard<std::mutex> lk(sys->mu);
@@ -1143,6 +1197,7 @@ int adfem_system_assemble_elasticity_d(adfem_system* sys, const double* E_d, con
 
 int adfem_system_solve_d(adfem_system* sys, double* u_d, const adfem_solver_opts* opts, adfem_solver_stats* stats,
                          void* stream) {
+  ADFEM_RANGE("adfem_system_solve_d");
   if (!sys || !u_d) return fail(ADFEM_ERR_INVALID, "null argument");
   std::lock_guard<std::mutex> lk(sys->mu);
   if (!sys->assembled) return fail(ADFEM_ERR_INVALID, "system not assembled");
@@ -1163,6 +1218,7 @@ int adfem_system_solve_d(adfem_system* sys, double* u_d, const adfem_solver_opts
 
 int adfem_system_solve_profiled_d(adfem_system* sys, double* u_d, const adfem_solver_opts* opts,
                                   adfem_solver_stats* stats, double* kernel_ms, long long* launches, void* stream) {
+  ADFEM_RANGE("adfem_system_solve_profiled_d");
   if (!sys || !u_d || !kernel_ms || !launches) return fail(ADFEM_ERR_INVALID, "null argument");
   if (sys->kind != ADFEM_SYS_POISSON) return fail(ADFEM_ERR_UNSUPPORTED, "profiled solves are for Poisson systems");
   std::lock_guard<std::mutex> lk(sys->mu);
@@ -1181,6 +1237,7 @@ int adfem_system_solve_profiled_d(adfem_system* sys, double* u_d, const adfem_so
 }
 
 int adfem_system_solver_info(const adfem_system* sys, adfem_solver_info* info) {
+  ADFEM_RANGE("adfem_system_solver_info");
   if (!sys || !info) return fail(ADFEM_ERR_INVALID, "null argument");
   const Sell& A = sys->A;
   const Solver& sv = sys->solver;
@@ -1271,16 +1328,19 @@ extern "C" {
 
 int adfem_system_solve_packed_d(adfem_system** sys, int count, double** u_d, const adfem_solver_opts* opts,
                                 adfem_solver_stats* stats, void* stream) {
+  ADFEM_RANGE("adfem_system_solve_packed_d");
   return system_solve_packed(sys, count, u_d, nullptr, opts, stats, stream, false, nullptr);
 }
 
 int adfem_system_adjoint_packed_d(adfem_system** sys, int count, const double* const* g_d, double** lam_d,
                                   const adfem_solver_opts* opts, adfem_solver_stats* stats, void* stream) {
+  ADFEM_RANGE("adfem_system_adjoint_packed_d");
   return system_solve_packed(sys, count, lam_d, g_d, opts, stats, stream, true, nullptr);
 }
 
 int adfem_system_adjoint_d(adfem_system* sys, const double* g_d, double* lam_d, const adfem_solver_opts* opts,
                            adfem_solver_stats* stats, void* stream) {
+  ADFEM_RANGE("adfem_system_adjoint_d");
   if (!sys || !g_d || !lam_d) return fail(ADFEM_ERR_INVALID, "null argument");
   std::lock_guard<std::mutex> lk(sys->mu);
   if (!sys->assembled) return fail(ADFEM_ERR_INVALID, "system not assembled");
@@ -1302,6 +1362,7 @@ int adfem_system_adjoint_d(adfem_system* sys, const double* g_d, double* lam_d, 
 
 int adfem_system_grad_kappa_d(adfem_system* sys, const double* u_d, const double* lam_d, double* grad_kappa_d,
                               void* stream) {
+  ADFEM_RANGE("adfem_system_grad_kappa_d");
   if (!sys || !u_d || !lam_d || !grad_kappa_d) return fail(ADFEM_ERR_INVALID, "null argument");
   if (sys->kind != ADFEM_SYS_POISSON) return fail(ADFEM_ERR_INVALID, "not a Poisson system");
   ADFEM_TRY(kerr(launch_poisson_kappa_grad(*sys->mesh->m, u_d, lam_d, sys->isbd_ref.as<uint8_t>(), grad_kappa_d,
@@ -1327,6 +1388,7 @@ int adfem_system_grad_E_d(adfem_system* sys, const double* u_d, const double* la
 }
 
 int adfem_system_apply_d(adfem_system* sys, const double* x_d, double* y_d, void* stream) {
+  ADFEM_RANGE("adfem_system_apply_d");
   if (!sys || !x_d || !y_d) return fail(ADFEM_ERR_INVALID, "null argument");
   std::lock_guard<std::mutex> lk(sys->mu);
   if (!sys->assembled) return fail(ADFEM_ERR_INVALID, "system not assembled");
@@ -1339,6 +1401,7 @@ int adfem_system_apply_d(adfem_system* sys, const double* x_d, double* y_d, void
 }
 
 int adfem_system_rhs_d(adfem_system* sys, double* rhs_d, void* stream) {
+  ADFEM_RANGE("adfem_system_rhs_d");
   if (!sys || !rhs_d) return fail(ADFEM_ERR_INVALID, "null argument");
   std::lock_guard<std::mutex> lk(sys->mu);
   if (!sys->assembled) return fail(ADFEM_ERR_INVALID, "system not assembled");
@@ -1352,6 +1415,7 @@ int adfem_system_rhs_d(adfem_system* sys, double* rhs_d, void* stream) {
 
 int adfem_poisson_solve(adfem_system* sys, const double* kappa, const double* f, double* u,
                         const adfem_solver_opts* opts, adfem_solver_stats* stats) {
+  ADFEM_RANGE("adfem_poisson_solve");
   if (!sys || !kappa || !f || !u) return fail(ADFEM_ERR_INVALID, "null argument");
   if (sys->kind != ADFEM_SYS_POISSON) return fail(ADFEM_ERR_INVALID, "not a Poisson system");
   Mesh& m = *sys->mesh->m;
@@ -1371,6 +1435,7 @@ int adfem_poisson_solve(adfem_system* sys, const double* kappa, const double* f,
 // ================================================================== legacy layer
 long long* init_nnfem_mesh(double* vertices, int num_vertices, int* element_indices, int num_elements, int order,
                            int lorder, int degree, long long* nedges) {
+  ADFEM_RANGE("init_nnfem_mesh");
   (void)lorder;
   const bool ok = (degree == 1 && (order == 2 || order == -1)) || (degree == 2 && (order == 4 || order == -1));
   if (!ok) {
@@ -1412,35 +1477,43 @@ long long* init_nnfem_mesh(double* vertices, int num_vertices, int* element_indi
   }
 
 int mfem_get_ngauss(void) {
+  ADFEM_RANGE("mfem_get_ngauss");
   LEGACY_MESH("mfem_get_ngauss", 0);
   return (int)mesh_ngauss(*m);
 }
 void mfem_get_gauss(double* x, double* y) {
+  ADFEM_RANGE("mfem_get_gauss");
   LEGACY_MESH("mfem_get_gauss", );
   mesh_gauss(m, x, y);
 }
 void mfem_get_gauss_weights(double* w) {
+  ADFEM_RANGE("mfem_get_gauss_weights");
   LEGACY_MESH("mfem_get_gauss_weights", );
   mesh_gauss_weights(m, w);
 }
 void mfem_get_area(double* a) {
+  ADFEM_RANGE("mfem_get_area");
   LEGACY_MESH("mfem_get_area", );
   for (int64_t e = 0; e < m->ne; e++) a[e] = m->area[e];
 }
 int mfem_get_elem_ndof(void) {
+  ADFEM_RANGE("mfem_get_elem_ndof");
   LEGACY_MESH("mfem_get_elem_ndof", 0);
   return m->degree == 2 ? 6 : 3;
 }
 int mfem_get_ndof(void) {
+  ADFEM_RANGE("mfem_get_ndof");
   LEGACY_MESH("mfem_get_ndof", 0);
   return (int)mesh_ndof(m);
 }
 void mfem_get_connectivity(long long* conn) {
+  ADFEM_RANGE("mfem_get_connectivity");
   LEGACY_MESH("mfem_get_connectivity", );
   adfem_mesh h{m};
   legacy_report(adfem_mesh_connectivity(&h, conn), "mfem_get_connectivity");
 }
 void mfem_get_element_to_vertices(long long* elems) {
+  ADFEM_RANGE("mfem_get_element_to_vertices");
   LEGACY_MESH("mfem_get_element_to_vertices", );
   for (int64_t e = 0; e < m->ne; e++)
     for (int k = 0; k < 3; k++) elems[k * m->ne + e] = (long long)m->elem[3 * e + k] + 1;
@@ -1462,11 +1535,13 @@ static int legacy_laplace_coo(Mesh* m, long long* indices, double* vv, const dou
 }
 
 void FemLaplaceScalar_forward_Julia(long long* indices, double* vv, const double* kappa) {
+  ADFEM_RANGE("FemLaplaceScalar_forward_Julia");
   LEGACY_MESH("FemLaplaceScalar_forward_Julia", );
   legacy_report(legacy_laplace_coo(m, indices, vv, kappa), "FemLaplaceScalar_forward_Julia");
 }
 
 void FemSourceScalar_forward_Julia(double* rhs, const double* f) {
+  ADFEM_RANGE("FemSourceScalar_forward_Julia");
   LEGACY_MESH("FemSourceScalar_forward_Julia", );
   adfem_mesh h{m};
   legacy_report(adfem_source(&h, f, mesh_ngauss(*m), rhs, 1), "FemSourceScalar_forward_Julia");
@@ -1485,6 +1560,7 @@ static int legacy_stiffness_coo(Mesh* m, long long* indices, double* vv, const d
 }
 
 void ComputeFemStiffnessMatrixMfem_forward_Julia(long long* indices, double* vv, const double* hmat) {
+  ADFEM_RANGE("ComputeFemStiffnessMatrixMfem_forward_Julia");
   LEGACY_MESH("ComputeFemStiffnessMatrixMfem_forward_Julia", );
   legacy_report(legacy_stiffness_coo(m, indices, vv, hmat), "ComputeFemStiffnessMatrixMfem_forward_Julia");
 }
@@ -1501,6 +1577,7 @@ static int legacy_laplace_backward(Mesh* m, double* grad_kappa, const double* gr
 
 void FemLaplaceScalar_backward(double* grad_kappa, const double* grad_vv, const long long* indices, const double* vv,
                                const double* kappa) {
+  ADFEM_RANGE("FemLaplaceScalar_backward");
   (void)indices;
   (void)vv;
   (void)kappa;
@@ -1519,6 +1596,7 @@ static int legacy_source_backward(Mesh* m, double* grad_f, const double* grad_rh
 }
 
 void FemSourceScalar_backward(double* grad_f, const double* grad_rhs, const double* rhs, const double* f) {
+  ADFEM_RANGE("FemSourceScalar_backward");
   (void)rhs;
   (void)f;
   LEGACY_MESH("FemSourceScalar_backward", );
@@ -1536,6 +1614,7 @@ static int legacy_stiffness_backward(Mesh* m, double* grad_hmat, const double* g
 }
 
 void ComputeFemStiffnessMatrixMfem_backward(double* grad_hmat, const double* grad_vv) {
+  ADFEM_RANGE("ComputeFemStiffnessMatrixMfem_backward");
   LEGACY_MESH("ComputeFemStiffnessMatrixMfem_backward", );
   legacy_report(legacy_stiffness_backward(m, grad_hmat, grad_vv), "ComputeFemStiffnessMatrixMfem_backward");
 }
@@ -1554,6 +1633,7 @@ static int legacy_mass_coo(Mesh* m, long long* indices, double* vv, const double
 }
 
 void ComputeFemMassMatrix1_forward(long long* indices, double* vv, const double* rho) {
+  ADFEM_RANGE("ComputeFemMassMatrix1_forward");
   LEGACY_MESH("ComputeFemMassMatrix1_forward", );
   legacy_report(legacy_mass_coo(m, indices, vv, rho), "ComputeFemMassMatrix1_forward");
 }
@@ -1569,6 +1649,7 @@ static int legacy_mass_backward(Mesh* m, double* grad_rho, const double* grad_vv
 }
 
 void ComputeFemMassMatrix1_backward(double* grad_rho, const double* grad_vv, const double* vv, const double* rho) {
+  ADFEM_RANGE("ComputeFemMassMatrix1_backward");
   (void)vv;
   (void)rho;
   LEGACY_MESH("ComputeFemMassMatrix1_backward", );
@@ -1599,28 +1680,34 @@ static int legacy_to_gauss_backward(Mesh* m, bool vertex_only, double* grad_u, c
 }
 
 void FemToGaussPointsMfem_Julia(double* out, const double* u) {
+  ADFEM_RANGE("FemToGaussPointsMfem_Julia");
   LEGACY_MESH("FemToGaussPointsMfem_Julia", );
   legacy_report(legacy_to_gauss(m, true, out, u), "FemToGaussPointsMfem_Julia");
 }
 void FemToGaussPointsMfem_forward(double* out, const double* u) {
+  ADFEM_RANGE("FemToGaussPointsMfem_forward");
   LEGACY_MESH("FemToGaussPointsMfem_forward", );
   legacy_report(legacy_to_gauss(m, true, out, u), "FemToGaussPointsMfem_forward");
 }
 void FemToGaussPointsMfem_backward(double* grad_u, const double* grad_out, const double* out, const double* u) {
+  ADFEM_RANGE("FemToGaussPointsMfem_backward");
   (void)out;
   (void)u;
   LEGACY_MESH("FemToGaussPointsMfem_backward", );
   legacy_report(legacy_to_gauss_backward(m, true, grad_u, grad_out), "FemToGaussPointsMfem_backward");
 }
 void DofToGaussPointsMfem_forward_Julia(double* out, const double* u) {
+  ADFEM_RANGE("DofToGaussPointsMfem_forward_Julia");
   LEGACY_MESH("DofToGaussPointsMfem_forward_Julia", );
   legacy_report(legacy_to_gauss(m, false, out, u), "DofToGaussPointsMfem_forward_Julia");
 }
 void DofToGaussPointsMfem_forward(double* out, const double* u) {
+  ADFEM_RANGE("DofToGaussPointsMfem_forward");
   LEGACY_MESH("DofToGaussPointsMfem_forward", );
   legacy_report(legacy_to_gauss(m, false, out, u), "DofToGaussPointsMfem_forward");
 }
 void DofToGaussPointsMfem_backward(double* grad_u, const double* grad_out, const double* out, const double* u) {
+  ADFEM_RANGE("DofToGaussPointsMfem_backward");
   (void)out;
   (void)u;
   LEGACY_MESH("DofToGaussPointsMfem_backward", );
@@ -1630,6 +1717,7 @@ void DofToGaussPointsMfem_backward(double* grad_u, const double* grad_out, const
 // pcl_FemLaplaceScalar_Jacobian (FemLaplaceScalar.h:63-91, caller src/pcl.jl:34-38): H is
 // the caller's zeroed ngauss x elem_ndof^2 ngauss column-major matrix
 void pcl_FemLaplaceScalar_Jacobian(double* H) {
+  ADFEM_RANGE("pcl_FemLaplaceScalar_Jacobian");
   LEGACY_MESH("pcl_FemLaplaceScalar_Jacobian", );
   adfem_mesh h{m};
   legacy_report(adfem_pcl_laplace_jacobian(&h, H), "pcl_FemLaplaceScalar_Jacobian");
@@ -1658,6 +1746,7 @@ static int legacy_pcl_dirichlet(double* J, const long long* indices, const long 
 }
 
 void pcl_ImposeDirichlet(double* J, const long long* indices, const long long* bd, int bdN, int sN) {
+  ADFEM_RANGE("pcl_ImposeDirichlet");
   legacy_report(legacy_pcl_dirichlet(J, indices, bd, bdN, sN), "pcl_ImposeDirichlet");
 }
 
@@ -1687,17 +1776,21 @@ static int host_plane_bwd(int mode, const double* g, const double* E, const doub
 }
 
 void PlaneStrainMatrix_forward(double* out, const double* E, const double* nu, int N) {
+  ADFEM_RANGE("PlaneStrainMatrix_forward");
   legacy_report(host_plane(0, E, nu, N, out), "PlaneStrainMatrix_forward");
 }
 void PlaneStrainMatrix_backward(double* grad_nu, double* grad_E, const double* grad_out, const double* E,
                                 const double* nu, int N) {
+  ADFEM_RANGE("PlaneStrainMatrix_backward");
   legacy_report(host_plane_bwd(0, grad_out, E, nu, N, grad_E, grad_nu), "PlaneStrainMatrix_backward");
 }
 void PlaneStressMatrix_forward(double* out, const double* E, const double* nu, int N) {
+  ADFEM_RANGE("PlaneStressMatrix_forward");
   legacy_report(host_plane(1, E, nu, N, out), "PlaneStressMatrix_forward");
 }
 void PlaneStressMatrix_backward(double* grad_nu, double* grad_E, const double* grad_out, const double* E,
                                 const double* nu, int N) {
+  ADFEM_RANGE("PlaneStressMatrix_backward");
   legacy_report(host_plane_bwd(1, grad_out, E, nu, N, grad_E, grad_nu), "PlaneStressMatrix_backward");
 }
 

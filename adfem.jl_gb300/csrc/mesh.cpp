@@ -3,6 +3,7 @@
 // node->element incidence, the scalar CSR pattern, per-incidence slot offsets
 // and the sliced-ELL copy of the pattern.  Everything here runs once per mesh on
 // the host (threaded), then is uploaded; the per-call work is on the device.
+#include <atomic>
 #include <algorithm>
 #include <cmath>
 #include <cstring>
@@ -39,10 +40,23 @@ void DevBuf::release() {
   bytes = 0;
 }
 
+static std::atomic<long long> g_alloc_fail_countdown{-1};
+
+bool injected_alloc_failure() {
+  long long c = g_alloc_fail_countdown.load();
+  while (c >= 0) {
+    if (g_alloc_fail_countdown.compare_exchange_weak(c, c - 1)) return c == 0;
+  }
+  return false;
+}
+
+void arm_alloc_failure(long long k) { g_alloc_fail_countdown.store(k < 0 ? -1 : k); }
+
 int DevBuf::alloc(size_t nb) {
   if (p && nb <= bytes) return ADFEM_OK;
   release();
   if (nb == 0) return ADFEM_OK;
+  if (injected_alloc_failure()) return cuda_fail(cudaErrorMemoryAllocation, "cudaMalloc (injected failure)");
   std::lock_guard<std::mutex> lk(device_alloc_mutex());
   cudaError_t e = cudaMalloc(&p, nb);
   if (e != cudaSuccess) {
@@ -656,3 +670,8 @@ int mesh_space(Mesh* m, int degree, Space** out) {
 }
 
 }  // namespace adfem
+
+int adfem_debug_fail_alloc(long long k) {
+  adfem::arm_alloc_failure(k);
+  return ADFEM_OK;
+}

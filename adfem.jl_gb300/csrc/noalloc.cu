@@ -227,6 +227,7 @@ using namespace adfem;
 extern "C" int adfem_csr_pcg_noalloc_d(int n, const int* rowptr_d, const int* colind_d, const double* vals_d,
                                        const double* rhs_d, double* u_d, double rtol, int max_iter,
                                        int* iterations, double* relres, void* stream) {
+  ADFEM_RANGE("adfem_csr_pcg_noalloc_d");
   if (n <= 0 || !rowptr_d || !colind_d || !vals_d || !rhs_d || !u_d)
     return fail(ADFEM_ERR_INVALID, "csr_pcg_noalloc: null pointer or n <= 0");
   if ((int64_t)n > kNoAllocMaxRows)

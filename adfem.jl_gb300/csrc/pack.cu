@@ -541,7 +541,7 @@ int pack_graph(PackSlot& c) {
   std::lock_guard<std::mutex> lk(device_alloc_mutex());
   if (!c.h) ADFEM_CUDA(cudaMallocHost((void**)&c.h, bytes));
   if (!c.d.p) {
-    cudaError_t e = cudaMalloc(&c.d.p, bytes);
+    cudaError_t e = injected_alloc_failure() ? cudaErrorMemoryAllocation : cudaMalloc(&c.d.p, bytes);
     if (e != cudaSuccess) {
       c.d.p = nullptr;
       return cuda_fail(e, "cudaMalloc");

@@ -491,6 +491,7 @@ void adfem_server_config_default(adfem_server_config* cfg) {
 }
 
 int adfem_server_create(const adfem_server_config* cfg, adfem_server** out) {
+  ADFEM_RANGE("adfem_server_create");
   if (!out) return adfem::fail(ADFEM_ERR_INVALID, "null argument");
   *out = nullptr;
   auto S = std::make_unique<adfem_server>();
@@ -526,6 +527,7 @@ int adfem_server_create(const adfem_server_config* cfg, adfem_server** out) {
 }
 
 int adfem_server_destroy(adfem_server* srv) {
+  ADFEM_RANGE("adfem_server_destroy");
   if (!srv) return ADFEM_OK;
   {
     std::lock_guard<std::mutex> lk(srv->mu);
@@ -554,6 +556,7 @@ int adfem_server_destroy(adfem_server* srv) {
 }
 
 int adfem_server_submit(adfem_server* srv, const adfem_request* req, long long* ticket) {
+  ADFEM_RANGE("adfem_server_submit");
   if (!srv || !req || !ticket) return adfem::fail(ADFEM_ERR_INVALID, "null argument");
   const adfem::Mesh* m = adfem::mesh_of(req->mesh);
   if (!m) return adfem::fail(ADFEM_ERR_INVALID, "server: request without a mesh");
@@ -598,6 +601,7 @@ int adfem_server_submit(adfem_server* srv, const adfem_request* req, long long* 
 }
 
 int adfem_server_wait(adfem_server* srv, long long ticket, double timeout_ms, adfem_response* resp) {
+  ADFEM_RANGE("adfem_server_wait");
   if (!srv) return adfem::fail(ADFEM_ERR_INVALID, "null argument");
   std::unique_lock<std::mutex> lk(srv->mu);
   auto it = srv->jobs.find(ticket);
@@ -622,6 +626,7 @@ static double percentile(std::vector<double> v, double p) {
 }
 
 int adfem_server_get_stats(adfem_server* srv, adfem_server_stats* out) {
+  ADFEM_RANGE("adfem_server_get_stats");
   if (!srv || !out) return adfem::fail(ADFEM_ERR_INVALID, "null argument");
   std::lock_guard<std::mutex> lk(srv->mu);
   std::memset(out, 0, sizeof(*out));
@@ -652,6 +657,7 @@ int adfem_server_get_stats(adfem_server* srv, adfem_server_stats* out) {
 }
 
 int adfem_server_reset_stats(adfem_server* srv) {
+  ADFEM_RANGE("adfem_server_reset_stats");
   if (!srv) return adfem::fail(ADFEM_ERR_INVALID, "null argument");
   std::lock_guard<std::mutex> lk(srv->mu);
   srv->lat.clear();

@@ -27,6 +27,9 @@ _L = ctypes.c_longlong
 _D = ctypes.c_double
 
 
+SAN_LIB = os.path.join(BUILD, "libfem_oracle_san.so")
+
+
 def build(force: bool = False) -> str:
     """Compile fem_oracle.c into oracle/_build/libfem_oracle.so (gcc, no FMA contraction)."""
     os.makedirs(BUILD, exist_ok=True)
@@ -38,14 +41,30 @@ def build(force: bool = False) -> str:
     return LIB
 
 
+def build_sanitized() -> str:
+    """The same library instrumented with AddressSanitizer and UndefinedBehaviorSanitizer
+    (any finding aborts), for the memory-safety test of the oracle."""
+    os.makedirs(BUILD, exist_ok=True)
+    if not os.path.exists(SAN_LIB) or os.path.getmtime(SAN_LIB) < os.path.getmtime(SRC):
+        tmp = SAN_LIB + ".tmp%d" % os.getpid()
+        subprocess.check_call(["gcc", "-O1", "-g", "-fPIC", "-shared", "-ffp-contract=off", "-fno-omit-frame-pointer",
+                               "-fsanitize=address,undefined", "-fno-sanitize-recover=all", "-o", tmp, SRC,
+                               "-lm", "-lpthread"])
+        os.replace(tmp, SAN_LIB)
+    return SAN_LIB
+
+
 _lib = None
 
 
 def lib():
     global _lib
     if _lib is None:
-        build()
-        L = ctypes.CDLL(LIB)
+        path = os.environ.get("ADFEM_ORACLE_LIB")  # the sanitized build, for the memory-safety test
+        if not path:
+            build()
+            path = LIB
+        L = ctypes.CDLL(path)
         sig = {
             "orc_mesh_geometry": (_I, [_I, _P, _I, _P, _P, _P, _P, _P, _P, _P, _P, _P]),
             "orc_mesh_edges": (_L, [_I, _I, _P, _P]),
