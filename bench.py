@@ -428,16 +428,18 @@ SERVE_SIZES = sorted({int(round(16 * 2 ** (k / 4))) for k in range(25)})  # 16 .
 
 
 class ServeCatalog:
-    """Meshes and input fields of the serving workload, prepared before any timing: per
-    mesh size m (jittered m x m square, seed 0) the Dirichlet sets (Poisson: boundary;
-    elasticity: left edge clamped in x and y), 1% observation DOFs, the shared fields
-    (f = 1e5(x+y); nu = 0.3, body force (0, -1e6)) and two seeded variants of kappa =
-    1 + exp(0.5 G) and E = 1e9 exp(0.3 G) (G a unit-variance Fourier field)."""
+    """Meshes of the serving workload, prepared before any timing: per mesh size m (jittered
+    m x m square, seed 0) the Dirichlet sets (Poisson: boundary; elasticity: left edge
+    clamped in x and y), 1% observation DOFs and the shared fields (f = 1e5(x+y); nu = 0.3,
+    body force (0, -1e6)).  Each request's own field (kappa = 1 + exp(0.5 G) or
+    E = 1e9 exp(0.3 G), G a unit-variance 64-mode Fourier field) is drawn from the request's
+    seed by `fields`, also before the timing."""
 
-    def __init__(self, A, sizes, variants=2):
+    def __init__(self, A, sizes):
         import torch
         from adfem_gpu import synth
 
+        self.A = A
         self.sizes = sizes
         self.items = {}
         for m in sizes:
@@ -448,22 +450,19 @@ class ServeCatalog:
             nv = mesh.nnode
             left = synth.left_edge_nodes(coords) + 1
             rng = np.random.default_rng(m)
-            it = {"mesh": mesh, "ndof": (nv, 2 * nv),
+            it = {"mesh": mesh, "ndof": (nv, 2 * nv), "g": g,
                   "bd": (A.bcnode(mesh), np.concatenate([left, left + nv])),
                   "f": (1e5 * (g[:, 0] + g[:, 1])).cpu().numpy(),
-                  "nu": np.full(ng, 0.3), "fx": np.zeros(ng), "fy": np.full(ng, -1e6),
-                  "kappa": [], "E": [], "obs": []}
-            for v in range(variants):
-                G = synth.fourier_field(g[:, 0], g[:, 1], seed=1000 * m + v)
-                it["kappa"].append((1.0 + torch.exp(0.5 * G)).cpu().numpy())
-                it["E"].append((1e9 * torch.exp(0.3 * G)).cpu().numpy())
+                  "nu": np.full(ng, 0.3), "fx": np.zeros(ng), "fy": np.full(ng, -1e6), "obs": []}
             for nd in it["ndof"]:
                 ob = np.sort(rng.choice(np.arange(1, nd + 1), max(1, nd // 100), replace=False))
                 it["obs"].append((ob, 1e-3 * rng.standard_normal(ob.size)))
             self.items[m] = it
 
     def requests(self, count, seed):
-        """(m, kind, variant, with_gradient) for `count` requests with per-request draws."""
+        """(m, kind, field seed, with_gradient) for `count` requests with per-request draws:
+        m log-uniform in [16, 1024] (to the nearest catalog size), 80/20 Poisson/elasticity,
+        50% with a gradient, and a field seed of the request's own."""
         rng = np.random.default_rng(seed)
         lo, hi = math.log(16), math.log(1024)
         out = []
@@ -471,83 +470,146 @@ class ServeCatalog:
             mc = math.exp(rng.uniform(lo, hi))
             m = min(self.sizes, key=lambda s: abs(math.log(s) - math.log(mc)))
             kind = 0 if rng.random() < 0.8 else 1
-            out.append((m, kind, int(rng.integers(0, 2)), bool(rng.random() < 0.5)))
+            out.append((m, kind, int(rng.integers(1 << 31)), bool(rng.random() < 0.5)))
         return out
 
-    def submit(self, srv, req):
-        m, kind, v, grad = req
+    def fields(self, req):
+        """The request's input fields (host arrays) from its seed."""
+        import torch
+        from adfem_gpu import synth
+
+        m, kind, seed, _ = req
         it = self.items[m]
-        fields = (it["kappa"][v], it["f"]) if kind == 0 else (it["E"][v], it["nu"], it["fx"], it["fy"])
+        G = synth.fourier_field(it["g"][:, 0], it["g"][:, 1], seed=seed)
+        if kind == 0:
+            return ((1.0 + torch.exp(0.5 * G)).cpu().numpy(), it["f"])
+        return ((1e9 * torch.exp(0.3 * G)).cpu().numpy(), it["nu"], it["fx"], it["fy"])
+
+    def submit(self, srv, req, fields):
+        m, kind, _, grad = req
+        it = self.items[m]
         ob, uo = it["obs"][kind] if grad else (None, None)
         return srv.submit(it["mesh"], kind, fields, it["bd"][kind], obs=ob, uobs=uo)
 
     def dof(self, req):
         return self.items[req[0]]["ndof"][req[1]]
 
+    def reference(self, req, fields, rtol=1e-13):
+        """FP64 solution of the request's system at rtol 1e-13 (or its attainable floor)."""
+        import torch
 
-def run_serve(A, args, rank=0, world=1, dist=None):
-    """C5 serving workload through adfem_gpu.Server: a warm-up pass over every (size,
-    kind), a saturation run (all requests queued at once) and an open-loop sweep with
-    Poisson arrivals at fractions of the saturation throughput.  With several ranks each
-    runs a server replica on its GPU and takes its share of every request stream
-    (`shard`); throughput is all requests over the slowest replica's time, latency
-    percentiles are rank 0's."""
-    t0 = time.perf_counter()
-    cat = ServeCatalog(A, SERVE_SIZES)
-    setup_s = time.perf_counter() - t0
-    with A.Server(workers=args.serve_workers, precision="mixed", rtol=args.serve_rtol,
+        m, kind, _, _ = req
+        it = self.items[m]
+        dev = [torch.tensor(np.ascontiguousarray(a), device="cuda") for a in fields]
+        S = self.A.PoissonSystem(it["mesh"]) if kind == 0 else self.A.ElasticitySystem(it["mesh"])
+        S.set_dirichlet(it["bd"][kind])
+        S.assemble(*dev)
+        return S.solve(precision="fp64", rtol=rtol).cpu().numpy()
+
+
+def _serve_arm(cat, args, precision, rank, world, dist, reqs_sat, sweeps, fields):
+    """One serving arm (all requests at `precision`): warm-up over every (size, kind), a
+    saturation run (every request queued at t = 0), then open-loop Poisson arrivals at
+    fractions of the saturation throughput.  Returns (report, saturation-run solutions)."""
+    A = cat.A
+    with A.Server(workers=args.serve_workers, precision=precision, rtol=args.serve_rtol,
                   pack_max_dof=args.serve_pack_max_dof) as srv:
         warm = [(m, k, 0, True) for m in SERVE_SIZES for k in (0, 1)]
-        for t in [cat.submit(srv, r) for r in warm]:
+        for t in [cat.submit(srv, r, cat.fields(r)) for r in warm]:
             srv.wait(t)
-        # saturation: every request queued at t = 0
-        reqs = shard(cat.requests(args.serve_requests, seed=11), rank, world)
         srv.reset_stats()
         ts = time.perf_counter()
-        tickets = [cat.submit(srv, r) for r in reqs]
-        resps = [srv.wait(t)[0] for t in tickets]
+        tickets = [cat.submit(srv, r, fields[i]) for i, r in reqs_sat]
+        outs = [srv.wait(t) for t in tickets]
         wall = max_over_ranks(dist, time.perf_counter() - ts)
         st = srv.stats()
-        bad = sum(1 for r in resps if r["status"] != 0)
-        sat = {"requests": args.serve_requests, "wall_s": wall,
-               "throughput_req_s": replica_rate(world, len(reqs), wall),
-               "dof_per_s": replica_rate(world, sum(cat.dof(r) for r in reqs), wall), "p50_ms": st["p50_ms"], "p99_ms": st["p99_ms"],
-               "failed": bad, "gradients": sum(1 for r in reqs if r[3]), "packs": st["packs"],
+        sat = {"requests": len(reqs_sat) * world, "wall_s": wall,
+               "throughput_req_s": replica_rate(world, len(reqs_sat), wall),
+               "dof_per_s": replica_rate(world, sum(cat.dof(r) for _, r in reqs_sat), wall),
+               "p50_ms": st["p50_ms"], "p99_ms": st["p99_ms"], "failed": sum(1 for o in outs if o[0]["status"] != 0),
+               "gradients": sum(1 for _, r in reqs_sat if r[3]), "packs": st["packs"],
                "packed_requests": st["packed_requests"]}
-        # open loop: exponential inter-arrival gaps at a fraction of the saturation rate
+        sols = {i: o[1] for (i, _), o in zip(reqs_sat, outs)}
         sweep = []
-        for frac in args.serve_loads:
+        for frac, sub in sweeps:
             rate = frac * sat["throughput_req_s"]
-            sub = shard(cat.requests(args.serve_sweep_requests, seed=int(100 * frac)), rank, world)
             gaps = np.random.default_rng(int(1000 * frac) + rank).exponential(world / rate, len(sub))
             srv.reset_stats()
             ts = time.perf_counter()
             nxt = ts
             tickets = []
-            for r, gap in zip(sub, gaps):
+            for (i, r), gap in zip(sub, gaps):
                 nxt += gap
                 dt = nxt - time.perf_counter()
                 if dt > 0:
                     time.sleep(dt)
-                tickets.append(cat.submit(srv, r))
+                tickets.append(cat.submit(srv, r, fields[i]))
             rs = [srv.wait(t)[0] for t in tickets]
             wall = max_over_ranks(dist, time.perf_counter() - ts)
             s = srv.stats()
-            sweep.append({"offered_req_s": rate, "load": frac, "achieved_req_s": replica_rate(world, len(sub), wall),
+            sweep.append({"offered_req_s": rate, "load": frac, "requests": len(sub) * world,
+                          "achieved_req_s": replica_rate(world, len(sub), wall),
                           "p50_ms": s["p50_ms"], "p99_ms": s["p99_ms"], "p50_queue_ms": s["p50_queue_ms"],
                           "failed": sum(1 for r in rs if r["status"] != 0), "packs": s["packs"],
                           "packed_requests": s["packed_requests"]})
         cache = srv.stats()
     ref = min(sweep, key=lambda x: abs(x["load"] - 0.5)) if sweep else None
-    return {"workload": "C5 mix: 80/20 Poisson/elasticity, m log-uniform in [16,1024] rounded to %d sizes "
-                        "(ratio 2^(1/4)), 50%% with a misfit gradient (1%% observations), seeded fields"
-                        % len(SERVE_SIZES),
-            "workers": args.serve_workers, "rtol": args.serve_rtol, "precision": "mixed",
-            "pack_max_dof": args.serve_pack_max_dof if args.serve_pack_max_dof != 0 else 16384,
+    return {"precision": precision, "rtol": args.serve_rtol,
             "p50_ms": ref["p50_ms"] if ref else sat["p50_ms"], "p99_ms": ref["p99_ms"] if ref else sat["p99_ms"],
-            "latency_at_load": ref["load"] if ref else 1.0,
-            "saturation": sat, "sweep": sweep, "setup_s": setup_s,
-            "resident_systems": cache["resident_systems"], "device_bytes": cache["device_bytes"]}
+            "latency_at_load": ref["load"] if ref else 1.0, "saturation": sat, "sweep": sweep,
+            "resident_systems": cache["resident_systems"], "device_bytes": cache["device_bytes"]}, sols
+
+
+def run_serve(A, args, rank=0, world=1, dist=None):
+    """C5 serving workload through adfem_gpu.Server, a mixed-precision arm and an FP64 arm on
+    the same request streams: per-request seeded fields, a saturation run of
+    `serve_requests` requests and open-loop Poisson arrivals (`serve_sweep_requests` each) at
+    the `serve_loads` fractions of each arm's saturation throughput.  The error of a sample of
+    the saturation run's solutions (both arms) is measured against an FP64 solve of the same
+    request at rtol 1e-13.  With several ranks each runs a server replica on its GPU and takes
+    its share of every stream (`shard`); throughput is all requests over the slowest
+    replica's time, latency percentiles are rank 0's."""
+    t0 = time.perf_counter()
+    cat = ServeCatalog(A, SERVE_SIZES)
+    all_reqs = cat.requests(args.serve_requests, seed=11)
+    sat_reqs = shard(list(enumerate(all_reqs)), rank, world)
+    streams, base = [], len(all_reqs)
+    for frac in args.serve_loads:
+        sub = cat.requests(args.serve_sweep_requests, seed=int(100 * frac))
+        streams.append((frac, [(base + j, r) for j, r in enumerate(sub)]))
+        base += len(sub)
+    sweeps = [(frac, shard(sub, rank, world)) for frac, sub in streams]
+    fields = {}
+    for i, r in sat_reqs + [x for _, sub in sweeps for x in sub]:
+        fields[i] = cat.fields(r)
+    setup_s = time.perf_counter() - t0
+    arms, sols = {}, {}
+    for prec in args.serve_precisions:
+        arms[prec], sols[prec] = _serve_arm(cat, args, prec, rank, world, dist, sat_reqs, sweeps, fields)
+    # accuracy of a sample of the served solutions against FP64 at rtol 1e-13
+    acc = None
+    if rank == 0 and args.serve_check > 0 and sat_reqs:
+        rng = np.random.default_rng(5)
+        pick = [sat_reqs[j] for j in sorted(rng.choice(len(sat_reqs), min(args.serve_check, len(sat_reqs)),
+                                                       replace=False))]
+        errs = {p: [] for p in sols}
+        for i, r in pick:
+            uref = cat.reference(r, fields[i])
+            sc = max(float(np.abs(uref).max()), 1e-300)
+            for p in sols:
+                errs[p].append(float(np.abs(sols[p][i] - uref).max()) / sc)
+        acc = {"sample": len(pick), "reference": "FP64 solve of the same request at rtol 1e-13",
+               **{p: {"max_rel_err": max(v), "median_rel_err": statistics.median(v)} for p, v in errs.items()}}
+    out = {"workload": "C5 mix: 80/20 Poisson/elasticity, m log-uniform in [16,1024] (to the nearest of %d sizes, "
+                       "ratio 2^(1/4)), 50%% with a misfit gradient (1%% observations), each request's kappa or E "
+                       "from its own seed" % len(SERVE_SIZES),
+           "workers": args.serve_workers, "rtol": args.serve_rtol,
+           "pack_max_dof": args.serve_pack_max_dof if args.serve_pack_max_dof != 0 else 16384,
+           "setup_s": setup_s, "arms": arms, "accuracy_vs_fp64": acc}
+    head = arms.get("mixed") or next(iter(arms.values()))
+    out.update({"p50_ms": head["p50_ms"], "p99_ms": head["p99_ms"], "latency_at_load": head["latency_at_load"],
+                "saturation": head["saturation"], "sweep": head["sweep"]})
+    return out
 
 
 # ----------------------------------------------------------------------------- C2, C4
@@ -1149,12 +1211,14 @@ def main():
     ap.add_argument("--ref-iters", type=int, default=200, help="reference arm: PCG iterations per step")
     ap.add_argument("--fp64-iters", type=int, default=FP64_ITERS_DEFAULT)
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--serve-requests", type=int, default=300,
+    ap.add_argument("--serve-requests", type=int, default=400,
                     help="serving workload: requests of the saturation run (0 skips serving)")
-    ap.add_argument("--serve-sweep-requests", type=int, default=150)
+    ap.add_argument("--serve-sweep-requests", type=int, default=300)
+    ap.add_argument("--serve-precisions", nargs="*", default=["mixed", "fp64"])
+    ap.add_argument("--serve-check", type=int, default=24, help="served solutions checked against FP64 at rtol 1e-13")
     ap.add_argument("--serve-loads", type=float, nargs="*", default=[0.5, 0.8])
     ap.add_argument("--serve-workers", type=int, default=8)
-    ap.add_argument("--serve-rtol", type=float, default=1e-9)
+    ap.add_argument("--serve-rtol", type=float, default=1e-10)
     ap.add_argument("--serve-pack-max-dof", type=int, default=0,
                     help="requests up to this many DOFs are solved in packed launches (0: library default; -1: off)")
     ap.add_argument("--only-serve", action="store_true", help="run only the serving leg and print it")
