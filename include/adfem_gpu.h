@@ -53,7 +53,7 @@ ADFEM_API const char *adfem_version(void);
 /* Testing hook, no counterpart in the reference: makes the k-th following device
  * allocation of the library (k = 0: the next one) fail once, exactly as if cudaMalloc
  * had returned cudaErrorMemoryAllocation, so callers can check that every entry point
- * reports ADFEM_ERR_CUDA and the library stays usable.  k < 0 disarms it.  Returns
+ * reports ADFEM_ERR_NOMEM and the library stays usable.  k < 0 disarms it.  Returns
  * ADFEM_OK. */
 ADFEM_API int adfem_debug_fail_alloc(long long k);
 

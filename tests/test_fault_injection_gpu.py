@@ -4,8 +4,8 @@ adfem_debug_fail_alloc(k) makes the k-th following device allocation of the libr
 as if cudaMalloc had returned cudaErrorMemoryAllocation (nothing reaches the driver).  The
 test walks k over every allocation a small Poisson pipeline makes (mesh, resident system,
 assembly, mixed and FP64 solves, adjoint, gradient, Array-arm matrix, K\\F): each run either
-completes with the reference results or fails with ADFEM_ERR_CUDA and the injected
-message -- never a crash or a wrong answer -- and after each failure the same pipeline runs
+completes with the reference results or fails with ADFEM_ERR_NOMEM (the status every
+entry reports for cudaErrorMemoryAllocation) and the injected message -- never a crash or a wrong answer -- and after each failure the same pipeline runs
 again to the same bits.
 """
 import numpy as np
@@ -58,7 +58,7 @@ def test_every_injected_allocation_failure_is_a_status(oracle, gpulib):
             try:
                 got = _pipeline(gpulib, *case)
             except gpulib.AdFemError as e:
-                assert e.status == _lib.ERR_CUDA, str(e)
+                assert e.status == _lib.ERR_NOMEM, str(e)
                 assert "injected" in str(e), str(e)
                 failures += 1
             else:
