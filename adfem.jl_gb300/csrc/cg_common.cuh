@@ -69,6 +69,106 @@ __device__ __forceinline__ float2 warp_sum_pair(float v) {
   return make_float2(h, l);
 }
 
+// ---- double-float arithmetic: a value as an unevaluated FP32 pair h + l (~48 bits).
+// Explicitly rounded intrinsics keep the compiler from fusing or reassociating the error
+// terms.  Used where FP64 would put long chains of dependent FP64 instructions on the
+// critical path: on GB300 an FP64 instruction has a long latency as well as a low rate,
+// and the end-of-launch reduction of the banded iteration (one warp, then one thread)
+// measured ~10 us per iteration with FP64 sums and divisions.
+__device__ __forceinline__ float2 df_norm(float s, float e) {
+  const float h = __fadd_rn(s, e);
+  return make_float2(h, __fsub_rn(e, __fsub_rn(h, s)));
+}
+__device__ __forceinline__ float2 df_add(float2 a, float2 b) {
+  const float s = __fadd_rn(a.x, b.x);
+  const float bb = __fsub_rn(s, a.x);
+  float e = __fadd_rn(__fsub_rn(a.x, __fsub_rn(s, bb)), __fsub_rn(b.x, bb));
+  e = __fadd_rn(e, __fadd_rn(a.y, b.y));
+  return df_norm(s, e);
+}
+__device__ __forceinline__ float2 df_neg(float2 a) { return make_float2(-a.x, -a.y); }
+__device__ __forceinline__ float2 df_mul(float2 a, float2 b) {
+  const float p = __fmul_rn(a.x, b.x);
+  float e = fmaf(a.x, b.x, -p);
+  e = fmaf(a.x, b.y, e);
+  e = fmaf(a.y, b.x, e);
+  return df_norm(p, e);
+}
+__device__ __forceinline__ float2 df_div(float2 a, float2 b) {
+  const float q1 = __fdiv_rn(a.x, b.x);
+  const float2 r = df_add(a, df_neg(df_mul(make_float2(q1, 0.0f), b)));
+  const float q2 = __fdiv_rn(r.x, b.x);
+  return df_norm(q1, q2);
+}
+__device__ __forceinline__ double df_to_d(float2 a) { return (double)a.x + (double)a.y; }
+__device__ __forceinline__ float2 d_to_df(double d) {
+  const float h = (float)d;
+  return make_float2(h, (float)(d - (double)h));
+}
+
+// Grid sum of FP32 per-thread partials kept as FP32 pairs all the way: pair sums within
+// each warp, across the block's warps (warp 0) and across the blocks (warp 0 of the last
+// block to arrive, in block order); no FP64 instruction.  partials: NV * gridDim.x pairs.
+// Returns true in the last block (block-uniform); tot is valid in thread 0.
+template <int NV, int BT>
+__device__ __forceinline__ bool reduce_grid_pair(float (&v)[NV], float2* partials, unsigned* counter,
+                                                 float2 (&tot)[NV]) {
+  static_assert(BT % 32 == 0 && BT <= 1024, "block size");
+  __shared__ float2 sh[NV][BT / 32];
+  __shared__ bool last;
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  float2 w[NV];
+#pragma unroll
+  for (int j = 0; j < NV; j++) w[j] = warp_sum_pair(v[j]);
+  if (lane == 0)
+#pragma unroll
+    for (int j = 0; j < NV; j++) sh[j][wid] = w[j];
+  __syncthreads();
+  if (wid == 0) {
+#pragma unroll
+    for (int j = 0; j < NV; j++) {
+      float2 x = lane < BT / 32 ? sh[j][lane] : make_float2(0.0f, 0.0f);
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1)
+        x = df_add(x, make_float2(__shfl_xor_sync(0xffffffffu, x.x, o), __shfl_xor_sync(0xffffffffu, x.y, o)));
+      w[j] = x;
+    }
+    if (lane == 0) {
+#pragma unroll
+      for (int j = 0; j < NV; j++) partials[j * gridDim.x + blockIdx.x] = w[j];
+      __threadfence();
+      const unsigned prev = atomicAdd(counter, 1u);
+      last = (prev == gridDim.x - 1);
+    }
+  }
+  __syncthreads();
+  if (!last) return false;
+  if (wid == 0) {
+    __threadfence();
+    float2 s[NV];
+#pragma unroll
+    for (int j = 0; j < NV; j++) s[j] = make_float2(0.0f, 0.0f);
+    for (int b = lane; b < (int)gridDim.x; b += 32)
+#pragma unroll
+      for (int j = 0; j < NV; j++) {
+        const float2 pv = __ldcg(partials + j * gridDim.x + b);
+        s[j] = df_add(s[j], pv);
+      }
+#pragma unroll
+    for (int j = 0; j < NV; j++)
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1)
+        s[j] = df_add(s[j], make_float2(__shfl_xor_sync(0xffffffffu, s[j].x, o),
+                                        __shfl_xor_sync(0xffffffffu, s[j].y, o)));
+    if (lane == 0) {
+#pragma unroll
+      for (int j = 0; j < NV; j++) tot[j] = s[j];
+      *counter = 0u;
+    }
+  }
+  return true;
+}
+
 template <int NV, int BT, bool PAIR = false>
 __device__ __forceinline__ bool reduce_grid_w(float (&v)[NV], double* partials, unsigned* counter, double (&tot)[NV]) {
   static_assert(BT % 32 == 0 && BT <= 1024, "block size");

@@ -75,13 +75,18 @@ __device__ __forceinline__ unsigned pair_mask() { return 3u << (threadIdx.x & 30
 // so that the vectors the next iteration reads again (Z, P, q^, Y, D, about as large as
 // L2) stay cached, and those vectors are stored with evict-last (ADFEM_ZCG_KEEP_STORES=0
 // at build time turns that off).
-// The iteration's dot products: ADFEM_ZCG_WRED=2 sums them within each warp as FP32 pairs
-// (error-free two-sums, ~48 bits) and in FP64 by one warp per block (reduce_grid_w); 1:
-// plain FP32 within warps; 0: FP64 block sums by every warp.  Measured on GB300 at 4M DOF:
-// 0 -> 62.3 us per iteration, 1 -> 57.6 us but 3.4% more iterations (the rounding of the
-// residual estimate), 2 -> 60.2 us with the iterates of 0.
+// The iteration's dot products: ADFEM_ZCG_WRED=3 (default) sums them as FP32 pairs
+// (error-free two-sums, ~48 bits) within warps, across warps and across blocks, and the
+// last block computes the step lengths in the same double-float arithmetic
+// (reduce_grid_pair); 2: FP32 pairs within each warp, FP64 across warps and blocks and in
+// the step lengths (reduce_grid_w); 1: plain FP32 within warps; 0: FP64 block sums by every
+// warp.  Measured on GB300 at 4M DOF (per iteration): 0 -> 62.3 us, 1 -> 57.6 us but 3.4%
+// more iterations (the rounding of the residual estimate), 2 -> 60.2 us with the iterates
+// of 0 (52.9 us with the later 1024-thread blocks); with 2, the end-of-launch reduction --
+// chains of dependent FP64 additions, shuffles and divisions in one warp and one thread,
+// while every other SM waits -- took ~10 us of each iteration (per-block timestamps).
 #ifndef ADFEM_ZCG_WRED
-#define ADFEM_ZCG_WRED 2
+#define ADFEM_ZCG_WRED 3
 #endif
 #ifndef ADFEM_ZCG_KEEP_STORES
 #define ADFEM_ZCG_KEEP_STORES 1
@@ -302,6 +307,40 @@ __global__ void __launch_bounds__(BT, 1024 / BT) k_zcg_iter(ZcgArgs A) {
     }
   }
 
+#if ADFEM_ZCG_WRED == 3
+  // FP32 pairs end to end (the default): the reduction and the step-length arithmetic of the
+  // last block spend no FP64 instruction on the critical path between two launches
+  float v[4] = {pq, pkq, qq, rr};
+  float2 tot2[4];
+  const bool lastb = reduce_grid_pair<4, BT>(v, reinterpret_cast<float2*>(A.partials), &st->counter[0], tot2);
+  if (lastb && threadIdx.x == 0) {
+    const float2 pq2 = tot2[0], qq2 = tot2[2], rho2 = tot2[3];
+    const double rho = df_to_d(rho2), pqd = df_to_d(pq2);
+    const float2 zq2 = (full_zq && st->ar != 0.0) ? d_to_df((pqd - st->ap * df_to_d(tot2[1])) / st->ar) : pq2;
+    if (!isfinite(rho) || !isfinite(pqd)) {
+      st->done = 2;
+    } else if (rho <= st->stop2) {
+      st->final_req = 1;
+      st->done = 3;
+    } else if (rho <= st->ru2 || it >= st->max_iter) {
+      st->done = 3;  // the FP64 residual decides
+    } else if (!(pqd > 0.0)) {
+      st->done = 2;
+    } else {
+      const float2 al = df_div(rho2, pq2);
+      const float2 az = df_mul(al, zq2);
+      const float2 est = df_add(df_add(rho2, df_neg(make_float2(2.0f * az.x, 2.0f * az.y))),
+                                df_mul(df_mul(al, al), qq2));
+      const float2 apf = est.x > 0.0f ? df_div(est, rho2) : make_float2(0.0f, 0.0f);
+      st->alpha_prev = st->alpha;
+      st->alpha = df_to_d(al);
+      st->ar = 1.0;
+      st->ap = df_to_d(apf);
+      st->rho = rho;
+      st->iters = it + 1;
+    }
+  }
+#else
   double tot[4];
   bool lastb;
   if constexpr (ADFEM_ZCG_WRED) {
@@ -334,6 +373,7 @@ __global__ void __launch_bounds__(BT, 1024 / BT) k_zcg_iter(ZcgArgs A) {
       st->iters = it + 1;
     }
   }
+#endif
 }
 
 // Operator copies for the banded path from the unscaled FP64 sliced-ELL values:
