@@ -148,7 +148,22 @@ __device__ __forceinline__ bool reduce_grid_pair(float (&v)[NV], float2* partial
     float2 s[NV];
 #pragma unroll
     for (int j = 0; j < NV; j++) s[j] = make_float2(0.0f, 0.0f);
-    for (int b = lane; b < (int)gridDim.x; b += 32)
+    // up to 160 blocks: each lane loads all of its partials before adding (one L2 round
+    // trip instead of one per 32 blocks), then the rest, if any, in the plain loop
+    constexpr int kB = 5;
+    float2 pl[kB][NV];
+#pragma unroll
+    for (int q = 0; q < kB; q++) {
+      const int b = lane + 32 * q;
+#pragma unroll
+      for (int j = 0; j < NV; j++)
+        pl[q][j] = b < (int)gridDim.x ? __ldcg(partials + j * gridDim.x + b) : make_float2(0.0f, 0.0f);
+    }
+#pragma unroll
+    for (int q = 0; q < kB; q++)
+#pragma unroll
+      for (int j = 0; j < NV; j++) s[j] = df_add(s[j], pl[q][j]);
+    for (int b = lane + 32 * kB; b < (int)gridDim.x; b += 32)
 #pragma unroll
       for (int j = 0; j < NV; j++) {
         const float2 pv = __ldcg(partials + j * gridDim.x + b);
