@@ -141,6 +141,21 @@ __global__ void __launch_bounds__(BT, 1024 / BT) k_zcg_iter(ZcgArgs A) {
   float* __restrict__ yl = A.yl;
   const float a = (float)st->alpha, ar = (float)st->ar, ap = (float)st->ap;
   const float a2 = (float)st->alpha_prev;
+#if ADFEM_ZCG_WRED == 3
+  // the scalars the last block's step-length code reads, fetched now by thread 0 (the one
+  // thread that uses them): after the reduction they would be a chain of dependent global
+  // loads on the critical path between two launches
+  __shared__ double s_sc[6];
+  __shared__ int s_maxit;
+  if (threadIdx.x == 0) {
+    s_sc[0] = st->alpha;
+    s_sc[1] = st->ar;
+    s_sc[2] = st->ap;
+    s_sc[3] = st->stop2;
+    s_sc[4] = st->ru2;
+    s_maxit = st->max_iter;
+  }
+#endif
   const bool ydo = (it & 1) == 0;   // the two-step solution update runs on even iterations
   const bool full_zq = ar != 1.0f;  // uniform
   const uint64_t pol = l2_evict_first_policy();
@@ -316,13 +331,14 @@ __global__ void __launch_bounds__(BT, 1024 / BT) k_zcg_iter(ZcgArgs A) {
   if (lastb && threadIdx.x == 0) {
     const float2 pq2 = tot2[0], qq2 = tot2[2], rho2 = tot2[3];
     const double rho = df_to_d(rho2), pqd = df_to_d(pq2);
-    const float2 zq2 = (full_zq && st->ar != 0.0) ? d_to_df((pqd - st->ap * df_to_d(tot2[1])) / st->ar) : pq2;
+    const double ar_d = s_sc[1], ap_d = s_sc[2];
+    const float2 zq2 = (full_zq && ar_d != 0.0) ? d_to_df((pqd - ap_d * df_to_d(tot2[1])) / ar_d) : pq2;
     if (!isfinite(rho) || !isfinite(pqd)) {
       st->done = 2;
-    } else if (rho <= st->stop2) {
+    } else if (rho <= s_sc[3]) {
       st->final_req = 1;
       st->done = 3;
-    } else if (rho <= st->ru2 || it >= st->max_iter) {
+    } else if (rho <= s_sc[4] || it >= s_maxit) {
       st->done = 3;  // the FP64 residual decides
     } else if (!(pqd > 0.0)) {
       st->done = 2;
@@ -332,7 +348,7 @@ __global__ void __launch_bounds__(BT, 1024 / BT) k_zcg_iter(ZcgArgs A) {
       const float2 est = df_add(df_add(rho2, df_neg(make_float2(2.0f * az.x, 2.0f * az.y))),
                                 df_mul(df_mul(al, al), qq2));
       const float2 apf = est.x > 0.0f ? df_div(est, rho2) : make_float2(0.0f, 0.0f);
-      st->alpha_prev = st->alpha;
+      st->alpha_prev = s_sc[0];
       st->alpha = df_to_d(al);
       st->ar = 1.0;
       st->ap = df_to_d(apf);
