@@ -101,6 +101,8 @@ __device__ __forceinline__ float2 df_div(float2 a, float2 b) {
   return df_norm(q1, q2);
 }
 __device__ __forceinline__ double df_to_d(float2 a) { return (double)a.x + (double)a.y; }
+// a <= b for normalised pairs (|l| at most half an ulp of h)
+__device__ __forceinline__ bool df_le(float2 a, float2 b) { return a.x < b.x || (a.x == b.x && a.y <= b.y); }
 __device__ __forceinline__ float2 d_to_df(double d) {
   const float h = (float)d;
   return make_float2(h, (float)(d - (double)h));

@@ -145,14 +145,15 @@ __global__ void __launch_bounds__(BT, 1024 / BT) k_zcg_iter(ZcgArgs A) {
   // the scalars the last block's step-length code reads, fetched now by thread 0 (the one
   // thread that uses them): after the reduction they would be a chain of dependent global
   // loads on the critical path between two launches
-  __shared__ double s_sc[6];
+  __shared__ double s_sc[3];
+  __shared__ float2 s_th[2];  // the stopping and replacement thresholds as FP32 pairs
   __shared__ int s_maxit;
   if (threadIdx.x == 0) {
     s_sc[0] = st->alpha;
     s_sc[1] = st->ar;
     s_sc[2] = st->ap;
-    s_sc[3] = st->stop2;
-    s_sc[4] = st->ru2;
+    s_th[0] = d_to_df(st->stop2);
+    s_th[1] = d_to_df(st->ru2);
     s_maxit = st->max_iter;
   }
 #endif
@@ -330,17 +331,19 @@ __global__ void __launch_bounds__(BT, 1024 / BT) k_zcg_iter(ZcgArgs A) {
   const bool lastb = reduce_grid_pair<4, BT>(v, reinterpret_cast<float2*>(A.partials), &st->counter[0], tot2);
   if (lastb && threadIdx.x == 0) {
     const float2 pq2 = tot2[0], qq2 = tot2[2], rho2 = tot2[3];
-    const double rho = df_to_d(rho2), pqd = df_to_d(pq2);
-    const double ar_d = s_sc[1], ap_d = s_sc[2];
-    const float2 zq2 = (full_zq && ar_d != 0.0) ? d_to_df((pqd - ap_d * df_to_d(tot2[1])) / ar_d) : pq2;
-    if (!isfinite(rho) || !isfinite(pqd)) {
+    // decisions in pair arithmetic against the thresholds prepared at entry: no dependent
+    // FP64 instruction before the branch
+    float2 zq2 = pq2;
+    if (full_zq && s_sc[1] != 0.0)
+      zq2 = d_to_df((df_to_d(pq2) - s_sc[2] * df_to_d(tot2[1])) / s_sc[1]);  // after a replacement only
+    if (!isfinite(rho2.x) || !isfinite(pq2.x)) {
       st->done = 2;
-    } else if (rho <= s_sc[3]) {
+    } else if (df_le(rho2, s_th[0])) {
       st->final_req = 1;
       st->done = 3;
-    } else if (rho <= s_sc[4] || it >= s_maxit) {
+    } else if (df_le(rho2, s_th[1]) || it >= s_maxit) {
       st->done = 3;  // the FP64 residual decides
-    } else if (!(pqd > 0.0)) {
+    } else if (!(pq2.x > 0.0f)) {
       st->done = 2;
     } else {
       const float2 al = df_div(rho2, pq2);
@@ -352,7 +355,7 @@ __global__ void __launch_bounds__(BT, 1024 / BT) k_zcg_iter(ZcgArgs A) {
       st->alpha = df_to_d(al);
       st->ar = 1.0;
       st->ap = df_to_d(apf);
-      st->rho = rho;
+      st->rho = df_to_d(rho2);
       st->iters = it + 1;
     }
   }
