@@ -82,6 +82,7 @@ SIGNATURES = {
     "adfem_last_error": (ctypes.c_char_p, []),
     "adfem_version": (ctypes.c_char_p, []),
     "adfem_debug_fail_alloc": (c_i, [c_ll]),
+    "adfem_debug_check_code": (c_i, []),
     "init_nnfem_mesh": (ctypes.POINTER(c_ll), [c_p, c_i, c_p, c_i, c_i, c_i, c_i, c_p]),
     "mfem_get_ngauss": (c_i, []),
     "mfem_get_gauss": (None, [c_p, c_p]),

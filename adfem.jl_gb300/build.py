@@ -43,10 +43,14 @@ def _headers():
         glob.glob(os.path.join(INCLUDE, "*.h"))
 
 
-def _compile(src: str, extra: list[str]) -> str:
-    obj = os.path.join(BUILD, os.path.basename(src) + ".o")
+CHECKS_BUILD = os.path.join(HERE, "_build_checks")
+CHECKS_LIB = os.path.join(LIBDIR, "libadfem_gpu_checks.so")
+
+
+def _compile(src: str, extra: list[str], build_dir: str = BUILD, always: bool = False) -> str:
+    obj = os.path.join(build_dir, os.path.basename(src) + ".o")
     newest_dep = max([os.path.getmtime(src)] + [os.path.getmtime(h) for h in _headers()])
-    if os.path.exists(obj) and os.path.getmtime(obj) >= newest_dep and not extra:
+    if os.path.exists(obj) and os.path.getmtime(obj) >= newest_dep and not always:
         return obj
     cmd = [nvcc()] + NVCC_FLAGS + extra + ["-c", src, "-o", obj + ".tmp"]
     r = subprocess.run(cmd, capture_output=True, text=True)
@@ -56,24 +60,28 @@ def _compile(src: str, extra: list[str]) -> str:
     return obj
 
 
-def build(verbose: bool = False, ptxas_info: bool = False) -> str:
-    os.makedirs(BUILD, exist_ok=True)
+def build(verbose: bool = False, ptxas_info: bool = False, checks: bool = False) -> str:
+    """Build the library; checks=True builds the debug variant instead (-DADFEM_CHECKS: kernels
+    check the indices they compute and record failures, see checks.cuh) as
+    lib/libadfem_gpu_checks.so, with its objects in _build_checks."""
+    build_dir, lib = (CHECKS_BUILD, CHECKS_LIB) if checks else (BUILD, LIB)
+    os.makedirs(build_dir, exist_ok=True)
     os.makedirs(LIBDIR, exist_ok=True)
-    extra = ["-Xptxas", "-v"] if ptxas_info else []
+    extra = (["-Xptxas", "-v"] if ptxas_info else []) + (["-DADFEM_CHECKS"] if checks else [])
     srcs = _sources()
-    with cf.ThreadPoolExecutor(max_workers=min(8, len(srcs))) as ex:
-        objs = list(ex.map(lambda s: _compile(s, extra), srcs))
-    if (not os.path.exists(LIB)) or any(os.path.getmtime(o) > os.path.getmtime(LIB) for o in objs) or extra:
-        tmp = LIB + ".tmp%d" % os.getpid()
+    with cf.ThreadPoolExecutor(max_workers=min(16, len(srcs))) as ex:
+        objs = list(ex.map(lambda s: _compile(s, extra, build_dir, ptxas_info), srcs))
+    if (not os.path.exists(lib)) or any(os.path.getmtime(o) > os.path.getmtime(lib) for o in objs) or ptxas_info:
+        tmp = lib + ".tmp%d" % os.getpid()
         cmd = [nvcc()] + ARCH + ["-shared", "-o", tmp] + objs + ["-lpthread", "-ldl"]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError("link failed:\n%s\n%s" % (" ".join(cmd), r.stdout + r.stderr))
-        os.replace(tmp, LIB)
+        os.replace(tmp, lib)
     if verbose:
-        print("built", LIB)
-    return LIB
+        print("built", lib)
+    return lib
 
 
 if __name__ == "__main__":
-    build(verbose=True, ptxas_info="-v" in sys.argv)
+    build(verbose=True, ptxas_info="-v" in sys.argv, checks="--checks" in sys.argv)

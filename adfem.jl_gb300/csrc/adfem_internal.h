@@ -45,6 +45,12 @@ struct NvtxRange {
 #define ADFEM_RANGE(name) ::adfem::NvtxRange _adfem_range_(name)
 
 // Armed by adfem_debug_fail_alloc: true when this device allocation is to fail (once).
+// Debug build (-DADFEM_CHECKS): the first failed index check of each translation unit, as
+// a source line (0: none; release builds always 0); reading clears it.
+int check_line_solver();
+int check_line_zcg();
+int check_line_assemble();
+
 bool injected_alloc_failure();
 void arm_alloc_failure(long long k);
 

@@ -13,6 +13,7 @@
 //    output value once.  The diagonal is the negated sum of the off-diagonals
 //    (P1 element matrices have zero row sums).
 #include "adfem_internal.h"
+#include "checks.cuh"
 
 namespace adfem {
 
@@ -88,6 +89,7 @@ __device__ __forceinline__ void laplace_row_acc(int64_t i, const int32_t* __rest
     const double sg = sigma[e];
     const unsigned b = (a == 0) ? 1 : 0, c = (a == 2) ? 1 : 2;
     const unsigned ob = inc_off(y, b), oc = inc_off(y, c);
+    if (!ADFEM_DCHECK(ob < (unsigned)w && oc < (unsigned)w && ob < MAXW && oc < MAXW)) continue;
     acc[ob][t] = fma(gpair(g, a, b), sg, acc[ob][t]);
     acc[oc][t] = fma(gpair(g, a, c), sg, acc[oc][t]);
   }
@@ -375,5 +377,7 @@ cudaError_t launch_poisson_kappa_grad(const Mesh& m, const double* u, const doub
                                                          isbd, grad_kappa);
   return cudaGetLastError();
 }
+
+ADFEM_CHECK_READER(check_line_assemble)
 
 }  // namespace adfem

@@ -25,6 +25,7 @@
 #include <thread>
 
 #include "cg_common.cuh"
+#include "checks.cuh"
 
 namespace adfem {
 
@@ -88,7 +89,9 @@ __global__ void k_scale_values(int64_t n, const int32_t* __restrict__ sptr, cons
     const double v = val[idx];
     rowsum += v;
     const double t = si * v;
-    val[idx] = t * (double)s[colof<D16>(col, idx, r)];
+    int j = colof<D16>(col, idx, r);
+    if (!ADFEM_DCHECK(j >= 0 && j < n)) j = (int)r;
+    val[idx] = t * (double)s[j];
     valD[idx] = t;
     val32[idx] = (float)t;
   }
@@ -153,7 +156,8 @@ __global__ void __launch_bounds__(kT) k_residual64(int64_t n, const int32_t* __r
     double s = 0.0;
     for (int k = 0; k < w; k++) {
       const int64_t idx = base + 32 * (int64_t)k;
-      const int j = colof<D16>(col, idx, r);
+      int j = colof<D16>(col, idx, r);
+      if (!ADFEM_DCHECK(j >= 0 && j < n)) j = (int)r;
       const double t = (j == r) ? yr : fma((double)sc[j], y[j], -zr);
       s = fma(valD[idx], t, s);
     }
@@ -233,6 +237,7 @@ struct RowRegs {
       v[k] = k < w ? __ldg(val + base + 32 * k) : V(0);
       int jk = (int)r;
       if (k < w) jk = so >= 0 ? (int)r + (int)__ldg(pp + k) : colof<D16>(col, base + 32 * k, r);
+      if (!ADFEM_DCHECK(jk >= 0 && jk < n)) jk = (int)r;
       j[k] = jk;
     }
   }
@@ -271,7 +276,9 @@ __global__ void __launch_bounds__(kT, PF ? 4 : 1) k_cg64_spmv(int64_t n, const i
       double s = 0.0;
       for (int k = 0; k < w; k++) {
         const int64_t idx = base + 32 * (int64_t)k;
-        s = fma(val[idx], p[colof<D16>(col, idx, r)], s);
+        int j = colof<D16>(col, idx, r);
+        if (!ADFEM_DCHECK(j >= 0 && j < n)) j = (int)r;
+        s = fma(val[idx], p[j], s);
       }
       q[r] = s;
       acc = fma(p[r], s, acc);
@@ -410,7 +417,8 @@ __global__ void __launch_bounds__(kT, PF ? 4 : 1) k_cg32_spmv(int64_t n, const i
       float s = 0.0f;
       for (int k = 0; k < w; k++) {
         const int64_t idx = base + 32 * (int64_t)k;
-        const int j = colof<D16>(col, idx, row);
+        int j = colof<D16>(col, idx, row);
+        if (!ADFEM_DCHECK(j >= 0 && j < n)) j = (int)row;
         const float pj = fmaf(ap, pold[j], ar * r[j]);
         const float t = (j == row) ? pr : fmaf(sc[j], pj, -zr);
         s = fmaf(val[idx], t, s);
@@ -543,7 +551,8 @@ __global__ void k_apply(int64_t n, const int32_t* __restrict__ sptr, const void*
   double acc = 0.0;
   for (int k = 0; k < w; k++) {
     const int64_t idx = base + 32 * (int64_t)k;
-    const int j = colof<D16>(col, idx, r);
+    int j = colof<D16>(col, idx, r);
+    if (!ADFEM_DCHECK(j >= 0 && j < n)) j = (int)r;
     acc = fma(val[idx], x[j] / (double)s[j], acc);
   }
   y[r] = acc / (double)s[r];
@@ -1159,5 +1168,7 @@ int solver_apply(Solver& S, const double* x, double* y, cudaStream_t user) {
   ADFEM_CUDA(cudaGetLastError());
   return ADFEM_OK;
 }
+
+ADFEM_CHECK_READER(check_line_solver)
 
 }  // namespace adfem

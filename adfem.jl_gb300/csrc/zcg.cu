@@ -41,6 +41,7 @@
 #include <vector>
 
 #include "cg_common.cuh"
+#include "checks.cuh"
 
 namespace adfem {
 
@@ -270,7 +271,11 @@ __global__ void __launch_bounds__(BT, 1024 / BT) k_zcg_iter(ZcgArgs A) {
         float tv;
         if (dl[k] == 0) tv = Pi;
         else if (B2 && dl[k] == dpart) tv = Pp;
-        else tv = __fsub_rn(sP[i + dl[k] - wlo], (B2 && (dl[k] & 1)) ? Pp : Pi);
+        else {
+          int w_ = i + dl[k] - wlo;
+          if (!ADFEM_DCHECK(w_ >= 0 && w_ < whi - wlo)) w_ = i - wlo;
+          tv = __fsub_rn(sP[w_], (B2 && (dl[k] & 1)) ? Pp : Pi);
+        }
         s = fmaf(v[k], tv, s);
       }
       float qh;
@@ -502,7 +507,11 @@ __global__ void __launch_bounds__(kT) k_zres64(int64_t n, const int32_t* __restr
       double t;
       if (dl == 0) t = yr;
       else if (block2 && dl == dpart) t = yp;
-      else t = y[r + dl] - ((block2 && (dl & 1)) ? yp : yr);
+      else {
+        int64_t j = r + dl;
+        if (!ADFEM_DCHECK(j >= 0 && j < n)) j = r;
+        t = y[j] - ((block2 && (dl & 1)) ? yp : yr);
+      }
       s = fma(valz[idx], t, s);
     }
     const double ri = b[r] - s;
@@ -947,6 +956,11 @@ __global__ void __launch_bounds__(BT, 1) k_dcg_iter(DcgArgs A) {
 #pragma unroll
         for (int h = 0; h < MAXW / 4; h++) {
           const int4 x = pv[h];
+#ifdef ADFEM_CHECKS
+          if (!ADFEM_DCHECK(i - wlo + min(min(x.x, x.y), min(x.z, x.w)) >= 0 &&
+                            i - wlo + max(max(x.x, x.y), max(x.z, x.w)) < whi - wlo))
+            continue;
+#endif
           if (4 * h < zw) s = fma(v[4 * h], sPi[x.x], s);
           if (4 * h + 1 < zw) s = fma(v[4 * h + 1], sPi[x.y], s);
           if (4 * h + 2 < zw) s = fma(v[4 * h + 2], sPi[x.z], s);
@@ -957,7 +971,9 @@ __global__ void __launch_bounds__(BT, 1) k_dcg_iter(DcgArgs A) {
 #pragma unroll
         for (int k = 0; k < MAXW; k++) {
           const int dk = k < zw ? (int)__ldg(A.colz + base + 32 * k) : 0;
-          s = fma(v[k], sP[i + dk - wlo], s);
+          int w_ = i + dk - wlo;
+          if (!ADFEM_DCHECK(w_ >= 0 && w_ < whi - wlo)) w_ = i - wlo;
+          s = fma(v[k], sP[w_], s);
         }
       }
       qnew[i] = s;
@@ -1137,5 +1153,7 @@ int zcg_clear(Solver& S, cudaStream_t st) {
     ADFEM_CUDA(cudaMemsetAsync(b->p, 0, n4, st));
   return ADFEM_OK;
 }
+
+ADFEM_CHECK_READER(check_line_zcg)
 
 }  // namespace adfem

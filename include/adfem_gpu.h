@@ -56,6 +56,12 @@ ADFEM_API const char *adfem_version(void);
  * reports ADFEM_ERR_NOMEM and the library stays usable.  k < 0 disarms it.  Returns
  * ADFEM_OK. */
 ADFEM_API int adfem_debug_fail_alloc(long long k);
+/* Testing hook, no counterpart in the reference: in the debug build (-DADFEM_CHECKS, a
+ * second library built by build.py --checks) kernels check the indices they compute before
+ * using them and record the first failure instead of faulting; this returns it as
+ * 100000 * unit + source line (unit 1: solver.cu, 2: zcg.cu, 3: assemble.cu), 0 when no check
+ * failed (always 0 in release builds), -1 if the flags cannot be read, and clears it. */
+ADFEM_API int adfem_debug_check_code(void);
 
 /* ====================================================================
  * Layer 1: libadmfem-compatible symbols (current-mesh global state)
