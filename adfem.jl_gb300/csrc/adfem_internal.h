@@ -195,6 +195,8 @@ int64_t mesh_bcnode(Mesh* m, int64_t* out1);
 // Reverse Cuthill-McKee renumbering of the mesh nodes (pi[node] = new index); returns
 // the bandwidth of the renumbered pattern.
 int64_t mesh_rcm(const Mesh& m, std::vector<int32_t>& pi);
+int64_t graph_rcm(int64_t n, const std::vector<int32_t>& rowptr, const std::vector<int32_t>& colind,
+                  std::vector<int32_t>& pi);
 // Gauss points per element (3 for the order-2 rule of P1, 6 for the order-4 rule of P2)
 inline int mesh_ng(const Mesh& m) { return m.degree == 2 ? 6 : 3; }
 inline int64_t mesh_ngauss(const Mesh& m) { return (int64_t)mesh_ng(m) * m.ne; }

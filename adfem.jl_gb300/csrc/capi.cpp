@@ -1253,6 +1253,7 @@ int adfem_system_solver_info(const adfem_system* sys, adfem_solver_info* info) {
   info->renumbered = sys->renumbered ? 1 : 0;
   info->banded_fp64 = sv.dcg ? 1 : 0;
   info->fp64_tile_rows = sv.dcg ? sv.dS : 0;
+  info->ring_stages = sv.zcg ? sv.zns : 0;
   return ADFEM_OK;
 }
 

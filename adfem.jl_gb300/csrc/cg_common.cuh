@@ -108,6 +108,114 @@ __device__ __forceinline__ float2 d_to_df(double d) {
   return make_float2(h, (float)(d - (double)h));
 }
 
+// Sum of two FP32 pairs with an error-free two-sum of the high parts (the butterfly step of
+// warp_sum_pair); symmetric in its arguments, so both lanes of a butterfly get one result.
+__device__ __forceinline__ float2 pair_add(float2 a, float2 b) {
+  const float s = __fadd_rn(a.x, b.x);
+  const float bb = __fsub_rn(s, a.x);
+  const float e = __fadd_rn(__fsub_rn(a.x, __fsub_rn(s, bb)), __fsub_rn(b.x, bb));
+  return make_float2(s, __fadd_rn(__fadd_rn(a.y, b.y), e));
+}
+__device__ __forceinline__ float2 shfl_pair(float2 a, int o) {
+  return make_float2(__shfl_xor_sync(0xffffffffu, a.x, o), __shfl_xor_sync(0xffffffffu, a.y, o));
+}
+
+// Warp sums of four quantities as FP32 pairs, transposed: at the first two butterfly
+// levels each lane sends the quantities it does not keep (half of them, then one), so
+// the warp spends 12 shuffles instead of 40; lane L ends with the total of quantity
+// 2 ((L >> 4) & 1) + ((L >> 3) & 1) (lanes 0, 8, 16, 24 hold quantities 0..3).  After a
+// phase of global stores the shuffles queue behind the stores in the memory pipe, so their
+// number sets the time of the block reduction.
+__device__ __forceinline__ float2 warp_sum_pair4(const float2 (&x)[4]) {
+  const int lane = threadIdx.x & 31;
+  const bool b4 = (lane & 16) != 0, b3 = (lane & 8) != 0;
+  float2 k0 = b4 ? x[2] : x[0], k1 = b4 ? x[3] : x[1];
+  const float2 r0 = shfl_pair(b4 ? x[0] : x[2], 16), r1 = shfl_pair(b4 ? x[1] : x[3], 16);
+  k0 = pair_add(k0, r0);
+  k1 = pair_add(k1, r1);
+  float2 k = pair_add(b3 ? k1 : k0, shfl_pair(b3 ? k0 : k1, 8));
+#pragma unroll
+  for (int o = 4; o > 0; o >>= 1) k = pair_add(k, shfl_pair(k, o));
+  return k;
+}
+
+// Grid sum of four FP32 per-thread values as FP32 pairs (the reduction of the banded mixed
+// iteration), in two parts so that the caller can issue work between them.
+// reduce4_arrive: transposed warp sums, the block's warps summed by warp 0 the same way,
+// the block's partials stored and the block counted in; returns true in the last block to
+// arrive (block-uniform).  reduce4_finish (last block, warp 0): the blocks' partials summed,
+// each lane over its blocks in block order, then across lanes; tot valid in lane 0.
+// Deterministic; no FP64 instruction.  partials: 4 * gridDim.x pairs.
+template <int BT>
+__device__ __forceinline__ bool reduce4_arrive(const float (&v)[4], float2* partials, unsigned* counter) {
+  static_assert(BT % 32 == 0 && BT <= 1024, "block size");
+  __shared__ float2 sh[4][BT / 32];
+  __shared__ bool last;
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const int q = lane >> 3;  // the quantity a lane holds after warp_sum_pair4 (lanes 0, 8, 16, 24)
+  {
+    const float2 x[4] = {make_float2(v[0], 0.0f), make_float2(v[1], 0.0f), make_float2(v[2], 0.0f),
+                         make_float2(v[3], 0.0f)};
+    const float2 w = warp_sum_pair4(x);
+    if ((lane & 7) == 0) sh[q][wid] = w;
+  }
+  __syncthreads();
+  if (wid == 0) {
+    float2 x[4];
+#pragma unroll
+    for (int j = 0; j < 4; j++) x[j] = lane < BT / 32 ? sh[j][lane] : make_float2(0.0f, 0.0f);
+    const float2 w = warp_sum_pair4(x);
+    if ((lane & 7) == 0) partials[q * gridDim.x + blockIdx.x] = w;
+    __threadfence();
+    __syncwarp();
+    if (lane == 0) {
+      const unsigned prev = atomicAdd(counter, 1u);
+      last = (prev == gridDim.x - 1);
+    }
+  }
+  __syncthreads();
+  return last;
+}
+
+template <int BT>
+__device__ __forceinline__ void reduce4_finish(float2* partials, unsigned* counter, float2 (&tot)[4]) {
+  const int lane = threadIdx.x & 31;
+  __threadfence();
+  // up to 160 blocks: each lane loads all of its partials before adding (one L2 round
+  // trip), then the rest, if any, in the plain loop
+  constexpr int kB = 5;
+  float2 pl[kB][4];
+#pragma unroll
+  for (int b5 = 0; b5 < kB; b5++) {
+    const int b = lane + 32 * b5;
+#pragma unroll
+    for (int j = 0; j < 4; j++)
+      pl[b5][j] = b < (int)gridDim.x ? __ldcg(partials + j * gridDim.x + b) : make_float2(0.0f, 0.0f);
+  }
+  float2 s[4];
+#pragma unroll
+  for (int j = 0; j < 4; j++) {
+    s[j] = pl[0][j];
+#pragma unroll
+    for (int b5 = 1; b5 < kB; b5++) s[j] = pair_add(s[j], pl[b5][j]);
+  }
+  for (int b = lane + 32 * kB; b < (int)gridDim.x; b += 32)
+#pragma unroll
+    for (int j = 0; j < 4; j++) s[j] = pair_add(s[j], __ldcg(partials + j * gridDim.x + b));
+  const float2 r = warp_sum_pair4(s);
+  // lane 0 collects the four totals (normalised pairs for the step-length arithmetic)
+  const float2 r1 = make_float2(__shfl_sync(0xffffffffu, r.x, 8), __shfl_sync(0xffffffffu, r.y, 8));
+  const float2 r2 = make_float2(__shfl_sync(0xffffffffu, r.x, 16), __shfl_sync(0xffffffffu, r.y, 16));
+  const float2 r3 = make_float2(__shfl_sync(0xffffffffu, r.x, 24), __shfl_sync(0xffffffffu, r.y, 24));
+  if (lane == 0) {
+    tot[0] = df_norm(r.x, r.y);
+    tot[1] = df_norm(r1.x, r1.y);
+    tot[2] = df_norm(r2.x, r2.y);
+    tot[3] = df_norm(r3.x, r3.y);
+    *counter = 0u;
+  }
+}
+
 // Grid sum of FP32 per-thread partials kept as FP32 pairs all the way: pair sums within
 // each warp, across the block's warps (warp 0) and across the blocks (warp 0 of the last
 // block to arrive, in block order); no FP64 instruction.  partials: NV * gridDim.x pairs.

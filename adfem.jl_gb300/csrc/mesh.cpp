@@ -481,8 +481,15 @@ int64_t mesh_bcnode(Mesh* m, int64_t* out1) {
 // the last node reached), neighbours visited in ascending degree, the whole order then
 // reversed.  pi[node] = new index.  Returns the bandwidth max |pi(i) - pi(j)| over the
 // pattern.
-int64_t mesh_rcm(const Mesh& m, std::vector<int32_t>& pi) {
-  const int64_t n = m.nv;
+int64_t mesh_rcm(const Mesh& m, std::vector<int32_t>& pi) { return graph_rcm(m.nv, m.rowptr, m.colind, pi); }
+
+// The same order for any symmetric graph in CSR form (a degree-2 DOF graph, for instance).
+int64_t graph_rcm(int64_t n, const std::vector<int32_t>& rowptr, const std::vector<int32_t>& colind,
+                  std::vector<int32_t>& pi) {
+  struct G {
+    const std::vector<int32_t>& rowptr;
+    const std::vector<int32_t>& colind;
+  } m{rowptr, colind};
   auto deg = [&](int64_t i) { return m.rowptr[i + 1] - m.rowptr[i]; };
   std::vector<int32_t> order;
   order.reserve(n);

@@ -970,6 +970,9 @@ static int capture_chunk(Solver& S, Path path, int chunk, cudaGraphExec_t* out) 
   });
 }
 
+// the solve's outcome is decided: converged, breakdown, max_iter or a kernel wait that gave up
+static bool finished(int done) { return done == 1 || done == 2 || done == 4 || done == 5; }
+
 struct GraphExecGuard {
   cudaGraphExec_t g = nullptr;
   ~GraphExecGuard() {
@@ -1069,7 +1072,7 @@ int solver_solve(Solver& S, const double* rhs, double* u, const uint8_t* zero_ro
       ADFEM_CUDA(cudaStreamSynchronize(st));
       tm.collect();
       cur = S.h_state[0];
-      if (cur.done == 1 || cur.done == 2 || cur.done == 4) break;
+      if (finished(cur.done)) break;
     }
   } else if (prof) {
     // kernel-by-kernel loop with an event pair around every launch
@@ -1084,7 +1087,7 @@ int solver_solve(Solver& S, const double* rhs, double* u, const uint8_t* zero_ro
       ADFEM_CUDA(cudaStreamSynchronize(st));
       tm.collect();
       cur = S.h_state[0];
-      if (cur.done == 1 || cur.done == 2 || cur.done == 4) break;
+      if (finished(cur.done)) break;
     }
   } else {
     // pipelined host loop: keep one chunk in flight beyond the one being checked
@@ -1100,7 +1103,7 @@ int solver_solve(Solver& S, const double* rhs, double* u, const uint8_t* zero_ro
       ADFEM_CUDA(cudaEventRecord(S.ev[2 + (1 - slot)], st));
       ADFEM_CUDA(cudaEventSynchronize(S.ev[2 + slot]));
       cur = S.h_state[slot];
-      if (cur.done == 1 || cur.done == 2 || cur.done == 4) break;
+      if (finished(cur.done)) break;
       slot = 1 - slot;
     }
   }
@@ -1140,6 +1143,7 @@ int solver_solve(Solver& S, const double* rhs, double* u, const uint8_t* zero_ro
   int status = ADFEM_OK;
   if (cur.done == 2) status = ADFEM_ERR_BREAKDOWN;
   else if (cur.done == 4) status = ADFEM_ERR_NOT_CONVERGED;
+  else if (cur.done == 5) status = ADFEM_ERR_CUDA;
   const double relres = fin.bnorm2 > 0.0 ? std::sqrt(fin.rr64 / fin.bnorm2) : 0.0;
   if (stats) {
     stats->iterations = fin.iters;
@@ -1150,6 +1154,7 @@ int solver_solve(Solver& S, const double* rhs, double* u, const uint8_t* zero_ro
     stats->launches = launches;
   }
   if (status == ADFEM_ERR_BREAKDOWN) return fail(status, "CG breakdown: p.Ap <= 0 or non-finite (operator not SPD?)");
+  if (status == ADFEM_ERR_CUDA) return fail(status, "banded CG: a wait on the shared-memory matrix ring timed out");
   if (status == ADFEM_ERR_NOT_CONVERGED)
     return fail(status, "CG did not reach rtol within max_iter (relres " + std::to_string(relres) + ")");
   return ADFEM_OK;

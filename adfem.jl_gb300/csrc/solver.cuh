@@ -19,12 +19,14 @@ struct CgState {
   double rr64;         // last FP64 true-residual norm^2 (mixed) / final check
   int iters;           // inner iterations done
   int max_iter;
-  int done;            // 0 running, 1 converged, 2 breakdown, 3 residual replacement due, 4 max_iter
+  int done;            // 0 running, 1 converged, 2 breakdown, 3 residual replacement due, 4 max_iter,
+                       // 5 a bounded wait inside a kernel gave up (see fault)
   int updates;         // residual replacements done (mixed)
   int final_req;       // the last replacement was requested because the recurrence residual met rtol
   int floor_hit;       // stopped at the attainable accuracy of the FP64 residual
   int final_seen;      // mixed: a replacement requested by rtol has already failed the true-residual test
   double last_rr64;    // FP64 residual norm^2 at the previous replacement (mixed: once final_seen)
+  int fault;           // banded ring variant: a wait on a shared-memory stage timed out
   unsigned counter[4]; // last-block arrival counters (returned to 0 by the last block)
 };
 
@@ -57,6 +59,9 @@ struct Solver {
   int zS = 0;              // rows per super-tile
   int zK = 0;              // super-tiles per block
   int zW = 0;              // shared-memory positions per super-tile (zS + 2 zH)
+  int zns = 0;             // stages of the shared-memory matrix ring (0: the plain variant)
+  bool zrefill = true;     // the ring serves every row (else only the first zns stages)
+  bool zpdl = true;        // iterations launched as programmatic dependent launches
   int64_t zL = 0;
   size_t zsmem = 0;
   DevBuf z1, zq1;          // second buffers of the Z and q^ ping-pong pairs (first: r32, q32)

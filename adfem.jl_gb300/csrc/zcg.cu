@@ -66,6 +66,8 @@ struct ZcgArgs {
   float* yl;
   CgState* st;
   double* partials;
+  int ns;      // stages of the matrix ring (RING variants; 0 otherwise)
+  int refill;  // RING: 1 the ring is refilled through phase 2, 0 only the first ns stages come through it
 };
 
 // Lanes of the current node pair (rows 2a, 2a+1 sit in lanes 2j, 2j+1 of a warp): the
@@ -92,6 +94,15 @@ __device__ __forceinline__ unsigned pair_mask() { return 3u << (threadIdx.x & 30
 #ifndef ADFEM_ZCG_KEEP_STORES
 #define ADFEM_ZCG_KEEP_STORES 1
 #endif
+// With WRED 3: 1 (default) sums the four dot products with the transposed warp reduction
+// (reduce4_arrive / reduce4_finish, 12 shuffles per warp) and issues the q^ stores of each
+// thread's last rows after its block's partials are out; 0 with one butterfly per quantity
+// (40 shuffles) after all stores.  After phase 2 the reduction's shuffles wait behind the
+// SM's queued global stores: per-block timestamps at 4M DOF gave 2.4 us from the end of
+// phase 2 to the warp sums with 40 shuffles, 1.8 us with 12.
+#ifndef ADFEM_ZCG_RED4
+#define ADFEM_ZCG_RED4 1
+#endif
 __device__ __forceinline__ uint64_t l2_evict_first_policy() {
   uint64_t p;
   asm volatile("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(p));
@@ -111,6 +122,62 @@ __device__ __forceinline__ float ld_stream(const float* a, uint64_t pol) {
   return v;
 }
 
+// Programmatic dependent launch (launches with the programmatic-serialization attribute):
+// wait for the previous grid in the stream to complete with its memory visible (a no-op
+// when launched without the attribute), and let the next grid be scheduled.
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void pdl_trigger() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+
+// ---- the matrix ring of the RING variants: each stage holds the fixed-width values of
+// BT consecutive rows (contiguous in global memory), copied by the bulk-copy engine
+// (cp.async.bulk, this GPU's memory into this CTA's shared memory) and tracked by a
+// full and an empty mbarrier per stage.
+static constexpr int kZMaxStages = 4;
+__device__ __forceinline__ uint32_t smem_addr(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+__device__ __forceinline__ void mbar_init(uint64_t* b, unsigned count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(b)), "r"(count) : "memory");
+}
+// makes the initialised barriers visible to the bulk-copy engine (async proxy)
+__device__ __forceinline__ void mbar_init_fence() {
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* b, unsigned bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(b)), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ void mbar_arrive(uint64_t* b) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_addr(b)) : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* b, unsigned parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}"
+      : "=r"(ok)
+      : "r"(smem_addr(b)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+// Waits for the phase of the given parity to complete; gives up after 2^31 SM cycles
+// (about a second) and returns false.
+__device__ __forceinline__ bool mbar_wait(uint64_t* b, unsigned parity) {
+  if (mbar_try_wait(b, parity)) return true;
+  const long long t0 = clock64();
+  while (!mbar_try_wait(b, parity))
+    if (clock64() - t0 > (1ll << 31)) return false;
+  return true;
+}
+// global -> shared bulk copy (16-byte aligned addresses, size a multiple of 16) completing
+// on the mbarrier, with an L2 cache policy
+__device__ __forceinline__ void bulk_load(void* dst, const void* src, unsigned bytes, uint64_t* bar, uint64_t pol) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes.L2::cache_hint [%0], [%1], %2, [%3], %4;" ::"r"(
+          smem_addr(dst)),
+      "l"(src), "r"(bytes), "r"(smem_addr(bar)), "l"(pol)
+      : "memory");
+}
+
 // Positions and row indices are 32-bit (the plan requires n and the fixed-width layout
 // to stay below 2^31).  A warp's 32 rows are one slice (block ranges and super-tiles are
 // multiples of 32 rows), so the pattern/no-pattern branch is warp-uniform.
@@ -121,15 +188,31 @@ __device__ __forceinline__ float ld_stream(const float* a, uint64_t pol) {
 // preconditioner is then the node-block Jacobi M = blockdiag(K_aa) (2x2 per node): a row
 // and its partner are neighbouring lanes of one warp (block ranges, windows and tiles
 // start at even rows), so M and M^-1 are applied with one lane shuffle.
-template <int MAXW, int BT, int U1, int U2, bool B2>
+//
+// RING: phase 2 reads the matrix values from a shared-memory ring of A.ns stages of BT
+// rows each, filled by bulk copies that thread 0 issues; the first stages are issued at
+// kernel entry (the values do not depend on the iteration), so they load during phase 1
+// and the phase barrier.  A row's diagonal and slice pattern id are loaded one stage
+// ahead into registers.  Thread 0 refills a stage once every warp has released it.
+// The arithmetic and its order are those of the plain variant, so the iterates are
+// bit-identical.
+template <int MAXW, int BT, int U1, int U2, bool B2, bool RING>
 __global__ void __launch_bounds__(BT, 1024 / BT) k_zcg_iter(ZcgArgs A) {
   static_assert(MAXW % 4 == 0, "pattern rows are loaded as int4");
+  extern __shared__ __align__(128) float zsm[];
+  const int stagef = RING ? BT * A.zw : 0;                        // floats per ring stage
+  float* ring = zsm;                                              // RING: A.ns stages (16-byte aligned)
+  int* spool = reinterpret_cast<int*>(zsm + (RING ? A.ns * stagef : 0));  // column patterns
+  float* sP = reinterpret_cast<float*>(spool) + ((A.npool + 3) & ~3);    // P_k of the super-tile's positions
+  // (the column patterns are fixed for the solve: copied while the previous launch may
+  // still be finishing)
+  for (int j = threadIdx.x; j < A.npool; j += BT) spool[j] = __ldg(A.pool + j);
+  // programmatic dependent launch: this launch's blocks start as the previous launch's
+  // blocks exit; the state and the vectors are read only after it has completed
+  pdl_wait();
+  pdl_trigger();
   CgState* st = A.st;
   if (st->done) return;
-  extern __shared__ float zsm[];
-  int* spool = reinterpret_cast<int*>(zsm);           // column patterns (16-byte aligned)
-  float* sP = zsm + ((A.npool + 3) & ~3);             // P_k of the super-tile's positions
-  for (int j = threadIdx.x; j < A.npool; j += BT) spool[j] = __ldg(A.pool + j);
   const int it = st->iters;
   const int cur = it & 1, nxt = cur ^ 1;
   const float* __restrict__ zprev = A.z[cur];
@@ -169,12 +252,73 @@ __global__ void __launch_bounds__(BT, 1024 / BT) k_zcg_iter(ZcgArgs A) {
   const int bhi = min(blo + (int)A.L, n);
   float pq = 0.f, pkq = 0.f, qq = 0.f, rr = 0.f;
 
+  // ---- RING: stage t covers chunk c of super-tile j (t = j * cs + c, cs chunks of BT rows
+  // per full super-tile); the copy is rounded up to whole 32-row slices (the fixed-width
+  // layout holds every slice in full, padding included)
+  __shared__ uint64_t s_full[RING ? kZMaxStages : 1], s_empty[RING ? kZMaxStages : 1];
+  __shared__ int s_fault;
+  int nstage = 0, t = 0;
+  bool fault = false;
+  auto issue = [&](int ts) {
+    const int cs = (A.S + BT - 1) / BT;
+    const int j = ts / cs;
+    const int r0 = blo + j * A.S + (ts - j * cs) * BT;
+    const int r1 = min(min(r0 + BT, blo + (j + 1) * A.S), bhi);
+    const int slot = ts % A.ns;
+    const unsigned bytes = (unsigned)(((r1 - r0 + 31) & ~31) * zw) * (unsigned)sizeof(float);
+    mbar_expect_tx(&s_full[slot], bytes);
+    bulk_load(ring + slot * stagef, A.val + (size_t)r0 * zw, bytes, &s_full[slot], pol);
+  };
+  if constexpr (RING) {
+    const int cs = (A.S + BT - 1) / BT;
+    const int nsup = (bhi - blo + A.S - 1) / A.S;
+    nstage = (nsup - 1) * cs + (bhi - blo - (nsup - 1) * A.S + BT - 1) / BT;
+    if (tid == 0) {
+      s_fault = 0;
+      for (int s = 0; s < A.ns; s++) {
+        mbar_init(&s_full[s], 1);
+        mbar_init(&s_empty[s], BT / 32);
+      }
+      mbar_init_fence();
+      for (int ts = 0; ts < min(A.ns, nstage); ts++) issue(ts);
+    }
+    if (!A.refill) nstage = min(A.ns, nstage);  // stages that go through the ring
+  }
+  // q^ of the rows of this thread's last trip, not yet stored: rows dbase + u BT, u < dcnt
+  float dq[U2];
+  int dbase = 0, dcnt = 0;
+  auto put = [&](int i, float qh) {
+    if constexpr (ADFEM_ZCG_KEEP_STORES) st_keep(qnew + i, qh, keep);
+    else qnew[i] = qh;
+  };
+  auto flush = [&]() {
+#pragma unroll
+    for (int u = 0; u < U2; u++)
+      if (u < dcnt) put(dbase + u * BT, dq[u]);
+    dcnt = 0;
+  };
+  // RING: diagonal (block row) and slice pattern id of this thread's row in the next stage
+  float nd = 0.f, nc = 0.f;
+  int npid = -1;
+  auto fetch_dc = [&](int i, float& d, float& c, int& pid) {
+    if constexpr (B2) {
+      const float2 b = __ldg(A.bz + i);
+      d = b.x;
+      c = b.y;
+    } else {
+      d = __ldg(A.dz + i);
+      c = 0.f;
+    }
+    pid = __ldg(A.zpid + (i >> 5));
+  };
+
   for (int lo = blo; lo < bhi; lo += A.S) {
     const int hi = min(lo + A.S, bhi);
     // (B2: the window starts and ends at even positions, so lane pairs hold node pairs)
     const int wlo = B2 ? (max(lo - A.H, 0) & ~1) : max(lo - A.H, 0);
     const int whi = B2 ? min((hi + A.H + 1) & ~1, n) : min(hi + A.H, n);
     if (lo != blo) __syncthreads();  // the previous super-tile's gathers are done
+    if (RING && lo + tid < hi) fetch_dc(lo + tid, nd, nc, npid);
     // ---- phase 1: P_k for [wlo, whi) into shared memory; Z, P, Y of own rows.  All loads
     // of a trip (U1 positions per thread) are issued before any store.
     struct In {
@@ -243,7 +387,7 @@ __global__ void __launch_bounds__(BT, 1024 / BT) k_zcg_iter(ZcgArgs A) {
     }
     __syncthreads();
     // ---- phase 2: q = K P_k for the rows [lo, hi)
-    auto row = [&](int i, const float (&v)[MAXW], float d, float c, int pid) {
+    auto row = [&](int i, const float (&v)[MAXW], float d, float c, int pid) -> float {
       const float Pi = sP[i - wlo];
       const float Pp = B2 ? sP[(i ^ 1) - wlo] : Pi;  // partner DOF (B2: rows come in even/odd pairs)
       const int dpart = (i & 1) ? -1 : 1;            // column delta of the partner DOF
@@ -289,11 +433,10 @@ __global__ void __launch_bounds__(BT, 1024 / BT) k_zcg_iter(ZcgArgs A) {
       } else {
         qh = __fdiv_rn(s, d);
       }
-      if constexpr (ADFEM_ZCG_KEEP_STORES) st_keep(qnew + i, qh, keep);
-      else qnew[i] = qh;
       pq = fmaf(Pi, s, pq);
       qq = fmaf(s, qh, qq);
       if (full_zq) pkq = fmaf(__ldg(pprev + i), s, pkq);
+      return qh;
     };
     // fixed-width layout: entry k of row i at (i>>5)*32*zw + 32k + (i&31) (padding: value 0,
     // delta 0), so the loads of a row depend on nothing but i
@@ -311,20 +454,65 @@ __global__ void __launch_bounds__(BT, 1024 / BT) k_zcg_iter(ZcgArgs A) {
       }
       pid = __ldg(A.zpid + (i >> 5));
     };
-    int i = lo + tid;
+    int c0 = lo;
+    if constexpr (RING) {
+      // one row per thread and stage; the stage's local layout is the global one (slice
+      // tid/32, entry k of lane tid%32 at 32k)
+      for (; c0 < hi && (A.refill || t < A.ns); c0 += BT, t++) {
+        const int i = c0 + tid;
+        const float d = nd, c = nc;
+        const int pid = npid;
+        if (i + BT < hi) fetch_dc(i + BT, nd, nc, npid);
+        const int slot = t % A.ns;
+        const unsigned par = (unsigned)(t / A.ns) & 1u;
+        if (!mbar_wait(&s_full[slot], par)) fault = true;
+        if (i < hi) {
+          const float* sv = ring + slot * stagef + (tid >> 5) * (32 * zw) + (tid & 31);
+          float v[MAXW];
+#pragma unroll
+          for (int k = 0; k < MAXW; k++) v[k] = k < zw ? sv[32 * k] : 0.f;
+          put(i, row(i, v, d, c, pid));
+        }
+        __syncwarp();
+        if ((tid & 31) == 0) mbar_arrive(&s_empty[slot]);
+        if (tid == 0 && A.refill && t + A.ns < nstage) {
+          if (!mbar_wait(&s_empty[slot], par)) fault = true;
+          issue(t + A.ns);
+        }
+      }
+    }
+    // rows not served by the ring: loaded by the threads; the q^ of a trip is stored after
+    // the next trip's loads are issued (or at the end of the launch)
+    int i = c0 + tid;
     for (; i + (U2 - 1) * BT < hi; i += U2 * BT) {  // U2 rows per thread and trip, loads first
       float v[U2][MAXW], d[U2], c[U2];
       int pid[U2];
 #pragma unroll
       for (int u = 0; u < U2; u++) fetch(i + u * BT, v[u], d[u], c[u], pid[u]);
+      flush();
 #pragma unroll
-      for (int u = 0; u < U2; u++) row(i + u * BT, v[u], d[u], c[u], pid[u]);
+      for (int u = 0; u < U2; u++) dq[u] = row(i + u * BT, v[u], d[u], c[u], pid[u]);
+      dbase = i;
+      dcnt = U2;
     }
     for (; i < hi; i += BT) {
-      float v0[MAXW], d0, c0;
+      float v0[MAXW], d0, cc0;
       int g0;
-      fetch(i, v0, d0, c0, g0);
-      row(i, v0, d0, c0, g0);
+      fetch(i, v0, d0, cc0, g0);
+      flush();
+      dq[0] = row(i, v0, d0, cc0, g0);
+      dbase = i;
+      dcnt = 1;
+    }
+  }
+  if constexpr (RING) {
+    // a wait that gave up: the stages still in flight are waited for (again bounded), so no
+    // copy lands in the shared memory of a finished block, and the solve stops with done = 5
+    if (fault) s_fault = 1;
+    __syncthreads();
+    if (s_fault && tid == 0) {
+      for (int ts = max(0, nstage - A.ns); ts < nstage; ts++) mbar_wait(&s_full[ts % A.ns], (unsigned)(ts / A.ns) & 1u);
+      atomicExch(&st->fault, 1);
     }
   }
 
@@ -333,7 +521,17 @@ __global__ void __launch_bounds__(BT, 1024 / BT) k_zcg_iter(ZcgArgs A) {
   // last block spend no FP64 instruction on the critical path between two launches
   float v[4] = {pq, pkq, qq, rr};
   float2 tot2[4];
+#if ADFEM_ZCG_RED4
+  const bool lastb = reduce4_arrive<BT>(v, reinterpret_cast<float2*>(A.partials), &st->counter[0]);
+  // the deferred q^ stores go out once the block is counted in; warp 0 of the last block
+  // stores after the step lengths (the fence of reduce4_finish would wait for them)
+  const bool w0last = lastb && (threadIdx.x >> 5) == 0;
+  if (!w0last) flush();
+  if (w0last) reduce4_finish<BT>(reinterpret_cast<float2*>(A.partials), &st->counter[0], tot2);
+#else
+  flush();
   const bool lastb = reduce_grid_pair<4, BT>(v, reinterpret_cast<float2*>(A.partials), &st->counter[0], tot2);
+#endif
   if (lastb && threadIdx.x == 0) {
     const float2 pq2 = tot2[0], qq2 = tot2[2], rho2 = tot2[3];
     // decisions in pair arithmetic against the thresholds prepared at entry: no dependent
@@ -341,7 +539,9 @@ __global__ void __launch_bounds__(BT, 1024 / BT) k_zcg_iter(ZcgArgs A) {
     float2 zq2 = pq2;
     if (full_zq && s_sc[1] != 0.0)
       zq2 = d_to_df((df_to_d(pq2) - s_sc[2] * df_to_d(tot2[1])) / s_sc[1]);  // after a replacement only
-    if (!isfinite(rho2.x) || !isfinite(pq2.x)) {
+    if (RING && *reinterpret_cast<volatile int*>(&st->fault)) {
+      st->done = 5;
+    } else if (!isfinite(rho2.x) || !isfinite(pq2.x)) {
       st->done = 2;
     } else if (df_le(rho2, s_th[0])) {
       st->final_req = 1;
@@ -364,7 +564,11 @@ __global__ void __launch_bounds__(BT, 1024 / BT) k_zcg_iter(ZcgArgs A) {
       st->iters = it + 1;
     }
   }
+#if ADFEM_ZCG_RED4
+  if (w0last) flush();
+#endif
 #else
+  flush();
   double tot[4];
   bool lastb;
   if constexpr (ADFEM_ZCG_WRED) {
@@ -377,7 +581,9 @@ __global__ void __launch_bounds__(BT, 1024 / BT) k_zcg_iter(ZcgArgs A) {
   if (lastb && threadIdx.x == 0) {
     const double pqd = tot[0], qqd = tot[2], rho = tot[3];
     const double zqd = (full_zq && st->ar != 0.0) ? (pqd - st->ap * tot[1]) / st->ar : pqd;
-    if (!isfinite(rho) || !isfinite(pqd)) {
+    if (RING && *reinterpret_cast<volatile int*>(&st->fault)) {
+      st->done = 5;
+    } else if (!isfinite(rho) || !isfinite(pqd)) {
       st->done = 2;
     } else if (rho <= st->stop2) {
       st->final_req = 1;
@@ -615,6 +821,10 @@ static constexpr int kZPerSM = 1024 / kZBT;          // resident blocks per SM (
 #endif
 static constexpr int kZU1 = ADFEM_ZCG_U1;            // phase-1 positions per thread and trip
 static constexpr int kZU2 = ADFEM_ZCG_U2;            // phase-2 matrix rows per thread and trip
+#ifndef ADFEM_ZCG_U1_RING
+#define ADFEM_ZCG_U1_RING 3
+#endif
+static constexpr int kZU1R = ADFEM_ZCG_U1_RING;      // phase-1 positions per thread and trip, ring variant
 #ifndef ADFEM_ZCG_U2_WIDE
 #define ADFEM_ZCG_U2_WIDE 1
 #endif
@@ -622,6 +832,10 @@ static constexpr int kZU2 = ADFEM_ZCG_U2;            // phase-2 matrix rows per 
 // per thread (they spill)
 static constexpr int kZU2W = ADFEM_ZCG_U2_WIDE;
 static constexpr size_t kZSmemBlock = (kZPerSM >= 2 ? 100 : 200) * 1024;  // shared memory per block
+// ring variants: window + pattern pool + ring stages (the static shared memory of the
+// kernel -- reductions, scalars, mbarriers, ~1.2 KB -- comes on top, within the 227 KB a
+// block may hold)
+static constexpr size_t kZSmemRing = 225 * 1024;
 
 // Distinct slice column patterns (at most kZMaxPatterns; further slices use their
 // per-entry deltas), padded to the kernel's unrolled width per row parity, and the
@@ -669,9 +883,10 @@ static int zcg_build_pool(Solver& S) {
   return ADFEM_OK;
 }
 
-template <int MAXW, bool B2>
+template <int MAXW, bool B2, bool RING = false>
 static int zcg_configure(Solver& S, int sms) {
-  auto kern = k_zcg_iter<MAXW, kZBT, kZU1, (MAXW > 8 ? kZU2W : kZU2), B2>;
+  auto kern = k_zcg_iter<MAXW, kZBT, (RING ? kZU1R : kZU1), (MAXW > 8 ? kZU2W : kZU2), B2, RING>;
+  const size_t limit = RING ? kZSmemRing : kZSmemBlock;
   // The shared-memory limit is raised once per process to the most any plan uses:
   // changing a kernel's attributes while another thread captures a graph with that
   // kernel invalidates the capture.
@@ -679,10 +894,10 @@ static int zcg_configure(Solver& S, int sms) {
   static cudaError_t set_err = cudaSuccess;
   std::call_once(once, [&] {
     std::lock_guard<std::mutex> lk(device_alloc_mutex());
-    set_err = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kZSmemBlock);
+    set_err = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)limit);
   });
   if (set_err != cudaSuccess) return cuda_fail(set_err, "cudaFuncSetAttribute");
-  if (S.zsmem > kZSmemBlock) return fail(ADFEM_ERR_INVALID, "banded CG plan exceeds its shared-memory limit");
+  if (S.zsmem > limit) return fail(ADFEM_ERR_INVALID, "banded CG plan exceeds its shared-memory limit");
   int per = 0;
   ADFEM_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kern, kZBT, S.zsmem));
   if (per < 1) return fail(ADFEM_ERR_CUDA, "banded CG kernel cannot be resident");
@@ -725,9 +940,33 @@ int zcg_plan(Solver& S, int sms) {
   S.zH = H;
   S.zW = S.zS + 2 * H + 2;  // (+2: windows of 2-DOF operators are widened to even ends)
   S.zsmem = pool_bytes + sizeof(float) * (size_t)S.zW;
+  // the matrix ring (8-wide operators, opt-in with ADFEM_ZCG_RING=2..4: at most that many
+  // stages of kZBT rows, as many as fit beside the window, at least 2).  Measured slower on
+  // GB300 at 4M DOF (71 us per iteration with 3 stages, 69 with 2, against 50 for the
+  // plain variant; only the first stages through the ring: 64 / 55 us): the larger shared-
+  // memory footprint leaves less L1 for the loads in flight of phase 1 and of the rows the
+  // threads load (phase 1 19 -> 29 us with 3 stages), and one refill per stage after every
+  // warp released it keeps too few bytes in flight in phase 2.
+  S.zns = 0;
+  const char* renv = std::getenv("ADFEM_ZCG_RING");
+  if (A.maxw <= 8 && renv && renv[0] >= '2' && renv[0] <= '9') {
+    const int cap = std::min(kZMaxStages, std::atoi(renv));
+    const size_t stage = sizeof(float) * (size_t)kZBT * (size_t)S.zw;
+    for (int ns = cap; ns >= 2; ns--)
+      if (S.zsmem + ns * stage <= kZSmemRing) {
+        S.zns = ns;
+        break;
+      }
+    S.zsmem += S.zns * stage;
+    const char* fenv = std::getenv("ADFEM_ZCG_RING_REFILL");
+    S.zrefill = !(fenv && fenv[0] == '0');
+  }
+  const char* penv = std::getenv("ADFEM_ZCG_PDL");
+  S.zpdl = !(penv && penv[0] == '0');
   // (the block form is decided after the layout pass below; both 16-wide variants have
   // the same resources, so the plan is made with the plain one)
-  if (A.maxw <= 8) ADFEM_TRY((zcg_configure<8, false>(S, sms)));
+  if (A.maxw <= 8 && S.zns) ADFEM_TRY((zcg_configure<8, false, true>(S, sms)));
+  else if (A.maxw <= 8) ADFEM_TRY((zcg_configure<8, false>(S, sms)));
   else ADFEM_TRY((zcg_configure<16, false>(S, sms)));
   if (A.maxw > 8) ADFEM_TRY((zcg_configure<16, true>(S, sms)));
   const size_t n4 = sizeof(float) * (size_t)S.n;
@@ -797,14 +1036,36 @@ static ZcgArgs zcg_args(Solver& S) {
   z.yl = S.yl32.as<float>();
   z.st = S.state.as<CgState>();
   z.partials = S.partials.as<double>();
+  z.ns = S.zns;
+  z.refill = S.zrefill ? 1 : 0;
   return z;
+}
+
+// Launch with the programmatic-serialization attribute (S.zpdl): in a stream or a captured
+// graph, the next iteration's blocks are scheduled as this one's exit and wait inside the
+// kernel (griddepcontrol.wait) for its completion, which hides the launch latency between
+// two iterations.
+template <class Kern>
+static void zlaunch(Kern kern, const Solver& S, cudaStream_t st, const ZcgArgs& z) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3((unsigned)S.zgrid);
+  cfg.blockDim = dim3(kZBT);
+  cfg.dynamicSmemBytes = S.zsmem;
+  cfg.stream = st;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  at[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = S.zpdl ? 1 : 0;
+  cudaLaunchKernelEx(&cfg, kern, z);
 }
 
 void zcg_enqueue_iter(Solver& S, cudaStream_t st) {
   const ZcgArgs z = zcg_args(S);
-  if (S.A->maxw <= 8) k_zcg_iter<8, kZBT, kZU1, kZU2, false><<<S.zgrid, kZBT, S.zsmem, st>>>(z);
-  else if (S.zblock2) k_zcg_iter<16, kZBT, kZU1, kZU2W, true><<<S.zgrid, kZBT, S.zsmem, st>>>(z);
-  else k_zcg_iter<16, kZBT, kZU1, kZU2W, false><<<S.zgrid, kZBT, S.zsmem, st>>>(z);
+  if (S.A->maxw <= 8 && S.zns) zlaunch(k_zcg_iter<8, kZBT, kZU1R, kZU2, false, true>, S, st, z);
+  else if (S.A->maxw <= 8) zlaunch(k_zcg_iter<8, kZBT, kZU1, kZU2, false, false>, S, st, z);
+  else if (S.zblock2) zlaunch(k_zcg_iter<16, kZBT, kZU1, kZU2W, true, false>, S, st, z);
+  else zlaunch(k_zcg_iter<16, kZBT, kZU1, kZU2W, false, false>, S, st, z);
 }
 
 void zcg_enqueue_init(Solver& S, cudaStream_t st, const double* rhs, const uint8_t* zero_rows, const double* u0,

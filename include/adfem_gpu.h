@@ -395,6 +395,8 @@ typedef struct adfem_solver_info {
   int banded_fp64;            /* 1: FP64 solves use the one-kernel banded FP64 iteration (same layout and
                                  fusion as the mixed one), 0: the three-kernel FP64 iteration */
   int fp64_tile_rows;         /* rows per super-tile of the banded FP64 iteration (0 if not used) */
+  int ring_stages;            /* stages of the shared-memory matrix ring of the banded mixed iteration
+                                 (bulk copies of 1024 rows each; 0: values loaded by the threads) */
 } adfem_solver_info;
 ADFEM_API int adfem_system_solver_info(const adfem_system *sys, adfem_solver_info *info);
 /* Packed solves of small systems: the systems (each assembled, at most 65536 DOFs,

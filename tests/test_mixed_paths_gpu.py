@@ -198,3 +198,67 @@ def test_system_reports_banded_layout(oracle, gpulib, monkeypatch):
     assert info["ring"] >= 2 * info["band"] + 32
     u = S.solve(precision="mixed", rtol=RTOL_MIXED)
     assert rel(u.cpu().numpy(), oracle.spsolve(B, r)) < ERR_BAR
+
+
+def _ring_system(gpulib, m):
+    import torch
+
+    coords, elems = synth.jittered_square(m, seed=2)
+    mesh = gpulib.Mesh(coords, elems)
+    g = gpulib.gauss_nodes(mesh)
+    G = synth.fourier_field(g[:, 0], g[:, 1], seed=1)
+    kappa = 1 + np.exp(synth.contrast_sigma(G, 1e3) * G)
+    f = 1e5 * (g[:, 0] + g[:, 1])
+    S = gpulib.PoissonSystem(mesh)
+    S.set_dirichlet(gpulib.bcnode(mesh))
+    S.assemble(torch.tensor(kappa, device="cuda"), torch.tensor(f, device="cuda"))
+    return S
+
+
+@pytest.mark.parametrize("ring,smax,refill", [("3", "", "1"), ("2", "", "1"), ("3", "1504", "1"), ("2", "2080", "1"),
+                                              ("2", "", "0")])
+def test_matrix_ring_bit_identical_to_plain_variant(gpulib, monkeypatch, ring, smax, refill):
+    """The opt-in ring variant of the banded mixed iteration (matrix values streamed into
+    shared memory by bulk copies; refill 0: only the first stages) does the plain variant's
+    arithmetic in the same order: same iterations, bit-identical solution.  1M DOF: several
+    ring refills per block; with a super-tile cap the stages straddle no super-tile (partial
+    stages at each tile's end).  Both variants run as programmatic dependent launches."""
+    monkeypatch.delenv("ADFEM_ZCG", raising=False)
+    monkeypatch.delenv("ADFEM_ZCG_PDL", raising=False)
+    monkeypatch.setenv("ADFEM_ZCG_RING_REFILL", refill)
+    if smax:
+        monkeypatch.setenv("ADFEM_ZCG_SMAX", smax)
+    else:
+        monkeypatch.delenv("ADFEM_ZCG_SMAX", raising=False)
+    monkeypatch.delenv("ADFEM_ZCG_RING", raising=False)
+    plain = _ring_system(gpulib, 1000)
+    monkeypatch.setenv("ADFEM_ZCG_RING", ring)
+    ringed = _ring_system(gpulib, 1000)
+    ip, ir = plain.solver_info(), ringed.solver_info()
+    assert ip["banded"] == 1 and ip["ring_stages"] == 0
+    assert ir["banded"] == 1 and ir["ring_stages"] == int(ring)
+    assert ir["rows_per_block"] > 3 * 1024  # refills happen
+    u0 = plain.solve(precision="mixed", rtol=RTOL_MIXED)
+    s0 = plain.last_stats
+    u1 = ringed.solve(precision="mixed", rtol=RTOL_MIXED)
+    s1 = ringed.last_stats
+    assert s0.status == 0 and s1.status == 0 and s0.relres <= 1e-10
+    assert s1.iterations == s0.iterations and s1.updates == s0.updates
+    assert np.array_equal(u1.cpu().numpy(), u0.cpu().numpy())
+
+
+def test_dependent_launches_bit_identical(gpulib, monkeypatch):
+    """Programmatic dependent launches of the banded iteration (the default) change only when
+    a launch's blocks start: same iterations and bit-identical solution as plain launches."""
+    monkeypatch.delenv("ADFEM_ZCG", raising=False)
+    monkeypatch.delenv("ADFEM_ZCG_RING", raising=False)
+    monkeypatch.delenv("ADFEM_ZCG_SMAX", raising=False)
+    monkeypatch.setenv("ADFEM_ZCG_PDL", "0")
+    plain = _ring_system(gpulib, 600)
+    monkeypatch.delenv("ADFEM_ZCG_PDL", raising=False)
+    dep = _ring_system(gpulib, 600)
+    u0 = plain.solve(precision="mixed", rtol=RTOL_MIXED)
+    u1 = dep.solve(precision="mixed", rtol=RTOL_MIXED)
+    assert plain.last_stats.status == 0 and dep.last_stats.status == 0
+    assert dep.last_stats.iterations == plain.last_stats.iterations
+    assert np.array_equal(u1.cpu().numpy(), u0.cpu().numpy())
