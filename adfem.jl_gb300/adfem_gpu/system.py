@@ -120,21 +120,26 @@ class _System:
 
 
 class PoissonSystem(_System):
-    """-div(kappa grad u) = f on a P1 mesh with u = bdval on the Dirichlet nodes."""
+    """-div(kappa grad u) = f on a P1 or P2 mesh with u = bdval on the Dirichlet DOFs
+    (kappa and f at the mesh's Gauss points: 3 per element for P1, 6 for P2)."""
 
     kind = _lib.SYS_POISSON
 
     def assemble(self, kappa, f):
-        ng = 3 * self.mesh.nelem
+        from . import get_ngauss
+
+        ng = get_ngauss(self.mesh)
         _dev(kappa, ng, "kappa")
         _dev(f, ng, "f")
         check(_lib.load().adfem_system_assemble_poisson_d(self._h, ptr(kappa), ptr(f), _cur_stream()), "assemble")
 
     def grad_kappa(self, u, lam):
+        from . import get_ngauss
+
         torch = _torch()
         _dev(u, self.ndof, "u")
         _dev(lam, self.ndof, "lam")
-        g = torch.empty(3 * self.mesh.nelem, dtype=torch.float64, device="cuda")
+        g = torch.empty(get_ngauss(self.mesh), dtype=torch.float64, device="cuda")
         check(_lib.load().adfem_system_grad_kappa_d(self._h, ptr(u), ptr(lam), ptr(g), _cur_stream()), "grad_kappa")
         return g
 

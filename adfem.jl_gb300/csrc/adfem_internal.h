@@ -50,6 +50,7 @@ struct NvtxRange {
 int check_line_solver();
 int check_line_zcg();
 int check_line_assemble();
+int check_line_generic();
 
 bool injected_alloc_failure();
 void arm_alloc_failure(long long k);
@@ -277,6 +278,18 @@ cudaError_t launch_gen_stiffness_matrix(const Mesh& m, const Space& sp, const do
                                         bool transpose, cudaStream_t st);
 cudaError_t launch_gen_source(const Mesh& m, const Space& sp, const double* f, double* rhs, bool accumulate,
                               cudaStream_t st);
+// resident P2 (or P1) Poisson system from the space sp: element matrices into ke (nd^2
+// per element), then Laplace rows + load + Dirichlet into the system's sliced-ELL values
+// (sptr; nperm / kperm as for launch_poisson_system; diagpos_space: diagonal slot of each
+// space pattern row); isbd, bdval, rhs in solver order
+cudaError_t launch_gen_poisson_system(const Mesh& m, const Space& sp, const double* kappa, const double* f, double* ke,
+                                      const uint8_t* isbd, const double* bdval, double* sell_vals, double* rhs,
+                                      const int32_t* sptr, const int32_t* diagpos_space, const int32_t* nperm,
+                                      const uint8_t* kperm, cudaStream_t st);
+// dL/dkappa per Gauss point of sp's rule: -w_k grad(lam).grad(u), lam zero where
+// isbd_space == 1 (u, lam in space order)
+cudaError_t launch_gen_kappa_grad(const Mesh& m, const Space& sp, const double* u, const double* lam,
+                                  const uint8_t* isbd_space, double* grad_kappa, cudaStream_t st);
 cudaError_t launch_gen_source_backward(const Mesh& m, const Space& sp, const double* grad_rhs, double* grad_f,
                                        cudaStream_t st);
 // values at the Gauss points of the mesh's rule: through the P1 shape of the vertices

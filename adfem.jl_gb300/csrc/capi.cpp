@@ -46,6 +46,8 @@ struct adfem_system {
   DevBuf dofmap;     // int32 [ndof] reference DOF -> solver DOF (elasticity or renumbered)
   DevBuf rhs;        // double [ndof]
   DevBuf sigma, src3, srcy3, Dbar;  // per-element scratch
+  DevBuf ke;                        // P2 Poisson: element matrices (36 per element)
+  DevBuf sdiag;                     // P2 Poisson: diagonal slot of each space pattern row
   DevBuf t0, t1, t2;                // ndof scratch (interleaving, host staging)
   DevBuf in0, in1;                  // host-staging of per-Gauss-point inputs
   Solver solver;
@@ -114,10 +116,15 @@ int system_set_bd(adfem_system* s, const long long* bd, long long nbd, const dou
     val[q] = bdval ? bdval[k] : 0.0;
   }
   const int nc = el ? 2 : 1;
-  for (int64_t i = 0; i < m.nv; i++) {
+  // the scalar pattern of the operator: the mesh's, or the P2 space's (built at creation)
+  const Space* sp = m.degree == 2 ? m.space[2].get() : nullptr;
+  const int64_t nn = sp ? sp->ndof : m.nv;
+  const std::vector<int32_t>& RP = sp ? sp->rowptr : m.rowptr;
+  const std::vector<int32_t>& CI = sp ? sp->colind : m.colind;
+  for (int64_t i = 0; i < nn; i++) {
     bool near = false;
-    for (int32_t k = m.rowptr[i]; k < m.rowptr[i + 1]; k++)
-      for (int c = 0; c < nc; c++) near |= tag[sdof(m.colind[k], c)] == 1;
+    for (int32_t k = RP[i]; k < RP[i + 1]; k++)
+      for (int c = 0; c < nc; c++) near |= tag[sdof(CI[k], c)] == 1;
     if (!near) continue;
     for (int c = 0; c < nc; c++)
       if (tag[sdof(i, c)] == 0) {
@@ -1005,56 +1012,79 @@ int adfem_system_create(adfem_mesh* mesh, int kind, adfem_system** out) {
   if (!mesh || !out) return fail(ADFEM_ERR_INVALID, "null argument");
   if (kind != ADFEM_SYS_POISSON && kind != ADFEM_SYS_ELASTICITY) return fail(ADFEM_ERR_INVALID, "unknown kind");
   *out = nullptr;
-  if (mesh->m->degree != 1)
-    return fail(ADFEM_ERR_UNSUPPORTED, "resident systems are built on P1 meshes (assemble P2 operators and use "
-                                       "adfem_csc_solve)");
   std::unique_ptr<adfem_system> s(new adfem_system());
   s->mesh = mesh;
   s->kind = kind;
   Mesh& m = *mesh->m;
+  const bool p2 = m.degree == 2;
+  if (p2 && kind != ADFEM_SYS_POISSON)
+    return fail(ADFEM_ERR_UNSUPPORTED, "resident elasticity systems are built on P1 meshes (assemble P2 "
+                                       "stiffness operators and use adfem_csc_solve)");
   if (kind == ADFEM_SYS_ELASTICITY && m.maxrow > 16)
     return fail(ADFEM_ERR_UNSUPPORTED, "elasticity systems support at most 15 neighbours per node");
-  // node numbering of the solver: reverse Cuthill-McKee when it at least halves the band
+  // the scalar pattern the operator lives on: the mesh's (P1, one DOF per node) or that of
+  // the P2 space (vertex DOFs, then one per edge)
+  Space* sp = nullptr;
+  if (p2) {
+    std::lock_guard<std::mutex> lk(m.mu);
+    ADFEM_TRY(mesh_space(&m, 2, &sp));
+    if (sp->maxrow > 24) return fail(ADFEM_ERR_UNSUPPORTED, "P2 systems support at most 24 entries per row");
+  }
+  const int64_t nn = p2 ? sp->ndof : m.nv;
+  const std::vector<int32_t>& RP = p2 ? sp->rowptr : m.rowptr;
+  const std::vector<int32_t>& CI = p2 ? sp->colind : m.colind;
+  int64_t band0 = m.sell.band;
+  if (p2) {
+    band0 = 0;
+    for (int64_t i = 0; i < nn; i++)
+      for (int32_t k = RP[i]; k < RP[i + 1]; k++) band0 = std::max<int64_t>(band0, std::llabs((long long)CI[k] - i));
+  }
+  // DOF numbering of the solver: reverse Cuthill-McKee when it at least halves the band
   // (not tried when the band is already within 4 sqrt(n), about what RCM reaches on a
-  // planar mesh)
+  // planar mesh; the P2 numbering -- vertices, then edges -- always has a wide band)
   {
     std::vector<int32_t> pi;
-    const bool try_rcm = (double)m.sell.band > 4.0 * std::sqrt((double)m.nv);
-    const int64_t rb = try_rcm ? mesh_rcm(m, pi) : m.sell.band;
-    s->renumbered = try_rcm && 2 * rb < m.sell.band;
+    const bool try_rcm = (double)band0 > 4.0 * std::sqrt((double)nn);
+    const int64_t rb = try_rcm ? graph_rcm(nn, RP, CI, pi) : band0;
+    s->renumbered = try_rcm && 2 * rb < band0;
     if (s->renumbered) s->hperm = std::move(pi);
     else {
-      s->hperm.resize(m.nv);
-      for (int64_t i = 0; i < m.nv; i++) s->hperm[i] = (int32_t)i;
+      s->hperm.resize(nn);
+      for (int64_t i = 0; i < nn; i++) s->hperm[i] = (int32_t)i;
     }
   }
   const std::vector<int32_t>& pi = s->hperm;
   // scalar pattern in solver order: row pi(i) holds the sorted pi(j); kp = rank of each
-  // mesh slot in its renumbered row
-  std::vector<int32_t> rpS(m.nv + 1, 0), ciS(m.nnz), dpS(m.nv);
-  std::vector<uint8_t> kp(m.nnz);
+  // pattern slot in its renumbered row
+  const int64_t nnzS = (int64_t)CI.size();
+  std::vector<int32_t> rpS(nn + 1, 0), ciS(nnzS), dpS(nn), dpRef(nn, 0);
+  std::vector<uint8_t> kp(nnzS);
   {
-    std::vector<int32_t> inv(m.nv);
-    for (int64_t i = 0; i < m.nv; i++) inv[pi[i]] = (int32_t)i;
-    for (int64_t r = 0; r < m.nv; r++) rpS[r + 1] = rpS[r] + (m.rowptr[inv[r] + 1] - m.rowptr[inv[r]]);
+    std::vector<int32_t> inv(nn);
+    for (int64_t i = 0; i < nn; i++) inv[pi[i]] = (int32_t)i;
+    for (int64_t r = 0; r < nn; r++) rpS[r + 1] = rpS[r] + (RP[inv[r] + 1] - RP[inv[r]]);
     std::vector<std::pair<int32_t, int32_t>> tmp;
-    for (int64_t i = 0; i < m.nv; i++) {
+    for (int64_t i = 0; i < nn; i++) {
       tmp.clear();
-      for (int32_t k = m.rowptr[i]; k < m.rowptr[i + 1]; k++) tmp.emplace_back(pi[m.colind[k]], k - m.rowptr[i]);
+      for (int32_t k = RP[i]; k < RP[i + 1]; k++) {
+        tmp.emplace_back(pi[CI[k]], k - RP[i]);
+        if (CI[k] == i) dpRef[i] = k - RP[i];
+      }
       std::sort(tmp.begin(), tmp.end());
       const int64_t r = pi[i];
       for (size_t q = 0; q < tmp.size(); q++) {
         ciS[rpS[r] + q] = tmp[q].first;
-        kp[m.rowptr[i] + tmp[q].second] = (uint8_t)q;
+        kp[RP[i] + tmp[q].second] = (uint8_t)q;
         if (tmp[q].first == r) dpS[r] = (int32_t)q;
       }
     }
   }
   if (kind == ADFEM_SYS_POISSON) {
-    s->ndof = m.nv;
-    ADFEM_TRY(sell_build_pattern(m.nv, rpS.data(), ciS.data(), s->A, 1));
+    s->ndof = nn;
+    ADFEM_TRY(sell_build_pattern(nn, rpS.data(), ciS.data(), s->A, 1));
     ADFEM_TRY(to_dev(s->diagpos, dpS.data(), dpS.size()));
     if (s->renumbered) ADFEM_TRY(to_dev(s->dofmap, pi.data(), pi.size()));
+    if (p2) ADFEM_TRY(to_dev(s->sdiag, dpRef.data(), dpRef.size()));
   } else {
     s->ndof = 2 * m.nv;
     std::vector<int32_t> rp2(2 * m.nv + 1, 0), dp2(2 * m.nv);
@@ -1121,6 +1151,26 @@ static int assemble_poisson(adfem_system* sys, const double* kappa_d, const doub
                             cudaEvent_t* ev) {
   Mesh& m = *sys->mesh->m;
   sys->assembled = false;
+  if (m.degree == 2) {
+    // P2: element matrices of the order-4 rule, then one pass over the DOF rows (Laplace
+    // row + load + Dirichlet into the sliced-ELL operator)
+    const Space& sp = *m.space[2];
+    ADFEM_TRY(sys->ke.alloc(sizeof(double) * 36 * (size_t)m.ne));
+    if (ev) ADFEM_CUDA(cudaEventRecord(ev[0], st));
+    if (ev) ADFEM_CUDA(cudaEventRecord(ev[1], st));
+    ADFEM_TRY(kerr(launch_gen_poisson_system(m, sp, kappa_d, f_d, sys->ke.as<double>(), sys->isbd.as<uint8_t>(),
+                                             sys->bdval.as<double>(), sys->A.val64.as<double>(),
+                                             sys->rhs.as<double>(), sys->A.sptr.as<int32_t>(),
+                                             sys->sdiag.as<int32_t>(),
+                                             sys->renumbered ? sys->nperm.as<int32_t>() : nullptr,
+                                             sys->renumbered ? sys->kperm.as<uint8_t>() : nullptr, st),
+                   "P2 poisson system"));
+    if (ev) ADFEM_CUDA(cudaEventRecord(ev[2], st));
+    ADFEM_TRY(solver_prepare(sys->solver, sys->diagpos.as<int32_t>(), st));
+    if (ev) ADFEM_CUDA(cudaEventRecord(ev[3], st));
+    sys->assembled = true;
+    return ADFEM_OK;
+  }
   ADFEM_TRY(sys->sigma.alloc(sizeof(double) * m.ne));
   ADFEM_TRY(sys->src3.alloc(sizeof(double) * 3 * m.ne));
   if (ev) ADFEM_CUDA(cudaEventRecord(ev[0], st));
@@ -1366,8 +1416,14 @@ int adfem_system_grad_kappa_d(adfem_system* sys, const double* u_d, const double
   ADFEM_RANGE("adfem_system_grad_kappa_d");
   if (!sys || !u_d || !lam_d || !grad_kappa_d) return fail(ADFEM_ERR_INVALID, "null argument");
   if (sys->kind != ADFEM_SYS_POISSON) return fail(ADFEM_ERR_INVALID, "not a Poisson system");
-  ADFEM_TRY(kerr(launch_poisson_kappa_grad(*sys->mesh->m, u_d, lam_d, sys->isbd_ref.as<uint8_t>(), grad_kappa_d,
-                                           S(stream)),
+  const Mesh& m = *sys->mesh->m;
+  if (m.degree == 2) {
+    ADFEM_TRY(kerr(launch_gen_kappa_grad(m, *m.space[2], u_d, lam_d, sys->isbd_ref.as<uint8_t>(), grad_kappa_d,
+                                         S(stream)),
+                   "P2 kappa grad"));
+    return ADFEM_OK;
+  }
+  ADFEM_TRY(kerr(launch_poisson_kappa_grad(m, u_d, lam_d, sys->isbd_ref.as<uint8_t>(), grad_kappa_d, S(stream)),
                  "kappa grad"));
   return ADFEM_OK;
 }
@@ -1420,16 +1476,17 @@ int adfem_poisson_solve(adfem_system* sys, const double* kappa, const double* f,
   if (!sys || !kappa || !f || !u) return fail(ADFEM_ERR_INVALID, "null argument");
   if (sys->kind != ADFEM_SYS_POISSON) return fail(ADFEM_ERR_INVALID, "not a Poisson system");
   Mesh& m = *sys->mesh->m;
-  const size_t ng = 3 * (size_t)m.ne;
+  const size_t ng = (size_t)mesh_ngauss(m);
   ADFEM_TRY(sys->in0.alloc(sizeof(double) * ng));
   ADFEM_TRY(sys->in1.alloc(sizeof(double) * ng));
   ADFEM_CUDA(cudaMemcpy(sys->in0.p, kappa, sizeof(double) * ng, cudaMemcpyHostToDevice));
   ADFEM_CUDA(cudaMemcpy(sys->in1.p, f, sizeof(double) * ng, cudaMemcpyHostToDevice));
   ADFEM_TRY(adfem_system_assemble_poisson_d(sys, sys->in0.as<double>(), sys->in1.as<double>(), nullptr));
-  if (opts && opts->warm_start) ADFEM_CUDA(cudaMemcpy(sys->t2.p, u, sizeof(double) * m.nv, cudaMemcpyHostToDevice));
+  const size_t nd = (size_t)sys->ndof;
+  if (opts && opts->warm_start) ADFEM_CUDA(cudaMemcpy(sys->t2.p, u, sizeof(double) * nd, cudaMemcpyHostToDevice));
   const int r = adfem_system_solve_d(sys, sys->t2.as<double>(), opts, stats, nullptr);
   if (r != ADFEM_OK && r != ADFEM_ERR_NOT_CONVERGED) return r;
-  ADFEM_CUDA(cudaMemcpy(u, sys->t2.p, sizeof(double) * m.nv, cudaMemcpyDeviceToHost));
+  ADFEM_CUDA(cudaMemcpy(u, sys->t2.p, sizeof(double) * nd, cudaMemcpyDeviceToHost));
   return r;
 }
 

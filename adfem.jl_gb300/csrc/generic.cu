@@ -22,11 +22,13 @@
 
 #include "adfem_internal.h"
 #include "cg_common.cuh"
+#include "checks.cuh"
 
 namespace adfem {
 namespace {
 
 constexpr int kGT = 256;
+constexpr int kRowBTs = 128;  // rows per block of the resident-system row kernel
 
 // rule points (xi, eta, weight) on the reference triangle: order 2 (3 points, P1) and
 // order 4 (6 points, P2: the published Strang-Fix/Dunavant rule); same constants as
@@ -603,6 +605,106 @@ __global__ void __launch_bounds__(kGT) k_gen_to_gauss_backward(int64_t nrow, con
   }
 }
 
+// ---------------------------------------------------------------- resident P2 systems
+// Poisson system rows of a degree-DEG space: one thread per DOF row i (space order), the
+// row summed from the element matrices ke in ascending element order, the load
+// sum_e sum_k f_k phi_a(x_k) w_k over the same incidence, and the Dirichlet condition
+// applied as by the P1 system kernel: a Dirichlet row (tag 1) becomes the identity row
+// with rhs = bdval; a row next to Dirichlet DOFs (tag 2) moves those columns into the
+// right-hand side lift.  Values go to the system's sliced-ELL operator: row nperm[i],
+// slot kperm[rowptr[i] + k] (identity without renumbering); isbd, bdval, rhs in solver
+// order.  Deterministic: every value is summed by one thread in a fixed order.
+template <int DEG, int MAXW>
+__global__ void __launch_bounds__(kRowBTs) k_gen_poisson_rows(
+    int64_t ndof, const int32_t* __restrict__ rowptr, const int32_t* __restrict__ colind,
+    const int32_t* __restrict__ inc_ptr, const uint4* __restrict__ inc, const double* __restrict__ area,
+    const double* __restrict__ ke, const double* __restrict__ f, const int32_t* __restrict__ sptr,
+    const uint8_t* __restrict__ isbd, const double* __restrict__ bdval, double* __restrict__ vals,
+    double* __restrict__ rhs, const int32_t* __restrict__ nperm, const uint8_t* __restrict__ kperm,
+    const int32_t* __restrict__ diagpos) {
+  constexpr int ND = Tab<DEG>::ND, NG = Tab<DEG>::NG;
+  __shared__ Tab<DEG> T;
+  __shared__ double acc[MAXW][kRowBTs];
+  tab_init(T);
+  const int t = threadIdx.x;
+  const int64_t i = (int64_t)blockIdx.x * kRowBTs + t;
+  if (i >= ndof) return;
+  const int32_t r0 = rowptr[i];
+  const int w = rowptr[i + 1] - r0;
+  const int64_t ri = nperm ? (int64_t)nperm[i] : i;
+  const int64_t base = (int64_t)sptr[ri >> 5] + (ri & 31);
+  const uint8_t tag = isbd[ri];
+  auto slot = [&](int k) -> int64_t { return base + 32 * (int64_t)(kperm ? (int)kperm[r0 + k] : k); };
+  if (tag == 1) {
+    const int dp = diagpos[i];
+    for (int k = 0; k < w; k++) vals[slot(k)] = (k == dp) ? 1.0 : 0.0;
+    rhs[ri] = bdval[ri];
+    return;
+  }
+  for (int k = 0; k < w; k++) acc[k][t] = 0.0;
+  double r = 0.0;
+  for (int32_t s = inc_ptr[i]; s < inc_ptr[i + 1]; s++) {
+    const uint4 rec = inc[s];
+    const int a = (int)rec.y;
+    const double* K = ke + ((int64_t)rec.x * ND + a) * ND;
+#pragma unroll
+    for (int b = 0; b < ND; b++) {
+      const unsigned o = space_off(rec, b);
+      if (!ADFEM_DCHECK(o < (unsigned)w && o < (unsigned)MAXW)) continue;
+      acc[o][t] += K[b];
+    }
+    const double ar = area[rec.x];
+#pragma unroll
+    for (int k = 0; k < NG; k++) r += f[(int64_t)rec.x * NG + k] * T.h[k][a] * weight_at(T, k, ar);
+  }
+  if (tag == 2) {
+    for (int k = 0; k < w; k++) {
+      const int64_t j = nperm ? (int64_t)nperm[colind[r0 + k]] : (int64_t)colind[r0 + k];
+      if (isbd[j] == 1) {
+        r = fma(-acc[k][t], bdval[j], r);
+        acc[k][t] = 0.0;
+      }
+    }
+  }
+  rhs[ri] = r;
+  for (int k = 0; k < w; k++) vals[slot(k)] = acc[k][t];
+}
+
+// dL/dkappa at Gauss point k of element e for the resident system: -w_k grad(lam).grad(u)
+// at x_k, lam zero on the Dirichlet DOFs (isbd_ref in space order) -- the composition of
+// the sparse-solve gradient (-lam_i u_j per entry), the Dirichlet backward and the
+// FemLaplaceScalar backward, with the element matrix's rank-one structure per point.
+template <int DEG>
+__global__ void __launch_bounds__(kGT) k_gen_kappa_grad(int64_t ne, const int32_t* __restrict__ dof,
+                                                        const double* __restrict__ area,
+                                                        const double2* __restrict__ grad,
+                                                        const double* __restrict__ u, const double* __restrict__ lam,
+                                                        const uint8_t* __restrict__ isbd, double* __restrict__ gk) {
+  constexpr int ND = Tab<DEG>::ND, NG = Tab<DEG>::NG;
+  __shared__ Tab<DEG> T;
+  tab_init(T);
+  for (int64_t gp = gtid(); gp < ne * NG; gp += gstride()) {
+    const int64_t e = gp / NG;
+    const int k = (int)(gp - e * NG);
+    double2 g[3];
+    load_grad(grad, e, g);
+    double hx[ND], hy[ND];
+    grads_all(T, k, g, hx, hy);
+    double ux = 0.0, uy = 0.0, lx = 0.0, ly = 0.0;
+#pragma unroll
+    for (int b = 0; b < ND; b++) {
+      const int32_t d = dof[ND * e + b];
+      const double ub = u[d];
+      const double lb = isbd[d] == 1 ? 0.0 : lam[d];
+      ux = fma(hx[b], ub, ux);
+      uy = fma(hy[b], ub, uy);
+      lx = fma(hx[b], lb, lx);
+      ly = fma(hy[b], lb, ly);
+    }
+    gk[gp] = -weight_at(T, k, area[e]) * fma(lx, ux, ly * uy);
+  }
+}
+
 // ---------------------------------------------------------------- PCL
 __global__ void __launch_bounds__(kGT) k_fill(int64_t n, double v, double* __restrict__ out) {
   for (int64_t i = gtid(); i < n; i += gstride()) out[i] = v;
@@ -725,6 +827,44 @@ cudaError_t launch_gen_matrix(const Mesh& m, const Space& sp, GenOp op, const do
   return cudaGetLastError();
 }
 
+cudaError_t launch_gen_poisson_system(const Mesh& m, const Space& sp, const double* kappa, const double* f, double* ke,
+                                      const uint8_t* isbd, const double* bdval, double* sell_vals, double* rhs,
+                                      const int32_t* sptr, const int32_t* diagpos_space, const int32_t* nperm,
+                                      const uint8_t* kperm, cudaStream_t st) {
+  const int g = grid_for(m.ne);
+  const double* area = sp.d_area.as<double>();
+  const double2* grad = m.d_grad.as<double2>();
+  GEN_DISPATCH(sp, (k_gen_ke<1, 0><<<g, kGT, 0, st>>>(m.ne, area, grad, kappa, ke)),
+               (k_gen_ke<2, 0><<<g, kGT, 0, st>>>(m.ne, area, grad, kappa, ke)));
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  if (sp.maxrow > 24) return cudaErrorNotSupported;  // (P2 rows of a triangle mesh: 19 for valence 6)
+  const unsigned gr = (unsigned)((sp.ndof + kRowBTs - 1) / kRowBTs);
+  const int32_t* rp = sp.d_rowptr.as<int32_t>();
+  const int32_t* ci = sp.d_colind.as<int32_t>();
+  const int32_t* ip = sp.d_inc_ptr.as<int32_t>();
+  const uint4* inc = sp.d_inc.as<uint4>();
+  GEN_DISPATCH(sp,
+               (k_gen_poisson_rows<1, 24><<<gr, kRowBTs, 0, st>>>(sp.ndof, rp, ci, ip, inc, area, ke, f, sptr, isbd,
+                                                                  bdval, sell_vals, rhs, nperm, kperm,
+                                                                  diagpos_space)),
+               (k_gen_poisson_rows<2, 24><<<gr, kRowBTs, 0, st>>>(sp.ndof, rp, ci, ip, inc, area, ke, f, sptr, isbd,
+                                                                  bdval, sell_vals, rhs, nperm, kperm,
+                                                                  diagpos_space)));
+  return cudaGetLastError();
+}
+
+cudaError_t launch_gen_kappa_grad(const Mesh& m, const Space& sp, const double* u, const double* lam,
+                                  const uint8_t* isbd_space, double* grad_kappa, cudaStream_t st) {
+  const int g = grid_for(m.ne * sp.ng);
+  const int32_t* dof = sp.d_dof.as<int32_t>();
+  const double* area = sp.d_area.as<double>();
+  const double2* grad = m.d_grad.as<double2>();
+  GEN_DISPATCH(sp, (k_gen_kappa_grad<1><<<g, kGT, 0, st>>>(m.ne, dof, area, grad, u, lam, isbd_space, grad_kappa)),
+               (k_gen_kappa_grad<2><<<g, kGT, 0, st>>>(m.ne, dof, area, grad, u, lam, isbd_space, grad_kappa)));
+  return cudaGetLastError();
+}
+
 cudaError_t launch_gen_stiffness_matrix(const Mesh& m, const Space& sp, const double* D, double* ke, double* vals,
                                         bool transpose, cudaStream_t st) {
   const int g = grid_for(m.ne * 2 * sp.nd);
@@ -806,5 +946,7 @@ cudaError_t launch_gen_to_gauss_backward(const Mesh& m, const Space& sp, bool ve
   }
   return cudaGetLastError();
 }
+
+ADFEM_CHECK_READER(check_line_generic)
 
 }  // namespace adfem

@@ -684,8 +684,9 @@ int adfem_debug_fail_alloc(long long k) {
 }
 
 int adfem_debug_check_code(void) {
-  const int parts[3] = {adfem::check_line_solver(), adfem::check_line_zcg(), adfem::check_line_assemble()};
-  for (int k = 0; k < 3; k++)
+  const int parts[4] = {adfem::check_line_solver(), adfem::check_line_zcg(), adfem::check_line_assemble(),
+                        adfem::check_line_generic()};
+  for (int k = 0; k < 4; k++)
     if (parts[k] != 0) return parts[k] < 0 ? -1 : 100000 * (k + 1) + parts[k];
   return 0;
 }

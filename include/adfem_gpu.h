@@ -59,7 +59,7 @@ ADFEM_API int adfem_debug_fail_alloc(long long k);
 /* Testing hook, no counterpart in the reference: in the debug build (-DADFEM_CHECKS, a
  * second library built by build.py --checks) kernels check the indices they compute before
  * using them and record the first failure instead of faulting; this returns it as
- * 100000 * unit + source line (unit 1: solver.cu, 2: zcg.cu, 3: assemble.cu), 0 when no check
+ * 100000 * unit + source line (unit 1: solver.cu, 2: zcg.cu, 3: assemble.cu, 4: generic.cu), 0 when no check
  * failed (always 0 in release builds), -1 if the flags cannot be read, and clears it. */
 ADFEM_API int adfem_debug_check_code(void);
 
@@ -328,7 +328,11 @@ ADFEM_API int adfem_csc_solve(long long n, const long long *colptr1, const long 
  * sliced-ELL form (FP64 and FP32 Jacobi-scaled copies) with its right-hand side and
  * CG work vectors, so repeated solves and adjoint solves reuse them. */
 enum { ADFEM_SYS_POISSON = 0, ADFEM_SYS_ELASTICITY = 1 };
-/* P1 meshes only (a P2 mesh gives ADFEM_ERR_UNSUPPORTED: assemble its operators and use adfem_csc_solve) */
+/* Poisson systems on P1 or P2 meshes (P2: the vertex-then-edge DOFs of the mesh's space,
+ * kappa and f at the 6 points per element of the order-4 rule; DOFs renumbered for the
+ * solver by reverse Cuthill-McKee, inputs and outputs in the reference order); elasticity
+ * systems on P1 meshes (a P2 mesh gives ADFEM_ERR_UNSUPPORTED: assemble its stiffness
+ * operator and use adfem_csc_solve). */
 ADFEM_API int adfem_system_create(adfem_mesh *mesh, int kind, adfem_system **out);
 ADFEM_API int adfem_system_destroy(adfem_system *sys);
 /* Dirichlet data: bd 1-based DOF ids (for elasticity DOF ids in the [x; y] ordering,
@@ -353,9 +357,10 @@ ADFEM_API int adfem_system_solve_d(adfem_system *sys, double *u_d, const adfem_s
 /* Adjoint solve K lambda = g (K symmetric); lambda is zero on Dirichlet DOFs. */
 ADFEM_API int adfem_system_adjoint_d(adfem_system *sys, const double *g_d, double *lam_d,
                                      const adfem_solver_opts *opts, adfem_solver_stats *stats, void *stream);
-/* dL/dkappa at every Gauss point: -w_e (grad lam_e).(grad u_e) (equal for the 3 points of
- * an element); the composition of the reference's FemLaplaceScalar, ImposeDirichlet and
- * sparse-solve gradients. */
+/* dL/dkappa at every Gauss point: -w (grad lam).(grad u) at the point (P1: equal for the 3
+ * points of an element; P2: the quadratic fields' gradients at each of the 6 points), lam
+ * zero on the Dirichlet DOFs; the composition of the reference's FemLaplaceScalar,
+ * ImposeDirichlet and sparse-solve gradients. */
 ADFEM_API int adfem_system_grad_kappa_d(adfem_system *sys, const double *u_d, const double *lam_d,
                                         double *grad_kappa_d, void *stream);
 /* dL/dE at every Gauss point for the plane-strain material used by the last

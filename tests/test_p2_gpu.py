@@ -258,7 +258,7 @@ def test_p2_input_checks(gpulib):
     with pytest.raises(gpulib.AdFemError):
         gpulib.compute_fem_laplace_matrix1(np.ones(3 * G.nelem), G)  # P1 length on a P2 mesh
     with pytest.raises(gpulib.AdFemError):
-        gpulib.PoissonSystem(G)  # resident systems are P1
+        gpulib.ElasticitySystem(G)  # resident elasticity systems are P1
     with pytest.raises(gpulib.AdFemError):
         gpulib.Mesh(coords, elems, degree=2, order=2)
 
@@ -325,3 +325,65 @@ def test_mesh_from_file(oracle, gpulib, tmp_path, degree):
     kappa = 1 + np.random.default_rng(1).random(O.ngauss)
     assert row_scaled_err(gpulib.compute_fem_laplace_matrix1(kappa, G), O.laplace_csc(kappa)) < TOL
     np.testing.assert_array_equal(gpulib.bcnode(G), O.bcnode())
+
+
+def _p2_case(oracle, gpulib, m, seed, bdval=False):
+    coords, elems = synth.jittered_square(m, seed=seed)
+    O = oracle.OracleSpace(coords, elems, 2)
+    G = gpulib.Mesh(coords, elems, degree=2)
+    g = O.gauss_nodes()
+    G1 = synth.fourier_field(g[:, 0], g[:, 1], seed=1)
+    kappa = 1 + np.exp(synth.contrast_sigma(G1, 1e2) * G1)
+    f = 1e3 * (1 + g[:, 0] - 2 * g[:, 1])
+    bd = O.bcnode()
+    dn = O.dof_nodes()
+    bv = (np.sin(3 * dn[bd - 1, 0]) + dn[bd - 1, 1]) if bdval else np.zeros(bd.size)
+    B, r = oracle.dirichlet_csc(O.laplace_csc(kappa), O.source(f), bd, bv)
+    return O, G, kappa, f, bd, bv, B, r
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+@pytest.mark.parametrize("m,seed,bdval", [(12, 0, False), (30, 4, True)])
+def test_p2_resident_system_forward_adjoint_gradient(oracle, gpulib, precision, m, seed, bdval):
+    """Resident P2 Poisson system (order-4 rule, vertex-then-edge DOFs, solver in reverse
+    Cuthill-McKee order): right-hand side and operator against the oracle's Dirichlet-
+    imposed P2 system, forward solve against the direct solve, adjoint solve, and
+    dL/dkappa at the 6 Gauss points against the reference's backward chain (sparse-solve
+    gradient -lam_i u_j per stored entry, ImposeDirichlet backward, FemLaplaceScalar
+    backward over the P2 element matrices)."""
+    import torch
+
+    O, G, kappa, f, bd, bv, B, r = _p2_case(oracle, gpulib, m, seed, bdval)
+    S = gpulib.PoissonSystem(G)
+    assert S.ndof == O.ndof
+    S.set_dirichlet(bd, bv)
+    S.assemble(torch.tensor(kappa, device="cuda"), torch.tensor(f, device="cuda"))
+    info = S.solver_info()
+    assert info["rows"] == O.ndof and info["renumbered"] == 1
+    assert rel(S.rhs().cpu().numpy(), r) < TOL
+    x = np.random.default_rng(seed).standard_normal(O.ndof)
+    assert rel(S.apply(torch.tensor(x, device="cuda")).cpu().numpy(), B @ x) < TOL
+    rtol = 1e-13 if precision == "fp64" else 1e-11
+    u = S.solve(precision=precision, rtol=rtol)
+    assert S.last_stats.status == 0
+    u0 = oracle.spsolve(B, r)
+    assert rel(u.cpu().numpy(), u0) < 1e-9
+    np.testing.assert_array_equal(u.cpu().numpy()[bd - 1], bv)
+    # adjoint of a misfit on a tenth of the DOFs
+    obs = synth.observation_nodes(O.ndof, seed=3, frac=0.1)
+    gu = np.zeros(O.ndof)
+    gu[obs] = 1.0  # (0-based ids)
+    gu_t = torch.tensor(gu, device="cuda")
+    lam = S.adjoint(gu_t, precision=precision, rtol=rtol)
+    assert S.last_stats.status == 0
+    gz = gu.copy()
+    gz[bd - 1] = 0.0
+    lam0 = oracle.spsolve(B.T.tocsc(), gz)
+    assert rel(lam.cpu().numpy(), lam0) < 1e-9
+    gk = S.grad_kappa(u, lam).cpu().numpy()
+    uu, ll = u0, lam0.copy()
+    ll[bd - 1] = 0.0
+    idx, vv = O.laplace_coo(kappa)
+    gref = O.laplace_coo_backward(-ll[idx[:, 0]] * uu[idx[:, 1]])
+    assert gk.size == O.ngauss
+    assert rel(gk, gref) < 1e-7
