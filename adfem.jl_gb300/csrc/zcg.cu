@@ -199,6 +199,7 @@ __device__ __forceinline__ void bulk_load(void* dst, const void* src, unsigned b
 template <int MAXW, int BT, int U1, int U2, bool B2, bool RING>
 __global__ void __launch_bounds__(BT, 1024 / BT) k_zcg_iter(ZcgArgs A) {
   static_assert(MAXW % 4 == 0, "pattern rows are loaded as int4");
+  constexpr int kNDP = MAXW > 16 ? MAXW / 2 : 1;  // words of prefetched column deltas (24-wide rows)
   extern __shared__ __align__(128) float zsm[];
   const int stagef = RING ? BT * A.zw : 0;                        // floats per ring stage
   float* ring = zsm;                                              // RING: A.ns stages (16-byte aligned)
@@ -387,12 +388,16 @@ __global__ void __launch_bounds__(BT, 1024 / BT) k_zcg_iter(ZcgArgs A) {
     }
     __syncthreads();
     // ---- phase 2: q = K P_k for the rows [lo, hi)
-    auto row = [&](int i, const float (&v)[MAXW], float d, float c, int pid) -> float {
+    auto row = [&](int i, const float (&v)[MAXW], float d, float c, int pid, const unsigned (&dpk)[kNDP]) -> float {
       const float Pi = sP[i - wlo];
       const float Pp = B2 ? sP[(i ^ 1) - wlo] : Pi;  // partner DOF (B2: rows come in even/odd pairs)
       const int dpart = (i & 1) ? -1 : 1;            // column delta of the partner DOF
-      int dl[MAXW];
-      if (pid >= 0) {
+      // (24-wide rows: the column deltas were loaded with the values, two int16 per word, and
+      // are unpacked as they are used)
+      int dl[MAXW > 16 ? 1 : MAXW];
+      if constexpr (MAXW > 16) {
+        dl[0] = 0;
+      } else if (pid >= 0) {
         // the slice's column pattern (int32, padded with 0 to MAXW per row parity)
         const int4* pv = reinterpret_cast<const int4*>(spool) + (pid * A.period + (A.period == 2 ? (i & 1) : 0)) *
                                                                      (MAXW / 4);
@@ -412,13 +417,14 @@ __global__ void __launch_bounds__(BT, 1024 / BT) k_zcg_iter(ZcgArgs A) {
       float s = 0.f;
 #pragma unroll
       for (int k = 0; k < MAXW; k++) {
+        const int dk = MAXW > 16 ? (int)(short)(dpk[k >> 1] >> (16 * (k & 1))) : dl[MAXW > 16 ? 0 : k];
         float tv;
-        if (dl[k] == 0) tv = Pi;
-        else if (B2 && dl[k] == dpart) tv = Pp;
+        if (dk == 0) tv = Pi;
+        else if (B2 && dk == dpart) tv = Pp;
         else {
-          int w_ = i + dl[k] - wlo;
+          int w_ = i + dk - wlo;
           if (!ADFEM_DCHECK(w_ >= 0 && w_ < whi - wlo)) w_ = i - wlo;
-          tv = __fsub_rn(sP[w_], (B2 && (dl[k] & 1)) ? Pp : Pi);
+          tv = __fsub_rn(sP[w_], (B2 && (dk & 1)) ? Pp : Pi);
         }
         s = fmaf(v[k], tv, s);
       }
@@ -440,10 +446,20 @@ __global__ void __launch_bounds__(BT, 1024 / BT) k_zcg_iter(ZcgArgs A) {
     };
     // fixed-width layout: entry k of row i at (i>>5)*32*zw + 32k + (i&31) (padding: value 0,
     // delta 0), so the loads of a row depend on nothing but i
-    auto fetch = [&](int i, float (&v)[MAXW], float& d, float& c, int& pid) {
+    auto fetch = [&](int i, float (&v)[MAXW], float& d, float& c, int& pid, unsigned (&dpk)[kNDP]) {
       const int base = (i >> 5) * (32 * zw) + (i & 31);
 #pragma unroll
       for (int k = 0; k < MAXW; k++) v[k] = k < zw ? ld_stream(A.val + base + 32 * k, pol) : 0.f;
+      if constexpr (MAXW > 16) {
+#pragma unroll
+        for (int k = 0; k < MAXW; k += 2) {
+          const unsigned a0 = k < zw ? (unsigned)(unsigned short)__ldg(A.colz + base + 32 * k) : 0u;
+          const unsigned a1 = k + 1 < zw ? (unsigned)(unsigned short)__ldg(A.colz + base + 32 * (k + 1)) : 0u;
+          dpk[k >> 1] = a0 | (a1 << 16);
+        }
+      } else {
+        dpk[0] = 0u;
+      }
       if constexpr (B2) {
         const float2 b = __ldg(A.bz + i);
         d = b.x;
@@ -452,7 +468,7 @@ __global__ void __launch_bounds__(BT, 1024 / BT) k_zcg_iter(ZcgArgs A) {
         d = __ldg(A.dz + i);
         c = 0.f;
       }
-      pid = __ldg(A.zpid + (i >> 5));
+      pid = MAXW > 16 ? -1 : __ldg(A.zpid + (i >> 5));
     };
     int c0 = lo;
     if constexpr (RING) {
@@ -471,7 +487,8 @@ __global__ void __launch_bounds__(BT, 1024 / BT) k_zcg_iter(ZcgArgs A) {
           float v[MAXW];
 #pragma unroll
           for (int k = 0; k < MAXW; k++) v[k] = k < zw ? sv[32 * k] : 0.f;
-          put(i, row(i, v, d, c, pid));
+          const unsigned dpk[kNDP] = {};
+          put(i, row(i, v, d, c, pid, dpk));
         }
         __syncwarp();
         if ((tid & 31) == 0) mbar_arrive(&s_empty[slot]);
@@ -487,20 +504,22 @@ __global__ void __launch_bounds__(BT, 1024 / BT) k_zcg_iter(ZcgArgs A) {
     for (; i + (U2 - 1) * BT < hi; i += U2 * BT) {  // U2 rows per thread and trip, loads first
       float v[U2][MAXW], d[U2], c[U2];
       int pid[U2];
+      unsigned dpk[U2][kNDP];
 #pragma unroll
-      for (int u = 0; u < U2; u++) fetch(i + u * BT, v[u], d[u], c[u], pid[u]);
+      for (int u = 0; u < U2; u++) fetch(i + u * BT, v[u], d[u], c[u], pid[u], dpk[u]);
       flush();
 #pragma unroll
-      for (int u = 0; u < U2; u++) dq[u] = row(i + u * BT, v[u], d[u], c[u], pid[u]);
+      for (int u = 0; u < U2; u++) dq[u] = row(i + u * BT, v[u], d[u], c[u], pid[u], dpk[u]);
       dbase = i;
       dcnt = U2;
     }
     for (; i < hi; i += BT) {
       float v0[MAXW], d0, cc0;
       int g0;
-      fetch(i, v0, d0, cc0, g0);
+      unsigned dp0[kNDP];
+      fetch(i, v0, d0, cc0, g0, dp0);
       flush();
-      dq[0] = row(i, v0, d0, cc0, g0);
+      dq[0] = row(i, v0, d0, cc0, g0, dp0);
       dbase = i;
       dcnt = 1;
     }
@@ -883,9 +902,17 @@ static int zcg_build_pool(Solver& S) {
   return ADFEM_OK;
 }
 
+// threads per block of a variant: 24-wide rows hold 24 values and 12 words of column
+// deltas per thread, which do not fit in the 64 registers of a 1024-thread block
+template <int MAXW>
+constexpr int zbt() {
+  return MAXW > 16 ? 768 : kZBT;
+}
+
 template <int MAXW, bool B2, bool RING = false>
 static int zcg_configure(Solver& S, int sms) {
-  auto kern = k_zcg_iter<MAXW, kZBT, (RING ? kZU1R : kZU1), (MAXW > 8 ? kZU2W : kZU2), B2, RING>;
+  constexpr int BT = zbt<MAXW>();
+  auto kern = k_zcg_iter<MAXW, BT, (RING ? kZU1R : kZU1), (MAXW > 8 ? kZU2W : kZU2), B2, RING>;
   const size_t limit = RING ? kZSmemRing : kZSmemBlock;
   // The shared-memory limit is raised once per process to the most any plan uses:
   // changing a kernel's attributes while another thread captures a graph with that
@@ -899,8 +926,9 @@ static int zcg_configure(Solver& S, int sms) {
   if (set_err != cudaSuccess) return cuda_fail(set_err, "cudaFuncSetAttribute");
   if (S.zsmem > limit) return fail(ADFEM_ERR_INVALID, "banded CG plan exceeds its shared-memory limit");
   int per = 0;
-  ADFEM_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kern, kZBT, S.zsmem));
+  ADFEM_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kern, BT, S.zsmem));
   if (per < 1) return fail(ADFEM_ERR_CUDA, "banded CG kernel cannot be resident");
+  S.zbt = BT;
   const int64_t want = (int64_t)sms * per;
   // at least one band width of rows per block, so that halos stay below twice the rows
   int64_t L = (S.n + want - 1) / want;
@@ -917,12 +945,12 @@ int zcg_plan(Solver& S, int sms) {
   S.zcg = false;
   const char* env = std::getenv("ADFEM_ZCG");
   if (env && env[0] == '0') return ADFEM_OK;
-  if (!A.delta16 || A.maxw > 16 || A.maxw < 1 || A.band > 32767 || S.n < 1) return ADFEM_OK;
+  if (!A.delta16 || A.maxw > 24 || A.maxw < 1 || A.band > 32767 || S.n < 1) return ADFEM_OK;
   // 32-bit positions and fixed-width indices
   if (A.nslices * 32 * (int64_t)A.maxw >= INT32_MAX || S.n + A.band >= INT32_MAX) return ADFEM_OK;
   const int H = (int)A.band;
   S.zw = A.maxw;
-  S.zps = S.zw <= 8 ? 8 : 16;
+  S.zps = S.zw <= 8 ? 8 : (S.zw <= 16 ? 16 : 24);
   ADFEM_TRY(zcg_build_pool(S));
   const size_t pool_bytes = sizeof(int32_t) * (size_t)((S.znpool + 3) & ~3);
   // super-tile rows: the whole per-block range when it fits beside its 2H halo, else the
@@ -967,8 +995,9 @@ int zcg_plan(Solver& S, int sms) {
   // the same resources, so the plan is made with the plain one)
   if (A.maxw <= 8 && S.zns) ADFEM_TRY((zcg_configure<8, false, true>(S, sms)));
   else if (A.maxw <= 8) ADFEM_TRY((zcg_configure<8, false>(S, sms)));
-  else ADFEM_TRY((zcg_configure<16, false>(S, sms)));
-  if (A.maxw > 8) ADFEM_TRY((zcg_configure<16, true>(S, sms)));
+  else if (A.maxw <= 16) ADFEM_TRY((zcg_configure<16, false>(S, sms)));
+  else ADFEM_TRY((zcg_configure<24, false>(S, sms)));
+  if (A.maxw > 8 && A.maxw <= 16) ADFEM_TRY((zcg_configure<16, true>(S, sms)));
   const size_t n4 = sizeof(float) * (size_t)S.n;
   ADFEM_TRY(S.z1.alloc(n4));
   ADFEM_TRY(S.zq1.alloc(n4));
@@ -993,7 +1022,7 @@ int zcg_plan(Solver& S, int sms) {
   ADFEM_CUDA(cudaStreamSynchronize(0));
   int no_partner = 0;
   ADFEM_CUDA(cudaMemcpy(&no_partner, flag.p, sizeof(int), cudaMemcpyDeviceToHost));
-  S.zblock2 = A.pat_period == 2 && !no_partner && A.maxw > 8;
+  S.zblock2 = A.pat_period == 2 && !no_partner && A.maxw > 8 && A.maxw <= 16;
   if (S.zblock2) ADFEM_TRY(S.bz32.alloc(sizeof(float2) * (size_t)S.n));
 
   S.zcg = true;
@@ -1049,7 +1078,7 @@ template <class Kern>
 static void zlaunch(Kern kern, const Solver& S, cudaStream_t st, const ZcgArgs& z) {
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3((unsigned)S.zgrid);
-  cfg.blockDim = dim3(kZBT);
+  cfg.blockDim = dim3((unsigned)S.zbt);
   cfg.dynamicSmemBytes = S.zsmem;
   cfg.stream = st;
   cudaLaunchAttribute at[1];
@@ -1064,6 +1093,7 @@ void zcg_enqueue_iter(Solver& S, cudaStream_t st) {
   const ZcgArgs z = zcg_args(S);
   if (S.A->maxw <= 8 && S.zns) zlaunch(k_zcg_iter<8, kZBT, kZU1R, kZU2, false, true>, S, st, z);
   else if (S.A->maxw <= 8) zlaunch(k_zcg_iter<8, kZBT, kZU1, kZU2, false, false>, S, st, z);
+  else if (S.A->maxw > 16) zlaunch(k_zcg_iter<24, zbt<24>(), kZU1, kZU2W, false, false>, S, st, z);
   else if (S.zblock2) zlaunch(k_zcg_iter<16, kZBT, kZU1, kZU2W, true, false>, S, st, z);
   else zlaunch(k_zcg_iter<16, kZBT, kZU1, kZU2W, false, false>, S, st, z);
 }

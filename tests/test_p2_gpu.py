@@ -360,6 +360,7 @@ def test_p2_resident_system_forward_adjoint_gradient(oracle, gpulib, precision, 
     S.assemble(torch.tensor(kappa, device="cuda"), torch.tensor(f, device="cuda"))
     info = S.solver_info()
     assert info["rows"] == O.ndof and info["renumbered"] == 1
+    assert info["banded"] == 1  # 19-entry P2 rows: the 24-wide banded mixed iteration
     assert rel(S.rhs().cpu().numpy(), r) < TOL
     x = np.random.default_rng(seed).standard_normal(O.ndof)
     assert rel(S.apply(torch.tensor(x, device="cuda")).cpu().numpy(), B @ x) < TOL
@@ -387,3 +388,22 @@ def test_p2_resident_system_forward_adjoint_gradient(oracle, gpulib, precision, 
     gref = O.laplace_coo_backward(-ll[idx[:, 0]] * uu[idx[:, 1]])
     assert gk.size == O.ngauss
     assert rel(gk, gref) < 1e-7
+
+
+def test_p2_banded_and_scaled_mixed_paths_agree(oracle, gpulib, monkeypatch):
+    """The P2 operator on the 24-wide banded mixed iteration and on the scaled two-kernel
+    mixed iteration (forced with ADFEM_ZCG=0): both within the 1e-10 mixed-precision bar
+    of the direct solve."""
+    import torch
+
+    O, G, kappa, f, bd, bv, B, r = _p2_case(oracle, gpulib, 40, 5, True)
+    u0 = oracle.spsolve(B, r)
+    for zcg, banded in (("1", 1), ("0", 0)):
+        monkeypatch.setenv("ADFEM_ZCG", zcg)
+        S = gpulib.PoissonSystem(G)
+        S.set_dirichlet(bd, bv)
+        S.assemble(torch.tensor(kappa, device="cuda"), torch.tensor(f, device="cuda"))
+        assert S.solver_info()["banded"] == banded
+        u = S.solve(precision="mixed", rtol=1e-12)
+        assert S.last_stats.status == 0
+        assert rel(u.cpu().numpy(), u0) < 1e-10
