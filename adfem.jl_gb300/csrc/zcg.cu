@@ -848,7 +848,8 @@ static constexpr int kZU1R = ADFEM_ZCG_U1_RING;      // phase-1 positions per th
 #define ADFEM_ZCG_U2_WIDE 1
 #endif
 // rows per trip of the 16-wide variants: two rows of 16 entries do not fit in 64 registers
-// per thread (they spill)
+// per thread (they spill); 768-thread blocks with two rows per trip (79 registers, no
+// spills) measured 49.5 against 48.9 us per iteration at 2M-DOF elasticity
 static constexpr int kZU2W = ADFEM_ZCG_U2_WIDE;
 static constexpr size_t kZSmemBlock = (kZPerSM >= 2 ? 100 : 200) * 1024;  // shared memory per block
 // ring variants: window + pattern pool + ring stages (the static shared memory of the
