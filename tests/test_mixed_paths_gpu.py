@@ -262,3 +262,37 @@ def test_dependent_launches_bit_identical(gpulib, monkeypatch):
     assert plain.last_stats.status == 0 and dep.last_stats.status == 0
     assert dep.last_stats.iterations == plain.last_stats.iterations
     assert np.array_equal(u1.cpu().numpy(), u0.cpu().numpy())
+
+
+@pytest.mark.parametrize("smax", ["", "64"])
+def test_elasticity_block_form_super_tiles(oracle, gpulib, monkeypatch, smax):
+    """The interleaved 2-DOF (node-block Jacobi) banded variant with and without block ranges
+    split into super-tiles (each with its own halo; the q^ stores deferred across tiles)."""
+    import torch
+
+    monkeypatch.delenv("ADFEM_ZCG", raising=False)
+    if smax:
+        monkeypatch.setenv("ADFEM_ZCG_SMAX", smax)
+    else:
+        monkeypatch.delenv("ADFEM_ZCG_SMAX", raising=False)
+    coords, elems = synth.jittered_square(70, seed=8)
+    O = oracle.OracleMesh(coords, elems)
+    g = O.gauss_nodes()
+    E = 1e9 * np.exp(0.3 * synth.fourier_field(g[:, 0], g[:, 1], seed=2))
+    nu = np.full(O.ngauss, 0.3)
+    fx, fy = np.zeros(O.ngauss), np.full(O.ngauss, -1e6)
+    left = synth.left_edge_nodes(coords)
+    bd = np.concatenate([left + 1, left + 1 + O.ndof])
+    B, r = oracle.dirichlet_csc(O.stiffness_csc(oracle.plane_strain(E, nu, 0)),
+                                np.concatenate([O.source(fx), O.source(fy)]), bd, np.zeros(bd.size))
+    S = gpulib.ElasticitySystem(gpulib.Mesh(coords, elems))
+    S.set_dirichlet(bd)
+    t = lambda a: torch.tensor(a, device="cuda")  # noqa: E731
+    S.assemble(t(E), t(nu), t(fx), t(fy))
+    info = S.solver_info()
+    assert info["banded"] == 1
+    if smax:
+        assert info["rows_per_block"] > int(smax)  # several super-tiles per block
+    u = S.solve(precision="mixed", rtol=RTOL_MIXED)
+    assert S.last_stats.status == 0
+    assert rel(u.cpu().numpy(), oracle.spsolve(B, r)) < ERR_BAR

@@ -407,3 +407,28 @@ def test_p2_banded_and_scaled_mixed_paths_agree(oracle, gpulib, monkeypatch):
         u = S.solve(precision="mixed", rtol=1e-12)
         assert S.last_stats.status == 0
         assert rel(u.cpu().numpy(), u0) < 1e-10
+
+
+def test_p2_system_super_tiles_and_packed(oracle, gpulib, monkeypatch):
+    """P2 systems on the 24-wide banded iteration with block ranges split into super-tiles,
+    and a small P2 system through the packed solver (one thread block per system)."""
+    import torch
+
+    O, G, kappa, f, bd, bv, B, r = _p2_case(oracle, gpulib, 60, 2, True)
+    u0 = oracle.spsolve(B, r)
+    monkeypatch.setenv("ADFEM_ZCG_SMAX", "96")
+    S = gpulib.PoissonSystem(G)
+    S.set_dirichlet(bd, bv)
+    S.assemble(torch.tensor(kappa, device="cuda"), torch.tensor(f, device="cuda"))
+    info = S.solver_info()
+    assert info["banded"] == 1 and info["rows_per_block"] > 96
+    u = S.solve(precision="mixed", rtol=1e-12)
+    assert S.last_stats.status == 0 and rel(u.cpu().numpy(), u0) < 1e-10
+    monkeypatch.delenv("ADFEM_ZCG_SMAX", raising=False)
+    Os, Gs, ks, fs, bds, bvs, Bs, rs = _p2_case(oracle, gpulib, 10, 3, True)
+    P = gpulib.PoissonSystem(Gs)
+    P.set_dirichlet(bds, bvs)
+    P.assemble(torch.tensor(ks, device="cuda"), torch.tensor(fs, device="cuda"))
+    (up,), (stp,) = gpulib.system.solve_packed([P], rtol=1e-12)
+    assert stp.status == 0
+    assert rel(up.cpu().numpy(), oracle.spsolve(Bs, rs)) < 1e-10
