@@ -61,6 +61,7 @@ struct Solver {
   int zW = 0;              // shared-memory positions per super-tile (zS + 2 zH)
   int zns = 0;             // stages of the shared-memory matrix ring (0: the plain variant)
   int zbt = 1024;          // threads per block of the variant in use
+  bool zvarw = false;      // FP32 copy in the sliced layout (variable slice widths), 24-wide rows
   bool zrefill = true;     // the ring serves every row (else only the first zns stages)
   bool zpdl = true;        // iterations launched as programmatic dependent launches
   int64_t zL = 0;

@@ -66,6 +66,7 @@ struct ZcgArgs {
   float* yl;
   CgState* st;
   double* partials;
+  const int32_t* sptr;  // 24-wide variant: slice offsets of the sliced layout (entries), variable widths
   int ns;      // stages of the matrix ring (RING variants; 0 otherwise)
   int refill;  // RING: 1 the ring is refilled through phase 2, 0 only the first ns stages come through it
 };
@@ -446,15 +447,26 @@ __global__ void __launch_bounds__(BT, 1024 / BT) k_zcg_iter(ZcgArgs A) {
     };
     // fixed-width layout: entry k of row i at (i>>5)*32*zw + 32k + (i&31) (padding: value 0,
     // delta 0), so the loads of a row depend on nothing but i
+    // 24-wide rows: slice offsets of the sliced layout for this thread's row of the trip
+    // (sp0, sp1), loaded one trip ahead (nsp0, nsp1) so that the value loads do not wait for them
+    int sp0 = 0, sp1 = 0, nsp0 = 0, nsp1 = 0;
+    auto slice_of = [&](int i, int& a, int& b) {
+      if constexpr (MAXW > 16) {
+        a = __ldg(A.sptr + (i >> 5));
+        b = __ldg(A.sptr + (i >> 5) + 1);
+      }
+    };
     auto fetch = [&](int i, float (&v)[MAXW], float& d, float& c, int& pid, unsigned (&dpk)[kNDP]) {
-      const int base = (i >> 5) * (32 * zw) + (i & 31);
+      // (24-wide: the slice's own width, entry k of row i at sptr[i/32] + 32k + i%32)
+      const int base = MAXW > 16 ? sp0 + (i & 31) : (i >> 5) * (32 * zw) + (i & 31);
+      const int wr = MAXW > 16 ? (sp1 - sp0) >> 5 : zw;
 #pragma unroll
-      for (int k = 0; k < MAXW; k++) v[k] = k < zw ? ld_stream(A.val + base + 32 * k, pol) : 0.f;
+      for (int k = 0; k < MAXW; k++) v[k] = k < wr ? ld_stream(A.val + base + 32 * k, pol) : 0.f;
       if constexpr (MAXW > 16) {
 #pragma unroll
         for (int k = 0; k < MAXW; k += 2) {
-          const unsigned a0 = k < zw ? (unsigned)(unsigned short)__ldg(A.colz + base + 32 * k) : 0u;
-          const unsigned a1 = k + 1 < zw ? (unsigned)(unsigned short)__ldg(A.colz + base + 32 * (k + 1)) : 0u;
+          const unsigned a0 = k < wr ? (unsigned)(unsigned short)__ldg(A.colz + base + 32 * k) : 0u;
+          const unsigned a1 = k + 1 < wr ? (unsigned)(unsigned short)__ldg(A.colz + base + 32 * (k + 1)) : 0u;
           dpk[k >> 1] = a0 | (a1 << 16);
         }
       } else {
@@ -501,17 +513,22 @@ __global__ void __launch_bounds__(BT, 1024 / BT) k_zcg_iter(ZcgArgs A) {
     // rows not served by the ring: loaded by the threads; the q^ of a trip is stored after
     // the next trip's loads are issued (or at the end of the launch)
     int i = c0 + tid;
+    static_assert(MAXW <= 16 || U2 == 1, "24-wide rows: one row per thread and trip");
+    if (i < hi) slice_of(i, sp0, sp1);
     for (; i + (U2 - 1) * BT < hi; i += U2 * BT) {  // U2 rows per thread and trip, loads first
       float v[U2][MAXW], d[U2], c[U2];
       int pid[U2];
       unsigned dpk[U2][kNDP];
 #pragma unroll
       for (int u = 0; u < U2; u++) fetch(i + u * BT, v[u], d[u], c[u], pid[u], dpk[u]);
+      if (MAXW > 16 && i + BT < hi) slice_of(i + BT, nsp0, nsp1);
       flush();
 #pragma unroll
       for (int u = 0; u < U2; u++) dq[u] = row(i + u * BT, v[u], d[u], c[u], pid[u], dpk[u]);
       dbase = i;
       dcnt = U2;
+      sp0 = nsp0;
+      sp1 = nsp1;
     }
     for (; i < hi; i += BT) {
       float v0[MAXW], d0, cc0;
@@ -642,7 +659,7 @@ __global__ void k_zprep(int64_t n, const int32_t* __restrict__ sptr, const int16
   int64_t base;
   int w;
   sell_row(sptr, r, base, w);
-  const int64_t fbase = ((r >> 5) * 32) * zw + (r & 31);
+  const int64_t fbase = zw > 0 ? ((r >> 5) * 32) * zw + (r & 31) : base;  // (zw 0: the sliced layout itself)
   const int dpart = (r & 1) ? -1 : 1;
   double rs = 0.0, ro = 0.0;  // same-component / other-component row sums
   for (int k = 0; k < w; k++) {
@@ -784,7 +801,7 @@ __global__ void k_zlayout(int64_t n, const int32_t* __restrict__ sptr, const int
   int64_t base;
   int w;
   sell_row(sptr, r, base, w);
-  const int64_t fbase = ((r >> 5) * 32) * zw + (r & 31);
+  const int64_t fbase = zw > 0 ? ((r >> 5) * 32) * zw + (r & 31) : base;  // (zw 0: the sliced layout itself)
   const int dpart = (r & 1) ? -1 : 1;
   bool found = false;
   for (int k = 0; k < w; k++) {
@@ -1005,7 +1022,11 @@ int zcg_plan(Solver& S, int sms) {
   ADFEM_TRY(S.dz32.alloc(n4));
   // FP64 copy in the sliced-ELL layout; FP32 copy and column deltas in the fixed-width layout
   const size_t ne = (size_t)std::max<int64_t>(A.nent, 1);
-  const size_t nf = (size_t)std::max<int64_t>(A.nslices, 1) * 32 * (size_t)S.zw;
+  // 24-wide rows (P2): the FP32 copy and the column deltas keep the sliced layout's variable
+  // slice widths (rows of one length are grouped into slices when the system is built);
+  // narrower rows: the fixed-width layout
+  S.zvarw = A.maxw > 16;
+  const size_t nf = S.zvarw ? ne : (size_t)std::max<int64_t>(A.nslices, 1) * 32 * (size_t)S.zw;
   ADFEM_TRY(S.valz64.alloc(sizeof(double) * ne));
   ADFEM_TRY(S.valz32.alloc(sizeof(float) * nf));
   ADFEM_TRY(S.colz16.alloc(sizeof(int16_t) * nf));
@@ -1015,7 +1036,7 @@ int zcg_plan(Solver& S, int sms) {
   DevBuf flag;
   ADFEM_TRY(flag.alloc(sizeof(int)));
   ADFEM_CUDA(cudaMemset(flag.p, 0, sizeof(int)));
-  k_zlayout<<<(unsigned)((S.n + kT - 1) / kT), kT>>>(S.n, A.sptr.as<int32_t>(), A.col.as<int16_t>(), S.zw,
+  k_zlayout<<<(unsigned)((S.n + kT - 1) / kT), kT>>>(S.n, A.sptr.as<int32_t>(), A.col.as<int16_t>(), S.zvarw ? 0 : S.zw,
                                                      S.colz16.as<int16_t>(), flag.as<int>());
   ADFEM_CUDA(cudaGetLastError());
   // legacy-stream sync, not a device-wide one: other threads may be capturing graphs on
@@ -1034,7 +1055,7 @@ int zcg_prepare(Solver& S, const int32_t* diagpos_dev, int* bad_dev, cudaStream_
   const Sell& A = *S.A;
   const unsigned nb = (unsigned)((S.n + kT - 1) / kT);
   k_zprep<<<nb, kT, 0, st>>>(S.n, A.sptr.as<int32_t>(), A.col.as<int16_t>(), A.val64.as<double>(), diagpos_dev,
-                             S.zw, S.zblock2 ? 1 : 0, S.valz64.as<double>(), S.valz32.as<float>(),
+                             S.zvarw ? 0 : S.zw, S.zblock2 ? 1 : 0, S.valz64.as<double>(), S.valz32.as<float>(),
                              S.dz32.as<float>(), S.zblock2 ? S.bz32.as<float2>() : nullptr, bad_dev);
   ADFEM_CUDA(cudaGetLastError());
   return ADFEM_OK;
@@ -1067,6 +1088,7 @@ static ZcgArgs zcg_args(Solver& S) {
   z.st = S.state.as<CgState>();
   z.partials = S.partials.as<double>();
   z.ns = S.zns;
+  z.sptr = A.sptr.as<int32_t>();
   z.refill = S.zrefill ? 1 : 0;
   return z;
 }
