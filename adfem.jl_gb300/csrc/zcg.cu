@@ -921,7 +921,9 @@ static int zcg_build_pool(Solver& S) {
 }
 
 // threads per block of a variant: 24-wide rows hold 24 values and 12 words of column
-// deltas per thread, which do not fit in the 64 registers of a 1024-thread block
+// deltas per thread, which do not fit in the 64 registers of a 1024-thread block (512-thread
+// blocks with two rows per thread and trip, 125 registers, measured 156 against 125 us per
+// iteration at 4M-DOF P2)
 template <int MAXW>
 constexpr int zbt() {
   return MAXW > 16 ? 768 : kZBT;
