@@ -1028,7 +1028,8 @@ int adfem_system_create(adfem_mesh* mesh, int kind, adfem_system** out) {
   if (p2) {
     std::lock_guard<std::mutex> lk(m.mu);
     ADFEM_TRY(mesh_space(&m, 2, &sp));
-    if (sp->maxrow > 24) return fail(ADFEM_ERR_UNSUPPORTED, "P2 systems support at most 24 entries per row");
+    // (rows of up to 24 entries take the banded mixed iteration, longer ones the scaled one)
+    if (sp->maxrow > 32) return fail(ADFEM_ERR_UNSUPPORTED, "P2 systems support at most 32 entries per row");
   }
   const int64_t nn = p2 ? sp->ndof : m.nv;
   const std::vector<int32_t>& RP = p2 ? sp->rowptr : m.rowptr;

@@ -838,19 +838,19 @@ cudaError_t launch_gen_poisson_system(const Mesh& m, const Space& sp, const doub
                (k_gen_ke<2, 0><<<g, kGT, 0, st>>>(m.ne, area, grad, kappa, ke)));
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return e;
-  if (sp.maxrow > 24) return cudaErrorNotSupported;  // (P2 rows of a triangle mesh: 19 for valence 6)
+  // (P2 rows of a triangle mesh: 19 entries for a vertex of valence 6, 25 for valence 8)
+  if (sp.maxrow > 32) return cudaErrorNotSupported;
   const unsigned gr = (unsigned)((sp.ndof + kRowBTs - 1) / kRowBTs);
   const int32_t* rp = sp.d_rowptr.as<int32_t>();
   const int32_t* ci = sp.d_colind.as<int32_t>();
   const int32_t* ip = sp.d_inc_ptr.as<int32_t>();
   const uint4* inc = sp.d_inc.as<uint4>();
-  GEN_DISPATCH(sp,
-               (k_gen_poisson_rows<1, 24><<<gr, kRowBTs, 0, st>>>(sp.ndof, rp, ci, ip, inc, area, ke, f, sptr, isbd,
-                                                                  bdval, sell_vals, rhs, nperm, kperm,
-                                                                  diagpos_space)),
-               (k_gen_poisson_rows<2, 24><<<gr, kRowBTs, 0, st>>>(sp.ndof, rp, ci, ip, inc, area, ke, f, sptr, isbd,
-                                                                  bdval, sell_vals, rhs, nperm, kperm,
-                                                                  diagpos_space)));
+#define ADFEM_GPR(DEG, W)                                                                                        \
+  k_gen_poisson_rows<DEG, W><<<gr, kRowBTs, 0, st>>>(sp.ndof, rp, ci, ip, inc, area, ke, f, sptr, isbd, bdval, \
+                                                     sell_vals, rhs, nperm, kperm, diagpos_space)
+  if (sp.maxrow <= 24) GEN_DISPATCH(sp, (ADFEM_GPR(1, 24)), (ADFEM_GPR(2, 24)));
+  else GEN_DISPATCH(sp, (ADFEM_GPR(1, 32)), (ADFEM_GPR(2, 32)));
+#undef ADFEM_GPR
   return cudaGetLastError();
 }
 

@@ -432,3 +432,48 @@ def test_p2_system_super_tiles_and_packed(oracle, gpulib, monkeypatch):
     (up,), (stp,) = gpulib.system.solve_packed([P], rtol=1e-12)
     assert stp.status == 0
     assert rel(up.cpu().numpy(), oracle.spsolve(Bs, rs)) < 1e-10
+
+
+def _union_jack(m):
+    """m x m unit-square grid whose cells are split along alternating diagonals: interior
+    vertices alternate between valence 4 and 8 (P2 rows of 25 entries)."""
+    x = np.linspace(0.0, 1.0, m + 1)
+    X, Y = np.meshgrid(x, x, indexing="xy")
+    coords = np.stack([X.ravel(), Y.ravel()], axis=1)
+    el = []
+    for j in range(m):
+        for i in range(m):
+            a, b = j * (m + 1) + i, j * (m + 1) + i + 1
+            c, d = a + m + 1, b + m + 1
+            if (i + j) % 2 == 0:
+                el += [(a, b, d), (a, d, c)]
+            else:
+                el += [(a, b, c), (b, d, c)]
+    return coords, np.array(el, dtype=np.int64) + 1
+
+
+def test_p2_system_long_rows_take_the_scaled_path(oracle, gpulib):
+    """P2 rows longer than the banded iteration's 24 (valence-8 vertices: 25 entries) are
+    assembled by the 32-wide row kernel and solved on the scaled mixed path."""
+    import torch
+
+    coords, elems = _union_jack(24)
+    O = oracle.OracleSpace(coords, elems, 2)
+    G = gpulib.Mesh(coords, elems, degree=2)
+    g = O.gauss_nodes()
+    kappa = 1.0 + g[:, 0] ** 2 + np.sin(3 * g[:, 1])
+    f = 1e3 * (1.0 + g[:, 0] - g[:, 1])
+    bd = O.bcnode()
+    B, r = oracle.dirichlet_csc(O.laplace_csc(kappa), O.source(f), bd, np.zeros(bd.size))
+    cp, _ = G.pattern()
+    assert np.diff(cp).max() > 24  # the P2 pattern (exact zeros included) has 25-entry rows
+    S = gpulib.PoissonSystem(G)
+    S.set_dirichlet(bd)
+    S.assemble(torch.tensor(kappa, device="cuda"), torch.tensor(f, device="cuda"))
+    assert S.solver_info()["banded"] == 0
+    assert rel(S.rhs().cpu().numpy(), r) < TOL
+    u0 = oracle.spsolve(B, r)
+    for prec, rtol in (("fp64", 1e-13), ("mixed", 1e-12)):
+        u = S.solve(precision=prec, rtol=rtol)
+        assert S.last_stats.status == 0
+        assert rel(u.cpu().numpy(), u0) < 1e-10
