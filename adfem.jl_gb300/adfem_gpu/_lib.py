@@ -33,7 +33,8 @@ class SolverStats(ctypes.Structure):
 class SolverInfo(ctypes.Structure):
     _fields_ = [("rows", c_ll), ("stored", c_ll), ("uniform_entries", c_ll), ("slices", c_ll), ("band", c_ll),
                 ("banded", c_i), ("blocks", c_i), ("rows_per_block", c_ll), ("ring", c_i), ("renumbered", c_i),
-                ("banded_fp64", c_i), ("fp64_tile_rows", c_i), ("ring_stages", c_i)]
+                ("banded_fp64", c_i), ("fp64_tile_rows", c_i), ("ring_stages", c_i),
+                ("assembly_pairs", c_i)]
 
 
 class ServerConfig(ctypes.Structure):

@@ -177,6 +177,9 @@ struct Mesh {
   DevBuf d_rowptr;   // int32 [nv+1]
   DevBuf d_colind;   // int32 [nnz]
   DevBuf d_diagpos;  // int32 [nv] position of the diagonal within its row
+  // geometry as FP32 pairs for the pair-arithmetic Poisson system kernel (built on first
+  // use, mesh_geo_pairs): gpa {g01, g02}, gpb {g12, w/6}, gpc {w/2}
+  DevBuf d_gpa, d_gpb, d_gpc;
 
   Sell sell;         // scalar pattern in sliced-ELL (values unused here)
   DevBuf d_sell2;    // (built lazily) interleaved 2-dof pattern: see Elasticity
@@ -236,6 +239,15 @@ cudaError_t launch_poisson_system(const Mesh& m, const double* sigma, const doub
                                   const double* bdval_dense, double* sell_vals, double* rhs, const int32_t* sptr,
                                   const int32_t* diagpos_mesh, const int32_t* nperm, const uint8_t* kperm,
                                   cudaStream_t st);
+// the same system in FP32-pair arithmetic (rows of up to 16 entries; the geometry pairs must
+// exist: mesh_geo_pairs): element pass (sigma_e and the load terms as pairs), then the rows
+int mesh_geo_pairs(Mesh& m);
+cudaError_t launch_element_prepass_pairs(const Mesh& m, const double* kappa, const double* f, float2* sigma,
+                                         float2* src3, cudaStream_t st);
+cudaError_t launch_poisson_system_pairs(const Mesh& m, const float2* sigma, const float2* src3, const uint8_t* isbd,
+                                        const double* bdval_dense, double* sell_vals, double* rhs,
+                                        const int32_t* sptr, const int32_t* diagpos_mesh, const int32_t* nperm,
+                                        const uint8_t* kperm, cudaStream_t st);
 // adjoint element kernel: grad_kappa[3e+k] = -w_e (grad lam_e).(grad u_e), lam zero on bd
 cudaError_t launch_poisson_kappa_grad(const Mesh& m, const double* u, const double* lam, const uint8_t* isbd,
                                       double* grad_kappa, cudaStream_t st);

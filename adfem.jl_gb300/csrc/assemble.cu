@@ -14,6 +14,7 @@
 //    (P1 element matrices have zero row sums).
 #include "adfem_internal.h"
 #include "checks.cuh"
+#include "pairs.cuh"
 
 namespace adfem {
 
@@ -248,6 +249,191 @@ __global__ void __launch_bounds__(kBlock) k_poisson_system(
   }
   rhs[ri] = r;
   for (int k = 0; k < w; k++) vals[base + 32 * (PERM ? (int)kperm[r0 + k] : k)] = acc[k][t];
+}
+
+// ---------------------------------------------------------------------------
+// The same fused Poisson system in FP32-pair arithmetic.  GB300 retires FP64 instructions
+// ~70x slower than FP32 / integer ones, and the FP64 kernels above are bound by them
+// (0.41 ms at 4M DOF for 184M FP64 operations, 0.7 of the FP64 issue rate); here every
+// operation is a pair operation (~48 bits: each value lands within ~1e-14 relative of the
+// FP64 one), the FP64 inputs are split into pairs with integer instructions (d2p, in the
+// element pass k_element_prepass_p: once per input) and each output costs one FP64 add
+// (p2d).  The thread owning node i walks its elements in ascending order as the FP64 kernel
+// does: the two off-diagonal entries g_ab sigma_e, g_ac sigma_e and the element's load term
+// for vertex a; the diagonal is the negated sum of the off-diagonals.  Geometry pairs per
+// element (gpa: g01, g02; gpb: g12, w/6; gpc: w/2) are derived once per mesh
+// (mesh_geo_pairs).  (Splitting kappa and f in this pass instead, once per vertex of each
+// element, measured 0.39 ms at 4M DOF against 0.41 ms for the FP64 kernels.)
+template <int MAXW, bool PERM>
+__global__ void __launch_bounds__(kBlock) k_poisson_system_p(
+    int64_t n, const int32_t* __restrict__ inc_ptr, const uint2* __restrict__ inc, const float4* __restrict__ gpa,
+    const float4* __restrict__ gpb, const float2* __restrict__ sigma, const float2* __restrict__ src3,
+    const int32_t* __restrict__ rowptr, const int32_t* __restrict__ colind,
+    const int32_t* __restrict__ diagpos, const int32_t* __restrict__ sptr, const uint8_t* __restrict__ isbd,
+    const double* __restrict__ bdval, double* __restrict__ vals, double* __restrict__ rhs,
+    const int32_t* __restrict__ nperm, const uint8_t* __restrict__ kperm) {
+  __shared__ float2 acc[MAXW][kBlock];
+  const int t = threadIdx.x;
+  const int64_t i = gtid();
+  if (i >= n) return;
+  const int w = rowptr[i + 1] - rowptr[i];
+  const int32_t r0 = rowptr[i];
+  const int64_t ri = PERM ? (int64_t)nperm[i] : i;
+  const int dp = diagpos[i];
+  const int64_t base = (int64_t)sptr[ri >> 5] + (ri & 31);
+  const uint8_t tag = isbd[ri];
+  if (tag == 1) {
+    const int dps = PERM ? (int)kperm[r0 + dp] : dp;
+    for (int k = 0; k < w; k++) vals[base + 32 * k] = (k == dps) ? 1.0 : 0.0;
+    rhs[ri] = bdval[ri];
+    return;
+  }
+  for (int k = 0; k < w; k++) acc[k][t] = make_float2(0.0f, 0.0f);
+  float2 r = make_float2(0.0f, 0.0f);
+  // incidences in batches of kIB: all record loads, then all element loads, then the sums
+  // (two dependent load steps per batch instead of two per incidence), in element order
+  constexpr int kIB = 4;
+  const int32_t s1 = inc_ptr[i + 1];
+  for (int32_t sb = inc_ptr[i]; sb < s1; sb += kIB) {
+    uint2 rec[kIB];
+#pragma unroll
+    for (int u = 0; u < kIB; u++) rec[u] = sb + u < s1 ? inc[sb + u] : make_uint2(0u, 0u);
+    float4 A[kIB];
+    float2 G[kIB], SG[kIB], SR[kIB];
+#pragma unroll
+    for (int u = 0; u < kIB; u++) {
+      const unsigned e = rec[u].x, a = inc_a(rec[u].y);
+      A[u] = gpa[e];
+      G[u] = reinterpret_cast<const float2*>(gpb)[2 * (int64_t)e];  // g12
+      SG[u] = sigma[e];
+      SR[u] = src3[3 * (int64_t)e + a];
+    }
+#pragma unroll
+    for (int u = 0; u < kIB; u++) {
+      if (sb + u >= s1) break;
+      const unsigned y = rec[u].y, a = inc_a(y);
+      const unsigned b = (a == 0) ? 1 : 0, c = (a == 2) ? 1 : 2;
+      const unsigned ob = inc_off(y, b), oc = inc_off(y, c);
+      if (!ADFEM_DCHECK(ob < (unsigned)w && oc < (unsigned)w && ob < MAXW && oc < MAXW)) continue;
+      // g of the pairs (a, b) and (a, c): (0,1) (0,2) for a = 0, (0,1) (1,2) for a = 1, (0,2) (1,2) for a = 2
+      const float2 g01 = make_float2(A[u].x, A[u].y), g02 = make_float2(A[u].z, A[u].w);
+      const float2 gab = a == 2 ? g02 : g01;
+      const float2 gac = a == 0 ? g02 : G[u];
+      acc[ob][t] = df_add(acc[ob][t], df_mul(gab, SG[u]));
+      acc[oc][t] = df_add(acc[oc][t], df_mul(gac, SG[u]));
+      r = df_add(r, SR[u]);
+    }
+  }
+  float2 d = make_float2(0.0f, 0.0f);
+  for (int k = 0; k < w; k++)
+    if (k != dp) d = df_add(d, acc[k][t]);
+  acc[dp][t] = df_neg(d);
+  if (tag == 2) {
+    for (int k = 0; k < w; k++) {
+      const int64_t j = PERM ? (int64_t)nperm[colind[r0 + k]] : (int64_t)colind[r0 + k];
+      if (isbd[j] == 1) {
+        r = df_add(r, df_neg(df_mul(acc[k][t], d2p(bdval[j]))));
+        acc[k][t] = make_float2(0.0f, 0.0f);
+      }
+    }
+  }
+  rhs[ri] = p2d(r);
+  for (int k = 0; k < w; k++) vals[base + 32 * (PERM ? (int)kperm[r0 + k] : k)] = p2d(acc[k][t]);
+}
+
+// Element pass of the pair-arithmetic system: sigma_e = kappa_0 + kappa_1 + kappa_2 and the
+// three load terms src_e[r] = w (S/6 + f_k*(r)/2) as FP32 pairs (each FP64 input split once
+// per element instead of once per vertex of the element)
+__global__ void k_element_prepass_p(int64_t ne, const double* __restrict__ kappa, const double* __restrict__ f,
+                                    const float4* __restrict__ gpb, const float2* __restrict__ gpc,
+                                    float2* __restrict__ sigma, float2* __restrict__ src3) {
+  const int64_t e = gtid();
+  if (e >= ne) return;
+  const double* kp = kappa + 3 * e;
+  sigma[e] = df_add(df_add(d2p(kp[0]), d2p(kp[1])), d2p(kp[2]));
+  const double* fp = f + 3 * e;
+  const float2 f0 = d2p(fp[0]), f1 = d2p(fp[1]), f2 = d2p(fp[2]);
+  const float4 B = gpb[e];
+  const float2 w6 = make_float2(B.z, B.w), w2 = gpc[e];
+  const float2 t = df_mul(df_add(df_add(f0, f1), f2), w6);
+  src3[3 * e] = df_add(t, df_mul(f0, w2));
+  src3[3 * e + 1] = df_add(t, df_mul(f2, w2));
+  src3[3 * e + 2] = df_add(t, df_mul(f1, w2));
+}
+
+// geometry pairs of every element from the FP64 geometry (once per mesh)
+__global__ void k_geo_pairs(int64_t ne, const double4* __restrict__ geo, float4* __restrict__ gpa,
+                            float4* __restrict__ gpb, float2* __restrict__ gpc) {
+  const int64_t e = gtid();
+  if (e >= ne) return;
+  const double4 g = geo[e];
+  auto split = [](double v) {
+    const float h = __double2float_rn(v);
+    return make_float2(h, __double2float_rn(v - (double)h));
+  };
+  const float2 a = split(g.x), b = split(g.y), c = split(g.z), w6 = split(g.w / 6.0), w2 = split(g.w * 0.5);
+  gpa[e] = make_float4(a.x, a.y, b.x, b.y);
+  gpb[e] = make_float4(c.x, c.y, w6.x, w6.y);
+  gpc[e] = w2;
+}
+
+int mesh_geo_pairs(Mesh& m) {
+  std::lock_guard<std::mutex> lk(m.mu);
+  if (m.d_gpc.p) return ADFEM_OK;
+  DevBuf a, b, c;
+  ADFEM_TRY(a.alloc(sizeof(float4) * (size_t)std::max<int64_t>(m.ne, 1)));
+  ADFEM_TRY(b.alloc(sizeof(float4) * (size_t)std::max<int64_t>(m.ne, 1)));
+  ADFEM_TRY(c.alloc(sizeof(float2) * (size_t)std::max<int64_t>(m.ne, 1)));
+  if (m.ne > 0) {
+    k_geo_pairs<<<nblocks(m.ne), kBlock>>>(m.ne, m.d_geo.as<double4>(), a.as<float4>(), b.as<float4>(),
+                                            c.as<float2>());
+    ADFEM_CUDA(cudaGetLastError());
+    // (legacy-stream sync, not a device-wide one: other threads may be capturing graphs)
+    ADFEM_CUDA(cudaStreamSynchronize(0));
+  }
+  std::swap(m.d_gpa.p, a.p);
+  std::swap(m.d_gpa.bytes, a.bytes);
+  std::swap(m.d_gpb.p, b.p);
+  std::swap(m.d_gpb.bytes, b.bytes);
+  std::swap(m.d_gpc.p, c.p);
+  std::swap(m.d_gpc.bytes, c.bytes);
+  return ADFEM_OK;
+}
+
+cudaError_t launch_element_prepass_pairs(const Mesh& m, const double* kappa, const double* f, float2* sigma,
+                                         float2* src3, cudaStream_t st) {
+  k_element_prepass_p<<<nblocks(m.ne), kBlock, 0, st>>>(m.ne, kappa, f, m.d_gpb.as<float4>(), m.d_gpc.as<float2>(),
+                                                         sigma, src3);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_poisson_system_pairs(const Mesh& m, const float2* sigma, const float2* src3, const uint8_t* isbd,
+                                        const double* bdval_dense, double* sell_vals, double* rhs,
+                                        const int32_t* sptr, const int32_t* diagpos_mesh, const int32_t* nperm,
+                                        const uint8_t* kperm, cudaStream_t st) {
+  const auto* ip = m.d_inc_ptr.as<int32_t>();
+  const auto* inc = m.d_inc.as<uint2>();
+  const auto* gpa = m.d_gpa.as<float4>();
+  const auto* gpb = m.d_gpb.as<float4>();
+  const auto* rp = m.d_rowptr.as<int32_t>();
+  const auto* ci = m.d_colind.as<int32_t>();
+  const unsigned nb = nblocks(m.nv);
+#define ADFEM_PSP(W)                                                                                             \
+  do {                                                                                                           \
+    if (nperm)                                                                                                   \
+      k_poisson_system_p<W, true><<<nb, kBlock, 0, st>>>(m.nv, ip, inc, gpa, gpb, sigma, src3, rp, ci,            \
+                                                         diagpos_mesh, sptr, isbd, bdval_dense, sell_vals, rhs,  \
+                                                         nperm, kperm);                                          \
+    else                                                                                                         \
+      k_poisson_system_p<W, false><<<nb, kBlock, 0, st>>>(m.nv, ip, inc, gpa, gpb, sigma, src3, rp, ci,           \
+                                                          diagpos_mesh, sptr, isbd, bdval_dense, sell_vals, rhs, \
+                                                          nullptr, nullptr);                                     \
+  } while (0)
+  if (m.maxrow <= 8) ADFEM_PSP(8);
+  else if (m.maxrow <= 16) ADFEM_PSP(16);
+  else return cudaErrorNotSupported;  // (the FP64 kernel serves wider rows)
+#undef ADFEM_PSP
+  return cudaGetLastError();
 }
 
 cudaError_t launch_poisson_system(const Mesh& m, const double* sigma, const double* src3, const uint8_t* isbd,

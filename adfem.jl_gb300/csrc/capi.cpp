@@ -52,6 +52,9 @@ struct adfem_system {
   DevBuf in0, in1;                  // host-staging of per-Gauss-point inputs
   Solver solver;
   bool assembled = false;
+  // P1 Poisson assembly in FP32-pair arithmetic (rows of up to 16 entries;
+  // ADFEM_ASM_PAIRS=0 at creation selects the FP64 kernels)
+  bool pairs = false;
   std::mutex mu;
 };
 
@@ -1103,6 +1106,8 @@ int adfem_system_create(adfem_mesh* mesh, int kind, adfem_system** out) {
   }
   if (kind == ADFEM_SYS_POISSON) {
     s->ndof = nn;
+    const char* penv = std::getenv("ADFEM_ASM_PAIRS");
+    s->pairs = !p2 && m.maxrow <= 16 && !(penv && penv[0] == '0');
     ADFEM_TRY(sell_build_pattern(nn, rpS.data(), ciS.data(), s->A, 1));
     ADFEM_TRY(to_dev(s->diagpos, dpS.data(), dpS.size()));
     if (s->renumbered) ADFEM_TRY(to_dev(s->dofmap, pi.data(), pi.size()));
@@ -1193,18 +1198,37 @@ static int assemble_poisson(adfem_system* sys, const double* kappa_d, const doub
     sys->assembled = true;
     return ADFEM_OK;
   }
-  ADFEM_TRY(sys->sigma.alloc(sizeof(double) * m.ne));
-  ADFEM_TRY(sys->src3.alloc(sizeof(double) * 3 * m.ne));
-  if (ev) ADFEM_CUDA(cudaEventRecord(ev[0], st));
-  ADFEM_TRY(kerr(launch_element_prepass(m, kappa_d, f_d, sys->sigma.as<double>(), sys->src3.as<double>(), st),
-                 "element prepass"));
-  if (ev) ADFEM_CUDA(cudaEventRecord(ev[1], st));
-  ADFEM_TRY(kerr(launch_poisson_system(m, sys->sigma.as<double>(), sys->src3.as<double>(), sys->isbd.as<uint8_t>(),
-                                       sys->bdval.as<double>(), sys->A.val64.as<double>(), sys->rhs.as<double>(),
-                                       sys->A.sptr.as<int32_t>(), m.d_diagpos.as<int32_t>(),
-                                       sys->renumbered ? sys->nperm.as<int32_t>() : nullptr,
-                                       sys->renumbered ? sys->kperm.as<uint8_t>() : nullptr, st),
-                 "poisson system"));
+  if (sys->pairs) {
+    // FP32-pair arithmetic: element pass (sigma and load terms as pairs, 32 B per element),
+    // then the rows
+    ADFEM_TRY(mesh_geo_pairs(m));
+    ADFEM_TRY(sys->sigma.alloc(sizeof(float2) * m.ne));
+    ADFEM_TRY(sys->src3.alloc(sizeof(float2) * 3 * m.ne));
+    if (ev) ADFEM_CUDA(cudaEventRecord(ev[0], st));
+    ADFEM_TRY(kerr(launch_element_prepass_pairs(m, kappa_d, f_d, sys->sigma.as<float2>(), sys->src3.as<float2>(), st),
+                   "element prepass (pairs)"));
+    if (ev) ADFEM_CUDA(cudaEventRecord(ev[1], st));
+    ADFEM_TRY(kerr(launch_poisson_system_pairs(m, sys->sigma.as<float2>(), sys->src3.as<float2>(),
+                                               sys->isbd.as<uint8_t>(), sys->bdval.as<double>(),
+                                               sys->A.val64.as<double>(), sys->rhs.as<double>(),
+                                               sys->A.sptr.as<int32_t>(), m.d_diagpos.as<int32_t>(),
+                                               sys->renumbered ? sys->nperm.as<int32_t>() : nullptr,
+                                               sys->renumbered ? sys->kperm.as<uint8_t>() : nullptr, st),
+                   "poisson system (pairs)"));
+  } else {
+    ADFEM_TRY(sys->sigma.alloc(sizeof(double) * m.ne));
+    ADFEM_TRY(sys->src3.alloc(sizeof(double) * 3 * m.ne));
+    if (ev) ADFEM_CUDA(cudaEventRecord(ev[0], st));
+    ADFEM_TRY(kerr(launch_element_prepass(m, kappa_d, f_d, sys->sigma.as<double>(), sys->src3.as<double>(), st),
+                   "element prepass"));
+    if (ev) ADFEM_CUDA(cudaEventRecord(ev[1], st));
+    ADFEM_TRY(kerr(launch_poisson_system(m, sys->sigma.as<double>(), sys->src3.as<double>(),
+                                         sys->isbd.as<uint8_t>(), sys->bdval.as<double>(), sys->A.val64.as<double>(),
+                                         sys->rhs.as<double>(), sys->A.sptr.as<int32_t>(), m.d_diagpos.as<int32_t>(),
+                                         sys->renumbered ? sys->nperm.as<int32_t>() : nullptr,
+                                         sys->renumbered ? sys->kperm.as<uint8_t>() : nullptr, st),
+                   "poisson system"));
+  }
   if (ev) ADFEM_CUDA(cudaEventRecord(ev[2], st));
   ADFEM_TRY(solver_prepare(sys->solver, sys->diagpos.as<int32_t>(), st));
   if (ev) ADFEM_CUDA(cudaEventRecord(ev[3], st));
@@ -1326,6 +1350,7 @@ int adfem_system_solver_info(const adfem_system* sys, adfem_solver_info* info) {
   info->banded_fp64 = sv.dcg ? 1 : 0;
   info->fp64_tile_rows = sv.dcg ? sv.dS : 0;
   info->ring_stages = sv.zcg ? sv.zns : 0;
+  info->assembly_pairs = sys->pairs ? 1 : 0;
   return ADFEM_OK;
 }
 

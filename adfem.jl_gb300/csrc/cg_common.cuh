@@ -2,6 +2,7 @@
 // sliced-ELL row access, deterministic block/grid reductions, the FP32 hi+lo axpy
 // and the residual-replacement bookkeeping of the mixed solves.
 #pragma once
+#include "pairs.cuh"
 #include "solver.cuh"
 
 namespace adfem {
@@ -67,45 +68,6 @@ __device__ __forceinline__ float2 warp_sum_pair(float v) {
     h = s;
   }
   return make_float2(h, l);
-}
-
-// ---- double-float arithmetic: a value as an unevaluated FP32 pair h + l (~48 bits).
-// Explicitly rounded intrinsics keep the compiler from fusing or reassociating the error
-// terms.  Used where FP64 would put long chains of dependent FP64 instructions on the
-// critical path: on GB300 an FP64 instruction has a long latency as well as a low rate,
-// and the end-of-launch reduction of the banded iteration (one warp, then one thread)
-// measured ~10 us per iteration with FP64 sums and divisions.
-__device__ __forceinline__ float2 df_norm(float s, float e) {
-  const float h = __fadd_rn(s, e);
-  return make_float2(h, __fsub_rn(e, __fsub_rn(h, s)));
-}
-__device__ __forceinline__ float2 df_add(float2 a, float2 b) {
-  const float s = __fadd_rn(a.x, b.x);
-  const float bb = __fsub_rn(s, a.x);
-  float e = __fadd_rn(__fsub_rn(a.x, __fsub_rn(s, bb)), __fsub_rn(b.x, bb));
-  e = __fadd_rn(e, __fadd_rn(a.y, b.y));
-  return df_norm(s, e);
-}
-__device__ __forceinline__ float2 df_neg(float2 a) { return make_float2(-a.x, -a.y); }
-__device__ __forceinline__ float2 df_mul(float2 a, float2 b) {
-  const float p = __fmul_rn(a.x, b.x);
-  float e = fmaf(a.x, b.x, -p);
-  e = fmaf(a.x, b.y, e);
-  e = fmaf(a.y, b.x, e);
-  return df_norm(p, e);
-}
-__device__ __forceinline__ float2 df_div(float2 a, float2 b) {
-  const float q1 = __fdiv_rn(a.x, b.x);
-  const float2 r = df_add(a, df_neg(df_mul(make_float2(q1, 0.0f), b)));
-  const float q2 = __fdiv_rn(r.x, b.x);
-  return df_norm(q1, q2);
-}
-__device__ __forceinline__ double df_to_d(float2 a) { return (double)a.x + (double)a.y; }
-// a <= b for normalised pairs (|l| at most half an ulp of h)
-__device__ __forceinline__ bool df_le(float2 a, float2 b) { return a.x < b.x || (a.x == b.x && a.y <= b.y); }
-__device__ __forceinline__ float2 d_to_df(double d) {
-  const float h = (float)d;
-  return make_float2(h, (float)(d - (double)h));
 }
 
 // Sum of two FP32 pairs with an error-free two-sum of the high parts (the butterfly step of

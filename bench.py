@@ -1117,16 +1117,21 @@ def run_ours(args, rank, world, dist):
     ne_ = mesh.nelem
     ng_ = 3 * ne_
     # algorithmic bytes of the assembly proper (element pass + rows): kappa and f at the
-    # Gauss points, per-element geometry (32 B) and the three incidence records (24 B), the
-    # operator values (8 B per stored entry) and the load vector
-    asm_bytes = 16 * ng_ + 56 * ne_ + 8 * nent + 8 * n
+    # Gauss points, per-element geometry (32 B as FP64; 40 B as the FP32 pairs of the
+    # pair-arithmetic kernel) and the three incidence records (24 B), the operator values
+    # (8 B per stored entry) and the load vector
+    pairs_asm = bool(S.solver_info().get("assembly_pairs", 0))
+    asm_bytes = 16 * ng_ + ((40 if pairs_asm else 32) + 24) * ne_ + 8 * nent + 8 * n
     asm_s = (ph[0] + ph[1]) * 1e-3
     # the Laplace-assembly byte model of the scope table: kappa at the Gauss points, node
     # coordinates, connectivity, a 36-byte element-to-CSR-slot map, each CSR value written once
     nnz_ = int(mesh.pattern()[1].size)
     laplace_bytes = 8 * ng_ + 16 * n + 12 * ne_ + 36 * ne_ + 8 * nnz_
-    fp64_ops = 11 * ne_ + 24 * n  # element pass; rows: 2 FMA per incidence, diagonal, load gather
-    assembly = {"element_pass_ms": ph[0], "rows_ms": ph[1], "solver_conversion_ms": ph[2], "total_ms": asm_ms,
+    # FP64 kernels: element pass 11 per element; rows: 2 FMA per incidence, diagonal, load
+    # gather.  Pair kernel: one FP64 add per output value (the pair -> FP64 conversion)
+    fp64_ops = (nent + n) if pairs_asm else 11 * ne_ + 24 * n
+    assembly = {"arithmetic": "fp32 pairs, one pass" if pairs_asm else "fp64, element pass + rows",
+                "element_pass_ms": ph[0], "rows_ms": ph[1], "solver_conversion_ms": ph[2], "total_ms": asm_ms,
                 "bytes": asm_bytes, "achieved_gbs": asm_bytes / asm_s / 1e9, "hbm_frac": asm_bytes / asm_s / 1e9 / hbm,
                 "laplace_model_bytes": laplace_bytes,
                 "hbm_frac_laplace_model": laplace_bytes / asm_s / 1e9 / hbm,

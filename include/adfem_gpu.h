@@ -402,6 +402,7 @@ typedef struct adfem_solver_info {
   int fp64_tile_rows;         /* rows per super-tile of the banded FP64 iteration (0 if not used) */
   int ring_stages;            /* stages of the shared-memory matrix ring of the banded mixed iteration
                                  (bulk copies of 1024 rows each; 0: values loaded by the threads) */
+  int assembly_pairs;         /* 1: the Poisson assembly runs in FP32-pair arithmetic in one pass */
 } adfem_solver_info;
 ADFEM_API int adfem_system_solver_info(const adfem_system *sys, adfem_solver_info *info);
 /* Packed solves of small systems: the systems (each assembled, at most 65536 DOFs,
