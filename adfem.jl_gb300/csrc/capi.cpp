@@ -52,8 +52,10 @@ struct adfem_system {
   DevBuf in0, in1;                  // host-staging of per-Gauss-point inputs
   Solver solver;
   bool assembled = false;
-  // P1 Poisson assembly in FP32-pair arithmetic (rows of up to 16 entries;
-  // ADFEM_ASM_PAIRS=0 at creation selects the FP64 kernels)
+  // P1 Poisson assembly in FP32-pair arithmetic (opt-in with ADFEM_ASM_PAIRS=1 at creation;
+  // rows of up to 16 entries).  Not the default: its ~1e-14 relative differences in the
+  // matrix entries moved the 4M-DOF mixed solution from 1.7e-11 to 6.7e-11 relative error
+  // against the refined FP64 reference, for an assembly 0.05 ms faster.
   bool pairs = false;
   std::mutex mu;
 };
@@ -1107,7 +1109,7 @@ int adfem_system_create(adfem_mesh* mesh, int kind, adfem_system** out) {
   if (kind == ADFEM_SYS_POISSON) {
     s->ndof = nn;
     const char* penv = std::getenv("ADFEM_ASM_PAIRS");
-    s->pairs = !p2 && m.maxrow <= 16 && !(penv && penv[0] == '0');
+    s->pairs = !p2 && m.maxrow <= 16 && penv && penv[0] == '1';
     ADFEM_TRY(sell_build_pattern(nn, rpS.data(), ciS.data(), s->A, 1));
     ADFEM_TRY(to_dev(s->diagpos, dpS.data(), dpS.size()));
     if (s->renumbered) ADFEM_TRY(to_dev(s->dofmap, pi.data(), pi.size()));
