@@ -279,3 +279,32 @@ def test_not_converged_and_breakdown_are_statuses(oracle, gpulib):
     kn[5] = float("nan")
     with pytest.raises(AdFemError):
         S.assemble(kn, f)
+
+
+@pytest.mark.parametrize("bdval", [False, True])
+def test_pair_arithmetic_assembly(oracle, gpulib, monkeypatch, bdval):
+    """The opt-in FP32-pair-arithmetic assembly of resident P1 Poisson systems
+    (ADFEM_ASM_PAIRS=1): right-hand side and operator against the oracle's Dirichlet-imposed
+    system at the 1e-12 value bar, and the FP64 and mixed solves against the direct solve."""
+    import torch
+
+    monkeypatch.setenv("ADFEM_ASM_PAIRS", "1")
+    coords, elems = synth.jittered_square(48, seed=5)
+    O = oracle.OracleMesh(coords, elems)
+    g = O.gauss_nodes()
+    kappa, f = synth.poisson_c1_fields(g[:, 0], g[:, 1])
+    bd = O.bcnode()
+    bv = (np.sin(3 * coords[bd - 1, 0]) + coords[bd - 1, 1]) if bdval else np.zeros(bd.size)
+    B, r = oracle.dirichlet_csc(O.laplace_csc(kappa), O.source(f), bd, bv)
+    S = gpulib.PoissonSystem(gpulib.Mesh(coords, elems))
+    S.set_dirichlet(bd, bv)
+    S.assemble(torch.tensor(kappa, device="cuda"), torch.tensor(f, device="cuda"))
+    assert S.solver_info()["assembly_pairs"] == 1
+    assert rel(S.rhs().cpu().numpy(), r) < 1e-12
+    x = np.random.default_rng(1).standard_normal(O.ndof)
+    assert rel(S.apply(torch.tensor(x, device="cuda")).cpu().numpy(), B @ x) < 1e-12
+    u0 = oracle.spsolve(B, r)
+    for prec in ("fp64", "mixed"):
+        u = S.solve(precision=prec, rtol=RTOL[prec])
+        assert S.last_stats.status == 0
+        assert rel(u.cpu().numpy(), u0) < 1e-9
