@@ -1111,7 +1111,13 @@ static void zlaunch(Kern kern, const Solver& S, cudaStream_t st, const ZcgArgs& 
   at[0].val.programmaticStreamSerializationAllowed = 1;
   cfg.attrs = at;
   cfg.numAttrs = S.zpdl ? 1 : 0;
-  cudaLaunchKernelEx(&cfg, kern, z);
+  if (cudaLaunchKernelEx(&cfg, kern, z) != cudaSuccess && S.zpdl) {
+    // without the attribute (the launch then reports its own error, if any, to the caller's
+    // cudaGetLastError)
+    (void)cudaGetLastError();
+    cfg.numAttrs = 0;
+    cudaLaunchKernelEx(&cfg, kern, z);
+  }
 }
 
 void zcg_enqueue_iter(Solver& S, cudaStream_t st) {
