@@ -36,6 +36,13 @@
 // so every warp keeps its loads in flight independently.  Halo positions belong to
 // neighbouring blocks and are recomputed there bit-identically; the Z, P and q^ buffers
 // are ping-pong pairs, so halos always read the previous iteration's values.
+//
+// Variants: 8-wide rows (P1 Poisson; an opt-in RING form streams the matrix through
+// shared memory), 16-wide rows (plain, or the node-block form B2 of interleaved 2-DOF
+// elasticity), 24-wide rows in 768-thread blocks reading the sliced layout with per-slice
+// widths (P2).  The four dot products are reduced by reduce4_arrive / reduce4_finish; each
+// thread's last q^ stores are issued after its block is counted in.  Launches are
+// programmatic dependent launches (griddepcontrol) in the solver's graphs.
 #include <cstdlib>
 #include <mutex>
 #include <vector>
@@ -55,8 +62,8 @@ struct ZcgArgs {
   const int32_t* zpid;  // per slice: id of its column pattern in `pool`, or -1 (per-entry deltas in colz)
   const int32_t* pool;  // [pattern id][period][MAXW] column deltas, padded with 0 (copied to shared memory)
   int npool;            // ints in pool
-  const int16_t* colz;  // fixed-width sliced-ELL column deltas
-  const float* val;   // fixed-width sliced-ELL values, FP32 difference form, physical scale
+  const int16_t* colz;  // column deltas (fixed-width layout; 24-wide: the sliced layout)
+  const float* val;   // FP32 difference-form values, physical scale (same layout as colz)
   const float* dz;    // fp32(K_ii)
   const float2* bz;   // B2: per row {K_ii, K_(i,i^1)} in FP32, the row of its node's 2x2 block
   float* z[2];
