@@ -797,6 +797,37 @@ def run_c4(A, args):
     torch.cuda.synchronize()
     out["grads_per_s"] = args.c4_steps / (time.perf_counter() - t0)
     out["grad_norm"] = float(gE.norm())
+    # the E-gradient at full size: FP64 adjoint gradient against central differences of the
+    # misfit (FP64 solves at rtol 1e-13, warm-started from the unperturbed solution) along
+    # random unit directions, and the mixed gradient against the FP64 one
+    if args.c4_dirs > 0:
+        def loss(Ev, grad):
+            S.assemble(Ev, nu, fx, fy)
+            uu = u_ref.clone()
+            S.solve(uu, precision="fp64", rtol=1e-13, warm=True)
+            r = uu[obs] - uobs
+            if not grad:
+                return float((r * r).sum()), None
+            g = torch.zeros_like(uu)
+            g[obs] = 2 * r
+            lm = S.adjoint(g, precision="fp64", rtol=1e-13)
+            return float((r * r).sum()), S.grad_E(uu, lm, Ev, nu)
+
+        _, g64 = loss(E, True)
+        eps = 1e-4 * float(E.norm())
+        gen = torch.Generator(device="cuda").manual_seed(8)
+        errs, errs_n = [], []
+        for _ in range(args.c4_dirs):
+            d = torch.randn(E.numel(), dtype=torch.float64, device="cuda", generator=gen)
+            d /= d.norm()
+            an = float((g64 * d).sum())
+            fd = (loss(E + eps * d, False)[0] - loss(E - eps * d, False)[0]) / (2 * eps)
+            errs.append(abs(fd - an) / max(abs(an), 1e-300))
+            errs_n.append(abs(fd - an) / float(g64.norm()))
+        S.assemble(E, nu, fx, fy)
+        out["grad_check"] = {"directions": args.c4_dirs, "eps": eps, "max_rel_err": max(errs),
+                             "median_rel_err": statistics.median(errs), "max_err_over_grad_norm": max(errs_n),
+                             "grad_mixed_vs_fp64_rel": float((gE - g64).norm() / g64.norm())}
     return out
 
 
@@ -1269,6 +1300,7 @@ def main():
     ap.add_argument("--c2-dirs", type=int, default=32, help="finite-difference directions of the gradient check")
     ap.add_argument("--c4-m", type=int, default=1000, help="elasticity cells per side (0 skips)")
     ap.add_argument("--c4-steps", type=int, default=1)
+    ap.add_argument("--c4-dirs", type=int, default=4, help="finite-difference directions of the E-gradient check")
     ap.add_argument("--p2-m", type=int, default=1000, help="P2 / mass / interpolation ops cells per side (0 skips)")
     ap.add_argument("--p2-cpu-m", type=int, default=120, help="P2 oracle sample cells per side")
     ap.add_argument("--p2-solve-m", type=int, default=200, help="P2 exact-solution solve cells per side")
