@@ -308,3 +308,47 @@ def test_pair_arithmetic_assembly(oracle, gpulib, monkeypatch, bdval):
         u = S.solve(precision=prec, rtol=RTOL[prec])
         assert S.last_stats.status == 0
         assert rel(u.cpu().numpy(), u0) < 1e-9
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_elasticity_gradient_matches_reference_chain(oracle, gpulib, precision):
+    """dL/dE of a resident elasticity system against the reference's backward ops composed on
+    the CPU: sparse-solve gradient -lam_i u_j per stored COO entry (lam zero on Dirichlet
+    DOFs), ComputeFemStiffnessMatrixMfem backward (ComputeFemStiffnessMatrixMfem.h:50-81),
+    then PlaneStrainAndStress backward (PlaneStrainAndStress.h:20-44)."""
+    import torch
+
+    coords, elems = synth.jittered_square(16, seed=3)
+    O = oracle.OracleMesh(coords, elems)
+    g = O.gauss_nodes()
+    E = 1e9 * np.exp(0.3 * synth.fourier_field(g[:, 0], g[:, 1], seed=5))
+    nu = np.full(O.ngauss, 0.3)
+    D = oracle.plane_strain(E, nu, 0)
+    fx, fy = np.full(O.ngauss, 2e5), np.full(O.ngauss, -1e6)
+    left = synth.left_edge_nodes(coords)
+    bd = np.concatenate([left + 1, left + 1 + O.ndof])
+    B, r = oracle.dirichlet_csc(O.stiffness_csc(D), np.concatenate([O.source(fx), O.source(fy)]), bd,
+                                np.zeros(bd.size))
+    u0 = oracle.spsolve(B, r)
+    obs = synth.observation_nodes(2 * O.ndof, seed=9, frac=0.05)
+    uobs = 1.01 * u0[obs]
+    gu = np.zeros(2 * O.ndof)
+    gu[obs] = 2 * (u0[obs] - uobs)
+    gz = gu.copy()
+    gz[bd - 1] = 0.0
+    lam0 = oracle.spsolve(B.T.tocsc(), gz)
+    lam0[bd - 1] = 0.0
+    idx, _ = O.stiffness_coo(D)
+    gD = O.stiffness_coo_backward(-lam0[idx[:, 0]] * u0[idx[:, 1]])
+    gE_ref, _ = oracle.plane_strain_backward(gD.reshape(-1), E, nu, 0)
+
+    S = gpulib.ElasticitySystem(gpulib.Mesh(coords, elems))
+    S.set_dirichlet(bd)
+    t = lambda a: torch.tensor(a, device="cuda")  # noqa: E731
+    S.assemble(t(E), t(nu), t(fx), t(fy))
+    u = S.solve(precision=precision, rtol=RTOL[precision])
+    assert S.last_stats.status == 0 and rel(u.cpu().numpy(), u0) < 1e-9
+    lam = S.adjoint(t(gu), precision=precision, rtol=RTOL[precision])
+    assert S.last_stats.status == 0 and rel(lam.cpu().numpy(), lam0) < 1e-9
+    gE = S.grad_E(u, lam, t(E), t(nu)).cpu().numpy()
+    assert rel(gE, gE_ref) < 1e-7
