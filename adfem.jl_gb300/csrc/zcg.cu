@@ -525,8 +525,37 @@ __global__ void __launch_bounds__(BT, 1024 / BT) k_zcg_iter(ZcgArgs A) {
     // the next trip's loads are issued (or at the end of the launch)
     int i = c0 + tid;
     static_assert(MAXW <= 16 || U2 == 1, "24-wide rows: one row per thread and trip");
-    if (i < hi) slice_of(i, sp0, sp1);
-    for (; i + (U2 - 1) * BT < hi; i += U2 * BT) {  // U2 rows per thread and trip, loads first
+    if constexpr (MAXW > 16) {
+      // 24-wide rows are grouped by length within windows of 8 slices, so the slice width
+      // depends on the slice's position in its window; with a fixed warp -> slice map and a
+      // multiple of 8 warps, warp w would take the slice at position w mod 8 on every trip
+      // and the warps of the widest positions would finish last.  The warp's slice of the
+      // trip rotates by one per trip: each warp meets every position, and the rows of a trip
+      // are still the BT rows from the trip's first row (a thread's rows increase, so it stops
+      // at its first row past hi)
+      constexpr int kNW = BT / 32;
+      int slot = tid >> 5;
+      int tb = c0;  // the trip's first row
+      if (i < hi) slice_of(i, sp0, sp1);
+      while (i < hi) {
+        float v0[MAXW], d0, cc0;
+        int g0;
+        unsigned dp0[kNDP];
+        fetch(i, v0, d0, cc0, g0, dp0);
+        tb += BT;
+        slot = slot + 1 == kNW ? 0 : slot + 1;
+        const int ni = tb + 32 * slot + (tid & 31);
+        if (ni < hi) slice_of(ni, nsp0, nsp1);
+        flush();
+        dq[0] = row(i, v0, d0, cc0, g0, dp0);
+        dbase = i;
+        dcnt = 1;
+        sp0 = nsp0;
+        sp1 = nsp1;
+        i = ni;
+      }
+    }
+    for (; MAXW <= 16 && i + (U2 - 1) * BT < hi; i += U2 * BT) {  // U2 rows per thread and trip, loads first
       float v[U2][MAXW], d[U2], c[U2];
       int pid[U2];
       unsigned dpk[U2][kNDP];
@@ -541,7 +570,7 @@ __global__ void __launch_bounds__(BT, 1024 / BT) k_zcg_iter(ZcgArgs A) {
       sp0 = nsp0;
       sp1 = nsp1;
     }
-    for (; i < hi; i += BT) {
+    for (; MAXW <= 16 && i < hi; i += BT) {
       float v0[MAXW], d0, cc0;
       int g0;
       unsigned dp0[kNDP];
