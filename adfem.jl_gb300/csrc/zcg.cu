@@ -400,6 +400,9 @@ __global__ void __launch_bounds__(BT, 1024 / BT) k_zcg_iter(ZcgArgs A) {
     }
     __syncthreads();
     // ---- phase 2: q = K P_k for the rows [lo, hi)
+    // 24-wide rows: slice offsets of the sliced layout for this thread's row of the trip
+    // (sp0, sp1), loaded one trip ahead (nsp0, nsp1) so that the value loads do not wait for them
+    int sp0 = 0, sp1 = 0, nsp0 = 0, nsp1 = 0;
     auto row = [&](int i, const float (&v)[MAXW], float d, float c, int pid, const unsigned (&dpk)[kNDP]) -> float {
       const float Pi = sP[i - wlo];
       const float Pp = B2 ? sP[(i ^ 1) - wlo] : Pi;  // partner DOF (B2: rows come in even/odd pairs)
@@ -426,9 +429,13 @@ __global__ void __launch_bounds__(BT, 1024 / BT) k_zcg_iter(ZcgArgs A) {
 #pragma unroll
         for (int k = 0; k < MAXW; k++) dl[k] = k < zw ? (int)__ldg(A.colz + base + 32 * k) : 0;
       }
+      // (24-wide rows: the slice's own width, uniform over the warp, ends the row: a 9-entry
+      // edge row does not spend the instructions of 24)
+      const int wrow = MAXW > 16 ? (sp1 - sp0) >> 5 : MAXW;
       float s = 0.f;
 #pragma unroll
       for (int k = 0; k < MAXW; k++) {
+        if (k >= wrow) break;
         const int dk = MAXW > 16 ? (int)(short)(dpk[k >> 1] >> (16 * (k & 1))) : dl[MAXW > 16 ? 0 : k];
         float tv;
         if (dk == 0) tv = Pi;
@@ -458,9 +465,6 @@ __global__ void __launch_bounds__(BT, 1024 / BT) k_zcg_iter(ZcgArgs A) {
     };
     // fixed-width layout: entry k of row i at (i>>5)*32*zw + 32k + (i&31) (padding: value 0,
     // delta 0), so the loads of a row depend on nothing but i
-    // 24-wide rows: slice offsets of the sliced layout for this thread's row of the trip
-    // (sp0, sp1), loaded one trip ahead (nsp0, nsp1) so that the value loads do not wait for them
-    int sp0 = 0, sp1 = 0, nsp0 = 0, nsp1 = 0;
     auto slice_of = [&](int i, int& a, int& b) {
       if constexpr (MAXW > 16) {
         a = __ldg(A.sptr + (i >> 5));
