@@ -1306,6 +1306,8 @@ def main():
     ap.add_argument("--p2-solve-m", type=int, default=200, help="P2 exact-solution solve cells per side")
     ap.add_argument("--only-p2", action="store_true",
                     help="profiling aid: run only the P2 / mass / interpolation leg and print it")
+    ap.add_argument("--only-c4", action="store_true",
+                    help="profiling aid: run only the elasticity leg and print it")
     ap.add_argument("--trace-iters", type=int, default=0,
                     help="profiling aid: run one truncated step (this many CG iterations) and exit")
     args = ap.parse_args()
@@ -1316,10 +1318,15 @@ def main():
     dist = None
     if args.impl == "reference":
         return run_reference(args, rank, world)
-    if args.only_p2 or args.only_serve:
+    if args.only_p2 or args.only_serve or args.only_c4:
         import adfem_gpu as A
 
-        out = {"p2_4M": run_p2(A, args)} if args.only_p2 else {"serve": run_serve(A, args)}
+        if args.only_p2:
+            out = {"p2_4M": run_p2(A, args)}
+        elif args.only_c4:
+            out = {"elasticity_2M": run_c4(A, args)}
+        else:
+            out = {"serve": run_serve(A, args)}
         print(json.dumps(out), flush=True)
         return 0
     if world > 1:
