@@ -222,6 +222,10 @@ enum class Layout { CSR = 0, CSRT = 1, SELL = 2 };
 // src_e[r] = w * sum_k f_k phi_r(x_k) (may be null)
 cudaError_t launch_element_prepass(const Mesh& m, const double* kappa, const double* f, double* sigma,
                                    double* src3, cudaStream_t st);
+// the same with src_e[r] = sum_k f_k phi_r(x_k), without the weight w (the input of
+// launch_poisson_system, whose rows apply w)
+cudaError_t launch_element_prepass_unweighted(const Mesh& m, const double* kappa, const double* f, double* sigma,
+                                              double* src3, cudaStream_t st);
 // Laplace values into the scalar pattern (CSR or sliced-ELL), no Dirichlet
 cudaError_t launch_laplace_rows(const Mesh& m, const double* sigma, double* vals, Layout lay, cudaStream_t st);
 // load vector: rhs[i] (+)= sum over incident elements of src_e[a]
@@ -232,7 +236,7 @@ cudaError_t launch_laplace_coo_backward(const Mesh& m, const double* grad_vv, do
 cudaError_t launch_source_backward(const Mesh& m, const double* grad_rhs, double* grad_f, cudaStream_t st);
 // fused Poisson system: Laplace + load + Dirichlet (bd rows -> identity, bd columns
 // dropped into the rhs lift), values into the system's sliced-ELL (sptr; full pattern,
-// dropped entries 0).  diagpos_mesh: diagonal slot of each mesh pattern row.  nperm /
+// dropped entries 0); src3 from launch_element_prepass_unweighted.  diagpos_mesh: diagonal slot of each mesh pattern row.  nperm /
 // kperm (NULL: no renumbering): solver row of each node and rank of each pattern slot in
 // its renumbered row; isbd, bdval and rhs are in solver order.
 cudaError_t launch_poisson_system(const Mesh& m, const double* sigma, const double* src3, const uint8_t* isbd,

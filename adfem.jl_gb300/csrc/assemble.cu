@@ -42,6 +42,11 @@ __device__ __forceinline__ double gpair(const double4& g, int a, int b) {
 // point k*(r) and 1/6 at the other two (k* = 0, 2, 1 for r = 0, 1, 2), so the sum is
 // w (S/6 + f_{k*}/2) with S = f0 + f1 + f2: 11 FP64 operations per element instead of 14
 // (the element pass is FP64-instruction bound on GB300).
+// WEIGHTED = false leaves out the factor w (8 FP64 operations per element, and no read of
+// the 32-byte geometry record, whose other three doubles came along with w in the same
+// sector: 640 of the pass's 868 MB at 4M DOF were reads, 256 MB of them geometry); the
+// fused Poisson row pass multiplies each term by w, which it reads with the geometry anyway.
+template <bool WEIGHTED>
 __global__ void k_element_prepass(int64_t ne, const double* __restrict__ kappa, const double* __restrict__ f,
                                   const double4* __restrict__ geo, double* __restrict__ sigma,
                                   double* __restrict__ src3) {
@@ -49,18 +54,30 @@ __global__ void k_element_prepass(int64_t ne, const double* __restrict__ kappa, 
   if (e >= ne) return;
   if (kappa) sigma[e] = kappa[3 * e] + kappa[3 * e + 1] + kappa[3 * e + 2];
   if (f) {
-    const double w = geo[e].w;
     const double f0 = f[3 * e], f1 = f[3 * e + 1], f2 = f[3 * e + 2];
     const double s6 = (f0 + f1 + f2) * (1.0 / 6.0);
-    src3[3 * e] = w * fma(f0, 0.5, s6);
-    src3[3 * e + 1] = w * fma(f2, 0.5, s6);
-    src3[3 * e + 2] = w * fma(f1, 0.5, s6);
+    if (WEIGHTED) {
+      const double w = geo[e].w;
+      src3[3 * e] = w * fma(f0, 0.5, s6);
+      src3[3 * e + 1] = w * fma(f2, 0.5, s6);
+      src3[3 * e + 2] = w * fma(f1, 0.5, s6);
+    } else {
+      src3[3 * e] = fma(f0, 0.5, s6);
+      src3[3 * e + 1] = fma(f2, 0.5, s6);
+      src3[3 * e + 2] = fma(f1, 0.5, s6);
+    }
   }
 }
 
 cudaError_t launch_element_prepass(const Mesh& m, const double* kappa, const double* f, double* sigma, double* src3,
                                    cudaStream_t st) {
-  k_element_prepass<<<nblocks(m.ne), kBlock, 0, st>>>(m.ne, kappa, f, m.d_geo.as<double4>(), sigma, src3);
+  k_element_prepass<true><<<nblocks(m.ne), kBlock, 0, st>>>(m.ne, kappa, f, m.d_geo.as<double4>(), sigma, src3);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_element_prepass_unweighted(const Mesh& m, const double* kappa, const double* f, double* sigma,
+                                              double* src3, cudaStream_t st) {
+  k_element_prepass<false><<<nblocks(m.ne), kBlock, 0, st>>>(m.ne, kappa, f, nullptr, sigma, src3);
   return cudaGetLastError();
 }
 
@@ -75,19 +92,24 @@ struct OutSELL {
   __device__ __forceinline__ int64_t at(int64_t i, int k) const { return (int64_t)sptr[i >> 5] + 32 * k + (i & 31); }
 };
 
-// accumulate the Laplace row of node i into acc[.][t]; returns the row length
-template <int MAXW>
-__device__ __forceinline__ void laplace_row_acc(int64_t i, const int32_t* __restrict__ inc_ptr,
-                                                const uint2* __restrict__ inc, const double4* __restrict__ geo,
-                                                const double* __restrict__ sigma, int w, int dp,
-                                                double (*acc)[kBlock], int t) {
+// Accumulate the Laplace row of node i into acc[.][t].  LOAD: in the same walk over the
+// incident elements, return the node's load sum_e w_e src3[e][a] (src3 without the weight;
+// the weight is the fourth double of the geometry record the row reads anyway).
+template <int MAXW, bool LOAD = false>
+__device__ __forceinline__ double laplace_row_acc(int64_t i, const int32_t* __restrict__ inc_ptr,
+                                                  const uint2* __restrict__ inc, const double4* __restrict__ geo,
+                                                  const double* __restrict__ sigma, int w, int dp,
+                                                  double (*acc)[kBlock], int t,
+                                                  const double* __restrict__ src3 = nullptr) {
   for (int k = 0; k < w; k++) acc[k][t] = 0.0;
+  double r = 0.0;
   const int32_t s1 = inc_ptr[i + 1];
   for (int32_t s = inc_ptr[i]; s < s1; s++) {
     const uint2 rec = inc[s];
     const unsigned e = rec.x, y = rec.y, a = inc_a(y);
     const double4 g = geo[e];
     const double sg = sigma[e];
+    if (LOAD) r = fma(g.w, src3[3 * (int64_t)e + a], r);
     const unsigned b = (a == 0) ? 1 : 0, c = (a == 2) ? 1 : 2;
     const unsigned ob = inc_off(y, b), oc = inc_off(y, c);
     if (!ADFEM_DCHECK(ob < (unsigned)w && oc < (unsigned)w && ob < MAXW && oc < MAXW)) continue;
@@ -98,6 +120,7 @@ __device__ __forceinline__ void laplace_row_acc(int64_t i, const int32_t* __rest
   for (int k = 0; k < w; k++)
     if (k != dp) d -= acc[k][t];
   acc[dp][t] = d;
+  return r;
 }
 
 template <int MAXW, class Out>
@@ -209,6 +232,11 @@ cudaError_t launch_source_rows(const Mesh& m, const double* src3, double* rhs, b
 // PERM: the system's DOFs are renumbered (nperm[node] = solver row); the row of mesh
 // node i goes to solver row nperm[i], its slot k to the rank kperm[rowptr[i] + k] of the
 // renumbered column in that row; isbd, bdval and rhs are in solver order.
+// src3 holds the element load terms without the weight (k_element_prepass<false>): the
+// row's one walk over its elements gathers them with the geometry and multiplies each by
+// its element's w in an FMA, in place of a plain add, so the row costs the same FP64
+// operations as with weighted terms (a second walk for the load, loading w once more,
+// measured 271 us against 234 us at 4M DOF).
 template <int MAXW, bool PERM>
 __global__ void __launch_bounds__(kBlock) k_poisson_system(
     int64_t n, const int32_t* __restrict__ inc_ptr, const uint2* __restrict__ inc, const double4* __restrict__ geo,
@@ -232,12 +260,7 @@ __global__ void __launch_bounds__(kBlock) k_poisson_system(
     rhs[ri] = bdval[ri];
     return;
   }
-  laplace_row_acc<MAXW>(i, inc_ptr, inc, geo, sigma, w, dp, acc, t);
-  double r = 0.0;
-  for (int32_t s = inc_ptr[i]; s < inc_ptr[i + 1]; s++) {
-    const uint2 rec = inc[s];
-    r += src3[3 * (int64_t)rec.x + inc_a(rec.y)];
-  }
+  double r = laplace_row_acc<MAXW, true>(i, inc_ptr, inc, geo, sigma, w, dp, acc, t, src3);
   if (tag == 2) {
     for (int k = 0; k < w; k++) {
       const int64_t j = PERM ? (int64_t)nperm[colind[r0 + k]] : (int64_t)colind[r0 + k];
@@ -254,7 +277,8 @@ __global__ void __launch_bounds__(kBlock) k_poisson_system(
 // ---------------------------------------------------------------------------
 // The same fused Poisson system in FP32-pair arithmetic.  GB300 retires FP64 instructions
 // ~70x slower than FP32 / integer ones, and the FP64 kernels above are bound by them
-// (0.41 ms at 4M DOF for 184M FP64 operations, 0.7 of the FP64 issue rate); here every
+// (0.41 ms at 4M DOF for 184M FP64 operations, 0.7 of the FP64 issue rate, when the element
+// pass applied the weight; 0.36 ms for 160M since the row pass applies it); here every
 // operation is a pair operation (~48 bits: each value lands within ~1e-14 relative of the
 // FP64 one), the FP64 inputs are split into pairs with integer instructions (d2p, in the
 // element pass k_element_prepass_p: once per input) and each output costs one FP64 add

@@ -1221,7 +1221,8 @@ static int assemble_poisson(adfem_system* sys, const double* kappa_d, const doub
     ADFEM_TRY(sys->sigma.alloc(sizeof(double) * m.ne));
     ADFEM_TRY(sys->src3.alloc(sizeof(double) * 3 * m.ne));
     if (ev) ADFEM_CUDA(cudaEventRecord(ev[0], st));
-    ADFEM_TRY(kerr(launch_element_prepass(m, kappa_d, f_d, sys->sigma.as<double>(), sys->src3.as<double>(), st),
+    ADFEM_TRY(kerr(launch_element_prepass_unweighted(m, kappa_d, f_d, sys->sigma.as<double>(),
+                                                     sys->src3.as<double>(), st),
                    "element prepass"));
     if (ev) ADFEM_CUDA(cudaEventRecord(ev[1], st));
     ADFEM_TRY(kerr(launch_poisson_system(m, sys->sigma.as<double>(), sys->src3.as<double>(),

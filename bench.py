@@ -1158,9 +1158,20 @@ def run_ours(args, rank, world, dist):
     # coordinates, connectivity, a 36-byte element-to-CSR-slot map, each CSR value written once
     nnz_ = int(mesh.pattern()[1].size)
     laplace_bytes = 8 * ng_ + 16 * n + 12 * ne_ + 36 * ne_ + 8 * nnz_
-    # FP64 kernels: element pass 11 per element; rows: 2 FMA per incidence, diagonal, load
-    # gather.  Pair kernel: one FP64 add per output value (the pair -> FP64 conversion)
-    fp64_ops = (nent + n) if pairs_asm else 11 * ne_ + 24 * n
+    # FP64 kernels: element pass 8 per element (sigma, and the load terms without the weight);
+    # rows: 2 FMA per incidence, diagonal, load gather (one FMA per incidence applies the
+    # weight).  Pair kernel: one FP64 add per output value (the pair -> FP64 conversion)
+    fp64_ops = (nent + n) if pairs_asm else 8 * ne_ + 24 * n
+    # DRAM traffic of the FP64 element pass and row pass from one ncu capture of this
+    # workload (profiles/traffic.json): the bytes the kernels actually move, including the
+    # per-element intermediate (sigma and the load terms, written and read back) that the
+    # algorithmic model leaves out
+    asm_traffic = None
+    if not pairs_asm:
+        tr = [profiled_traffic(k, args.m) for k in ("k_element_prepass", "k_poisson_system")]
+        if None not in tr:
+            asm_traffic = {"bytes": sum(tr), "element_pass": tr[0], "rows": tr[1],
+                           "achieved_gbs": sum(tr) / asm_s / 1e9, "hbm_frac": sum(tr) / asm_s / 1e9 / hbm}
     assembly = {"arithmetic": "fp32 pairs, one pass" if pairs_asm else "fp64, element pass + rows",
                 "element_pass_ms": ph[0], "rows_ms": ph[1], "solver_conversion_ms": ph[2], "total_ms": asm_ms,
                 "bytes": asm_bytes, "achieved_gbs": asm_bytes / asm_s / 1e9, "hbm_frac": asm_bytes / asm_s / 1e9 / hbm,
@@ -1168,6 +1179,7 @@ def run_ours(args, rank, world, dist):
                 "hbm_frac_laplace_model": laplace_bytes / asm_s / 1e9 / hbm,
                 "fp64_ops": fp64_ops, "fp64_tops": fp64_ops / asm_s / 1e12,
                 "fp64_frac_of_nominal": fp64_ops / asm_s / 1e12 / 0.625,
+                "dram_traffic": asm_traffic,
                 "dof_per_s": n / asm_s, "elements_per_s": ne_ / asm_s}
 
     # ------------------------------------------------------------------ e2e through host buffers

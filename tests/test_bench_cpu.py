@@ -65,6 +65,14 @@ def test_roofline_inputs():
     assert t is not None and 0.5 * 266157974 < t < 1.2 * 266157974
     assert bench.profiled_traffic("k_zcg_iter", 1000) is None  # recorded for the 2000x2000 workload only
     assert bench.profiled_traffic("no_such_kernel", 2000) is None
+    # the FP64 assembly kernels of the same workload: the element pass reads kappa and f
+    # (384 MB, no geometry) and writes sigma and the load terms (256 MB, part of it still
+    # in L2 at the end); the row pass writes at least the operator values of the
+    # 28M-entry pattern
+    ep = bench.profiled_traffic("k_element_prepass", 2000)
+    rows = bench.profiled_traffic("k_poisson_system", 2000)
+    assert ep is not None and 384e6 + 128e6 <= ep <= 384e6 + 256e6
+    assert rows is not None and rows > 8 * 28012001
 
 
 def test_shared_config_and_parity_helpers(oracle):
