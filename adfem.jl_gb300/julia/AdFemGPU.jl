@@ -129,7 +129,7 @@ struct SolverOpts
     chunk::Cint
     warm_start::Cint
 end
-SolverOpts(; rtol = 1e-12, max_iter = 200000, mixed = false, ru_delta = 0.5, chunk = 32) =
+SolverOpts(; rtol = 1e-12, max_iter = 200000, mixed = false, ru_delta = 0.1, chunk = 32) =
     SolverOpts(rtol, max_iter, mixed ? 1 : 0, ru_delta, chunk, 0)
 
 struct SolverStats
