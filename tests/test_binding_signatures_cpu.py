@@ -8,7 +8,10 @@ declarations and structs and compare them with:
     each argument has the declared kind (integer width, double, pointer depth, struct);
   * the Julia structs mirrored from the header: same field kinds, offsets and size;
   * the ctypes table of the Python mirror (adfem_gpu._lib.SIGNATURES) and its Structures;
-  * the status codes the mirror exports.
+  * the status codes the mirror exports;
+  * the reference's own call sites of the legacy symbols (src/MFEM/*.jl, src/pcl.jl), whose
+    ccall signatures tests/golden/make_reference_ccalls.py recorded in
+    tests/golden/reference_ccalls.json: each must match the header exactly.
 A mismatch here is an ABI break a Julia caller would only see as memory corruption.
 """
 import ctypes
@@ -154,7 +157,7 @@ def julia_kind(t):
 def julia_ccalls(text):
     """[(symbol, return type, [argument types])] of every ccall with a literal type tuple."""
     out = []
-    for m in re.finditer(r"ccall\(\(:(\w+),\s*\w+\),\s*", text):
+    for m in re.finditer(r"ccall\(\(:(\w+),\s*(?:\$\([\w.]+\)|\$?[\w.]+)\),\s*", text):
         rest = text[m.end():]
         ret, rest = rest.split(",", 1)
         rest = rest.lstrip()
@@ -309,3 +312,30 @@ def test_status_codes_match_header():
     assert len(codes) >= 11
     for name, v in codes.items():
         assert getattr(_lib, name[len("ADFEM_"):]) == v, name
+
+
+def test_header_matches_the_reference_callers():
+    """The legacy symbols are declared with the signatures the reference's own Julia code
+    ccalls them with (tests/golden/reference_ccalls.json, extracted from src/MFEM/MFEM.jl,
+    src/MFEM/MCore.jl, src/MFEM/MUtils.jl and src/pcl.jl by make_reference_ccalls.py), so
+    pointing AdFem's LIBMFEM at this library keeps every one of those call sites valid."""
+    import json
+
+    fix = json.load(open(os.path.join(ROOT, "tests", "golden", "reference_ccalls.json")))
+    calls = fix["calls"]
+    syms = {c["symbol"] for c in calls}
+    # the path's call sites: mesh construction and getters, the three forward ops, the
+    # Gauss-point interpolation ops and the PCL helpers
+    for s in ("init_nnfem_mesh", "mfem_get_ngauss", "mfem_get_gauss", "mfem_get_gauss_weights", "mfem_get_area",
+              "mfem_get_elem_ndof", "mfem_get_ndof", "mfem_get_connectivity", "mfem_get_element_to_vertices",
+              "FemLaplaceScalar_forward_Julia", "FemSourceScalar_forward_Julia",
+              "ComputeFemStiffnessMatrixMfem_forward_Julia", "FemToGaussPointsMfem_Julia",
+              "DofToGaussPointsMfem_forward_Julia", "pcl_ImposeDirichlet", "pcl_FemLaplaceScalar_Jacobian"):
+        assert s in syms, s
+    fns = header_functions()
+    for c in calls:
+        cret, cargs = fns[c["symbol"]]
+        assert _kinds_match(julia_kind(c["returns"]), cret), (c["site"], "return")
+        assert len(c["args"]) == len(cargs), (c["site"], len(c["args"]), len(cargs))
+        for k, (a, ca) in enumerate(zip(c["args"], cargs)):
+            assert julia_kind(a) == ca, (c["site"], "argument %d" % k, a, ca)
