@@ -1,5 +1,6 @@
 """Writes tests/golden/reference_ccalls.json: the signatures with which the reference's
-Julia code ccalls the native symbols of the path this library replaces.
+Julia code ccalls the native symbols of the path this library replaces, and the C++
+signatures of the op functions behind its TensorFlow custom ops (deps/MFEM/*/*.h).
 
 AdFem.jl calls its C++ library through `@eval ccall((:sym, $LIBMFEM), Ret, (ArgTypes...),
 args...)` (src/MFEM/MFEM.jl, src/MFEM/MCore.jl, src/MFEM/MUtils.jl, src/pcl.jl).  This
@@ -15,6 +16,7 @@ Run from the repository root:  python tests/golden/make_reference_ccalls.py [REF
 import glob
 import json
 import os
+import re
 import sys
 
 HERE = os.path.dirname(os.path.abspath(__file__))
@@ -36,13 +38,29 @@ def main():
             # line of the call site: first line that names the symbol in a ccall
             line = next(k + 1 for k, ln in enumerate(text.splitlines()) if "ccall((:%s," % sym in ln)
             calls.append({"symbol": sym, "returns": ret, "args": args, "site": "%s:%d" % (rel, line)})
+    # the op functions (forward / backward / Julia entry / PCL helper) defined in the
+    # reference's headers of the path, for the names this library exports: parameter types
+    # in order, int64 written as the reference writes it
+    ops = []
+    for path in sorted(glob.glob(os.path.join(ref, "deps", "MFEM", "*", "*.h"))):
+        text = open(path).read()
+        rel = os.path.relpath(path, ref)
+        for m in re.finditer(r"(?:extern \"C\"\s+)?void\s+(?:\w+::)?(\w+)\s*\(([^)]*)\)\s*\{", text):
+            name = m.group(1)
+            if name not in declared:
+                continue
+            params = [" ".join(p.split()) for p in m.group(2).split(",") if p.strip()]
+            types = [re.sub(r"\s*\b\w+$", "", p).replace(" *", "*").replace("* ", "*").strip() for p in params]
+            line = text[:m.start()].count("\n") + 1
+            ops.append({"symbol": name, "params": types, "site": "%s:%d" % (rel, line)})
     out = os.path.join(HERE, "reference_ccalls.json")
     with open(out, "w") as fh:
         json.dump({"what": "ccall signatures of the reference's Julia callers for the symbols this library "
-                           "exports (symbol, Julia return type, Julia argument types, call site)",
-                   "calls": calls}, fh, indent=1)
+                           "exports (symbol, Julia return type, Julia argument types, call site), and the "
+                           "C++ parameter types of the reference's op functions of the same names",
+                   "calls": calls, "ops": ops}, fh, indent=1)
         fh.write("\n")
-    print("wrote %s: %d call sites" % (out, len(calls)))
+    print("wrote %s: %d call sites, %d op functions" % (out, len(calls), len(ops)))
 
 
 if __name__ == "__main__":

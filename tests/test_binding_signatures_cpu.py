@@ -11,7 +11,9 @@ declarations and structs and compare them with:
   * the status codes the mirror exports;
   * the reference's own call sites of the legacy symbols (src/MFEM/*.jl, src/pcl.jl), whose
     ccall signatures tests/golden/make_reference_ccalls.py recorded in
-    tests/golden/reference_ccalls.json: each must match the header exactly.
+    tests/golden/reference_ccalls.json: each must match the header exactly;
+  * the reference's op functions of the same names (deps/MFEM/*/*.h, recorded in the same
+    fixture): parameter kinds in the reference's order.
 A mismatch here is an ABI break a Julia caller would only see as memory corruption.
 """
 import ctypes
@@ -339,3 +341,33 @@ def test_header_matches_the_reference_callers():
         assert len(c["args"]) == len(cargs), (c["site"], len(c["args"]), len(cargs))
         for k, (a, ca) in enumerate(zip(c["args"], cargs)):
             assert julia_kind(a) == ca, (c["site"], "argument %d" % k, a, ca)
+
+
+def _cxx_kind(t):
+    """A reference C++ parameter type ('const int64*', 'double*', 'int') -> (C base, depth)."""
+    t = t.replace("const", " ")
+    depth = t.count("*")
+    base = " ".join(t.replace("*", " ").split())
+    return {"int64": "long long", "long long": "long long"}.get(base, base), depth
+
+
+def test_header_matches_the_reference_op_functions():
+    """The exported compute functions behind the reference's TensorFlow custom ops
+    (forward, backward, the *_Julia entries and the PCL helpers of deps/MFEM/*/*.h) take the
+    reference's parameters in the reference's order (types as recorded in
+    tests/golden/reference_ccalls.json by make_reference_ccalls.py)."""
+    import json
+
+    ops = json.load(open(os.path.join(ROOT, "tests", "golden", "reference_ccalls.json")))["ops"]
+    names = {o["symbol"] for o in ops}
+    for s in ("FemLaplaceScalar_backward", "FemSourceScalar_backward", "ComputeFemStiffnessMatrixMfem_backward",
+              "PlaneStrainMatrix_forward", "PlaneStrainMatrix_backward", "PlaneStressMatrix_forward",
+              "PlaneStressMatrix_backward", "ComputeFemMassMatrix1_forward", "ComputeFemMassMatrix1_backward",
+              "FemToGaussPointsMfem_forward", "FemToGaussPointsMfem_backward", "DofToGaussPointsMfem_forward",
+              "DofToGaussPointsMfem_backward"):
+        assert s in names, s
+    fns = header_functions()
+    for o in ops:
+        cret, cargs = fns[o["symbol"]]
+        assert cret == ("void", 0), o["site"]
+        assert [_cxx_kind(t) for t in o["params"]] == cargs, (o["site"], o["params"], cargs)
