@@ -120,9 +120,9 @@ struct RowSlots {
   int x[3], y[3];
 };
 
-template <bool TRANSPOSE>
+template <bool TRANSPOSE, int BT = kB>
 __device__ __forceinline__ void elastic_row_add(const double* __restrict__ Db, const double2* __restrict__ gr, int a,
-                                                int c, const RowSlots& sl, double (*acc)[kB], int t) {
+                                                int c, const RowSlots& sl, double (*acc)[BT], int t) {
   double d[9];
 #pragma unroll
   for (int j = 0; j < 9; j++) d[j] = TRANSPOSE ? Db[(j % 3) * 3 + (j / 3)] : Db[j];
@@ -148,14 +148,17 @@ __device__ __forceinline__ void elastic_row_add(const double* __restrict__ Db, c
 // Reference [x-block; y-block] ordering, CSR rows r in [0, 2nv): node i = r mod nv,
 // component c = r / nv.  Row r holds the scalar row of i twice: x columns then
 // y columns.  Row pointer: x-rows at 2 rowptr[i], y-rows at 2 nnz + 2 rowptr[i].
-template <int MAXW, bool TRANSPOSE>
-__global__ void __launch_bounds__(kB) k_stiffness_rows(int64_t nv, int64_t nnz, const int32_t* __restrict__ inc_ptr,
+// BT threads per block: kB for rows of up to 16 scalar entries; meshes with vertices of up
+// to 63 neighbours (the most mesh_build accepts) take MAXW = 64 in blocks of 32 threads, so
+// the accumulator stays at 32 KB of static shared memory.
+template <int MAXW, bool TRANSPOSE, int BT = kB>
+__global__ void __launch_bounds__(BT) k_stiffness_rows(int64_t nv, int64_t nnz, const int32_t* __restrict__ inc_ptr,
                                                        const uint2* __restrict__ inc,
                                                        const double2* __restrict__ grad,
                                                        const double* __restrict__ Dbar,
                                                        const int32_t* __restrict__ rowptr,
                                                        double* __restrict__ vals) {
-  __shared__ double acc[2 * MAXW][kB];
+  __shared__ double acc[2 * MAXW][BT];
   const int t = threadIdx.x;
   const int64_t r = gtid();
   if (r >= 2 * nv) return;
@@ -172,7 +175,7 @@ __global__ void __launch_bounds__(kB) k_stiffness_rows(int64_t nv, int64_t nnz, 
       sl.x[b] = (int)inc_off(y, b);
       sl.y[b] = w + (int)inc_off(y, b);
     }
-    elastic_row_add<TRANSPOSE>(Dbar + 9 * (int64_t)e, grad + 3 * (int64_t)e, (int)a, c, sl, acc, t);
+    elastic_row_add<TRANSPOSE, BT>(Dbar + 9 * (int64_t)e, grad + 3 * (int64_t)e, (int)a, c, sl, acc, t);
   }
   const int64_t base = c ? 2 * nnz + 2 * (int64_t)rowptr[i] : 2 * (int64_t)rowptr[i];
   for (int k = 0; k < 2 * w; k++) vals[base + k] = acc[k][t];
@@ -190,6 +193,10 @@ cudaError_t launch_stiffness_rows(const Mesh& m, const double* Dbar, double* val
   } else if (m.maxrow <= 16) {
     if (transpose) k_stiffness_rows<16, true><<<nb, kB, 0, st>>>(m.nv, m.nnz, ip, inc, gr, Dbar, rp, vals);
     else k_stiffness_rows<16, false><<<nb, kB, 0, st>>>(m.nv, m.nnz, ip, inc, gr, Dbar, rp, vals);
+  } else if (m.maxrow <= 64) {
+    const unsigned nbw = nblk(2 * m.nv, 32);
+    if (transpose) k_stiffness_rows<64, true, 32><<<nbw, 32, 0, st>>>(m.nv, m.nnz, ip, inc, gr, Dbar, rp, vals);
+    else k_stiffness_rows<64, false, 32><<<nbw, 32, 0, st>>>(m.nv, m.nnz, ip, inc, gr, Dbar, rp, vals);
   } else {
     return cudaErrorNotSupported;
   }

@@ -1,0 +1,119 @@
+"""Meshes with a vertex of high valence: a fan of k triangles around a centre vertex inside
+rings of quads, so the centre's matrix row has k + 1 entries.  The row kernels keep a
+row in shared memory and switch to their wide variants above 24 scalar entries (Laplace)
+or 16 (stiffness); mesh_build accepts up to 63 neighbours.  The reference builds such
+meshes like any other (MFEM, src/MFEM/MFEM.jl:60-119), so the operators are compared with
+the oracle at the usual bar; the resident systems, whose fused row passes stop at 24
+(Poisson) and 16 (elasticity) entries, refuse them at creation with a status.
+"""
+import numpy as np
+import pytest
+import scipy.sparse as sp
+
+pytestmark = pytest.mark.gpu
+TOL = 1e-12
+
+
+def fan_mesh(k=40, rings=3, seed=0):
+    """Centre vertex 0, `rings` rings of k vertices (radius r / rings, inner rings jittered
+    radially by 2.5 %, odd rings rotated half a step), a fan of k triangles around the
+    centre and two triangles per quad between rings; elements 1-based."""
+    rng = np.random.default_rng(seed)
+    pts = [(0.0, 0.0)]
+    for r in range(1, rings + 1):
+        rad = r / rings
+        for j in range(k):
+            t = 2 * np.pi * (j + 0.5 * (r % 2)) / k
+            rr = rad * (1 + 0.05 * (rng.random() - 0.5)) if r < rings else rad
+            pts.append((rr * np.cos(t), rr * np.sin(t)))
+
+    def ring(r, j):
+        return 1 + (r - 1) * k + (j % k)
+
+    el = [(0, ring(1, j), ring(1, j + 1)) for j in range(k)]
+    for r in range(1, rings):
+        for j in range(k):
+            a, b, c, d = ring(r, j), ring(r, j + 1), ring(r + 1, j), ring(r + 1, j + 1)
+            el += [(a, c, d), (a, d, b)]
+    return np.array(pts), np.array(el, dtype=np.int64) + 1
+
+
+def row_scaled_err(A, B):
+    A, B = sp.csr_matrix(A), sp.csr_matrix(B)
+    d = abs(A - B).max(axis=1).toarray().ravel()
+    s = abs(B).max(axis=1).toarray().ravel()
+    s[s == 0] = 1.0
+    return float(np.max(d / s))
+
+
+def rel(a, b):
+    return float(np.max(np.abs(np.asarray(a) - np.asarray(b))) / max(np.max(np.abs(b)), 1e-300))
+
+
+@pytest.mark.parametrize("k", [30, 63])
+def test_wide_rows_laplace_source_stiffness(oracle, gpulib, k):
+    """Rows of 31 and 64 scalar entries (62 and 128 in the stiffness operator): Laplace and
+    stiffness CSC (the wide row kernels), the load, the COO ops, and K\\F on the wide
+    operator, against the oracle."""
+    import torch
+
+    from adfem_gpu import system as S
+
+    coords, elems = fan_mesh(k)
+    O = oracle.OracleMesh(coords, elems)
+    G = gpulib.Mesh(coords, elems)
+    g = O.gauss_nodes()
+    kappa = np.sin(g[:, 0]) * (1 + g[:, 1] ** 2) + 2
+    B = O.laplace_csc(kappa)
+    assert np.diff(B.indptr).max() == k + 1
+    A = gpulib.compute_fem_laplace_matrix1(kappa, G)
+    np.testing.assert_array_equal(A.indptr, B.indptr)
+    np.testing.assert_array_equal(A.indices, B.indices)
+    assert row_scaled_err(A, B) < TOL
+    f = 1e5 * (g[:, 0] + g[:, 1])
+    F = gpulib.compute_fem_source_term1(f, G)
+    assert rel(F, O.source(f)) < TOL
+    # device CSR values of the same operator
+    v = S.laplace_csr(G, torch.tensor(kappa, device="cuda")).cpu().numpy()
+    cp, rv = G.pattern()
+    assert row_scaled_err(sp.csr_matrix((v, rv - 1, cp - 1), shape=A.shape), B) < TOL
+    # stiffness, a non-symmetric D (checks the CSC transpose)
+    rng = np.random.default_rng(k)
+    D = rng.random((O.ngauss, 3, 3)) + np.eye(3)
+    As = gpulib.compute_fem_stiffness_matrix(D, G)
+    Bs = O.stiffness_csc(D)
+    np.testing.assert_array_equal(As.indptr, Bs.indptr)
+    np.testing.assert_array_equal(As.indices, Bs.indices)
+    assert row_scaled_err(As, Bs) < TOL
+    vs = S.stiffness_csr(G, torch.tensor(D.ravel(), device="cuda")).cpu().numpy()
+    cpe, rve = G.pattern_elasticity()
+    assert row_scaled_err(sp.csr_matrix((vs, rve - 1, cpe - 1), shape=As.shape), Bs) < TOL
+    idx, vv = S.stiffness_coo(G, torch.tensor(D.ravel(), device="cuda"))
+    oi, ov = O.stiffness_coo(D)
+    np.testing.assert_array_equal(idx.cpu().numpy(), oi)
+    assert rel(vv.cpu().numpy(), ov) < TOL
+    # K\F on the Dirichlet-imposed wide operator (the solver's plain-loop SpMV)
+    bd = O.bcnode()
+    Kb, Fb = oracle.dirichlet_csc(B, O.source(f), bd, np.zeros(bd.size))
+    u0 = oracle.spsolve(Kb, Fb)
+    for prec, rtol in (("fp64", 1e-13), ("mixed", 1e-12)):
+        u = gpulib.solve(Kb, Fb, precision=prec, rtol=rtol)
+        assert rel(u, u0) < 1e-9, prec
+
+
+def test_wide_rows_refused_by_resident_systems(oracle, gpulib):
+    """Resident systems fuse the rows with Dirichlet and the solver layout in kernels that
+    keep 24 (Poisson) or 16 (elasticity) entries per row: a 41-entry row is refused at
+    creation with ADFEM_ERR_UNSUPPORTED and a message naming the limit, and the mesh and
+    the library stay usable."""
+    from adfem_gpu import _lib
+
+    coords, elems = fan_mesh(40)
+    G = gpulib.Mesh(coords, elems)
+    for cls, what in ((gpulib.PoissonSystem, "23 neighbours"), (gpulib.ElasticitySystem, "15 neighbours")):
+        with pytest.raises(gpulib.AdFemError) as ei:
+            cls(G)
+        assert ei.value.status == _lib.ERR_UNSUPPORTED and what in str(ei.value)
+    O = oracle.OracleMesh(coords, elems)
+    kappa = np.ones(O.ngauss)
+    assert row_scaled_err(gpulib.compute_fem_laplace_matrix1(kappa, G), O.laplace_csc(kappa)) < TOL
