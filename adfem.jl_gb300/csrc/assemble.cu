@@ -95,11 +95,11 @@ struct OutSELL {
 // Accumulate the Laplace row of node i into acc[.][t].  LOAD: in the same walk over the
 // incident elements, return the node's load sum_e w_e src3[e][a] (src3 without the weight;
 // the weight is the fourth double of the geometry record the row reads anyway).
-template <int MAXW, bool LOAD = false>
+template <int MAXW, bool LOAD = false, int BT = kBlock>
 __device__ __forceinline__ double laplace_row_acc(int64_t i, const int32_t* __restrict__ inc_ptr,
                                                   const uint2* __restrict__ inc, const double4* __restrict__ geo,
                                                   const double* __restrict__ sigma, int w, int dp,
-                                                  double (*acc)[kBlock], int t,
+                                                  double (*acc)[BT], int t,
                                                   const double* __restrict__ src3 = nullptr) {
   for (int k = 0; k < w; k++) acc[k][t] = 0.0;
   double r = 0.0;
@@ -237,14 +237,16 @@ cudaError_t launch_source_rows(const Mesh& m, const double* src3, double* rhs, b
 // its element's w in an FMA, in place of a plain add, so the row costs the same FP64
 // operations as with weighted terms (a second walk for the load, loading w once more,
 // measured 271 us against 234 us at 4M DOF).
-template <int MAXW, bool PERM>
-__global__ void __launch_bounds__(kBlock) k_poisson_system(
+// BT threads per block: kBlock up to 24 entries per row; rows of up to 64 (vertices of up to
+// 63 neighbours, the most mesh_build accepts) in blocks of 64, 32 KB of static shared memory.
+template <int MAXW, bool PERM, int BT = kBlock>
+__global__ void __launch_bounds__(BT) k_poisson_system(
     int64_t n, const int32_t* __restrict__ inc_ptr, const uint2* __restrict__ inc, const double4* __restrict__ geo,
     const double* __restrict__ sigma, const double* __restrict__ src3, const int32_t* __restrict__ rowptr,
     const int32_t* __restrict__ colind, const int32_t* __restrict__ diagpos, const int32_t* __restrict__ sptr,
     const uint8_t* __restrict__ isbd, const double* __restrict__ bdval, double* __restrict__ vals,
     double* __restrict__ rhs, const int32_t* __restrict__ nperm, const uint8_t* __restrict__ kperm) {
-  __shared__ double acc[MAXW][kBlock];
+  __shared__ double acc[MAXW][BT];
   const int t = threadIdx.x;
   const int64_t i = gtid();
   if (i >= n) return;
@@ -260,7 +262,7 @@ __global__ void __launch_bounds__(kBlock) k_poisson_system(
     rhs[ri] = bdval[ri];
     return;
   }
-  double r = laplace_row_acc<MAXW, true>(i, inc_ptr, inc, geo, sigma, w, dp, acc, t, src3);
+  double r = laplace_row_acc<MAXW, true, BT>(i, inc_ptr, inc, geo, sigma, w, dp, acc, t, src3);
   if (tag == 2) {
     for (int k = 0; k < w; k++) {
       const int64_t j = PERM ? (int64_t)nperm[colind[r0 + k]] : (int64_t)colind[r0 + k];
@@ -483,7 +485,17 @@ cudaError_t launch_poisson_system(const Mesh& m, const double* sigma, const doub
   if (m.maxrow <= 8) ADFEM_PS(8);
   else if (m.maxrow <= 16) ADFEM_PS(16);
   else if (m.maxrow <= 24) ADFEM_PS(24);
-  else return cudaErrorNotSupported;
+  else if (m.maxrow <= 64) {
+    const unsigned nbw = nblocks(m.nv, 64);
+    if (nperm)
+      k_poisson_system<64, true, 64><<<nbw, 64, 0, st>>>(m.nv, ip, inc, geo, sigma, src3, rp, ci, dp, sptr, isbd,
+                                                           bdval_dense, sell_vals, rhs, nperm, kperm);
+    else
+      k_poisson_system<64, false, 64><<<nbw, 64, 0, st>>>(m.nv, ip, inc, geo, sigma, src3, rp, ci, dp, sptr, isbd,
+                                                            bdval_dense, sell_vals, rhs, nullptr, nullptr);
+  } else {
+    return cudaErrorNotSupported;
+  }
 #undef ADFEM_PS
   return cudaGetLastError();
 }

@@ -1027,11 +1027,6 @@ int adfem_system_create(adfem_mesh* mesh, int kind, adfem_system** out) {
                                        "stiffness operators and use adfem_csc_solve)");
   if (kind == ADFEM_SYS_ELASTICITY && m.maxrow > 16)
     return fail(ADFEM_ERR_UNSUPPORTED, "elasticity systems support at most 15 neighbours per node");
-  // the fused P1 Poisson row pass keeps rows of up to 24 entries in shared memory (the
-  // operator entries alone, adfem_laplace_csc / _csr_d, take up to 64)
-  if (kind == ADFEM_SYS_POISSON && !p2 && m.maxrow > 24)
-    return fail(ADFEM_ERR_UNSUPPORTED, "P1 Poisson systems support at most 23 neighbours per node (this mesh has " +
-                                           std::to_string(m.maxrow - 1) + ")");
   // the scalar pattern the operator lives on: the mesh's (P1, one DOF per node) or that of
   // the P2 space (vertex DOFs, then one per edge)
   Space* sp = nullptr;

@@ -1,10 +1,11 @@
 """Meshes with a vertex of high valence: a fan of k triangles around a centre vertex inside
 rings of quads, so the centre's matrix row has k + 1 entries.  The row kernels keep a
-row in shared memory and switch to their wide variants above 24 scalar entries (Laplace)
-or 16 (stiffness); mesh_build accepts up to 63 neighbours.  The reference builds such
-meshes like any other (MFEM, src/MFEM/MFEM.jl:60-119), so the operators are compared with
-the oracle at the usual bar; the resident systems, whose fused row passes stop at 24
-(Poisson) and 16 (elasticity) entries, refuse them at creation with a status.
+row in shared memory and switch to their wide variants above 24 scalar entries (Laplace,
+the fused Poisson system) or 16 (stiffness); mesh_build accepts up to 63 neighbours.  The
+reference builds such meshes like any other (MFEM, src/MFEM/MFEM.jl:60-119), so the
+operators and a resident Poisson system (forward, adjoint, kappa-gradient) are compared with
+the oracle at the usual bars; resident elasticity systems, whose fused row pass stops at 16
+entries, refuse them at creation with a status.
 """
 import numpy as np
 import pytest
@@ -101,19 +102,51 @@ def test_wide_rows_laplace_source_stiffness(oracle, gpulib, k):
         assert rel(u, u0) < 1e-9, prec
 
 
-def test_wide_rows_refused_by_resident_systems(oracle, gpulib):
-    """Resident systems fuse the rows with Dirichlet and the solver layout in kernels that
-    keep 24 (Poisson) or 16 (elasticity) entries per row: a 41-entry row is refused at
-    creation with ADFEM_ERR_UNSUPPORTED and a message naming the limit, and the mesh and
-    the library stay usable."""
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_wide_rows_resident_poisson_system(oracle, gpulib, precision):
+    """A resident Poisson system on a fan mesh with a 64-entry row (the 64-wide fused row
+    pass; the solver takes its scaled path above 24 entries): forward solve against the
+    direct solve (1e-9), and the kappa-gradient of a misfit against the reference's backward
+    chain (sparse-solve gradient, ImposeDirichlet backward, FemLaplaceScalar backward; 1e-7)."""
+    import torch
+
+    from test_solver_gpu import RTOL, oracle_kappa_gradient
+
+    coords, elems = fan_mesh(63)
+    O = oracle.OracleMesh(coords, elems)
+    g = O.gauss_nodes()
+    kappa = np.sin(g[:, 0]) * (1 + g[:, 1] ** 2) + 2
+    f = 1e5 * (g[:, 0] + g[:, 1])
+    bd = O.bcnode()
+    obs = np.arange(0, O.ndof, 7)
+    uobs = np.random.default_rng(5).standard_normal(obs.size) * 1e-3
+    gref, uref = oracle_kappa_gradient(oracle, O, kappa, f, bd, obs, uobs)
+    S = gpulib.PoissonSystem(gpulib.Mesh(coords, elems))
+    S.set_dirichlet(bd)
+    S.assemble(torch.tensor(kappa, device="cuda"), torch.tensor(f, device="cuda"))
+    assert S.solver_info()["banded"] == 0
+    u = S.solve(precision=precision, rtol=RTOL[precision])
+    assert S.last_stats.status == 0
+    assert rel(u.cpu().numpy(), uref) < 1e-9
+    ob = torch.tensor(obs, device="cuda")
+    gu = torch.zeros_like(u)
+    gu[ob] = 2 * (u[ob] - torch.tensor(uobs, device="cuda"))
+    lam = S.adjoint(gu, precision=precision, rtol=RTOL[precision])
+    assert rel(S.grad_kappa(u, lam).cpu().numpy(), gref) < 1e-7
+
+
+def test_wide_rows_refused_by_resident_elasticity_systems(oracle, gpulib):
+    """Resident elasticity systems fuse the rows with Dirichlet and the solver layout in a
+    kernel that keeps 16 scalar entries per row: a 41-entry row is refused at creation with
+    ADFEM_ERR_UNSUPPORTED and a message naming the limit, and the mesh and the library stay
+    usable."""
     from adfem_gpu import _lib
 
     coords, elems = fan_mesh(40)
     G = gpulib.Mesh(coords, elems)
-    for cls, what in ((gpulib.PoissonSystem, "23 neighbours"), (gpulib.ElasticitySystem, "15 neighbours")):
-        with pytest.raises(gpulib.AdFemError) as ei:
-            cls(G)
-        assert ei.value.status == _lib.ERR_UNSUPPORTED and what in str(ei.value)
+    with pytest.raises(gpulib.AdFemError) as ei:
+        gpulib.ElasticitySystem(G)
+    assert ei.value.status == _lib.ERR_UNSUPPORTED and "15 neighbours" in str(ei.value)
     O = oracle.OracleMesh(coords, elems)
     kappa = np.ones(O.ngauss)
     assert row_scaled_err(gpulib.compute_fem_laplace_matrix1(kappa, G), O.laplace_csc(kappa)) < TOL
