@@ -21,6 +21,7 @@ import numpy as np
 
 __all__ = [
     "jittered_square",
+    "fan_mesh",
     "fourier_modes",
     "fourier_field",
     "poisson_c1_fields",
@@ -61,6 +62,34 @@ def jittered_square(m: int, seed: int = 0, jitter: float = 0.2, n: int | None = 
     elems[0::2] = np.stack([a, b, c], axis=1)
     elems[1::2] = np.stack([b, c, d2], axis=1)
     return coords, elems + 1
+
+
+def fan_mesh(k: int = 40, rings: int = 3, seed: int = 0):
+    """A disk whose centre vertex has k neighbours: vertex 0 at the origin, ``rings`` rings
+    of k vertices at radius r / rings (inner rings jittered radially by up to 2.5 %, odd
+    rings rotated half a step), a fan of k triangles around the centre and two triangles
+    per quad between consecutive rings.  The centre's matrix row has k + 1 entries, far
+    above the 7 of a structured triangulation.
+
+    Returns ``(coords, elems)`` as ``jittered_square`` does (elems 1-based)."""
+    rng = np.random.default_rng(seed)
+    pts = [(0.0, 0.0)]
+    for r in range(1, rings + 1):
+        rad = r / rings
+        for j in range(k):
+            t = 2 * math.pi * (j + 0.5 * (r % 2)) / k
+            rr = rad * (1 + 0.05 * (rng.random() - 0.5)) if r < rings else rad
+            pts.append((rr * math.cos(t), rr * math.sin(t)))
+
+    def ring(r, j):
+        return 1 + (r - 1) * k + (j % k)
+
+    el = [(0, ring(1, j), ring(1, j + 1)) for j in range(k)]
+    for r in range(1, rings):
+        for j in range(k):
+            a, b, c, d = ring(r, j), ring(r, j + 1), ring(r + 1, j), ring(r + 1, j + 1)
+            el += [(a, c, d), (a, d, b)]
+    return np.array(pts), np.array(el, dtype=np.int64) + 1
 
 
 def fourier_modes(seed: int, nmodes: int = 64, kmax: float = 16 * math.pi):

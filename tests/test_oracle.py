@@ -299,3 +299,35 @@ def test_cpu_pcg_matches_direct(oracle):
     x, it, rr = oracle.pcg(B, z["r"], rtol=1e-14, threads=2)
     assert rr <= 1e-14
     np.testing.assert_allclose(x, z["u"], rtol=1e-10, atol=1e-10 * np.max(np.abs(z["u"])))
+
+
+@pytest.mark.parametrize("k", [30, 63])
+def test_high_valence_mesh_kats(oracle, k):
+    """The oracle on a fan mesh whose centre vertex has k neighbours (the wide-row GPU
+    tests' checker): the centre row has k + 1 entries; Laplace rows sum to zero; a linear
+    field is annihilated at interior nodes for constant kappa (patch test); the load of
+    f = 1 + x integrates f exactly (sum of areas times the centroid value); the stiffness
+    operator annihilates the rigid-body modes and is symmetric for a symmetric D."""
+    coords, elems = synth.fan_mesh(k)
+    M = oracle.OracleMesh(coords, elems)
+    rng = np.random.default_rng(k)
+    K = M.laplace_csc(1 + rng.random(M.ngauss))
+    assert np.diff(K.indptr).max() == k + 1
+    rows = np.abs(K).sum(axis=1).A1
+    assert np.max(np.abs(K.sum(axis=1).A1) / rows) < 1e-13
+    Kc = M.laplace_csc(np.full(M.ngauss, 1.5))
+    u = 1 + 2 * coords[:, 0] - 3 * coords[:, 1]
+    interior = np.setdiff1d(np.arange(M.ndof), M.bcnode() - 1)
+    assert interior.size == 1 + (3 - 1) * k  # the centre and the inner rings
+    assert np.max(np.abs((Kc @ u)[interior])) < 1e-12 * np.max(rows)
+    g = M.gauss_nodes()
+    e0 = np.asarray(elems) - 1
+    xc = coords[e0, 0].mean(axis=1)
+    exact = float(np.sum(M.area * (1 + xc)))
+    assert abs(M.source(1 + g[:, 0]).sum() - exact) < 1e-13 * abs(exact)
+    D = np.tile(np.array([[2.0, 1.0, 0.0], [1.0, 2.0, 0.0], [0.0, 0.0, 0.5]]), (M.ngauss, 1, 1))
+    Ks = M.stiffness_csc(D)
+    n = M.ndof
+    for v in (np.r_[np.ones(n), np.zeros(n)], np.r_[np.zeros(n), np.ones(n)], np.r_[-coords[:, 1], coords[:, 0]]):
+        assert np.abs(Ks @ v).max() < 1e-12 * np.abs(Ks).max()
+    assert abs(Ks - Ks.T).max() < 1e-15 * np.abs(Ks).max()

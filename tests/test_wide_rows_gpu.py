@@ -11,32 +11,10 @@ import numpy as np
 import pytest
 import scipy.sparse as sp
 
+from adfem_gpu.synth import fan_mesh
+
 pytestmark = pytest.mark.gpu
 TOL = 1e-12
-
-
-def fan_mesh(k=40, rings=3, seed=0):
-    """Centre vertex 0, `rings` rings of k vertices (radius r / rings, inner rings jittered
-    radially by 2.5 %, odd rings rotated half a step), a fan of k triangles around the
-    centre and two triangles per quad between rings; elements 1-based."""
-    rng = np.random.default_rng(seed)
-    pts = [(0.0, 0.0)]
-    for r in range(1, rings + 1):
-        rad = r / rings
-        for j in range(k):
-            t = 2 * np.pi * (j + 0.5 * (r % 2)) / k
-            rr = rad * (1 + 0.05 * (rng.random() - 0.5)) if r < rings else rad
-            pts.append((rr * np.cos(t), rr * np.sin(t)))
-
-    def ring(r, j):
-        return 1 + (r - 1) * k + (j % k)
-
-    el = [(0, ring(1, j), ring(1, j + 1)) for j in range(k)]
-    for r in range(1, rings):
-        for j in range(k):
-            a, b, c, d = ring(r, j), ring(r, j + 1), ring(r + 1, j), ring(r + 1, j + 1)
-            el += [(a, c, d), (a, d, b)]
-    return np.array(pts), np.array(el, dtype=np.int64) + 1
 
 
 def row_scaled_err(A, B):
