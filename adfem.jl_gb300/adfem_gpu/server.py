@@ -6,10 +6,16 @@ observations whose misfit gradient with respect to kappa (or E) comes back throu
 the adjoint.  Worker threads in the library run requests concurrently on their own
 CUDA streams and keep the systems of recently used meshes resident; see the C header
 for admission and eviction.  Host numpy arrays in and out.
+
+Tracing: ``Server(trace=path_or_file)`` appends one JSON line per completed request (when
+``wait`` returns it): ticket, kind, DOFs, observation count, requested precision, and the
+library's response (status, iterations, residual, misfit, queue / run / total ms, whether it
+ran in a packed launch, message).
 """
 from __future__ import annotations
 
 import ctypes
+import json
 
 import numpy as np
 
@@ -24,9 +30,11 @@ def _f64(a):
 class Server:
     def __init__(self, hbm_budget_bytes: int = 0, workers: int = 8, max_queue: int = 0, precision: str = "mixed",
                  rtol: float = 1e-10, max_iter: int = 200000, ru_delta: float = 0.1, chunk: int = 32,
-                 pack_max_dof: int = 0, pack_max: int = 0):
+                 pack_max_dof: int = 0, pack_max: int = 0, trace=None):
         """pack_max_dof: mixed-precision requests up to this many DOFs are solved in packed
-        launches (0: the library default, 16384; -1: never); pack_max: systems per pack."""
+        launches (0: the library default, 16384; -1: never); pack_max: systems per pack;
+        trace: a path (opened for appending) or a writable text file for the per-request
+        JSON lines, None for no trace."""
         from . import solver_opts
 
         L = _lib.load()
@@ -42,6 +50,9 @@ class Server:
         check(L.adfem_server_create(ctypes.byref(cfg), ctypes.byref(h)), "server_create")
         self._h = h
         self._live = {}  # ticket -> arrays the request points at (kept alive until it completes)
+        self._meta = {}  # ticket -> request description for the trace
+        self._trace_owned = isinstance(trace, str)
+        self._trace = open(trace, "a") if self._trace_owned else trace
 
     # ------------------------------------------------------------------ requests
     def submit(self, mesh, kind: int, fields, bd, bdval=None, obs=None, uobs=None, deadline_ms: float = 0.0,
@@ -86,6 +97,9 @@ class Server:
         t = ctypes.c_longlong()
         check(_lib.load().adfem_server_submit(self._h, ctypes.byref(r), ctypes.byref(t)), "server_submit")
         self._live[t.value] = (keep, u, grad)
+        if self._trace is not None:
+            self._meta[t.value] = {"kind": "elasticity" if kind == _lib.SYS_ELASTICITY else "poisson",
+                                   "ndof": int(ndof), "nobs": int(r.nobs), "precision": precision or "server"}
         return t.value
 
     def wait(self, ticket: int, timeout_ms: float = -1.0):
@@ -96,6 +110,12 @@ class Server:
         _, u, grad = self._live.pop(ticket)
         out = {name: getattr(resp, name) for name, _ in resp._fields_}
         out["message"] = out["message"].decode(errors="replace")
+        if self._trace is not None:
+            rec = {"ticket": int(ticket)}
+            rec.update(self._meta.pop(ticket, {}))
+            rec.update(out)
+            self._trace.write(json.dumps(rec) + "\n")
+            self._trace.flush()
         return out, u, grad
 
     def stats(self) -> dict:
@@ -111,6 +131,10 @@ class Server:
             _lib._LIB.adfem_server_destroy(self._h)
             self._h = None
             self._live.clear()
+            self._meta.clear()
+        if getattr(self, "_trace_owned", False) and self._trace is not None:
+            self._trace.close()
+            self._trace = None
 
     def __del__(self):
         try:
