@@ -1,0 +1,117 @@
+// CPU harness for the library's host mesh code (adfem.jl_gb300/csrc/mesh.cpp), built with
+// AddressSanitizer and UndefinedBehaviorSanitizer by tests/test_host_mesh_sanitized.py.
+//
+// mesh.cpp uploads what it builds through four CUDA runtime calls; here they are stood in
+// for by host memory (cudaMalloc -> malloc, cudaMemcpy -> memcpy), so the whole host path
+// -- orientation fix, geometry, incidence, CSR pattern, sliced-ELL layout with its
+// slice-uniform column patterns, edges, boundary nodes, the P2 space -- runs without a
+// GPU, and what it "uploaded" can be read back.  The extern "C" functions below are what
+// the test calls through ctypes.  Test infrastructure only: nothing in the library uses it.
+#include <cstdlib>
+#include <cstring>
+
+#include "adfem_internal.h"
+
+extern "C" {
+cudaError_t cudaMalloc(void** p, size_t n) {
+  *p = std::malloc(n ? n : 1);
+  return *p ? cudaSuccess : cudaErrorMemoryAllocation;
+}
+cudaError_t cudaFree(void* p) {
+  std::free(p);
+  return cudaSuccess;
+}
+cudaError_t cudaMemcpy(void* dst, const void* src, size_t n, cudaMemcpyKind) {
+  std::memcpy(dst, src, n);
+  return cudaSuccess;
+}
+const char* cudaGetErrorString(cudaError_t) { return "host stand-in"; }
+}
+
+namespace adfem {
+const char* last_error_cstr();  // mesh.cpp: message of the calling thread's last failure
+// the debug-build index-check readers live with the kernels; nothing was checked here
+int check_line_solver() { return 0; }
+int check_line_zcg() { return 0; }
+int check_line_assemble() { return 0; }
+int check_line_generic() { return 0; }
+}  // namespace adfem
+
+using adfem::Mesh;
+
+extern "C" {
+int hm_build(const double* xyz, long long nv, const int* elems0, long long ne, void** out) {
+  Mesh* m = nullptr;
+  const int st = adfem::mesh_build(xyz, nv, elems0, ne, &m);
+  *out = m;
+  return st;
+}
+const char* hm_error() { return adfem::last_error_cstr(); }
+void hm_destroy(void* h) { delete static_cast<Mesh*>(h); }
+void hm_sizes(void* h, long long* nnz, int* maxrow, int* flipped) {
+  const Mesh* m = static_cast<Mesh*>(h);
+  *nnz = m->nnz;
+  *maxrow = m->maxrow;
+  *flipped = m->flipped;
+}
+void hm_pattern(void* h, int* rowptr, int* colind) {
+  const Mesh* m = static_cast<Mesh*>(h);
+  std::memcpy(rowptr, m->rowptr.data(), sizeof(int) * m->rowptr.size());
+  std::memcpy(colind, m->colind.data(), sizeof(int) * m->colind.size());
+}
+long long hm_bcnode(void* h, long long* out) {
+  return adfem::mesh_bcnode(static_cast<Mesh*>(h), reinterpret_cast<int64_t*>(out));
+}
+long long hm_edges(void* h, long long* out) {
+  Mesh* m = static_cast<Mesh*>(h);
+  if (adfem::mesh_edges(m) != ADFEM_OK) return -1;
+  if (out) std::memcpy(out, m->edges.data(), sizeof(long long) * m->edges.size());
+  return m->nedges;
+}
+void hm_area(void* h, double* a) {
+  const Mesh* m = static_cast<Mesh*>(h);
+  std::memcpy(a, m->area.data(), sizeof(double) * m->area.size());
+}
+void hm_gauss(void* h, double* x, double* y) { adfem::mesh_gauss(static_cast<Mesh*>(h), x, y); }
+// the sliced-ELL copy of the pattern as uploaded: nslices, stored entries, widest slice;
+// with non-null arrays, slice pointers [nslices + 1] and the column of every stored entry
+// [nent] (decoded from the int16 deltas or int32 columns, through the slice-uniform
+// patterns where a slice has one)
+void hm_sell(void* h, long long* nslices, long long* nent, int* maxw, int* sptr, int* col) {
+  const adfem::Sell& s = static_cast<Mesh*>(h)->sell;
+  *nslices = s.nslices;
+  *nent = s.nent;
+  *maxw = s.maxw;
+  if (!sptr) return;
+  const int32_t* sp = s.sptr.as<int32_t>();
+  std::memcpy(sptr, sp, sizeof(int) * (s.nslices + 1));
+  const int32_t* spat = s.spat.as<int32_t>();
+  const int16_t* pat = s.pat.as<int16_t>();
+  for (int64_t sl = 0; sl < s.nslices; sl++) {
+    const int w = (sp[sl + 1] - sp[sl]) / 32;
+    for (int k = 0; k < w; k++)
+      for (int l = 0; l < 32; l++) {
+        const int64_t r = 32 * sl + l, q = sp[sl] + 32 * k + l;
+        int64_t c;
+        if (spat && spat[sl] >= 0) c = r + pat[spat[sl] + (r % s.pat_period) * w + k];
+        else if (s.delta16) c = r + s.col.as<int16_t>()[q];
+        else c = s.col.as<int32_t>()[q];
+        col[q] = (int)c;
+      }
+  }
+}
+// the P2 (or P1) space: DOFs, pattern entries and widest row; with non-null arrays, its
+// CSR pattern
+int hm_space(void* h, int degree, long long* ndof, long long* nnz, int* maxrow, int* rowptr, int* colind) {
+  Mesh* m = static_cast<Mesh*>(h);
+  adfem::Space* sp = nullptr;
+  const int st = adfem::mesh_space(m, degree, &sp);
+  if (st != ADFEM_OK) return st;
+  *ndof = sp->ndof;
+  *nnz = sp->nnz;
+  *maxrow = sp->maxrow;
+  if (rowptr) std::memcpy(rowptr, sp->rowptr.data(), sizeof(int) * sp->rowptr.size());
+  if (colind) std::memcpy(colind, sp->colind.data(), sizeof(int) * sp->colind.size());
+  return ADFEM_OK;
+}
+}
