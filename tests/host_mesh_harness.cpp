@@ -100,6 +100,14 @@ void hm_sell(void* h, long long* nslices, long long* nent, int* maxw, int* sptr,
       }
   }
 }
+// reverse Cuthill-McKee order of the mesh's node graph (pi[node] = new index) and the band it
+// reports
+long long hm_rcm(void* h, int* pi) {
+  std::vector<int32_t> p;
+  const int64_t band = adfem::mesh_rcm(*static_cast<Mesh*>(h), p);
+  std::memcpy(pi, p.data(), sizeof(int) * p.size());
+  return band;
+}
 // the P2 (or P1) space: DOFs, pattern entries and widest row; with non-null arrays, its
 // CSR pattern
 int hm_space(void* h, int degree, long long* ndof, long long* nnz, int* maxrow, int* rowptr, int* colind) {

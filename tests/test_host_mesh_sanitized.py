@@ -8,6 +8,8 @@ links it with host-memory stand-ins for the four CUDA runtime calls it makes, in
   * builds structured, jittered, fan (63-neighbour vertex) and reoriented meshes and checks
     the pattern, boundary nodes, edges, areas, Gauss points and P2 space against the oracle,
     and every stored entry of the sliced-ELL copy against the pattern;
+  * renumbers a shuffled mesh by reverse Cuthill-McKee (the solver's DOF order) and checks
+    the permutation and the band it reports;
   * feeds the invalid meshes the entry rejects (vertex index out of range, a degenerate
     triangle, a vertex in no element, a vertex with 70 neighbours) and checks the statuses;
   * makes each device allocation of a mesh build fail in turn (adfem_debug_fail_alloc) and
@@ -44,6 +46,7 @@ H.hm_gauss.argtypes = [vp, vp, vp]
 H.hm_sell.argtypes = [vp, vp, vp, vp, vp, vp]
 H.hm_space.argtypes = [vp, ctypes.c_int, vp, vp, vp, vp, vp]
 H.adfem_debug_fail_alloc.argtypes = [ll]
+H.hm_rcm.argtypes = [vp, vp]; H.hm_rcm.restype = ll
 
 def P(a):
     return a.ctypes.data
@@ -104,6 +107,25 @@ c, e = synth.jittered_square(5, seed=2)
 cases.append((c, e[:, ::-1].copy()))  # every triangle clockwise: all reoriented
 for c, e in cases:
     check_mesh(c, e)
+
+# reverse Cuthill-McKee on a mesh whose nodes were shuffled: a permutation, the band it
+# reports is the band of the renumbered pattern, and far below the shuffled one
+c, e = synth.jittered_square(30, seed=5)
+perm = np.random.default_rng(6).permutation(c.shape[0])
+inv = np.argsort(perm)
+cs, es = c[perm], inv[e - 1] + 1
+st, h = build(cs, es); assert st == 0
+n = cs.shape[0]
+nnz, maxrow, flipped = ctypes.c_longlong(), ctypes.c_int(), ctypes.c_int()
+H.hm_sizes(h, ctypes.byref(nnz), ctypes.byref(maxrow), ctypes.byref(flipped))
+rp = np.empty(n + 1, np.int32); ci = np.empty(nnz.value, np.int32); H.hm_pattern(h, P(rp), P(ci))
+pi = np.empty(n, np.int32)
+band = H.hm_rcm(h, P(pi))
+assert np.array_equal(np.sort(pi), np.arange(n))
+rows = np.repeat(np.arange(n), np.diff(rp))
+assert band == np.abs(pi[rows] - pi[ci]).max()
+assert band <= np.abs(rows - ci).max() // 4 and band <= 2 * 31 + 8, band
+H.hm_destroy(h)
 
 # invalid meshes: a status and a message, no crash
 c, e = synth.jittered_square(3, seed=0)
