@@ -30,6 +30,7 @@ const char* cudaGetErrorString(cudaError_t) { return "host stand-in"; }
 
 namespace adfem {
 const char* last_error_cstr();  // mesh.cpp: message of the calling thread's last failure
+int sell_build_pattern(int64_t n, const int32_t* rowptr, const int32_t* colind, Sell& s, int period);
 // the debug-build index-check readers live with the kernels; nothing was checked here
 int check_line_solver() { return 0; }
 int check_line_zcg() { return 0; }
@@ -73,12 +74,10 @@ void hm_area(void* h, double* a) {
   std::memcpy(a, m->area.data(), sizeof(double) * m->area.size());
 }
 void hm_gauss(void* h, double* x, double* y) { adfem::mesh_gauss(static_cast<Mesh*>(h), x, y); }
-// the sliced-ELL copy of the pattern as uploaded: nslices, stored entries, widest slice;
-// with non-null arrays, slice pointers [nslices + 1] and the column of every stored entry
-// [nent] (decoded from the int16 deltas or int32 columns, through the slice-uniform
-// patterns where a slice has one)
-void hm_sell(void* h, long long* nslices, long long* nent, int* maxw, int* sptr, int* col) {
-  const adfem::Sell& s = static_cast<Mesh*>(h)->sell;
+// the sliced-ELL layout s: nslices, stored entries, widest slice; with non-null arrays, slice
+// pointers [nslices + 1] and the column of every stored entry [nent] (decoded from the int16
+// deltas or int32 columns, through the slice-uniform patterns where a slice has one)
+static void sell_decode(const adfem::Sell& s, long long* nslices, long long* nent, int* maxw, int* sptr, int* col) {
   *nslices = s.nslices;
   *nent = s.nent;
   *maxw = s.maxw;
@@ -99,6 +98,24 @@ void hm_sell(void* h, long long* nslices, long long* nent, int* maxw, int* sptr,
         col[q] = (int)c;
       }
   }
+}
+// the mesh's sliced-ELL copy of its pattern, as uploaded
+void hm_sell(void* h, long long* nslices, long long* nent, int* maxw, int* sptr, int* col) {
+  sell_decode(static_cast<Mesh*>(h)->sell, nslices, nent, maxw, sptr, col);
+}
+// sell_build_pattern on any CSR pattern (period 2: slice-uniform patterns per row parity, as
+// for interleaved 2-DOF operators); info = {delta16, uniform slices, band}.  Two calls: sizes
+// with null arrays, then the decoded layout.
+int hm_sell_build(long long n, const int* rowptr, const int* colind, int period, long long* nslices, long long* nent,
+                  int* maxw, long long* info, int* sptr, int* col) {
+  adfem::Sell s;
+  const int st = adfem::sell_build_pattern(n, rowptr, colind, s, period);
+  if (st != ADFEM_OK) return st;
+  info[0] = s.delta16 ? 1 : 0;
+  info[1] = s.uniform_slices;
+  info[2] = s.band;
+  sell_decode(s, nslices, nent, maxw, sptr, col);
+  return ADFEM_OK;
 }
 // reverse Cuthill-McKee order of the mesh's node graph (pi[node] = new index) and the band it
 // reports

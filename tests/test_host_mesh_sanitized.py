@@ -10,6 +10,9 @@ links it with host-memory stand-ins for the four CUDA runtime calls it makes, in
     and every stored entry of the sliced-ELL copy against the pattern;
   * renumbers a shuffled mesh by reverse Cuthill-McKee (the solver's DOF order) and checks
     the permutation and the band it reports;
+  * lays out the interleaved 2-DOF pattern of an elasticity operator (slice-uniform column
+    patterns per row parity) and a pattern with a band beyond int16 (int32 columns) in
+    sliced ELL, and decodes every stored entry;
   * feeds the invalid meshes the entry rejects (vertex index out of range, a degenerate
     triangle, a vertex in no element, a vertex with 70 neighbours) and checks the statuses;
   * makes each device allocation of a mesh build fail in turn (adfem_debug_fail_alloc) and
@@ -47,6 +50,7 @@ H.hm_sell.argtypes = [vp, vp, vp, vp, vp, vp]
 H.hm_space.argtypes = [vp, ctypes.c_int, vp, vp, vp, vp, vp]
 H.adfem_debug_fail_alloc.argtypes = [ll]
 H.hm_rcm.argtypes = [vp, vp]; H.hm_rcm.restype = ll
+H.hm_sell_build.argtypes = [ll, vp, vp, ctypes.c_int, vp, vp, vp, vp, vp, vp]
 
 def P(a):
     return a.ctypes.data
@@ -126,6 +130,45 @@ rows = np.repeat(np.arange(n), np.diff(rp))
 assert band == np.abs(pi[rows] - pi[ci]).max()
 assert band <= np.abs(rows - ci).max() // 4 and band <= 2 * 31 + 8, band
 H.hm_destroy(h)
+
+# sliced-ELL layouts of other patterns: the interleaved 2-DOF pattern of an elasticity
+# operator (slice-uniform patterns per row parity) and a pattern whose band exceeds the
+# int16 deltas (int32 columns, padding on the diagonal)
+def sell_check(rp, ci, period):
+    n = rp.size - 1
+    ns, nent, maxw = ctypes.c_longlong(), ctypes.c_longlong(), ctypes.c_int()
+    info = np.zeros(3, np.int64)
+    assert H.hm_sell_build(n, P(rp), P(ci), period, ctypes.byref(ns), ctypes.byref(nent), ctypes.byref(maxw),
+                           P(info), None, None) == 0
+    sp = np.empty(ns.value + 1, np.int32); col = np.empty(max(nent.value, 1), np.int32)
+    H.hm_sell_build(n, P(rp), P(ci), period, ctypes.byref(ns), ctypes.byref(nent), ctypes.byref(maxw), P(info),
+                    P(sp), P(col))
+    for r in range(n):
+        s = r // 32; w = (sp[s + 1] - sp[s]) // 32
+        got = col[sp[s] + 32 * np.arange(w) + (r % 32)]
+        row = ci[rp[r]:rp[r + 1]]
+        assert np.array_equal(got[:row.size], row) and np.all(got[row.size:] == r), r
+    return info
+
+c, e = synth.jittered_square(100, seed=7)
+st, h = build(c, e); assert st == 0
+n = c.shape[0]
+nnz, maxrow, flipped = ctypes.c_longlong(), ctypes.c_int(), ctypes.c_int()
+H.hm_sizes(h, ctypes.byref(nnz), ctypes.byref(maxrow), ctypes.byref(flipped))
+rp = np.empty(n + 1, np.int32); ci = np.empty(nnz.value, np.int32); H.hm_pattern(h, P(rp), P(ci))
+H.hm_destroy(h)
+rows2 = [np.sort(np.r_[2 * ci[rp[i]:rp[i + 1]], 2 * ci[rp[i]:rp[i + 1]] + 1]) for i in range(n) for _ in (0, 1)]
+rp2 = np.r_[0, np.cumsum([r.size for r in rows2])].astype(np.int32)
+ci2 = np.concatenate(rows2).astype(np.int32)
+info = sell_check(rp2, ci2, 2)
+assert info[0] == 1 and info[1] > 0  # int16 deltas; interior slices share a pattern
+far = 40000
+rows3 = [sorted({max(i - 1, 0), i, min(i + 1, far - 1)} | ({i + 35000} if i < 5000 else set())
+                | ({i - 35000} if i >= 35000 else set())) for i in range(far)]
+rp3 = np.r_[0, np.cumsum([len(r) for r in rows3])].astype(np.int32)
+ci3 = np.concatenate([np.array(r) for r in rows3]).astype(np.int32)
+info = sell_check(rp3, ci3, 1)
+assert info[0] == 0 and info[2] == 35000
 
 # invalid meshes: a status and a message, no crash
 c, e = synth.jittered_square(3, seed=0)
