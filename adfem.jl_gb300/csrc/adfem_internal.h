@@ -236,9 +236,10 @@ cudaError_t launch_laplace_coo_backward(const Mesh& m, const double* grad_vv, do
 cudaError_t launch_source_backward(const Mesh& m, const double* grad_rhs, double* grad_f, cudaStream_t st);
 // fused Poisson system: Laplace + load + Dirichlet (bd rows -> identity, bd columns
 // dropped into the rhs lift), values into the system's sliced-ELL (sptr; full pattern,
-// dropped entries 0); src3 from launch_element_prepass_unweighted.  diagpos_mesh: diagonal slot of each mesh pattern row.  nperm /
-// kperm (NULL: no renumbering): solver row of each node and rank of each pattern slot in
-// its renumbered row; isbd, bdval and rhs are in solver order.
+// dropped entries 0); src3 from launch_element_prepass_unweighted.  diagpos_mesh: diagonal
+// slot of each mesh pattern row.  nperm / kperm (NULL: no renumbering): solver row of each
+// node and rank of each pattern slot in its renumbered row; isbd, bdval and rhs are in
+// solver order.  Rows of up to 64 entries.
 cudaError_t launch_poisson_system(const Mesh& m, const double* sigma, const double* src3, const uint8_t* isbd,
                                   const double* bdval_dense, double* sell_vals, double* rhs, const int32_t* sptr,
                                   const int32_t* diagpos_mesh, const int32_t* nperm, const uint8_t* kperm,
