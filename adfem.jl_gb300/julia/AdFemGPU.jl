@@ -66,6 +66,23 @@ function compute_fem_laplace_matrix1(kappa::Vector{Float64}, m::GMesh)
     SparseMatrixCSC(m.ndof, m.ndof, colptr, rowval, nzval)
 end
 
+"""compute_fem_stiffness_matrix(D, mesh) (MCore.jl:296-315): the 2ndof x 2ndof operator in the
+reference's [x block; y block] ordering, with D[i, :, :] the 3x3 material matrix at Gauss point i,
+built on the GPU as a SparseMatrixCSC."""
+function compute_fem_stiffness_matrix(D::Array{Float64,3}, m::GMesh)
+    size(D) == (m.ngauss, 3, 3) || error("D must be ngauss x 3 x 3")
+    hmat = vec(permutedims(D, (3, 2, 1)))  # row-major 3x3 per Gauss point, as MCore.jl:298-307
+    n2 = 2 * m.ndof
+    colptr = Vector{Int64}(undef, n2 + 1)
+    rowval = Vector{Int64}(undef, 4 * m.nnz)
+    check(ccall((:adfem_mesh_pattern_elasticity, LIB), Cint, (Ptr{Cvoid}, Ptr{Clonglong}, Ptr{Clonglong}),
+                m.h, colptr, rowval))
+    nzval = Vector{Float64}(undef, length(rowval))
+    check(ccall((:adfem_stiffness_csc, LIB), Cint, (Ptr{Cvoid}, Ptr{Cdouble}, Clonglong, Ptr{Cdouble}),
+                m.h, hmat, length(hmat), nzval))
+    SparseMatrixCSC(n2, n2, colptr, rowval, nzval)
+end
+
 """compute_fem_mass_matrix1(ρ, mesh) (MCore.jl:170-181)."""
 function compute_fem_mass_matrix1(rho::Vector{Float64}, m::GMesh)
     colptr, rowval = pattern(m)
@@ -150,6 +167,46 @@ function gpu_solve(K::SparseMatrixCSC{Float64,Int64}, F::Vector{Float64}; kw...)
                 (Clonglong, Ptr{Clonglong}, Ptr{Clonglong}, Ptr{Cdouble}, Ptr{Cdouble}, Ptr{Cdouble}, Ref{SolverOpts},
                  Ref{SolverStats}), size(K, 1), K.colptr, K.rowval, K.nzval, F, u, o, s))
     u
+end
+
+"""A resident Poisson system: the operator's pattern, the solver's layout and its vectors stay on
+the GPU between calls, so repeated solves on one mesh (an inverse problem, a parameter sweep) pay
+only for the new coefficients.  `set_dirichlet!` fixes the Dirichlet DOFs and values once;
+`poisson_solve!` then assembles K(κ) and F(f), imposes the Dirichlet values and solves K\\F in one
+call (mixed precision by default: FP32 iterations with FP64 residual replacement)."""
+mutable struct PoissonSystem
+    h::Ptr{Cvoid}
+    mesh::GMesh  # the system refers to the mesh: keep it alive as long as the system
+    ndof::Int
+    function PoissonSystem(m::GMesh)
+        h = Ref{Ptr{Cvoid}}(C_NULL)
+        check(ccall((:adfem_system_create, LIB), Cint, (Ptr{Cvoid}, Cint, Ptr{Ptr{Cvoid}}), m.h, 0, h))
+        s = new(h[], m, m.ndof)
+        finalizer(x -> ccall((:adfem_system_destroy, LIB), Cint, (Ptr{Cvoid},), x.h), s)
+        return s
+    end
+end
+
+"""Dirichlet DOFs `bd` (1-based, e.g. `bcnode(mesh)`) with values `bdval`."""
+function set_dirichlet!(s::PoissonSystem, bd::Vector{Int64}, bdval::Vector{Float64} = zeros(length(bd)))
+    length(bdval) == length(bd) || error("bd and bdval lengths differ")
+    check(ccall((:adfem_system_set_dirichlet, LIB), Cint, (Ptr{Cvoid}, Ptr{Clonglong}, Clonglong, Ptr{Cdouble}),
+                s.h, bd, length(bd), bdval))
+    s
+end
+
+"""u = K(κ) \\ F(f) with the Dirichlet values imposed, κ and f at the Gauss points; returns
+(u, stats).  `warm_start = true` starts from the u passed in."""
+function poisson_solve!(u::Vector{Float64}, s::PoissonSystem, kappa::Vector{Float64}, f::Vector{Float64};
+                        mixed::Bool = true, rtol::Real = 3e-10, max_iter::Integer = 200000, warm_start::Bool = false)
+    length(u) == s.ndof || error("u must have ndof entries")
+    length(kappa) == s.mesh.ngauss && length(f) == s.mesh.ngauss || error("kappa and f: one value per Gauss point")
+    o = Ref(SolverOpts(rtol, max_iter, mixed ? 1 : 0, 0.1, 32, warm_start ? 1 : 0))
+    st = Ref{SolverStats}()
+    check(ccall((:adfem_poisson_solve, LIB), Cint,
+                (Ptr{Cvoid}, Ptr{Cdouble}, Ptr{Cdouble}, Ptr{Cdouble}, Ref{SolverOpts}, Ref{SolverStats}),
+                s.h, kappa, f, u, o, st))
+    u, st[]
 end
 
 end # module
