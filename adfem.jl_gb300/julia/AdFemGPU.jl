@@ -8,8 +8,9 @@ Julia bindings of libadfem_gpu.so for AdFem.jl users.
   makes `Mesh`, `compute_fem_laplace_matrix1`, `compute_fem_source_term1` and
   `compute_fem_stiffness_matrix` run on the GPU unchanged.
 * This module adds the direct SparseMatrixCSC outputs (no COO + `sparse` round trip)
-  for P1 and P2 meshes (Laplace, mass), the Gauss-point interpolation ops, the
-  Dirichlet imposition and `K\\F` on the GPU.
+  for P1 and P2 meshes (Laplace, mass, stiffness), the Gauss-point interpolation ops,
+  the Dirichlet imposition, `K\\F` on the GPU, and resident Poisson systems that keep
+  the operator and the solver on the GPU across solves.
 """
 module AdFemGPU
 
