@@ -371,3 +371,39 @@ def test_header_matches_the_reference_op_functions():
         cret, cargs = fns[o["symbol"]]
         assert cret == ("void", 0), o["site"]
         assert [_cxx_kind(t) for t in o["params"]] == cargs, (o["site"], o["params"], cargs)
+
+
+def _julia_structure(text):
+    """Block depth and bracket balance of Julia source, strings and comments removed: the
+    keywords that open a block (at bracket depth 0; a `for` inside brackets is a
+    comprehension) against `end`.  Returns (final block depth, lowest block depth, final
+    bracket depth, lowest bracket depth)."""
+    text = re.sub(r'"""(.*?)"""', " ", text, flags=re.S)
+    text = re.sub(r'"(?:\\.|[^"\\])*"', " ", text)
+    text = re.sub(r"#.*", " ", text)
+    openers = {"function", "struct", "module", "begin", "for", "while", "if", "let", "do", "try", "quote", "macro"}
+    block = bracket = 0
+    low_block = low_bracket = 0
+    for tok in re.findall(r"[A-Za-z_][A-Za-z_0-9!]*|[()\[\]{}]", text):
+        if tok in "([{":
+            bracket += 1
+        elif tok in ")]}":
+            bracket -= 1
+            low_bracket = min(low_bracket, bracket)
+        elif bracket == 0 and tok in openers:
+            block += 1
+        elif bracket == 0 and tok == "end":
+            block -= 1
+            low_block = min(low_block, block)
+    return block, low_block, bracket, low_bracket
+
+
+@pytest.mark.parametrize("src", ["AdFemGPU.jl", "INTEGRATION.md"])
+def test_julia_sources_are_balanced(src):
+    """No Julia here to parse the binding: at least every block it opens is closed by an
+    `end` and every bracket is closed, in order."""
+    text = dict(julia_sources())[src]
+    assert _julia_structure(text) == (0, 0, 0, 0)
+    # the checker itself sees an unclosed block and a stray bracket
+    assert _julia_structure("function f(x)\n  x\n")[0] == 1
+    assert _julia_structure("f(x))")[3] == -1
