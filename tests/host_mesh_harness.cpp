@@ -49,6 +49,14 @@ int hm_build(const double* xyz, long long nv, const int* elems0, long long ne, v
 }
 const char* hm_error() { return adfem::last_error_cstr(); }
 void hm_destroy(void* h) { delete static_cast<Mesh*>(h); }
+// what adfem_mesh_create does for a degree-2 mesh after mesh_build: the degree, then its space
+int hm_make_p2(void* h) {
+  Mesh* m = static_cast<Mesh*>(h);
+  m->degree = 2;
+  adfem::Space* sp = nullptr;
+  return adfem::mesh_space(m, 2, &sp);
+}
+void hm_gauss_weights(void* h, double* w) { adfem::mesh_gauss_weights(static_cast<Mesh*>(h), w); }
 void hm_sizes(void* h, long long* nnz, int* maxrow, int* flipped) {
   const Mesh* m = static_cast<Mesh*>(h);
   *nnz = m->nnz;

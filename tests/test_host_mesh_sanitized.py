@@ -50,6 +50,8 @@ H.hm_sell.argtypes = [vp, vp, vp, vp, vp, vp]
 H.hm_space.argtypes = [vp, ctypes.c_int, vp, vp, vp, vp, vp]
 H.adfem_debug_fail_alloc.argtypes = [ll]
 H.hm_rcm.argtypes = [vp, vp]; H.hm_rcm.restype = ll
+H.hm_make_p2.argtypes = [vp]
+H.hm_gauss_weights.argtypes = [vp, vp]
 H.hm_sell_build.argtypes = [ll, vp, vp, ctypes.c_int, vp, vp, vp, vp, vp, vp]
 
 def P(a):
@@ -102,6 +104,17 @@ def check_mesh(coords, elems):
     H.hm_space(h, 2, ctypes.byref(nd), ctypes.byref(nz), ctypes.byref(mr), P(rp2), P(ci2))
     K2 = S.laplace_csc(np.ones(S.ngauss))
     assert nd.value == S.ndof and np.array_equal(rp2, K2.indptr) and np.array_equal(ci2, K2.indices)
+    H.hm_destroy(h)
+    # the same mesh as a degree-2 mesh: 6 Gauss points per element (order-4 rule), boundary
+    # DOFs with the boundary edges' DOFs after the vertices
+    st, h = build(coords, elems)
+    assert st == 0 and H.hm_make_p2(h) == 0
+    g6x = np.empty(S.ngauss); g6y = np.empty(S.ngauss); H.hm_gauss(h, P(g6x), P(g6y))
+    assert np.allclose(np.stack([g6x, g6y], 1), S.gauss_nodes(), rtol=0, atol=1e-15)
+    w6 = np.empty(S.ngauss); H.hm_gauss_weights(h, P(w6))
+    assert abs(w6.sum() - M.area.sum()) < 1e-13 * M.area.sum()  # the weights integrate 1
+    nb = H.hm_bcnode(h, None); bd2 = np.empty(nb, np.int64); H.hm_bcnode(h, P(bd2))
+    assert np.array_equal(bd2, S.bcnode())
     H.hm_destroy(h)
 
 cases = [synth.jittered_square(1, seed=0, jitter=0.0), synth.jittered_square(2, seed=0, jitter=0.0),
